@@ -1,0 +1,199 @@
+"""Pins the CPU oracle to the reference's own known answers before anything is checked
+against it: Philox vectors, rule definitions, classic patterns, scheme properties,
+Moran's I and Lenia direct-vs-FFT. ReferenceBackend-style and ArrayBackend-style
+(threaded, halo-padded) oracle runs must agree exactly, as the reference's conformance
+battery demands of every backend (test/backend_conformance.jl:264-287)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_philox_known_answers(oracle):
+    """test/test_random.jl:4-14 (vectors extracted into tests/golden/philox_kat.json)."""
+    with open(os.path.join(GOLDEN, "philox_kat.json")) as f:
+        kats = json.load(f)["vectors"]
+    assert len(kats) == 3
+    for v in kats:
+        assert oracle.philox4x32(v["ctr"], v["key"]) == tuple(v["out"])
+
+
+def test_uniform_pure_and_in_range(oracle):
+    """test/test_random.jl:18-56."""
+    u = oracle.uniform
+    assert u(1, 7, 3, 1) == u(1, 7, 3, 1)
+    assert u(1, 7, 3, 1) != u(1, 8, 3, 1)
+    assert u(1, 7, 3, 1) != u(1, 7, 4, 1)
+    assert u(1, 7, 3, 1) != u(2, 7, 3, 1)
+    assert u(1, 7, 3, 1) != u(1, 7, 3, 2)
+    xs = np.array([u(2026, i, 0, k) for i in range(1, 2001) for k in range(1, 5)])
+    assert np.all((xs >= 0) & (xs < 1))
+    assert abs(xs.mean() - 0.5) < 0.01
+    assert abs((xs < 0.25).mean() - 0.25) < 0.02
+    ys = np.array([oracle.uniform32(2026, i, 0, 1) for i in range(1, 5001)])
+    assert np.all((ys >= 0) & (ys < 1)) and abs(ys.mean() - 0.5) < 0.015
+    # the FP64 draw is built from words 1 and 2 of the Philox output, the FP32 draw from word 1
+    r = oracle.philox4x32((7, 0, 3, 2), (1, 0))
+    assert u(1, 7, 3, 2) == (((r[0] << 32) | r[1]) >> 11) * 2.0 ** -53
+    assert oracle.uniform32(1, 7, 3, 2) == np.float32(r[0] >> 8) * np.float32(2.0 ** -24)
+
+
+def naive_generations(birth, survive, C, u):
+    """test/test_rules.jl:23-32, restated: Moore(1) on a torus; C = 2 is Life."""
+    m, n = u.shape
+    out = np.zeros_like(u)
+    for i in range(m):
+        for j in range(n):
+            live = sum(u[(i + a) % m, (j + b) % n] == 1
+                       for a in (-1, 0, 1) for b in (-1, 0, 1) if (a, b) != (0, 0))
+            s = u[i, j]
+            if s == 0:
+                out[i, j] = 1 if live in birth else 0
+            elif s == 1:
+                out[i, j] = 1 if live in survive else (2 if C > 2 else 0)
+            else:
+                out[i, j] = s + 1 if s + 1 < C else 0
+    return out
+
+
+@pytest.mark.parametrize("b,s,C", [([3], [2, 3], 2), ([3, 6], [2, 3], 2), ([2], [], 2),
+                                   ([2], [], 3), ([2], [3, 4, 5], 4)])
+def test_life_generations_against_definition(oracle, b, s, C):
+    rng = np.random.default_rng(C * 10 + len(b))
+    for _ in range(3):
+        u = rng.integers(0, C, size=(12, 15)).astype(np.int8)
+        rule = oracle.RULE_LIFE if C == 2 else oracle.RULE_GENERATIONS
+        P = oracle.Problem(rule, 12, 15, birth=oracle.mask(b), survive=oracle.mask(s), states=C)
+        assert np.array_equal(oracle.step_reference(P, u, 0), naive_generations(b, s, C, u))
+        assert np.array_equal(oracle.run_array(P, u, 0, 1, nthreads=3), naive_generations(b, s, C, u))
+
+
+def test_classic_patterns(oracle):
+    """Blinker, block and glider (test/test_rules.jl:109-122)."""
+    life = oracle.Problem(oracle.RULE_LIFE, 5, 5, birth=oracle.mask([3]), survive=oracle.mask([2, 3]))
+    blinker = np.zeros((5, 5), np.int8)
+    blinker[2, 1:4] = 1
+    assert np.array_equal(oracle.run_array(life, blinker, 0, 1), blinker.T)
+    assert np.array_equal(oracle.run_array(life, blinker, 0, 2), blinker)
+    g = np.zeros((10, 10), np.int8)
+    g[1, 2] = g[2, 3] = 1
+    g[3, 1:4] = 1
+    life10 = oracle.Problem(oracle.RULE_LIFE, 10, 10, birth=oracle.mask([3]), survive=oracle.mask([2, 3]))
+    assert np.array_equal(oracle.run_array(life10, g, 0, 4), np.roll(g, (1, 1), (0, 1)))
+    assert np.array_equal(oracle.run_array(life10, g, 0, 40), np.roll(g, (10, 10), (0, 1)))
+
+
+def conformance_problems(oracle):
+    """Int8 cases of the reference's conformance battery that this path covers
+    (test/backend_conformance.jl:171-211), plus Larger-than-Life and forest fire."""
+    o = oracle
+    B3S23 = dict(birth=o.mask([3]), survive=o.mask([2, 3]))
+    return [
+        ("Life on a torus", o.Problem(o.RULE_LIFE, 20, 24, **B3S23), 30, None),
+        ("Life on a cylinder", o.Problem(o.RULE_LIFE, 20, 24, boundary=(o.PERIODIC, o.CONSTANT), **B3S23), 30, None),
+        ("radius-2 von Neumann, mixed edges",
+         o.Problem(o.RULE_LIFE, 15, 17, nbhd=o.VON_NEUMANN, radius=2, birth=o.mask([3]),
+                   survive=o.mask([2, 3, 4, 5]), boundary=(o.REFLECTING, o.CONSTANT), constant=(0, 1)), 20, None),
+        ("Brian's Brain", o.Problem(o.RULE_GENERATIONS, 18, 18, birth=o.mask([2]), survive=0, states=3), 25, None),
+        ("Moore(4) wider than the torus", o.Problem(o.RULE_LIFE, 3, 7, radius=4, birth=o.mask([5, 6, 7]),
+                                                     survive=o.mask([4, 5, 6, 7, 8])), 8, None),
+        ("Larger than Life, Moore(5)", o.Problem(o.RULE_LIFE, 40, 37, radius=5, birth=o.mask(range(34, 46)),
+                                                 survive=o.mask(range(34, 59))), 12, None),
+        ("Stochastic(0.4) Life", o.Problem(o.RULE_LIFE, 20, 20, seed=2, scheme=o.STOCHASTIC, scheme_p=0.4,
+                                           **B3S23), 15, None),
+        ("Stochastic(0.5f0) Life", o.Problem(o.RULE_LIFE, 20, 20, seed=12, scheme=o.STOCHASTIC, scheme_p=0.5,
+                                             scheme_p_f32=True, **B3S23), 15, None),
+        ("Checkerboard majority", o.Problem(o.RULE_LIFE, 18, 18, nbhd=o.VON_NEUMANN, birth=o.mask([5, 6, 7, 8]),
+                                            survive=o.mask([4, 5, 6, 7, 8]), scheme=o.CHECKERBOARD), 10, None),
+        ("forest fire, Grid Constant(0)", o.Problem(o.RULE_FOREST_FIRE, 40, 30, nbhd=o.VON_NEUMANN, seed=3,
+                                                    boundary=(o.CONSTANT, o.CONSTANT)), 30, (0.3, 0.01)),
+        ("forest fire, Float32 parameters", o.Problem(o.RULE_FOREST_FIRE, 33, 21, nbhd=o.VON_NEUMANN, seed=5,
+                                                      params_f32=True), 30, (0.3, 0.01)),
+    ]
+
+
+def test_array_equals_reference(oracle):
+    rng = np.random.default_rng(2026)
+    for name, P, steps, params in conformance_problems(oracle):
+        C = P.states if P.rule == oracle.RULE_GENERATIONS else (3 if P.rule == oracle.RULE_FOREST_FIRE else 2)
+        u = rng.integers(0, C, size=(P.n1, P.n2)).astype(np.int8)
+        ref = u.copy()
+        for t in range(steps):
+            ref = oracle.step_reference(P, ref, t, params)
+        for nt in (1, 4):
+            got = oracle.run_array(P, u, 0, steps, params, nthreads=nt)
+            assert np.array_equal(got, ref), (name, nt)
+        assert not np.array_equal(ref, u), name  # the battery is not vacuous
+
+
+def test_stochastic_one_is_synchronous(oracle):
+    """test/test_schemes.jl:8-9."""
+    o = oracle
+    u = np.random.default_rng(11).integers(0, 2, (20, 20)).astype(np.int8)
+    a = o.Problem(o.RULE_LIFE, 20, 20, birth=o.mask([3]), survive=o.mask([2, 3]), scheme=o.STOCHASTIC, scheme_p=1.0)
+    b = o.Problem(o.RULE_LIFE, 20, 20, birth=o.mask([3]), survive=o.mask([2, 3]))
+    assert np.array_equal(o.run_array(a, u, 0, 5), o.run_array(b, u, 0, 5))
+
+
+def test_checkerboard_against_definition(oracle):
+    """schemes.jl:42-51: even index sums first, then odd ones, each reading the
+    state the first half left (1-based indices)."""
+    o = oracle
+    u = np.random.default_rng(5).integers(0, 2, (9, 8)).astype(np.int8)
+    P = o.Problem(o.RULE_LIFE, 9, 8, nbhd=o.VON_NEUMANN, birth=o.mask([2, 3]), survive=o.mask([1, 2]),
+                  scheme=o.CHECKERBOARD)
+    v = u.copy()
+    for odd in (0, 1):
+        w = v.copy()
+        for i in range(9):
+            for j in range(8):
+                if ((i + 1 + j + 1) % 2) != odd:
+                    continue
+                n = sum(v[(i + a) % 9, (j + b) % 8] == 1 for a, b in ((0, -1), (-1, 0), (1, 0), (0, 1)))
+                w[i, j] = (n in (1, 2)) if v[i, j] == 1 else (n in (2, 3))
+        v = w
+    assert np.array_equal(o.step_reference(P, u, 0), v)
+
+
+def test_forest_fire_rates(oracle):
+    """bernoulli(p) hits at rate p (test/test_random.jl:51-56) through the rule."""
+    o = oracle
+    P = o.Problem(o.RULE_FOREST_FIRE, 200, 100, nbhd=o.VON_NEUMANN, seed=9, boundary=(o.CONSTANT, o.CONSTANT))
+    u = o.run_array(P, np.zeros((200, 100), np.int8), 0, 1, (0.3, 0.0))
+    assert abs((u == 1).mean() - 0.3) < 0.015
+    assert np.all(o.run_array(P, np.zeros((200, 100), np.int8), 0, 3, (0.0, 0.0)) == 0)
+    full = o.run_array(P, np.ones((200, 100), np.int8), 0, 1, (0.0, 1.0))
+    assert np.all(full == 2)
+
+
+def test_morans_i(oracle):
+    """test/test_extras.jl:140-144 (measures.jl:91-107)."""
+    o = oracle
+    checker = np.array([[(i + j) % 2 for j in range(1, 7)] for i in range(1, 7)], np.int8)
+    assert abs(o.morans_i(o.Problem(o.RULE_LIFE, 6, 6), checker) + 1.0) < 1e-12
+    stripes = np.array([[1 if j <= 3 else 0 for j in range(1, 7)] for i in range(1, 7)], np.int8)
+    grid = o.Problem(o.RULE_LIFE, 6, 6, boundary=(o.CONSTANT, o.CONSTANT))
+    assert o.morans_i(grid, stripes) > 0.5
+    assert np.isnan(o.morans_i(o.Problem(o.RULE_LIFE, 3, 3), np.ones((3, 3), np.int8)))
+    counts, other = o.state_counts(np.array([[0, 1], [0, 0]], np.int8), 3)
+    assert counts == [3, 1, 0] and other == 0
+
+
+def test_lenia_direct_vs_fft(oracle):
+    """test/test_extras.jl:121-123: FP64 direct and FFT agree to 1e-10 after 10 steps."""
+    rng = np.random.default_rng(4)
+    u = np.zeros((64, 64))
+    u[20:40, 20:40] = rng.random((20, 20))
+    off, w = oracle.lenia_weights(13)
+    assert len(w) == 516 and abs(w.sum() - 1) < 1e-14
+    fft = oracle.LeniaFFT(64, 64)
+    a = u.copy()
+    b = u.copy()
+    for _ in range(10):
+        a = oracle.lenia_step_direct(a, nthreads=4)
+        b = fft.step(b)
+    assert np.max(np.abs(a - b)) < 1e-10
+    assert np.max(np.abs(a - u)) > 1e-3  # it moved
