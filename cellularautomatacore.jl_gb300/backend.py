@@ -1,0 +1,203 @@
+"""GB300Backend: the reference's backend contract (src/backends.jl:4-14) implemented over
+libgbca.so. Method names follow the contract with Julia's `!` dropped:
+
+    supports(backend, scheme)                    src/backends.jl:89-95
+    check_problem(backend, prob, scheme)         src/backends.jl:97-105
+    allocate_state(backend, prob, scheme)        src/backends.jl:107-119
+    advance(backend, state, prob, scheme, p, t)  src/backends.jl:121-130  (advance!)
+    current_state(backend, state)                src/backends.jl:132-139
+    set_state(backend, state, u)                 src/backends.jl:141-148  (set_state!)
+    read_cell / write_cell                       src/backends.jl:380-383  (write_cell!)
+
+`advance` is one step from t to t + 1, as the integrator calls it (src/problem.jl:455).
+The backend queues consecutive steps and hands them to the library as one call when
+anything reads or replaces the state, or when the parameters change, so the device runs
+them temporally blocked. Results are those of ReferenceBackend, bit for bit for the Int8
+rules (draws keyed as src/random.jl:102-107)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+from .errors import ArgumentError, IncompatibleSpaceError, StateShapeError
+from .model import (Checkerboard, Constant, ForestFire, Generations, Lattice, Lenia, Life, Moore, Stochastic,
+                    Synchronous, VonNeumann)
+
+
+class GB300Backend:
+    """Run the sweep on the GPU through libgbca.so (hand-written sm_103a kernels).
+    Needs a CUDA device; there is no CPU fallback."""
+
+    def __repr__(self):
+        return "GB300Backend()"
+
+    def __eq__(self, other):
+        return isinstance(other, GB300Backend)
+
+    def __hash__(self):
+        return hash("GB300Backend")
+
+
+def supports(backend, scheme) -> bool:
+    """src/backends.jl:153: the gated synchronous schemes."""
+    return isinstance(backend, GB300Backend) and isinstance(scheme, (Synchronous, Stochastic, Checkerboard))
+
+
+def _params_tuple(rule, p):
+    """The rule's numbers from the integrator's p: forest fire reads p.p and p.f."""
+    if not isinstance(rule, ForestFire):
+        return ()
+    if p is None:
+        raise ArgumentError("the forest-fire rule needs parameters (p=..., f=...)")
+    get = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
+    vals = (float(get("p")), float(get("f")))
+    if rule.float32:
+        vals = tuple(float(np.float32(v)) for v in vals)
+    return vals
+
+
+def make_desc(prob, scheme) -> capi.Desc:
+    """The gbca_desc of a problem; raises the reference's errors for what the backend
+    cannot run (the checks of check_problem)."""
+    space, rule = prob.space, prob.rule
+    if not isinstance(space, Lattice):
+        raise IncompatibleSpaceError("GB300Backend needs a lattice")
+    d = capi.Desc()
+    d.n1, d.n2 = space.dims
+    for a, b in enumerate(space.boundaries):
+        d.boundary[a] = b.kind
+        d.constant[a] = float(b.value) if isinstance(b, Constant) else 0.0
+    d.seed = int(prob.seed) % (1 << 64)
+    if isinstance(scheme, Stochastic):
+        d.scheme, d.scheme_p, d.scheme_p_f32 = capi.STOCHASTIC, scheme.p, int(scheme.float32)
+    elif isinstance(scheme, Checkerboard):
+        d.scheme = capi.CHECKERBOARD
+    else:
+        d.scheme = capi.SYNCHRONOUS
+    if isinstance(rule, Lenia):
+        d.rule = capi.RULE_LENIA
+        d.lenia_method = capi.FFT if rule.method == "fft" else capi.DIRECT
+        d.lenia_R, d.lenia_npeaks = rule.R, len(rule.peaks)
+        if len(rule.peaks) > capi.MAX_PEAKS:
+            raise ArgumentError(f"GB300Backend runs Lenia with at most {capi.MAX_PEAKS} peaks")
+        for k, v in enumerate(rule.peaks):
+            d.lenia_peaks[k] = v
+        d.lenia_mu, d.lenia_sigma, d.lenia_dt = rule.mu, rule.sigma, rule.dt
+        if np.asarray(prob.u0).dtype != np.float32:
+            raise ArgumentError("GB300Backend runs Lenia on a Float32 state")
+        return d
+    nb = prob.neighbours
+    if not isinstance(nb, (Moore, VonNeumann)):
+        raise ArgumentError("GB300Backend runs Moore(r) and VonNeumann(r) neighbourhoods")
+    d.nbhd, d.radius = nb.kind, nb.radius
+    if np.asarray(prob.u0).dtype != np.int8:
+        raise ArgumentError("GB300Backend runs Life, Generations and forest-fire rules on Int8 states")
+    if isinstance(rule, Life):
+        d.rule, d.birth, d.survive, d.states = capi.RULE_LIFE, rule.birth, rule.survive, 2
+    elif isinstance(rule, Generations):
+        d.rule, d.birth, d.survive, d.states = capi.RULE_GENERATIONS, rule.birth, rule.survive, rule.states
+    elif isinstance(rule, ForestFire):
+        d.rule, d.params_f32 = capi.RULE_FOREST_FIRE, int(rule.float32)
+    else:
+        raise ArgumentError(f"GB300Backend cannot run {type(rule).__name__}: arbitrary LocalRules cannot cross "
+                            "the C ABI; use Life, Generations, ForestFire or Lenia")
+    return d
+
+
+def check_problem(backend, prob, scheme) -> None:
+    d = make_desc(prob, scheme)
+    capi.check(capi.lib().gbca_check(ctypes.byref(d)))
+
+
+class GB300State:
+    """The backend's state: a library handle plus the queue of steps not yet run."""
+
+    def __init__(self, desc: capi.Desc, dtype):
+        self.desc, self.dtype = desc, np.dtype(dtype)
+        self.dims = (int(desc.n1), int(desc.n2))
+        self.handle = ctypes.c_void_p()
+        capi.check(capi.lib().gbca_create(ctypes.byref(desc), ctypes.byref(self.handle)))
+        self.pending, self.pending_t0, self.pending_params = 0, 0, ()
+
+    def flush(self):
+        if self.pending:
+            vals = self.pending_params
+            arr = (ctypes.c_double * max(1, len(vals)))(*vals)
+            n, self.pending = self.pending, 0
+            capi.check(capi.lib().gbca_advance(self.handle, self.pending_t0, n, arr, len(vals)))
+
+    def close(self):
+        if self.handle:
+            capi.lib().gbca_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def nbytes(self):
+        return self.dims[0] * self.dims[1] * self.dtype.itemsize
+
+
+def allocate_state(backend, prob, scheme) -> GB300State:
+    d = make_desc(prob, scheme)
+    st = GB300State(d, np.float32 if d.rule == capi.RULE_LENIA else np.int8)
+    set_state(backend, st, prob.u0)
+    return st
+
+
+def advance(backend, st: GB300State, prob, scheme, p, t: int) -> None:
+    """One step t -> t + 1 (queued)."""
+    params = _params_tuple(prob.rule, p)
+    if st.pending and st.pending_t0 + st.pending == t and params == st.pending_params:
+        st.pending += 1
+        return
+    st.flush()
+    st.pending_t0, st.pending, st.pending_params = int(t), 1, params
+
+
+def current_state(backend, st: GB300State) -> np.ndarray:
+    """A host copy in the layout of u0 (column-major)."""
+    st.flush()
+    out = np.empty(st.dims, dtype=st.dtype, order="F")
+    capi.check(capi.lib().gbca_get_state(st.handle, out.ctypes.data, out.nbytes))
+    return out
+
+
+def set_state(backend, st: GB300State, u) -> None:
+    st.flush()
+    a = np.asarray(u)
+    if a.shape != st.dims:
+        raise StateShapeError(f"the state has size {a.shape}, the space {st.dims}")
+    a = np.asfortranarray(a.astype(st.dtype, copy=False))
+    capi.check(capi.lib().gbca_set_state(st.handle, a.ctypes.data, a.nbytes))
+
+
+def read_cell(backend, st: GB300State, I):
+    st.flush()
+    i, j = I
+    out = np.zeros(1, dtype=st.dtype)
+    capi.check(capi.lib().gbca_read_cell(st.handle, int(i), int(j), out.ctypes.data))
+    return out[0]
+
+
+def write_cell(backend, st: GB300State, I, v) -> None:
+    st.flush()
+    i, j = I
+    val = np.array([v], dtype=st.dtype)
+    capi.check(capi.lib().gbca_write_cell(st.handle, int(i), int(j), val.ctypes.data))
+
+
+def device_summaries(st: GB300State, nvals: int = 3):
+    """state_counts (src/measures.jl:14-20) and Moran's I (src/measures.jl:91-107) of the
+    current state, computed on the device: (counts[0:nvals], cells outside, morans)."""
+    st.flush()
+    counts = (ctypes.c_int64 * max(1, nvals))()
+    other = ctypes.c_int64()
+    mi = ctypes.c_double()
+    capi.check(capi.lib().gbca_summaries(st.handle, counts, nvals, ctypes.byref(other), ctypes.byref(mi)))
+    return [int(counts[k]) for k in range(nvals)], int(other.value), float(mi.value)

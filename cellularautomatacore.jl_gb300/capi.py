@@ -1,0 +1,92 @@
+"""ctypes bindings of libgbca.so (include/gbca.h). The library is the product: when it
+is missing or cannot load, every call here raises; there is no CPU fallback."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import errors
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgbca.so")
+
+OK, ERR_ARGUMENT, ERR_INCOMPATIBLE_SPACE, ERR_UNSUPPORTED, ERR_STATE, ERR_CUDA, ERR_OOM, ERR_TIMEOUT, ERR_BUSY = range(9)
+RULE_LIFE, RULE_GENERATIONS, RULE_FOREST_FIRE, RULE_LENIA = 1, 2, 3, 4
+MOORE, VON_NEUMANN = 1, 2
+PERIODIC, REFLECTING, CONSTANT = 0, 1, 2
+SYNCHRONOUS, STOCHASTIC, CHECKERBOARD = 0, 1, 2
+DIRECT, FFT = 0, 1
+MAX_PEAKS = 8
+
+
+class Desc(ctypes.Structure):
+    """gbca_desc."""
+    _fields_ = [
+        ("rule", ctypes.c_int32), ("nbhd", ctypes.c_int32), ("radius", ctypes.c_int32), ("states", ctypes.c_int32),
+        ("birth", ctypes.c_uint64), ("survive", ctypes.c_uint64), ("n1", ctypes.c_int64), ("n2", ctypes.c_int64),
+        ("boundary", ctypes.c_int32 * 2), ("constant", ctypes.c_double * 2), ("seed", ctypes.c_uint64),
+        ("scheme", ctypes.c_int32), ("scheme_p_f32", ctypes.c_int32), ("scheme_p", ctypes.c_double),
+        ("params_f32", ctypes.c_int32), ("lenia_method", ctypes.c_int32), ("lenia_R", ctypes.c_int32),
+        ("lenia_npeaks", ctypes.c_int32), ("lenia_peaks", ctypes.c_double * MAX_PEAKS),
+        ("lenia_mu", ctypes.c_double), ("lenia_sigma", ctypes.c_double), ("lenia_dt", ctypes.c_double),
+    ]
+
+
+# every symbol include/gbca.h declares, with (restype, argtypes)
+_P = ctypes.POINTER
+_V = ctypes.c_void_p
+_I64 = ctypes.c_int64
+SIGNATURES = {
+    "gbca_last_error": (ctypes.c_char_p, []),
+    "gbca_version": (ctypes.c_int32, []),
+    "gbca_device_count": (ctypes.c_int32, []),
+    "gbca_check": (ctypes.c_int, [_P(Desc)]),
+    "gbca_create": (ctypes.c_int, [_P(Desc), _P(_V)]),
+    "gbca_destroy": (ctypes.c_int, [_V]),
+    "gbca_set_state": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
+    "gbca_get_state": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
+    "gbca_advance": (ctypes.c_int, [_V, _I64, _I64, _P(ctypes.c_double), ctypes.c_int32]),
+    "gbca_read_cell": (ctypes.c_int, [_V, _I64, _I64, _V]),
+    "gbca_write_cell": (ctypes.c_int, [_V, _I64, _I64, _V]),
+    "gbca_sync": (ctypes.c_int, [_V]),
+    "gbca_summaries": (ctypes.c_int, [_V, _P(_I64), ctypes.c_int32, _P(_I64), _P(ctypes.c_double)]),
+    "gbca_device_state": (ctypes.c_int, [_V, _P(_V), _P(_I64)]),
+    "gbca_threshold": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_int32]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise errors.GPUError(f"libgbca.so is not built ({LIB_PATH}); run __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    """Raise the reference's exception type for a nonzero status."""
+    if rc == OK:
+        return
+    msg = lib().gbca_last_error().decode(errors="replace")
+    raise {
+        ERR_ARGUMENT: errors.ArgumentError,
+        ERR_INCOMPATIBLE_SPACE: errors.IncompatibleSpaceError,
+        ERR_UNSUPPORTED: errors.UnsupportedCombinationError,
+        ERR_STATE: errors.StateShapeError,
+        ERR_OOM: errors.OutOfDeviceMemory,
+        ERR_TIMEOUT: errors.DeviceTimeout,
+        ERR_BUSY: errors.Busy,
+    }.get(rc, errors.GPUError)(msg)
+
+
+def threshold(p: float, f32: bool = False) -> int:
+    return int(lib().gbca_threshold(float(p), int(bool(f32))))

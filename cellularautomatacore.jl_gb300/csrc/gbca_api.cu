@@ -1,0 +1,347 @@
+// gbca_api.cu — the C ABI of libgbca.so (include/gbca.h): handles, state transfer,
+// advance with kernel selection, single-cell access and device summaries.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "gbca_internal.cuh"
+#include "lenia.cuh"
+#include "measures.cuh"
+
+struct gbca_handle {
+    gbca_desc d;
+    size_t esize = 1;
+    int64_t pitch = 0;  // bytes between columns
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    cudaStream_t stream = nullptr;
+    unsigned long long* acc = nullptr;       // device accumulator for summaries
+    unsigned long long* acc_host = nullptr;  // pinned copy
+    int nsm = 148;
+    gbca::LeniaPlan* lenia = nullptr;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char msg[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof msg, fmt, ap);
+    va_end(ap);
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(GBCA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define GBCA_CUDA(call, what)                          \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+bool is_int8_rule(int32_t r) {
+    return r == GBCA_RULE_LIFE || r == GBCA_RULE_GENERATIONS || r == GBCA_RULE_FOREST_FIRE;
+}
+
+int check_desc(const gbca_desc* d) {
+    if (!d) return fail(GBCA_ERR_ARGUMENT, "null problem description");
+    if (d->rule < GBCA_RULE_LIFE || d->rule > GBCA_RULE_LENIA)
+        return fail(GBCA_ERR_ARGUMENT, "GB300Backend runs Life, Generations, forest-fire and Lenia rules; got rule kind %d",
+                    d->rule);
+    if (d->n1 <= 0 || d->n2 <= 0)
+        return fail(GBCA_ERR_ARGUMENT, "lattice dimensions must be positive, got (%lld, %lld)", (long long)d->n1,
+                    (long long)d->n2);
+    if (d->n1 > (int64_t)1 << 31 || d->n2 > (int64_t)1 << 31 || d->n1 * d->n2 > ((int64_t)1 << 40))
+        return fail(GBCA_ERR_ARGUMENT, "lattice of %lld x %lld cells is too large", (long long)d->n1,
+                    (long long)d->n2);
+    for (int a = 0; a < 2; ++a)
+        if (d->boundary[a] < GBCA_PERIODIC || d->boundary[a] > GBCA_CONSTANT)
+            return fail(GBCA_ERR_ARGUMENT, "unknown boundary kind %d on axis %d", d->boundary[a], a + 1);
+    if (d->scheme < GBCA_SYNCHRONOUS || d->scheme > GBCA_CHECKERBOARD)
+        return fail(GBCA_ERR_UNSUPPORTED, "GB300Backend runs Synchronous, Stochastic and Checkerboard schemes");
+    if (d->scheme == GBCA_STOCHASTIC && !(d->scheme_p > 0.0 && d->scheme_p <= 1.0))
+        return fail(GBCA_ERR_ARGUMENT, "update probability must be in (0, 1], got %g", d->scheme_p);
+    if (is_int8_rule(d->rule)) {
+        if (d->nbhd != GBCA_MOORE && d->nbhd != GBCA_VON_NEUMANN)
+            return fail(GBCA_ERR_ARGUMENT, "GB300Backend runs Moore(r) and VonNeumann(r) neighbourhoods");
+        if (d->radius < 1 || d->radius > 64)
+            return fail(GBCA_ERR_ARGUMENT, "neighbourhood radius must be in 1:64, got %d", d->radius);
+        for (int a = 0; a < 2; ++a) {
+            if (d->boundary[a] != GBCA_CONSTANT) continue;
+            const double v = d->constant[a];
+            if (!(v == std::floor(v) && v >= -128.0 && v <= 127.0))
+                return fail(GBCA_ERR_INCOMPATIBLE_SPACE,
+                            "the boundary Constant(%g) does not fit: a state of Int8 cannot hold it", v);
+        }
+        if (d->rule == GBCA_RULE_GENERATIONS && (d->states < 2 || d->states > 127))
+            return fail(GBCA_ERR_ARGUMENT, "a Generations rule needs 2 to 127 states on Int8, got %d", d->states);
+    } else {
+        if (d->lenia_R < 1 || d->lenia_R > 64)
+            return fail(GBCA_ERR_ARGUMENT, "Lenia radius R must be in 1:64, got %d", d->lenia_R);
+        if (d->lenia_npeaks < 1 || d->lenia_npeaks > GBCA_MAX_PEAKS)
+            return fail(GBCA_ERR_ARGUMENT, "Lenia needs 1 to %d peaks, got %d", GBCA_MAX_PEAKS, d->lenia_npeaks);
+        if (!(d->lenia_sigma > 0.0)) return fail(GBCA_ERR_ARGUMENT, "sigma must be positive, got %g", d->lenia_sigma);
+        if (!(d->lenia_dt > 0.0 && d->lenia_dt <= 1.0))
+            return fail(GBCA_ERR_ARGUMENT, "dt must be in (0, 1], got %g", d->lenia_dt);
+        if (d->scheme != GBCA_SYNCHRONOUS)
+            return fail(GBCA_ERR_UNSUPPORTED, "GB300Backend runs Lenia with Synchronous() only");
+        if (d->lenia_method == GBCA_FFT && (d->boundary[0] != GBCA_PERIODIC || d->boundary[1] != GBCA_PERIODIC))
+            return fail(GBCA_ERR_ARGUMENT,
+                        "field :potential uses method=:fft, which needs periodic boundaries on every axis");
+        for (int a = 0; a < 2; ++a)
+            if (d->boundary[a] == GBCA_CONSTANT && d->constant[a] != 0.0)
+                return fail(GBCA_ERR_UNSUPPORTED, "GB300Backend runs Lenia with Constant(0) edges only");
+    }
+    return GBCA_OK;
+}
+
+uint64_t threshold(double p, bool f32) {
+    if (f32) {
+        const float pf = (float)p;
+        if (!(pf > 0.0f)) return 0;
+        if (pf >= 1.0f) return (uint64_t)1 << 24;
+        return (uint64_t)std::ceil((double)pf * 16777216.0);
+    }
+    if (!(p > 0.0)) return 0;
+    if (p >= 1.0) return (uint64_t)1 << 53;
+    return (uint64_t)std::ceil(p * 9007199254740992.0);
+}
+
+gbca::SweepParams base_params(const gbca_handle* h) {
+    const gbca_desc& d = h->d;
+    gbca::SweepParams p;
+    std::memset(&p, 0, sizeof p);
+    p.n1 = d.n1;
+    p.n2 = d.n2;
+    p.pitch = h->pitch;
+    for (int a = 0; a < 2; ++a) {
+        p.bnd[a] = d.boundary[a];
+        p.cval[a] = d.boundary[a] == GBCA_CONSTANT ? (int32_t)d.constant[a] : 0;
+    }
+    p.rule = d.rule;
+    p.nbhd = d.nbhd;
+    p.radius = d.radius;
+    p.states = d.states;
+    p.birth = d.birth;
+    p.survive = d.survive;
+    p.seed = d.seed;
+    p.scheme = d.scheme;
+    p.gate_f32 = d.scheme_p_f32;
+    p.gate_thr = d.scheme == GBCA_STOCHASTIC ? threshold(d.scheme_p, d.scheme_p_f32 != 0) : 0;
+    p.params_f32 = d.params_f32;
+    p.ngates = d.scheme == GBCA_CHECKERBOARD ? 2 : 1;
+    return p;
+}
+
+int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams) {
+    gbca::SweepParams p = base_params(h);
+    if (h->d.rule == GBCA_RULE_FOREST_FIRE) {
+        if (!params || nparams < 2)
+            return fail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
+        p.thr_p = threshold(params[0], h->d.params_f32 != 0);
+        p.thr_f = threshold(params[1], h->d.params_f32 != 0);
+    }
+    const bool fire = gbca::fire_fast_supported(p);
+    const bool life = !fire && gbca::life_simd_supported(p);
+    while (nsteps > 0) {
+        int64_t k;
+        cudaError_t e;
+        const int8_t* src = (const int8_t*)h->buf[h->cur];
+        int8_t* dst = (int8_t*)h->buf[h->cur ^ 1];
+        p.t0 = t;
+        if (fire) {
+            k = nsteps < 8 ? nsteps : 8;
+            p.nsub = (int32_t)k;
+            e = gbca::launch_fire(p, src, dst, h->stream);
+        } else if (life) {
+            k = nsteps < 4 ? nsteps : 4;
+            p.nsub = (int32_t)k;
+            e = gbca::launch_life_simd(p, src, dst, h->stream);
+        } else {
+            const int r = p.radius;
+            int64_t per = 32 / (r * p.ngates);
+            if (per < 1) per = 1;
+            k = nsteps < per ? nsteps : per;
+            p.nsub = (int32_t)(k * p.ngates);
+            p.tile_x = p.tile_y = 64;
+            p.halo_x = p.halo_y = p.nsub * r;
+            e = gbca::launch_generic(p, src, dst, h->stream);
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+        h->cur ^= 1;
+        t += k;
+        nsteps -= k;
+    }
+    return GBCA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbca_last_error(void) { return g_err.c_str(); }
+
+int32_t gbca_version(void) { return 100; }
+
+int32_t gbca_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+uint64_t gbca_threshold(double p, int32_t f32) { return threshold(p, f32 != 0); }
+
+int gbca_check(const gbca_desc* desc) { return check_desc(desc); }
+
+int gbca_create(const gbca_desc* desc, gbca_handle** out) {
+    if (!out) return fail(GBCA_ERR_ARGUMENT, "null output handle");
+    *out = nullptr;
+    int rc = check_desc(desc);
+    if (rc != GBCA_OK) return rc;
+    if (gbca_device_count() < 1) return fail(GBCA_ERR_CUDA, "no CUDA device is visible");
+    gbca_handle* h = new gbca_handle();
+    h->d = *desc;
+    h->esize = desc->rule == GBCA_RULE_LENIA ? 4 : 1;
+    const int64_t row = desc->n1 * (int64_t)h->esize;
+    h->pitch = (row + 127) / 128 * 128;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev);
+    const size_t bytes = (size_t)h->pitch * (size_t)desc->n2;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf[0], bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf[1], bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&h->acc, gbca::kMeasureWords * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->acc_host, gbca::kMeasureWords * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->buf[0], 0, bytes, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->buf[1], 0, bytes, h->stream);
+    if (e == cudaSuccess && desc->rule == GBCA_RULE_LENIA) {
+        rc = gbca::lenia_create(*desc, h->pitch, h->stream, &h->lenia, g_err);
+        if (rc != GBCA_OK) {
+            gbca_destroy(h);
+            return rc;
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        const bool oom = e == cudaErrorMemoryAllocation;
+        gbca_destroy(h);
+        cudaGetLastError();
+        return oom ? fail(GBCA_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed", 2 * bytes)
+                   : cuda_fail(e, "gbca_create");
+    }
+    *out = h;
+    return GBCA_OK;
+}
+
+int gbca_destroy(gbca_handle* h) {
+    if (!h) return GBCA_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->lenia) gbca::lenia_destroy(h->lenia);
+    cudaFree(h->buf[0]);
+    cudaFree(h->buf[1]);
+    cudaFree(h->acc);
+    if (h->acc_host) cudaFreeHost(h->acc_host);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GBCA_OK;
+}
+
+int gbca_set_state(gbca_handle* h, const void* host, size_t nbytes) {
+    if (!h || !host) return fail(GBCA_ERR_ARGUMENT, "null handle or state");
+    const size_t row = (size_t)h->d.n1 * h->esize;
+    if (nbytes != row * (size_t)h->d.n2)
+        return fail(GBCA_ERR_STATE, "the state has %zu bytes, the lattice needs %zu", nbytes, row * (size_t)h->d.n2);
+    GBCA_CUDA(cudaMemcpy2DAsync(h->buf[h->cur], (size_t)h->pitch, host, row, row, (size_t)h->d.n2,
+                                cudaMemcpyHostToDevice, h->stream),
+              "set_state copy");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_state");
+    return GBCA_OK;
+}
+
+int gbca_get_state(gbca_handle* h, void* host, size_t nbytes) {
+    if (!h || !host) return fail(GBCA_ERR_ARGUMENT, "null handle or state");
+    const size_t row = (size_t)h->d.n1 * h->esize;
+    if (nbytes != row * (size_t)h->d.n2)
+        return fail(GBCA_ERR_STATE, "the buffer has %zu bytes, the lattice needs %zu", nbytes, row * (size_t)h->d.n2);
+    GBCA_CUDA(cudaMemcpy2DAsync(host, row, h->buf[h->cur], (size_t)h->pitch, row, (size_t)h->d.n2,
+                                cudaMemcpyDeviceToHost, h->stream),
+              "current_state copy");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "current_state");
+    return GBCA_OK;
+}
+
+int gbca_advance(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (nsteps < 0) return fail(GBCA_ERR_ARGUMENT, "nsteps must be non-negative, got %lld", (long long)nsteps);
+    if (nsteps == 0) return GBCA_OK;
+    if (h->d.rule == GBCA_RULE_LENIA) {
+        const int rc = gbca::lenia_advance(h->lenia, (const float*)h->buf[h->cur], (float*)h->buf[h->cur ^ 1], nsteps,
+                                           h->stream, &h->cur, h->buf, g_err);
+        return rc;
+    }
+    return advance_int8(h, t, nsteps, params, nparams);
+}
+
+int gbca_read_cell(gbca_handle* h, int64_t i, int64_t j, void* out) {
+    if (!h || !out) return fail(GBCA_ERR_ARGUMENT, "null handle or output");
+    if (i < 1 || i > h->d.n1 || j < 1 || j > h->d.n2)
+        return fail(GBCA_ERR_ARGUMENT, "index (%lld, %lld) is outside the %lld x %lld lattice", (long long)i,
+                    (long long)j, (long long)h->d.n1, (long long)h->d.n2);
+    const char* src = (const char*)h->buf[h->cur] + (i - 1) * (int64_t)h->esize + (j - 1) * h->pitch;
+    GBCA_CUDA(cudaMemcpyAsync(out, src, h->esize, cudaMemcpyDeviceToHost, h->stream), "read_cell");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "read_cell");
+    return GBCA_OK;
+}
+
+int gbca_write_cell(gbca_handle* h, int64_t i, int64_t j, const void* value) {
+    if (!h || !value) return fail(GBCA_ERR_ARGUMENT, "null handle or value");
+    if (i < 1 || i > h->d.n1 || j < 1 || j > h->d.n2)
+        return fail(GBCA_ERR_ARGUMENT, "index (%lld, %lld) is outside the %lld x %lld lattice", (long long)i,
+                    (long long)j, (long long)h->d.n1, (long long)h->d.n2);
+    char* dst = (char*)h->buf[h->cur] + (i - 1) * (int64_t)h->esize + (j - 1) * h->pitch;
+    GBCA_CUDA(cudaMemcpyAsync(dst, value, h->esize, cudaMemcpyHostToDevice, h->stream), "write_cell");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "write_cell");
+    return GBCA_OK;
+}
+
+int gbca_sync(gbca_handle* h) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "sync");
+    return GBCA_OK;
+}
+
+int gbca_summaries(gbca_handle* h, int64_t* counts, int32_t nvals, int64_t* other, double* morans) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (h->d.rule == GBCA_RULE_LENIA) return fail(GBCA_ERR_UNSUPPORTED, "summaries need an Int8 state");
+    if (nvals < 0 || nvals > 128) return fail(GBCA_ERR_ARGUMENT, "nvals must be in 0:128, got %d", nvals);
+    GBCA_CUDA(gbca::launch_measures((const int8_t*)h->buf[h->cur], h->d.n1, h->d.n2, h->pitch, h->d.boundary[0],
+                                    h->d.boundary[1], h->acc, h->nsm, h->stream),
+              "summaries launch");
+    GBCA_CUDA(cudaMemcpyAsync(h->acc_host, h->acc, gbca::kMeasureWords * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, h->stream),
+              "summaries copy");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "summaries");
+    gbca::finish_measures(h->acc_host, h->d.n1 * h->d.n2, counts, nvals, other, morans);
+    return GBCA_OK;
+}
+
+int gbca_device_state(gbca_handle* h, void** dptr, int64_t* pitch) {
+    if (!h || !dptr) return fail(GBCA_ERR_ARGUMENT, "null handle or output");
+    *dptr = h->buf[h->cur];
+    if (pitch) *pitch = h->pitch;
+    return GBCA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+// gbca_internal.cuh — device helpers shared by the sweep kernels of libgbca.so:
+// the counter-based Philox4x32-10 draws keyed as src/random.jl:102-107, the
+// boundary mapping of src/spaces.jl:46-51, and the launch parameters of a sweep.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gbca.h"
+
+namespace gbca {
+
+// ----------------------------------------------------------------- Philox4x32-10
+
+constexpr uint32_t kPhM0 = 0xD2511F53u;
+constexpr uint32_t kPhM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhW0 = 0x9E3779B9u;
+constexpr uint32_t kPhW1 = 0xBB67AE85u;
+
+// Words 1 and 2 of philox4x32(ctr, key) (src/random.jl:24-37): ten rounds, the key
+// bumped after rounds 1..9. Only words 1 and 2 feed the draws (random.jl:109-120),
+// so round 10 needs one of its two products.
+__device__ __forceinline__ uint2 philox_w01(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                            uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const uint32_t hi0 = __umulhi(kPhM0, c0), lo0 = kPhM0 * c0;
+        const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += kPhW0; k1 += kPhW1;
+    }
+    const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
+    return make_uint2(hi1 ^ c1 ^ k0, lo1);
+}
+
+// The draw of cell `id` (1-based column-major linear index, backends.jl:446) at time t
+// with draw index k: counter (id lo, id hi, t mod 2^32, k), key (seed lo, seed hi).
+__device__ __forceinline__ uint2 cell_draw(uint64_t seed, uint64_t id, int64_t t, uint32_t k) {
+    return philox_w01((uint32_t)id, (uint32_t)(id >> 32), (uint32_t)(uint64_t)t, k,
+                      (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// uniform(...) < p, evaluated exactly as an integer compare against a host-computed
+// threshold: for a Float64 p the 53-bit integer x of random.jl:118-119, for a Float32 p
+// the 24-bit integer of random.jl:111.
+__device__ __forceinline__ bool draw_below(uint2 w, uint64_t thr, bool f32) {
+    if (f32) return (uint64_t)(w.x >> 8) < thr;
+    return ((((uint64_t)w.x << 32) | (uint64_t)w.y) >> 11) < thr;
+}
+
+// Per-step constant part of a cell draw: the counter words that do not depend on the
+// cell (t in word 3, the id's high word 0 in word 2) make the first product of round 1
+// and both words of round 2's first product uniform across a sub-step. DrawStep holds
+// them; draw_fast() then needs 17 per-cell 32x32 products instead of 19. Valid only for
+// ids below 2^32 (lattices of fewer than 4.29e9 cells); the caller checks that.
+struct DrawStep {
+    uint32_t c0_1, c1_1;  // words 1, 2 after round 1 (uniform)
+    uint32_t hi0_2, lo0_2;  // M0 * c0_1 (uniform, used in round 2)
+    uint32_t k0, k1;      // key
+};
+
+__device__ __forceinline__ DrawStep draw_step(uint64_t seed, int64_t t) {
+    DrawStep s;
+    s.k0 = (uint32_t)seed;
+    s.k1 = (uint32_t)(seed >> 32);
+    const uint32_t c2 = (uint32_t)(uint64_t)t;
+    const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
+    s.c0_1 = hi1 ^ 0u ^ s.k0;  // c1 = id hi = 0
+    s.c1_1 = lo1;
+    s.hi0_2 = __umulhi(kPhM0, s.c0_1);
+    s.lo0_2 = kPhM0 * s.c0_1;
+    return s;
+}
+
+__device__ __forceinline__ uint2 draw_fast(const DrawStep& s, uint32_t id, uint32_t k) {
+    // round 1 (c0 = id, c1 = 0, c2 = t, c3 = k)
+    const uint32_t hi0 = __umulhi(kPhM0, id), lo0 = kPhM0 * id;
+    uint32_t c0 = s.c0_1, c1 = s.c1_1, c2 = hi0 ^ k ^ s.k1, c3 = lo0;
+    uint32_t k0 = s.k0 + kPhW0, k1 = s.k1 + kPhW1;
+    // round 2: the M0 product of c0 is uniform
+    {
+        const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = s.hi0_2 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = s.lo0_2;
+        k0 += kPhW0; k1 += kPhW1;
+    }
+#pragma unroll
+    for (int r = 2; r < 9; ++r) {
+        const uint32_t hi0r = __umulhi(kPhM0, c0), lo0r = kPhM0 * c0;
+        const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0r ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0r;
+        k0 += kPhW0; k1 += kPhW1;
+    }
+    const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
+    return make_uint2(hi1 ^ c1 ^ k0, lo1);
+}
+
+// ----------------------------------------------------------------- boundaries
+
+// 0-based version of _map_axis (src/spaces.jl:46-51): the mapped index, or -1 when the
+// index lies beyond a Constant edge.
+__host__ __device__ __forceinline__ int64_t map_axis(int32_t b, int64_t g, int64_t n) {
+    if (b == GBCA_PERIODIC) {
+        int64_t m = g % n;
+        return m < 0 ? m + n : m;
+    }
+    if (b == GBCA_REFLECTING) {
+        int64_t m = g % (2 * n);
+        if (m < 0) m += 2 * n;
+        return m < n ? m : 2 * n - 1 - m;
+    }
+    return (g >= 0 && g < n) ? g : -1;
+}
+
+// ----------------------------------------------------------------- sweep parameters
+
+// Everything a sweep launch needs besides the buffers. Plain data, passed by value.
+struct SweepParams {
+    int64_t n1, n2, pitch;     // lattice dims; bytes between consecutive columns
+    int32_t bnd[2];
+    int32_t cval[2];           // Constant value per axis (as the state's element value)
+    int32_t rule, nbhd, radius, states;
+    uint64_t birth, survive;
+    uint64_t seed;
+    int32_t scheme;            // gate kind
+    int32_t gate_f32;
+    uint64_t gate_thr;         // Stochastic(p) threshold
+    uint64_t thr_p, thr_f;     // forest fire thresholds (draws 1 and 2)
+    int32_t params_f32;
+    int32_t nsub;              // sub-steps in this launch (steps * gates)
+    int32_t ngates;            // 2 for Checkerboard, else 1
+    int32_t sub0;              // index of the first sub-step within its step (0 or 1)
+    int64_t t0;                // time of the first sub-step's step
+    int32_t tile_x, tile_y;    // output tile
+    int32_t halo_x, halo_y;    // loaded halo (>= nsub * radius)
+};
+
+// Launchers (one translation unit each).
+cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
+bool life_simd_supported(const SweepParams& p);
+cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
+bool fire_fast_supported(const SweepParams& p);
+cudaError_t launch_fire(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
+
+}  // namespace gbca

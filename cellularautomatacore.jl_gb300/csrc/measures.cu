@@ -1,0 +1,104 @@
+// measures.cu — state_counts (src/measures.jl:14-20) and Moran's I with VonNeumann(1)
+// (src/measures.jl:91-107) on an Int8 state in HBM, as exact integer sums.
+//
+// Moran's I is  n/W * sum_i sum_{j in N(i)} (x_i - m)(x_j - m) / sum_i (x_i - m)^2  with
+// m = S/n. Expanding the products, it is a ratio of integers,
+//   (n^2 P - n S Q + W S^2) / (W (n S2 - S^2)),
+// where S = sum x, S2 = sum x^2, P = sum over neighbour pairs of x_i x_j, Q = sum over
+// pairs of (x_i + x_j) and W the number of pairs. The kernel accumulates those integers
+// (order-independent, so every launch shape gives the same bits); the host finishes the
+// ratio in 128-bit integers and divides once.
+#include "gbca_internal.cuh"
+#include "measures.cuh"
+
+namespace gbca {
+
+namespace {
+
+__global__ void __launch_bounds__(256) k_measures(const int8_t* __restrict__ u, int64_t n1, int64_t n2,
+                                                  int64_t pitch, int32_t b1, int32_t b2,
+                                                  unsigned long long* __restrict__ acc) {
+    __shared__ unsigned int hist[256];
+    __shared__ long long sums[5];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) hist[k] = 0;
+    if (threadIdx.x < 5) sums[threadIdx.x] = 0;
+    __syncthreads();
+    long long S = 0, S2 = 0, P = 0, Q = 0, W = 0;
+    const int64_t n = n1 * n2;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = k % n1, j = k / n1;
+        const int x = u[i + j * pitch];
+        atomicAdd(&hist[x + 128], 1u);
+        S += x;
+        S2 += x * x;
+        // VonNeumann(1) offsets in the reference's order: (0,-1), (-1,0), (1,0), (0,1)
+        const int di[4] = {0, -1, 1, 0}, dj[4] = {-1, 0, 0, 1};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int64_t a = map_axis(b1, i + di[q], n1), b = map_axis(b2, j + dj[q], n2);
+            if (a < 0 || b < 0) continue;  // beyond a Constant edge: not a neighbour
+            const int y = u[a + b * pitch];
+            P += x * y;
+            Q += x + y;
+            W += 1;
+        }
+    }
+    // warp reduction, then one atomic per warp into shared, one per block into global
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        S += __shfl_down_sync(0xffffffffu, S, o);
+        S2 += __shfl_down_sync(0xffffffffu, S2, o);
+        P += __shfl_down_sync(0xffffffffu, P, o);
+        Q += __shfl_down_sync(0xffffffffu, Q, o);
+        W += __shfl_down_sync(0xffffffffu, W, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd((unsigned long long*)&sums[0], (unsigned long long)S);
+        atomicAdd((unsigned long long*)&sums[1], (unsigned long long)S2);
+        atomicAdd((unsigned long long*)&sums[2], (unsigned long long)P);
+        atomicAdd((unsigned long long*)&sums[3], (unsigned long long)Q);
+        atomicAdd((unsigned long long*)&sums[4], (unsigned long long)W);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 256; k += blockDim.x)
+        if (hist[k]) atomicAdd(&acc[k], (unsigned long long)hist[k]);
+    if (threadIdx.x < 5) atomicAdd(&acc[256 + threadIdx.x], (unsigned long long)sums[threadIdx.x]);
+}
+
+}  // namespace
+
+cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t b1, int32_t b2,
+                            unsigned long long* acc, int nsm, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(acc, 0, kMeasureWords * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    const int64_t n = n1 * n2;
+    int64_t blocks = (n + 255) / 256;
+    const int64_t cap = (int64_t)nsm * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_measures<<<(unsigned)blocks, 256, 0, st>>>(u, n1, n2, pitch, b1, b2, acc);
+    return cudaGetLastError();
+}
+
+void finish_measures(const unsigned long long* acc, int64_t n, int64_t* counts, int32_t nvals, int64_t* other,
+                     double* morans) {
+    int64_t inrange = 0;
+    for (int v = 0; v < nvals; ++v) {
+        const int64_t c = (v >= 0 && v < 128) ? (int64_t)acc[v + 128] : 0;
+        if (counts) counts[v] = c;
+        inrange += c;
+    }
+    if (other) *other = n - inrange;
+    if (!morans) return;
+    const __int128 S = (long long)acc[256], S2 = (long long)acc[257], P = (long long)acc[258];
+    const __int128 Q = (long long)acc[259], W = (long long)acc[260], N = n;
+    const __int128 num = N * N * P - N * S * Q + W * S * S;
+    const __int128 den = W * (N * S2 - S * S);
+    if (den == 0 || W == 0) {
+        *morans = __builtin_nan("");
+        return;
+    }
+    *morans = (double)((long double)num / (long double)den);
+}
+
+}  // namespace gbca

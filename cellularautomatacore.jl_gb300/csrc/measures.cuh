@@ -1,0 +1,19 @@
+// measures.cuh — device summaries of an Int8 state (counts per value, Moran's I sums).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbca {
+
+// Accumulator layout: [0, 256) histogram of value + 128; then S, S2, P, Q, W.
+constexpr int kMeasureWords = 261;
+
+cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t b1, int32_t b2,
+                            unsigned long long* acc, int nsm, cudaStream_t st);
+
+// counts[v] for v < nvals, *other = cells outside, *morans from the integer sums
+// (NaN for a constant field). Any output pointer may be null.
+void finish_measures(const unsigned long long* acc, int64_t n, int64_t* counts, int32_t nvals, int64_t* other,
+                     double* morans);
+
+}  // namespace gbca

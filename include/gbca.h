@@ -1,0 +1,136 @@
+/*
+ * gbca.h — C ABI of libgbca.so, the GB300 (sm_103a) backend for the synchronous
+ * halo-padded stencil sweep of CellularAutomataCore.jl.
+ *
+ * Each entry point replaces one method of the reference's backend contract
+ * (src/backends.jl:4-14, declared `public` in src/CellularAutomataCore.jl:257), as the
+ * KernelAbstractions GPUBackend implements it (ext/CellularAutomataCoreKernelAbstractionsExt.jl).
+ * Plain C types only: pointers, sizes, fixed-width integers and doubles. No exception
+ * crosses the ABI: every call returns a status (GBCA_OK = 0) and gbca_last_error() gives
+ * the message of the calling thread's last failure.
+ *
+ * States are single-layer, column-major (axis 1 contiguous), exactly the layout of the
+ * reference's `u0` arrays: Int8 for Life / Generations / forest fire, Float32 for Lenia.
+ * Indices are 1-based, as in Julia. A handle owns its device buffers and one CUDA stream;
+ * a handle is not thread-safe, distinct handles are.
+ */
+#ifndef GBCA_H
+#define GBCA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes; the host glue maps them to the reference's exception types */
+#define GBCA_OK 0
+#define GBCA_ERR_ARGUMENT 1            /* ArgumentError */
+#define GBCA_ERR_INCOMPATIBLE_SPACE 2  /* IncompatibleSpaceError (src/errors.jl) */
+#define GBCA_ERR_UNSUPPORTED 3         /* UnsupportedCombinationError (src/errors.jl:124-132) */
+#define GBCA_ERR_STATE 4               /* StateShapeError / InvalidStateError */
+#define GBCA_ERR_CUDA 5                /* a CUDA runtime or cuFFT failure */
+#define GBCA_ERR_OUT_OF_MEMORY 6       /* device memory or an HBM budget is exhausted */
+#define GBCA_ERR_TIMEOUT 7             /* a bounded device-side wait gave up */
+#define GBCA_ERR_BUSY 8                /* a queue is full; retry later */
+
+/* ---- problem description (what check_problem / allocate_state receive as `prob`) */
+enum { GBCA_RULE_LIFE = 1, GBCA_RULE_GENERATIONS = 2, GBCA_RULE_FOREST_FIRE = 3, GBCA_RULE_LENIA = 4 };
+enum { GBCA_MOORE = 1, GBCA_VON_NEUMANN = 2 };
+enum { GBCA_PERIODIC = 0, GBCA_REFLECTING = 1, GBCA_CONSTANT = 2 };
+enum { GBCA_SYNCHRONOUS = 0, GBCA_STOCHASTIC = 1, GBCA_CHECKERBOARD = 2 };
+enum { GBCA_DIRECT = 0, GBCA_FFT = 1 };
+enum { GBCA_INT8 = 1, GBCA_FLOAT32 = 2 };
+
+#define GBCA_MAX_PEAKS 8
+
+typedef struct gbca_desc {
+    int32_t rule;            /* GBCA_RULE_*                                         */
+    int32_t nbhd;            /* GBCA_MOORE / GBCA_VON_NEUMANN (src/neighbourhoods.jl:21,35) */
+    int32_t radius;          /* neighbourhood radius r >= 1                          */
+    int32_t states;          /* Generations: C (src/rules.jl:424-429)               */
+    uint64_t birth;          /* Life / Generations masks: bit n <=> count n (rules.jl:267-275) */
+    uint64_t survive;
+    int64_t n1, n2;          /* lattice dims (src/spaces.jl:94-110)                  */
+    int32_t boundary[2];     /* GBCA_PERIODIC / GBCA_REFLECTING / GBCA_CONSTANT per axis */
+    double constant[2];      /* the Constant(value) of each axis                     */
+    uint64_t seed;           /* prob.seed (src/problem.jl:90)                        */
+    int32_t scheme;          /* GBCA_SYNCHRONOUS / GBCA_STOCHASTIC / GBCA_CHECKERBOARD */
+    int32_t scheme_p_f32;    /* Stochastic(p) with a Float32 p (schemes.jl:86-88)     */
+    double scheme_p;
+    int32_t params_f32;      /* forest fire: p and f are Float32 (random.jl:130)     */
+    int32_t lenia_method;    /* GBCA_DIRECT / GBCA_FFT (src/lenia.jl:24-32)          */
+    int32_t lenia_R;
+    int32_t lenia_npeaks;
+    double lenia_peaks[GBCA_MAX_PEAKS];
+    double lenia_mu, lenia_sigma, lenia_dt;
+} gbca_desc;
+
+typedef struct gbca_handle gbca_handle;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* gbca_last_error(void);
+
+/* Library version: major * 10000 + minor * 100 + patch. */
+int32_t gbca_version(void);
+
+/* Number of CUDA devices (0 without a GPU); never fails. */
+int32_t gbca_device_count(void);
+
+/* Replaces check_problem(b, prob, scheme) (src/backends.jl:97-105; the KA version
+ * ext/CellularAutomataCoreKernelAbstractionsExt.jl:42-49). Validates a description
+ * without touching the GPU. */
+int gbca_check(const gbca_desc* desc);
+
+/* Replaces allocate_state(b, prob, scheme) (src/backends.jl:107-119; KA ext :51-59):
+ * checks the description, allocates the device state on the current device and zeroes
+ * it. The caller then uploads prob.u0 with gbca_set_state. */
+int gbca_create(const gbca_desc* desc, gbca_handle** out);
+
+/* Frees the device buffers and the stream. */
+int gbca_destroy(gbca_handle* h);
+
+/* Replaces set_state!(b, st, u) (src/backends.jl:141-148; KA ext :132-140): copies a
+ * whole host state (n1*n2 elements, column-major) to the device. */
+int gbca_set_state(gbca_handle* h, const void* host, size_t nbytes);
+
+/* Replaces current_state(b, st) (src/backends.jl:132-139; KA ext :126-130): waits for
+ * pending work and copies the whole state to host memory. */
+int gbca_get_state(gbca_handle* h, void* host, size_t nbytes);
+
+/* Replaces advance!(b, st, prob, scheme, p, t) (src/backends.jl:121-130; KA ext :92-110),
+ * `nsteps` times: the state goes from time t to t + nsteps. `params` is the integrator's
+ * p: forest fire {p, f}; unused otherwise (may be NULL with nparams = 0). Work is queued
+ * on the handle's stream; the call returns before it finishes. */
+int gbca_advance(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams);
+
+/* Replaces read_cell(b, st, I) (src/backends.jl:380; KA ext :142): one element at the
+ * 1-based index (i, j), written to `out` (1 byte for Int8, 4 for Float32). */
+int gbca_read_cell(gbca_handle* h, int64_t i, int64_t j, void* out);
+
+/* Replaces write_cell!(b, st, I, v) (src/backends.jl:381-383; KA ext :143-148). */
+int gbca_write_cell(gbca_handle* h, int64_t i, int64_t j, const void* value);
+
+/* Waits for the handle's queued work. */
+int gbca_sync(gbca_handle* h);
+
+/* state_counts (src/measures.jl:14-20) and Moran's I with VonNeumann(1) on the problem's
+ * lattice (src/measures.jl:91-107), computed on the device from the current Int8 state.
+ * counts[v] for v in 0..nvals-1; *other gets the number of cells outside that range.
+ * *morans is NaN for a constant field (where the reference raises ArgumentError). */
+int gbca_summaries(gbca_handle* h, int64_t* counts, int32_t nvals, int64_t* other, double* morans);
+
+/* Device pointer of the current state buffer (pitch in bytes between columns in *pitch),
+ * valid until the next gbca_advance / gbca_destroy. For callers that keep inputs in HBM. */
+int gbca_device_state(gbca_handle* h, void** dptr, int64_t* pitch);
+
+/* Host helper: the integer threshold T with  uniform < p  <=>  x < T, where x is the
+ * 53-bit (f32 = 0: random.jl:116-120) or 24-bit (f32 = 1: random.jl:109-114) integer
+ * behind the draw. NaN and p <= 0 give 0; p >= 1 gives 2^53 (2^24). */
+uint64_t gbca_threshold(double p, int32_t f32);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

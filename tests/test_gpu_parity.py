@@ -1,0 +1,180 @@
+"""GPU parity: the GB300 backend, driven through solve() and the C ABI, reproduces the
+oracle (the reference's ReferenceBackend / ArrayBackend arithmetic) bit for bit on the
+Int8 conformance cases, as test/backend_conformance.jl:264-287 demands of every backend
+(`sol.t == ref.t && sol.u == ref.u`)."""
+import zlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ca():
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.load_package()
+    if m.capi.lib().gbca_device_count() < 1:
+        pytest.fail("no CUDA device visible")
+    return m
+
+
+def spec_pair(ca, o, kind, n1, n2, *, nb="moore", r=1, birth=(), survive=(), states=2, bnd=("p", "p"),
+              const=(0, 0), seed=0, scheme="sync", sp=1.0, sp32=False, f32=False):
+    """The same problem for the product (rule, space, scheme) and for the oracle."""
+    bk = {"p": (ca.Periodic(), o.PERIODIC), "r": (ca.Reflecting(), o.REFLECTING)}
+    bounds, obounds = [], []
+    for a, b in enumerate(bnd):
+        if b == "c":
+            bounds.append(ca.Constant(const[a]))
+            obounds.append(o.CONSTANT)
+        else:
+            bounds.append(bk[b][0])
+            obounds.append(bk[b][1])
+    N = ca.Moore(r) if nb == "moore" else ca.VonNeumann(r)
+    if kind == "life":
+        rule = ca.Life(list(birth), list(survive), neighbourhood=N)
+        orule = o.RULE_LIFE
+    elif kind == "gen":
+        rule = ca.Generations("B" + "".join(map(str, birth)) + "/S" + "".join(map(str, survive)) + f"/C{states}",
+                              neighbourhood=N)
+        orule = o.RULE_GENERATIONS
+    else:
+        rule = ca.ForestFire(neighbourhood=N, float32=f32)
+        orule = o.RULE_FOREST_FIRE
+    scheme = {"sync": ca.Synchronous(), "stoch": ca.Stochastic(sp, float32=sp32), "check": ca.Checkerboard()}[scheme]
+    P = o.Problem(orule, n1, n2, nbhd=o.MOORE if nb == "moore" else o.VON_NEUMANN, radius=r,
+                  birth=o.mask(birth), survive=o.mask(survive), states=states, boundary=tuple(obounds),
+                  constant=tuple(int(c) for c in const), seed=seed,
+                  scheme={ca.Synchronous: o.SYNCHRONOUS, ca.Stochastic: o.STOCHASTIC,
+                          ca.Checkerboard: o.CHECKERBOARD}[type(scheme)],
+                  scheme_p=scheme.p if isinstance(scheme, ca.Stochastic) else 1.0, scheme_p_f32=sp32, params_f32=f32)
+    return rule, ca.Lattice((n1, n2), tuple(bounds)), scheme, P
+
+
+CASES = [
+    # name, kind, dims, kwargs, steps, saveat, params
+    ("Life on a torus", "life", (20, 24), dict(birth=[3], survive=[2, 3]), 30, 1, None),
+    ("Life on a cylinder", "life", (20, 24), dict(birth=[3], survive=[2, 3], bnd=("p", "c")), 30, 7, None),
+    ("radius-2 von Neumann, mixed edges", "life", (15, 17),
+     dict(nb="vn", r=2, birth=[3], survive=[2, 3, 4, 5], bnd=("r", "c"), const=(0, 1)), 20, 3, None),
+    ("Brian's Brain", "gen", (18, 18), dict(birth=[2], survive=[], states=3), 25, 5, None),
+    ("Star Wars, reflecting", "gen", (37, 29), dict(birth=[2], survive=[3, 4, 5], states=4, bnd=("r", "r")), 25, 25,
+     None),
+    ("Moore(4) wider than the torus", "life", (3, 7), dict(r=4, birth=[5, 6, 7], survive=[4, 5, 6, 7, 8]), 8, 1,
+     None),
+    ("Larger than Life Moore(5) torus", "life", (97, 83), dict(r=5, birth=range(34, 46), survive=range(34, 59)), 40,
+     10, None),
+    ("Larger than Life Moore(3) grid", "life", (70, 90),
+     dict(r=3, birth=range(9, 15), survive=range(8, 20), bnd=("c", "c")), 30, 10, None),
+    ("Stochastic(0.4) Life", "life", (20, 20), dict(birth=[3], survive=[2, 3], seed=2, scheme="stoch", sp=0.4), 15,
+     1, None),
+    ("Stochastic(0.5f0) Life", "life", (33, 20),
+     dict(birth=[3], survive=[2, 3], seed=12, scheme="stoch", sp=0.5, sp32=True), 15, 5, None),
+    ("Checkerboard majority", "life", (18, 18),
+     dict(nb="vn", birth=[5, 6, 7, 8], survive=[4, 5, 6, 7, 8], scheme="check"), 10, 1, None),
+    ("Checkerboard odd torus", "life", (19, 17), dict(nb="vn", birth=[2, 3], survive=[1, 2], scheme="check"), 12, 4,
+     None),
+    ("forest fire, small grid", "fire", (40, 30), dict(nb="vn", seed=3, bnd=("c", "c")), 30, 3, (0.3, 0.01)),
+    ("forest fire, Float32 parameters, torus", "fire", (33, 21), dict(nb="vn", seed=5, f32=True), 30, 10,
+     (0.3, 0.01)),
+    ("forest fire, tiled grid", "fire", (1000, 700), dict(nb="vn", seed=3, bnd=("c", "c")), 37, 37, (0.05, 0.001)),
+    ("forest fire, tiled torus", "fire", (800, 520), dict(nb="vn", seed=8), 21, 7, (0.05, 0.001)),
+    ("forest fire, reflecting, Moore(1)", "fire", (130, 90), dict(nb="moore", seed=4, bnd=("r", "r")), 20, 10,
+     (0.1, 0.002)),
+    ("forest fire, Stochastic(0.7)", "fire", (64, 80), dict(nb="vn", seed=6, scheme="stoch", sp=0.7), 20, 5,
+     (0.2, 0.01)),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_conformance(ca, oracle, case):
+    name, kind, (n1, n2), kw, steps, saveat, params = case
+    rule, space, scheme, P = spec_pair(ca, oracle, kind, n1, n2, **kw)
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
+    C = 3 if kind == "fire" else P.states
+    u0 = rng.integers(0, C, (n1, n2)).astype(np.int8)
+    pd = None if params is None else {"p": params[0], "f": params[1]}
+    prob = ca.CAProblem.new(rule, u0, steps, pd, space=space, seed=kw.get("seed", 0))
+    sol = ca.solve(prob, scheme, backend=ca.GB300Backend(), saveat=saveat)
+    ts, us = oracle.solve(P, u0, steps, saveat=saveat, params=params, nthreads=8)
+    assert sol.t == ts
+    for k, (a, b) in enumerate(zip(sol.u, us)):
+        assert np.array_equal(a, b), f"{name}: save {k} (t = {ts[k]}) differs in {(a != b).sum()} cells"
+    assert not np.array_equal(us[-1], u0)
+
+
+def test_highlife_128_config(ca, oracle):
+    """Life(:highlife) on a 128x128 torus, Bernoulli(0.5) Int8 soup from seed 1, 200 steps, saveat=20:
+    all 11 saved states equal the oracle's."""
+    u0 = np.random.default_rng(1).integers(0, 2, (128, 128)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.Life(":highlife"), u0, 200)
+    sol = ca.solve(prob, ca.Synchronous(), backend=ca.GB300Backend(), saveat=20)
+    P = oracle.Problem(oracle.RULE_LIFE, 128, 128, birth=oracle.mask([3, 6]), survive=oracle.mask([2, 3]))
+    ts, us = oracle.solve(P, u0, 200, saveat=20, nthreads=8)
+    assert sol.t == ts == list(range(0, 201, 20))
+    assert all(np.array_equal(a, b) for a, b in zip(sol.u, us))
+
+
+def test_state_round_trip_and_cells(ca):
+    u = np.random.default_rng(3).integers(-128, 128, (37, 45)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), np.zeros((37, 45), np.int8), 5, {"p": 0.1, "f": 0.0})
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    ca.set_state(B, st, u)
+    assert np.array_equal(ca.current_state(B, st), u)
+    assert ca.read_cell(B, st, (5, 7)) == u[4, 6]
+    ca.write_cell(B, st, (37, 45), -7)
+    assert ca.read_cell(B, st, (37, 45)) == -7
+    with pytest.raises(ca.ArgumentError):
+        ca.read_cell(B, st, (38, 1))
+    with pytest.raises(ca.StateShapeError):
+        ca.set_state(B, st, np.zeros((3, 3), np.int8))
+    st.close()
+
+
+def test_integrator_modification_and_reinit(ca, oracle):
+    """test/test_backend_interface.jl:86-97: a changed integ.u is applied before the next
+    step; reinit! replays the run (draws are a pure function of seed, cell and time)."""
+    u0 = np.random.default_rng(4).integers(0, 3, (50, 40)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 20, {"p": 0.2, "f": 0.01}, space=ca.Grid(50, 40), seed=9)
+    integ = ca.init(prob, backend=ca.GB300Backend())
+    ca.step(integ, 4)
+    u = integ.u.copy()
+    u[0, 0] = 2
+    integ.u = u
+    ca.step(integ)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, 50, 40, nbhd=oracle.VON_NEUMANN, seed=9,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    ref = oracle.run_array(P, u0, 0, 4, (0.2, 0.01))
+    ref[0, 0] = 2
+    ref = oracle.run_array(P, ref, 4, 1, (0.2, 0.01))
+    assert np.array_equal(integ.u, ref) and integ.t == 5
+    # parameters changed by a callback apply from the next step on
+    integ.p = {"p": 0.0, "f": 0.0}
+    ca.step(integ, 3)
+    assert np.array_equal(integ.u, oracle.run_array(P, ref, 5, 3, (0.0, 0.0)))
+    ca.reinit(integ)
+    ca.step(integ, 6)
+    assert np.array_equal(integ.u, oracle.run_array(P, u0, 0, 6, (0.2, 0.01)))
+
+
+def test_device_summaries(ca, oracle):
+    rng = np.random.default_rng(5)
+    for bnd, ob in (((ca.Periodic(), ca.Periodic()), (oracle.PERIODIC, oracle.PERIODIC)),
+                    ((ca.Constant(0), ca.Constant(0)), (oracle.CONSTANT, oracle.CONSTANT)),
+                    ((ca.Reflecting(), ca.Constant(0)), (oracle.REFLECTING, oracle.CONSTANT))):
+        u = rng.integers(0, 3, (300, 170)).astype(np.int8)
+        prob = ca.CAProblem.new(ca.ForestFire(), u, 1, {"p": 0.0, "f": 0.0}, space=ca.Lattice((300, 170), bnd))
+        B = ca.GB300Backend()
+        st = ca.allocate_state(B, prob, ca.Synchronous())
+        counts, other, mi = ca.device_summaries(st, 3)
+        want_counts, want_other = oracle.state_counts(u, 3)
+        want_mi = oracle.morans_i(oracle.Problem(oracle.RULE_LIFE, 300, 170, boundary=ob), u)
+        assert counts == want_counts and other == want_other
+        assert abs(mi - want_mi) <= 1e-12 * max(1.0, abs(want_mi)), (mi, want_mi)
+        st.close()
+    checker = np.array([[(i + j) % 2 for j in range(6)] for i in range(6)], np.int8)
+    st = ca.allocate_state(ca.GB300Backend(), ca.CAProblem.new(ca.Life(), checker, 1), ca.Synchronous())
+    assert abs(ca.device_summaries(st, 2)[2] + 1.0) < 1e-15  # test/test_extras.jl:140-141
