@@ -1,0 +1,362 @@
+"""Benchmark of the GB300 stencil-sweep backend (one JSON line on rank 0).
+
+Workload (the single-instance sweeps at scale):
+  (a) Larger than Life, Moore(5), birth 34..45 / survive 34..58, 8192 x 8192 Int8 torus,
+      density 0.5 from seed 2, 1000 Synchronous steps;
+  (b) forest fire, VonNeumann(1), Int8 codes {0 empty, 1 tree, 2 fire}, 16384 x 16384 Grid
+      with Constant(0) edges, all empty at t = 0, p = 0.03, f = 1e-4, seed 3, 500 steps.
+One bench step runs both from their initial states. Metric: Gcell-updates/s
+(cells x steps / time) over the whole step.
+
+  value : device-resident — initial states are copied device-to-device into the handles,
+          then advanced; CUDA events on the stream the library launches on.
+  e2e   : the same through the C ABI with host buffers — set_state from pinned host memory,
+          advance, current_state back to pinned host memory, every step.
+  roofline: the dominant kernel (by device time), algorithmic bytes 2 B per cell-update
+          (Int8 read + write) over its average launch duration, against the measured HBM copy
+          bandwidth in MEASURED_PEAKS.json.
+  cpu_baseline: the CPU oracle (C restatement of the reference's threaded ArrayBackend slab
+          sweep) on a bounded sample of the same workload, on this host's cores.
+
+--impl reference times that CPU implementation alone (the reference is Julia, which is not
+installed; its C restatement runs in its place) on bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LTL = dict(name="ltl", n1=8192, n2=8192, steps=1000, radius=5)
+FIRE = dict(name="fire", n1=16384, n2=16384, steps=500, p=0.03, f=1e-4, seed=3)
+BYTES_PER_CELL_UPDATE = 2  # one Int8 read + one Int8 write
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def initial_states():
+    rng = np.random.Generator(np.random.PCG64(2))
+    ltl0 = np.asfortranarray((rng.random((LTL["n1"], LTL["n2"])) < 0.5).astype(np.int8))
+    fire0 = np.zeros((FIRE["n1"], FIRE["n2"]), dtype=np.int8, order="F")
+    return ltl0, fire0
+
+
+def cell_updates():
+    return LTL["n1"] * LTL["n2"] * LTL["steps"] + FIRE["n1"] * FIRE["n2"] * FIRE["steps"]
+
+
+def descs(capi):
+    from cellularautomatacore_jl_gb300.model import Life
+    d1 = capi.Desc()
+    life = Life(range(34, 46), range(34, 59))
+    d1.rule, d1.nbhd, d1.radius, d1.states = capi.RULE_LIFE, capi.MOORE, 5, 2
+    d1.birth, d1.survive = life.birth, life.survive
+    d1.n1, d1.n2, d1.seed = LTL["n1"], LTL["n2"], 2
+    d2 = capi.Desc()
+    d2.rule, d2.nbhd, d2.radius = capi.RULE_FOREST_FIRE, capi.VON_NEUMANN, 1
+    d2.n1, d2.n2, d2.seed = FIRE["n1"], FIRE["n2"], FIRE["seed"]
+    d2.boundary[0] = d2.boundary[1] = capi.CONSTANT
+    return d1, d2
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.proc = index, None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from its committed ncu summary, when there is one
+    (a line 'traffic_bytes_per_launch: N')."""
+    for name in os.listdir(os.path.join(ROOT, "profiles")) if os.path.isdir(os.path.join(ROOT, "profiles")) else []:
+        if name.startswith(kernel) and name.endswith(".md"):
+            with open(os.path.join(ROOT, "profiles", name)) as f:
+                for line in f:
+                    if line.strip().startswith("traffic_bytes_per_launch:"):
+                        return float(line.split(":", 1)[1])
+    return None
+
+
+def cpu_sample(nthreads: int):
+    """The oracle (C restatement of ArrayBackend's threaded slab sweep) on a bounded sample:
+    3 LtL steps on the 8192^2 torus and 1 forest-fire step on the 16384^2 grid."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as o
+    o.build()
+    ltl0, _ = initial_states()
+    P1 = o.Problem(o.RULE_LIFE, LTL["n1"], LTL["n2"], radius=5, birth=o.mask(range(34, 46)),
+                   survive=o.mask(range(34, 59)))
+    P2 = o.Problem(o.RULE_FOREST_FIRE, FIRE["n1"], FIRE["n2"], nbhd=o.VON_NEUMANN, seed=FIRE["seed"],
+                   boundary=(o.CONSTANT, o.CONSTANT))
+    # a fire state with trees, fires and empty cells (the all-empty start only draws once)
+    rng = np.random.Generator(np.random.PCG64(3))
+    pct = rng.integers(0, 100, size=(FIRE["n2"], FIRE["n1"]), dtype=np.int8).T
+    fire_mid = np.asfortranarray((pct >= 40).astype(np.int8) + (pct >= 99).astype(np.int8))
+    t0 = time.perf_counter()
+    o.run_array(P1, ltl0, 0, 3, None, nthreads)
+    t1 = time.perf_counter()
+    o.run_array(P2, fire_mid, 0, 1, (FIRE["p"], FIRE["f"]), nthreads)
+    t2 = time.perf_counter()
+    cu = 3 * LTL["n1"] * LTL["n2"] + FIRE["n1"] * FIRE["n2"]
+    # weight the two parts as the full workload does (1000:500 steps on 8192^2:16384^2)
+    r1 = 3 * LTL["n1"] * LTL["n2"] / (t1 - t0)
+    r2 = FIRE["n1"] * FIRE["n2"] / (t2 - t1)
+    w1 = LTL["n1"] * LTL["n2"] * LTL["steps"]
+    w2 = FIRE["n1"] * FIRE["n2"] * FIRE["steps"]
+    rate = (w1 + w2) / (w1 / r1 + w2 / r2)
+    return {"value": rate / 1e9, "unit": "Gcell-updates/s", "cores": nthreads, "kind": "port",
+            "sample": "C restatement of ArrayBackend (threaded slabs): 3 steps of the 8192^2 LtL torus and 1 step "
+                      "of the 16384^2 forest-fire grid (40% empty, 59% trees, 1% fire), combined with the "
+                      "workload's 1000:500 step weights",
+            "parts_gcells": {"ltl": r1 / 1e9, "fire": r2 / 1e9}, "seconds": t2 - t0, "cell_updates": cu}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(nthreads)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_sample(nthreads)["value"])
+    wall = time.perf_counter() - t0
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": "Gcell-updates/s", "value": v, "unit": "Gcell-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int8", "data": "synthetic",
+            "config": {"workload": "single-instance sweeps: LtL Moore(5) 8192^2 torus x1000 + forest fire "
+                                   "16384^2 Grid x500 (bounded CPU samples per step)"},
+            "cpu_baseline": {"value": v, "unit": "Gcell-updates/s", "cores": nthreads, "kind": "port",
+                             "sample": "per step: 3 LtL steps on 8192^2 + 1 forest-fire step on 16384^2"},
+            "e2e": {"value": v, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    ca = ge.load_package()
+    capi = ca.capi
+    lib = capi.lib()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    ltl0, fire0 = initial_states()
+    d1, d2 = descs(capi)
+    handles = []
+    for d in (d1, d2):
+        h = ctypes.c_void_p()
+        capi.check(lib.gbca_create(ctypes.byref(d), ctypes.byref(h)))
+        handles.append(h)
+    stream = torch.cuda.Stream()
+    for h in handles:
+        capi.check(lib.gbca_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+    # pristine device copies of the initial states (column-major bytes)
+    dev0 = [torch.from_numpy(np.ascontiguousarray(a.T)).cuda() for a in (ltl0, fire0)]
+    params_fire = (ctypes.c_double * 2)(FIRE["p"], FIRE["f"])
+    sizes = [(LTL["n1"], LTL["n2"]), (FIRE["n1"], FIRE["n2"])]
+
+    def step_resident(events=None):
+        for k, (h, d0, (n1, n2)) in enumerate(zip(handles, dev0, sizes)):
+            capi.check(lib.gbca_set_state_device(h, ctypes.c_void_p(d0.data_ptr()), n1))
+            if events is not None:
+                events[2 * k].record(stream)
+            if k == 0:
+                capi.check(lib.gbca_advance(h, 0, LTL["steps"], None, 0))
+            else:
+                capi.check(lib.gbca_advance(h, 0, FIRE["steps"], params_fire, 2))
+            if events is not None:
+                events[2 * k + 1].record(stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step_resident()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = lib.gbca_kernel_launches()
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for k in range(args.steps):
+            step_resident(ev[k])
+        stop.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = lib.gbca_kernel_launches() - launches0
+    ms_total = start.elapsed_time(stop)
+    part_ms = [sum(e[0].elapsed_time(e[1]) for e in ev), sum(e[2].elapsed_time(e[3]) for e in ev)]
+    if dist is not None:
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_per_step = ms_total / args.steps
+    value = world * cell_updates() / (ms_per_step * 1e-3) / 1e9
+
+    # ---- roofline of the dominant kernel
+    per_pass = {"ltl": 4, "fire": 8}
+    parts = {}
+    for name, cfg, ms in (("ltl", LTL, part_ms[0]), ("fire", FIRE, part_ms[1])):
+        launches_part = -(-cfg["steps"] // per_pass[name])
+        cu = cfg["n1"] * cfg["n2"] * cfg["steps"]
+        avg_launch_s = ms / args.steps / launches_part * 1e-3
+        alg_bytes_launch = BYTES_PER_CELL_UPDATE * cfg["n1"] * cfg["n2"] * (cfg["steps"] / launches_part)
+        parts[name] = {"ms": ms / args.steps, "gcell_updates_s": cu / (ms / args.steps * 1e-3) / 1e9,
+                       "launches": launches_part, "avg_launch_us": avg_launch_s * 1e6,
+                       "alg_bytes_per_launch": alg_bytes_launch, "achieved_gbs": alg_bytes_launch / avg_launch_s / 1e9}
+    dom = max(parts, key=lambda k: parts[k]["ms"])
+    kernel = {"ltl": "k_life", "fire": "k_fire"}[dom]
+    peak, peak_src = measured_peaks()
+    achieved = parts[dom]["achieved_gbs"]
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_src, "kernel": kernel, "traffic": profiled_traffic(kernel)}
+    for name in parts:
+        parts[name]["hbm_frac_per_effective_step"] = parts[name]["achieved_gbs"] / peak
+
+    # ---- end to end through the C ABI with host buffers
+    host_in = [torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory() for a in (ltl0, fire0)]
+    host_out = [torch.empty_like(x).pin_memory() for x in host_in]
+    for h in handles:
+        capi.check(lib.gbca_set_stream(h, None))
+
+    def step_e2e():
+        for k, (h, hi, ho) in enumerate(zip(handles, host_in, host_out)):
+            nb = hi.numel()
+            capi.check(lib.gbca_set_state(h, ctypes.c_void_p(hi.data_ptr()), nb))
+            if k == 0:
+                capi.check(lib.gbca_advance(h, 0, LTL["steps"], None, 0))
+            else:
+                capi.check(lib.gbca_advance(h, 0, FIRE["steps"], params_fire, 2))
+            capi.check(lib.gbca_get_state(h, ctypes.c_void_p(ho.data_ptr()), nb))
+
+    step_e2e()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    nbytes = sum(x.numel() for x in host_in)
+    e2e = {"value": world * cell_updates() / (e2e_s / args.steps) / 1e9, "unit": "Gcell-updates/s",
+           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_sample(os.cpu_count() or 1)
+    for h in handles:
+        lib.gbca_destroy(h)
+    if rank == 0:
+        line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "int8", "data": "synthetic",
+                "config": {"workload": "single-instance sweeps: Larger-than-Life Moore(5) B34..45/S34..58 on an "
+                                       "8192^2 Int8 torus x 1000 steps + forest fire VonNeumann(1) on a 16384^2 Grid "
+                                       "Constant(0) x 500 steps (p=0.03, f=1e-4)",
+                           "cell_updates_per_step": cell_updates(), "parallelism": f"replicas x{world}",
+                           "l2": "inputs larger than L2: the 16384^2 state is 268 MB, and each step re-copies "
+                                 "335 MB of initial states"},
+                "roofline": roofline, "parts": parts, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clocks.summary(), "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -45,12 +45,15 @@ SIGNATURES = {
     "gbca_destroy": (ctypes.c_int, [_V]),
     "gbca_set_state": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
     "gbca_get_state": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
+    "gbca_set_state_device": (ctypes.c_int, [_V, _V, _I64]),
     "gbca_advance": (ctypes.c_int, [_V, _I64, _I64, _P(ctypes.c_double), ctypes.c_int32]),
     "gbca_read_cell": (ctypes.c_int, [_V, _I64, _I64, _V]),
     "gbca_write_cell": (ctypes.c_int, [_V, _I64, _I64, _V]),
     "gbca_sync": (ctypes.c_int, [_V]),
     "gbca_summaries": (ctypes.c_int, [_V, _P(_I64), ctypes.c_int32, _P(_I64), _P(ctypes.c_double)]),
     "gbca_device_state": (ctypes.c_int, [_V, _P(_V), _P(_I64)]),
+    "gbca_set_stream": (ctypes.c_int, [_V, _V]),
+    "gbca_kernel_launches": (ctypes.c_int64, []),
     "gbca_threshold": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_int32]),
 }
 

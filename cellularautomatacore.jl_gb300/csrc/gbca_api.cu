@@ -16,7 +16,8 @@ struct gbca_handle {
     int64_t pitch = 0;  // bytes between columns
     void* buf[2] = {nullptr, nullptr};
     int cur = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // the stream work is queued on
+    cudaStream_t own_stream = nullptr;  // the handle's own stream
     unsigned long long* acc = nullptr;       // device accumulator for summaries
     unsigned long long* acc_host = nullptr;  // pinned copy
     int nsm = 148;
@@ -162,7 +163,8 @@ int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
             p.nsub = (int32_t)k;
             e = gbca::launch_fire(p, src, dst, h->stream);
         } else if (life) {
-            k = nsteps < 4 ? nsteps : 4;
+            const int64_t per = gbca::life_steps_per_pass(p);
+            k = nsteps < per ? nsteps : per;
             p.nsub = (int32_t)k;
             e = gbca::launch_life_simd(p, src, dst, h->stream);
         } else {
@@ -176,6 +178,7 @@ int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
             e = gbca::launch_generic(p, src, dst, h->stream);
         }
         if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+        gbca::count_launch();
         h->cur ^= 1;
         t += k;
         nsteps -= k;
@@ -219,7 +222,8 @@ int gbca_create(const gbca_desc* desc, gbca_handle** out) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev);
     const size_t bytes = (size_t)h->pitch * (size_t)desc->n2;
-    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    h->stream = h->own_stream;
     if (e == cudaSuccess) e = cudaMalloc(&h->buf[0], bytes);
     if (e == cudaSuccess) e = cudaMalloc(&h->buf[1], bytes);
     if (e == cudaSuccess) e = cudaMalloc(&h->acc, gbca::kMeasureWords * sizeof(unsigned long long));
@@ -253,7 +257,7 @@ int gbca_destroy(gbca_handle* h) {
     cudaFree(h->buf[1]);
     cudaFree(h->acc);
     if (h->acc_host) cudaFreeHost(h->acc_host);
-    if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return GBCA_OK;
 }
@@ -267,6 +271,17 @@ int gbca_set_state(gbca_handle* h, const void* host, size_t nbytes) {
                                 cudaMemcpyHostToDevice, h->stream),
               "set_state copy");
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_state");
+    return GBCA_OK;
+}
+
+int gbca_set_state_device(gbca_handle* h, const void* dptr, int64_t src_pitch) {
+    if (!h || !dptr) return fail(GBCA_ERR_ARGUMENT, "null handle or state");
+    const size_t row = (size_t)h->d.n1 * h->esize;
+    if (src_pitch < (int64_t)row) return fail(GBCA_ERR_ARGUMENT, "source pitch %lld is below a column's %zu bytes",
+                                              (long long)src_pitch, row);
+    GBCA_CUDA(cudaMemcpy2DAsync(h->buf[h->cur], (size_t)h->pitch, dptr, (size_t)src_pitch, row, (size_t)h->d.n2,
+                                cudaMemcpyDeviceToDevice, h->stream),
+              "set_state_device copy");
     return GBCA_OK;
 }
 
@@ -336,6 +351,16 @@ int gbca_summaries(gbca_handle* h, int64_t* counts, int32_t nvals, int64_t* othe
     gbca::finish_measures(h->acc_host, h->d.n1 * h->d.n2, counts, nvals, other, morans);
     return GBCA_OK;
 }
+
+int gbca_set_stream(gbca_handle* h, void* stream) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    cudaStream_t next = stream ? (cudaStream_t)stream : h->own_stream;
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_stream");
+    h->stream = next;
+    return GBCA_OK;
+}
+
+int64_t gbca_kernel_launches(void) { return gbca::launches_so_far(); }
 
 int gbca_device_state(gbca_handle* h, void** dptr, int64_t* pitch) {
     if (!h || !dptr) return fail(GBCA_ERR_ARGUMENT, "null handle or output");

@@ -137,10 +137,15 @@ struct SweepParams {
     int32_t halo_x, halo_y;    // loaded halo (>= nsub * radius)
 };
 
+// Process-wide count of kernel launches (gbca_kernel_launches).
+void count_launch(int64_t n = 1);
+int64_t launches_so_far();
+
 // Launchers (one translation unit each).
 cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 bool life_simd_supported(const SweepParams& p);
 cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
+int life_steps_per_pass(const SweepParams& p);
 bool fire_fast_supported(const SweepParams& p);
 cudaError_t launch_fire(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 

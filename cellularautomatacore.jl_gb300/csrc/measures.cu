@@ -8,6 +8,8 @@
 // pairs of (x_i + x_j) and W the number of pairs. The kernel accumulates those integers
 // (order-independent, so every launch shape gives the same bits); the host finishes the
 // ratio in 128-bit integers and divides once.
+#include <atomic>
+
 #include "gbca_internal.cuh"
 #include "measures.cuh"
 
@@ -77,8 +79,16 @@ cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pit
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     k_measures<<<(unsigned)blocks, 256, 0, st>>>(u, n1, n2, pitch, b1, b2, acc);
+    count_launch();
     return cudaGetLastError();
 }
+
+namespace {
+std::atomic<int64_t> g_launches{0};
+}
+
+void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+int64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 void finish_measures(const unsigned long long* acc, int64_t n, int64_t* counts, int32_t nvals, int64_t* other,
                      double* morans) {

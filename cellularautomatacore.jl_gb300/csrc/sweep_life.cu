@@ -1,7 +1,407 @@
-// sweep_life.cu — placeholder until the box-sum Life-like kernel lands.
+// sweep_life.cu — Life-like and Larger-than-Life rules (src/rules.jl:354-389) on Moore(r),
+// r = 1..5, Synchronous, as a bit-sliced, temporally blocked sweep.
+//
+// Layout. Global memory keeps the user's Int8 column-major state. A CTA stages its tile
+// plus a halo of K*r cells in shared memory as ONE BIT PER CELL: bit b of word w of a
+// row is the indicator (state == 1) of the cell at x = 32w + b (src/rules.jl:377-383
+// counts exactly the neighbours equal to 1, and the next state depends on the centre
+// only through the same test, so the indicator is all the dynamics reads). Each row has
+// a zero guard word on each side.
+//
+// Counting. A thread owns a column of 32 cells (one word) and a run of rows. For each
+// row it forms the 2r+1 horizontally shifted copies of its word (funnel shifts with the
+// neighbour words) and adds them with a full-adder tree into a bit-sliced count Hx
+// (2-4 bit planes); a register ring keeps the last 2r+1 Hx rows and a bit-sliced running
+// sum V = sum of Hx over rows y-r..y+r is updated by one add and one subtract per row.
+// V is the Moore box count including the centre.
+//
+// Rule. A dead cell is born when V lies in one of the birth intervals, a live cell
+// survives when V - 1 lies in a survive interval, i.e. V in the interval shifted by one.
+// Counts of 64 and more never match (UInt64 masks, rules.jl:388). V >= L for a constant
+// L is a chain of majority gates, g = maj(v_i, g, m_i) with m_i = 0 where bit i of L is 1
+// and ~0 where it is 0 — one LOP3 per bit with m_i read from the parameter bank.
+//
+// Temporal blocking: K sub-steps per HBM pass; the computed region shrinks by r per
+// sub-step. Periodic and reflecting halos are images of lattice cells and evolve like
+// them; cells beyond a Constant edge are reset to the constant after every sub-step.
 #include "gbca_internal.cuh"
 
 namespace gbca {
-bool life_simd_supported(const SweepParams&) { return false; }
-cudaError_t launch_life_simd(const SweepParams&, const int8_t*, int8_t*, cudaStream_t) { return cudaErrorNotSupported; }
+
+namespace {
+
+constexpr int kMaxIntervals = 8;
+constexpr int kLifeThreads = 256;
+
+struct LifeTables {
+    int32_t n[2];                                // interval counts: [0] dead cells, [1] live cells
+    uint32_t m[2][kMaxIntervals][2][8];          // [kind][interval][lo, hi+1][bit] majority masks
+};
+
+struct LifeGeom {
+    int32_t tw, hw;   // core words, halo words (each side) per row
+    int32_t ty, hy;   // core rows, halo rows (each side)
+    int32_t sw, sy;   // smem row pitch in words (tw + 2hw + 2 guards), rows (ty + 2hy)
+    int32_t K;        // sub-steps
+};
+
+template <int R>
+struct LifeBits {
+    static constexpr int N = 2 * R + 1;
+    static constexpr int H = N < 4 ? 2 : (N < 8 ? 3 : 4);                        // planes of Hx
+    static constexpr int V = N * N < 16 ? 4 : (N * N < 32 ? 5 : (N * N < 64 ? 6 : 7));  // planes of V
+};
+
+__device__ __forceinline__ uint32_t maj3(uint32_t a, uint32_t b, uint32_t c) { return (a & b) | (a & c) | (b & c); }
+
+__device__ __forceinline__ void fa(uint32_t a, uint32_t b, uint32_t c, uint32_t& s, uint32_t& k) {
+    s = a ^ b ^ c;
+    k = maj3(a, b, c);
+}
+
+// Bit-sliced count of the 2r+1 words x[0..2r] (full-adder trees, hand-reduced).
+template <int R>
+__device__ __forceinline__ void hcount(const uint32_t* x, uint32_t* h) {
+    if constexpr (R == 1) {
+        fa(x[0], x[1], x[2], h[0], h[1]);
+    } else if constexpr (R == 2) {
+        uint32_t s1, k1, k2;
+        fa(x[0], x[1], x[2], s1, k1);
+        fa(x[3], x[4], s1, h[0], k2);
+        h[1] = k1 ^ k2;
+        h[2] = k1 & k2;
+    } else if constexpr (R == 3) {
+        uint32_t s1, k1, s2, k2, k3;
+        fa(x[0], x[1], x[2], s1, k1);
+        fa(x[3], x[4], x[5], s2, k2);
+        fa(x[6], s1, s2, h[0], k3);
+        fa(k1, k2, k3, h[1], h[2]);
+    } else if constexpr (R == 4) {
+        uint32_t s1, k1, s2, k2, s3, k3, k4, t, m1, m2;
+        fa(x[0], x[1], x[2], s1, k1);
+        fa(x[3], x[4], x[5], s2, k2);
+        fa(x[6], x[7], x[8], s3, k3);
+        fa(s1, s2, s3, h[0], k4);
+        fa(k1, k2, k3, t, m1);
+        h[1] = t ^ k4;
+        m2 = t & k4;
+        h[2] = m1 ^ m2;
+        h[3] = m1 & m2;
+    } else {
+        static_assert(R == 5, "r = 1..5");
+        uint32_t s1, k1, s2, k2, s3, k3, s4, k4, k5, t1, m1, m2;
+        fa(x[0], x[1], x[2], s1, k1);
+        fa(x[3], x[4], x[5], s2, k2);
+        fa(x[6], x[7], x[8], s3, k3);
+        fa(x[9], x[10], s1, s4, k4);
+        fa(s2, s3, s4, h[0], k5);
+        fa(k1, k2, k3, t1, m1);
+        fa(k4, k5, t1, h[1], m2);
+        h[2] = m1 ^ m2;
+        h[3] = m1 & m2;
+    }
+}
+
+// Hx of one row: p points at the thread's word (guards make p[-1] and p[1] valid).
+template <int R>
+__device__ __forceinline__ void hrow(const uint32_t* p, uint32_t* h) {
+    const uint32_t l = p[-1], c = p[0], r = p[1];
+    uint32_t x[2 * R + 1];
+#pragma unroll
+    for (int d = 1; d <= R; ++d) {
+        x[R - d] = __funnelshift_l(l, c, d);  // cell x - d
+        x[R + d] = __funnelshift_r(c, r, d);  // cell x + d
+    }
+    x[R] = c;
+    hcount<R>(x, h);
+}
+
+template <int BH, int BV>
+__device__ __forceinline__ void vadd(uint32_t* v, const uint32_t* h) {
+    uint32_t c = v[0] & h[0];
+    v[0] ^= h[0];
+#pragma unroll
+    for (int i = 1; i < BV; ++i) {
+        if (i < BH) {
+            const uint32_t s = v[i] ^ h[i] ^ c;
+            c = maj3(v[i], h[i], c);
+            v[i] = s;
+        } else {
+            const uint32_t s = v[i] ^ c;
+            c = v[i] & c;
+            v[i] = s;
+        }
+    }
+}
+
+template <int BH, int BV>
+__device__ __forceinline__ void vsub(uint32_t* v, const uint32_t* h) {
+    uint32_t b = ~v[0] & h[0];
+    v[0] ^= h[0];
+#pragma unroll
+    for (int i = 1; i < BV; ++i) {
+        if (i < BH) {
+            const uint32_t d = v[i] ^ h[i] ^ b;
+            b = maj3(~v[i], h[i], b);
+            v[i] = d;
+        } else {
+            const uint32_t d = v[i] ^ b;
+            b = ~v[i] & b;
+            v[i] = d;
+        }
+    }
+}
+
+template <int BV>
+__device__ __forceinline__ uint32_t ge(const uint32_t* v, const uint32_t* m) {
+    uint32_t g = 0xFFFFFFFFu;
+#pragma unroll
+    for (int i = 0; i < BV; ++i) g = maj3(v[i], g, m[i]);
+    return g;
+}
+
+template <int BV>
+__device__ __forceinline__ uint32_t life_rule(const uint32_t* v, uint32_t c, const LifeTables& tb) {
+    uint32_t out[2] = {0u, 0u};
+#pragma unroll
+    for (int kind = 0; kind < 2; ++kind) {
+#pragma unroll
+        for (int k = 0; k < kMaxIntervals; ++k) {
+            if (k < tb.n[kind]) out[kind] |= ge<BV>(v, tb.m[kind][k][0]) & ~ge<BV>(v, tb.m[kind][k][1]);
+        }
+    }
+    return (c & out[1]) | (~c & out[0]);
+}
+
+template <int R>
+__device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw, int w,
+                                            int r0, int r1, const LifeTables& tb) {
+    constexpr int N = LifeBits<R>::N, BH = LifeBits<R>::H, BV = LifeBits<R>::V;
+    const uint32_t* ca = A + 1 + w;
+    uint32_t* cb = B + 1 + w;
+    uint32_t ring[N][BH];
+    uint32_t v[BV];
+#pragma unroll
+    for (int i = 0; i < BV; ++i) v[i] = 0u;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        hrow<R>(ca + (r0 - R + k) * sw, ring[k]);
+        vadd<BH, BV>(v, ring[k]);
+    }
+    for (int y0 = r0; y0 < r1; y0 += N) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const int y = y0 + k;
+            if (y < r1) {
+                cb[y * sw] = life_rule<BV>(v, ca[y * sw], tb);
+                if (y + 1 < r1) {
+                    vsub<BH, BV>(v, ring[k]);
+                    hrow<R>(ca + (y + R + 1) * sw, ring[k]);
+                    vadd<BH, BV>(v, ring[k]);
+                }
+            }
+        }
+    }
+}
+
+// Indicator bits (byte == 1) of 4 bytes, in bits 0..3.
+__device__ __forceinline__ uint32_t ones4(uint32_t w) {
+    const uint32_t t = w ^ 0x01010101u;
+    const uint32_t nz = ((t & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | t;
+    const uint32_t z = (~nz & 0x80808080u) >> 7;
+    return (z * 0x10204080u) >> 28;
+}
+
+__device__ __forceinline__ uint32_t ones16(int4 q) {
+    return ones4((uint32_t)q.x) | (ones4((uint32_t)q.y) << 4) | (ones4((uint32_t)q.z) << 8) |
+           (ones4((uint32_t)q.w) << 12);
+}
+
+// Bits 0..3 of b as four bytes 0/1.
+__device__ __forceinline__ uint32_t bytes4(uint32_t b) { return ((b & 0xFu) * 0x00204081u) & 0x01010101u; }
+
+__device__ __forceinline__ int4 bytes16(uint32_t b) {
+    return make_int4((int)bytes4(b), (int)bytes4(b >> 4), (int)bytes4(b >> 8), (int)bytes4(b >> 12));
+}
+
+// 32 indicator bits of the cells gx .. gx+31 of lattice column-row `row` (already mapped in y).
+__device__ __forceinline__ uint32_t load_bits32(const SweepParams& p, const int8_t* __restrict__ row, int64_t gx) {
+    int64_t a = -1;
+    if (gx >= 0 && gx + 32 <= p.n1) a = gx;
+    else if (p.bnd[0] == GBCA_PERIODIC && (p.n1 & 31) == 0) a = map_axis(GBCA_PERIODIC, gx, p.n1);
+    if (a >= 0) {
+        const int4* q = (const int4*)(row + a);
+        return ones16(q[0]) | (ones16(q[1]) << 16);
+    }
+    uint32_t bits = 0;
+    for (int b = 0; b < 32; ++b) {
+        const int64_t mx = map_axis(p.bnd[0], gx + b, p.n1);
+        const int v = mx < 0 ? p.cval[0] : row[mx];
+        bits |= (uint32_t)(v == 1) << b;
+    }
+    return bits;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g, LifeTables tb,
+                                                       const int8_t* __restrict__ src, int8_t* __restrict__ dst) {
+    extern __shared__ __align__(16) uint32_t smw[];
+    uint32_t* A = smw;
+    uint32_t* B = smw + g.sw * g.sy;
+    const int W = g.tw + 2 * g.hw;
+    const int64_t X0 = (int64_t)blockIdx.x * (32 * g.tw) - 32 * g.hw;  // lattice x of local cell 0
+    const int64_t Y0 = (int64_t)blockIdx.y * g.ty - g.hy;              // lattice y of local row 0
+    const uint32_t cb0 = p.cval[0] == 1 ? 0xFFFFFFFFu : 0u, cb1 = p.cval[1] == 1 ? 0xFFFFFFFFu : 0u;
+
+    for (int q = threadIdx.x; q < W * g.sy; q += blockDim.x) {
+        const int lw = q % W, ly = q / W;
+        const int64_t my = map_axis(p.bnd[1], Y0 + ly, p.n2);
+        const uint32_t bits = my < 0 ? cb1 : load_bits32(p, src + my * p.pitch, X0 + 32 * lw);
+        A[ly * g.sw + 1 + lw] = bits;
+        B[ly * g.sw + 1 + lw] = bits;
+    }
+    for (int ly = threadIdx.x; ly < g.sy; ly += blockDim.x) {
+        A[ly * g.sw] = A[ly * g.sw + W + 1] = 0u;
+        B[ly * g.sw] = B[ly * g.sw + W + 1] = 0u;
+    }
+    // does the loaded region reach beyond a Constant edge?
+    const bool fix = (p.bnd[0] == GBCA_CONSTANT && (X0 < 0 || X0 + 32 * W > p.n1)) ||
+                     (p.bnd[1] == GBCA_CONSTANT && (Y0 < 0 || Y0 + g.sy > p.n2));
+    __syncthreads();
+
+    for (int s = 0; s < g.K; ++s) {
+        const int ex = (g.K - 1 - s) * R;
+        const int y_lo = g.hy - ex, y_hi = g.hy + g.ty + ex;
+        const int w_lo = (32 * g.hw - ex) >> 5, w_hi = (32 * (g.hw + g.tw) + ex + 31) >> 5;
+        const int nw = w_hi - w_lo;
+        const int nseg = blockDim.x / nw;
+        const int seg = threadIdx.x / nw;
+        if (seg < nseg) {
+            const int rows = y_hi - y_lo;
+            const int r0 = y_lo + (seg * rows) / nseg, r1 = y_lo + ((seg + 1) * rows) / nseg;
+            if (r1 > r0) life_column<R>(A, B, g.sw, w_lo + threadIdx.x % nw, r0, r1, tb);
+        }
+        __syncthreads();
+        if (fix) {
+            for (int q = threadIdx.x; q < nw * (y_hi - y_lo); q += blockDim.x) {
+                const int lw = w_lo + q % nw, ly = y_lo + q / nw;
+                const int64_t gy = Y0 + ly, gx = X0 + 32 * lw;
+                uint32_t* wp = B + ly * g.sw + 1 + lw;
+                if (p.bnd[1] == GBCA_CONSTANT && (gy < 0 || gy >= p.n2)) {
+                    *wp = cb1;
+                } else if (p.bnd[0] == GBCA_CONSTANT && (gx < 0 || gx + 32 > p.n1)) {
+                    uint32_t out = 0;
+                    for (int b = 0; b < 32; ++b) out |= (uint32_t)(gx + b < 0 || gx + b >= p.n1) << b;
+                    *wp = (*wp & ~out) | (cb0 & out);
+                }
+            }
+            __syncthreads();
+        }
+        uint32_t* t = A; A = B; B = t;
+    }
+
+    for (int q = threadIdx.x; q < g.tw * g.ty; q += blockDim.x) {
+        const int lw = g.hw + q % g.tw, ly = g.hy + q / g.tw;
+        const int64_t gy = Y0 + ly, gx = X0 + 32 * lw;
+        if (gy >= p.n2 || gx >= p.n1) continue;
+        const uint32_t bits = A[ly * g.sw + 1 + lw];
+        int8_t* out = dst + gy * p.pitch + gx;
+        if (gx + 32 <= p.n1) {
+            ((int4*)out)[0] = bytes16(bits);
+            ((int4*)out)[1] = bytes16(bits >> 16);
+        } else {
+            for (int b = 0; gx + b < p.n1; ++b) out[b] = (int8_t)((bits >> b) & 1u);
+        }
+    }
+}
+
+// Intervals of consecutive set bits of a count mask, as intervals of V = count + shift,
+// clipped to V <= vmax. Returns false when there are more than kMaxIntervals.
+bool intervals(uint64_t mask, int shift, int vmax, int* lo, int* hi, int* n) {
+    *n = 0;
+    for (int c = 0; c < 64;) {
+        if (!((mask >> c) & 1u)) { ++c; continue; }
+        int e = c;
+        while (e + 1 < 64 && ((mask >> (e + 1)) & 1u)) ++e;
+        int a = c + shift, b = e + shift;
+        if (b > vmax) b = vmax;
+        if (a <= b) {
+            if (*n == kMaxIntervals) return false;
+            lo[*n] = a;
+            hi[*n] = b;
+            ++*n;
+        }
+        c = e + 1;
+    }
+    return true;
+}
+
+bool make_tables(const SweepParams& p, LifeTables* tb) {
+    const int N = 2 * p.radius + 1, vmax = N * N;
+    int lo[kMaxIntervals], hi[kMaxIntervals], n;
+    for (int kind = 0; kind < 2; ++kind) {
+        // dead cells: V = count (centre 0), V <= N^2 - 1; live cells: V = count + 1
+        if (!intervals(kind == 0 ? p.birth : p.survive, kind, kind == 0 ? vmax - 1 : vmax, lo, hi, &n)) return false;
+        tb->n[kind] = n;
+        for (int k = 0; k < kMaxIntervals; ++k)
+            for (int j = 0; j < 2; ++j) {
+                const int L = k < n ? (j == 0 ? lo[k] : hi[k] + 1) : 0;
+                for (int i = 0; i < 8; ++i) tb->m[kind][k][j][i] = ((L >> i) & 1) ? 0u : 0xFFFFFFFFu;
+            }
+    }
+    return true;
+}
+
+template <int R>
+cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
+                     cudaStream_t st) {
+    const size_t smem = 2 * (size_t)g.sw * (size_t)g.sy * 4;
+    cudaError_t e = cudaFuncSetAttribute(k_life<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((p.n1 + 32 * g.tw - 1) / (32 * g.tw)), (unsigned)((p.n2 + g.ty - 1) / g.ty));
+    k_life<R><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool life_simd_supported(const SweepParams& p) {
+    if (p.rule != GBCA_RULE_LIFE || p.nbhd != GBCA_MOORE || p.radius < 1 || p.radius > 5 ||
+        p.scheme != GBCA_SYNCHRONOUS || p.pitch % 16 != 0)
+        return false;
+    LifeTables tb;
+    return make_tables(p, &tb);
+}
+
+int life_steps_per_pass(const SweepParams& p) {
+    switch (p.radius) {
+        case 1: return 16;
+        case 2: return 8;
+        case 3: return 6;
+        case 4: return 5;
+        default: return 4;
+    }
+}
+
+cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st) {
+    LifeTables tb;
+    if (!make_tables(p, &tb)) return cudaErrorNotSupported;
+    LifeGeom g;
+    g.K = p.nsub;
+    g.hy = g.K * p.radius;
+    g.hw = (g.hy + 31) / 32;
+    const int64_t words = (p.n1 + 31) / 32;
+    g.tw = words < 32 ? (int)words : 32;
+    g.ty = p.n2 < 216 ? (int)p.n2 : 216;
+    g.sw = g.tw + 2 * g.hw + 2;
+    g.sy = g.ty + 2 * g.hy;
+    switch (p.radius) {
+        case 1: return launch_r<1>(p, g, tb, src, dst, st);
+        case 2: return launch_r<2>(p, g, tb, src, dst, st);
+        case 3: return launch_r<3>(p, g, tb, src, dst, st);
+        case 4: return launch_r<4>(p, g, tb, src, dst, st);
+        default: return launch_r<5>(p, g, tb, src, dst, st);
+    }
+}
+
 }  // namespace gbca

@@ -95,6 +95,11 @@ int gbca_destroy(gbca_handle* h);
  * whole host state (n1*n2 elements, column-major) to the device. */
 int gbca_set_state(gbca_handle* h, const void* host, size_t nbytes);
 
+/* set_state! from a state already in device memory (a CuArray, say): `dptr` holds n2
+ * columns of n1 elements, `src_pitch` bytes apart (n1 * element size when packed). The
+ * copy is queued on the handle's stream. */
+int gbca_set_state_device(gbca_handle* h, const void* dptr, int64_t src_pitch);
+
 /* Replaces current_state(b, st) (src/backends.jl:132-139; KA ext :126-130): waits for
  * pending work and copies the whole state to host memory. */
 int gbca_get_state(gbca_handle* h, void* host, size_t nbytes);
@@ -124,6 +129,16 @@ int gbca_summaries(gbca_handle* h, int64_t* counts, int32_t nvals, int64_t* othe
 /* Device pointer of the current state buffer (pitch in bytes between columns in *pitch),
  * valid until the next gbca_advance / gbca_destroy. For callers that keep inputs in HBM. */
 int gbca_device_state(gbca_handle* h, void** dptr, int64_t* pitch);
+
+/* Run the handle's work on `stream` (a cudaStream_t; NULL restores the handle's own
+ * stream) from the next call on, after waiting for what was queued before. Lets a caller
+ * order the sweep with its own work and time it with events on the same stream.
+ * No counterpart in the reference (its GPUBackend synchronizes after every step). */
+int gbca_set_stream(gbca_handle* h, void* stream);
+
+/* Number of kernels this library has launched in the process so far (all handles).
+ * A diagnostic with no counterpart in the reference. */
+int64_t gbca_kernel_launches(void);
 
 /* Host helper: the integer threshold T with  uniform < p  <=>  x < T, where x is the
  * 53-bit (f32 = 0: random.jl:116-120) or 24-bit (f32 = 1: random.jl:109-114) integer

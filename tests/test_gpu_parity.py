@@ -155,6 +155,7 @@ def test_integrator_modification_and_reinit(ca, oracle):
     integ.p = {"p": 0.0, "f": 0.0}
     ca.step(integ, 3)
     assert np.array_equal(integ.u, oracle.run_array(P, ref, 5, 3, (0.0, 0.0)))
+    integ.p = prob.p  # reinit! keeps the integrator's p (src/problem.jl:508-531)
     ca.reinit(integ)
     ca.step(integ, 6)
     assert np.array_equal(integ.u, oracle.run_array(P, u0, 0, 6, (0.2, 0.01)))
