@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", choices=["ltl", "fire", "lenia", "lenia-fft"], default=None,
+                    help="time single passes of one kernel on an n x n lattice (for profiling)")
+    ap.add_argument("--n", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -205,8 +208,70 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_case(args):
+    """`steps` timed passes (one kernel launch each for the sweeps, one step for Lenia) of
+    one workload on an n x n lattice after `warmup` untimed ones."""
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    ca = ge.load_package()
+    capi, lib = ca.capi, ca.capi.lib()
+    n = args.n
+    d1, d2 = descs(capi)
+    rng = np.random.Generator(np.random.PCG64(2))
+    if args.case == "ltl":
+        d, per, params, dtype = d1, 4, None, np.int8
+        u0 = (rng.random((n, n)) < 0.5).astype(np.int8)
+    elif args.case == "fire":
+        d, per, dtype = d2, 8, np.int8
+        params = (ctypes.c_double * 2)(FIRE["p"], FIRE["f"])
+        pct = rng.integers(0, 100, size=(n, n), dtype=np.int8)
+        u0 = (pct >= 40).astype(np.int8) + (pct >= 99).astype(np.int8)
+    else:
+        d = capi.Desc()
+        d.rule, d.lenia_R, d.lenia_npeaks, d.lenia_peaks[0] = capi.RULE_LENIA, 13, 1, 1.0
+        d.lenia_mu, d.lenia_sigma, d.lenia_dt = 0.15, 0.015, 0.1
+        d.lenia_method = capi.FFT if args.case == "lenia-fft" else capi.DIRECT
+        per, params, dtype = 1, None, np.float32
+        u0 = np.zeros((n, n), np.float32)
+        c = n // 2
+        u0[c - 128:c + 128, c - 128:c + 128] = rng.random((256, 256))
+    d.n1 = d.n2 = n
+    h = ctypes.c_void_p()
+    capi.check(lib.gbca_create(ctypes.byref(d), ctypes.byref(h)))
+    a = np.asfortranarray(u0.astype(dtype))
+    capi.check(lib.gbca_set_state(h, a.ctypes.data, a.nbytes))
+    stream = torch.cuda.Stream()
+    capi.check(lib.gbca_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+    nparams = 2 if params is not None else 0
+    t = 0
+    for _ in range(args.warmup):
+        capi.check(lib.gbca_advance(h, t, per, params, nparams))
+        t += per
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        capi.check(lib.gbca_advance(h, t, per, params, nparams))
+        t += per
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    cu = n * n * per
+    out = {"case": args.case, "n": n, "steps_per_pass": per, "ms_per_pass": ms,
+           "gcell_updates_s": cu / (ms * 1e-3) / 1e9}
+    if args.case in ("ltl", "fire"):
+        out["hbm_frac_per_effective_step"] = BYTES_PER_CELL_UPDATE * cu / (ms * 1e-3) / 1e9 / measured_peaks()[0]
+    else:
+        out["gflops_direct_equiv"] = n * n * 516 * 2 / (ms * 1e-3) / 1e9
+    print(json.dumps(out))
+    lib.gbca_destroy(h)
+
+
 def main():
     args = parse()
+    if args.case:
+        return run_case(args)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

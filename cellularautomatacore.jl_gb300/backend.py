@@ -85,8 +85,10 @@ def make_desc(prob, scheme) -> capi.Desc:
         for k, v in enumerate(rule.peaks):
             d.lenia_peaks[k] = v
         d.lenia_mu, d.lenia_sigma, d.lenia_dt = rule.mu, rule.sigma, rule.dt
-        if np.asarray(prob.u0).dtype != np.float32:
-            raise ArgumentError("GB300Backend runs Lenia on a Float32 state")
+        d.lenia_f64 = int(rule.precision == "Float64")
+        want = np.float64 if d.lenia_f64 else np.float32
+        if np.asarray(prob.u0).dtype != want:
+            raise ArgumentError(f"Lenia(precision={rule.precision}) needs a {rule.precision} state")
         return d
     nb = prob.neighbours
     if not isinstance(nb, (Moore, VonNeumann)):
@@ -145,7 +147,8 @@ class GB300State:
 
 def allocate_state(backend, prob, scheme) -> GB300State:
     d = make_desc(prob, scheme)
-    st = GB300State(d, np.float32 if d.rule == capi.RULE_LENIA else np.int8)
+    dtype = (np.float64 if d.lenia_f64 else np.float32) if d.rule == capi.RULE_LENIA else np.int8
+    st = GB300State(d, dtype)
     set_state(backend, st, prob.u0)
     return st
 

@@ -27,7 +27,8 @@ class Desc(ctypes.Structure):
         ("boundary", ctypes.c_int32 * 2), ("constant", ctypes.c_double * 2), ("seed", ctypes.c_uint64),
         ("scheme", ctypes.c_int32), ("scheme_p_f32", ctypes.c_int32), ("scheme_p", ctypes.c_double),
         ("params_f32", ctypes.c_int32), ("lenia_method", ctypes.c_int32), ("lenia_R", ctypes.c_int32),
-        ("lenia_npeaks", ctypes.c_int32), ("lenia_peaks", ctypes.c_double * MAX_PEAKS),
+        ("lenia_npeaks", ctypes.c_int32), ("lenia_f64", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("lenia_peaks", ctypes.c_double * MAX_PEAKS),
         ("lenia_mu", ctypes.c_double), ("lenia_sigma", ctypes.c_double), ("lenia_dt", ctypes.c_double),
     ]
 

@@ -215,7 +215,7 @@ int gbca_create(const gbca_desc* desc, gbca_handle** out) {
     if (gbca_device_count() < 1) return fail(GBCA_ERR_CUDA, "no CUDA device is visible");
     gbca_handle* h = new gbca_handle();
     h->d = *desc;
-    h->esize = desc->rule == GBCA_RULE_LENIA ? 4 : 1;
+    h->esize = desc->rule == GBCA_RULE_LENIA ? (desc->lenia_f64 ? 8 : 4) : 1;
     const int64_t row = desc->n1 * (int64_t)h->esize;
     h->pitch = (row + 127) / 128 * 128;
     int dev = 0;
@@ -302,9 +302,7 @@ int gbca_advance(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
     if (nsteps < 0) return fail(GBCA_ERR_ARGUMENT, "nsteps must be non-negative, got %lld", (long long)nsteps);
     if (nsteps == 0) return GBCA_OK;
     if (h->d.rule == GBCA_RULE_LENIA) {
-        const int rc = gbca::lenia_advance(h->lenia, (const float*)h->buf[h->cur], (float*)h->buf[h->cur ^ 1], nsteps,
-                                           h->stream, &h->cur, h->buf, g_err);
-        return rc;
+        return gbca::lenia_advance(h->lenia, nsteps, h->stream, &h->cur, h->buf, g_err);
     }
     return advance_int8(h, t, nsteps, params, nparams);
 }

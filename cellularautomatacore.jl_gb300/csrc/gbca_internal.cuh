@@ -102,6 +102,7 @@ __device__ __forceinline__ uint2 draw_fast(const DrawStep& s, uint32_t id, uint3
 // 0-based version of _map_axis (src/spaces.jl:46-51): the mapped index, or -1 when the
 // index lies beyond a Constant edge.
 __host__ __device__ __forceinline__ int64_t map_axis(int32_t b, int64_t g, int64_t n) {
+    if ((uint64_t)g < (uint64_t)n) return g;  // inside: every boundary maps to itself
     if (b == GBCA_PERIODIC) {
         int64_t m = g % n;
         return m < 0 ? m + n : m;

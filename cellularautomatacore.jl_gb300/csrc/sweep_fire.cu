@@ -18,12 +18,15 @@ namespace {
 constexpr int kFireTX = 256, kFireTY = 128;
 constexpr int kFireThreadsX = 32, kFireThreadsY = 16;
 
+// One draw site for both draw indices, so that lanes of a warp holding empty cells
+// (draw 1) and trees (draw 2) share one Philox evaluation instead of running two.
 __device__ __forceinline__ int8_t fire_cell(int8_t c, const int8_t* a, int sx, const DrawStep& ds, uint32_t id,
                                             uint64_t thr_p, uint64_t thr_f, bool f32) {
     if (c == 2) return 0;
-    if (c == 0) return draw_below(draw_fast(ds, id, 1u), thr_p, f32) ? 1 : 0;
-    if (a[-1] == 2 || a[1] == 2 || a[-sx] == 2 || a[sx] == 2) return 2;
-    return draw_below(draw_fast(ds, id, 2u), thr_f, f32) ? 2 : 1;
+    const bool empty = c == 0;
+    if (!empty && (a[-1] == 2 || a[1] == 2 || a[-sx] == 2 || a[sx] == 2)) return 2;
+    const bool hit = draw_below(draw_fast(ds, id, empty ? 1u : 2u), empty ? thr_p : thr_f, f32);
+    return empty ? (hit ? 1 : 0) : (hit ? 2 : 1);
 }
 
 template <bool INTERIOR>

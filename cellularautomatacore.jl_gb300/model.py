@@ -254,24 +254,26 @@ class ForestFire:
 
 
 class Lenia:
-    """Lenia (src/lenia.jl:17-47) in Float32: potential U from the LeniaKernel(R; peaks)
-    field, then clamp(c + dt (2 exp(-(U - mu)^2 / 2 sigma^2) - 1), 0, 1)."""
+    """Lenia (src/lenia.jl:17-47): potential U from the LeniaKernel(R; peaks) field, then
+    clamp(c + dt (2 exp(-(U - mu)^2 / 2 sigma^2) - 1), 0, 1), in the precision of the
+    state (precision="Float32" or "Float64", as the reference's `precision` keyword)."""
 
-    def __init__(self, R=13, mu=0.15, sigma=0.015, dt=0.1, peaks=(1.0,), method="direct", precision="Float32"):
+    def __init__(self, R=13, mu=0.15, sigma=0.015, dt=0.1, peaks=(1.0,), method="direct", precision="Float64"):
         if not sigma > 0:
             raise ArgumentError(f"σ must be positive, got {sigma}")
         if not 0 < dt <= 1:
             raise ArgumentError(f"dt must be in (0, 1], got {dt}")
         if method not in ("direct", "fft"):
             raise ArgumentError(f"method must be :direct or :fft, got :{method}")
-        if precision != "Float32":
-            raise ArgumentError("GB300Backend runs Lenia with precision=Float32")
+        if precision not in ("Float32", "Float64"):
+            raise ArgumentError(f"precision must be Float32 or Float64, got {precision}")
         if R < 1:
             raise ArgumentError(f"R must be at least 1, got {R}")
         if len(peaks) < 1:
             raise ArgumentError("at least one peak is needed")
         self.R, self.mu, self.sigma, self.dt = int(R), float(mu), float(sigma), float(dt)
         self.peaks, self.method, self.neighbourhood = tuple(float(x) for x in peaks), method, None
+        self.precision = precision
 
     def validate_state(self, u0):
         if not np.issubdtype(np.asarray(u0).dtype, np.floating):

@@ -10,7 +10,8 @@
  * the message of the calling thread's last failure.
  *
  * States are single-layer, column-major (axis 1 contiguous), exactly the layout of the
- * reference's `u0` arrays: Int8 for Life / Generations / forest fire, Float32 for Lenia.
+ * reference's `u0` arrays: Int8 for Life / Generations / forest fire, Float32 or Float64
+ * for Lenia.
  * Indices are 1-based, as in Julia. A handle owns its device buffers and one CUDA stream;
  * a handle is not thread-safe, distinct handles are.
  */
@@ -63,6 +64,8 @@ typedef struct gbca_desc {
     int32_t lenia_method;    /* GBCA_DIRECT / GBCA_FFT (src/lenia.jl:24-32)          */
     int32_t lenia_R;
     int32_t lenia_npeaks;
+    int32_t lenia_f64;       /* Lenia(; precision=Float64): a Float64 state (src/lenia.jl:24-31) */
+    int32_t reserved;
     double lenia_peaks[GBCA_MAX_PEAKS];
     double lenia_mu, lenia_sigma, lenia_dt;
 } gbca_desc;
@@ -111,7 +114,7 @@ int gbca_get_state(gbca_handle* h, void* host, size_t nbytes);
 int gbca_advance(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams);
 
 /* Replaces read_cell(b, st, I) (src/backends.jl:380; KA ext :142): one element at the
- * 1-based index (i, j), written to `out` (1 byte for Int8, 4 for Float32). */
+ * 1-based index (i, j), written to `out` (1 byte for Int8, 4 for Float32, 8 for Float64). */
 int gbca_read_cell(gbca_handle* h, int64_t i, int64_t j, void* out);
 
 /* Replaces write_cell!(b, st, I, v) (src/backends.jl:381-383; KA ext :143-148). */

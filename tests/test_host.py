@@ -154,6 +154,8 @@ def test_problem_validation(ca):
     assert ca.supports(B, ca.Synchronous()) and ca.supports(B, ca.Stochastic(0.5)) and ca.supports(B, ca.Checkerboard())
     with pytest.raises(ca.ArgumentError):
         ca.check_problem(B, ca.CAProblem.new(ca.Life(), np.zeros((8, 8), np.int32), 1), ca.Synchronous())
+    with pytest.raises(ca.ArgumentError):  # a Float32 rule on a Float64 state
+        ca.check_problem(B, ca.CAProblem.new(ca.Lenia(precision="Float32"), np.zeros((8, 8)), 1), ca.Synchronous())
     with pytest.raises(ca.ArgumentError):
-        ca.check_problem(B, ca.CAProblem.new(ca.Lenia(method="fft"), np.zeros((8, 8), np.float32), 1,
+        ca.check_problem(B, ca.CAProblem.new(ca.Lenia(method="fft", precision="Float32"), np.zeros((8, 8), np.float32), 1,
                                              space=ca.Grid(8, 8)), ca.Synchronous())
