@@ -17,6 +17,7 @@ PERIODIC, REFLECTING, CONSTANT = 0, 1, 2
 SYNCHRONOUS, STOCHASTIC, CHECKERBOARD = 0, 1, 2
 DIRECT, FFT = 0, 1
 MAX_PEAKS = 8
+NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 
 
 class Desc(ctypes.Structure):
@@ -56,6 +57,7 @@ SIGNATURES = {
     "gbca_set_stream": (ctypes.c_int, [_V, _V]),
     "gbca_kernel_launches": (ctypes.c_int64, []),
     "gbca_threshold": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_int32]),
+    "gbca_advance_noalloc": (ctypes.c_int, [_P(Desc), _V, _I64, _I64, _I64, _P(ctypes.c_double), ctypes.c_int32, _V]),
 }
 
 _lib = None

@@ -188,6 +188,11 @@ int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
 
 }  // namespace
 
+namespace gbca {
+// Lets other translation units of the library report through gbca_last_error().
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace gbca
+
 extern "C" {
 
 const char* gbca_last_error(void) { return g_err.c_str(); }

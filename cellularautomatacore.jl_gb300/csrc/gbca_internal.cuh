@@ -138,6 +138,9 @@ struct SweepParams {
     int32_t halo_x, halo_y;    // loaded halo (>= nsub * radius)
 };
 
+// The message gbca_last_error() returns on this thread.
+void set_last_error(const char* msg);
+
 // Process-wide count of kernel launches (gbca_kernel_launches).
 void count_launch(int64_t n = 1);
 int64_t launches_so_far();

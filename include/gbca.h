@@ -143,6 +143,30 @@ int gbca_set_stream(gbca_handle* h, void* stream);
  * A diagnostic with no counterpart in the reference. */
 int64_t gbca_kernel_launches(void);
 
+/* Size of the device scratch array behind gbca_advance_noalloc: the largest state, in bytes
+ * (pitch * n2), that it accepts. Every GPU that loads the library holds this array until
+ * the process exits. */
+#define GBCA_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
+
+/* gbca_advance for callers that cannot allocate device memory when they need a sweep: code
+ * running while a memory pool owns the device (a CuArray pool, a caching allocator sized to
+ * the card), a real-time loop that must not take the allocator's locks, or a plug-in whose
+ * host forbids allocation after start-up. No counterpart in the reference.
+ *
+ * Advances the Int8 state at `state` (n2 columns of desc->n1 bytes, `pitch` bytes apart,
+ * 16-byte aligned, pitch a multiple of 16 for the fast kernels) by `nsteps` steps from time
+ * t, in place, on `stream` (a cudaStream_t; NULL is the legacy default stream). It allocates
+ * nothing and creates no stream: the buffer the sweep alternates with is a file-scope device
+ * array of GBCA_NOALLOC_SCRATCH_BYTES; larger states are refused with GBCA_ERR_ARGUMENT, and
+ * Lenia (whose FFT plans allocate) with GBCA_ERR_UNSUPPORTED. Results are those of
+ * gbca_advance, bit for bit. The work is queued; the call returns before it finishes.
+ *
+ * The first call on a device looks up the scratch array's address there (make it before
+ * any stream capture on that device). All calls share the array and it keeps the last
+ * call's contents: calls that overlap on the GPU race on it, so serialise them. */
+int gbca_advance_noalloc(const gbca_desc* desc, void* state, int64_t pitch, int64_t t, int64_t nsteps,
+                         const double* params, int32_t nparams, void* stream);
+
 /* Host helper: the integer threshold T with  uniform < p  <=>  x < T, where x is the
  * 53-bit (f32 = 0: random.jl:116-120) or 24-bit (f32 = 1: random.jl:109-114) integer
  * behind the draw. NaN and p <= 0 give 0; p >= 1 gives 2^53 (2^24). */
