@@ -57,6 +57,14 @@ SIGNATURES = {
     "gbca_set_stream": (ctypes.c_int, [_V, _V]),
     "gbca_kernel_launches": (ctypes.c_int64, []),
     "gbca_threshold": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_int32]),
+    "gbca_ensemble_create": (ctypes.c_int, [_P(Desc), ctypes.c_int32, _P(_V)]),
+    "gbca_ensemble_destroy": (ctypes.c_int, [_V]),
+    "gbca_ensemble_set_state": (ctypes.c_int, [_V, ctypes.c_int32, _V, ctypes.c_size_t]),
+    "gbca_ensemble_fill": (ctypes.c_int, [_V, ctypes.c_int32]),
+    "gbca_ensemble_run": (ctypes.c_int, [_V, _P(_I64), _P(_I64), _P(ctypes.c_double), ctypes.c_int32]),
+    "gbca_ensemble_sync": (ctypes.c_int, [_V]),
+    "gbca_ensemble_summaries": (ctypes.c_int, [_V, _P(_I64), ctypes.c_int32, _P(_I64), _P(ctypes.c_double)]),
+    "gbca_ensemble_get_state": (ctypes.c_int, [_V, ctypes.c_int32, _V, ctypes.c_size_t]),
     "gbca_advance_noalloc": (ctypes.c_int, [_P(Desc), _V, _I64, _I64, _I64, _P(ctypes.c_double), ctypes.c_int32, _V]),
 }
 

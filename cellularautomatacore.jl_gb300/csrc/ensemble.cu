@@ -1,0 +1,510 @@
+// ensemble.cu — batched ensembles: many Int8 problems of different sizes, rules and
+// parameters advanced together by ONE persistent kernel launch, captured in a CUDA graph.
+//
+// This replaces solving an EnsembleProblem trajectory by trajectory (src/problem.jl:571-589,
+// SciMLBase's EnsembleSerial / EnsembleThreads; src/calibration.jl:66-91 for ABC), where
+// every trajectory allocates, uploads and launches per step on its own.
+//
+// Scheduling: the host sorts the instances by work (cells x steps), largest first; each CTA
+// of a grid sized to fill the GPU pulls the next instance from an atomic counter and runs
+// it to the end alone, so no CTA ever waits for another (no inter-CTA barrier, no spin).
+// Largest-first keeps the tail short.
+//
+// Per instance, in one CTA:
+//  * small lattices, (n1 + 2r)(n2 + 2r) <= kEnsBuf bytes, live entirely in shared memory: a
+//    halo of r cells is refreshed from the boundary map before every step (the halo fill of
+//    src/backends.jl:425-442) and all steps run without touching global memory;
+//  * larger ones are swept tile by tile with temporal blocking (K steps per pass, halo K r),
+//    ping-ponging between the instance's two buffers in global memory (mostly L2-resident).
+// At the end the CTA reduces the final state to the exact integers behind state_counts and
+// Moran's I (src/measures.jl:14-20,91-107) — the same sums, hence the same bits, as
+// gbca_summaries on a single handle.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "ensemble.cuh"
+#include "gbca_internal.cuh"
+#include "measures.cuh"
+
+namespace gbca {
+
+namespace {
+
+constexpr int kEnsThreads = 256;
+constexpr int kEnsTile = 128;
+constexpr int kEnsMaxHalo = 8;
+constexpr int kEnsSide = kEnsTile + 2 * kEnsMaxHalo;  // 144
+constexpr int kEnsBuf = kEnsSide * kEnsSide;          // bytes per shared buffer
+
+__device__ __forceinline__ bool fast_fire(const EnsInstance& I) {
+    return I.rule == GBCA_RULE_FOREST_FIRE && I.nbhd == GBCA_VON_NEUMANN && I.radius == 1;
+}
+
+// The next state of the cell at offset o of a shared buffer with row pitch sx: the rule of
+// src/rules.jl:385-389 / :446-456 or the forest fire, neighbours read from the buffer.
+__device__ __forceinline__ int8_t ens_update(const EnsInstance& I, const int8_t* A, int sx, int o, uint64_t id,
+                                             int64_t t, const DrawStep& ds, const PhiloxKeys& K, bool ff) {
+    const int8_t c = A[o];
+    if (ff) {
+        if (c == 2) return 0;
+        const bool empty = c == 0;
+        if (!empty && (A[o - 1] == 2 || A[o + 1] == 2 || A[o - sx] == 2 || A[o + sx] == 2)) return 2;
+        const bool hit = draw_below(draw_fast(ds, K, (uint32_t)id, empty ? 1u : 2u), empty ? I.thr_p : I.thr_f,
+                                    I.params_f32 != 0);
+        return empty ? (hit ? 1 : 0) : (hit ? 2 : 1);
+    }
+    const int r = I.radius;
+    int n = 0;
+    bool fire = false;
+    for (int dj = -r; dj <= r; ++dj) {
+        const int rr = I.nbhd == GBCA_MOORE ? r : r - (dj < 0 ? -dj : dj);
+        const int8_t* row = A + o + dj * sx;
+        for (int di = -rr; di <= rr; ++di) {
+            if (di == 0 && dj == 0) continue;
+            const int8_t v = row[di];
+            n += v == 1;
+            fire |= v == 2;
+        }
+    }
+    if (I.rule == GBCA_RULE_LIFE) {
+        const uint64_t mask = c == 1 ? I.survive : I.birth;
+        return (int8_t)(n < 64 ? (mask >> n) & 1u : 0u);
+    }
+    if (I.rule == GBCA_RULE_GENERATIONS) {
+        const int s = c;
+        if (s == 0) return (int8_t)(n < 64 ? (I.birth >> n) & 1u : 0u);
+        if (s == 1) {
+            if (n < 64 && ((I.survive >> n) & 1u)) return c;
+            return (int8_t)(I.states > 2 ? 2 : 0);
+        }
+        return (int8_t)(s + 1 < I.states ? s + 1 : 0);
+    }
+    if (c == 2) return 0;
+    if (c == 0) return draw_below(cell_draw(I.seed, id, t, 1), I.thr_p, I.params_f32 != 0) ? 1 : 0;
+    if (fire) return 2;
+    return draw_below(cell_draw(I.seed, id, t, 2), I.thr_f, I.params_f32 != 0) ? 2 : 1;
+}
+
+__device__ __forceinline__ int8_t boundary_value(const EnsInstance& I, const int8_t* base, int64_t pitch, int64_t gx,
+                                                 int64_t gy) {
+    const int64_t mx = map_axis(I.bnd0, gx, I.n1), my = map_axis(I.bnd1, gy, I.n2);
+    if (my < 0) return (int8_t)I.cval1;
+    if (mx < 0) return (int8_t)I.cval0;
+    return base[mx + my * pitch];
+}
+
+// The whole lattice in shared memory, padded by r on every side.
+__device__ void run_in_smem(const EnsInstance& I, int8_t* pool, int8_t* A, int8_t* B, const PhiloxKeys& K) {
+    const int r = I.radius, n1 = (int)I.n1, n2 = (int)I.n2, P1 = n1 + 2 * r;
+    int8_t* g = pool + I.off[I.cur];
+    for (int q = threadIdx.x; q < n1 * n2; q += blockDim.x) {
+        const int x = q % n1, y = q / n1;
+        A[(y + r) * P1 + x + r] = g[x + (int64_t)y * I.pitch];
+    }
+    const bool ff = fast_fire(I);
+    const int ring = 2 * r * P1 + 2 * r * n2;  // halo cells
+    for (int64_t s = 0; s < I.nsteps; ++s) {
+        __syncthreads();
+        for (int q = threadIdx.x; q < ring; q += blockDim.x) {  // refresh the halo from the interior
+            int hx, hy;
+            if (q < 2 * r * P1) {
+                const int row = q / P1;
+                hx = q % P1;
+                hy = row < r ? row : n2 + row;  // rows 0..r-1 and n2+r..n2+2r-1
+            } else {
+                const int q2 = q - 2 * r * P1, col = q2 % (2 * r);
+                hy = r + q2 / (2 * r);
+                hx = col < r ? col : n1 + col;
+            }
+            A[hy * P1 + hx] = boundary_value(I, A + r * P1 + r, P1, hx - r, hy - r);
+        }
+        __syncthreads();
+        const int64_t t = I.t0 + s;
+        const DrawStep ds = draw_step(K, t);
+        for (int q = threadIdx.x; q < n1 * n2; q += blockDim.x) {
+            const int x = q % n1, y = q / n1, o = (y + r) * P1 + x + r;
+            B[o] = ens_update(I, A, P1, o, (uint64_t)q + 1u, t, ds, K, ff);
+        }
+        int8_t* tmp = A; A = B; B = tmp;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < n1 * n2; q += blockDim.x) {
+        const int x = q % n1, y = q / n1;
+        g[x + (int64_t)y * I.pitch] = A[(y + r) * P1 + x + r];
+    }
+}
+
+// Tiles of kEnsTile x kEnsTile with K-step temporal blocking through the two global buffers.
+// Returns the buffer index holding the final state.
+__device__ int run_tiled(const EnsInstance& I, int8_t* pool, int8_t* A0, int8_t* B0, const PhiloxKeys& K) {
+    const int r = I.radius;
+    const bool ff = fast_fire(I);
+    const int Kmax = kEnsMaxHalo / r;
+    const int ntx = (int)((I.n1 + kEnsTile - 1) / kEnsTile), nty = (int)((I.n2 + kEnsTile - 1) / kEnsTile);
+    int cur = I.cur;
+    for (int64_t s0 = 0; s0 < I.nsteps; s0 += Kmax) {
+        const int k = (int)((I.nsteps - s0) < Kmax ? (I.nsteps - s0) : Kmax);
+        const int H = k * r, S = kEnsTile + 2 * H;
+        const int8_t* src = pool + I.off[cur];
+        int8_t* dst = pool + I.off[cur ^ 1];
+        for (int tile = 0; tile < ntx * nty; ++tile) {
+            const int64_t X0 = (int64_t)(tile % ntx) * kEnsTile, Y0 = (int64_t)(tile / ntx) * kEnsTile;
+            int8_t* A = A0;
+            int8_t* B = B0;
+            __syncthreads();
+            for (int q = threadIdx.x; q < S * S; q += blockDim.x) {
+                const int lx = q % S, ly = q / S;
+                A[q] = boundary_value(I, src, I.pitch, X0 - H + lx, Y0 - H + ly);
+            }
+            __syncthreads();
+            for (int sub = 0; sub < k; ++sub) {
+                const int64_t t = I.t0 + s0 + sub;
+                const DrawStep ds = draw_step(K, t);
+                const int ex = (k - 1 - sub) * r, lo = H - ex, w = kEnsTile + 2 * ex;
+                for (int q = threadIdx.x; q < w * w; q += blockDim.x) {
+                    const int lx = lo + q % w, ly = lo + q / w, o = ly * S + lx;
+                    const int64_t mx = map_axis(I.bnd0, X0 - H + lx, I.n1), my = map_axis(I.bnd1, Y0 - H + ly, I.n2);
+                    if (mx < 0 || my < 0) {
+                        B[o] = (int8_t)(my < 0 ? I.cval1 : I.cval0);
+                        continue;
+                    }
+                    B[o] = ens_update(I, A, S, o, (uint64_t)(mx + my * I.n1) + 1u, t, ds, K, ff);
+                }
+                __syncthreads();
+                int8_t* tmp = A; A = B; B = tmp;
+            }
+            for (int q = threadIdx.x; q < kEnsTile * kEnsTile; q += blockDim.x) {
+                const int64_t gx = X0 + q % kEnsTile, gy = Y0 + q / kEnsTile;
+                if (gx < I.n1 && gy < I.n2) dst[gx + gy * I.pitch] = A[(H + q / kEnsTile) * S + H + q % kEnsTile];
+            }
+        }
+        __syncthreads();  // the whole pass is written before the next one reads it
+        cur ^= 1;
+    }
+    return cur;
+}
+
+// Integer summaries of a state (values 0..7 counted, Moran's I sums over VonNeumann(1)).
+__device__ __noinline__ void summarize(const EnsInstance& I, const int8_t* base, int64_t pitch, EnsSummary* out) {
+    __shared__ unsigned long long red[kEnsSumWords];
+    for (int k = threadIdx.x; k < kEnsSumWords; k += blockDim.x) red[k] = 0ull;
+    __syncthreads();
+    long long acc[kEnsSumWords];
+#pragma unroll
+    for (int k = 0; k < kEnsSumWords; ++k) acc[k] = 0;
+    const int64_t n = I.n1 * I.n2;
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+        const int64_t i = q % I.n1, j = q / I.n1;
+        const int x = base[i + j * pitch];
+        if (x >= 0 && x < kEnsCounts) {
+#pragma unroll
+            for (int v = 0; v < kEnsCounts; ++v) acc[v] += (x == v);
+        } else {
+            acc[kEnsCounts] += 1;
+        }
+        acc[kEnsCounts + 1] += x;
+        acc[kEnsCounts + 2] += x * x;
+        const int di[4] = {0, -1, 1, 0}, dj[4] = {-1, 0, 0, 1};
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            const int64_t a = map_axis(I.bnd0, i + di[d], I.n1), b = map_axis(I.bnd1, j + dj[d], I.n2);
+            if (a < 0 || b < 0) continue;
+            const int y = base[a + b * pitch];
+            acc[kEnsCounts + 3] += x * y;
+            acc[kEnsCounts + 4] += x + y;
+            acc[kEnsCounts + 5] += 1;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kEnsSumWords; ++k) {
+        long long v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&red[k], (unsigned long long)v);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kEnsSumWords; k += blockDim.x) out->w[k] = (long long)red[k];
+}
+
+__global__ void __launch_bounds__(kEnsThreads) k_ensemble(const EnsInstance* __restrict__ insts,
+                                                          const int* __restrict__ order, int n,
+                                                          int* __restrict__ counter, int8_t* __restrict__ pool,
+                                                          EnsSummary* __restrict__ out, int* __restrict__ final_cur) {
+    __shared__ __align__(16) int8_t sA[kEnsBuf];
+    __shared__ __align__(16) int8_t sB[kEnsBuf];
+    __shared__ int s_q;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_q = atomicAdd(counter, 1);
+        __syncthreads();
+        const int q = s_q;
+        if (q >= n) return;
+        const int i = order[q];
+        const EnsInstance I = insts[i];
+        const PhiloxKeys K = philox_keys_dev(I.seed);
+        int cur = I.cur;
+        if (I.nsteps > 0) {
+            if (I.small) {
+                run_in_smem(I, pool, sA, sB, K);
+            } else {
+                cur = run_tiled(I, pool, sA, sB, K);
+            }
+        }
+        __syncthreads();
+        summarize(I, pool + I.off[cur], I.pitch, &out[i]);
+        if (threadIdx.x == 0) final_cur[i] = cur;
+    }
+}
+
+thread_local std::string g_ens_err;
+
+int efail(int code, const char* fmt, ...) {
+    char msg[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof msg, fmt, ap);
+    va_end(ap);
+    set_last_error(msg);
+    return code;
+}
+
+}  // namespace
+
+}  // namespace gbca
+
+using namespace gbca;
+
+struct gbca_ensemble {
+    int32_t n = 0;
+    std::vector<gbca_desc> descs;
+    std::vector<EnsInstance> h_inst;
+    EnsInstance* d_inst = nullptr;
+    int* d_order = nullptr;
+    int* d_counter = nullptr;
+    int* d_cur = nullptr;
+    EnsSummary* d_out = nullptr;
+    EnsSummary* h_out = nullptr;
+    int* h_cur = nullptr;
+    int8_t* pool = nullptr;
+    size_t pool_bytes = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int grid = 0;
+    bool ran = false;
+};
+
+extern "C" {
+
+int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out) {
+    if (!out || !descs || n < 1) return efail(GBCA_ERR_ARGUMENT, "an ensemble needs at least one problem");
+    *out = nullptr;
+    std::vector<EnsInstance> inst((size_t)n);
+    size_t off = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        const gbca_desc& d = descs[i];
+        int rc = gbca_check(&d);
+        if (rc != GBCA_OK) return rc;
+        if (d.rule == GBCA_RULE_LENIA) return efail(GBCA_ERR_UNSUPPORTED, "ensemble instance %d: Lenia is not batched", i);
+        if (d.scheme != GBCA_SYNCHRONOUS)
+            return efail(GBCA_ERR_UNSUPPORTED, "ensemble instance %d: batched ensembles run Synchronous()", i);
+        if (d.radius > kEnsMaxHalo)
+            return efail(GBCA_ERR_UNSUPPORTED, "ensemble instance %d: radius %d above %d", i, d.radius, kEnsMaxHalo);
+        if (d.n1 * d.n2 >= ((int64_t)1 << 32) - 1)
+            return efail(GBCA_ERR_ARGUMENT, "ensemble instance %d: more than 2^32 - 2 cells", i);
+        EnsInstance& I = inst[(size_t)i];
+        std::memset(&I, 0, sizeof I);
+        I.n1 = d.n1;
+        I.n2 = d.n2;
+        I.pitch = d.n1;
+        I.off[0] = (int64_t)off;
+        off += (size_t)(d.n1 * d.n2 + 255) / 256 * 256;
+        I.off[1] = (int64_t)off;
+        off += (size_t)(d.n1 * d.n2 + 255) / 256 * 256;
+        I.rule = d.rule;
+        I.nbhd = d.nbhd;
+        I.radius = d.radius;
+        I.states = d.states;
+        I.birth = d.birth;
+        I.survive = d.survive;
+        I.seed = d.seed;
+        I.params_f32 = d.params_f32;
+        I.bnd0 = d.boundary[0];
+        I.bnd1 = d.boundary[1];
+        I.cval0 = d.boundary[0] == GBCA_CONSTANT ? (int32_t)d.constant[0] : 0;
+        I.cval1 = d.boundary[1] == GBCA_CONSTANT ? (int32_t)d.constant[1] : 0;
+        I.small = (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= kEnsBuf;
+    }
+    if (gbca_device_count() < 1) return efail(GBCA_ERR_CUDA, "no CUDA device is visible");
+    gbca_ensemble* e = new gbca_ensemble();
+    e->n = n;
+    e->descs.assign(descs, descs + n);
+    e->h_inst = inst;
+    e->pool_bytes = off;
+    cudaError_t c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (c == cudaSuccess) c = cudaMalloc(&e->pool, e->pool_bytes);
+    if (c == cudaSuccess) c = cudaMalloc(&e->d_inst, sizeof(EnsInstance) * n);
+    if (c == cudaSuccess) c = cudaMalloc(&e->d_order, sizeof(int) * n);
+    if (c == cudaSuccess) c = cudaMalloc(&e->d_counter, sizeof(int));
+    if (c == cudaSuccess) c = cudaMalloc(&e->d_cur, sizeof(int) * n);
+    if (c == cudaSuccess) c = cudaMalloc(&e->d_out, sizeof(EnsSummary) * n);
+    if (c == cudaSuccess) c = cudaMallocHost(&e->h_out, sizeof(EnsSummary) * n);
+    if (c == cudaSuccess) c = cudaMallocHost(&e->h_cur, sizeof(int) * n);
+    if (c == cudaSuccess) c = cudaMemsetAsync(e->pool, 0, e->pool_bytes, e->stream);
+    if (c == cudaSuccess) c = cudaMemsetAsync(e->d_out, 0, sizeof(EnsSummary) * n, e->stream);
+    if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
+    int dev = 0, nsm = 0, per = 0;
+    if (c == cudaSuccess) c = cudaGetDevice(&dev);
+    if (c == cudaSuccess) c = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (c == cudaSuccess) c = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ensemble, kEnsThreads, 0);
+    if (c != cudaSuccess) {
+        const bool oom = c == cudaErrorMemoryAllocation;
+        gbca_ensemble_destroy(e);
+        cudaGetLastError();
+        return oom ? efail(GBCA_ERR_OUT_OF_MEMORY, "ensemble allocation of %zu bytes failed", off)
+                   : efail(GBCA_ERR_CUDA, "gbca_ensemble_create: %s", cudaGetErrorString(c));
+    }
+    e->grid = nsm * (per > 0 ? per : 1);
+    *out = e;
+    return GBCA_OK;
+}
+
+int gbca_ensemble_destroy(gbca_ensemble* e) {
+    if (!e) return GBCA_OK;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    cudaFree(e->pool);
+    cudaFree(e->d_inst);
+    cudaFree(e->d_order);
+    cudaFree(e->d_counter);
+    cudaFree(e->d_cur);
+    cudaFree(e->d_out);
+    if (e->h_out) cudaFreeHost(e->h_out);
+    if (e->h_cur) cudaFreeHost(e->h_cur);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return GBCA_OK;
+}
+
+int gbca_ensemble_set_state(gbca_ensemble* e, int32_t i, const void* host, size_t nbytes) {
+    if (!e || !host || i < 0 || i >= e->n) return efail(GBCA_ERR_ARGUMENT, "bad ensemble, instance or state");
+    const EnsInstance& I = e->h_inst[(size_t)i];
+    if (nbytes != (size_t)(I.n1 * I.n2))
+        return efail(GBCA_ERR_STATE, "instance %d has %lld cells, the state %zu bytes", i, (long long)(I.n1 * I.n2),
+                     nbytes);
+    cudaError_t c = cudaMemcpyAsync(e->pool + I.off[I.cur], host, nbytes, cudaMemcpyHostToDevice, e->stream);
+    if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble set_state: %s", cudaGetErrorString(c));
+    return GBCA_OK;
+}
+
+int gbca_ensemble_fill(gbca_ensemble* e, int32_t value) {
+    if (!e) return efail(GBCA_ERR_ARGUMENT, "null ensemble");
+    if (value < -128 || value > 127) return efail(GBCA_ERR_ARGUMENT, "fill value %d is not an Int8", value);
+    cudaError_t c = cudaMemsetAsync(e->pool, value & 0xFF, e->pool_bytes, e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble fill: %s", cudaGetErrorString(c));
+    return GBCA_OK;
+}
+
+int gbca_ensemble_run(gbca_ensemble* e, const int64_t* t0, const int64_t* nsteps, const double* params,
+                      int32_t nparams) {
+    if (!e || !nsteps) return efail(GBCA_ERR_ARGUMENT, "null ensemble or step counts");
+    std::vector<int64_t> work((size_t)e->n);
+    for (int32_t i = 0; i < e->n; ++i) {
+        EnsInstance& I = e->h_inst[(size_t)i];
+        const gbca_desc& d = e->descs[(size_t)i];
+        if (nsteps[i] < 0) return efail(GBCA_ERR_ARGUMENT, "instance %d: negative step count", i);
+        I.t0 = t0 ? t0[i] : 0;
+        I.nsteps = nsteps[i];
+        if (d.rule == GBCA_RULE_FOREST_FIRE) {
+            if (!params || nparams < 2) return efail(GBCA_ERR_ARGUMENT, "forest-fire instances need (p, f) each");
+            I.thr_p = gbca_threshold(params[(size_t)i * nparams], d.params_f32);
+            I.thr_f = gbca_threshold(params[(size_t)i * nparams + 1], d.params_f32);
+        }
+        work[(size_t)i] = I.n1 * I.n2 * (I.nsteps > 0 ? I.nsteps : 0);
+    }
+    std::vector<int> order((size_t)e->n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[(size_t)a] > work[(size_t)b]; });
+    cudaError_t c = cudaMemcpyAsync(e->d_inst, e->h_inst.data(), sizeof(EnsInstance) * e->n, cudaMemcpyHostToDevice,
+                                    e->stream);
+    if (c == cudaSuccess)
+        c = cudaMemcpyAsync(e->d_order, order.data(), sizeof(int) * e->n, cudaMemcpyHostToDevice, e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble upload: %s", cudaGetErrorString(c));
+    if (!e->exec) {  // capture the run once: reset the work counter, one persistent launch
+        cudaGraph_t g = nullptr;
+        c = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+        if (c == cudaSuccess) {
+            cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream);
+            k_ensemble<<<e->grid, kEnsThreads, 0, e->stream>>>(e->d_inst, e->d_order, e->n, e->d_counter, e->pool,
+                                                               e->d_out, e->d_cur);
+            c = cudaStreamEndCapture(e->stream, &g);
+        }
+        if (c == cudaSuccess) c = cudaGraphInstantiate(&e->exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble graph capture: %s", cudaGetErrorString(c));
+    }
+    c = cudaGraphLaunch(e->exec, e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble launch: %s", cudaGetErrorString(c));
+    count_launch();
+    // results come back with the summaries; the buffer holding each final state too
+    c = cudaMemcpyAsync(e->h_cur, e->d_cur, sizeof(int) * e->n, cudaMemcpyDeviceToHost, e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble result copy: %s", cudaGetErrorString(c));
+    e->ran = true;
+    return GBCA_OK;
+}
+
+int gbca_ensemble_sync(gbca_ensemble* e) {
+    if (!e) return efail(GBCA_ERR_ARGUMENT, "null ensemble");
+    cudaError_t c = cudaStreamSynchronize(e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble sync: %s", cudaGetErrorString(c));
+    if (e->ran) {
+        for (int32_t i = 0; i < e->n; ++i) e->h_inst[(size_t)i].cur = e->h_cur[i];
+        e->ran = false;
+    }
+    return GBCA_OK;
+}
+
+int gbca_ensemble_summaries(gbca_ensemble* e, int64_t* counts, int32_t nvals, int64_t* other, double* morans) {
+    if (!e) return efail(GBCA_ERR_ARGUMENT, "null ensemble");
+    if (nvals < 0 || nvals > kEnsCounts) return efail(GBCA_ERR_ARGUMENT, "nvals must be in 0:%d", kEnsCounts);
+    int rc = gbca_ensemble_sync(e);
+    if (rc != GBCA_OK) return rc;
+    cudaError_t c = cudaMemcpyAsync(e->h_out, e->d_out, sizeof(EnsSummary) * e->n, cudaMemcpyDeviceToHost, e->stream);
+    if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble summaries: %s", cudaGetErrorString(c));
+    for (int32_t i = 0; i < e->n; ++i) {
+        const long long* w = e->h_out[i].w;
+        const int64_t ncell = e->h_inst[(size_t)i].n1 * e->h_inst[(size_t)i].n2;
+        int64_t inrange = 0;
+        for (int v = 0; v < kEnsCounts; ++v) {
+            if (v < nvals && counts) counts[(size_t)i * nvals + v] = w[v];
+            if (v < nvals) inrange += w[v];
+        }
+        if (other) other[i] = ncell - inrange;
+        if (morans)
+            morans[i] = morans_from_sums(w[kEnsCounts + 1], w[kEnsCounts + 2], w[kEnsCounts + 3], w[kEnsCounts + 4],
+                                         w[kEnsCounts + 5], ncell);
+    }
+    return GBCA_OK;
+}
+
+int gbca_ensemble_get_state(gbca_ensemble* e, int32_t i, void* host, size_t nbytes) {
+    if (!e || !host || i < 0 || i >= e->n) return efail(GBCA_ERR_ARGUMENT, "bad ensemble, instance or buffer");
+    int rc = gbca_ensemble_sync(e);
+    if (rc != GBCA_OK) return rc;
+    const EnsInstance& I = e->h_inst[(size_t)i];
+    if (nbytes != (size_t)(I.n1 * I.n2))
+        return efail(GBCA_ERR_STATE, "instance %d has %lld cells, the buffer %zu bytes", i, (long long)(I.n1 * I.n2),
+                     nbytes);
+    cudaError_t c = cudaMemcpyAsync(host, e->pool + I.off[I.cur], nbytes, cudaMemcpyDeviceToHost, e->stream);
+    if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble get_state: %s", cudaGetErrorString(c));
+    return GBCA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,27 @@
+// ensemble.cuh — device descriptors and results of the batched ensemble engine.
+#pragma once
+#include <cstdint>
+
+namespace gbca {
+
+constexpr int kEnsCounts = 8;                  // values 0..7 are counted per instance
+constexpr int kEnsSumWords = kEnsCounts + 6;   // counts, cells outside 0..7, S, S2, P, Q, W
+
+// One instance, as the persistent kernel reads it.
+struct EnsInstance {
+    int64_t n1, n2, pitch;   // lattice dims, bytes between columns
+    int64_t off[2];          // byte offsets of its two buffers in the pool
+    int64_t t0, nsteps;      // time of the first step and step count of the next run
+    uint64_t birth, survive, seed, thr_p, thr_f;
+    int32_t rule, nbhd, radius, states;
+    int32_t params_f32, bnd0, bnd1, cval0, cval1;
+    int32_t cur;             // buffer holding the current state
+    int32_t small;           // fits in shared memory with its halo
+    int32_t pad;
+};
+
+struct EnsSummary {
+    long long w[kEnsSumWords];
+};
+
+}  // namespace gbca

@@ -24,14 +24,13 @@ __device__ __forceinline__ uint2 philox_w01(uint32_t c0, uint32_t c1, uint32_t c
                                             uint32_t k0, uint32_t k1) {
 #pragma unroll
     for (int r = 0; r < 9; ++r) {
-        const uint32_t hi0 = __umulhi(kPhM0, c0), lo0 = kPhM0 * c0;
-        const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
-        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        const uint64_t p0 = (uint64_t)kPhM0 * c0, p1 = (uint64_t)kPhM1 * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
         k0 += kPhW0; k1 += kPhW1;
     }
-    const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
-    return make_uint2(hi1 ^ c1 ^ k0, lo1);
+    const uint64_t p1 = (uint64_t)kPhM1 * c2;
+    return make_uint2((uint32_t)(p1 >> 32) ^ c1 ^ k0, (uint32_t)p1);
 }
 
 // The draw of cell `id` (1-based column-major linear index, backends.jl:446) at time t
@@ -49,52 +48,75 @@ __device__ __forceinline__ bool draw_below(uint2 w, uint64_t thr, bool f32) {
     return ((((uint64_t)w.x << 32) | (uint64_t)w.y) >> 11) < thr;
 }
 
+// The ten round keys of a seed: (seed lo + r W0, seed hi + r W1), r = 0..9 (random.jl:31-33).
+// Passed in the kernel parameters, so each key XOR is one three-input LOP3 with a
+// parameter-bank operand instead of a per-thread running sum.
+struct PhiloxKeys {
+    uint32_t k0[10], k1[10];
+};
+
+__host__ __device__ inline PhiloxKeys philox_keys(uint64_t seed) {
+    PhiloxKeys K;
+    uint32_t a = (uint32_t)seed, b = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        K.k0[r] = a;
+        K.k1[r] = b;
+        a += kPhW0;
+        b += kPhW1;
+    }
+    return K;
+}
+
+// One Philox round with both 32x32 products as single 64-bit multiplies.
+__device__ __forceinline__ void philox_round(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3, uint32_t k0,
+                                             uint32_t k1) {
+    const uint64_t p0 = (uint64_t)kPhM0 * c0, p1 = (uint64_t)kPhM1 * c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    c1 = (uint32_t)p1;
+    c3 = (uint32_t)p0;
+    c0 = n0;
+    c2 = n2;
+}
+
 // Per-step constant part of a cell draw: the counter words that do not depend on the
 // cell (t in word 3, the id's high word 0 in word 2) make the first product of round 1
 // and both words of round 2's first product uniform across a sub-step. DrawStep holds
 // them; draw_fast() then needs 17 per-cell 32x32 products instead of 19. Valid only for
 // ids below 2^32 (lattices of fewer than 4.29e9 cells); the caller checks that.
 struct DrawStep {
-    uint32_t c0_1, c1_1;  // words 1, 2 after round 1 (uniform)
+    uint32_t c0_1, c1_1;    // words 1, 2 after round 1 (uniform)
     uint32_t hi0_2, lo0_2;  // M0 * c0_1 (uniform, used in round 2)
-    uint32_t k0, k1;      // key
 };
 
-__device__ __forceinline__ DrawStep draw_step(uint64_t seed, int64_t t) {
+__device__ __forceinline__ PhiloxKeys philox_keys_dev(uint64_t seed) { return philox_keys(seed); }
+
+__device__ __forceinline__ DrawStep draw_step(const PhiloxKeys& K, int64_t t) {
     DrawStep s;
-    s.k0 = (uint32_t)seed;
-    s.k1 = (uint32_t)(seed >> 32);
-    const uint32_t c2 = (uint32_t)(uint64_t)t;
-    const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
-    s.c0_1 = hi1 ^ 0u ^ s.k0;  // c1 = id hi = 0
-    s.c1_1 = lo1;
-    s.hi0_2 = __umulhi(kPhM0, s.c0_1);
-    s.lo0_2 = kPhM0 * s.c0_1;
+    const uint64_t p1 = (uint64_t)kPhM1 * (uint32_t)(uint64_t)t;
+    s.c0_1 = (uint32_t)(p1 >> 32) ^ K.k0[0];  // ^ c1, the id's high word, which is 0
+    s.c1_1 = (uint32_t)p1;
+    const uint64_t p0 = (uint64_t)kPhM0 * s.c0_1;
+    s.hi0_2 = (uint32_t)(p0 >> 32);
+    s.lo0_2 = (uint32_t)p0;
     return s;
 }
 
-__device__ __forceinline__ uint2 draw_fast(const DrawStep& s, uint32_t id, uint32_t k) {
-    // round 1 (c0 = id, c1 = 0, c2 = t, c3 = k)
-    const uint32_t hi0 = __umulhi(kPhM0, id), lo0 = kPhM0 * id;
-    uint32_t c0 = s.c0_1, c1 = s.c1_1, c2 = hi0 ^ k ^ s.k1, c3 = lo0;
-    uint32_t k0 = s.k0 + kPhW0, k1 = s.k1 + kPhW1;
-    // round 2: the M0 product of c0 is uniform
-    {
-        const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
-        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = s.hi0_2 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = s.lo0_2;
-        k0 += kPhW0; k1 += kPhW1;
+// Words 1 and 2 of the draw of cell `id` (< 2^32) with draw index k at the sub-step of s.
+__device__ __forceinline__ uint2 draw_fast(const DrawStep& s, const PhiloxKeys& K, uint32_t id, uint32_t k) {
+    const uint64_t q = (uint64_t)kPhM0 * id;  // round 1: c0 = id, c2 = t, c3 = k
+    uint32_t c0 = s.c0_1, c1 = s.c1_1, c2 = (uint32_t)(q >> 32) ^ k ^ K.k1[0], c3 = (uint32_t)q;
+    {   // round 2: the M0 product of c0 is uniform
+        const uint64_t p1 = (uint64_t)kPhM1 * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ K.k0[1], n2 = s.hi0_2 ^ c3 ^ K.k1[1];
+        c1 = (uint32_t)p1;
+        c3 = s.lo0_2;
+        c0 = n0;
+        c2 = n2;
     }
 #pragma unroll
-    for (int r = 2; r < 9; ++r) {
-        const uint32_t hi0r = __umulhi(kPhM0, c0), lo0r = kPhM0 * c0;
-        const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
-        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0r ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0r;
-        k0 += kPhW0; k1 += kPhW1;
-    }
-    const uint32_t hi1 = __umulhi(kPhM1, c2), lo1 = kPhM1 * c2;
-    return make_uint2(hi1 ^ c1 ^ k0, lo1);
+    for (int r = 2; r < 9; ++r) philox_round(c0, c1, c2, c3, K.k0[r], K.k1[r]);
+    const uint64_t p1 = (uint64_t)kPhM1 * c2;  // round 10: words 1 and 2 only
+    return make_uint2((uint32_t)(p1 >> 32) ^ c1 ^ K.k0[9], (uint32_t)p1);
 }
 
 // ----------------------------------------------------------------- boundaries
@@ -136,6 +158,7 @@ struct SweepParams {
     int64_t t0;                // time of the first sub-step's step
     int32_t tile_x, tile_y;    // output tile
     int32_t halo_x, halo_y;    // loaded halo (>= nsub * radius)
+    PhiloxKeys keys;           // round keys of `seed` (set by the launchers that use them)
 };
 
 // The message gbca_last_error() returns on this thread.

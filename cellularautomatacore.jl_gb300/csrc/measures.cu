@@ -100,15 +100,16 @@ void finish_measures(const unsigned long long* acc, int64_t n, int64_t* counts, 
     }
     if (other) *other = n - inrange;
     if (!morans) return;
-    const __int128 S = (long long)acc[256], S2 = (long long)acc[257], P = (long long)acc[258];
-    const __int128 Q = (long long)acc[259], W = (long long)acc[260], N = n;
+    *morans = morans_from_sums((long long)acc[256], (long long)acc[257], (long long)acc[258], (long long)acc[259],
+                               (long long)acc[260], n);
+}
+
+double morans_from_sums(long long s, long long s2, long long p, long long q, long long w, int64_t n) {
+    const __int128 S = s, S2 = s2, P = p, Q = q, W = w, N = n;
     const __int128 num = N * N * P - N * S * Q + W * S * S;
     const __int128 den = W * (N * S2 - S * S);
-    if (den == 0 || W == 0) {
-        *morans = __builtin_nan("");
-        return;
-    }
-    *morans = (double)((long double)num / (long double)den);
+    if (den == 0 || W == 0) return __builtin_nan("");
+    return (double)((long double)num / (long double)den);
 }
 
 }  // namespace gbca

@@ -16,4 +16,7 @@ cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pit
 void finish_measures(const unsigned long long* acc, int64_t n, int64_t* counts, int32_t nvals, int64_t* other,
                      double* morans);
 
+// Moran's I from its integer sums (S, S2, P, Q, W) over n cells; NaN for a constant field.
+double morans_from_sums(long long S, long long S2, long long P, long long Q, long long W, int64_t n);
+
 }  // namespace gbca

@@ -160,20 +160,20 @@ __device__ __forceinline__ uint32_t ge(const uint32_t* v, const uint32_t* m) {
     return g;
 }
 
-template <int BV>
+// NI interval tests per kind, unrolled with no branches; the tables fill unused intervals
+// with an empty one (lo = 1, hi + 1 = 0), which never matches.
+template <int BV, int NI>
 __device__ __forceinline__ uint32_t life_rule(const uint32_t* v, uint32_t c, const LifeTables& tb) {
-    uint32_t out[2] = {0u, 0u};
+    uint32_t dead = 0u, live = 0u;
 #pragma unroll
-    for (int kind = 0; kind < 2; ++kind) {
-#pragma unroll
-        for (int k = 0; k < kMaxIntervals; ++k) {
-            if (k < tb.n[kind]) out[kind] |= ge<BV>(v, tb.m[kind][k][0]) & ~ge<BV>(v, tb.m[kind][k][1]);
-        }
+    for (int k = 0; k < NI; ++k) {
+        dead |= ge<BV>(v, tb.m[0][k][0]) & ~ge<BV>(v, tb.m[0][k][1]);
+        live |= ge<BV>(v, tb.m[1][k][0]) & ~ge<BV>(v, tb.m[1][k][1]);
     }
-    return (c & out[1]) | (~c & out[0]);
+    return (c & live) | (~c & dead);
 }
 
-template <int R>
+template <int R, int NI>
 __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw, int w,
                                             int r0, int r1, const LifeTables& tb) {
     constexpr int N = LifeBits<R>::N, BH = LifeBits<R>::H, BV = LifeBits<R>::V;
@@ -193,7 +193,7 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
         for (int k = 0; k < N; ++k) {
             const int y = y0 + k;
             if (y < r1) {
-                cb[y * sw] = life_rule<BV>(v, ca[y * sw], tb);
+                cb[y * sw] = life_rule<BV, NI>(v, ca[y * sw], tb);
                 if (y + 1 < r1) {
                     vsub<BH, BV>(v, ring[k]);
                     hrow<R>(ca + (y + R + 1) * sw, ring[k]);
@@ -242,7 +242,7 @@ __device__ __forceinline__ uint32_t load_bits32(const SweepParams& p, const int8
     return bits;
 }
 
-template <int R>
+template <int R, int NI>
 __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g, LifeTables tb,
                                                        const int8_t* __restrict__ src, int8_t* __restrict__ dst) {
     extern __shared__ __align__(16) uint32_t smw[];
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
         if (seg < nseg) {
             const int rows = y_hi - y_lo;
             const int r0 = y_lo + (seg * rows) / nseg, r1 = y_lo + ((seg + 1) * rows) / nseg;
-            if (r1 > r0) life_column<R>(A, B, g.sw, w_lo + threadIdx.x % nw, r0, r1, tb);
+            if (r1 > r0) life_column<R, NI>(A, B, g.sw, w_lo + threadIdx.x % nw, r0, r1, tb);
         }
         __syncthreads();
         if (fix) {
@@ -345,22 +345,31 @@ bool make_tables(const SweepParams& p, LifeTables* tb) {
         tb->n[kind] = n;
         for (int k = 0; k < kMaxIntervals; ++k)
             for (int j = 0; j < 2; ++j) {
-                const int L = k < n ? (j == 0 ? lo[k] : hi[k] + 1) : 0;
+                const int L = k < n ? (j == 0 ? lo[k] : hi[k] + 1) : (j == 0 ? 1 : 0);  // unused: empty
                 for (int i = 0; i < 8; ++i) tb->m[kind][k][j][i] = ((L >> i) & 1) ? 0u : 0xFFFFFFFFu;
             }
     }
     return true;
 }
 
+template <int R, int NI>
+cudaError_t launch_rn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
+                      cudaStream_t st) {
+    const size_t smem = 2 * (size_t)g.sw * (size_t)g.sy * 4;
+    cudaError_t e = cudaFuncSetAttribute(k_life<R, NI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((p.n1 + 32 * g.tw - 1) / (32 * g.tw)), (unsigned)((p.n2 + g.ty - 1) / g.ty));
+    k_life<R, NI><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
+    return cudaGetLastError();
+}
+
 template <int R>
 cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                      cudaStream_t st) {
-    const size_t smem = 2 * (size_t)g.sw * (size_t)g.sy * 4;
-    cudaError_t e = cudaFuncSetAttribute(k_life<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)((p.n1 + 32 * g.tw - 1) / (32 * g.tw)), (unsigned)((p.n2 + g.ty - 1) / g.ty));
-    k_life<R><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
-    return cudaGetLastError();
+    const int ni = tb.n[0] > tb.n[1] ? tb.n[0] : tb.n[1];
+    if (ni <= 1) return launch_rn<R, 1>(p, g, tb, src, dst, st);
+    if (ni <= 2) return launch_rn<R, 2>(p, g, tb, src, dst, st);
+    return launch_rn<R, kMaxIntervals>(p, g, tb, src, dst, st);
 }
 
 }  // namespace

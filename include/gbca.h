@@ -143,6 +143,36 @@ int gbca_set_stream(gbca_handle* h, void* stream);
  * A diagnostic with no counterpart in the reference. */
 int64_t gbca_kernel_launches(void);
 
+/* ---- batched ensembles: many problems advanced by one persistent, graph-captured launch.
+ * Replaces solving an EnsembleProblem one trajectory at a time (src/problem.jl:571-589 with
+ * SciMLBase's EnsembleSerial / EnsembleThreads; src/calibration.jl:66-91 for ABC): each
+ * instance is its own gbca_desc (its size, rule, boundaries and seed — seed_trajectory gives
+ * trajectory i the seed prob.seed + i), Int8 rules, Synchronous, radius <= 8. */
+typedef struct gbca_ensemble gbca_ensemble;
+
+/* Allocates every instance's two state buffers (zeroed) in one pool. */
+int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out);
+int gbca_ensemble_destroy(gbca_ensemble* e);
+
+/* Initial state of instance i (n1*n2 bytes, column-major), or every cell of every instance. */
+int gbca_ensemble_set_state(gbca_ensemble* e, int32_t i, const void* host, size_t nbytes);
+int gbca_ensemble_fill(gbca_ensemble* e, int32_t value);
+
+/* Advances instance i by nsteps[i] steps from time t0[i] (t0 may be NULL for 0), with its
+ * parameters at params[i * nparams ...] (forest fire: p, f). One graph launch; queued. At the
+ * end of the run every instance's state counts and Moran's I sums are computed on the device. */
+int gbca_ensemble_run(gbca_ensemble* e, const int64_t* t0, const int64_t* nsteps, const double* params,
+                      int32_t nparams);
+int gbca_ensemble_sync(gbca_ensemble* e);
+
+/* state_counts and Moran's I (src/measures.jl:14-20,91-107) of every instance's state at the
+ * end of the last run: counts[i * nvals + v] for v < nvals <= 8, other[i], morans[i] (NaN for a
+ * constant field). The same integers, hence the same bits, as gbca_summaries on one handle. */
+int gbca_ensemble_summaries(gbca_ensemble* e, int64_t* counts, int32_t nvals, int64_t* other, double* morans);
+
+/* current_state of instance i. */
+int gbca_ensemble_get_state(gbca_ensemble* e, int32_t i, void* host, size_t nbytes);
+
 /* Size of the device scratch array behind gbca_advance_noalloc: the largest state, in bytes
  * (pitch * n2), that it accepts. Every GPU that loads the library holds this array until
  * the process exits. */

@@ -1,0 +1,140 @@
+"""Batched ensembles on the GPU: one persistent launch over instances of different sizes,
+rules, boundaries, seeds, parameters and step counts must give, instance by instance, the
+final states of one solve per instance and of the oracle, and state counts / Moran's I
+identical (==) to the single-handle device summaries (src/problem.jl:571-589,
+src/measures.jl:14-20,91-107). ABC on the batched ensemble equals the serial ensemble
+(test/test_calibration.jl:21-33)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ca():
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.load_package()
+    if m.capi.lib().gbca_device_count() < 1:
+        pytest.fail("no CUDA device visible")
+    return m
+
+
+def mixed_problems(ca, n=36, seed=7):
+    rng = np.random.default_rng(seed)
+    probs = []
+    for i in range(n):
+        side1 = int(rng.integers(10, 320))
+        side2 = int(rng.integers(10, 320))
+        steps = int(rng.integers(5, 40))
+        kind = i % 4
+        if kind == 0:
+            rule, space, p, C = ca.ForestFire(), ca.Grid(side1, side2), {"p": float(rng.uniform(0.01, 0.3)),
+                                                                        "f": float(rng.uniform(1e-4, 1e-2))}, 3
+        elif kind == 1:
+            rule, space, p, C = ca.Life("B3/S23"), ca.Torus(side1, side2), None, 2
+        elif kind == 2:
+            rule, space, p, C = ca.Generations(":brians_brain"), ca.Torus(side1, side2), None, 3
+        else:
+            rule = ca.Life(range(3, 9), range(2, 10), neighbourhood=ca.Moore(2))
+            space, p, C = ca.Lattice((side1, side2), (ca.Reflecting(), ca.Constant(0))), None, 2
+        u0 = rng.integers(0, C, (side1, side2)).astype(np.int8)
+        probs.append(ca.CAProblem.new(rule, u0, steps, p, space=space, seed=100 + i))
+    return probs
+
+
+def single(ca, prob, t0, nsteps, u):
+    """One problem alone through a GB300 handle: final state and device summaries."""
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    ca.set_state(B, st, u)
+    for t in range(t0, t0 + nsteps):
+        ca.advance(B, st, prob, ca.Synchronous(), prob.p, t)
+    out = ca.current_state(B, st)
+    counts, other, mi = ca.device_summaries(st, 3)
+    st.close()
+    return out, counts, other, mi
+
+
+def test_batched_equals_one_solve_per_instance(ca, oracle):
+    probs = mixed_problems(ca)
+    ens = ca.BatchedEnsemble(probs)
+    ens.set_initial_states()
+    states = [np.asarray(p.u0) for p in probs]
+    t0 = [0] * len(probs)
+    for rnd in range(2):  # the second run continues the first
+        steps = [p.tspan[1] for p in probs] if rnd == 0 else [7 + (i % 5) for i in range(len(probs))]
+        ens.run(t0=t0, nsteps=steps)
+        counts, other, morans = ens.summaries(3)
+        for i, p in enumerate(probs):
+            got = ens.state(i)
+            want, c1, o1, m1 = single(ca, p, t0[i], steps[i], states[i])
+            assert np.array_equal(got, want), f"instance {i} ({p.rule}, {p.space.dims}) run {rnd}"
+            assert list(counts[i]) == c1 and other[i] == o1
+            assert (morans[i] == m1) or (np.isnan(morans[i]) and np.isnan(m1)), (i, morans[i], m1)
+            states[i] = got
+            t0[i] += steps[i]
+    # and against the oracle for a few instances
+    for i in (0, 1, 2, 3):
+        p = probs[i]
+        o = oracle
+        if isinstance(p.rule, ca.ForestFire):
+            P = o.Problem(o.RULE_FOREST_FIRE, *p.space.dims, nbhd=o.VON_NEUMANN, seed=p.seed,
+                          boundary=(o.CONSTANT, o.CONSTANT))
+            par = (p.p["p"], p.p["f"])
+        elif isinstance(p.rule, ca.Generations):
+            P = o.Problem(o.RULE_GENERATIONS, *p.space.dims, birth=p.rule.birth, survive=p.rule.survive, states=3,
+                          seed=p.seed)
+            par = None
+        elif p.neighbours.radius == 1:
+            P = o.Problem(o.RULE_LIFE, *p.space.dims, birth=p.rule.birth, survive=p.rule.survive, seed=p.seed)
+            par = None
+        else:
+            P = o.Problem(o.RULE_LIFE, *p.space.dims, radius=2, birth=p.rule.birth, survive=p.rule.survive,
+                          boundary=(o.REFLECTING, o.CONSTANT), seed=p.seed)
+            par = None
+        want = o.run_array(P, p.u0, 0, t0[i], par, nthreads=8)
+        assert np.array_equal(states[i], want), i
+    ens.close()
+
+
+def test_forest_fire_ensemble_from_empty(ca):
+    """The batched forest-fire ensemble shape (square sides log-uniform, p ~ U(0.01, 0.1),
+    f ~ LogU(1e-5, 1e-3), seeds 1..n, all empty at t = 0), at 48 instances and 120 steps."""
+    rng = np.random.Generator(np.random.PCG64(4096))
+    n = 48
+    sides = np.round(np.exp(rng.uniform(np.log(64), np.log(1024), n))).astype(int)
+    ps = rng.uniform(0.01, 0.1, n)
+    fs = np.exp(rng.uniform(np.log(1e-5), np.log(1e-3), n))
+    probs = [ca.CAProblem.new(ca.ForestFire(), np.zeros((s, s), np.int8), 120, {"p": ps[i], "f": fs[i]},
+                              space=ca.Grid(int(s), int(s)), seed=i + 1) for i, s in enumerate(sides)]
+    res = ca.solve_ensemble(ca.EnsembleProblem(probs[0]), trajectories=1)  # the API path works
+    assert len(res.u) == 1
+    ens = ca.BatchedEnsemble(probs)
+    ens.fill(0)
+    ens.run()
+    counts, other, morans = ens.summaries(3)
+    for i in (0, 5, int(np.argmax(sides)), int(np.argmin(sides))):
+        _, c1, o1, m1 = single(ca, probs[i], 0, 120, np.zeros((sides[i], sides[i]), np.int8))
+        assert list(counts[i]) == c1 and other[i] == o1 and morans[i] == m1
+    assert counts.sum() == int((sides.astype(np.int64) ** 2).sum())
+    ens.close()
+
+
+def test_abc_batched_equals_serial(ca):
+    """Proposal i runs with seed prob.seed + i and p = proposals[i]; distances and acceptance
+    do not depend on the ensemble algorithm (test/test_calibration.jl:21-33)."""
+    u0 = np.zeros((40, 30), np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 25, {"p": 0.1, "f": 0.001}, space=ca.Grid(40, 30), seed=3)
+    observed = ca.final_state(ca.solve(prob.remake(seed=100), save_everystep=False))
+    trees = lambda u: int((np.asarray(u) == 1).sum())
+    dist = lambda sol, obs: abs(trees(ca.final_state(sol)) - trees(obs))
+    proposals = [{"p": float(b), "f": 0.001} for b in np.arange(0.02, 0.4, 0.02)]
+    res = ca.abc_rejection(prob, proposals, dist, observed, keep=4)
+    ser = ca.abc_rejection(prob, proposals, dist, observed, keep=4, ensemblealg=object())
+    assert res.proposal_distances == ser.proposal_distances
+    assert res.samples == ser.samples and len(res.samples) == 4
+    for i in (1, 6, 12):
+        s = ca.solve(prob.remake(p=proposals[i - 1], seed=prob.seed + i), save_everystep=False)
+        assert res.proposal_distances[i - 1] == dist(s, observed)
+    assert res.distances == sorted(res.proposal_distances)[:4]

@@ -85,6 +85,10 @@ CASES = [
      (0.1, 0.002)),
     ("forest fire, Stochastic(0.7)", "fire", (64, 80), dict(nb="vn", seed=6, scheme="stoch", sp=0.7), 20, 5,
      (0.2, 0.01)),
+    ("forest fire, p = 1 and f = 1", "fire", (520, 300), dict(nb="vn", seed=2, bnd=("c", "c")), 10, 3, (1.0, 1.0)),
+    ("forest fire, p = 0, f = 1, Float32", "fire", (300, 260), dict(nb="vn", seed=2, f32=True), 9, 9, (0.0, 1.0)),
+    ("forest fire, reflecting edges, tiled", "fire", (700, 300), dict(nb="vn", seed=12, bnd=("r", "p")), 17, 17,
+     (0.07, 0.003)),
 ]
 
 
