@@ -268,6 +268,94 @@ def run_case(args):
     lib.gbca_destroy(h)
 
 
+ENS = dict(n=4096, steps=500, plain_sample=256)
+
+
+def ensemble_instances():
+    """4096 forest-fire instances: square sides log-uniform in 64..1024, p ~ U(0.01, 0.1),
+    f ~ LogU(1e-5, 1e-3), seeds 1..4096 (numpy PCG64(4096))."""
+    rng = np.random.Generator(np.random.PCG64(4096))
+    n = ENS["n"]
+    sides = np.round(np.exp(rng.uniform(np.log(64), np.log(1024), n))).astype(np.int64)
+    ps = rng.uniform(0.01, 0.1, n)
+    fs = np.exp(rng.uniform(np.log(1e-5), np.log(1e-3), n))
+    return sides, ps, fs, np.arange(1, n + 1)
+
+
+def fire_desc(capi, side, seed):
+    d = capi.Desc()
+    d.rule, d.nbhd, d.radius = capi.RULE_FOREST_FIRE, capi.VON_NEUMANN, 1
+    d.n1 = d.n2 = int(side)
+    d.boundary[0] = d.boundary[1] = capi.CONSTANT
+    d.seed = int(seed)
+    return d
+
+
+def bench_batched(capi, lib, warmup: int, steps: int):
+    """The batched ensemble (one persistent graph-captured launch per run) against one solve
+    per instance through the same library, on a random sample; summaries compared exactly."""
+    sides, ps, fs, seeds = ensemble_instances()
+    n = len(sides)
+    descs = (capi.Desc * n)()
+    for i in range(n):
+        descs[i] = fire_desc(capi, sides[i], seeds[i])
+    e = ctypes.c_void_p()
+    capi.check(lib.gbca_ensemble_create(descs, n, ctypes.byref(e)))
+    T0 = (ctypes.c_int64 * n)()
+    S = (ctypes.c_int64 * n)(*([ENS["steps"]] * n))
+    P = (ctypes.c_double * (2 * n))(*np.column_stack([ps, fs]).ravel().tolist())
+
+    def run():
+        capi.check(lib.gbca_ensemble_fill(e, 0))
+        capi.check(lib.gbca_ensemble_run(e, T0, S, P, 2))
+        capi.check(lib.gbca_ensemble_sync(e))
+
+    for _ in range(warmup):
+        run()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        run()
+    t_batched = (time.perf_counter() - t0) / steps
+    C = (ctypes.c_int64 * (3 * n))()
+    O = (ctypes.c_int64 * n)()
+    M = (ctypes.c_double * n)()
+    capi.check(lib.gbca_ensemble_summaries(e, C, 3, O, M))
+    lib.gbca_ensemble_destroy(e)
+
+    # one solve per instance: create, upload, advance, summaries, destroy — a random sample
+    rng = np.random.Generator(np.random.PCG64(1))
+    sample = rng.choice(n, ENS["plain_sample"], replace=False)
+    exact = 0
+    t0 = time.perf_counter()
+    for i in sample:
+        h = ctypes.c_void_p()
+        d = fire_desc(capi, sides[i], seeds[i])
+        capi.check(lib.gbca_create(ctypes.byref(d), ctypes.byref(h)))
+        zeros = np.zeros(int(sides[i]) ** 2, np.int8)
+        capi.check(lib.gbca_set_state(h, zeros.ctypes.data, zeros.nbytes))
+        pr = (ctypes.c_double * 2)(ps[i], fs[i])
+        capi.check(lib.gbca_advance(h, 0, ENS["steps"], pr, 2))
+        c3 = (ctypes.c_int64 * 3)()
+        o1 = ctypes.c_int64()
+        m1 = ctypes.c_double()
+        capi.check(lib.gbca_summaries(h, c3, 3, ctypes.byref(o1), ctypes.byref(m1)))
+        lib.gbca_destroy(h)
+        same = list(c3) == [C[3 * i + k] for k in range(3)] and (m1.value == M[i] or (np.isnan(m1.value) and
+                                                                                          np.isnan(M[i])))
+        exact += bool(same)
+    t_plain = time.perf_counter() - t0
+    cu = float((sides.astype(np.float64) ** 2).sum()) * ENS["steps"]
+    sample_cu = float((sides[sample].astype(np.float64) ** 2).sum()) * ENS["steps"]
+    plain_sims = len(sample) / t_plain
+    return {"workload": "4096 forest-fire instances, square Grid sides log-uniform 64..1024, p ~ U(0.01, 0.1), "
+                        "f ~ LogU(1e-5, 1e-3), seeds 1..4096, all empty at t = 0, 500 steps each",
+            "sims_per_s": n / t_batched, "s_per_run": t_batched, "gcell_updates_s": cu / t_batched / 1e9,
+            "plain_sims_per_s": plain_sims, "plain_sample": len(sample),
+            "plain_gcell_updates_s": sample_cu / t_plain / 1e9,
+            "speedup_vs_plain": (n / t_batched) / plain_sims,
+            "exact_matches_in_sample": exact, "launches_per_run": 1}
+
+
 def main():
     args = parse()
     if args.case:
@@ -401,6 +489,8 @@ def main():
     e2e = {"value": world * cell_updates() / (e2e_s / args.steps) / 1e9, "unit": "Gcell-updates/s",
            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3}
 
+    batched = bench_batched(capi, lib, max(1, args.warmup // 2), max(1, args.steps // 2)) if rank == 0 else None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(os.cpu_count() or 1)
@@ -417,7 +507,7 @@ def main():
                            "l2": "inputs larger than L2: the 16384^2 state is 268 MB, and each step re-copies "
                                  "335 MB of initial states"},
                 "roofline": roofline, "parts": parts, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clocks.summary(), "cpu_baseline": cpu}
+                "clocks": clocks.summary(), "cpu_baseline": cpu, "batched": batched}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

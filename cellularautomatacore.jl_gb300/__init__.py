@@ -4,7 +4,7 @@ The compute path is libgbca.so (hand-written sm_103a CUDA, C ABI in include/gbca
 this package is the host-side mirror of the reference's interface over it:
 model types (spaces, neighbourhoods, rules, schemes), the backend contract
 (GB300Backend and its functions) and the SciML-style problem / solve layer."""
-from . import backend, capi, ensemble, errors, model, problem
+from . import backend, capi, ensemble, errors, model, problem, serving
 from .backend import (GB300Backend, GB300State, advance, allocate_state, check_problem, current_state,
                       device_summaries, read_cell, set_state, supports, write_cell)
 from .errors import (ArgumentError, GPUError, IncompatibleSpaceError, InvalidStateError, RuleParseError,
@@ -15,6 +15,7 @@ from .model import (GENERATIONS_PRESETS, LIFE_PRESETS, Checkerboard, Constant, F
 from .problem import (CAProblem, CASolution, DiscreteCallback, EnsembleProblem, final_state, init, reinit, remake,
                       seed_trajectory, solve, solve_ensemble_serial, solve_integrator, step)
 
+from .serving import Server
 from .ensemble import ABCResult, BatchedEnsemble, EnsembleGB300, EnsembleResult, abc_rejection, solve_ensemble
 
 __version__ = "0.1.0"

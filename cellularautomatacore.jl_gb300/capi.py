@@ -34,6 +34,19 @@ class Desc(ctypes.Structure):
     ]
 
 
+class ServerConfig(ctypes.Structure):
+    """gbca_server_config."""
+    _fields_ = [("hbm_budget", ctypes.c_uint64), ("chunk_steps", ctypes.c_int32), ("big_cells", ctypes.c_int32),
+                ("max_big", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Result(ctypes.Structure):
+    """gbca_result."""
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("counts", ctypes.c_int64 * 8), ("other", ctypes.c_int64), ("morans", ctypes.c_double),
+                ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double)]
+
+
 # every symbol include/gbca.h declares, with (restype, argtypes)
 _P = ctypes.POINTER
 _V = ctypes.c_void_p
@@ -65,6 +78,12 @@ SIGNATURES = {
     "gbca_ensemble_sync": (ctypes.c_int, [_V]),
     "gbca_ensemble_summaries": (ctypes.c_int, [_V, _P(_I64), ctypes.c_int32, _P(_I64), _P(ctypes.c_double)]),
     "gbca_ensemble_get_state": (ctypes.c_int, [_V, ctypes.c_int32, _V, ctypes.c_size_t]),
+    "gbca_server_start": (ctypes.c_int, [_P(ServerConfig), _P(_V)]),
+    "gbca_server_submit": (ctypes.c_int, [_V, _P(Desc), _V, ctypes.c_size_t, ctypes.c_double, ctypes.c_uint64, _I64,
+                                          _I64, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_uint64)]),
+    "gbca_server_poll": (ctypes.c_int, [_V, _P(Result), ctypes.c_int32, _P(ctypes.c_int32)]),
+    "gbca_server_status": (ctypes.c_int, [_V, _P(_I64), _P(_I64), _P(ctypes.c_double)]),
+    "gbca_server_stop": (ctypes.c_int, [_V]),
     "gbca_advance_noalloc": (ctypes.c_int, [_P(Desc), _V, _I64, _I64, _I64, _P(ctypes.c_double), ctypes.c_int32, _V]),
 }
 

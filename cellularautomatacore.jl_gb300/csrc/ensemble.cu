@@ -256,12 +256,11 @@ __global__ void __launch_bounds__(kEnsThreads) k_ensemble(const EnsInstance* __r
             }
         }
         __syncthreads();
-        summarize(I, pool + I.off[cur], I.pitch, &out[i]);
+        if (I.summarize) summarize(I, pool + I.off[cur], I.pitch, &out[i]);
         if (threadIdx.x == 0) final_cur[i] = cur;
     }
 }
 
-thread_local std::string g_ens_err;
 
 int efail(int code, const char* fmt, ...) {
     char msg[512];
@@ -274,6 +273,25 @@ int efail(int code, const char* fmt, ...) {
 }
 
 }  // namespace
+
+cudaError_t launch_ensemble(const EnsInstance* d_inst, const int* d_order, int n, int* d_counter, int8_t* pool,
+                            EnsSummary* d_out, int* d_cur, int grid, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    k_ensemble<<<grid, kEnsThreads, 0, st>>>(d_inst, d_order, n, d_counter, pool, d_out, d_cur);
+    count_launch();
+    return cudaGetLastError();
+}
+
+int ensemble_grid() {
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ensemble, kEnsThreads, 0);
+    return nsm * (per > 0 ? per : 1);
+}
+
+int ensemble_smem_cells() { return kEnsBuf; }
 
 }  // namespace gbca
 
@@ -338,6 +356,7 @@ int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out)
         I.cval0 = d.boundary[0] == GBCA_CONSTANT ? (int32_t)d.constant[0] : 0;
         I.cval1 = d.boundary[1] == GBCA_CONSTANT ? (int32_t)d.constant[1] : 0;
         I.small = (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= kEnsBuf;
+        I.summarize = 1;
     }
     if (gbca_device_count() < 1) return efail(GBCA_ERR_CUDA, "no CUDA device is visible");
     gbca_ensemble* e = new gbca_ensemble();

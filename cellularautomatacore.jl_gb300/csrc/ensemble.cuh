@@ -1,6 +1,7 @@
 // ensemble.cuh — device descriptors and results of the batched ensemble engine.
 #pragma once
 #include <cstdint>
+#include <cuda_runtime.h>
 
 namespace gbca {
 
@@ -17,11 +18,19 @@ struct EnsInstance {
     int32_t params_f32, bnd0, bnd1, cval0, cval1;
     int32_t cur;             // buffer holding the current state
     int32_t small;           // fits in shared memory with its halo
-    int32_t pad;
+    int32_t summarize;       // reduce the final state to its summaries at the end of the run
 };
 
 struct EnsSummary {
     long long w[kEnsSumWords];
 };
+
+// One persistent launch over n instances (order: the queue order); resets the counter first.
+cudaError_t launch_ensemble(const EnsInstance* d_inst, const int* d_order, int n, int* d_counter, int8_t* pool,
+                            EnsSummary* d_out, int* d_cur, int grid, cudaStream_t st);
+// Grid size that fills the current device with resident CTAs.
+int ensemble_grid();
+// Instances with (n1 + 2r)(n2 + 2r) <= this many cells run in shared memory.
+int ensemble_smem_cells();
 
 }  // namespace gbca

@@ -116,73 +116,12 @@ uint64_t threshold(double p, bool f32) {
     return (uint64_t)std::ceil(p * 9007199254740992.0);
 }
 
-gbca::SweepParams base_params(const gbca_handle* h) {
-    const gbca_desc& d = h->d;
-    gbca::SweepParams p;
-    std::memset(&p, 0, sizeof p);
-    p.n1 = d.n1;
-    p.n2 = d.n2;
-    p.pitch = h->pitch;
-    for (int a = 0; a < 2; ++a) {
-        p.bnd[a] = d.boundary[a];
-        p.cval[a] = d.boundary[a] == GBCA_CONSTANT ? (int32_t)d.constant[a] : 0;
-    }
-    p.rule = d.rule;
-    p.nbhd = d.nbhd;
-    p.radius = d.radius;
-    p.states = d.states;
-    p.birth = d.birth;
-    p.survive = d.survive;
-    p.seed = d.seed;
-    p.scheme = d.scheme;
-    p.gate_f32 = d.scheme_p_f32;
-    p.gate_thr = d.scheme == GBCA_STOCHASTIC ? threshold(d.scheme_p, d.scheme_p_f32 != 0) : 0;
-    p.params_f32 = d.params_f32;
-    p.ngates = d.scheme == GBCA_CHECKERBOARD ? 2 : 1;
-    return p;
-}
-
 int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams) {
-    gbca::SweepParams p = base_params(h);
-    if (h->d.rule == GBCA_RULE_FOREST_FIRE) {
-        if (!params || nparams < 2)
-            return fail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
-        p.thr_p = threshold(params[0], h->d.params_f32 != 0);
-        p.thr_f = threshold(params[1], h->d.params_f32 != 0);
-    }
-    const bool fire = gbca::fire_fast_supported(p);
-    const bool life = !fire && gbca::life_simd_supported(p);
-    while (nsteps > 0) {
-        int64_t k;
-        cudaError_t e;
-        const int8_t* src = (const int8_t*)h->buf[h->cur];
-        int8_t* dst = (int8_t*)h->buf[h->cur ^ 1];
-        p.t0 = t;
-        if (fire) {
-            k = nsteps < 8 ? nsteps : 8;
-            p.nsub = (int32_t)k;
-            e = gbca::launch_fire(p, src, dst, h->stream);
-        } else if (life) {
-            const int64_t per = gbca::life_steps_per_pass(p);
-            k = nsteps < per ? nsteps : per;
-            p.nsub = (int32_t)k;
-            e = gbca::launch_life_simd(p, src, dst, h->stream);
-        } else {
-            const int r = p.radius;
-            int64_t per = 32 / (r * p.ngates);
-            if (per < 1) per = 1;
-            k = nsteps < per ? nsteps : per;
-            p.nsub = (int32_t)(k * p.ngates);
-            p.tile_x = p.tile_y = 64;
-            p.halo_x = p.halo_y = p.nsub * r;
-            e = gbca::launch_generic(p, src, dst, h->stream);
-        }
-        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
-        gbca::count_launch();
-        h->cur ^= 1;
-        t += k;
-        nsteps -= k;
-    }
+    if (h->d.rule == GBCA_RULE_FOREST_FIRE && (!params || nparams < 2))
+        return fail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
+    int8_t* const bufs[2] = {(int8_t*)h->buf[0], (int8_t*)h->buf[1]};
+    const cudaError_t e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, t, nsteps, params, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
     return GBCA_OK;
 }
 

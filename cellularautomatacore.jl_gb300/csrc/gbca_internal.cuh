@@ -168,6 +168,12 @@ void set_last_error(const char* msg);
 void count_launch(int64_t n = 1);
 int64_t launches_so_far();
 
+// Kernel selection and temporally blocked passes for an Int8 problem (sweep_dispatch.cu):
+// nsteps steps between bufs[*cur] and bufs[*cur ^ 1], *cur updated.
+SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params);
+cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
+                       const double* params, cudaStream_t st);
+
 // Launchers (one translation unit each).
 cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 bool life_simd_supported(const SweepParams& p);

@@ -1,0 +1,542 @@
+// server.cu — a device-resident request loop with continuous batching.
+//
+// Clients submit simulation requests (an Int8 problem, its initial state, a step count and
+// parameters) at any time; a scheduler thread owns the GPU and returns each request's
+// summary statistics (state counts and Moran's I, src/measures.jl) as soon as it finishes.
+//
+//  * Admission by HBM budget: request states live in one device arena of a fixed size; a
+//    request is admitted, in arrival order, when its two buffers fit, and its memory is
+//    released the moment it finishes. A request larger than the whole arena is refused.
+//  * Continuous batching: the scheduler works in iterations. In each one every admitted
+//    request advances by up to `chunk_steps` steps: all small requests together in one
+//    persistent ensemble launch (ensemble.cu; one CTA per request), the large ones as
+//    temporally blocked multi-CTA sweeps on their own streams, concurrently with it.
+//    Requests that arrive while an iteration runs join at the next one; finished requests
+//    leave and free their memory for the queue.
+//  * Results are exact: a request's steps, draws and summaries are those it would get alone
+//    (the draws depend only on its seed, cell and time).
+// The scheduler never waits on the device inside a kernel: each iteration ends with a
+// stream synchronisation on the host, so there is no device-side spin to bound.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ensemble.cuh"
+#include "gbca_internal.cuh"
+#include "measures.cuh"
+
+namespace gbca {
+
+namespace {
+
+// Bernoulli(density) soup of 0/1 from a seed: draw (seed; cell id, 0, 0xFFFFFFFF, 0xFFFFFFFE),
+// a counter the rules never use. A synthetic-input generator for requests without a state.
+__global__ void k_soup(int8_t* __restrict__ buf, int64_t n1, int64_t n2, int64_t pitch, uint64_t seed, uint32_t thr24) {
+    const int64_t n = n1 * n2;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint2 w = cell_draw(seed, (uint64_t)q + 1u, (int64_t)0xFFFFFFFFu, 0xFFFFFFFEu);
+        buf[(q % n1) + (q / n1) * pitch] = (int8_t)((w.x >> 8) < thr24 ? 1 : 0);
+    }
+}
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// First-fit allocator over a device arena (offsets only; the host owns the books).
+class Arena {
+  public:
+    explicit Arena(size_t cap = 0) { reset(cap); }
+    void reset(size_t cap) {
+        free_.clear();
+        cap_ = cap;
+        if (cap) free_[0] = cap;
+    }
+    bool alloc(size_t n, size_t* off) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= n) {
+                *off = it->first;
+                const size_t rest = it->second - n, at = it->first + n;
+                free_.erase(it);
+                if (rest) free_[at] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t n) {
+        auto it = free_.emplace(off, n).first;
+        auto next = std::next(it);
+        if (next != free_.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_.erase(next);
+        }
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    size_t capacity() const { return cap_; }
+
+  private:
+    std::map<size_t, size_t> free_;
+    size_t cap_ = 0;
+};
+
+struct Request {
+    uint64_t id = 0;
+    gbca_desc d;
+    std::vector<int8_t> u0;  // empty: zeros or a soup
+    double density = 0.0;
+    uint64_t init_seed = 0;
+    int64_t t0 = 0, nsteps = 0, done = 0;
+    double params[2] = {0.0, 0.0};
+    size_t off = 0, bytes = 0;
+    int64_t pitch = 0;
+    int cur = 0;
+    bool big = false;
+    double t_submit = 0.0, t_admit = 0.0;
+};
+
+int sfail(int code, const char* fmt, ...) {
+    char msg[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof msg, fmt, ap);
+    va_end(ap);
+    set_last_error(msg);
+    return code;
+}
+
+}  // namespace
+
+}  // namespace gbca
+
+using namespace gbca;
+
+struct gbca_server {
+    gbca_server_config cfg;
+    int device = 0;
+    int8_t* arena_base = nullptr;
+    Arena arena;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Request*> inbox;
+    std::deque<gbca_result> outbox;
+    std::thread th;
+    bool stopping = false;
+    bool dead = false;
+    uint64_t next_id = 1;
+    std::chrono::steady_clock::time_point t_start;
+    int64_t queued = 0, active_n = 0;
+    // scheduler-owned device resources
+    cudaStream_t s_small = nullptr;
+    std::vector<cudaStream_t> s_big;
+    EnsInstance* d_inst = nullptr;
+    int* d_order = nullptr;
+    int* d_counter = nullptr;
+    EnsSummary* d_out = nullptr;
+    int* d_cur = nullptr;
+    EnsSummary* h_out = nullptr;
+    int* h_cur = nullptr;
+    int cap_small = 0;
+    unsigned long long* d_acc = nullptr;
+    unsigned long long* h_acc = nullptr;
+    int grid = 0;
+
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    }
+};
+
+namespace {
+
+gbca_result make_result(const Request* r, int status, double t_done) {
+    gbca_result res;
+    std::memset(&res, 0, sizeof res);
+    res.id = r->id;
+    res.status = status;
+    res.morans = __builtin_nan("");
+    res.t_submit = r->t_submit;
+    res.t_admit = r->t_admit;
+    res.t_done = t_done;
+    return res;
+}
+
+bool grow_small(gbca_server* S, int need) {
+    if (need <= S->cap_small) return true;
+    int cap = std::max(need, 2 * S->cap_small + 64);
+    cudaFree(S->d_inst);
+    cudaFree(S->d_order);
+    cudaFree(S->d_out);
+    cudaFree(S->d_cur);
+    if (S->h_out) cudaFreeHost(S->h_out);
+    if (S->h_cur) cudaFreeHost(S->h_cur);
+    S->d_inst = nullptr;
+    S->d_order = S->d_cur = nullptr;
+    S->d_out = S->h_out = nullptr;
+    S->h_cur = nullptr;
+    cudaError_t e = cudaMalloc(&S->d_inst, sizeof(EnsInstance) * cap);
+    if (e == cudaSuccess) e = cudaMalloc(&S->d_order, sizeof(int) * cap);
+    if (e == cudaSuccess) e = cudaMalloc(&S->d_out, sizeof(EnsSummary) * cap);
+    if (e == cudaSuccess) e = cudaMalloc(&S->d_cur, sizeof(int) * cap);
+    if (e == cudaSuccess) e = cudaMallocHost(&S->h_out, sizeof(EnsSummary) * cap);
+    if (e == cudaSuccess) e = cudaMallocHost(&S->h_cur, sizeof(int) * cap);
+    if (e != cudaSuccess) return false;
+    S->cap_small = cap;
+    return true;
+}
+
+EnsInstance small_instance(const Request* r, int64_t steps, bool last) {
+    EnsInstance I;
+    std::memset(&I, 0, sizeof I);
+    const gbca_desc& d = r->d;
+    I.n1 = d.n1;
+    I.n2 = d.n2;
+    I.pitch = r->pitch;
+    I.off[0] = (int64_t)r->off;
+    I.off[1] = (int64_t)(r->off + r->bytes / 2);
+    I.t0 = r->t0 + r->done;
+    I.nsteps = steps;
+    I.birth = d.birth;
+    I.survive = d.survive;
+    I.seed = d.seed;
+    if (d.rule == GBCA_RULE_FOREST_FIRE) {
+        I.thr_p = gbca_threshold(r->params[0], d.params_f32);
+        I.thr_f = gbca_threshold(r->params[1], d.params_f32);
+    }
+    I.rule = d.rule;
+    I.nbhd = d.nbhd;
+    I.radius = d.radius;
+    I.states = d.states;
+    I.params_f32 = d.params_f32;
+    I.bnd0 = d.boundary[0];
+    I.bnd1 = d.boundary[1];
+    I.cval0 = d.boundary[0] == GBCA_CONSTANT ? (int32_t)d.constant[0] : 0;
+    I.cval1 = d.boundary[1] == GBCA_CONSTANT ? (int32_t)d.constant[1] : 0;
+    I.cur = r->cur;
+    I.small = (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= ensemble_smem_cells();
+    I.summarize = last ? 1 : 0;
+    return I;
+}
+
+// Admit pending requests in arrival order while the arena has room.
+cudaError_t admit(gbca_server* S, std::deque<Request*>& pending, std::vector<Request*>& active,
+                  std::vector<gbca_result>& done) {
+    while (!pending.empty()) {
+        Request* r = pending.front();
+        const gbca_desc& d = r->d;
+        r->big = d.n1 * d.n2 > (int64_t)S->cfg.big_cells;
+        r->pitch = r->big ? (d.n1 + 127) / 128 * 128 : d.n1;
+        const size_t one = align256((size_t)(r->pitch * d.n2));
+        r->bytes = 2 * one;
+        if (r->bytes > S->arena.capacity()) {
+            done.push_back(make_result(r, GBCA_ERR_OUT_OF_MEMORY, S->now()));
+            pending.pop_front();
+            delete r;
+            continue;
+        }
+        if (!S->arena.alloc(r->bytes, &r->off)) break;
+        int8_t* buf = S->arena_base + r->off;
+        cudaError_t e;
+        if (!r->u0.empty()) {
+            e = cudaMemcpy2DAsync(buf, (size_t)r->pitch, r->u0.data(), (size_t)d.n1, (size_t)d.n1, (size_t)d.n2,
+                                  cudaMemcpyHostToDevice, S->s_small);
+            std::vector<int8_t>().swap(r->u0);
+        } else if (r->density > 0.0) {
+            const uint32_t thr = (uint32_t)gbca_threshold(r->density, 1);
+            k_soup<<<S->grid, 256, 0, S->s_small>>>(buf, d.n1, d.n2, r->pitch, r->init_seed, thr);
+            count_launch();
+            e = cudaGetLastError();
+        } else {
+            e = cudaMemsetAsync(buf, 0, one, S->s_small);
+        }
+        if (e != cudaSuccess) return e;
+        r->cur = 0;
+        r->done = 0;
+        r->t_admit = S->now();
+        active.push_back(r);
+        pending.pop_front();
+    }
+    return cudaSuccess;
+}
+
+void scheduler(gbca_server* S) {
+    cudaSetDevice(S->device);
+    std::deque<Request*> pending;
+    std::vector<Request*> active;
+    std::vector<gbca_result> done;
+    const int nbig = (int)S->s_big.size();
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lock(S->mu);
+            while (S->inbox.empty() && pending.empty() && active.empty() && !S->stopping)
+                S->cv.wait_for(lock, std::chrono::milliseconds(50));
+            while (!S->inbox.empty()) {
+                pending.push_back(S->inbox.front());
+                S->inbox.pop_front();
+            }
+            if (S->stopping && pending.empty() && active.empty()) break;
+        }
+        cudaError_t e = admit(S, pending, active, done);
+        // one iteration: every small request in one ensemble launch, large ones on their streams
+        std::vector<Request*> smalls, bigs;
+        for (Request* r : active) (r->big ? bigs : smalls).push_back(r);
+        if (bigs.size() > (size_t)nbig) bigs.resize((size_t)nbig);  // the rest wait for a stream
+        std::vector<int64_t> step_small(smalls.size()), step_big(bigs.size());
+        if (e == cudaSuccess && !smalls.empty()) {
+            if (!grow_small(S, (int)smalls.size())) e = cudaErrorMemoryAllocation;
+            std::vector<EnsInstance> inst(smalls.size());
+            std::vector<int64_t> work(smalls.size());
+            for (size_t j = 0; j < smalls.size() && e == cudaSuccess; ++j) {
+                Request* r = smalls[j];
+                const int64_t rem = r->nsteps - r->done;
+                step_small[j] = rem < S->cfg.chunk_steps ? rem : S->cfg.chunk_steps;
+                inst[j] = small_instance(r, step_small[j], step_small[j] == rem);
+                work[j] = r->d.n1 * r->d.n2 * step_small[j];
+            }
+            std::vector<int> order(smalls.size());
+            std::iota(order.begin(), order.end(), 0);
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(S->d_inst, inst.data(), sizeof(EnsInstance) * inst.size(), cudaMemcpyHostToDevice,
+                                    S->s_small);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(S->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice,
+                                    S->s_small);
+            if (e == cudaSuccess)
+                e = launch_ensemble(S->d_inst, S->d_order, (int)inst.size(), S->d_counter, S->arena_base, S->d_out,
+                                    S->d_cur, S->grid, S->s_small);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(S->h_out, S->d_out, sizeof(EnsSummary) * inst.size(), cudaMemcpyDeviceToHost,
+                                    S->s_small);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(S->h_cur, S->d_cur, sizeof(int) * inst.size(), cudaMemcpyDeviceToHost, S->s_small);
+        }
+        for (size_t j = 0; j < bigs.size() && e == cudaSuccess; ++j) {
+            Request* r = bigs[j];
+            const int64_t rem = r->nsteps - r->done;
+            step_big[j] = rem < S->cfg.chunk_steps ? rem : S->cfg.chunk_steps;
+            int8_t* const bufs[2] = {S->arena_base + r->off, S->arena_base + r->off + r->bytes / 2};
+            e = sweep_int8(r->d, r->pitch, bufs, &r->cur, r->t0 + r->done, step_big[j], r->params, S->s_big[j]);
+            if (e == cudaSuccess && step_big[j] == rem) {
+                unsigned long long* acc = S->d_acc + (size_t)j * kMeasureWords;
+                e = launch_measures(bufs[r->cur], r->d.n1, r->d.n2, r->pitch, r->d.boundary[0], r->d.boundary[1], acc,
+                                    S->grid / 4 > 0 ? S->grid / 4 : 1, S->s_big[j]);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(S->h_acc + (size_t)j * kMeasureWords, acc,
+                                        kMeasureWords * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                        S->s_big[j]);
+            }
+        }
+        if (e == cudaSuccess && !smalls.empty()) e = cudaStreamSynchronize(S->s_small);
+        for (size_t j = 0; j < bigs.size() && e == cudaSuccess; ++j) e = cudaStreamSynchronize(S->s_big[j]);
+        const double t = S->now();
+        std::vector<Request*> finished;
+        if (e != cudaSuccess) {
+            // the device failed: every admitted and queued request fails with it
+            for (Request* r : active) done.push_back(make_result(r, GBCA_ERR_CUDA, t));
+            for (Request* r : pending) done.push_back(make_result(r, GBCA_ERR_CUDA, t));
+            for (Request* r : active) delete r;
+            for (Request* r : pending) delete r;
+            active.clear();
+            pending.clear();
+            std::lock_guard<std::mutex> lock(S->mu);
+            S->dead = true;
+            for (auto& res : done) S->outbox.push_back(res);
+            done.clear();
+            S->stopping = true;
+            continue;
+        }
+        for (size_t j = 0; j < smalls.size(); ++j) {
+            Request* r = smalls[j];
+            r->cur = S->h_cur[j];
+            r->done += step_small[j];
+            if (r->done >= r->nsteps) {
+                gbca_result res = make_result(r, GBCA_OK, t);
+                const long long* w = S->h_out[j].w;
+                const int64_t ncell = r->d.n1 * r->d.n2;
+                int64_t inrange = 0;
+                for (int v = 0; v < kEnsCounts; ++v) {
+                    res.counts[v] = w[v];
+                    inrange += w[v];
+                }
+                res.other = ncell - inrange;
+                res.morans = morans_from_sums(w[kEnsCounts + 1], w[kEnsCounts + 2], w[kEnsCounts + 3],
+                                              w[kEnsCounts + 4], w[kEnsCounts + 5], ncell);
+                done.push_back(res);
+                finished.push_back(r);
+            }
+        }
+        for (size_t j = 0; j < bigs.size(); ++j) {
+            Request* r = bigs[j];
+            r->done += step_big[j];
+            if (r->done >= r->nsteps) {
+                gbca_result res = make_result(r, GBCA_OK, t);
+                finish_measures(S->h_acc + (size_t)j * kMeasureWords, r->d.n1 * r->d.n2, res.counts, kEnsCounts,
+                                &res.other, &res.morans);
+                done.push_back(res);
+                finished.push_back(r);
+            }
+        }
+        for (Request* r : finished) {
+            S->arena.release(r->off, r->bytes);
+            active.erase(std::find(active.begin(), active.end(), r));
+            delete r;
+        }
+        std::lock_guard<std::mutex> lock(S->mu);
+        for (auto& res : done) S->outbox.push_back(res);
+        done.clear();
+        S->queued = (int64_t)(pending.size() + S->inbox.size());
+        S->active_n = (int64_t)active.size();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbca_server_start(const gbca_server_config* cfg, gbca_server** out) {
+    if (!cfg || !out) return sfail(GBCA_ERR_ARGUMENT, "null configuration or output");
+    *out = nullptr;
+    if (cfg->hbm_budget < 4096 || cfg->chunk_steps < 1 || cfg->max_big < 1 || cfg->max_big > 64 ||
+        cfg->big_cells < 0)
+        return sfail(GBCA_ERR_ARGUMENT, "server configuration out of range");
+    if (gbca_device_count() < 1) return sfail(GBCA_ERR_CUDA, "no CUDA device is visible");
+    gbca_server* S = new gbca_server();
+    S->cfg = *cfg;
+    S->t_start = std::chrono::steady_clock::now();
+    cudaGetDevice(&S->device);
+    cudaError_t e = cudaMalloc(&S->arena_base, (size_t)cfg->hbm_budget);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->s_small, cudaStreamNonBlocking);
+    S->s_big.assign((size_t)cfg->max_big, nullptr);
+    for (auto& st : S->s_big)
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&S->d_counter, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&S->d_acc, sizeof(unsigned long long) * kMeasureWords * cfg->max_big);
+    if (e == cudaSuccess) e = cudaMallocHost(&S->h_acc, sizeof(unsigned long long) * kMeasureWords * cfg->max_big);
+    if (e != cudaSuccess) {
+        const bool oom = e == cudaErrorMemoryAllocation;
+        cudaGetLastError();
+        cudaFree(S->arena_base);
+        cudaFree(S->d_counter);
+        cudaFree(S->d_acc);
+        if (S->h_acc) cudaFreeHost(S->h_acc);
+        if (S->s_small) cudaStreamDestroy(S->s_small);
+        for (auto st : S->s_big)
+            if (st) cudaStreamDestroy(st);
+        delete S;
+        return oom ? sfail(GBCA_ERR_OUT_OF_MEMORY, "the server's HBM budget of %llu bytes cannot be allocated",
+                           (unsigned long long)cfg->hbm_budget)
+                   : sfail(GBCA_ERR_CUDA, "server start: %s", cudaGetErrorString(e));
+    }
+    S->arena.reset((size_t)cfg->hbm_budget);
+    S->grid = ensemble_grid();
+    S->th = std::thread(scheduler, S);
+    *out = S;
+    return GBCA_OK;
+}
+
+int gbca_server_submit(gbca_server* S, const gbca_desc* d, const void* u0, size_t nbytes, double init_density,
+                       uint64_t init_seed, int64_t t0, int64_t nsteps, const double* params, int32_t nparams,
+                       uint64_t* id) {
+    if (!S || !d) return sfail(GBCA_ERR_ARGUMENT, "null server or problem");
+    const int rc = gbca_check(d);
+    if (rc != GBCA_OK) return rc;
+    if (d->rule == GBCA_RULE_LENIA || d->scheme != GBCA_SYNCHRONOUS || d->radius > 8)
+        return sfail(GBCA_ERR_UNSUPPORTED, "the server runs Int8 rules, Synchronous(), radius <= 8");
+    if (nsteps < 0) return sfail(GBCA_ERR_ARGUMENT, "negative step count");
+    if (d->rule == GBCA_RULE_FOREST_FIRE && (!params || nparams < 2))
+        return sfail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
+    if (u0 && nbytes != (size_t)(d->n1 * d->n2))
+        return sfail(GBCA_ERR_STATE, "the state has %zu bytes, the lattice %lld cells", nbytes,
+                     (long long)(d->n1 * d->n2));
+    if (!(init_density >= 0.0 && init_density <= 1.0))
+        return sfail(GBCA_ERR_ARGUMENT, "initial density must be in [0, 1]");
+    Request* r = new Request();
+    r->d = *d;
+    if (u0) r->u0.assign((const int8_t*)u0, (const int8_t*)u0 + nbytes);
+    r->density = init_density;
+    r->init_seed = init_seed;
+    r->t0 = t0;
+    r->nsteps = nsteps;
+    if (params && nparams >= 2) {
+        r->params[0] = params[0];
+        r->params[1] = params[1];
+    }
+    {
+        std::lock_guard<std::mutex> lock(S->mu);
+        if (S->stopping) {
+            delete r;
+            return sfail(GBCA_ERR_BUSY, "the server is stopping");
+        }
+        r->id = S->next_id++;
+        r->t_submit = S->now();
+        S->inbox.push_back(r);
+        ++S->queued;
+    }
+    S->cv.notify_one();
+    if (id) *id = r->id;
+    return GBCA_OK;
+}
+
+int gbca_server_poll(gbca_server* S, gbca_result* out, int32_t max, int32_t* n) {
+    if (!S || !n || (max > 0 && !out)) return sfail(GBCA_ERR_ARGUMENT, "null server or output");
+    std::lock_guard<std::mutex> lock(S->mu);
+    int32_t k = 0;
+    while (k < max && !S->outbox.empty()) {
+        out[k++] = S->outbox.front();
+        S->outbox.pop_front();
+    }
+    *n = k;
+    return GBCA_OK;
+}
+
+int gbca_server_status(gbca_server* S, int64_t* queued, int64_t* active, double* clock) {
+    if (!S) return sfail(GBCA_ERR_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lock(S->mu);
+    if (queued) *queued = S->queued;
+    if (active) *active = S->active_n;
+    if (clock) *clock = S->now();
+    return S->dead ? sfail(GBCA_ERR_CUDA, "the server stopped after a device failure") : GBCA_OK;
+}
+
+int gbca_server_stop(gbca_server* S) {
+    if (!S) return GBCA_OK;
+    {
+        std::lock_guard<std::mutex> lock(S->mu);
+        S->stopping = true;
+    }
+    S->cv.notify_all();
+    if (S->th.joinable()) S->th.join();
+    for (Request* r : S->inbox) delete r;
+    cudaFree(S->arena_base);
+    cudaFree(S->d_inst);
+    cudaFree(S->d_order);
+    cudaFree(S->d_counter);
+    cudaFree(S->d_out);
+    cudaFree(S->d_cur);
+    cudaFree(S->d_acc);
+    if (S->h_out) cudaFreeHost(S->h_out);
+    if (S->h_cur) cudaFreeHost(S->h_cur);
+    if (S->h_acc) cudaFreeHost(S->h_acc);
+    if (S->s_small) cudaStreamDestroy(S->s_small);
+    for (auto st : S->s_big)
+        if (st) cudaStreamDestroy(st);
+    delete S;
+    return GBCA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+// sweep_dispatch.cu — picks the sweep kernel for an Int8 problem and runs nsteps steps as
+// temporally blocked passes: the forest-fire kernel (VonNeumann(1), Synchronous), the
+// bit-sliced Life-like kernel (Moore(r <= 5), Synchronous), else the general kernel.
+#include <cstring>
+
+#include "gbca_internal.cuh"
+
+namespace gbca {
+
+SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params) {
+    SweepParams p;
+    std::memset(&p, 0, sizeof p);
+    p.n1 = d.n1;
+    p.n2 = d.n2;
+    p.pitch = pitch;
+    for (int a = 0; a < 2; ++a) {
+        p.bnd[a] = d.boundary[a];
+        p.cval[a] = d.boundary[a] == GBCA_CONSTANT ? (int32_t)d.constant[a] : 0;
+    }
+    p.rule = d.rule;
+    p.nbhd = d.nbhd;
+    p.radius = d.radius;
+    p.states = d.states;
+    p.birth = d.birth;
+    p.survive = d.survive;
+    p.seed = d.seed;
+    p.scheme = d.scheme;
+    p.gate_f32 = d.scheme_p_f32;
+    p.gate_thr = d.scheme == GBCA_STOCHASTIC ? gbca_threshold(d.scheme_p, d.scheme_p_f32) : 0;
+    p.params_f32 = d.params_f32;
+    p.ngates = d.scheme == GBCA_CHECKERBOARD ? 2 : 1;
+    if (d.rule == GBCA_RULE_FOREST_FIRE && params) {
+        p.thr_p = gbca_threshold(params[0], d.params_f32);
+        p.thr_f = gbca_threshold(params[1], d.params_f32);
+    }
+    return p;
+}
+
+cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
+                       const double* params, cudaStream_t st) {
+    SweepParams p = sweep_params(d, pitch, params);
+    const bool fire = fire_fast_supported(p);
+    const bool life = !fire && life_simd_supported(p);
+    while (nsteps > 0) {
+        int64_t k;
+        cudaError_t e;
+        const int8_t* src = bufs[*cur];
+        int8_t* dst = bufs[*cur ^ 1];
+        p.t0 = t;
+        if (fire) {
+            k = nsteps < 8 ? nsteps : 8;
+            p.nsub = (int32_t)k;
+            e = launch_fire(p, src, dst, st);
+        } else if (life) {
+            const int64_t per = life_steps_per_pass(p);
+            k = nsteps < per ? nsteps : per;
+            p.nsub = (int32_t)k;
+            e = launch_life_simd(p, src, dst, st);
+        } else {
+            int64_t per = 32 / (p.radius * p.ngates);
+            if (per < 1) per = 1;
+            k = nsteps < per ? nsteps : per;
+            p.nsub = (int32_t)(k * p.ngates);
+            p.tile_x = p.tile_y = 64;
+            p.halo_x = p.halo_y = p.nsub * p.radius;
+            e = launch_generic(p, src, dst, st);
+        }
+        if (e != cudaSuccess) return e;
+        count_launch();
+        *cur ^= 1;
+        t += k;
+        nsteps -= k;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace gbca

@@ -173,6 +173,53 @@ int gbca_ensemble_summaries(gbca_ensemble* e, int64_t* counts, int32_t nvals, in
 /* current_state of instance i. */
 int gbca_ensemble_get_state(gbca_ensemble* e, int32_t i, void* host, size_t nbytes);
 
+/* ---- serving: a device-resident request loop with continuous batching. Clients submit
+ * simulation requests at any time; a scheduler thread admits them in arrival order while
+ * their state buffers fit the HBM budget, advances every admitted request by up to
+ * chunk_steps steps per iteration (small requests together in one persistent launch, large
+ * ones as multi-CTA sweeps on their own streams), and returns each request's state counts and
+ * Moran's I as soon as it finishes. A request's result does not depend on what else runs.
+ * No counterpart in the reference (its unit of work is one solve at a time). */
+typedef struct gbca_server gbca_server;
+
+typedef struct gbca_server_config {
+    uint64_t hbm_budget;   /* bytes of device memory for request states (two buffers each) */
+    int32_t chunk_steps;   /* steps per request per iteration */
+    int32_t big_cells;     /* requests above this many cells run as their own multi-CTA sweeps */
+    int32_t max_big;       /* large requests advanced concurrently (one stream each), 1..64 */
+    int32_t reserved;
+} gbca_server_config;
+
+typedef struct gbca_result {
+    uint64_t id;
+    int32_t status;        /* GBCA_OK, or GBCA_ERR_OUT_OF_MEMORY for a request larger than the budget */
+    int32_t reserved;
+    int64_t counts[8];     /* cells holding 0..7 */
+    int64_t other;         /* cells holding any other value */
+    double morans;         /* Moran's I, VonNeumann(1) on the request's lattice; NaN if constant */
+    double t_submit, t_admit, t_done;  /* seconds on the server's clock */
+} gbca_result;
+
+int gbca_server_start(const gbca_server_config* cfg, gbca_server** out);
+
+/* Queue a request: an Int8 problem (Synchronous, radius <= 8), its initial state (u0: n1*n2
+ * bytes, column-major; or NULL for a Bernoulli(init_density) soup of 0/1 drawn from
+ * init_seed on the device, all zeros for density 0), nsteps steps from time t0, parameters
+ * (forest fire: p, f). Returns at once with the request's id. */
+int gbca_server_submit(gbca_server* s, const gbca_desc* d, const void* u0, size_t nbytes, double init_density,
+                       uint64_t init_seed, int64_t t0, int64_t nsteps, const double* params, int32_t nparams,
+                       uint64_t* id);
+
+/* Up to `max` finished requests' results, oldest first; *n gets how many. Never blocks. */
+int gbca_server_poll(gbca_server* s, gbca_result* out, int32_t max, int32_t* n);
+
+/* Requests waiting for admission, requests admitted, and the server's clock (seconds). */
+int gbca_server_status(gbca_server* s, int64_t* queued, int64_t* active, double* clock);
+
+/* Stop accepting requests, finish every queued and admitted one, free everything.
+ * Results not yet polled are lost. */
+int gbca_server_stop(gbca_server* s);
+
 /* Size of the device scratch array behind gbca_advance_noalloc: the largest state, in bytes
  * (pitch * n2), that it accepts. Every GPU that loads the library holds this array until
  * the process exits. */
