@@ -49,9 +49,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
     ap.add_argument("--case", choices=["ltl", "fire", "lenia", "lenia-fft"], default=None,
                     help="time single passes of one kernel on an n x n lattice (for profiling)")
     ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--no-tune", action="store_true", help="keep the kernels' default sweep geometry")
     return ap.parse_args()
 
 
@@ -244,6 +246,10 @@ def run_case(args):
     stream = torch.cuda.Stream()
     capi.check(lib.gbca_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
     nparams = 2 if params is not None else 0
+    geometry = None
+    if args.case in ("ltl", "fire") and not args.no_tune:
+        geometry = tune(capi, lib, h, params, nparams)
+        per = geometry[0] or per
     t = 0
     for _ in range(args.warmup):
         capi.check(lib.gbca_advance(h, t, per, params, nparams))
@@ -258,7 +264,7 @@ def run_case(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     cu = n * n * per
-    out = {"case": args.case, "n": n, "steps_per_pass": per, "ms_per_pass": ms,
+    out = {"case": args.case, "n": n, "steps_per_pass": per, "geometry": geometry, "ms_per_pass": ms,
            "gcell_updates_s": cu / (ms * 1e-3) / 1e9}
     if args.case in ("ltl", "fire"):
         out["hbm_frac_per_effective_step"] = BYTES_PER_CELL_UPDATE * cu / (ms * 1e-3) / 1e9 / measured_peaks()[0]
@@ -269,6 +275,13 @@ def run_case(args):
 
 
 ENS = dict(n=4096, steps=500, plain_sample=256)
+
+
+def tune(capi, lib, h, params, nparams):
+    """The autotuner's (steps per pass, tile rows) for the handle's shape, timed on its state."""
+    k, rows = ctypes.c_int32(), ctypes.c_int32()
+    capi.check(lib.gbca_tune(h, params, nparams, ctypes.byref(k), ctypes.byref(rows)))
+    return int(k.value), int(rows.value)
 
 
 def ensemble_instances():
@@ -356,6 +369,138 @@ def bench_batched(capi, lib, warmup: int, steps: int):
             "exact_matches_in_sample": exact, "launches_per_run": 1}
 
 
+SERVE = dict(rate=2000.0, seconds=2.0, plain_sample=48, hbm_budget=8 << 30, chunk_steps=100,
+             big_cells=1 << 16, max_big=16)
+
+
+def serve_requests(n: int, seed: int = 2000):
+    """n requests of the served stream: Poisson arrivals at SERVE['rate'] per second; rule
+    uniform over {Life B3/S23, Generations B2/S/C3, forest fire with p ~ U(0.01, 0.1),
+    f ~ LogU(1e-5, 1e-3)}; square side log-uniform in 64..4096; steps uniform in 50..1000;
+    independent seeds. Life and Generations start from a density-0.5 soup, the fire empty."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    arrivals = np.cumsum(rng.exponential(1.0 / SERVE["rate"], n))
+    kinds = rng.integers(0, 3, n)
+    sides = np.round(np.exp(rng.uniform(np.log(64), np.log(4096), n))).astype(np.int64)
+    steps = rng.integers(50, 1001, n)
+    ps = rng.uniform(0.01, 0.1, n)
+    fs = np.exp(rng.uniform(np.log(1e-5), np.log(1e-3), n))
+    seeds = rng.integers(1, 2 ** 62, n)
+    return arrivals, kinds, sides, steps, ps, fs, seeds
+
+
+def serve_desc(capi, kind, side, seed):
+    from cellularautomatacore_jl_gb300.model import Generations, Life
+    if kind == 2:
+        return fire_desc(capi, side, seed)
+    d = capi.Desc()
+    r = Life("B3/S23") if kind == 0 else Generations("B2/S/C3")
+    d.rule = capi.RULE_LIFE if kind == 0 else capi.RULE_GENERATIONS
+    d.nbhd, d.radius, d.states = capi.MOORE, 1, 2 if kind == 0 else 3
+    d.birth, d.survive = r.birth, r.survive
+    d.n1 = d.n2 = int(side)
+    d.seed = int(seed)
+    return d
+
+
+def run_stream(capi, lib, n, rate, seed):
+    """Submit n requests of the served stream at Poisson rate `rate` into a fresh server and
+    collect every result; returns (results {id: (status, t_submit, t_done)}, requests, wall)."""
+    arrivals, kinds, sides, steps, ps, fs, seeds = serve_requests(n, seed)
+    arrivals = arrivals * (SERVE["rate"] / rate)
+    cfg = capi.ServerConfig()
+    cfg.hbm_budget, cfg.chunk_steps = SERVE["hbm_budget"], SERVE["chunk_steps"]
+    cfg.big_cells, cfg.max_big = SERVE["big_cells"], SERVE["max_big"]
+    srv = ctypes.c_void_p()
+    capi.check(lib.gbca_server_start(ctypes.byref(cfg), ctypes.byref(srv)))
+    descs = [serve_desc(capi, kinds[i], sides[i], seeds[i]) for i in range(n)]
+    res_buf = (capi.Result * 4096)()
+    got = {}
+    rid = ctypes.c_uint64()
+    nres = ctypes.c_int32()
+
+    def drain():
+        capi.check(lib.gbca_server_poll(srv, res_buf, 4096, ctypes.byref(nres)))
+        for k in range(nres.value):
+            r = res_buf[k]
+            got[int(r.id)] = (r.status, r.t_submit, r.t_done)
+
+    t0 = time.perf_counter()
+    for i in range(n):
+        while time.perf_counter() - t0 < arrivals[i]:
+            drain()
+        P = (ctypes.c_double * 2)(ps[i], fs[i])
+        dens = 0.0 if kinds[i] == 2 else 0.5
+        capi.check(lib.gbca_server_submit(srv, ctypes.byref(descs[i]), None, 0, dens, int(seeds[i]), 0, int(steps[i]),
+                                          P, 2 if kinds[i] == 2 else 0, ctypes.byref(rid)))
+    while len(got) < n:
+        drain()
+        time.sleep(0.001)
+    wall = time.perf_counter() - t0
+    lib.gbca_server_stop(srv)
+    return got, (arrivals, kinds, sides, steps, ps, fs, seeds, descs), wall
+
+
+def bench_served(capi, lib):
+    """Poisson arrivals at 2000 requests/s for SERVE['seconds'] s into the continuous-batching
+    server (far above what one GPU completes, so latency is mostly queueing), then a stream at
+    half the measured capacity (latency of the loop itself); latency = result time - submit
+    time. Then the plain path: the same kind of requests one at a time through a handle each
+    (create, upload, advance, summaries, destroy), on a sample."""
+    n = int(SERVE["rate"] * SERVE["seconds"])
+    got, reqs, wall = run_stream(capi, lib, n, SERVE["rate"], 2000)
+    arrivals, kinds, sides, steps, ps, fs, seeds, descs = reqs
+    lat = np.array([v[2] - v[1] for v in got.values()])
+    t_first = min(v[1] for v in got.values())
+    t_last = max(v[2] for v in got.values())
+    cu = float((sides.astype(np.float64) ** 2 * steps).sum())
+    served = {"workload": f"{n} requests, Poisson arrivals at {SERVE['rate']:.0f}/s for {SERVE['seconds']} s; rule "
+                          "uniform over Life B3/S23, Generations B2/S/C3, forest fire; side log-uniform 64..4096; steps "
+                          "50..1000", "requests": n, "ok": int(sum(1 for v in got.values() if v[0] == 0)),
+              "sims_per_s": n / (t_last - t_first), "gcell_updates_s": cu / (t_last - t_first) / 1e9,
+              "offered_gcell_updates_s": cu / arrivals[-1] / 1e9,
+              "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+              "wall_s": wall, "config": {k: SERVE[k] for k in ("hbm_budget", "chunk_steps", "big_cells", "max_big")}}
+
+    # the plain per-request path on a random sample, one request at a time
+    rng = np.random.Generator(np.random.PCG64(5))
+    sample = rng.choice(n, SERVE["plain_sample"], replace=False)
+    lat_plain, t_sum = [], 0.0
+    for i in sample:
+        u0 = (rng.random(int(sides[i]) ** 2) < 0.5).astype(np.int8) if kinds[i] != 2 else \
+            np.zeros(int(sides[i]) ** 2, np.int8)
+        d = descs[i]
+        P = (ctypes.c_double * 2)(ps[i], fs[i])
+        ts = time.perf_counter()
+        h = ctypes.c_void_p()
+        capi.check(lib.gbca_create(ctypes.byref(d), ctypes.byref(h)))
+        capi.check(lib.gbca_set_state(h, u0.ctypes.data, u0.nbytes))
+        capi.check(lib.gbca_advance(h, 0, int(steps[i]), P, 2 if kinds[i] == 2 else 0))
+        c8 = (ctypes.c_int64 * 8)()
+        o1 = ctypes.c_int64()
+        m1 = ctypes.c_double()
+        capi.check(lib.gbca_summaries(h, c8, 8, ctypes.byref(o1), ctypes.byref(m1)))
+        lib.gbca_destroy(h)
+        dt = time.perf_counter() - ts
+        t_sum += dt
+        lat_plain.append(dt)
+    # a stream at half the measured capacity, for the loop's latency when it keeps up
+    rate2 = 0.5 * served["sims_per_s"]
+    n2 = max(50, int(rate2 * 3.0))
+    got2, reqs2, _ = run_stream(capi, lib, n2, rate2, 2001)
+    lat2 = np.array([v[2] - v[1] for v in got2.values()])
+    t2a, t2b = min(v[1] for v in got2.values()), max(v[2] for v in got2.values())
+    served["at_half_capacity"] = {"rate_per_s": rate2, "requests": n2,
+                                  "ok": int(sum(1 for v in got2.values() if v[0] == 0)),
+                                  "sims_per_s": n2 / (t2b - t2a), "latency_p50_s": float(np.percentile(lat2, 50)),
+                                  "latency_p99_s": float(np.percentile(lat2, 99))}
+    served["plain_sims_per_s"] = len(sample) / t_sum
+    served["plain_sample"] = len(sample)
+    served["plain_service_p50_s"] = float(np.percentile(lat_plain, 50))
+    served["speedup_vs_plain"] = served["sims_per_s"] / served["plain_sims_per_s"]
+    return served
+
+
 def main():
     args = parse()
     if args.case:
@@ -409,6 +554,12 @@ def main():
             if events is not None:
                 events[2 * k + 1].record(stream)
 
+    # the autotuner picks each sweep's geometry on the initial states (untimed, like warm-up)
+    geometry = {}
+    for name, h, d0, (n1, n2) in zip(("ltl", "fire"), handles, dev0, sizes):
+        capi.check(lib.gbca_set_state_device(h, ctypes.c_void_p(d0.data_ptr()), n1))
+        if not args.no_tune:
+            geometry[name] = tune(capi, lib, h, params_fire if name == "fire" else None, 2 if name == "fire" else 0)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             step_resident()
@@ -438,7 +589,7 @@ def main():
     value = world * cell_updates() / (ms_per_step * 1e-3) / 1e9
 
     # ---- roofline of the dominant kernel
-    per_pass = {"ltl": 4, "fire": 8}
+    per_pass = {"ltl": geometry.get("ltl", (0, 0))[0] or 4, "fire": geometry.get("fire", (0, 0))[0] or 8}
     parts = {}
     for name, cfg, ms in (("ltl", LTL, part_ms[0]), ("fire", FIRE, part_ms[1])):
         launches_part = -(-cfg["steps"] // per_pass[name])
@@ -490,6 +641,7 @@ def main():
            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3}
 
     batched = bench_batched(capi, lib, max(1, args.warmup // 2), max(1, args.steps // 2)) if rank == 0 else None
+    served = bench_served(capi, lib) if rank == 0 and not args.no_serve else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -504,10 +656,11 @@ def main():
                                        "8192^2 Int8 torus x 1000 steps + forest fire VonNeumann(1) on a 16384^2 Grid "
                                        "Constant(0) x 500 steps (p=0.03, f=1e-4)",
                            "cell_updates_per_step": cell_updates(), "parallelism": f"replicas x{world}",
+                           "geometry": {k: {"steps_per_pass": v[0], "tile_rows": v[1]} for k, v in geometry.items()},
                            "l2": "inputs larger than L2: the 16384^2 state is 268 MB, and each step re-copies "
                                  "335 MB of initial states"},
                 "roofline": roofline, "parts": parts, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clocks.summary(), "cpu_baseline": cpu, "batched": batched}
+                "clocks": clocks.summary(), "cpu_baseline": cpu, "batched": batched, "served": served}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "ensemble.cuh"
+#include "fire_words.cuh"
 #include "gbca_internal.cuh"
 #include "measures.cuh"
 
@@ -189,6 +190,97 @@ __device__ int run_tiled(const EnsInstance& I, int8_t* pool, int8_t* A0, int8_t*
     return cur;
 }
 
+// Forest fire (VonNeumann(1)) with the whole lattice in shared memory, four cells per work
+// item: cell (x, y) lives at byte (y + 1) * P1 + x + 4 of a row pitch P1 = 4 ceil((n1 + 8) / 4),
+// so the interior starts on a word; the halo (row -1, row n2, column -1, column n1) is
+// refreshed from the boundary map before every step.
+__device__ void run_in_smem_fire(const EnsInstance& I, int8_t* pool, int8_t* A, int8_t* B, const PhiloxKeys& K,
+                                 const FireGeom& g) {
+    const int n1 = (int)I.n1, n2 = (int)I.n2, P1 = (n1 + 8 + 3) / 4 * 4;
+    int8_t* gl = pool + I.off[I.cur];
+    for (int q = threadIdx.x; q < n1 * n2; q += blockDim.x) {
+        const int x = q % n1, y = q / n1;
+        A[(y + 1) * P1 + x + 4] = gl[x + (int64_t)y * I.pitch];
+    }
+    const int ring = 2 * (n1 + 2) + 2 * n2;
+    for (int64_t s = 0; s < I.nsteps; ++s) {
+        __syncthreads();
+        for (int q = threadIdx.x; q < ring; q += blockDim.x) {
+            int x, y;
+            if (q < 2 * (n1 + 2)) {
+                x = q % (n1 + 2) - 1;
+                y = q < n1 + 2 ? -1 : n2;
+            } else {
+                const int q2 = q - 2 * (n1 + 2);
+                y = q2 >> 1;
+                x = (q2 & 1) ? n1 : -1;
+            }
+            A[(y + 1) * P1 + x + 4] = boundary_value(I, A + P1 + 4, P1, x, y);
+        }
+        __syncthreads();
+        const DrawStep ds = draw_step(K, I.t0 + s);
+        fire_substep_words<false>((const uint32_t*)A, (uint32_t*)B, P1 / 4, 1, (n1 + 3) / 4, 1, n2, -4, -1, g, ds, K,
+                                  threadIdx.x, blockDim.x, s == 0);
+        int8_t* tmp = A; A = B; B = tmp;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < n1 * n2; q += blockDim.x) {
+        const int x = q % n1, y = q / n1;
+        gl[x + (int64_t)y * I.pitch] = A[(y + 1) * P1 + x + 4];
+    }
+}
+
+// Forest fire on tiles of kEnsTile^2 through the two global buffers, 8 steps per pass,
+// four cells per work item. Returns the buffer holding the final state.
+__device__ int run_tiled_fire(const EnsInstance& I, int8_t* pool, int8_t* A0, int8_t* B0, const PhiloxKeys& K,
+                              const FireGeom& g) {
+    constexpr int HX = kEnsMaxHalo, SX = kEnsTile + 2 * HX, SW = SX / 4;
+    const int ntx = (int)((I.n1 + kEnsTile - 1) / kEnsTile), nty = (int)((I.n2 + kEnsTile - 1) / kEnsTile);
+    int cur = I.cur;
+    for (int64_t s0 = 0; s0 < I.nsteps; s0 += kEnsMaxHalo) {
+        const int k = (int)((I.nsteps - s0) < kEnsMaxHalo ? (I.nsteps - s0) : kEnsMaxHalo);
+        const int SY = kEnsTile + 2 * k;
+        const int8_t* src = pool + I.off[cur];
+        int8_t* dst = pool + I.off[cur ^ 1];
+        for (int tile = 0; tile < ntx * nty; ++tile) {
+            const int64_t X0 = (int64_t)(tile % ntx) * kEnsTile, Y0 = (int64_t)(tile / ntx) * kEnsTile;
+            int8_t* A = A0;
+            int8_t* B = B0;
+            __syncthreads();
+            for (int q = threadIdx.x; q < SX * SY; q += blockDim.x) {
+                const int lx = q % SX, ly = q / SX;
+                A[q] = boundary_value(I, src, I.pitch, X0 - HX + lx, Y0 - k + ly);
+            }
+            __syncthreads();
+            const bool interior = X0 - HX >= 0 && X0 + kEnsTile + HX <= I.n1 && Y0 - k >= 0 &&
+                                  Y0 + kEnsTile + k <= I.n2;
+            for (int sub = 0; sub < k; ++sub) {
+                const DrawStep ds = draw_step(K, I.t0 + s0 + sub);
+                const int ex = k - 1 - sub;
+                const int w_lo = (HX - ex) >> 2, w_hi = (HX + kEnsTile + ex + 3) >> 2;
+                const bool exact = s0 == 0 && sub == 0;  // the run's first step may read any Int8 value
+                if (interior)
+                    fire_substep_words<false>((const uint32_t*)A, (uint32_t*)B, SW, w_lo, w_hi - w_lo, k - ex,
+                                              kEnsTile + 2 * ex, X0 - HX, Y0 - k, g, ds, K, threadIdx.x, blockDim.x,
+                                              exact);
+                else
+                    fire_substep_words<true>((const uint32_t*)A, (uint32_t*)B, SW, w_lo, w_hi - w_lo, k - ex,
+                                             kEnsTile + 2 * ex, X0 - HX, Y0 - k, g, ds, K, threadIdx.x, blockDim.x,
+                                             exact);
+                __syncthreads();
+                int8_t* tmp = A; A = B; B = tmp;
+            }
+            for (int q = threadIdx.x; q < kEnsTile * kEnsTile; q += blockDim.x) {
+                const int64_t gx = X0 + q % kEnsTile, gy = Y0 + q / kEnsTile;
+                if (gx < I.n1 && gy < I.n2) dst[gx + gy * I.pitch] = A[(k + q / kEnsTile) * SX + HX + q % kEnsTile];
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    return cur;
+}
+
 // Integer summaries of a state (values 0..7 counted, Moran's I sums over VonNeumann(1)).
 __device__ __noinline__ void summarize(const EnsInstance& I, const int8_t* base, int64_t pitch, EnsSummary* out) {
     __shared__ unsigned long long red[kEnsSumWords];
@@ -249,7 +341,19 @@ __global__ void __launch_bounds__(kEnsThreads) k_ensemble(const EnsInstance* __r
         const PhiloxKeys K = philox_keys_dev(I.seed);
         int cur = I.cur;
         if (I.nsteps > 0) {
-            if (I.small) {
+            if (fast_fire(I)) {
+                FireGeom g;
+                g.n1 = I.n1;
+                g.n2 = I.n2;
+                g.bnd0 = I.bnd0;
+                g.bnd1 = I.bnd1;
+                g.cst0 = (uint32_t)(uint8_t)I.cval0 * 0x01010101u;
+                g.cst1 = (uint32_t)(uint8_t)I.cval1 * 0x01010101u;
+                fire_thresholds(I.thr_p, I.thr_f, I.params_f32 != 0, g);
+                g.exact_always = fire_odd_constant(I.bnd0, I.cval0, I.bnd1, I.cval1);
+                if (I.small) run_in_smem_fire(I, pool, sA, sB, K, g);
+                else cur = run_tiled_fire(I, pool, sA, sB, K, g);
+            } else if (I.small) {
                 run_in_smem(I, pool, sA, sB, K);
             } else {
                 cur = run_tiled(I, pool, sA, sB, K);
@@ -292,6 +396,12 @@ int ensemble_grid() {
 }
 
 int ensemble_smem_cells() { return kEnsBuf; }
+
+bool ensemble_fits_smem(const gbca_desc& d) {
+    if (d.rule == GBCA_RULE_FOREST_FIRE && d.nbhd == GBCA_VON_NEUMANN && d.radius == 1)
+        return (d.n1 + 8 + 3) / 4 * 4 * (d.n2 + 2) <= kEnsBuf;
+    return (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= kEnsBuf;
+}
 
 }  // namespace gbca
 
@@ -355,7 +465,7 @@ int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out)
         I.bnd1 = d.boundary[1];
         I.cval0 = d.boundary[0] == GBCA_CONSTANT ? (int32_t)d.constant[0] : 0;
         I.cval1 = d.boundary[1] == GBCA_CONSTANT ? (int32_t)d.constant[1] : 0;
-        I.small = (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= kEnsBuf;
+        I.small = ensemble_fits_smem(d) ? 1 : 0;
         I.summarize = 1;
     }
     if (gbca_device_count() < 1) return efail(GBCA_ERR_CUDA, "no CUDA device is visible");

@@ -3,6 +3,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "gbca.h"
+
 namespace gbca {
 
 constexpr int kEnsCounts = 8;                  // values 0..7 are counted per instance
@@ -30,7 +32,9 @@ cudaError_t launch_ensemble(const EnsInstance* d_inst, const int* d_order, int n
                             EnsSummary* d_out, int* d_cur, int grid, cudaStream_t st);
 // Grid size that fills the current device with resident CTAs.
 int ensemble_grid();
-// Instances with (n1 + 2r)(n2 + 2r) <= this many cells run in shared memory.
+// Bytes of each of the two shared buffers a CTA of the ensemble kernel has.
 int ensemble_smem_cells();
+// Whether an instance runs with its whole lattice (and halo) in shared memory.
+bool ensemble_fits_smem(const gbca_desc& d);
 
 }  // namespace gbca

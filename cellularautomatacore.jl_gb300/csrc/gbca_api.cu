@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "gbca_internal.cuh"
 #include "lenia.cuh"
@@ -22,6 +23,9 @@ struct gbca_handle {
     unsigned long long* acc_host = nullptr;  // pinned copy
     int nsm = 148;
     gbca::LeniaPlan* lenia = nullptr;
+    bool states_valid = true;  // every state is one the rule produces (see scan_states)
+    bool forced = false;       // gbca_set_geometry pinned the sweep geometry
+    gbca::SweepChoice force = {0, 0};
 };
 
 namespace {
@@ -116,12 +120,111 @@ uint64_t threshold(double p, bool f32) {
     return (uint64_t)std::ceil(p * 9007199254740992.0);
 }
 
+// Whether every cell of the current state is one the rule produces — 0..C-1 for Generations,
+// 0..2 for the forest fire — from a device histogram of the state.
+cudaError_t scan_states(gbca_handle* h, bool* valid) {
+    cudaError_t e = gbca::launch_measures((const int8_t*)h->buf[h->cur], h->d.n1, h->d.n2, h->pitch,
+                                          h->d.boundary[0], h->d.boundary[1], h->acc, h->nsm, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->acc_host, h->acc, 256 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return e;
+    const int nv = h->d.rule == GBCA_RULE_GENERATIONS ? h->d.states : 3;
+    unsigned long long inside = 0;
+    for (int v = 0; v < nv && v < 128; ++v) inside += h->acc_host[128 + v];
+    *valid = inside == (unsigned long long)(h->d.n1 * h->d.n2);
+    return cudaSuccess;
+}
+
+bool scanned_rule(const gbca_handle* h) {
+    return h->d.rule == GBCA_RULE_GENERATIONS || h->d.rule == GBCA_RULE_FOREST_FIRE;
+}
+
+// A state written by the caller may hold values the rule never produces; the fast paths
+// assume it does not, so scan it once (the rule keeps valid states valid).
+int ensure_scanned(gbca_handle* h) {
+    if (!scanned_rule(h) || h->states_valid) return GBCA_OK;
+    bool valid = false;
+    const cudaError_t e = scan_states(h, &valid);
+    if (e != cudaSuccess) return cuda_fail(e, "state scan");
+    h->states_valid = valid;
+    return GBCA_OK;
+}
+
 int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams) {
     if (h->d.rule == GBCA_RULE_FOREST_FIRE && (!params || nparams < 2))
         return fail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
+    const int rc = ensure_scanned(h);
+    if (rc != GBCA_OK) return rc;
     int8_t* const bufs[2] = {(int8_t*)h->buf[0], (int8_t*)h->buf[1]};
-    const cudaError_t e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, t, nsteps, params, h->stream);
+    const cudaError_t e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, t, nsteps, params, h->stream,
+                                           scanned_rule(h) && h->states_valid, h->forced ? &h->force : nullptr);
+    if (h->d.rule == GBCA_RULE_FOREST_FIRE) h->states_valid = true;  // a step leaves only 0, 1 and 2
     if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+    return GBCA_OK;
+}
+
+// The sweep parameters of the handle's next call, for the kernel-selection predicates.
+gbca::SweepParams handle_params(const gbca_handle* h, const double* params) {
+    gbca::SweepParams p = gbca::sweep_params(h->d, h->pitch, params);
+    p.states_valid = scanned_rule(h) && h->states_valid ? 1 : 0;
+    return p;
+}
+
+// Times nsteps steps of each candidate geometry from the handle's current state (restored
+// before every run and at the end) and returns the fastest per step.
+int time_candidates(gbca_handle* h, const std::vector<gbca::SweepChoice>& cands, const double* params,
+                    gbca::SweepChoice* best) {
+    const size_t bytes = (size_t)h->pitch * (size_t)h->d.n2;
+    const int cur0 = h->cur;
+    void* saved = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t e = cudaMalloc(&saved, bytes);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(saved, h->buf[cur0], bytes, cudaMemcpyDeviceToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    float best_ms = 0.0f;
+    int8_t* const bufs[2] = {(int8_t*)h->buf[0], (int8_t*)h->buf[1]};
+    const bool valid = scanned_rule(h) && h->states_valid;
+    for (size_t c = 0; c < cands.size() && e == cudaSuccess; ++c) {
+        // a whole number of passes, about 48 steps, so that every candidate runs full passes
+        const int per = cands[c].steps_per_pass;
+        const int64_t nsteps = (int64_t)per * ((48 + per - 1) / per);
+        float ms_min = 0.0f;
+        for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+            h->cur = cur0;
+            e = cudaMemcpyAsync(h->buf[cur0], saved, bytes, cudaMemcpyDeviceToDevice, h->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
+            if (e == cudaSuccess)
+                e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, 1, nsteps, params, h->stream, valid, &cands[c]);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[1], h->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            ms /= (float)nsteps;
+            if (rep == 0 || ms < ms_min) ms_min = ms;
+        }
+        if (e == cudaSuccess && (c == 0 || ms_min < best_ms)) {
+            best_ms = ms_min;
+            *best = cands[c];
+        }
+    }
+    h->cur = cur0;
+    if (saved) {
+        const cudaError_t e2 = cudaMemcpyAsync(h->buf[cur0], saved, bytes, cudaMemcpyDeviceToDevice, h->stream);
+        if (e == cudaSuccess) e = e2;
+        const cudaError_t e3 = cudaStreamSynchronize(h->stream);
+        if (e == cudaSuccess) e = e3;
+        cudaFree(saved);
+    }
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? fail(GBCA_ERR_OUT_OF_MEMORY, "the tuner's copy of the state (%zu bytes) "
+                                                     "did not fit", bytes)
+                                              : cuda_fail(e, "gbca_tune");
+    }
     return GBCA_OK;
 }
 
@@ -214,6 +317,7 @@ int gbca_set_state(gbca_handle* h, const void* host, size_t nbytes) {
     GBCA_CUDA(cudaMemcpy2DAsync(h->buf[h->cur], (size_t)h->pitch, host, row, row, (size_t)h->d.n2,
                                 cudaMemcpyHostToDevice, h->stream),
               "set_state copy");
+    h->states_valid = false;
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_state");
     return GBCA_OK;
 }
@@ -226,6 +330,7 @@ int gbca_set_state_device(gbca_handle* h, const void* dptr, int64_t src_pitch) {
     GBCA_CUDA(cudaMemcpy2DAsync(h->buf[h->cur], (size_t)h->pitch, dptr, (size_t)src_pitch, row, (size_t)h->d.n2,
                                 cudaMemcpyDeviceToDevice, h->stream),
               "set_state_device copy");
+    h->states_valid = false;
     return GBCA_OK;
 }
 
@@ -251,6 +356,60 @@ int gbca_advance(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
     return advance_int8(h, t, nsteps, params, nparams);
 }
 
+int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* steps_per_pass, int32_t* tile_rows) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (steps_per_pass) *steps_per_pass = 0;
+    if (tile_rows) *tile_rows = 0;
+    if (h->d.rule == GBCA_RULE_LENIA) return GBCA_OK;  // nothing to tune
+    if (h->d.rule == GBCA_RULE_FOREST_FIRE && (!params || nparams < 2))
+        return fail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
+    int rc = ensure_scanned(h);
+    if (rc != GBCA_OK) return rc;
+    const std::vector<gbca::SweepChoice> cands = gbca::sweep_candidates(handle_params(h, params));
+    if (cands.empty()) return GBCA_OK;  // the general kernel: one geometry
+    gbca::SweepChoice best = cands[0];
+    rc = time_candidates(h, cands, params, &best);
+    if (rc != GBCA_OK) return rc;
+    gbca::store_choice(h->d, best);
+    if (steps_per_pass) *steps_per_pass = best.steps_per_pass;
+    if (tile_rows) *tile_rows = best.tile_rows;
+    return GBCA_OK;
+}
+
+int gbca_forget_tuning(void) {
+    gbca::forget_choices();
+    return GBCA_OK;
+}
+
+int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (steps_per_pass == 0 && tile_rows == 0) {
+        h->forced = false;
+        return GBCA_OK;
+    }
+    if (steps_per_pass < 1 || steps_per_pass > 64 || tile_rows < 0)
+        return fail(GBCA_ERR_ARGUMENT, "steps per pass must lie in 1..64 and tile rows be non-negative, got %d, %d",
+                    (int)steps_per_pass, (int)tile_rows);
+    if (h->d.rule == GBCA_RULE_LENIA)
+        return fail(GBCA_ERR_UNSUPPORTED, "sweep geometry applies to the Int8 sweep kernels, not to Lenia");
+    const int rc = ensure_scanned(h);
+    if (rc != GBCA_OK) return rc;
+    const gbca::SweepParams p = handle_params(h, nullptr);
+    if (gbca::fire_fast_supported(p)) {
+        if (tile_rows != 0) return fail(GBCA_ERR_ARGUMENT, "the forest-fire kernel's tile height is fixed; pass 0");
+    } else if (gbca::life_simd_supported(p)) {
+        if (tile_rows > 0 && !gbca::life_choice_fits(p, steps_per_pass, tile_rows))
+            return fail(GBCA_ERR_ARGUMENT, "%d steps per pass on tiles %d rows high exceed shared memory",
+                        (int)steps_per_pass, (int)tile_rows);
+    } else {
+        return fail(GBCA_ERR_UNSUPPORTED, "this problem runs on the general kernel, whose geometry is fixed");
+    }
+    h->force.steps_per_pass = steps_per_pass;
+    h->force.tile_rows = tile_rows;
+    h->forced = true;
+    return GBCA_OK;
+}
+
 int gbca_read_cell(gbca_handle* h, int64_t i, int64_t j, void* out) {
     if (!h || !out) return fail(GBCA_ERR_ARGUMENT, "null handle or output");
     if (i < 1 || i > h->d.n1 || j < 1 || j > h->d.n2)
@@ -269,6 +428,7 @@ int gbca_write_cell(gbca_handle* h, int64_t i, int64_t j, const void* value) {
                     (long long)j, (long long)h->d.n1, (long long)h->d.n2);
     char* dst = (char*)h->buf[h->cur] + (i - 1) * (int64_t)h->esize + (j - 1) * h->pitch;
     GBCA_CUDA(cudaMemcpyAsync(dst, value, h->esize, cudaMemcpyHostToDevice, h->stream), "write_cell");
+    h->states_valid = false;
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "write_cell");
     return GBCA_OK;
 }

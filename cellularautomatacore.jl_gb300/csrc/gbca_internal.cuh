@@ -3,6 +3,8 @@
 // boundary mapping of src/spaces.jl:46-51, and the launch parameters of a sweep.
 #pragma once
 
+#include <vector>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -159,6 +161,9 @@ struct SweepParams {
     int32_t tile_x, tile_y;    // output tile
     int32_t halo_x, halo_y;    // loaded halo (>= nsub * radius)
     PhiloxKeys keys;           // round keys of `seed` (set by the launchers that use them)
+    int32_t states_valid;      // every state is known to be one the rule produces (Generations
+                               // 0..C-1, forest fire 0..2)
+    int32_t pad_;
 };
 
 // The message gbca_last_error() returns on this thread.
@@ -171,14 +176,33 @@ int64_t launches_so_far();
 // Kernel selection and temporally blocked passes for an Int8 problem (sweep_dispatch.cu):
 // nsteps steps between bufs[*cur] and bufs[*cur ^ 1], *cur updated.
 SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params);
+// A kernel geometry choice: steps per temporally blocked pass and tile height (0 = default).
+struct SweepChoice {
+    int32_t steps_per_pass;
+    int32_t tile_rows;
+};
+
+// states_valid: every state is known to be one the rule produces (Generations: 0..C-1,
+// enabling the bit-sliced kernel; forest fire: 0..2, enabling bit tests on the first step).
+// force: use this geometry instead of the autotuner's cached pick (tune.cu).
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
-                       const double* params, cudaStream_t st);
+                       const double* params, cudaStream_t st, bool states_valid = false,
+                       const SweepChoice* force = nullptr);
+
+// The autotuner's cached choice for a problem shape (tune.cu); false when it has none.
+bool tuned_choice(const gbca_desc& d, SweepChoice* out);
+void store_choice(const gbca_desc& d, const SweepChoice& c);
+void forget_choices();
+// The geometries the autotuner times for a problem (empty: the general kernel, nothing to tune).
+std::vector<SweepChoice> sweep_candidates(const SweepParams& p);
 
 // Launchers (one translation unit each).
 cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 bool life_simd_supported(const SweepParams& p);
 cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 int life_steps_per_pass(const SweepParams& p);
+// Whether a pass of `steps` steps on tiles `rows` high fits the bit-sliced kernel's shared memory.
+bool life_choice_fits(const SweepParams& p, int steps, int rows);
 bool fire_fast_supported(const SweepParams& p);
 cudaError_t launch_fire(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 

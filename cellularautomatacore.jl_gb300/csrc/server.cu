@@ -107,6 +107,7 @@ struct Request {
     int64_t pitch = 0;
     int cur = 0;
     bool big = false;
+    bool valid = true;  // every initial state is one the rule produces
     double t_submit = 0.0, t_admit = 0.0;
 };
 
@@ -227,7 +228,7 @@ EnsInstance small_instance(const Request* r, int64_t steps, bool last) {
     I.cval0 = d.boundary[0] == GBCA_CONSTANT ? (int32_t)d.constant[0] : 0;
     I.cval1 = d.boundary[1] == GBCA_CONSTANT ? (int32_t)d.constant[1] : 0;
     I.cur = r->cur;
-    I.small = (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= ensemble_smem_cells();
+    I.small = ensemble_fits_smem(d) ? 1 : 0;
     I.summarize = last ? 1 : 0;
     return I;
 }
@@ -330,7 +331,9 @@ void scheduler(gbca_server* S) {
             const int64_t rem = r->nsteps - r->done;
             step_big[j] = rem < S->cfg.chunk_steps ? rem : S->cfg.chunk_steps;
             int8_t* const bufs[2] = {S->arena_base + r->off, S->arena_base + r->off + r->bytes / 2};
-            e = sweep_int8(r->d, r->pitch, bufs, &r->cur, r->t0 + r->done, step_big[j], r->params, S->s_big[j]);
+            e = sweep_int8(r->d, r->pitch, bufs, &r->cur, r->t0 + r->done, step_big[j], r->params, S->s_big[j],
+                           r->valid);
+            r->valid = r->valid || r->d.rule == GBCA_RULE_FOREST_FIRE;  // a fire step leaves only 0, 1, 2
             if (e == cudaSuccess && step_big[j] == rem) {
                 unsigned long long* acc = S->d_acc + (size_t)j * kMeasureWords;
                 e = launch_measures(bufs[r->cur], r->d.n1, r->d.n2, r->pitch, r->d.boundary[0], r->d.boundary[1], acc,
@@ -467,7 +470,15 @@ int gbca_server_submit(gbca_server* S, const gbca_desc* d, const void* u0, size_
         return sfail(GBCA_ERR_ARGUMENT, "initial density must be in [0, 1]");
     Request* r = new Request();
     r->d = *d;
-    if (u0) r->u0.assign((const int8_t*)u0, (const int8_t*)u0 + nbytes);
+    if (u0) {
+        r->u0.assign((const int8_t*)u0, (const int8_t*)u0 + nbytes);
+        const int nv = d->rule == GBCA_RULE_GENERATIONS ? d->states : (d->rule == GBCA_RULE_FOREST_FIRE ? 3 : 256);
+        for (int8_t v : r->u0)
+            if (v < 0 || v >= nv) {
+                r->valid = false;
+                break;
+            }
+    }
     r->density = init_density;
     r->init_seed = init_seed;
     r->t0 = t0;

@@ -1,6 +1,7 @@
 // sweep_dispatch.cu — picks the sweep kernel for an Int8 problem and runs nsteps steps as
 // temporally blocked passes: the forest-fire kernel (VonNeumann(1), Synchronous), the
-// bit-sliced Life-like kernel (Moore(r <= 5), Synchronous), else the general kernel.
+// bit-sliced kernel (Life-like on Moore(r <= 5); Generations with C <= 4 on Moore(r <= 2)
+// when every state is known to lie in 0..C-1), else the general kernel.
 #include <cstring>
 
 #include "gbca_internal.cuh"
@@ -37,10 +38,15 @@ SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params
 }
 
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
-                       const double* params, cudaStream_t st) {
+                       const double* params, cudaStream_t st, bool states_valid, const SweepChoice* force) {
     SweepParams p = sweep_params(d, pitch, params);
+    p.states_valid = states_valid ? 1 : 0;
     const bool fire = fire_fast_supported(p);
     const bool life = !fire && life_simd_supported(p);
+    SweepChoice choice = {0, 0};
+    if (force) choice = *force;
+    else if (fire || life) tuned_choice(d, &choice);  // the autotuner's pick for this shape, if any
+    p.tile_y = choice.tile_rows;
     while (nsteps > 0) {
         int64_t k;
         cudaError_t e;
@@ -48,11 +54,13 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
         int8_t* dst = bufs[*cur ^ 1];
         p.t0 = t;
         if (fire) {
-            k = nsteps < 8 ? nsteps : 8;
+            const int64_t per = choice.steps_per_pass > 0 ? choice.steps_per_pass : 8;
+            k = nsteps < per ? nsteps : per;
             p.nsub = (int32_t)k;
             e = launch_fire(p, src, dst, st);
+            p.states_valid = 1;  // a pass leaves only 0, 1 and 2
         } else if (life) {
-            const int64_t per = life_steps_per_pass(p);
+            const int64_t per = choice.steps_per_pass > 0 ? choice.steps_per_pass : life_steps_per_pass(p);
             k = nsteps < per ? nsteps : per;
             p.nsub = (int32_t)k;
             e = launch_life_simd(p, src, dst, st);

@@ -9,6 +9,7 @@
 // draw_fast() hoists the products that do not depend on the cell out of the cell loop,
 // and temporal blocking (nsub steps per pass, halo nsub) keeps HBM traffic at
 // 2 B / nsub per cell-update.
+#include "fire_words.cuh"
 #include "gbca_internal.cuh"
 
 namespace gbca {
@@ -17,21 +18,6 @@ namespace {
 
 constexpr int kFireTX = 256, kFireTY = 128;
 constexpr int kFireThreadsX = 32, kFireThreadsY = 16;
-
-// Bytes equal to 2 -> bit 7 of that byte set (exact: no carries cross bytes).
-__device__ __forceinline__ uint32_t bytes_eq(uint32_t x, uint32_t pattern) {
-    const uint32_t z = x ^ pattern;
-    return ~(((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
-}
-
-// uniform < p as one 64-bit compare of the raw Philox words: (w.x:w.y) >> 11 < T is
-// (w.x:w.y) < T * 2^11 (Float64 p), and (w.x >> 8) < T is w.x < T * 2^8 (Float32 p).
-// T = 2^53 (p >= 1) would overflow T * 2^11; `all` marks it (every draw is below p).
-__device__ __forceinline__ bool below_u(uint2 w, uint64_t U, bool all, bool f32) {
-    if (all) return true;
-    if (f32) return (uint64_t)w.x < U;
-    return ((((uint64_t)w.x) << 32) | (uint64_t)w.y) < U;
-}
 
 // Four cells (one 32-bit word of the shared tile) per work item: neighbour tests in byte
 // SIMD, then four independent Philox chains.
@@ -61,67 +47,22 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
     }
     __syncthreads();
 
-    const bool f32 = p.params_f32 != 0;
-    const bool all_p = !f32 && p.thr_p >= ((uint64_t)1 << 53), all_f = !f32 && p.thr_f >= ((uint64_t)1 << 53);
-    const uint64_t Up = f32 ? (p.thr_p << 8) : (all_p ? 0 : p.thr_p << 11);
-    const uint64_t Uf = f32 ? (p.thr_f << 8) : (all_f ? 0 : p.thr_f << 11);
-    const uint32_t n1 = (uint32_t)p.n1;
-    const uint32_t cst1 = (uint32_t)(uint8_t)p.cval[1] * 0x01010101u, cst0 = (uint32_t)(uint8_t)p.cval[0];
+    FireGeom g;
+    g.n1 = p.n1;
+    g.n2 = p.n2;
+    g.bnd0 = p.bnd[0];
+    g.bnd1 = p.bnd[1];
+    g.cst0 = (uint32_t)(uint8_t)p.cval[0] * 0x01010101u;
+    g.cst1 = (uint32_t)(uint8_t)p.cval[1] * 0x01010101u;
+    fire_thresholds(p.thr_p, p.thr_f, p.params_f32 != 0, g);
+    g.exact_always = fire_odd_constant(p.bnd[0], p.cval[0], p.bnd[1], p.cval[1]);
     for (int s = 0; s < p.nsub; ++s) {
         const DrawStep ds = draw_step(p.keys, p.t0 + s);
         const int ex = p.nsub - 1 - s;
         const int w_lo = (hx - ex) >> 2, w_hi = (hx + kFireTX + ex + 3) >> 2;  // words covering the region
-        const int y_lo = hy - ex, nw = w_hi - w_lo, nrows = kFireTY + 2 * ex;
-        const uint32_t* A32 = (const uint32_t*)A;
-        uint32_t* B32 = (uint32_t*)B;
-        for (int it = tid; it < nw * nrows; it += nthr) {
-            const int lw = w_lo + it % nw, ly = y_lo + it / nw;
-            const int o = ly * sw + lw;
-            const uint32_t C = A32[o], Wl = A32[o - 1], Wr = A32[o + 1], Up_ = A32[o - sw], Dn = A32[o + sw];
-            const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
-            const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
-            const uint32_t burning = bytes_eq(Lf, 0x02020202u) | bytes_eq(Rt, 0x02020202u) |
-                                     bytes_eq(Up_, 0x02020202u) | bytes_eq(Dn, 0x02020202u);
-            const uint32_t fire = bytes_eq(C, 0x02020202u), empty = bytes_eq(C, 0u);
-            const int64_t gy = Y0 - hy + ly, gx0 = X0 - hx + 4 * lw;
-            uint32_t outmask = 0;  // bytes beyond a Constant edge
-            uint32_t my = (uint32_t)gy, mx0 = (uint32_t)gx0;
-            uint32_t mxb[4];
-            bool rowout = false;
-            if (!INTERIOR) {
-                const int64_t m = map_axis(p.bnd[1], gy, p.n2);
-                rowout = m < 0;
-                my = (uint32_t)m;
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const int64_t mb = map_axis(p.bnd[0], gx0 + b, p.n1);
-                    mxb[b] = (uint32_t)mb;
-                    if (mb < 0) outmask |= 0xFFu << (8 * b);
-                }
-            }
-            const uint32_t base = my * n1 + 1u;
-            uint32_t res = 0;
-            uint2 w[4];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const uint32_t mx = INTERIOR ? mx0 + b : mxb[b];
-                const bool e = (empty >> (8 * b + 7)) & 1u;
-                w[b] = draw_fast(ds, p.keys, base + mx, e ? 1u : 2u);
-            }
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const bool e = (empty >> (8 * b + 7)) & 1u, f = (fire >> (8 * b + 7)) & 1u;
-                const bool nb = (burning >> (8 * b + 7)) & 1u;
-                const bool hit = below_u(w[b], e ? Up : Uf, e ? all_p : all_f, f32);
-                const uint32_t v = f ? 0u : (e ? (hit ? 1u : 0u) : ((nb || hit) ? 2u : 1u));
-                res |= v << (8 * b);
-            }
-            if (!INTERIOR) {
-                if (rowout) res = cst1;
-                else res = (res & ~outmask) | ((cst0 * 0x01010101u) & outmask);
-            }
-            B32[o] = res;
-        }
+        fire_substep_words<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
+                                      kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
+                                      s == 0 && !p.states_valid);
         __syncthreads();
         int8_t* t = A; A = B; B = t;
     }

@@ -1,5 +1,6 @@
 // sweep_life.cu — Life-like and Larger-than-Life rules (src/rules.jl:354-389) on Moore(r),
-// r = 1..5, Synchronous, as a bit-sliced, temporally blocked sweep.
+// r = 1..5, and Generations rules with up to 4 states on Moore(1..2), Synchronous, as a
+// bit-sliced, temporally blocked sweep.
 //
 // Layout. Global memory keeps the user's Int8 column-major state. A CTA stages its tile
 // plus a halo of K*r cells in shared memory as ONE BIT PER CELL: bit b of word w of a
@@ -21,6 +22,12 @@
 // L is a chain of majority gates, g = maj(v_i, g, m_i) with m_i = 0 where bit i of L is 1
 // and ~0 where it is 0 — one LOP3 per bit with m_i read from the parameter bank.
 //
+// Generations (src/rules.jl:446-456) with C <= 4 states runs in the same kernel with two
+// bit planes per cell (state = lo + 2 hi): the count reads the alive plane lo & ~hi, and the
+// next state is 1 for a born dead cell or a surviving live one, 2 for a live cell that does
+// not survive (C > 2), 3 for a state-2 cell when C = 4, else 0. The host guarantees that
+// every state lies in 0..C-1 (it scans the state on the device after the user writes it).
+//
 // Temporal blocking: K sub-steps per HBM pass; the computed region shrinks by r per
 // sub-step. Periodic and reflecting halos are images of lattice cells and evolve like
 // them; cells beyond a Constant edge are reset to the constant after every sub-step.
@@ -36,6 +43,7 @@ constexpr int kLifeThreads = 256;
 struct LifeTables {
     int32_t n[2];                                // interval counts: [0] dead cells, [1] live cells
     uint32_t m[2][kMaxIntervals][2][8];          // [kind][interval][lo, hi+1][bit] majority masks
+    uint32_t c3, c4;                             // Generations: ~0 when C > 2, when C == 4
 };
 
 struct LifeGeom {
@@ -102,10 +110,9 @@ __device__ __forceinline__ void hcount(const uint32_t* x, uint32_t* h) {
     }
 }
 
-// Hx of one row: p points at the thread's word (guards make p[-1] and p[1] valid).
+// Hx of one row from the thread's word c and its neighbours l, r.
 template <int R>
-__device__ __forceinline__ void hrow(const uint32_t* p, uint32_t* h) {
-    const uint32_t l = p[-1], c = p[0], r = p[1];
+__device__ __forceinline__ void hrow_words(uint32_t l, uint32_t c, uint32_t r, uint32_t* h) {
     uint32_t x[2 * R + 1];
 #pragma unroll
     for (int d = 1; d <= R; ++d) {
@@ -114,6 +121,17 @@ __device__ __forceinline__ void hrow(const uint32_t* p, uint32_t* h) {
     }
     x[R] = c;
     hcount<R>(x, h);
+}
+
+// Hx of one row: p points at the thread's word of plane 0 (guards make p[-1] and p[1]
+// valid); with two planes the counted cells are the alive ones, lo & ~hi.
+template <int R, int PL>
+__device__ __forceinline__ void hrow(const uint32_t* p, int ps, uint32_t* h) {
+    if constexpr (PL == 1) {
+        hrow_words<R>(p[-1], p[0], p[1], h);
+    } else {
+        hrow_words<R>(p[-1] & ~p[ps - 1], p[0] & ~p[ps], p[1] & ~p[ps + 1], h);
+    }
 }
 
 template <int BH, int BV>
@@ -163,19 +181,19 @@ __device__ __forceinline__ uint32_t ge(const uint32_t* v, const uint32_t* m) {
 // NI interval tests per kind, unrolled with no branches; the tables fill unused intervals
 // with an empty one (lo = 1, hi + 1 = 0), which never matches.
 template <int BV, int NI>
-__device__ __forceinline__ uint32_t life_rule(const uint32_t* v, uint32_t c, const LifeTables& tb) {
-    uint32_t dead = 0u, live = 0u;
+__device__ __forceinline__ void rule_hits(const uint32_t* v, const LifeTables& tb, uint32_t& dead, uint32_t& live) {
+    dead = 0u;
+    live = 0u;
 #pragma unroll
     for (int k = 0; k < NI; ++k) {
         dead |= ge<BV>(v, tb.m[0][k][0]) & ~ge<BV>(v, tb.m[0][k][1]);
         live |= ge<BV>(v, tb.m[1][k][0]) & ~ge<BV>(v, tb.m[1][k][1]);
     }
-    return (c & live) | (~c & dead);
 }
 
-template <int R, int NI>
-__device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw, int w,
-                                            int r0, int r1, const LifeTables& tb) {
+template <int R, int NI, int PL>
+__device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw, int ps,
+                                            int w, int r0, int r1, const LifeTables& tb) {
     constexpr int N = LifeBits<R>::N, BH = LifeBits<R>::H, BV = LifeBits<R>::V;
     const uint32_t* ca = A + 1 + w;
     uint32_t* cb = B + 1 + w;
@@ -185,7 +203,7 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
     for (int i = 0; i < BV; ++i) v[i] = 0u;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-        hrow<R>(ca + (r0 - R + k) * sw, ring[k]);
+        hrow<R, PL>(ca + (r0 - R + k) * sw, ps, ring[k]);
         vadd<BH, BV>(v, ring[k]);
     }
     for (int y0 = r0; y0 < r1; y0 += N) {
@@ -193,10 +211,20 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
         for (int k = 0; k < N; ++k) {
             const int y = y0 + k;
             if (y < r1) {
-                cb[y * sw] = life_rule<BV, NI>(v, ca[y * sw], tb);
+                uint32_t dead, live;
+                rule_hits<BV, NI>(v, tb, dead, live);
+                if constexpr (PL == 1) {
+                    const uint32_t c = ca[y * sw];
+                    cb[y * sw] = (c & live) | (~c & dead);
+                } else {  // Generations, state = lo + 2 hi
+                    const uint32_t lo = ca[y * sw], hi = ca[y * sw + ps];
+                    const uint32_t is0 = ~lo & ~hi, is1 = lo & ~hi, is2 = ~lo & hi;
+                    cb[y * sw] = (is0 & dead) | (is1 & live) | (is2 & tb.c4);
+                    cb[y * sw + ps] = (is1 & ~live & tb.c3) | (is2 & tb.c4);
+                }
                 if (y + 1 < r1) {
                     vsub<BH, BV>(v, ring[k]);
-                    hrow<R>(ca + (y + R + 1) * sw, ring[k]);
+                    hrow<R, PL>(ca + (y + R + 1) * sw, ps, ring[k]);
                     vadd<BH, BV>(v, ring[k]);
                 }
             }
@@ -215,6 +243,16 @@ __device__ __forceinline__ uint32_t ones4(uint32_t w) {
 __device__ __forceinline__ uint32_t ones16(int4 q) {
     return ones4((uint32_t)q.x) | (ones4((uint32_t)q.y) << 4) | (ones4((uint32_t)q.z) << 8) |
            (ones4((uint32_t)q.w) << 12);
+}
+
+// Bit `bit` of each of 4 bytes, in bits 0..3 (states 0..3: bit 0 = lo plane, bit 1 = hi).
+__device__ __forceinline__ uint32_t plane4(uint32_t w, int bit) {
+    return (((w >> bit) & 0x01010101u) * 0x10204080u) >> 28;
+}
+
+__device__ __forceinline__ uint32_t plane16(int4 q, int bit) {
+    return plane4((uint32_t)q.x, bit) | (plane4((uint32_t)q.y, bit) << 4) | (plane4((uint32_t)q.z, bit) << 8) |
+           (plane4((uint32_t)q.w, bit) << 12);
 }
 
 // Bits 0..3 of b as four bytes 0/1.
@@ -242,27 +280,62 @@ __device__ __forceinline__ uint32_t load_bits32(const SweepParams& p, const int8
     return bits;
 }
 
-template <int R, int NI>
+// Plane bits (state bit `bit`) of the cells gx .. gx+31 of an already mapped row.
+__device__ __forceinline__ uint32_t load_plane32(const SweepParams& p, const int8_t* __restrict__ row, int64_t gx,
+                                                 int bit) {
+    int64_t a = -1;
+    if (gx >= 0 && gx + 32 <= p.n1) a = gx;
+    else if (p.bnd[0] == GBCA_PERIODIC && (p.n1 & 31) == 0) a = map_axis(GBCA_PERIODIC, gx, p.n1);
+    if (a >= 0) {
+        const int4* q = (const int4*)(row + a);
+        return plane16(q[0], bit) | (plane16(q[1], bit) << 16);
+    }
+    uint32_t bits = 0;
+    for (int b = 0; b < 32; ++b) {
+        const int64_t mx = map_axis(p.bnd[0], gx + b, p.n1);
+        const int v = mx < 0 ? p.cval[0] : row[mx];
+        bits |= (uint32_t)((v >> bit) & 1) << b;
+    }
+    return bits;
+}
+
+template <int R, int NI, int PL>
 __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g, LifeTables tb,
                                                        const int8_t* __restrict__ src, int8_t* __restrict__ dst) {
     extern __shared__ __align__(16) uint32_t smw[];
+    const int ps = g.sw * g.sy;  // words between the planes of one buffer
     uint32_t* A = smw;
-    uint32_t* B = smw + g.sw * g.sy;
+    uint32_t* B = smw + PL * ps;
     const int W = g.tw + 2 * g.hw;
     const int64_t X0 = (int64_t)blockIdx.x * (32 * g.tw) - 32 * g.hw;  // lattice x of local cell 0
     const int64_t Y0 = (int64_t)blockIdx.y * g.ty - g.hy;              // lattice y of local row 0
-    const uint32_t cb0 = p.cval[0] == 1 ? 0xFFFFFFFFu : 0u, cb1 = p.cval[1] == 1 ? 0xFFFFFFFFu : 0u;
+    // the Constant values as plane bits (Life: the indicator; Generations: state bits)
+    uint32_t cb0[PL], cb1[PL];
+#pragma unroll
+    for (int pl = 0; pl < PL; ++pl) {
+        cb0[pl] = PL == 1 ? (p.cval[0] == 1 ? 0xFFFFFFFFu : 0u) : (((p.cval[0] >> pl) & 1) ? 0xFFFFFFFFu : 0u);
+        cb1[pl] = PL == 1 ? (p.cval[1] == 1 ? 0xFFFFFFFFu : 0u) : (((p.cval[1] >> pl) & 1) ? 0xFFFFFFFFu : 0u);
+    }
 
     for (int q = threadIdx.x; q < W * g.sy; q += blockDim.x) {
         const int lw = q % W, ly = q / W;
         const int64_t my = map_axis(p.bnd[1], Y0 + ly, p.n2);
-        const uint32_t bits = my < 0 ? cb1 : load_bits32(p, src + my * p.pitch, X0 + 32 * lw);
-        A[ly * g.sw + 1 + lw] = bits;
-        B[ly * g.sw + 1 + lw] = bits;
+#pragma unroll
+        for (int pl = 0; pl < PL; ++pl) {
+            uint32_t bits;
+            if (my < 0) bits = cb1[pl];
+            else if (PL == 1) bits = load_bits32(p, src + my * p.pitch, X0 + 32 * lw);
+            else bits = load_plane32(p, src + my * p.pitch, X0 + 32 * lw, pl);
+            A[pl * ps + ly * g.sw + 1 + lw] = bits;
+            B[pl * ps + ly * g.sw + 1 + lw] = bits;
+        }
     }
     for (int ly = threadIdx.x; ly < g.sy; ly += blockDim.x) {
-        A[ly * g.sw] = A[ly * g.sw + W + 1] = 0u;
-        B[ly * g.sw] = B[ly * g.sw + W + 1] = 0u;
+#pragma unroll
+        for (int pl = 0; pl < PL; ++pl) {
+            A[pl * ps + ly * g.sw] = A[pl * ps + ly * g.sw + W + 1] = 0u;
+            B[pl * ps + ly * g.sw] = B[pl * ps + ly * g.sw + W + 1] = 0u;
+        }
     }
     // does the loaded region reach beyond a Constant edge?
     const bool fix = (p.bnd[0] == GBCA_CONSTANT && (X0 < 0 || X0 + 32 * W > p.n1)) ||
@@ -279,20 +352,23 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
         if (seg < nseg) {
             const int rows = y_hi - y_lo;
             const int r0 = y_lo + (seg * rows) / nseg, r1 = y_lo + ((seg + 1) * rows) / nseg;
-            if (r1 > r0) life_column<R, NI>(A, B, g.sw, w_lo + threadIdx.x % nw, r0, r1, tb);
+            if (r1 > r0) life_column<R, NI, PL>(A, B, g.sw, ps, w_lo + threadIdx.x % nw, r0, r1, tb);
         }
         __syncthreads();
         if (fix) {
             for (int q = threadIdx.x; q < nw * (y_hi - y_lo); q += blockDim.x) {
                 const int lw = w_lo + q % nw, ly = y_lo + q / nw;
                 const int64_t gy = Y0 + ly, gx = X0 + 32 * lw;
-                uint32_t* wp = B + ly * g.sw + 1 + lw;
-                if (p.bnd[1] == GBCA_CONSTANT && (gy < 0 || gy >= p.n2)) {
-                    *wp = cb1;
-                } else if (p.bnd[0] == GBCA_CONSTANT && (gx < 0 || gx + 32 > p.n1)) {
-                    uint32_t out = 0;
-                    for (int b = 0; b < 32; ++b) out |= (uint32_t)(gx + b < 0 || gx + b >= p.n1) << b;
-                    *wp = (*wp & ~out) | (cb0 & out);
+#pragma unroll
+                for (int pl = 0; pl < PL; ++pl) {
+                    uint32_t* wp = B + pl * ps + ly * g.sw + 1 + lw;
+                    if (p.bnd[1] == GBCA_CONSTANT && (gy < 0 || gy >= p.n2)) {
+                        *wp = cb1[pl];
+                    } else if (p.bnd[0] == GBCA_CONSTANT && (gx < 0 || gx + 32 > p.n1)) {
+                        uint32_t out = 0;
+                        for (int b = 0; b < 32; ++b) out |= (uint32_t)(gx + b < 0 || gx + b >= p.n1) << b;
+                        *wp = (*wp & ~out) | (cb0[pl] & out);
+                    }
                 }
             }
             __syncthreads();
@@ -305,12 +381,20 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
         const int64_t gy = Y0 + ly, gx = X0 + 32 * lw;
         if (gy >= p.n2 || gx >= p.n1) continue;
         const uint32_t bits = A[ly * g.sw + 1 + lw];
+        const uint32_t hib = PL == 2 ? A[ps + ly * g.sw + 1 + lw] : 0u;
         int8_t* out = dst + gy * p.pitch + gx;
         if (gx + 32 <= p.n1) {
-            ((int4*)out)[0] = bytes16(bits);
-            ((int4*)out)[1] = bytes16(bits >> 16);
+            int4 q0 = bytes16(bits), q1 = bytes16(bits >> 16);
+            if (PL == 2) {
+                const int4 h0 = bytes16(hib), h1 = bytes16(hib >> 16);
+                q0 = make_int4(q0.x | (h0.x << 1), q0.y | (h0.y << 1), q0.z | (h0.z << 1), q0.w | (h0.w << 1));
+                q1 = make_int4(q1.x | (h1.x << 1), q1.y | (h1.y << 1), q1.z | (h1.z << 1), q1.w | (h1.w << 1));
+            }
+            ((int4*)out)[0] = q0;
+            ((int4*)out)[1] = q1;
         } else {
-            for (int b = 0; gx + b < p.n1; ++b) out[b] = (int8_t)((bits >> b) & 1u);
+            for (int b = 0; gx + b < p.n1; ++b)
+                out[b] = (int8_t)(((bits >> b) & 1u) | (PL == 2 ? ((hib >> b) & 1u) << 1 : 0u));
         }
     }
 }
@@ -349,39 +433,71 @@ bool make_tables(const SweepParams& p, LifeTables* tb) {
                 for (int i = 0; i < 8; ++i) tb->m[kind][k][j][i] = ((L >> i) & 1) ? 0u : 0xFFFFFFFFu;
             }
     }
+    tb->c3 = p.states > 2 ? 0xFFFFFFFFu : 0u;
+    tb->c4 = p.states == 4 ? 0xFFFFFFFFu : 0u;
     return true;
 }
 
-template <int R, int NI>
+// Tile geometry of a pass of K steps; rows = 0 takes the default height.
+LifeGeom life_geometry(const SweepParams& p, int K, int rows) {
+    LifeGeom g;
+    g.K = K;
+    g.hy = g.K * p.radius;
+    g.hw = (g.hy + 31) / 32;
+    const int64_t words = (p.n1 + 31) / 32;
+    g.tw = words < 32 ? (int)words : 32;
+    int ty = p.rule == GBCA_RULE_GENERATIONS ? 96 : 216;  // two planes: half the rows
+    if (rows > 0) ty = rows;
+    g.ty = p.n2 < ty ? (int)p.n2 : ty;
+    g.sw = g.tw + 2 * g.hw + 2;
+    g.sy = g.ty + 2 * g.hy;
+    return g;
+}
+
+size_t life_smem_bytes(const SweepParams& p, const LifeGeom& g) {
+    const int PL = p.rule == GBCA_RULE_GENERATIONS ? 2 : 1;
+    return 2 * PL * (size_t)g.sw * (size_t)g.sy * 4;
+}
+
+template <int R, int NI, int PL>
 cudaError_t launch_rn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                       cudaStream_t st) {
-    const size_t smem = 2 * (size_t)g.sw * (size_t)g.sy * 4;
-    cudaError_t e = cudaFuncSetAttribute(k_life<R, NI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = life_smem_bytes(p, g);
+    cudaError_t e = cudaFuncSetAttribute(k_life<R, NI, PL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((p.n1 + 32 * g.tw - 1) / (32 * g.tw)), (unsigned)((p.n2 + g.ty - 1) / g.ty));
-    k_life<R, NI><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
+    k_life<R, NI, PL><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
     return cudaGetLastError();
 }
 
-template <int R>
+template <int R, int PL>
 cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                      cudaStream_t st) {
     const int ni = tb.n[0] > tb.n[1] ? tb.n[0] : tb.n[1];
-    if (ni <= 1) return launch_rn<R, 1>(p, g, tb, src, dst, st);
-    if (ni <= 2) return launch_rn<R, 2>(p, g, tb, src, dst, st);
-    return launch_rn<R, kMaxIntervals>(p, g, tb, src, dst, st);
+    if (ni <= 1) return launch_rn<R, 1, PL>(p, g, tb, src, dst, st);
+    if (ni <= 2) return launch_rn<R, 2, PL>(p, g, tb, src, dst, st);
+    return launch_rn<R, kMaxIntervals, PL>(p, g, tb, src, dst, st);
 }
 
 }  // namespace
 
 bool life_simd_supported(const SweepParams& p) {
-    if (p.rule != GBCA_RULE_LIFE || p.nbhd != GBCA_MOORE || p.radius < 1 || p.radius > 5 ||
-        p.scheme != GBCA_SYNCHRONOUS || p.pitch % 16 != 0)
+    if (p.nbhd != GBCA_MOORE || p.radius < 1 || p.scheme != GBCA_SYNCHRONOUS || p.pitch % 16 != 0) return false;
+    if (p.rule == GBCA_RULE_LIFE) {
+        if (p.radius > 5) return false;
+    } else if (p.rule == GBCA_RULE_GENERATIONS) {
+        // two planes hold states 0..3; every state (and Constant value) must lie in 0..C-1
+        if (p.radius > 2 || p.states > 4 || !p.states_valid) return false;
+        for (int a = 0; a < 2; ++a)
+            if (p.bnd[a] == GBCA_CONSTANT && (p.cval[a] < 0 || p.cval[a] >= p.states)) return false;
+    } else {
         return false;
+    }
     LifeTables tb;
     return make_tables(p, &tb);
 }
 
+// Default steps per pass by radius (the halo grows by r per step).
 int life_steps_per_pass(const SweepParams& p) {
     switch (p.radius) {
         case 1: return 16;
@@ -392,24 +508,31 @@ int life_steps_per_pass(const SweepParams& p) {
     }
 }
 
+bool life_choice_fits(const SweepParams& p, int steps, int rows) {
+    if (steps < 1 || rows < 1) return false;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        optin = 227 * 1024;
+    }
+    return life_smem_bytes(p, life_geometry(p, steps, rows)) <= (size_t)optin;
+}
+
 cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st) {
     LifeTables tb;
     if (!make_tables(p, &tb)) return cudaErrorNotSupported;
-    LifeGeom g;
-    g.K = p.nsub;
-    g.hy = g.K * p.radius;
-    g.hw = (g.hy + 31) / 32;
-    const int64_t words = (p.n1 + 31) / 32;
-    g.tw = words < 32 ? (int)words : 32;
-    g.ty = p.n2 < 216 ? (int)p.n2 : 216;
-    g.sw = g.tw + 2 * g.hw + 2;
-    g.sy = g.ty + 2 * g.hy;
+    const LifeGeom g = life_geometry(p, p.nsub, p.tile_y);  // tile_y: the autotuner's pick, or 0
+    if (p.rule == GBCA_RULE_GENERATIONS) {
+        if (p.radius == 1) return launch_r<1, 2>(p, g, tb, src, dst, st);
+        return launch_r<2, 2>(p, g, tb, src, dst, st);
+    }
     switch (p.radius) {
-        case 1: return launch_r<1>(p, g, tb, src, dst, st);
-        case 2: return launch_r<2>(p, g, tb, src, dst, st);
-        case 3: return launch_r<3>(p, g, tb, src, dst, st);
-        case 4: return launch_r<4>(p, g, tb, src, dst, st);
-        default: return launch_r<5>(p, g, tb, src, dst, st);
+        case 1: return launch_r<1, 1>(p, g, tb, src, dst, st);
+        case 2: return launch_r<2, 1>(p, g, tb, src, dst, st);
+        case 3: return launch_r<3, 1>(p, g, tb, src, dst, st);
+        case 4: return launch_r<4, 1>(p, g, tb, src, dst, st);
+        default: return launch_r<5, 1>(p, g, tb, src, dst, st);
     }
 }
 

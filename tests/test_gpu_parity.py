@@ -85,6 +85,15 @@ CASES = [
      (0.1, 0.002)),
     ("forest fire, Stochastic(0.7)", "fire", (64, 80), dict(nb="vn", seed=6, scheme="stoch", sp=0.7), 20, 5,
      (0.2, 0.01)),
+    ("Brian's Brain, tiled torus", "gen", (300, 200), dict(birth=[2], survive=[], states=3), 30, 10, None),
+    ("Generations Moore(2), Constant edges", "gen", (150, 170),
+     dict(r=2, birth=[3, 4, 5], survive=[2, 3, 4, 5, 6], states=4, bnd=("c", "c"), const=(1, 2)), 20, 5, None),
+    ("Generations C=4 reflecting, tiled", "gen", (400, 130),
+     dict(birth=[2], survive=[3, 4, 5], states=4, bnd=("r", "p")), 25, 25, None),
+    ("forest fire, Constant(6) and Constant(2) edges", "fire", (600, 290),
+     dict(nb="vn", seed=4, bnd=("c", "c"), const=(6, 2)), 12, 4, (0.2, 0.01)),
+    ("forest fire, Constant(3) edges", "fire", (280, 130), dict(nb="vn", seed=5, bnd=("c", "p"), const=(3, 0)), 12, 6,
+     (0.2, 0.01)),
     ("forest fire, p = 1 and f = 1", "fire", (520, 300), dict(nb="vn", seed=2, bnd=("c", "c")), 10, 3, (1.0, 1.0)),
     ("forest fire, p = 0, f = 1, Float32", "fire", (300, 260), dict(nb="vn", seed=2, f32=True), 9, 9, (0.0, 1.0)),
     ("forest fire, reflecting edges, tiled", "fire", (700, 300), dict(nb="vn", seed=12, bnd=("r", "p")), 17, 17,
@@ -107,6 +116,44 @@ def test_conformance(ca, oracle, case):
     for k, (a, b) in enumerate(zip(sol.u, us)):
         assert np.array_equal(a, b), f"{name}: save {k} (t = {ts[k]}) differs in {(a != b).sum()} cells"
     assert not np.array_equal(us[-1], u0)
+
+
+def test_fire_states_outside_range(ca, oracle):
+    """A forest-fire state written with values other than 0, 1, 2 (trees in the rule) takes
+    exact byte compares on the first step and bit tests after it."""
+    rng = np.random.default_rng(9)
+    prob = ca.CAProblem.new(ca.ForestFire(), np.zeros((600, 300), np.int8), 20, {"p": 0.1, "f": 0.01},
+                            space=ca.Grid(600, 300), seed=4)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    odd = rng.integers(-4, 8, (600, 300)).astype(np.int8)
+    ca.set_state(B, st, odd)
+    for t in range(20):
+        ca.advance(B, st, prob, ca.Synchronous(), prob.p, t)
+    got = ca.current_state(B, st)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, 600, 300, nbhd=oracle.VON_NEUMANN, seed=4,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    assert np.array_equal(got, oracle.run_array(P, odd, 0, 20, (0.1, 0.01)))
+    st.close()
+
+
+def test_generations_states_outside_range(ca, oracle):
+    """A state written with values outside 0..C-1 (here -3..6 for C = 3) evolves as the
+    reference's rule says (s + 1 < C ? s + 1 : 0 for s not 0 or 1), through the general
+    kernel, and the bit-sliced kernel takes over once every state is valid again."""
+    rng = np.random.default_rng(8)
+    u0 = rng.integers(0, 3, (64, 96)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.Generations(":brians_brain"), u0, 10)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    odd = rng.integers(-3, 7, (64, 96)).astype(np.int8)
+    ca.set_state(B, st, odd)
+    for t in range(12):
+        ca.advance(B, st, prob, ca.Synchronous(), None, t)
+    got = ca.current_state(B, st)
+    P = oracle.Problem(oracle.RULE_GENERATIONS, 64, 96, birth=oracle.mask([2]), survive=0, states=3)
+    assert np.array_equal(got, oracle.run_array(P, odd, 0, 12))
+    st.close()
 
 
 def test_highlife_128_config(ca, oracle):

@@ -1,0 +1,150 @@
+"""The sweep autotuner and pinned geometries: every geometry a fast kernel accepts (steps per
+temporally blocked pass x tile height) gives the oracle's states bit for bit, tuning leaves
+the state as it found it, and a tuned shape keeps its results."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ca():
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.load_package()
+    if m.capi.lib().gbca_device_count() < 1:
+        pytest.fail("no CUDA device visible")
+    return m
+
+
+def _run(ca, prob, st, t0, n, p=None):
+    B = ca.GB300Backend()
+    for t in range(t0, t0 + n):
+        ca.advance(B, st, prob, ca.Synchronous(), p, t)
+    return ca.current_state(B, st)
+
+
+LTL = dict(birth=list(range(34, 46)), survive=list(range(34, 59)))
+
+
+@pytest.mark.parametrize("steps,rows", [(1, 64), (2, 96), (3, 144), (5, 256), (6, 176), (4, 0)])
+def test_ltl_geometries(ca, oracle, steps, rows):
+    """Larger than Life Moore(5) on a 333 x 301 torus, 23 steps (no geometry divides it)."""
+    u0 = np.random.default_rng(steps * 100 + rows).integers(0, 2, (333, 301)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.Life(LTL["birth"], LTL["survive"], neighbourhood=ca.Moore(5)), u0, 23)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, steps, rows)
+    got = _run(ca, prob, st, 0, 23)
+    P = oracle.Problem(oracle.RULE_LIFE, 333, 301, radius=5, birth=oracle.mask(LTL["birth"]),
+                       survive=oracle.mask(LTL["survive"]))
+    assert np.array_equal(got, oracle.run_array(P, u0, 0, 23, nthreads=8))
+    st.close()
+
+
+@pytest.mark.parametrize("steps,rows", [(32, 64), (24, 216), (8, 128), (12, 96)])
+def test_life_constant_edges_geometries(ca, oracle, steps, rows):
+    """HighLife on a 250 x 520 grid with Constant(1) on one axis, 50 steps."""
+    u0 = np.random.default_rng(steps + rows).integers(0, 2, (250, 520)).astype(np.int8)
+    space = ca.Lattice((250, 520), (ca.Periodic(), ca.Constant(1)))
+    prob = ca.CAProblem.new(ca.Life(":highlife"), u0, 50, space=space)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, steps, rows)
+    got = _run(ca, prob, st, 0, 50)
+    P = oracle.Problem(oracle.RULE_LIFE, 250, 520, birth=oracle.mask([3, 6]), survive=oracle.mask([2, 3]),
+                       boundary=(oracle.PERIODIC, oracle.CONSTANT), constant=(0, 1))
+    assert np.array_equal(got, oracle.run_array(P, u0, 0, 50, nthreads=8))
+    st.close()
+
+
+@pytest.mark.parametrize("steps,rows", [(4, 64), (16, 128), (6, 256)])
+def test_generations_geometries(ca, oracle, steps, rows):
+    """Star Wars (C = 4) on a 200 x 330 reflecting lattice, 30 steps."""
+    u0 = np.random.default_rng(rows).integers(0, 4, (200, 330)).astype(np.int8)
+    space = ca.Lattice((200, 330), (ca.Reflecting(), ca.Reflecting()))
+    prob = ca.CAProblem.new(ca.Generations("B2/S345/C4"), u0, 30, space=space)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, steps, rows)
+    got = _run(ca, prob, st, 0, 30)
+    P = oracle.Problem(oracle.RULE_GENERATIONS, 200, 330, birth=oracle.mask([2]), survive=oracle.mask([3, 4, 5]),
+                       states=4, boundary=(oracle.REFLECTING, oracle.REFLECTING))
+    assert np.array_equal(got, oracle.run_array(P, u0, 0, 30, nthreads=8))
+    st.close()
+
+
+@pytest.mark.parametrize("steps", [1, 2, 5, 12, 16])
+def test_fire_geometries(ca, oracle, steps):
+    """Forest fire on a 900 x 410 grid from t = 3, 29 steps."""
+    u0 = np.random.default_rng(steps).integers(0, 3, (900, 410)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 40, {"p": 0.05, "f": 0.002}, space=ca.Grid(900, 410), seed=7)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, steps, 0)
+    got = _run(ca, prob, st, 3, 29, prob.p)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, 900, 410, nbhd=oracle.VON_NEUMANN, seed=7,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    assert np.array_equal(got, oracle.run_array(P, u0, 3, 29, (0.05, 0.002), nthreads=8))
+    st.close()
+
+
+def test_tune_keeps_state_and_results(ca, oracle):
+    """gbca_tune on a 1536 x 1280 Life torus: the state is unchanged, the choice is a
+    candidate, and the tuned sweep still matches the oracle."""
+    u0 = np.random.default_rng(11).integers(0, 2, (1536, 1280)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.Life(":conway"), u0, 40)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    k, rows = ca.tune(st, prob)
+    assert k in (8, 12, 16, 24, 32) and rows in (64, 96, 128, 144, 176, 216, 256)
+    assert np.array_equal(ca.current_state(B, st), u0)
+    got = _run(ca, prob, st, 0, 40)
+    P = oracle.Problem(oracle.RULE_LIFE, 1536, 1280, birth=oracle.mask([3]), survive=oracle.mask([2, 3]))
+    assert np.array_equal(got, oracle.run_array(P, u0, 0, 40, nthreads=16))
+    st.close()
+    # a second handle of the same shape uses the cached choice
+    st2 = ca.allocate_state(B, prob, ca.Synchronous())
+    assert np.array_equal(_run(ca, prob, st2, 0, 40), got)
+    st2.close()
+    ca.capi.check(ca.capi.lib().gbca_forget_tuning())
+
+
+def test_tune_fire_and_general(ca, oracle):
+    u0 = np.random.default_rng(12).integers(0, 3, (1000, 600)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 20, {"p": 0.05, "f": 0.002}, space=ca.Grid(1000, 600), seed=3)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    k, rows = ca.tune(st, prob)
+    assert k in (2, 4, 6, 8, 12) and rows == 0
+    assert np.array_equal(ca.current_state(B, st), u0)
+    got = _run(ca, prob, st, 0, 20, prob.p)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, 1000, 600, nbhd=oracle.VON_NEUMANN, seed=3,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    assert np.array_equal(got, oracle.run_array(P, u0, 0, 20, (0.05, 0.002), nthreads=16))
+    st.close()
+    # von Neumann Life runs on the general kernel: nothing to tune, no geometry to pin
+    prob2 = ca.CAProblem.new(ca.Life([2, 3], [1, 2], neighbourhood=ca.VonNeumann(1)),
+                             np.zeros((64, 64), np.int8), 5)
+    st2 = ca.allocate_state(B, prob2, ca.Synchronous())
+    assert ca.tune(st2, prob2) == (0, 0)
+    with pytest.raises(ca.UnsupportedCombinationError):
+        ca.set_geometry(st2, 4, 0)
+    st2.close()
+    ca.capi.check(ca.capi.lib().gbca_forget_tuning())
+
+
+def test_geometry_refusals(ca):
+    B = ca.GB300Backend()
+    fire = ca.CAProblem.new(ca.ForestFire(), np.zeros((64, 64), np.int8), 5, {"p": 0.1, "f": 0.0})
+    st = ca.allocate_state(B, fire, ca.Synchronous())
+    with pytest.raises(ca.ArgumentError):
+        ca.set_geometry(st, 4, 128)  # the fire kernel's tile height is fixed
+    with pytest.raises(ca.ArgumentError):
+        ca.set_geometry(st, 0, 16)
+    with pytest.raises(ca.ArgumentError):
+        ca.set_geometry(st, 65, 0)
+    st.close()
+    ltl = ca.CAProblem.new(ca.Life(LTL["birth"], LTL["survive"], neighbourhood=ca.Moore(5)),
+                           np.zeros((4096, 4096), np.int8), 5)
+    st = ca.allocate_state(B, ltl, ca.Synchronous())
+    with pytest.raises(ca.ArgumentError):
+        ca.set_geometry(st, 6, 4000)  # far beyond shared memory
+    ca.set_geometry(st, 0, 0)
+    st.close()
