@@ -607,6 +607,12 @@ def main():
                 "peak_source": peak_src, "kernel": kernel, "traffic": profiled_traffic(kernel)}
     for name in parts:
         parts[name]["hbm_frac_per_effective_step"] = parts[name]["achieved_gbs"] / peak
+    # the forest fire's compute roof: one Philox4x32-10 draw per cell-update, measured alone
+    rate = ctypes.c_double()
+    capi.check(lib.gbca_philox_rate(20_000_000_000, ctypes.byref(rate)))
+    fire_draws = parts["fire"]["gcell_updates_s"] * 1e9
+    philox_roof = {"kernel": "k_fire", "achieved": fire_draws / 1e9, "peak": rate.value / 1e9, "unit": "Gdraws/s",
+                   "frac": fire_draws / rate.value, "peak_source": "measured in this run (draw-only kernel)"}
 
     # ---- end to end through the C ABI with host buffers
     host_in = [torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory() for a in (ltl0, fire0)]
@@ -659,7 +665,7 @@ def main():
                            "geometry": {k: {"steps_per_pass": v[0], "tile_rows": v[1]} for k, v in geometry.items()},
                            "l2": "inputs larger than L2: the 16384^2 state is 268 MB, and each step re-copies "
                                  "335 MB of initial states"},
-                "roofline": roofline, "parts": parts, "e2e": e2e, "gpu_launches": launches,
+                "roofline": roofline, "philox_roof": philox_roof, "parts": parts, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks.summary(), "cpu_baseline": cpu, "batched": batched, "served": served}
         print(json.dumps(line))
     if dist is not None:

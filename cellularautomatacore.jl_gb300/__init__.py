@@ -9,9 +9,10 @@ from .backend import (GB300Backend, GB300State, advance, allocate_state, check_p
                       device_summaries, read_cell, set_geometry, set_state, supports, tune, write_cell)
 from .errors import (ArgumentError, GPUError, IncompatibleSpaceError, InvalidStateError, RuleParseError,
                      StateShapeError, UnsupportedCombinationError)
-from .model import (GENERATIONS_PRESETS, LIFE_PRESETS, Checkerboard, Constant, ForestFire, Generations, Grid,
-                    Lattice, Lenia, Life, Moore, Periodic, Reflecting, Stochastic, Synchronous, Torus, VonNeumann,
-                    neighbourhood_offsets)
+from .model import (GENERATIONS_PRESETS, LIFE_PRESETS, AnisotropicKernel, Checkerboard, Constant, EmpiricalKernel,
+                    ExponentialKernel, ForestFire, GaussianKernel, Generations, Grid, KernelField, KernelSI, Lattice,
+                    Lenia, LeniaKernel, Life, Moore, Periodic, PowerLawKernel, Reflecting, Stochastic, Synchronous,
+                    Torus, UniformKernel, VonNeumann, kernel_weights, neighbourhood_offsets)
 from .problem import (CAProblem, CASolution, DiscreteCallback, EnsembleProblem, final_state, init, reinit, remake,
                       seed_trajectory, solve, solve_ensemble_serial, solve_integrator, step)
 

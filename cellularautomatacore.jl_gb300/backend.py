@@ -22,8 +22,8 @@ import numpy as np
 
 from . import capi
 from .errors import ArgumentError, IncompatibleSpaceError, StateShapeError
-from .model import (Checkerboard, Constant, ForestFire, Generations, Lattice, Lenia, Life, Moore, Stochastic,
-                    Synchronous, VonNeumann)
+from .model import (Checkerboard, Constant, ForestFire, Generations, KernelSI, Lattice, Lenia, Life, Moore,
+                    Stochastic, Synchronous, VonNeumann)
 
 
 class GB300Backend:
@@ -46,7 +46,17 @@ def supports(backend, scheme) -> bool:
 
 
 def _params_tuple(rule, p):
-    """The rule's numbers from the integrator's p: forest fire reads p.p and p.f."""
+    """The rule's numbers from the integrator's p: forest fire reads p.p and p.f, the
+    kernel-field SI rule p.β (or p.beta)."""
+    if isinstance(rule, KernelSI):
+        if p is None:
+            raise ArgumentError("the kernel-field SI rule needs its parameter β")
+        if isinstance(p, dict):
+            beta = p["β"] if "β" in p else p["beta"]
+        else:
+            beta = getattr(p, "β", None)
+            beta = getattr(p, "beta") if beta is None else beta
+        return (float(np.float32(beta)) if rule.float32 else float(beta),)
     if not isinstance(rule, ForestFire):
         return ()
     if p is None:
@@ -102,6 +112,12 @@ def make_desc(prob, scheme) -> capi.Desc:
         d.rule, d.birth, d.survive, d.states = capi.RULE_GENERATIONS, rule.birth, rule.survive, rule.states
     elif isinstance(rule, ForestFire):
         d.rule, d.params_f32 = capi.RULE_FOREST_FIRE, int(rule.float32)
+    elif isinstance(rule, KernelSI):
+        d.rule, d.params_f32 = capi.RULE_SI_FIELD, int(rule.float32)
+        if rule.field not in prob.fields:
+            raise ArgumentError(f"the rule reads field :{rule.field}, which the problem does not define")
+        if rule.covariate is not None and rule.covariate not in prob.covariates:
+            raise ArgumentError(f"the rule reads covariate :{rule.covariate}, which the problem does not define")
     else:
         raise ArgumentError(f"GB300Backend cannot run {type(rule).__name__}: arbitrary LocalRules cannot cross "
                             "the C ABI; use Life, Generations, ForestFire or Lenia")
@@ -145,10 +161,36 @@ class GB300State:
         return self.dims[0] * self.dims[1] * self.dtype.itemsize
 
 
+def _attach_environment(st: GB300State, prob) -> None:
+    """The problem's mask, the SI rule's kernel field and covariate, on the device."""
+    L = capi.lib()
+    if prob.mask is not None:
+        if st.desc.rule == capi.RULE_LENIA:
+            raise ArgumentError("GB300Backend runs masks with Int8 rules only")
+        m = np.asfortranarray(np.asarray(prob.mask, dtype=np.uint8))
+        capi.check(L.gbca_set_mask(st.handle, m.ctypes.data, m.nbytes))
+    rule = prob.rule
+    if isinstance(rule, KernelSI):
+        f = prob.fields[rule.field]
+        taps, weights, _ = f.resolve(prob.space, rule.field)
+        t = np.ascontiguousarray(np.asarray(taps, dtype=np.int32).reshape(-1))
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        capi.check(L.gbca_set_field(st.handle, len(w), t.ctypes.data, w.ctypes.data, int(f.precision == "Float32"),
+                                    capi.SOURCE_INDICATOR if f.source == "x == 1" else capi.SOURCE_IDENTITY,
+                                    capi.FFT if f.method == "fft" else capi.DIRECT))
+        if rule.covariate is not None:
+            c = np.asarray(prob.covariates[rule.covariate])
+            f32 = c.dtype == np.float32
+            c = np.asfortranarray(c.astype(np.float32 if f32 else np.float64, copy=False))
+            nt = c.shape[2] if c.ndim == 3 else 1
+            capi.check(L.gbca_set_covariate(st.handle, c.ctypes.data, nt, int(f32)))
+
+
 def allocate_state(backend, prob, scheme) -> GB300State:
     d = make_desc(prob, scheme)
     dtype = (np.float64 if d.lenia_f64 else np.float32) if d.rule == capi.RULE_LENIA else np.int8
     st = GB300State(d, dtype)
+    _attach_environment(st, prob)
     set_state(backend, st, prob.u0)
     return st
 

@@ -11,7 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libgbca.so")
 
 OK, ERR_ARGUMENT, ERR_INCOMPATIBLE_SPACE, ERR_UNSUPPORTED, ERR_STATE, ERR_CUDA, ERR_OOM, ERR_TIMEOUT, ERR_BUSY = range(9)
-RULE_LIFE, RULE_GENERATIONS, RULE_FOREST_FIRE, RULE_LENIA = 1, 2, 3, 4
+RULE_LIFE, RULE_GENERATIONS, RULE_FOREST_FIRE, RULE_LENIA, RULE_SI_FIELD = 1, 2, 3, 4, 5
+SOURCE_INDICATOR, SOURCE_IDENTITY = 0, 1
 MOORE, VON_NEUMANN = 1, 2
 PERIODIC, REFLECTING, CONSTANT = 0, 1, 2
 SYNCHRONOUS, STOCHASTIC, CHECKERBOARD = 0, 1, 2
@@ -71,6 +72,10 @@ SIGNATURES = {
     "gbca_kernel_launches": (ctypes.c_int64, []),
     "gbca_tune": (ctypes.c_int, [_V, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_int32), _P(ctypes.c_int32)]),
     "gbca_forget_tuning": (ctypes.c_int, []),
+    "gbca_set_mask": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
+    "gbca_set_field": (ctypes.c_int, [_V, ctypes.c_int32, _V, _V, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "gbca_set_covariate": (ctypes.c_int, [_V, _V, _I64, ctypes.c_int32]),
+    "gbca_philox_rate": (ctypes.c_int, [_I64, _P(ctypes.c_double)]),
     "gbca_set_geometry": (ctypes.c_int, [_V, ctypes.c_int32, ctypes.c_int32]),
     "gbca_threshold": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_int32]),
     "gbca_ensemble_create": (ctypes.c_int, [_P(Desc), ctypes.c_int32, _P(_V)]),

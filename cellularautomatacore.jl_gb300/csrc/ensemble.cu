@@ -438,6 +438,8 @@ int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out)
         int rc = gbca_check(&d);
         if (rc != GBCA_OK) return rc;
         if (d.rule == GBCA_RULE_LENIA) return efail(GBCA_ERR_UNSUPPORTED, "ensemble instance %d: Lenia is not batched", i);
+        if (d.rule == GBCA_RULE_SI_FIELD)
+            return efail(GBCA_ERR_UNSUPPORTED, "ensemble instance %d: kernel-field rules are not batched", i);
         if (d.scheme != GBCA_SYNCHRONOUS)
             return efail(GBCA_ERR_UNSUPPORTED, "ensemble instance %d: batched ensembles run Synchronous()", i);
         if (d.radius > kEnsMaxHalo)

@@ -1,5 +1,6 @@
 // gbca_api.cu — the C ABI of libgbca.so (include/gbca.h): handles, state transfer,
 // advance with kernel selection, single-cell access and device summaries.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -7,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "field.cuh"
 #include "gbca_internal.cuh"
 #include "lenia.cuh"
 #include "measures.cuh"
@@ -26,6 +28,16 @@ struct gbca_handle {
     bool states_valid = true;  // every state is one the rule produces (see scan_states)
     bool forced = false;       // gbca_set_geometry pinned the sweep geometry
     gbca::SweepChoice force = {0, 0};
+    // the environment (gbca_set_mask / gbca_set_field / gbca_set_covariate)
+    uint8_t* mask = nullptr;           // pitch bytes between columns
+    int2* taps = nullptr;
+    double* w64 = nullptr;
+    float* w32 = nullptr;
+    int32_t ntaps = 0, field_R = 0, field_f32 = 0, field_source = 0;
+    gbca::FieldFFT* field_fft = nullptr;
+    void* cov = nullptr;
+    int64_t cov_nt = 0;
+    int32_t cov_f32 = 0;
 };
 
 namespace {
@@ -53,13 +65,14 @@ int cuda_fail(cudaError_t e, const char* what) {
     } while (0)
 
 bool is_int8_rule(int32_t r) {
-    return r == GBCA_RULE_LIFE || r == GBCA_RULE_GENERATIONS || r == GBCA_RULE_FOREST_FIRE;
+    return r == GBCA_RULE_LIFE || r == GBCA_RULE_GENERATIONS || r == GBCA_RULE_FOREST_FIRE || r == GBCA_RULE_SI_FIELD;
 }
 
 int check_desc(const gbca_desc* d) {
     if (!d) return fail(GBCA_ERR_ARGUMENT, "null problem description");
-    if (d->rule < GBCA_RULE_LIFE || d->rule > GBCA_RULE_LENIA)
-        return fail(GBCA_ERR_ARGUMENT, "GB300Backend runs Life, Generations, forest-fire and Lenia rules; got rule kind %d",
+    if (d->rule < GBCA_RULE_LIFE || d->rule > GBCA_RULE_SI_FIELD)
+        return fail(GBCA_ERR_ARGUMENT,
+                    "GB300Backend runs Life, Generations, forest-fire, kernel-field SI and Lenia rules; got rule kind %d",
                     d->rule);
     if (d->n1 <= 0 || d->n2 <= 0)
         return fail(GBCA_ERR_ARGUMENT, "lattice dimensions must be positive, got (%lld, %lld)", (long long)d->n1,
@@ -151,14 +164,51 @@ int ensure_scanned(gbca_handle* h) {
     return GBCA_OK;
 }
 
+int advance_si(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams) {
+    if (!params || nparams < 1) return fail(GBCA_ERR_ARGUMENT, "the kernel-field SI rule needs its parameter beta");
+    if (h->ntaps < 1) return fail(GBCA_ERR_ARGUMENT, "the kernel-field SI rule needs a field (gbca_set_field)");
+    gbca::FieldSweep p;
+    std::memset(&p, 0, sizeof p);
+    p.n1 = h->d.n1;
+    p.n2 = h->d.n2;
+    p.pitch = h->pitch;
+    for (int a = 0; a < 2; ++a) {
+        p.bnd[a] = h->d.boundary[a];
+        p.cval[a] = h->d.boundary[a] == GBCA_CONSTANT ? (int32_t)h->d.constant[a] : 0;
+    }
+    p.seed = h->d.seed;
+    p.scheme = h->d.scheme;
+    p.gate_f32 = h->d.scheme_p_f32;
+    p.gate_thr = h->d.scheme == GBCA_STOCHASTIC ? threshold(h->d.scheme_p, h->d.scheme_p_f32 != 0) : 0;
+    p.mask = h->mask;
+    p.taps = h->taps;
+    p.w64 = h->w64;
+    p.w32 = h->w32;
+    p.ntaps = h->ntaps;
+    p.R = h->field_R;
+    p.field_f32 = h->field_f32;
+    p.source = h->field_source;
+    p.cov = h->cov;
+    p.cov_nt = h->cov_nt;
+    p.cov_f32 = h->cov_f32;
+    p.beta_f32 = h->d.params_f32;
+    p.beta = h->d.params_f32 ? (double)(float)params[0] : params[0];
+    int8_t* const bufs[2] = {(int8_t*)h->buf[0], (int8_t*)h->buf[1]};
+    const cudaError_t e = gbca::sweep_si(p, h->field_fft, bufs, &h->cur, t, nsteps, h->nsm, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel-field sweep");
+    return GBCA_OK;
+}
+
 int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams) {
+    if (h->d.rule == GBCA_RULE_SI_FIELD) return advance_si(h, t, nsteps, params, nparams);
     if (h->d.rule == GBCA_RULE_FOREST_FIRE && (!params || nparams < 2))
         return fail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
     const int rc = ensure_scanned(h);
     if (rc != GBCA_OK) return rc;
     int8_t* const bufs[2] = {(int8_t*)h->buf[0], (int8_t*)h->buf[1]};
     const cudaError_t e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, t, nsteps, params, h->stream,
-                                           scanned_rule(h) && h->states_valid, h->forced ? &h->force : nullptr);
+                                           scanned_rule(h) && h->states_valid, h->forced ? &h->force : nullptr,
+                                           h->mask);
     if (h->d.rule == GBCA_RULE_FOREST_FIRE) h->states_valid = true;  // a step leaves only 0, 1 and 2
     if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
     return GBCA_OK;
@@ -168,6 +218,7 @@ int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
 gbca::SweepParams handle_params(const gbca_handle* h, const double* params) {
     gbca::SweepParams p = gbca::sweep_params(h->d, h->pitch, params);
     p.states_valid = scanned_rule(h) && h->states_valid ? 1 : 0;
+    p.mask = h->mask;
     return p;
 }
 
@@ -196,7 +247,8 @@ int time_candidates(gbca_handle* h, const std::vector<gbca::SweepChoice>& cands,
             e = cudaMemcpyAsync(h->buf[cur0], saved, bytes, cudaMemcpyDeviceToDevice, h->stream);
             if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
             if (e == cudaSuccess)
-                e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, 1, nsteps, params, h->stream, valid, &cands[c]);
+                e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, 1, nsteps, params, h->stream, valid, &cands[c],
+                                     h->mask);
             if (e == cudaSuccess) e = cudaEventRecord(ev[1], h->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
             float ms = 0.0f;
@@ -303,6 +355,12 @@ int gbca_destroy(gbca_handle* h) {
     cudaFree(h->buf[0]);
     cudaFree(h->buf[1]);
     cudaFree(h->acc);
+    cudaFree(h->mask);
+    cudaFree(h->taps);
+    cudaFree(h->w64);
+    cudaFree(h->w32);
+    cudaFree(h->cov);
+    gbca::field_fft_destroy(h->field_fft);
     if (h->acc_host) cudaFreeHost(h->acc_host);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -360,7 +418,7 @@ int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* st
     if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
     if (steps_per_pass) *steps_per_pass = 0;
     if (tile_rows) *tile_rows = 0;
-    if (h->d.rule == GBCA_RULE_LENIA) return GBCA_OK;  // nothing to tune
+    if (h->d.rule == GBCA_RULE_LENIA || h->d.rule == GBCA_RULE_SI_FIELD) return GBCA_OK;  // nothing to tune
     if (h->d.rule == GBCA_RULE_FOREST_FIRE && (!params || nparams < 2))
         return fail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
     int rc = ensure_scanned(h);
@@ -390,8 +448,8 @@ int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows)
     if (steps_per_pass < 1 || steps_per_pass > 64 || tile_rows < 0)
         return fail(GBCA_ERR_ARGUMENT, "steps per pass must lie in 1..64 and tile rows be non-negative, got %d, %d",
                     (int)steps_per_pass, (int)tile_rows);
-    if (h->d.rule == GBCA_RULE_LENIA)
-        return fail(GBCA_ERR_UNSUPPORTED, "sweep geometry applies to the Int8 sweep kernels, not to Lenia");
+    if (h->d.rule == GBCA_RULE_LENIA || h->d.rule == GBCA_RULE_SI_FIELD)
+        return fail(GBCA_ERR_UNSUPPORTED, "sweep geometry applies to the Int8 stencil kernels only");
     const int rc = ensure_scanned(h);
     if (rc != GBCA_OK) return rc;
     const gbca::SweepParams p = handle_params(h, nullptr);
@@ -407,6 +465,93 @@ int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows)
     h->force.steps_per_pass = steps_per_pass;
     h->force.tile_rows = tile_rows;
     h->forced = true;
+    return GBCA_OK;
+}
+
+int gbca_set_mask(gbca_handle* h, const uint8_t* host, size_t nbytes) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (h->d.rule == GBCA_RULE_LENIA) return fail(GBCA_ERR_UNSUPPORTED, "GB300Backend runs masks with Int8 rules only");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_mask");
+    if (!host) {
+        cudaFree(h->mask);
+        h->mask = nullptr;
+        return GBCA_OK;
+    }
+    const size_t n1 = (size_t)h->d.n1, n2 = (size_t)h->d.n2;
+    if (nbytes != n1 * n2) return fail(GBCA_ERR_STATE, "the mask has %zu cells, the lattice %zu", nbytes, n1 * n2);
+    if (!h->mask) GBCA_CUDA(cudaMalloc(&h->mask, (size_t)h->pitch * n2), "mask allocation");
+    GBCA_CUDA(cudaMemcpy2DAsync(h->mask, (size_t)h->pitch, host, n1, n1, n2, cudaMemcpyHostToDevice, h->stream),
+              "mask copy");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_mask");
+    return GBCA_OK;
+}
+
+int gbca_set_field(gbca_handle* h, int32_t ntaps, const int32_t* taps, const double* weights, int32_t f32,
+                   int32_t source, int32_t method) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (h->d.rule != GBCA_RULE_SI_FIELD)
+        return fail(GBCA_ERR_UNSUPPORTED, "only the kernel-field SI rule reads a kernel field");
+    if (ntaps < 1 || !taps || !weights) return fail(GBCA_ERR_ARGUMENT, "a kernel field needs at least one tap");
+    if (source != GBCA_SOURCE_INDICATOR && source != GBCA_SOURCE_IDENTITY)
+        return fail(GBCA_ERR_ARGUMENT, "unknown field source %d", (int)source);
+    if (method != GBCA_DIRECT && method != GBCA_FFT) return fail(GBCA_ERR_ARGUMENT, "method must be direct or fft");
+    int R = 0;
+    for (int k = 0; k < 2 * ntaps; ++k) R = std::max(R, std::abs(taps[k]));
+    if (method == GBCA_DIRECT && R > 64)
+        return fail(GBCA_ERR_UNSUPPORTED, "direct kernel fields reach at most 64 cells, this one %d; use method=:fft", R);
+    if (method == GBCA_FFT && (h->d.boundary[0] != GBCA_PERIODIC || h->d.boundary[1] != GBCA_PERIODIC))
+        return fail(GBCA_ERR_ARGUMENT, "a field with method=:fft needs periodic boundaries on every axis");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_field");
+    cudaFree(h->taps);
+    cudaFree(h->w64);
+    cudaFree(h->w32);
+    gbca::field_fft_destroy(h->field_fft);
+    h->taps = nullptr;
+    h->w64 = nullptr;
+    h->w32 = nullptr;
+    h->field_fft = nullptr;
+    h->ntaps = 0;
+    std::vector<int2> t2((size_t)ntaps);
+    std::vector<float> wf((size_t)ntaps);
+    for (int k = 0; k < ntaps; ++k) {
+        t2[k] = make_int2(taps[2 * k], taps[2 * k + 1]);
+        wf[k] = (float)weights[k];
+    }
+    GBCA_CUDA(cudaMalloc(&h->taps, sizeof(int2) * ntaps), "field allocation");
+    GBCA_CUDA(cudaMalloc(&h->w64, sizeof(double) * ntaps), "field allocation");
+    GBCA_CUDA(cudaMalloc(&h->w32, sizeof(float) * ntaps), "field allocation");
+    GBCA_CUDA(cudaMemcpyAsync(h->taps, t2.data(), sizeof(int2) * ntaps, cudaMemcpyHostToDevice, h->stream), "field copy");
+    GBCA_CUDA(cudaMemcpyAsync(h->w64, weights, sizeof(double) * ntaps, cudaMemcpyHostToDevice, h->stream), "field copy");
+    GBCA_CUDA(cudaMemcpyAsync(h->w32, wf.data(), sizeof(float) * ntaps, cudaMemcpyHostToDevice, h->stream), "field copy");
+    if (method == GBCA_FFT) {
+        std::vector<int> tv(taps, taps + 2 * ntaps);
+        std::vector<double> wv(weights, weights + ntaps);
+        const int rc = gbca::field_fft_create(h->d.n1, h->d.n2, tv, wv, f32 != 0, h->stream, &h->field_fft, g_err);
+        if (rc != GBCA_OK) return rc;
+    }
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_field");
+    h->ntaps = ntaps;
+    h->field_R = R;
+    h->field_f32 = f32 != 0;
+    h->field_source = source;
+    return GBCA_OK;
+}
+
+int gbca_set_covariate(gbca_handle* h, const void* host, int64_t nt, int32_t f32) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (h->d.rule != GBCA_RULE_SI_FIELD) return fail(GBCA_ERR_UNSUPPORTED, "only the kernel-field SI rule reads a covariate");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_covariate");
+    cudaFree(h->cov);
+    h->cov = nullptr;
+    h->cov_nt = 0;
+    if (!host) return GBCA_OK;
+    if (nt < 1) return fail(GBCA_ERR_ARGUMENT, "a covariate needs at least one time slice, got %lld", (long long)nt);
+    const size_t bytes = (size_t)h->d.n1 * (size_t)h->d.n2 * (size_t)nt * (f32 ? sizeof(float) : sizeof(double));
+    GBCA_CUDA(cudaMalloc(&h->cov, bytes), "covariate allocation");
+    GBCA_CUDA(cudaMemcpyAsync(h->cov, host, bytes, cudaMemcpyHostToDevice, h->stream), "covariate copy");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_covariate");
+    h->cov_nt = nt;
+    h->cov_f32 = f32 != 0;
     return GBCA_OK;
 }
 

@@ -164,6 +164,7 @@ struct SweepParams {
     int32_t states_valid;      // every state is known to be one the rule produces (Generations
                                // 0..C-1, forest fire 0..2)
     int32_t pad_;
+    const uint8_t* mask;       // nonzero = the cell updates (pitch bytes between columns), or null
 };
 
 // The message gbca_last_error() returns on this thread.
@@ -185,9 +186,10 @@ struct SweepChoice {
 // states_valid: every state is known to be one the rule produces (Generations: 0..C-1,
 // enabling the bit-sliced kernel; forest fire: 0..2, enabling bit tests on the first step).
 // force: use this geometry instead of the autotuner's cached pick (tune.cu).
+// mask: cells whose byte is 0 keep their state (general kernel only).
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
                        const double* params, cudaStream_t st, bool states_valid = false,
-                       const SweepChoice* force = nullptr);
+                       const SweepChoice* force = nullptr, const uint8_t* mask = nullptr);
 
 // The autotuner's cached choice for a problem shape (tune.cu); false when it has none.
 bool tuned_choice(const gbca_desc& d, SweepChoice* out);

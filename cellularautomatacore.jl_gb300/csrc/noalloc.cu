@@ -75,6 +75,8 @@ extern "C" int gbca_advance_noalloc(const gbca_desc* desc, void* state, int64_t 
     if (rc != GBCA_OK) return rc;
     if (desc->rule == GBCA_RULE_LENIA)
         return nfail(GBCA_ERR_UNSUPPORTED, "gbca_advance_noalloc runs the Int8 rules; Lenia's FFT plans allocate");
+    if (desc->rule == GBCA_RULE_SI_FIELD)
+        return nfail(GBCA_ERR_UNSUPPORTED, "gbca_advance_noalloc runs no kernel-field rule (its field is set on a handle)");
     if (!state) return nfail(GBCA_ERR_ARGUMENT, "null state");
     if (((uintptr_t)state & 15u) != 0) return nfail(GBCA_ERR_ARGUMENT, "the state must be 16-byte aligned");
     if (pitch < desc->n1) return nfail(GBCA_ERR_ARGUMENT, "pitch %lld is below n1 = %lld", (long long)pitch,

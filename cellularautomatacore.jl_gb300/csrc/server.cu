@@ -458,7 +458,7 @@ int gbca_server_submit(gbca_server* S, const gbca_desc* d, const void* u0, size_
     if (!S || !d) return sfail(GBCA_ERR_ARGUMENT, "null server or problem");
     const int rc = gbca_check(d);
     if (rc != GBCA_OK) return rc;
-    if (d->rule == GBCA_RULE_LENIA || d->scheme != GBCA_SYNCHRONOUS || d->radius > 8)
+    if (d->rule == GBCA_RULE_LENIA || d->rule == GBCA_RULE_SI_FIELD || d->scheme != GBCA_SYNCHRONOUS || d->radius > 8)
         return sfail(GBCA_ERR_UNSUPPORTED, "the server runs Int8 rules, Synchronous(), radius <= 8");
     if (nsteps < 0) return sfail(GBCA_ERR_ARGUMENT, "negative step count");
     if (d->rule == GBCA_RULE_FOREST_FIRE && (!params || nparams < 2))

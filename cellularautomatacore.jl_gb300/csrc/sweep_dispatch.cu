@@ -38,9 +38,11 @@ SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params
 }
 
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
-                       const double* params, cudaStream_t st, bool states_valid, const SweepChoice* force) {
+                       const double* params, cudaStream_t st, bool states_valid, const SweepChoice* force,
+                       const uint8_t* mask) {
     SweepParams p = sweep_params(d, pitch, params);
     p.states_valid = states_valid ? 1 : 0;
+    p.mask = mask;
     const bool fire = fire_fast_supported(p);
     const bool life = !fire && life_simd_supported(p);
     SweepChoice choice = {0, 0};

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY) k_fire(SweepPara
 }  // namespace
 
 bool fire_fast_supported(const SweepParams& p) {
-    return p.rule == GBCA_RULE_FOREST_FIRE && p.nbhd == GBCA_VON_NEUMANN && p.radius == 1 &&
+    return !p.mask && p.rule == GBCA_RULE_FOREST_FIRE && p.nbhd == GBCA_VON_NEUMANN && p.radius == 1 &&
            p.scheme == GBCA_SYNCHRONOUS && p.n1 * p.n2 < ((int64_t)1 << 32) - 1 && p.pitch % 16 == 0;
 }
 

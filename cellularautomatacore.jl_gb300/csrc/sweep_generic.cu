@@ -9,7 +9,8 @@
 // per-cell update of src/backends.jl:444-455 over a region that shrinks by r per
 // sub-step, and writes the tile once. Cells of the halo that are periodic or reflected
 // images of lattice cells are updated with the id (hence the draws and the checkerboard
-// parity) of the cell they image; cells beyond a Constant edge keep the constant.
+// parity) of the cell they image; cells beyond a Constant edge keep the constant. Masked
+// cells (src/environment.jl:123-130) keep their state, images included.
 #include "gbca_internal.cuh"
 
 namespace gbca {
@@ -109,6 +110,10 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
                 }
             }
             const int8_t c = A[ly * sx + lx];
+            if (p.mask && !p.mask[mx + my * p.pitch]) {  // a masked cell keeps its state
+                B[ly * sx + lx] = c;
+                continue;
+            }
             const uint64_t id = (uint64_t)mx + (uint64_t)my * (uint64_t)p.n1 + 1u;
             bool open = true;  // src/schemes.jl:84-89
             if (p.scheme == GBCA_STOCHASTIC)

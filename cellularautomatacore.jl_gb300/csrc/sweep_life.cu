@@ -482,6 +482,7 @@ cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& 
 }  // namespace
 
 bool life_simd_supported(const SweepParams& p) {
+    if (p.mask) return false;
     if (p.nbhd != GBCA_MOORE || p.radius < 1 || p.scheme != GBCA_SYNCHRONOUS || p.pitch % 16 != 0) return false;
     if (p.rule == GBCA_RULE_LIFE) {
         if (p.radius > 5) return false;

@@ -6,6 +6,7 @@ lattices, Moore(r) / VonNeumann(r), Life / Generations / the forest-fire rule on
 states and Lenia on Float32 states."""
 from __future__ import annotations
 
+import math
 import re
 from dataclasses import dataclass, field
 
@@ -284,6 +285,204 @@ class Lenia:
 
     def __repr__(self):
         return f"Lenia(R={self.R}, μ={self.mu}, σ={self.sigma}, dt={self.dt})"
+
+
+class KernelSI:
+    """The kernel-field SI epidemic of the reference's conformance battery
+    (test/backend_conformance.jl:52-57 with a covariate, :72-75 in Float32) as a typed rule,
+    on Int8 states:
+
+        cell == 1 -> 1
+        otherwise -> bernoulli(ctx, 1 - exp(-p.β * covariate(ctx, cov) * field(ctx, name))) ? 1 : cell
+
+    `field` names a KernelField of the problem, `covariate` a covariate (None: the factor is
+    left out). `float32=True` means β is Float32; products promote as in Julia (Float32 stays
+    Float32 only against Float32)."""
+
+    def __init__(self, field="pressure", covariate=None, float32: bool = False):
+        self.field, self.covariate, self.float32 = field, covariate, float32
+        self.neighbourhood = None
+
+    def validate_state(self, u0):
+        if not np.issubdtype(np.asarray(u0).dtype, np.integer):
+            raise InvalidStateError("the kernel-field SI rule runs on integer (Int8) states")
+
+    def __repr__(self):
+        return f"KernelSI(field={self.field!r}, covariate={self.covariate!r})"
+
+
+# ---------------------------------------------------------------- dispersal kernels (src/kernels.jl)
+
+
+class GaussianKernel:
+    """Weight exp(-d^2 / 2 sigma^2), cut off at radius = ceil(3 sigma) (kernels.jl:21-30)."""
+
+    def __init__(self, sigma, radius=None):
+        if not sigma > 0:
+            raise ArgumentError(f"σ must be positive, got {sigma}")
+        self.sigma = float(sigma)
+        self.radius = int(math.ceil(3 * self.sigma)) if radius is None else int(radius)
+        if self.radius < 1:
+            raise ArgumentError(f"radius must be at least 1, got {self.radius}")
+
+    def value(self, d, o):
+        return math.exp(-(d * d) / (2 * (self.sigma * self.sigma)))
+
+
+class ExponentialKernel:
+    """Weight exp(-d / scale), cut off at radius = ceil(5 scale) (kernels.jl:38-47)."""
+
+    def __init__(self, scale, radius=None):
+        if not scale > 0:
+            raise ArgumentError(f"scale must be positive, got {scale}")
+        self.scale = float(scale)
+        self.radius = int(math.ceil(5 * self.scale)) if radius is None else int(radius)
+        if self.radius < 1:
+            raise ArgumentError(f"radius must be at least 1, got {self.radius}")
+
+    def value(self, d, o):
+        return math.exp(-d / self.scale)
+
+
+class PowerLawKernel:
+    """Weight (1 + d)^(-alpha), cut off at radius = 10 (kernels.jl:55-64)."""
+
+    def __init__(self, alpha, radius=10):
+        if not alpha > 0:
+            raise ArgumentError(f"α must be positive, got {alpha}")
+        if radius < 1:
+            raise ArgumentError(f"radius must be at least 1, got {radius}")
+        self.alpha, self.radius = float(alpha), int(radius)
+
+    def value(self, d, o):
+        return math.pow(1.0 + d, -self.alpha)
+
+
+class UniformKernel:
+    """Equal weight within distance radius (kernels.jl:71-78)."""
+
+    def __init__(self, radius):
+        if radius < 1:
+            raise ArgumentError(f"radius must be at least 1, got {radius}")
+        self.radius = int(radius)
+
+    def value(self, d, o):
+        return 1.0
+
+
+class LeniaKernel:
+    """The smooth shell kernel of Lenia (kernels.jl:87-104)."""
+
+    def __init__(self, R, peaks=(1.0,)):
+        if R < 1:
+            raise ArgumentError(f"R must be at least 1, got {R}")
+        if len(peaks) < 1:
+            raise ArgumentError("at least one peak is needed")
+        self.radius, self.peaks = int(R), tuple(float(p) for p in peaks)
+
+    def value(self, d, o):
+        r = d / self.radius
+        if r <= 0 or r >= 1:
+            return 0.0
+        B = len(self.peaks)
+        x = B * r
+        i = min(int(math.floor(x)), B - 1)
+        f = x - i
+        return self.peaks[i] * math.exp(4 - 1 / (f * (1 - f))) if 0 < f < 1 else 0.0
+
+
+class AnisotropicKernel:
+    """A base kernel tilted towards `direction` (radians; 0 = increasing column index, pi/2 =
+    decreasing row index) by exp(strength cos(theta - direction)) (kernels.jl:115-132)."""
+
+    def __init__(self, base, direction, strength):
+        if not strength >= 0:
+            raise ArgumentError(f"strength must be nonnegative, got {strength}")
+        self.base, self.direction, self.strength = base, float(direction), float(strength)
+        self.radius = base.radius
+
+    def value(self, d, o):
+        w = self.base.value(d, o)
+        if d == 0:
+            return w
+        theta = math.atan2(-o[0], o[1])
+        return w * math.exp(self.strength * math.cos(theta - self.direction))
+
+
+class EmpiricalKernel:
+    """A matrix of weights with odd sides, centred on the middle entry (kernels.jl:141-152)."""
+
+    def __init__(self, weights):
+        w = np.asarray(weights, dtype=np.float64)
+        if w.ndim != 2 or not all(n % 2 == 1 for n in w.shape):
+            raise ArgumentError(f"kernel matrix sides must be odd, got {w.shape}")
+        if not (np.all(w >= 0) and np.all(np.isfinite(w))):
+            raise ArgumentError("kernel weights must be finite and nonnegative")
+        if not w.sum() > 0:
+            raise ArgumentError("kernel weights must not all be zero")
+        self.weights = w
+        self.radius = max(n // 2 for n in w.shape)
+
+
+def kernel_weights(kernel, space=None, include_centre: bool = True):
+    """kernels.jl:174-203: the kernel's offsets (column-major order, first axis fastest) and
+    their weights normalised to sum to one (a running sum, then one division each)."""
+    offsets, weights = [], []
+    if isinstance(kernel, EmpiricalKernel):
+        c1, c2 = (kernel.weights.shape[0] + 1) // 2, (kernel.weights.shape[1] + 1) // 2
+        for j in range(1, kernel.weights.shape[1] + 1):
+            for i in range(1, kernel.weights.shape[0] + 1):
+                o = (i - c1, j - c2)
+                if o == (0, 0) and not include_centre:
+                    continue
+                w = float(kernel.weights[i - 1, j - 1])
+                if w > 0:
+                    offsets.append(o)
+                    weights.append(w)
+    else:
+        r = kernel.radius
+        for o2 in range(-r, r + 1):
+            for o1 in range(-r, r + 1):
+                if (o1, o2) == (0, 0) and not include_centre:
+                    continue
+                d = math.sqrt(float(o1 * o1) + float(o2 * o2))
+                if not d <= r + 1e-9:
+                    continue
+                w = float(kernel.value(d, (o1, o2)))
+                if w > 0:
+                    offsets.append((o1, o2))
+                    weights.append(w)
+    if not weights:
+        raise ArgumentError(f"kernel {kernel} has no positive weight")
+    s = 0.0
+    for w in weights:
+        s += w
+    return offsets, np.array([w / s for w in weights])
+
+
+class KernelField:
+    """KernelField(kernel, source; include_centre, method, precision) (environment.jl:22-41).
+    `source` is "x == 1" (the indicator the conformance battery uses) or "identity"."""
+
+    def __init__(self, kernel, source="identity", include_centre: bool = True, method: str = "direct",
+                 precision: str = "Float64"):
+        if method not in ("direct", "fft"):
+            raise ArgumentError(f"method must be :direct or :fft, got :{method}")
+        if source not in ("identity", "x == 1"):
+            raise ArgumentError(f"GB300Backend reads fields with source identity or x == 1, got {source!r}")
+        if precision not in ("Float32", "Float64"):
+            raise ArgumentError(f"precision must be Float32 or Float64, got {precision}")
+        self.kernel, self.source, self.include_centre = kernel, source, include_centre
+        self.method, self.precision = method, precision
+
+    def resolve(self, space, name):
+        """environment.jl:53-69: (taps to read, weights, radius)."""
+        offsets, weights = kernel_weights(self.kernel, space, include_centre=self.include_centre)
+        taps = [(-a, -b) for a, b in offsets]
+        if self.method == "fft" and not all(isinstance(b, Periodic) for b in space.boundaries):
+            raise ArgumentError(f"field :{name} uses method=:fft, which needs periodic boundaries on every axis")
+        radius = max(max(abs(a), abs(b)) for a, b in taps)
+        return taps, weights, radius
 
 
 def _check_values(rule, u0, allowed, msg):

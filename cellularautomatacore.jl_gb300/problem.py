@@ -27,9 +27,12 @@ class CAProblem:
     seed: int = 0
     kwargs: dict = field(default_factory=dict)
     neighbours: Any = None
+    covariates: dict = field(default_factory=dict)
+    fields: dict = field(default_factory=dict)
+    mask: Any = None
 
     @staticmethod
-    def new(rule, u0, tspan, p=None, space=None, seed=0, **kwargs):
+    def new(rule, u0, tspan, p=None, space=None, seed=0, covariates=None, fields=None, mask=None, **kwargs):
         for k in kwargs:
             if k not in ("callback", "saveat", "save_everystep", "save_start", "save_end", "backend"):
                 raise ArgumentError(f"unknown keyword {k}")
@@ -49,15 +52,34 @@ class CAProblem:
         nb = getattr(rule, "neighbourhood", None)
         nb = Moore(1) if nb is None else nb  # default_neighbourhood on a square lattice
         rule.validate_state(u0)
-        return CAProblem(rule, u0, ts, p, space, int(seed) % (1 << 64), dict(kwargs), nb)
+        covariates = dict(covariates or {})
+        for k, a in covariates.items():  # src/environment.jl:73-84
+            a = np.asarray(a)
+            if a.ndim not in (2, 3) or tuple(a.shape[:2]) != tuple(space.dims):
+                raise StateShapeError(f"covariate :{k} has size {a.shape}, the space {space.dims}")
+        if mask is not None:  # src/environment.jl:123-130
+            m = np.asarray(mask)
+            if m.dtype != np.bool_:
+                raise ArgumentError("mask must be an array of Bools")
+            if tuple(m.shape) != tuple(space.dims):
+                raise StateShapeError(f"the mask has size {m.shape}, the space {space.dims}")
+        fields = dict(fields or {})
+        for k, f in fields.items():  # src/environment.jl:53-69
+            from .model import KernelField
+            if not isinstance(f, KernelField):
+                raise ArgumentError(f"field :{k} must be a KernelField, got {type(f).__name__}")
+            f.resolve(space, k)
+        return CAProblem(rule, u0, ts, p, space, int(seed) % (1 << 64), dict(kwargs), nb, covariates, fields, mask)
 
     def remake(self, **changes):
         """src/problem.jl:103-113."""
-        args = dict(rule=self.rule, u0=self.u0, tspan=self.tspan, p=self.p, space=self.space, seed=self.seed)
+        args = dict(rule=self.rule, u0=self.u0, tspan=self.tspan, p=self.p, space=self.space, seed=self.seed,
+                    covariates=self.covariates, fields=self.fields, mask=self.mask)
         kwargs = changes.pop("kwargs", self.kwargs)
         args.update(changes)
         return CAProblem.new(args["rule"], args["u0"], args["tspan"], args["p"], space=args["space"],
-                             seed=args["seed"], **kwargs)
+                             seed=args["seed"], covariates=args["covariates"], fields=args["fields"],
+                             mask=args["mask"], **kwargs)
 
 
 def remake(prob: CAProblem, **changes) -> CAProblem:

@@ -37,7 +37,9 @@ extern "C" {
 #define GBCA_ERR_BUSY 8                /* a queue is full; retry later */
 
 /* ---- problem description (what check_problem / allocate_state receive as `prob`) */
-enum { GBCA_RULE_LIFE = 1, GBCA_RULE_GENERATIONS = 2, GBCA_RULE_FOREST_FIRE = 3, GBCA_RULE_LENIA = 4 };
+enum { GBCA_RULE_LIFE = 1, GBCA_RULE_GENERATIONS = 2, GBCA_RULE_FOREST_FIRE = 3, GBCA_RULE_LENIA = 4,
+       GBCA_RULE_SI_FIELD = 5 };
+enum { GBCA_SOURCE_INDICATOR = 0, GBCA_SOURCE_IDENTITY = 1 };
 enum { GBCA_MOORE = 1, GBCA_VON_NEUMANN = 2 };
 enum { GBCA_PERIODIC = 0, GBCA_REFLECTING = 1, GBCA_CONSTANT = 2 };
 enum { GBCA_SYNCHRONOUS = 0, GBCA_STOCHASTIC = 1, GBCA_CHECKERBOARD = 2 };
@@ -109,7 +111,12 @@ int gbca_get_state(gbca_handle* h, void* host, size_t nbytes);
 
 /* Replaces advance!(b, st, prob, scheme, p, t) (src/backends.jl:121-130; KA ext :92-110),
  * `nsteps` times: the state goes from time t to t + nsteps. `params` is the integrator's
- * p: forest fire {p, f}; unused otherwise (may be NULL with nparams = 0). Work is queued
+ * p: forest fire {p, f}; the kernel-field SI rule {beta}; unused otherwise (may be NULL
+ * with nparams = 0). The SI rule (GBCA_RULE_SI_FIELD) is the conformance battery's
+ * kernel-field epidemic (test/backend_conformance.jl:52-57,72-75) as a typed rule: a cell
+ * in state 1 stays 1, any other becomes 1 when bernoulli(ctx, 1 - exp(-beta * cov * field))
+ * (draw k = 1), with cov the covariate (or none) and field the kernel field; params_f32
+ * makes beta Float32, and products promote as in Julia. Work is queued
  * on the handle's stream; the call returns before it finishes. */
 int gbca_advance(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams);
 
@@ -119,6 +126,29 @@ int gbca_read_cell(gbca_handle* h, int64_t i, int64_t j, void* out);
 
 /* Replaces write_cell!(b, st, I, v) (src/backends.jl:381-383; KA ext :143-148). */
 int gbca_write_cell(gbca_handle* h, int64_t i, int64_t j, const void* value);
+
+/* ---- the environment of a sweep (src/environment.jl:82-148), attached after gbca_create.
+ *
+ * Replaces CAProblem's `mask` (problem.jl:20-27, environment.jl:123-130): cells whose byte is
+ * 0 never update, though their neighbours still read them (backends.jl:448-450). `host` holds
+ * n1*n2 bytes, column-major, nonzero = the cell updates; NULL removes the mask. Int8 rules
+ * only (GBCA_ERR_UNSUPPORTED for Lenia). A masked problem runs on the general kernel. */
+int gbca_set_mask(gbca_handle* h, const uint8_t* host, size_t nbytes);
+
+/* Replaces the resolved KernelField of a GBCA_RULE_SI_FIELD problem (environment.jl:53-69):
+ * `taps` holds ntaps (di, dj) offsets to READ (kernel_weights' offsets negated, in its order),
+ * `weights` their FP64-normalised weights (kernels.jl:174-189); f32 = 1 for
+ * precision = Float32 (weights cast after normalising, sum in Float32); source is
+ * GBCA_SOURCE_INDICATOR (x == 1) or GBCA_SOURCE_IDENTITY (x); method GBCA_DIRECT (taps
+ * within radius 64) or GBCA_FFT (periodic boundaries on both axes; the field agrees with
+ * the direct sum to rounding, as ext/CellularAutomataCoreFFTWExt.jl does). */
+int gbca_set_field(gbca_handle* h, int32_t ntaps, const int32_t* taps, const double* weights, int32_t f32,
+                   int32_t source, int32_t method);
+
+/* Replaces the covariate a GBCA_RULE_SI_FIELD rule reads (environment.jl:71-113): n1*n2*nt
+ * values, column-major, time last (slice mod1(t + 1, nt) at time t; nt = 1 for a fixed
+ * layer), Float64 (f32 = 0) or Float32 (f32 = 1); NULL removes it. */
+int gbca_set_covariate(gbca_handle* h, const void* host, int64_t nt, int32_t f32);
 
 /* Waits for the handle's queued work. */
 int gbca_sync(gbca_handle* h);
@@ -142,6 +172,12 @@ int gbca_set_stream(gbca_handle* h, void* stream);
 /* Number of kernels this library has launched in the process so far (all handles).
  * A diagnostic with no counterpart in the reference. */
 int64_t gbca_kernel_launches(void);
+
+/* Measured compute roof of the stochastic sweeps: Philox4x32-10 cell draws per second
+ * (random.jl:102-107 with the bernoulli compare of random.jl:129) when the GPU does nothing
+ * else, over about `draws` draws on the legacy default stream. The forest-fire rule makes one
+ * draw per cell-update. A diagnostic with no counterpart in the reference. */
+int gbca_philox_rate(int64_t draws, double* draws_per_s);
 
 /* ---- sweep autotuning. No counterpart in the reference (its kernels have one geometry).
  * A sweep geometry is (steps per temporally blocked pass, tile rows). gbca_tune times every

@@ -148,35 +148,149 @@ static int or_gate_open(const or_problem* P, int gate, int64_t i, int64_t j, uin
 
 static int or_ngates(const or_problem* P) { return P->scheme == OR_CHECKERBOARD ? 2 : 1; }
 
+/* ------------------------------------------------------------ environment */
+
+/* Julia's promotion for a product: Float32 * Float32 stays Float32, else Float64. */
+typedef struct { int f32; float f; double d; } or_num;
+
+static or_num or_num32(float f) { or_num r; r.f32 = 1; r.f = f; r.d = (double)f; return r; }
+static or_num or_num64(double d) { or_num r; r.f32 = 0; r.f = (float)d; r.d = d; return r; }
+static or_num or_mul(or_num a, or_num b) {
+    if (a.f32 && b.f32) return or_num32(a.f * b.f);
+    return or_num64(a.d * b.d);
+}
+
+/* environment.jl:151-160: field values of every cell from the state, boundary
+ * semantics on every read, taps in order. Columns j0..j1 (1-based). */
+typedef struct {
+    const or_problem* P;
+    const or_env* E;
+    const int8_t* cur;
+    double* f64;
+    float* f32;
+    const float* w32;
+    int64_t j0, j1;
+} or_field_job;
+
+static void* or_field_worker(void* arg) {
+    or_field_job* J = (or_field_job*)arg;
+    const or_problem* P = J->P;
+    const or_env* E = J->E;
+    for (int64_t j = J->j0; j <= J->j1; ++j)
+        for (int64_t i = 1; i <= P->n1; ++i) {
+            double s = 0.0;
+            float sf = 0.0f;
+            for (int k = 0; k < E->ntaps; ++k) {
+                int8_t v = or_boundary_read(P, J->cur, i + E->taps[2 * k], j + E->taps[2 * k + 1]);
+                double x = E->source ? (double)v : (v == 1 ? 1.0 : 0.0);
+                if (E->field_f32) sf += J->w32[k] * (float)x;
+                else s += E->weights[k] * x;
+            }
+            int64_t lin = (i - 1) + (j - 1) * P->n1;
+            if (E->field_f32) J->f32[lin] = sf;
+            else J->f64[lin] = s;
+        }
+    return NULL;
+}
+
+static void or_compute_field(const or_problem* P, const or_env* E, const int8_t* cur, double* f64, float* f32,
+                             int nthreads) {
+    float* w32 = (float*)malloc(sizeof(float) * (size_t)E->ntaps);
+    for (int k = 0; k < E->ntaps; ++k) w32[k] = (float)E->weights[k];
+    int nt = nthreads > 1 ? nthreads : 1;
+    if (nt > 64) nt = 64;
+    if (nt > P->n2) nt = (int)P->n2;
+    or_field_job jobs[64];
+    pthread_t th[64];
+    for (int k = 0; k < nt; ++k) {
+        or_field_job* J = &jobs[k];
+        J->P = P; J->E = E; J->cur = cur; J->f64 = f64; J->f32 = f32; J->w32 = w32;
+        J->j0 = (k * P->n2) / nt + 1;
+        J->j1 = ((k + 1) * P->n2) / nt;
+    }
+    if (nt == 1) or_field_worker(&jobs[0]);
+    else {
+        for (int k = 0; k < nt; ++k) pthread_create(&th[k], NULL, or_field_worker, &jobs[k]);
+        for (int k = 0; k < nt; ++k) pthread_join(th[k], NULL);
+    }
+    free(w32);
+}
+
+int or_kernel_field(const or_problem* P, const or_env* E, const int8_t* u, double* f64, float* f32) {
+    if (!E || E->ntaps < 1) return -3;
+    or_compute_field(P, E, u, f64, f32, 1);
+    return 0;
+}
+
+/* The typed kernel-field SI rule (test/backend_conformance.jl:52-57,72-75). */
+static int8_t or_si_rule(const or_problem* P, const or_env* E, int8_t c, int64_t lin, uint64_t id, int64_t t,
+                         const double* params, const double* f64, const float* f32) {
+    if (c == 1) return c;
+    or_num lam = P->params_f32 ? or_num32((float)params[0]) : or_num64(params[0]);
+    if (E->cov) {
+        int64_t nt = E->cov_nt > 0 ? E->cov_nt : 1;
+        int64_t slice = or_mod(t, nt);                      /* mod1(t + 1, nt) - 1 */
+        int64_t at = lin + slice * P->n1 * P->n2;
+        lam = or_mul(lam, E->cov_f32 ? or_num32(((const float*)E->cov)[at]) : or_num64(((const double*)E->cov)[at]));
+    }
+    lam = or_mul(lam, E->field_f32 ? or_num32(f32[lin]) : or_num64(f64[lin]));
+    if (lam.f32) {
+        float e = (float)exp(-(double)lam.f);              /* Float32 exp, correctly rounded */
+        float q = 1.0f - e;
+        return or_uniform32(P->seed, id, t, 1) < q ? 1 : c;
+    }
+    double q = 1.0 - exp(-lam.d);
+    return or_uniform(P->seed, id, t, 1) < q ? 1 : c;
+}
+
+static int or_masked(const or_env* E, int64_t lin) { return E && E->mask && !E->mask[lin]; }
+
 /* ------------------------------------------------------- ReferenceBackend step */
 
-/* backends.jl:264-278 (one gated sweep) and :314-322 (gates of one step). */
-int or_step_reference(const or_problem* P, int8_t* cur, int64_t t, const double* params) {
+/* backends.jl:264-278 (one gated sweep) and :314-322 (gates of one step); fields are
+ * computed once per step, before the gates (backends.jl:494-506). */
+int or_step_reference_env(const or_problem* P, const or_env* E, int8_t* cur, int64_t t, const double* params) {
     int32_t off[2 * 201 * 201];
     if (P->radius < 1 || P->radius > 100) return -1;
+    if (P->rule == OR_RULE_SI_FIELD && (!E || E->ntaps < 1)) return -3;
     int m = or_offsets(P->nbhd, P->radius, off);
     int64_t n1 = P->n1, n2 = P->n2, n = n1 * n2;
     int8_t* next = (int8_t*)malloc((size_t)n);
     int8_t* nb = (int8_t*)malloc((size_t)m);
-    if (!next || !nb) { free(next); free(nb); return -2; }
+    double* f64 = NULL;
+    float* f32 = NULL;
+    if (E && E->ntaps > 0) {
+        f64 = (double*)malloc(sizeof(double) * (size_t)n);
+        f32 = (float*)malloc(sizeof(float) * (size_t)n);
+    }
+    if (!next || !nb || (E && E->ntaps > 0 && (!f64 || !f32))) { free(next); free(nb); free(f64); free(f32); return -2; }
+    if (f64) or_compute_field(P, E, cur, f64, f32, 1);
     for (int g = 0; g < or_ngates(P); ++g) {
         for (int64_t j = 1; j <= n2; ++j)
             for (int64_t i = 1; i <= n1; ++i) {
-                uint64_t id = (uint64_t)((i - 1) + (j - 1) * n1 + 1);
-                int8_t c = cur[(i - 1) + (j - 1) * n1];
-                if (!or_gate_open(P, g, i, j, id, t)) {
-                    next[(i - 1) + (j - 1) * n1] = c;
+                int64_t lin = (i - 1) + (j - 1) * n1;
+                uint64_t id = (uint64_t)(lin + 1);
+                int8_t c = cur[lin];
+                if (or_masked(E, lin) || !or_gate_open(P, g, i, j, id, t)) {
+                    next[lin] = c;
+                    continue;
+                }
+                if (P->rule == OR_RULE_SI_FIELD) {
+                    next[lin] = or_si_rule(P, E, c, lin, id, t, params, f64, f32);
                     continue;
                 }
                 for (int k = 0; k < m; ++k)
                     nb[k] = or_boundary_read(P, cur, i + off[2 * k], j + off[2 * k + 1]);
-                next[(i - 1) + (j - 1) * n1] = or_rule(P, c, nb, m, id, t, params);
+                next[lin] = or_rule(P, c, nb, m, id, t, params);
             }
         memcpy(cur, next, (size_t)n);
     }
-    free(next);
-    free(nb);
+    free(next); free(nb); free(f64); free(f32);
     return 0;
+}
+
+int or_step_reference(const or_problem* P, int8_t* cur, int64_t t, const double* params) {
+    return or_step_reference_env(P, NULL, cur, t, params);
 }
 
 /* ------------------------------------------------------------ ArrayBackend run */
@@ -194,6 +308,9 @@ typedef struct {
     int64_t nchunks;
     int64_t next_chunk;      /* dynamic chunk counter (Threads.@threads :dynamic) */
     pthread_mutex_t lock;
+    const or_env* E;
+    const double* f64;       /* field values of this step (unpadded) */
+    const float* f32;
 } or_sweep_job;
 
 /* backends.jl:425-442: every halo cell gets the boundary value of its unpadded index. */
@@ -224,8 +341,13 @@ static void or_sweep_slab(or_sweep_job* J, int64_t lo, int64_t hi) {
             int64_t pos = (i - 1 + J->h) + (j - 1 + J->h) * J->p1;
             uint64_t id = (uint64_t)((i - 1) + (j - 1) * P->n1 + 1);
             int8_t c = J->cur[pos];
-            if (!or_gate_open(P, J->gate, i, j, id, J->t)) {
+            int64_t lin = (i - 1) + (j - 1) * P->n1;
+            if (or_masked(J->E, lin) || !or_gate_open(P, J->gate, i, j, id, J->t)) {
                 J->next[pos] = c;
+                continue;
+            }
+            if (P->rule == OR_RULE_SI_FIELD) {
+                J->next[pos] = or_si_rule(P, J->E, c, lin, id, J->t, J->params, J->f64, J->f32);
                 continue;
             }
             for (int k = 0; k < J->m; ++k) nb[k] = J->cur[pos + J->lin[k]];
@@ -250,8 +372,23 @@ static void* or_sweep_worker(void* arg) {
 
 int or_run_array(const or_problem* P, int8_t* state, int64_t t0, int64_t nsteps,
                  const double* params, int32_t nthreads) {
+    return or_run_array_env(P, NULL, state, t0, nsteps, params, nthreads);
+}
+
+int or_run_array_env(const or_problem* P, const or_env* E, int8_t* state, int64_t t0, int64_t nsteps,
+                     const double* params, int32_t nthreads) {
     int32_t off[2 * 201 * 201];
     if (P->radius < 1 || P->radius > 63) return -1;
+    if (P->rule == OR_RULE_SI_FIELD && (!E || E->ntaps < 1)) return -3;
+    double* f64 = NULL;
+    float* f32 = NULL;
+    int8_t* flat = NULL;
+    if (E && E->ntaps > 0) {
+        f64 = (double*)malloc(sizeof(double) * (size_t)(P->n1 * P->n2));
+        f32 = (float*)malloc(sizeof(float) * (size_t)(P->n1 * P->n2));
+        flat = (int8_t*)malloc((size_t)(P->n1 * P->n2));
+        if (!f64 || !f32 || !flat) { free(f64); free(f32); free(flat); return -2; }
+    }
     int m = or_offsets(P->nbhd, P->radius, off);
     int64_t h = P->radius > 1 ? P->radius : 1; /* backends.jl:405 */
     int64_t p1 = P->n1 + 2 * h, p2 = P->n2 + 2 * h;
@@ -266,10 +403,16 @@ int or_run_array(const or_problem* P, int8_t* state, int64_t t0, int64_t nsteps,
     or_sweep_job J;
     memset(&J, 0, sizeof J);
     J.P = P; J.h = h; J.p1 = p1; J.p2 = p2; J.lin = lin; J.m = m; J.params = params;
+    J.E = E; J.f64 = f64; J.f32 = f32;
     pthread_mutex_init(&J.lock, NULL);
     for (int64_t s = 0; s < nsteps; ++s) {
         J.t = t0 + s;
         or_fill_halo(P, cur, h, p1, p2);
+        if (f64) {  /* backends.jl:481-492: fields from the state at the start of the step */
+            for (int64_t j = 0; j < P->n2; ++j)
+                memcpy(flat + j * P->n1, cur + h + (j + h) * p1, (size_t)P->n1);
+            or_compute_field(P, E, flat, f64, f32, nthreads);
+        }
         for (int g = 0; g < or_ngates(P); ++g) {
             if (g > 0) or_fill_halo(P, cur, h, p1, p2);
             J.cur = cur; J.next = next; J.gate = g;
@@ -288,6 +431,7 @@ int or_run_array(const or_problem* P, int8_t* state, int64_t t0, int64_t nsteps,
         memcpy(state + j * P->n1, cur + h + (j + h) * p1, (size_t)P->n1);
     pthread_mutex_destroy(&J.lock);
     free(cur); free(next); free(lin); free(th);
+    free(f64); free(f32); free(flat);
     return 0;
 }
 
@@ -470,4 +614,59 @@ int or_lenia_step_f32(int64_t n1, int64_t n2, const int32_t* bnd, float* u, int3
                       const double* peaks, int32_t npeaks, double mu, double sigma, double dt,
                       int32_t nthreads) {
     return or_lenia_step(n1, n2, bnd, u, 1, R, peaks, npeaks, mu, sigma, dt, nthreads);
+}
+
+/* ------------------------------------------------------- dispersal kernels */
+
+/* kernels.jl:30,47,64,78,96-104,126-132: unnormalised weight at distance d, offset (o1, o2). */
+static double or_kernel_value(int32_t kind, double a, const double* peaks, int32_t npeaks, int32_t radius,
+                              double d) {
+    switch (kind) {
+        case 1: return exp(-(d * d) / (2.0 * (a * a)));       /* Gaussian(sigma = a) */
+        case 2: return exp(-d / a);                           /* Exponential(scale = a) */
+        case 3: return pow(1.0 + d, -a);                      /* PowerLaw(alpha = a) */
+        case 4: return 1.0;                                   /* Uniform */
+        case 5: return or_lenia_value(d, radius, peaks, npeaks);
+        default: return 0.0;
+    }
+}
+
+int or_kernel_weights(int32_t kind, int32_t aniso_base, double a, double b, double c, int32_t radius,
+                      const double* peaks, int32_t npeaks, const double* emp, int32_t emp_n1, int32_t emp_n2,
+                      int32_t include_centre, int32_t* off, double* w) {
+    int m = 0;
+    if (kind == 7) {  /* kernels.jl:190-203: the matrix entries, centred, column-major */
+        int c1 = (emp_n1 + 1) / 2, c2 = (emp_n2 + 1) / 2;
+        for (int j = 1; j <= emp_n2; ++j)
+            for (int i = 1; i <= emp_n1; ++i) {
+                int o1 = i - c1, o2 = j - c2;
+                if (o1 == 0 && o2 == 0 && !include_centre) continue;
+                double v = emp[(i - 1) + (j - 1) * emp_n1];
+                if (v > 0.0) { off[2 * m] = -o1; off[2 * m + 1] = -o2; w[m] = v; ++m; }
+            }
+    } else {
+        for (int o2 = -radius; o2 <= radius; ++o2)
+            for (int o1 = -radius; o1 <= radius; ++o1) {
+                if (o1 == 0 && o2 == 0 && !include_centre) continue;
+                double d = sqrt((double)(o1 * o1) + (double)(o2 * o2));   /* kernels.jl:154 */
+                if (!(d <= (double)radius + 1e-9)) continue;
+                double v;
+                if (kind == 6) {   /* kernels.jl:126-132 */
+                    v = or_kernel_value(aniso_base, a, peaks, npeaks, radius, d);
+                    if (d != 0.0) {
+                        /* Julia negates the Int offset: -0 is +0.0, so atan(0, x < 0) = +pi */
+                        double th = atan2((double)(-o1), (double)o2);
+                        v = v * exp(c * cos(th - b));
+                    }
+                } else {
+                    v = or_kernel_value(kind, a, peaks, npeaks, radius, d);
+                }
+                if (v > 0.0) { off[2 * m] = -o1; off[2 * m + 1] = -o2; w[m] = v; ++m; }
+            }
+    }
+    if (m == 0) return -1;
+    double s = 0.0;
+    for (int k = 0; k < m; ++k) s += w[k];
+    for (int k = 0; k < m; ++k) w[k] = w[k] / s;
+    return m;
 }

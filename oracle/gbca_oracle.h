@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-enum { OR_RULE_LIFE = 1, OR_RULE_GENERATIONS = 2, OR_RULE_FOREST_FIRE = 3 };
+enum { OR_RULE_LIFE = 1, OR_RULE_GENERATIONS = 2, OR_RULE_FOREST_FIRE = 3, OR_RULE_SI_FIELD = 5 };
 enum { OR_MOORE = 1, OR_VON_NEUMANN = 2 };
 enum { OR_PERIODIC = 0, OR_REFLECTING = 1, OR_CONSTANT = 2 };
 enum { OR_SYNCHRONOUS = 0, OR_STOCHASTIC = 1, OR_CHECKERBOARD = 2 };
@@ -62,6 +62,47 @@ int or_step_reference(const or_problem* P, int8_t* cur, int64_t t, const double*
  * nthreads <= 1 runs serially. state is updated in place. */
 int or_run_array(const or_problem* P, int8_t* state, int64_t t0, int64_t nsteps,
                  const double* params, int32_t nthreads);
+
+/* The environment of a sweep beyond the rule (environment.jl:82-148): a mask of cells
+ * that update (environment.jl:123-130, backends.jl:448-450), one kernel field
+ * (environment.jl:1-69,151-169) and one covariate layer (environment.jl:71-113).
+ * The SI rule (OR_RULE_SI_FIELD) is the conformance battery's kernel-field epidemic
+ * (test/backend_conformance.jl:52-57,72-75) as a typed rule: a cell in state 1 stays 1;
+ * any other cell becomes 1 with probability 1 - exp(-beta * cov * field), draw k = 1,
+ * where beta = params[0] (Float32 when P->params_f32), cov is the covariate at the cell
+ * (slice mod1(t + 1, nt)) or absent, and field = sum_k w_k * (u[I + o_k] == 1) in tap
+ * order, in Float32 when field_f32 (weights cast after FP64 normalisation). Products
+ * follow Julia's promotion: Float32 with Float32 stays Float32, anything else is Float64. */
+typedef struct or_env {
+    const uint8_t* mask;     /* n1*n2, nonzero = the cell updates; NULL: no mask */
+    int32_t ntaps;           /* kernel field taps; 0: no field */
+    int32_t field_f32;
+    const int32_t* taps;     /* offsets to read (already negated), (di, dj) pairs */
+    const double* weights;   /* FP64 normalised weights */
+    const void* cov;         /* n1*n2*cov_nt covariate values, or NULL */
+    int64_t cov_nt;          /* slices along time (1: a fixed layer) */
+    int32_t cov_f32;         /* covariate elements are Float32 */
+    int32_t source;          /* field source: 0 = (x == 1), 1 = x itself */
+} or_env;
+
+/* kernels.jl:174-189 for the dispersal kernels of kernels.jl:1-152 on a square lattice,
+ * then environment.jl:60-63 (negate the offsets). kind: 1 Gaussian(a = sigma),
+ * 2 Exponential(a = scale), 3 PowerLaw(a = alpha), 4 Uniform, 5 Lenia(peaks),
+ * 6 Anisotropic(base kind in aniso_base with a, direction b, strength c),
+ * 7 Empirical (matrix `emp` of emp_n1 x emp_n2, column-major). Returns the tap count
+ * written to off / w (room for (2*radius+1)^2), or -1 when no weight is positive. */
+int or_kernel_weights(int32_t kind, int32_t aniso_base, double a, double b, double c, int32_t radius,
+                      const double* peaks, int32_t npeaks, const double* emp, int32_t emp_n1, int32_t emp_n2,
+                      int32_t include_centre, int32_t* off, double* w);
+
+/* environment.jl:151-160: the field of every cell of u, into f64 (and its
+ * Float32 counterpart into f32 when E->field_f32); both arrays hold n1*n2 values. */
+int or_kernel_field(const or_problem* P, const or_env* E, const int8_t* u, double* f64, float* f32);
+
+/* or_step_reference / or_run_array with an environment (NULL = none). */
+int or_step_reference_env(const or_problem* P, const or_env* E, int8_t* cur, int64_t t, const double* params);
+int or_run_array_env(const or_problem* P, const or_env* E, int8_t* state, int64_t t0, int64_t nsteps,
+                     const double* params, int32_t nthreads);
 
 /* measures.jl:14-20: counts[v] for v in 0..nvals-1 (values outside are ignored,
  * *other receives their number). */

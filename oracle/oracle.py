@@ -25,7 +25,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-RULE_LIFE, RULE_GENERATIONS, RULE_FOREST_FIRE = 1, 2, 3
+RULE_LIFE, RULE_GENERATIONS, RULE_FOREST_FIRE, RULE_SI_FIELD = 1, 2, 3, 5
+# dispersal kernel kinds of or_kernel_weights
+K_GAUSSIAN, K_EXPONENTIAL, K_POWERLAW, K_UNIFORM, K_LENIA, K_ANISOTROPIC, K_EMPIRICAL = 1, 2, 3, 4, 5, 6, 7
 MOORE, VON_NEUMANN = 1, 2
 PERIODIC, REFLECTING, CONSTANT = 0, 1, 2
 SYNCHRONOUS, STOCHASTIC, CHECKERBOARD = 0, 1, 2
@@ -39,6 +41,14 @@ class OrProblem(ctypes.Structure):
         ("constant", ctypes.c_int32 * 2), ("seed", ctypes.c_uint64), ("scheme", ctypes.c_int32),
         ("scheme_p_f32", ctypes.c_int32), ("scheme_p", ctypes.c_double),
         ("params_f32", ctypes.c_int32), ("_pad", ctypes.c_int32),
+    ]
+
+
+class OrEnv(ctypes.Structure):
+    _fields_ = [
+        ("mask", ctypes.c_void_p), ("ntaps", ctypes.c_int32), ("field_f32", ctypes.c_int32),
+        ("taps", ctypes.c_void_p), ("weights", ctypes.c_void_p), ("cov", ctypes.c_void_p),
+        ("cov_nt", ctypes.c_int64), ("cov_f32", ctypes.c_int32), ("source", ctypes.c_int32),
     ]
 
 
@@ -71,6 +81,15 @@ def lib():
                                       P(ctypes.c_int64)]
         L.or_morans_i.argtypes = [P(OrProblem), ctypes.c_void_p]
         L.or_morans_i.restype = ctypes.c_double
+        L.or_step_reference_env.argtypes = [P(OrProblem), P(OrEnv), ctypes.c_void_p, ctypes.c_int64,
+                                            P(ctypes.c_double)]
+        L.or_run_array_env.argtypes = [P(OrProblem), P(OrEnv), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                       P(ctypes.c_double), ctypes.c_int32]
+        L.or_kernel_field.argtypes = [P(OrProblem), P(OrEnv), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.or_kernel_weights.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int32, P(ctypes.c_double), ctypes.c_int32,
+                                        P(ctypes.c_double), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                        P(ctypes.c_int32), P(ctypes.c_double)]
         L.or_lenia_weights.argtypes = [ctypes.c_int32, P(ctypes.c_double), ctypes.c_int32,
                                        P(ctypes.c_int32), P(ctypes.c_double)]
         for name in ("or_lenia_step_f64", "or_lenia_step_f32"):
@@ -135,6 +154,94 @@ def _params(params) -> ctypes.Array:
 def _u8(u: np.ndarray) -> np.ndarray:
     """A Fortran-ordered (column-major, axis 1 contiguous) Int8 copy."""
     return np.asfortranarray(np.array(u, dtype=np.int8, copy=True))
+
+
+@dataclass
+class Env:
+    """A sweep's environment: mask (True = the cell updates), one kernel field (taps to
+    read and FP64 weights, Float32 when field_f32) and one covariate (n1 x n2 or
+    n1 x n2 x nt, Float64 or Float32)."""
+    mask: np.ndarray | None = None
+    taps: np.ndarray | None = None
+    weights: np.ndarray | None = None
+    field_f32: bool = False
+    cov: np.ndarray | None = None
+    identity: bool = False       # field source x itself instead of x == 1
+
+    def c(self):
+        e = OrEnv()
+        e.source = int(self.identity)
+        keep = []
+        if self.mask is not None:
+            m = np.asfortranarray(np.asarray(self.mask, dtype=np.uint8))
+            keep.append(m)
+            e.mask = m.ctypes.data
+        if self.taps is not None:
+            t = np.ascontiguousarray(np.asarray(self.taps, dtype=np.int32).reshape(-1, 2))
+            w = np.ascontiguousarray(np.asarray(self.weights, dtype=np.float64))
+            keep += [t, w]
+            e.ntaps, e.taps, e.weights, e.field_f32 = len(w), t.ctypes.data, w.ctypes.data, int(self.field_f32)
+        if self.cov is not None:
+            c = np.asfortranarray(self.cov)
+            keep.append(c)
+            e.cov, e.cov_nt = c.ctypes.data, (c.shape[2] if c.ndim == 3 else 1)
+            e.cov_f32 = int(c.dtype == np.float32)
+        return e, keep
+
+
+def kernel_weights(kind: int, radius: int, a: float = 0.0, *, base: int = 0, direction: float = 0.0,
+                   strength: float = 0.0, peaks=(1.0,), empirical=None, include_centre: bool = True):
+    """kernels.jl:174-203 then environment.jl:60-63: (taps to read as (di, dj) rows, weights)."""
+    pk = (ctypes.c_double * max(1, len(peaks)))(*peaks)
+    if empirical is not None:
+        E = np.asfortranarray(np.asarray(empirical, dtype=np.float64))
+        cap = E.size
+        emp, e1, e2 = E.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), E.shape[0], E.shape[1]
+    else:
+        cap = (2 * radius + 1) ** 2
+        emp, e1, e2 = None, 0, 0
+    off = (ctypes.c_int32 * (2 * cap))()
+    w = (ctypes.c_double * cap)()
+    m = lib().or_kernel_weights(kind, base, a, direction, strength, radius, pk, len(peaks), emp, e1, e2,
+                                int(include_centre), off, w)
+    if m < 0:
+        raise ValueError("the kernel has no positive weight")
+    return np.array(off[:2 * m], dtype=np.int32).reshape(m, 2), np.array(w[:m])
+
+
+def kernel_field(prob: Problem, env: Env, u: np.ndarray):
+    """environment.jl:151-160: the field of every cell (Float64, or Float32 when env.field_f32)."""
+    a = _u8(u)
+    e, keep = env.c()
+    f64 = np.zeros(a.shape, dtype=np.float64, order="F")
+    f32 = np.zeros(a.shape, dtype=np.float32, order="F")
+    rc = lib().or_kernel_field(ctypes.byref(prob.c()), ctypes.byref(e), a.ctypes.data, f64.ctypes.data,
+                               f32.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"or_kernel_field failed: {rc}")
+    return f32 if env.field_f32 else f64
+
+
+def step_reference_env(prob: Problem, env: Env, u: np.ndarray, t: int, params=None) -> np.ndarray:
+    """One step with an environment (ReferenceBackend semantics)."""
+    a = _u8(u)
+    e, keep = env.c()
+    rc = lib().or_step_reference_env(ctypes.byref(prob.c()), ctypes.byref(e), a.ctypes.data, t, _params(params))
+    if rc != 0:
+        raise RuntimeError(f"or_step_reference_env failed: {rc}")
+    return a
+
+
+def run_array_env(prob: Problem, env: Env, u: np.ndarray, t0: int, nsteps: int, params=None,
+                  nthreads: int = 1) -> np.ndarray:
+    """nsteps steps with an environment (ArrayBackend semantics)."""
+    a = _u8(u)
+    e, keep = env.c()
+    rc = lib().or_run_array_env(ctypes.byref(prob.c()), ctypes.byref(e), a.ctypes.data, t0, nsteps,
+                                _params(params), nthreads)
+    if rc != 0:
+        raise RuntimeError(f"or_run_array_env failed: {rc}")
+    return a
 
 
 def step_reference(prob: Problem, u: np.ndarray, t: int, params=None) -> np.ndarray:
