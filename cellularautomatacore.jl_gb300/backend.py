@@ -237,6 +237,22 @@ def write_cell(backend, st: GB300State, I, v) -> None:
     capi.check(capi.lib().gbca_write_cell(st.handle, int(i), int(j), val.ctypes.data))
 
 
+def snapshot(st: GB300State) -> int:
+    """Queues a copy of the state after the queued steps (device staging, asynchronous copy
+    to pinned memory); returns a ticket for snapshot_fetch."""
+    st.flush()
+    ticket = ctypes.c_int64()
+    capi.check(capi.lib().gbca_snapshot(st.handle, ctypes.byref(ticket)))
+    return int(ticket.value)
+
+
+def snapshot_fetch(st: GB300State, ticket: int) -> np.ndarray:
+    """The state a snapshot captured (column-major, as u0)."""
+    out = np.empty(st.dims, dtype=st.dtype, order="F")
+    capi.check(capi.lib().gbca_snapshot_fetch(st.handle, int(ticket), out.ctypes.data, out.nbytes))
+    return out
+
+
 def device_summaries(st: GB300State, nvals: int = 3):
     """state_counts (src/measures.jl:14-20) and Moran's I (src/measures.jl:91-107) of the
     current state, computed on the device: (counts[0:nvals], cells outside, morans)."""

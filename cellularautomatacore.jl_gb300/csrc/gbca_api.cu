@@ -38,6 +38,18 @@ struct gbca_handle {
     void* cov = nullptr;
     int64_t cov_nt = 0;
     int32_t cov_f32 = 0;
+    // saved states staged on the device and copied out on a second stream (gbca_snapshot)
+    struct Snapshot {
+        void* dev = nullptr;          // packed n1 x n2 copy of the state
+        void* host = nullptr;         // pinned host copy
+        cudaEvent_t staged = nullptr;  // the device copy is complete
+        cudaEvent_t done = nullptr;    // the host copy is complete
+        int64_t ticket = 0;
+        bool busy = false;
+    };
+    std::vector<Snapshot> snaps;
+    cudaStream_t copy_stream = nullptr;
+    int64_t next_ticket = 1;
 };
 
 namespace {
@@ -361,6 +373,14 @@ int gbca_destroy(gbca_handle* h) {
     cudaFree(h->w32);
     cudaFree(h->cov);
     gbca::field_fft_destroy(h->field_fft);
+    if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+    for (auto& sn : h->snaps) {
+        cudaFree(sn.dev);
+        if (sn.host) cudaFreeHost(sn.host);
+        if (sn.staged) cudaEventDestroy(sn.staged);
+        if (sn.done) cudaEventDestroy(sn.done);
+    }
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->acc_host) cudaFreeHost(h->acc_host);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -582,6 +602,65 @@ int gbca_sync(gbca_handle* h) {
     if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "sync");
     return GBCA_OK;
+}
+
+int gbca_snapshot(gbca_handle* h, int64_t* ticket) {
+    if (!h || !ticket) return fail(GBCA_ERR_ARGUMENT, "null handle or ticket");
+    const size_t row = (size_t)h->d.n1 * h->esize, bytes = row * (size_t)h->d.n2;
+    if (!h->copy_stream) GBCA_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), "copy stream");
+    gbca_handle::Snapshot* sn = nullptr;
+    for (auto& x : h->snaps)
+        if (!x.busy) {
+            sn = &x;
+            break;
+        }
+    if (!sn) {
+        if (h->snaps.size() >= (size_t)GBCA_MAX_SNAPSHOTS)
+            return fail(GBCA_ERR_BUSY, "%d snapshots are waiting to be fetched", GBCA_MAX_SNAPSHOTS);
+        h->snaps.emplace_back();
+        sn = &h->snaps.back();
+        cudaError_t e = cudaMalloc(&sn->dev, bytes);
+        if (e == cudaSuccess) e = cudaMallocHost(&sn->host, bytes);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sn->staged, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sn->done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            cudaFree(sn->dev);
+            if (sn->host) cudaFreeHost(sn->host);
+            if (sn->staged) cudaEventDestroy(sn->staged);
+            if (sn->done) cudaEventDestroy(sn->done);
+            h->snaps.pop_back();
+            cudaGetLastError();
+            return e == cudaErrorMemoryAllocation ? fail(GBCA_ERR_OUT_OF_MEMORY, "snapshot buffers of %zu bytes", bytes)
+                                                  : cuda_fail(e, "snapshot set-up");
+        }
+    }
+    // stage on the device behind the queued steps, then copy out on the second stream, so
+    // the sweep goes on while the copy runs
+    GBCA_CUDA(cudaMemcpy2DAsync(sn->dev, row, h->buf[h->cur], (size_t)h->pitch, row, (size_t)h->d.n2,
+                                cudaMemcpyDeviceToDevice, h->stream),
+              "snapshot staging");
+    GBCA_CUDA(cudaEventRecord(sn->staged, h->stream), "snapshot");
+    GBCA_CUDA(cudaStreamWaitEvent(h->copy_stream, sn->staged, 0), "snapshot");
+    GBCA_CUDA(cudaMemcpyAsync(sn->host, sn->dev, bytes, cudaMemcpyDeviceToHost, h->copy_stream), "snapshot copy");
+    GBCA_CUDA(cudaEventRecord(sn->done, h->copy_stream), "snapshot");
+    sn->busy = true;
+    sn->ticket = h->next_ticket++;
+    *ticket = sn->ticket;
+    return GBCA_OK;
+}
+
+int gbca_snapshot_fetch(gbca_handle* h, int64_t ticket, void* host, size_t nbytes) {
+    if (!h || !host) return fail(GBCA_ERR_ARGUMENT, "null handle or buffer");
+    const size_t bytes = (size_t)h->d.n1 * h->esize * (size_t)h->d.n2;
+    if (nbytes != bytes) return fail(GBCA_ERR_STATE, "the buffer has %zu bytes, the lattice needs %zu", nbytes, bytes);
+    for (auto& sn : h->snaps) {
+        if (!sn.busy || sn.ticket != ticket) continue;
+        GBCA_CUDA(cudaEventSynchronize(sn.done), "snapshot fetch");
+        std::memcpy(host, sn.host, bytes);
+        sn.busy = false;
+        return GBCA_OK;
+    }
+    return fail(GBCA_ERR_ARGUMENT, "no pending snapshot %lld", (long long)ticket);
 }
 
 int gbca_summaries(gbca_handle* h, int64_t* counts, int32_t nvals, int64_t* other, double* morans) {

@@ -116,9 +116,20 @@ class CAIntegrator:
         self.prob, self.alg, self.backend, self.state = prob, alg, backend, state
         self.t, self.p = t, prob.p
         self.saveat, self.save_everystep, self.save_end = saveat, save_everystep, save_end
-        self.sol_u, self.sol_t, self.callbacks = [], [], callbacks
+        self._sol_u, self._pending = [], []  # saves, and the indices still held as snapshot tickets
+        self.sol_t, self.callbacks = [], callbacks
         self.retcode = "Default"
         self._u, self._fresh, self._modified = None, False, False
+
+    @property
+    def sol_u(self):
+        _fetch_saves(self, 0)
+        return self._sol_u
+
+    @sol_u.setter
+    def sol_u(self, v):
+        _fetch_saves(self, 0)
+        self._sol_u = v
 
     @property
     def u(self):
@@ -164,8 +175,31 @@ def _should_save(integ):
     return (t - t0) % s == 0 if np.isscalar(s) else t in s
 
 
+class _Snapshot:
+    """A saved state still on its way from the device (a gbca_snapshot ticket)."""
+    __slots__ = ("ticket",)
+
+    def __init__(self, ticket):
+        self.ticket = ticket
+
+
+def _fetch_saves(integ, keep: int):
+    """Collects the oldest pending snapshots until at most `keep` remain."""
+    while len(integ._pending) > keep:
+        k = integ._pending.pop(0)
+        integ._sol_u[k] = B.snapshot_fetch(integ.state, integ._sol_u[k].ticket)
+
+
 def _save(integ):
-    integ.sol_u.append(np.array(integ.u, copy=True, order="F"))
+    """A save. On the GB300 backend, a state not yet fetched is saved through the device-side
+    path: staged on the device and copied out while the sweep goes on (fetched later, at most
+    eight in flight); otherwise the integrator's state is copied."""
+    if isinstance(integ.backend, B.GB300Backend) and not integ._fresh:
+        integ._sol_u.append(_Snapshot(B.snapshot(integ.state)))
+        integ._pending.append(len(integ._sol_u) - 1)
+        _fetch_saves(integ, 8)
+    else:
+        integ._sol_u.append(np.array(integ.u, copy=True, order="F"))
     integ.sol_t.append(integ.t)
 
 

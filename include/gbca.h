@@ -150,6 +150,21 @@ int gbca_set_field(gbca_handle* h, int32_t ntaps, const int32_t* taps, const dou
  * layer), Float64 (f32 = 0) or Float32 (f32 = 1); NULL removes it. */
 int gbca_set_covariate(gbca_handle* h, const void* host, int64_t nt, int32_t f32);
 
+/* ---- the device-side save path: saved states staged on the device and copied out
+ * asynchronously through pinned buffers, so saveat does not stall the sweep.
+ * No counterpart in the reference (its integrator copies each saved state synchronously,
+ * src/problem.jl:336-370). */
+#define GBCA_MAX_SNAPSHOTS 64
+
+/* Queues a copy of the state as it will be after the work queued so far: a device-to-device
+ * copy on the handle's stream, then a device-to-host copy into pinned memory on a second
+ * stream. Returns at once with a ticket for gbca_snapshot_fetch. At most GBCA_MAX_SNAPSHOTS
+ * may wait to be fetched (GBCA_ERR_BUSY beyond). */
+int gbca_snapshot(gbca_handle* h, int64_t* ticket);
+
+/* Waits for snapshot `ticket` and copies it (column-major, n1*n2 elements) to `host`. */
+int gbca_snapshot_fetch(gbca_handle* h, int64_t ticket, void* host, size_t nbytes);
+
 /* Waits for the handle's queued work. */
 int gbca_sync(gbca_handle* h);
 
