@@ -54,6 +54,9 @@ def parse():
                     help="time single passes of one kernel on an n x n lattice (for profiling)")
     ap.add_argument("--n", type=int, default=4096)
     ap.add_argument("--no-tune", action="store_true", help="keep the kernels' default sweep geometry")
+    ap.add_argument("--spp", type=int, default=0, help="--case: pin this many steps per pass (no tuning)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-saves", action="store_true", help="skip the save-path measurement")
     return ap.parse_args()
 
 
@@ -247,7 +250,10 @@ def run_case(args):
     capi.check(lib.gbca_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
     nparams = 2 if params is not None else 0
     geometry = None
-    if args.case in ("ltl", "fire") and not args.no_tune:
+    if args.case in ("ltl", "fire") and args.spp > 0:
+        capi.check(lib.gbca_set_geometry(h, args.spp, 0))
+        per = args.spp
+    elif args.case in ("ltl", "fire") and not args.no_tune:
         geometry = tune(capi, lib, h, params, nparams)
         per = geometry[0] or per
     t = 0
@@ -282,6 +288,50 @@ def tune(capi, lib, h, params, nparams):
     k, rows = ctypes.c_int32(), ctypes.c_int32()
     capi.check(lib.gbca_tune(h, params, nparams, ctypes.byref(k), ctypes.byref(rows)))
     return int(k.value), int(rows.value)
+
+
+SAVES = [dict(name="highlife-128", rule="highlife", n=128, steps=200, saveat=20),
+         dict(name="conway-4096", rule="conway", n=4096, steps=200, saveat=20)]
+
+
+def bench_saves(ca, reps: int = 5):
+    """A solve with saveat through the public API (saves staged on the device and copied out
+    on a second stream) against the same run saving as the reference's integrator does: the
+    queued steps flushed and the state copied synchronously at every save."""
+    capi, lib = ca.capi, ca.capi.lib()
+    out = {}
+    for cfg in SAVES:
+        n, steps, every = cfg["n"], cfg["steps"], cfg["saveat"]
+        u0 = (np.random.Generator(np.random.PCG64(1)).random((n, n)) < 0.5).astype(np.int8)
+        prob = ca.CAProblem.new(ca.Life(":" + cfg["rule"]), u0, steps)
+        B = ca.GB300Backend()
+
+        def run_api():
+            return ca.solve(prob, ca.Synchronous(), backend=B, saveat=every)
+
+        def run_sync():
+            st = ca.allocate_state(B, prob, ca.Synchronous())
+            saves = [ca.current_state(B, st)]
+            for t in range(0, steps, every):
+                capi.check(lib.gbca_advance(st.handle, t, every, None, 0))
+                saves.append(ca.current_state(B, st))
+            st.close()
+            return saves
+
+        a, b = run_api(), run_sync()
+        assert all(np.array_equal(x, y) for x, y in zip(a.u, b)) and len(a.u) == len(b)
+        ta, tb = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            run_api()
+            ta.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            run_sync()
+            tb.append(time.perf_counter() - t0)
+        out[cfg["name"]] = {"saves": len(b), "solve_ms": statistics.median(ta) * 1e3,
+                            "sync_saves_ms": statistics.median(tb) * 1e3,
+                            "speedup": statistics.median(tb) / statistics.median(ta)}
+    return out
 
 
 def ensemble_instances():
@@ -646,7 +696,10 @@ def main():
     e2e = {"value": world * cell_updates() / (e2e_s / args.steps) / 1e9, "unit": "Gcell-updates/s",
            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3}
 
-    batched = bench_batched(capi, lib, max(1, args.warmup // 2), max(1, args.steps // 2)) if rank == 0 else None
+    batched = None
+    if rank == 0 and not args.no_batched:
+        batched = bench_batched(capi, lib, max(1, args.warmup // 2), max(1, args.steps // 2))
+    saves = bench_saves(ca) if rank == 0 and not args.no_saves else None
     served = bench_served(capi, lib) if rank == 0 and not args.no_serve else None
 
     cpu = None
@@ -666,7 +719,8 @@ def main():
                            "l2": "inputs larger than L2: the 16384^2 state is 268 MB, and each step re-copies "
                                  "335 MB of initial states"},
                 "roofline": roofline, "philox_roof": philox_roof, "parts": parts, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clocks.summary(), "cpu_baseline": cpu, "batched": batched, "served": served}
+                "clocks": clocks.summary(), "cpu_baseline": cpu, "batched": batched, "served": served,
+                "saves": saves}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
