@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--spp", type=int, default=0, help="--case: pin this many steps per pass (no tuning)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-saves", action="store_true", help="skip the save-path measurement")
+    ap.add_argument("--no-sparse", action="store_true", help="skip the active-tile measurement")
     return ap.parse_args()
 
 
@@ -331,6 +332,43 @@ def bench_saves(ca, reps: int = 5):
         out[cfg["name"]] = {"saves": len(b), "solve_ms": statistics.median(ta) * 1e3,
                             "sync_saves_ms": statistics.median(tb) * 1e3,
                             "speedup": statistics.median(tb) / statistics.median(ta)}
+    return out
+
+
+SPARSE = dict(n=16384, patch=1024, steps=500)
+
+
+def bench_sparse(ca):
+    """Active-tile sweeps against dense ones: Conway's Life on a 16384^2 torus, quiescent but
+    for a 1024^2 Bernoulli(0.5) soup in the centre (PCG64(5)), 500 steps; device time of the
+    advance, and the final states compared."""
+    import torch
+    capi, lib = ca.capi, ca.capi.lib()
+    n, m, steps = SPARSE["n"], SPARSE["patch"], SPARSE["steps"]
+    u0 = np.zeros((n, n), np.int8)
+    c = (n - m) // 2
+    u0[c:c + m, c:c + m] = (np.random.Generator(np.random.PCG64(5)).random((m, m)) < 0.5)
+    prob = ca.CAProblem.new(ca.Life(":conway"), u0, steps)
+    out, finals = {}, {}
+    for name, backend in (("dense", ca.GB300Backend()), ("active_tiles", ca.GB300Backend(background=0))):
+        st = ca.allocate_state(backend, prob, ca.Synchronous())
+        stream = torch.cuda.Stream()
+        capi.check(lib.gbca_set_stream(st.handle, ctypes.c_void_p(stream.cuda_stream)))
+        capi.check(lib.gbca_advance(st.handle, 0, 2, None, 0))  # warm-up
+        ca.set_state(backend, st, u0)  # timed from the initial state (tile flags rebuilt inside)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        capi.check(lib.gbca_advance(st.handle, 0, steps, None, 0))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        finals[name] = ca.current_state(backend, st)
+        out[name] = {"ms": ms, "gcell_updates_s": n * n * steps / (ms * 1e-3) / 1e9}
+        st.close()
+    out["equal"] = bool(np.array_equal(finals["dense"], finals["active_tiles"]))
+    out["speedup"] = out["dense"]["ms"] / out["active_tiles"]["ms"]
+    out["config"] = f"Life B3/S23 on a {n}^2 torus, {m}^2 soup in the centre, {steps} steps"
     return out
 
 
@@ -700,6 +738,7 @@ def main():
     if rank == 0 and not args.no_batched:
         batched = bench_batched(capi, lib, max(1, args.warmup // 2), max(1, args.steps // 2))
     saves = bench_saves(ca) if rank == 0 and not args.no_saves else None
+    sparse = bench_sparse(ca) if rank == 0 and not args.no_sparse else None
     served = bench_served(capi, lib) if rank == 0 and not args.no_serve else None
 
     cpu = None
@@ -720,7 +759,7 @@ def main():
                                  "335 MB of initial states"},
                 "roofline": roofline, "philox_roof": philox_roof, "parts": parts, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks.summary(), "cpu_baseline": cpu, "batched": batched, "served": served,
-                "saves": saves}
+                "saves": saves, "sparse": sparse}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -21,28 +21,43 @@ import ctypes
 import numpy as np
 
 from . import capi
-from .errors import ArgumentError, IncompatibleSpaceError, StateShapeError
+from .errors import ArgumentError, IncompatibleSpaceError, StateShapeError, UnsupportedCombinationError
 from .model import (Checkerboard, Constant, ForestFire, Generations, KernelSI, Lattice, Lenia, Life, Moore,
                     Stochastic, Synchronous, VonNeumann)
 
 
 class GB300Backend:
     """Run the sweep on the GPU through libgbca.so (hand-written sm_103a kernels).
-    Needs a CUDA device; there is no CPU fallback."""
+    Needs a CUDA device; there is no CPU fallback.
+
+    `background` switches on active-tile sweeps, the GPU form of
+    SparseBackend(background; tilesize) (src/sparse.jl): only tiles holding a non-background
+    cell, and tiles within reach of them, are swept. The rule must be quiescent."""
+
+    def __init__(self, background=None, tilesize: int = 64):
+        self.background, self.tilesize = background, int(tilesize)
 
     def __repr__(self):
-        return "GB300Backend()"
+        if self.background is None:
+            return "GB300Backend()"
+        return f"GB300Backend(background={self.background}, tilesize={self.tilesize})"
 
     def __eq__(self, other):
-        return isinstance(other, GB300Backend)
+        return isinstance(other, GB300Backend) and (self.background, self.tilesize) == \
+            (other.background, other.tilesize)
 
     def __hash__(self):
-        return hash("GB300Backend")
+        return hash(("GB300Backend", self.background, self.tilesize))
 
 
 def supports(backend, scheme) -> bool:
-    """src/backends.jl:153: the gated synchronous schemes."""
-    return isinstance(backend, GB300Backend) and isinstance(scheme, (Synchronous, Stochastic, Checkerboard))
+    """src/backends.jl:153: the gated synchronous schemes; active-tile sweeps run
+    Synchronous and Stochastic, as SparseBackend (src/sparse.jl:40)."""
+    if not isinstance(backend, GB300Backend):
+        return False
+    if backend.background is not None:
+        return isinstance(scheme, (Synchronous, Stochastic))
+    return isinstance(scheme, (Synchronous, Stochastic, Checkerboard))
 
 
 def _params_tuple(rule, p):
@@ -191,6 +206,10 @@ def allocate_state(backend, prob, scheme) -> GB300State:
     dtype = (np.float64 if d.lenia_f64 else np.float32) if d.rule == capi.RULE_LENIA else np.int8
     st = GB300State(d, dtype)
     _attach_environment(st, prob)
+    if getattr(backend, "background", None) is not None:
+        if not supports(backend, scheme):
+            raise UnsupportedCombinationError(repr(backend), repr(scheme))
+        capi.check(capi.lib().gbca_set_sparse(st.handle, 1, int(backend.background), backend.tilesize))
     set_state(backend, st, prob.u0)
     return st
 

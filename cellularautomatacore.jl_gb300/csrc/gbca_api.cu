@@ -50,6 +50,10 @@ struct gbca_handle {
     std::vector<Snapshot> snaps;
     cudaStream_t copy_stream = nullptr;
     int64_t next_ticket = 1;
+    // active-tile scheduling (gbca_set_sparse)
+    bool sparse_on = false;
+    bool sparse_dirty = true;  // the state changed outside a sweep: flags and buffers to rebuild
+    gbca::SparseTiles sparse = {};
 };
 
 namespace {
@@ -218,9 +222,27 @@ int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
     const int rc = ensure_scanned(h);
     if (rc != GBCA_OK) return rc;
     int8_t* const bufs[2] = {(int8_t*)h->buf[0], (int8_t*)h->buf[1]};
+    if (h->sparse_on) {
+        if (!gbca::rule_quiescent(h->d, params, h->sparse.background))
+            return fail(GBCA_ERR_ARGUMENT,
+                        "active-tile sweeps need a quiescent rule: a background cell (%d) with background neighbours "
+                        "changes under these parameters", (int)h->sparse.background);
+        if (h->sparse_dirty) {  // flags of the current state; the other buffer made equal to it
+            const size_t bytes = (size_t)h->pitch * (size_t)h->d.n2;
+            cudaError_t e = gbca::launch_tile_flags(bufs[h->cur], h->d.n1, h->d.n2, h->pitch, h->sparse,
+                                                    h->sparse.flags[h->cur], h->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(bufs[h->cur ^ 1], bufs[h->cur], bytes, cudaMemcpyDeviceToDevice, h->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(h->sparse.flags[h->cur ^ 1], h->sparse.flags[h->cur],
+                                    (size_t)h->sparse.tiles_x * h->sparse.tiles_y, cudaMemcpyDeviceToDevice, h->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "active-tile set-up");
+            h->sparse_dirty = false;
+        }
+    }
     const cudaError_t e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, t, nsteps, params, h->stream,
                                            scanned_rule(h) && h->states_valid, h->forced ? &h->force : nullptr,
-                                           h->mask);
+                                           h->mask, h->sparse_on ? &h->sparse : nullptr);
     if (h->d.rule == GBCA_RULE_FOREST_FIRE) h->states_valid = true;  // a step leaves only 0, 1 and 2
     if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
     return GBCA_OK;
@@ -274,6 +296,7 @@ int time_candidates(gbca_handle* h, const std::vector<gbca::SweepChoice>& cands,
         }
     }
     h->cur = cur0;
+    h->sparse_dirty = true;  // the other buffer now holds a candidate's result
     if (saved) {
         const cudaError_t e2 = cudaMemcpyAsync(h->buf[cur0], saved, bytes, cudaMemcpyDeviceToDevice, h->stream);
         if (e == cudaSuccess) e = e2;
@@ -381,6 +404,10 @@ int gbca_destroy(gbca_handle* h) {
         if (sn.done) cudaEventDestroy(sn.done);
     }
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    cudaFree(h->sparse.flags[0]);
+    cudaFree(h->sparse.flags[1]);
+    cudaFree(h->sparse.list);
+    cudaFree(h->sparse.count);
     if (h->acc_host) cudaFreeHost(h->acc_host);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -396,6 +423,7 @@ int gbca_set_state(gbca_handle* h, const void* host, size_t nbytes) {
                                 cudaMemcpyHostToDevice, h->stream),
               "set_state copy");
     h->states_valid = false;
+    h->sparse_dirty = true;
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_state");
     return GBCA_OK;
 }
@@ -409,6 +437,7 @@ int gbca_set_state_device(gbca_handle* h, const void* dptr, int64_t src_pitch) {
                                 cudaMemcpyDeviceToDevice, h->stream),
               "set_state_device copy");
     h->states_valid = false;
+    h->sparse_dirty = true;
     return GBCA_OK;
 }
 
@@ -594,6 +623,7 @@ int gbca_write_cell(gbca_handle* h, int64_t i, int64_t j, const void* value) {
     char* dst = (char*)h->buf[h->cur] + (i - 1) * (int64_t)h->esize + (j - 1) * h->pitch;
     GBCA_CUDA(cudaMemcpyAsync(dst, value, h->esize, cudaMemcpyHostToDevice, h->stream), "write_cell");
     h->states_valid = false;
+    h->sparse_dirty = true;
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "write_cell");
     return GBCA_OK;
 }
@@ -601,6 +631,51 @@ int gbca_write_cell(gbca_handle* h, int64_t i, int64_t j, const void* value) {
 int gbca_sync(gbca_handle* h) {
     if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "sync");
+    return GBCA_OK;
+}
+
+int gbca_set_sparse(gbca_handle* h, int32_t enable, int32_t background, int32_t tilesize) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_sparse");
+    if (!enable) {
+        h->sparse_on = false;
+        return GBCA_OK;
+    }
+    if (h->d.rule == GBCA_RULE_LENIA || h->d.rule == GBCA_RULE_SI_FIELD)
+        return fail(GBCA_ERR_ARGUMENT, "active-tile sweeps run rules without kernel fields (Life, Generations, forest fire)");
+    if (h->d.scheme == GBCA_CHECKERBOARD)
+        return fail(GBCA_ERR_UNSUPPORTED, "active-tile sweeps run Synchronous() and Stochastic(p)");
+    if (background < -128 || background > 127) return fail(GBCA_ERR_ARGUMENT, "the background must be an Int8 value");
+    if (tilesize <= 0) tilesize = 64;
+    if (tilesize < 8 || tilesize > 128)
+        return fail(GBCA_ERR_ARGUMENT, "tile side must lie in 8:128, got %d", (int)tilesize);
+    if (h->d.rule != GBCA_RULE_FOREST_FIRE && !gbca::rule_quiescent(h->d, nullptr, background))
+        return fail(GBCA_ERR_ARGUMENT,
+                    "active-tile sweeps need a quiescent rule: a background cell (%d) with background neighbours "
+                    "changes", (int)background);
+    const int tile_w = (tilesize + 31) / 32 * 32;  // whole 32-cell words for the bit-sliced kernel
+    const int tx = (int)((h->d.n1 + tile_w - 1) / tile_w), ty = (int)((h->d.n2 + tilesize - 1) / tilesize);
+    cudaFree(h->sparse.flags[0]);
+    cudaFree(h->sparse.flags[1]);
+    cudaFree(h->sparse.list);
+    cudaFree(h->sparse.count);
+    h->sparse = {};
+    const size_t n = (size_t)tx * ty;
+    cudaError_t e = cudaMalloc(&h->sparse.flags[0], n);
+    if (e == cudaSuccess) e = cudaMalloc(&h->sparse.flags[1], n);
+    if (e == cudaSuccess) e = cudaMalloc(&h->sparse.list, n * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&h->sparse.count, sizeof(int32_t));
+    if (e != cudaSuccess) {
+        h->sparse_on = false;
+        return cuda_fail(e, "active-tile allocation");
+    }
+    h->sparse.background = background;
+    h->sparse.tile_w = tile_w;
+    h->sparse.tile_h = tilesize;
+    h->sparse.tiles_x = tx;
+    h->sparse.tiles_y = ty;
+    h->sparse_on = true;
+    h->sparse_dirty = true;
     return GBCA_OK;
 }
 
@@ -690,6 +765,7 @@ int64_t gbca_kernel_launches(void) { return gbca::launches_so_far(); }
 
 int gbca_device_state(gbca_handle* h, void** dptr, int64_t* pitch) {
     if (!h || !dptr) return fail(GBCA_ERR_ARGUMENT, "null handle or output");
+    h->sparse_dirty = true;  // the caller may write through the pointer
     *dptr = h->buf[h->cur];
     if (pitch) *pitch = h->pitch;
     return GBCA_OK;

@@ -165,6 +165,25 @@ struct SweepParams {
                                // 0..C-1, forest fire 0..2)
     int32_t pad_;
     const uint8_t* mask;       // nonzero = the cell updates (pitch bytes between columns), or null
+    // active-tile scheduling: the tiles (ty * tiles_x + tx, tiles of tile_x x tile_y cells) to
+    // run, *tile_count of them; each run tile writes whether it holds a non-background cell
+    const int32_t* tile_list;
+    const int32_t* tile_count;
+    uint8_t* flags_out;
+    int32_t tiles_x;
+    int32_t background;
+};
+
+// Active-tile scheduling state of a handle (sweep_sparse.cu): only tiles holding a cell
+// other than `background`, and tiles within reach of them, are swept; the others are known
+// to stay background (the rule is quiescent).
+struct SparseTiles {
+    int32_t background;
+    int32_t tile_w, tile_h;    // tile size in cells (tile_w a multiple of 32)
+    int32_t tiles_x, tiles_y;
+    uint8_t* flags[2];         // per state buffer: the tile holds a non-background cell
+    int32_t* list;             // candidate tiles of the current pass
+    int32_t* count;
 };
 
 // The message gbca_last_error() returns on this thread.
@@ -187,9 +206,18 @@ struct SweepChoice {
 // enabling the bit-sliced kernel; forest fire: 0..2, enabling bit tests on the first step).
 // force: use this geometry instead of the autotuner's cached pick (tune.cu).
 // mask: cells whose byte is 0 keep their state (general kernel only).
+// sparse: sweep only the active tiles (general kernel, tiles of sparse->tile cells).
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
                        const double* params, cudaStream_t st, bool states_valid = false,
-                       const SweepChoice* force = nullptr, const uint8_t* mask = nullptr);
+                       const SweepChoice* force = nullptr, const uint8_t* mask = nullptr,
+                       const SparseTiles* sparse = nullptr);
+
+// Active-tile scheduling (sweep_sparse.cu).
+cudaError_t launch_candidates(const SweepParams& p, const SparseTiles& sp, int cur, int halo, cudaStream_t st);
+cudaError_t launch_tile_flags(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, const SparseTiles& sp,
+                              uint8_t* flags, cudaStream_t st);
+// Whether a background cell whose neighbours are all background stays background.
+bool rule_quiescent(const gbca_desc& d, const double* params, int32_t background);
 
 // The autotuner's cached choice for a problem shape (tune.cu); false when it has none.
 bool tuned_choice(const gbca_desc& d, SweepChoice* out);
@@ -200,8 +228,13 @@ std::vector<SweepChoice> sweep_candidates(const SweepParams& p);
 
 // Launchers (one translation unit each).
 cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
+// The general kernel over the tiles of p.tile_list (grid: the number of tiles of the lattice).
+cudaError_t launch_generic_tiles(const SweepParams& p, int ntiles, const int8_t* src, int8_t* dst, cudaStream_t st);
 bool life_simd_supported(const SweepParams& p);
 cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
+// The bit-sliced kernel over the tiles of p.tile_list (tiles of tile_w x tile_h cells).
+cudaError_t launch_life_tiles(const SweepParams& p, const SparseTiles& sp, const int8_t* src, int8_t* dst,
+                              cudaStream_t st);
 int life_steps_per_pass(const SweepParams& p);
 // Whether a pass of `steps` steps on tiles `rows` high fits the bit-sliced kernel's shared memory.
 bool life_choice_fits(const SweepParams& p, int steps, int rows);

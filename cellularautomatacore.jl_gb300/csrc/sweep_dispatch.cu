@@ -39,10 +39,50 @@ SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params
 
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
                        const double* params, cudaStream_t st, bool states_valid, const SweepChoice* force,
-                       const uint8_t* mask) {
+                       const uint8_t* mask, const SparseTiles* sparse) {
     SweepParams p = sweep_params(d, pitch, params);
     p.states_valid = states_valid ? 1 : 0;
     p.mask = mask;
+    if (sparse) {  // active tiles only: the bit-sliced kernel where it applies, else the general one
+        const int ntiles = sparse->tiles_x * sparse->tiles_y;
+        p.tiles_x = sparse->tiles_x;
+        p.background = sparse->background;
+        p.tile_list = sparse->list;
+        p.tile_count = sparse->count;
+        const bool life = life_simd_supported(p);
+        while (nsteps > 0) {
+            int64_t per;
+            if (life) {
+                per = life_steps_per_pass(p);
+                const int64_t cap = sparse->tile_h / (2 * p.radius);  // halo no deeper than half a tile
+                if (per > cap) per = cap > 0 ? cap : 1;
+            } else {
+                per = 32 / (p.radius * p.ngates);
+                if (per < 1) per = 1;
+            }
+            const int64_t k = nsteps < per ? nsteps : per;
+            p.nsub = (int32_t)(k * p.ngates);
+            p.t0 = t;
+            const int halo = p.nsub * p.radius;
+            cudaError_t e = launch_candidates(p, *sparse, *cur, halo, st);
+            if (e != cudaSuccess) return e;
+            p.flags_out = sparse->flags[*cur ^ 1];
+            if (life) {
+                e = launch_life_tiles(p, *sparse, bufs[*cur], bufs[*cur ^ 1], st);
+            } else {
+                p.tile_x = sparse->tile_w;
+                p.tile_y = sparse->tile_h;
+                p.halo_x = p.halo_y = halo;
+                e = launch_generic_tiles(p, ntiles, bufs[*cur], bufs[*cur ^ 1], st);
+            }
+            if (e != cudaSuccess) return e;
+            count_launch();
+            *cur ^= 1;
+            t += k;
+            nsteps -= k;
+        }
+        return cudaSuccess;
+    }
     const bool fire = fire_fast_supported(p);
     const bool life = !fire && life_simd_supported(p);
     SweepChoice choice = {0, 0};

@@ -65,6 +65,7 @@ __device__ __forceinline__ int8_t generic_rule(const SweepParams& p, const int8_
     return draw_below(cell_draw(p.seed, id, t, 2), p.thr_f, p.params_f32) ? 2 : 1;
 }
 
+template <bool TILES>
 __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __restrict__ src,
                                                  int8_t* __restrict__ dst) {
     extern __shared__ int8_t smem_g[];
@@ -72,7 +73,17 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
     const int sx = p.tile_x + 2 * hx, sy = p.tile_y + 2 * hy;
     int8_t* A = smem_g;
     int8_t* B = smem_g + sx * sy;
-    const int64_t X0 = (int64_t)blockIdx.x * p.tile_x, Y0 = (int64_t)blockIdx.y * p.tile_y;
+    int64_t X0, Y0;
+    int tile = 0;
+    if (TILES) {  // one CTA per listed tile; the rest of the grid has nothing to do
+        if ((int)blockIdx.x >= *p.tile_count) return;
+        tile = p.tile_list[blockIdx.x];
+        X0 = (int64_t)(tile % p.tiles_x) * p.tile_x;
+        Y0 = (int64_t)(tile / p.tiles_x) * p.tile_y;
+    } else {
+        X0 = (int64_t)blockIdx.x * p.tile_x;
+        Y0 = (int64_t)blockIdx.y * p.tile_y;
+    }
     const bool interior = X0 - hx >= 0 && X0 + p.tile_x + hx <= p.n1 && Y0 - hy >= 0 &&
                           Y0 + p.tile_y + hy <= p.n2;
 
@@ -126,10 +137,19 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
         int8_t* tmp = A; A = B; B = tmp;
     }
 
+    int active = 0;
     for (int idx = threadIdx.x; idx < p.tile_x * p.tile_y; idx += blockDim.x) {
         const int ox = idx % p.tile_x, oy = idx / p.tile_x;
         const int64_t gx = X0 + ox, gy = Y0 + oy;
-        if (gx < p.n1 && gy < p.n2) dst[gx + gy * p.pitch] = A[(hy + oy) * sx + hx + ox];
+        if (gx < p.n1 && gy < p.n2) {
+            const int8_t v = A[(hy + oy) * sx + hx + ox];
+            dst[gx + gy * p.pitch] = v;
+            if (TILES) active |= v != (int8_t)p.background;
+        }
+    }
+    if (TILES) {
+        active = __syncthreads_or(active);
+        if (threadIdx.x == 0) p.flags_out[tile] = (uint8_t)active;
     }
 }
 
@@ -139,11 +159,22 @@ cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst,
     const int sx = p.tile_x + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
     const size_t smem = 2 * (size_t)sx * (size_t)sy;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_generic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_generic<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     dim3 grid((unsigned)((p.n1 + p.tile_x - 1) / p.tile_x), (unsigned)((p.n2 + p.tile_y - 1) / p.tile_y));
-    k_generic<<<grid, 256, smem, st>>>(p, src, dst);
+    k_generic<false><<<grid, 256, smem, st>>>(p, src, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_generic_tiles(const SweepParams& p, int ntiles, const int8_t* src, int8_t* dst, cudaStream_t st) {
+    const int sx = p.tile_x + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
+    const size_t smem = 2 * (size_t)sx * (size_t)sy;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_generic<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_generic<true><<<(unsigned)ntiles, 256, smem, st>>>(p, src, dst);
     return cudaGetLastError();
 }
 

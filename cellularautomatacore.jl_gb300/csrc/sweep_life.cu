@@ -307,8 +307,15 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
     uint32_t* A = smw;
     uint32_t* B = smw + PL * ps;
     const int W = g.tw + 2 * g.hw;
-    const int64_t X0 = (int64_t)blockIdx.x * (32 * g.tw) - 32 * g.hw;  // lattice x of local cell 0
-    const int64_t Y0 = (int64_t)blockIdx.y * g.ty - g.hy;              // lattice y of local row 0
+    int bx = blockIdx.x, by = blockIdx.y, tile = 0;
+    if (p.tile_list) {  // active-tile sweeps: one CTA per listed tile, the rest has nothing to do
+        if ((int)blockIdx.x >= *p.tile_count) return;
+        tile = p.tile_list[blockIdx.x];
+        bx = tile % p.tiles_x;
+        by = tile / p.tiles_x;
+    }
+    const int64_t X0 = (int64_t)bx * (32 * g.tw) - 32 * g.hw;  // lattice x of local cell 0
+    const int64_t Y0 = (int64_t)by * g.ty - g.hy;              // lattice y of local row 0
     // the Constant values as plane bits (Life: the indicator; Generations: state bits)
     uint32_t cb0[PL], cb1[PL];
 #pragma unroll
@@ -376,12 +383,17 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
         uint32_t* t = A; A = B; B = t;
     }
 
+    int active = 0;  // a written cell differs from the background (active-tile sweeps)
+    const uint32_t bg0 = (p.background & 1) ? 0xFFFFFFFFu : 0u;                // the background's
+    const uint32_t bg1 = PL == 2 && (p.background & 2) ? 0xFFFFFFFFu : 0u;     // plane bits
     for (int q = threadIdx.x; q < g.tw * g.ty; q += blockDim.x) {
         const int lw = g.hw + q % g.tw, ly = g.hy + q / g.tw;
         const int64_t gy = Y0 + ly, gx = X0 + 32 * lw;
         if (gy >= p.n2 || gx >= p.n1) continue;
         const uint32_t bits = A[ly * g.sw + 1 + lw];
         const uint32_t hib = PL == 2 ? A[ps + ly * g.sw + 1 + lw] : 0u;
+        const uint32_t valid = gx + 32 <= p.n1 ? 0xFFFFFFFFu : ((1u << (p.n1 - gx)) - 1u);
+        active |= (((bits ^ bg0) | (PL == 2 ? hib ^ bg1 : 0u)) & valid) != 0u;
         int8_t* out = dst + gy * p.pitch + gx;
         if (gx + 32 <= p.n1) {
             int4 q0 = bytes16(bits), q1 = bytes16(bits >> 16);
@@ -396,6 +408,10 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
             for (int b = 0; gx + b < p.n1; ++b)
                 out[b] = (int8_t)(((bits >> b) & 1u) | (PL == 2 ? ((hib >> b) & 1u) << 1 : 0u));
         }
+    }
+    if (p.tile_list) {
+        active = __syncthreads_or(active);
+        if (threadIdx.x == 0) p.flags_out[tile] = (uint8_t)active;
     }
 }
 
@@ -461,22 +477,23 @@ size_t life_smem_bytes(const SweepParams& p, const LifeGeom& g) {
 
 template <int R, int NI, int PL>
 cudaError_t launch_rn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
-                      cudaStream_t st) {
+                      cudaStream_t st, int ntiles) {
     const size_t smem = life_smem_bytes(p, g);
     cudaError_t e = cudaFuncSetAttribute(k_life<R, NI, PL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((p.n1 + 32 * g.tw - 1) / (32 * g.tw)), (unsigned)((p.n2 + g.ty - 1) / g.ty));
+    if (ntiles > 0) grid = dim3((unsigned)ntiles, 1u);  // one CTA per listed tile
     k_life<R, NI, PL><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
     return cudaGetLastError();
 }
 
 template <int R, int PL>
 cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
-                     cudaStream_t st) {
+                     cudaStream_t st, int ntiles = 0) {
     const int ni = tb.n[0] > tb.n[1] ? tb.n[0] : tb.n[1];
-    if (ni <= 1) return launch_rn<R, 1, PL>(p, g, tb, src, dst, st);
-    if (ni <= 2) return launch_rn<R, 2, PL>(p, g, tb, src, dst, st);
-    return launch_rn<R, kMaxIntervals, PL>(p, g, tb, src, dst, st);
+    if (ni <= 1) return launch_rn<R, 1, PL>(p, g, tb, src, dst, st, ntiles);
+    if (ni <= 2) return launch_rn<R, 2, PL>(p, g, tb, src, dst, st, ntiles);
+    return launch_rn<R, kMaxIntervals, PL>(p, g, tb, src, dst, st, ntiles);
 }
 
 }  // namespace
@@ -534,6 +551,36 @@ cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* ds
         case 3: return launch_r<3, 1>(p, g, tb, src, dst, st);
         case 4: return launch_r<4, 1>(p, g, tb, src, dst, st);
         default: return launch_r<5, 1>(p, g, tb, src, dst, st);
+    }
+}
+
+}  // namespace gbca
+
+namespace gbca {
+
+cudaError_t launch_life_tiles(const SweepParams& p, const SparseTiles& sp, const int8_t* src, int8_t* dst,
+                              cudaStream_t st) {
+    LifeTables tb;
+    if (!make_tables(p, &tb)) return cudaErrorNotSupported;
+    LifeGeom g;
+    g.K = p.nsub;
+    g.hy = g.K * p.radius;
+    g.hw = (g.hy + 31) / 32;
+    g.tw = sp.tile_w / 32;
+    g.ty = sp.tile_h;
+    g.sw = g.tw + 2 * g.hw + 2;
+    g.sy = g.ty + 2 * g.hy;
+    const int n = sp.tiles_x * sp.tiles_y;
+    if (p.rule == GBCA_RULE_GENERATIONS) {
+        if (p.radius == 1) return launch_r<1, 2>(p, g, tb, src, dst, st, n);
+        return launch_r<2, 2>(p, g, tb, src, dst, st, n);
+    }
+    switch (p.radius) {
+        case 1: return launch_r<1, 1>(p, g, tb, src, dst, st, n);
+        case 2: return launch_r<2, 1>(p, g, tb, src, dst, st, n);
+        case 3: return launch_r<3, 1>(p, g, tb, src, dst, st, n);
+        case 4: return launch_r<4, 1>(p, g, tb, src, dst, st, n);
+        default: return launch_r<5, 1>(p, g, tb, src, dst, st, n);
     }
 }
 

@@ -150,6 +150,16 @@ int gbca_set_field(gbca_handle* h, int32_t ntaps, const int32_t* taps, const dou
  * layer), Float64 (f32 = 0) or Float32 (f32 = 1); NULL removes it. */
 int gbca_set_covariate(gbca_handle* h, const void* host, int64_t nt, int32_t f32);
 
+/* ---- active-tile scheduling: the GPU form of SparseBackend(background; tilesize)
+ * (src/sparse.jl:1-211). With enable = 1, each sweep runs only the tiles (tilesize x tilesize
+ * cells; 0 = 64) that hold a cell other than `background` or lie within reach of one, for
+ * quiescent rules: a background cell with background neighbours must stay background (Life
+ * without B0 on background 0, Generations on 0, the forest fire with p = 0 on empty or f = 0 on
+ * trees); GBCA_ERR_ARGUMENT otherwise (the forest fire is checked at each gbca_advance, whose
+ * parameters decide it). Synchronous and Stochastic only, as SparseBackend (sparse.jl:40);
+ * masks allowed. Results equal the dense sweep's. enable = 0 returns to dense sweeps. */
+int gbca_set_sparse(gbca_handle* h, int32_t enable, int32_t background, int32_t tilesize);
+
 /* ---- the device-side save path: saved states staged on the device and copied out
  * asynchronously through pinned buffers, so saveat does not stall the sweep.
  * No counterpart in the reference (its integrator copies each saved state synchronously,
