@@ -411,6 +411,10 @@ def bench_batched(capi, lib, warmup: int, steps: int):
         capi.check(lib.gbca_ensemble_run(e, T0, S, P, 2))
         capi.check(lib.gbca_ensemble_sync(e))
 
+    # the autotuner picks the batched kernel's tile side and pass depth (16-step probes)
+    capi.check(lib.gbca_ensemble_fill(e, 0))
+    tile, depth = ctypes.c_int32(), ctypes.c_int32()
+    capi.check(lib.gbca_ensemble_tune(e, 16, P, 2, ctypes.byref(tile), ctypes.byref(depth)))
     for _ in range(warmup):
         run()
     t0 = time.perf_counter()
@@ -454,7 +458,8 @@ def bench_batched(capi, lib, warmup: int, steps: int):
             "plain_sims_per_s": plain_sims, "plain_sample": len(sample),
             "plain_gcell_updates_s": sample_cu / t_plain / 1e9,
             "speedup_vs_plain": (n / t_batched) / plain_sims,
-            "exact_matches_in_sample": exact, "launches_per_run": 1}
+            "exact_matches_in_sample": exact, "launches_per_run": 1,
+            "geometry": {"tile": tile.value, "depth": depth.value, "picked_by": "gbca_ensemble_tune"}}
 
 
 SERVE = dict(rate=2000.0, seconds=2.0, plain_sample=48, hbm_budget=8 << 30, chunk_steps=100,

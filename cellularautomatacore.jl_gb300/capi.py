@@ -89,6 +89,9 @@ SIGNATURES = {
     "gbca_ensemble_sync": (ctypes.c_int, [_V]),
     "gbca_ensemble_summaries": (ctypes.c_int, [_V, _P(_I64), ctypes.c_int32, _P(_I64), _P(ctypes.c_double)]),
     "gbca_ensemble_get_state": (ctypes.c_int, [_V, ctypes.c_int32, _V, ctypes.c_size_t]),
+    "gbca_ensemble_set_geometry": (ctypes.c_int, [_V, ctypes.c_int32, ctypes.c_int32]),
+    "gbca_ensemble_tune": (ctypes.c_int, [_V, _I64, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_int32),
+                                          _P(ctypes.c_int32)]),
     "gbca_server_start": (ctypes.c_int, [_P(ServerConfig), _P(_V)]),
     "gbca_server_submit": (ctypes.c_int, [_V, _P(Desc), _V, ctypes.c_size_t, ctypes.c_double, ctypes.c_uint64, _I64,
                                           _I64, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_uint64)]),

@@ -11,7 +11,7 @@
 // Largest-first keeps the tail short.
 //
 // Per instance, in one CTA:
-//  * small lattices, (n1 + 2r)(n2 + 2r) <= kEnsBuf bytes, live entirely in shared memory: a
+//  * small lattices, (n1 + 2r)(n2 + 2r) <= (tile + 16)^2 bytes, live entirely in shared memory: a
 //    halo of r cells is refreshed from the boundary map before every step (the halo fill of
 //    src/backends.jl:425-442) and all steps run without touching global memory;
 //  * larger ones are swept tile by tile with temporal blocking (K steps per pass, halo K r),
@@ -37,10 +37,10 @@ namespace gbca {
 namespace {
 
 constexpr int kEnsThreads = 256;
-constexpr int kEnsTile = 128;
 constexpr int kEnsMaxHalo = 8;
-constexpr int kEnsSide = kEnsTile + 2 * kEnsMaxHalo;  // 144
-constexpr int kEnsBuf = kEnsSide * kEnsSide;          // bytes per shared buffer
+
+// Bytes of each of a CTA's two shared buffers for tiles of TILE x TILE cells.
+__host__ __device__ constexpr int ens_buf(int tile) { return (tile + 2 * kEnsMaxHalo) * (tile + 2 * kEnsMaxHalo); }
 
 __device__ __forceinline__ bool fast_fire(const EnsInstance& I) {
     return I.rule == GBCA_RULE_FOREST_FIRE && I.nbhd == GBCA_VON_NEUMANN && I.radius == 1;
@@ -140,21 +140,22 @@ __device__ void run_in_smem(const EnsInstance& I, int8_t* pool, int8_t* A, int8_
     }
 }
 
-// Tiles of kEnsTile x kEnsTile with K-step temporal blocking through the two global buffers.
-// Returns the buffer index holding the final state.
+// Tiles of TILE x TILE with I.depth-step temporal blocking through the two global
+// buffers. Returns the buffer index holding the final state.
+template <int TILE>
 __device__ int run_tiled(const EnsInstance& I, int8_t* pool, int8_t* A0, int8_t* B0, const PhiloxKeys& K) {
     const int r = I.radius;
     const bool ff = fast_fire(I);
-    const int Kmax = kEnsMaxHalo / r;
-    const int ntx = (int)((I.n1 + kEnsTile - 1) / kEnsTile), nty = (int)((I.n2 + kEnsTile - 1) / kEnsTile);
+    const int Kmax = I.depth;  // steps per pass, depth * r <= kEnsMaxHalo
+    const int ntx = (int)((I.n1 + TILE - 1) / TILE), nty = (int)((I.n2 + TILE - 1) / TILE);
     int cur = I.cur;
     for (int64_t s0 = 0; s0 < I.nsteps; s0 += Kmax) {
         const int k = (int)((I.nsteps - s0) < Kmax ? (I.nsteps - s0) : Kmax);
-        const int H = k * r, S = kEnsTile + 2 * H;
+        const int H = k * r, S = TILE + 2 * H;
         const int8_t* src = pool + I.off[cur];
         int8_t* dst = pool + I.off[cur ^ 1];
         for (int tile = 0; tile < ntx * nty; ++tile) {
-            const int64_t X0 = (int64_t)(tile % ntx) * kEnsTile, Y0 = (int64_t)(tile / ntx) * kEnsTile;
+            const int64_t X0 = (int64_t)(tile % ntx) * TILE, Y0 = (int64_t)(tile / ntx) * TILE;
             int8_t* A = A0;
             int8_t* B = B0;
             __syncthreads();
@@ -166,7 +167,7 @@ __device__ int run_tiled(const EnsInstance& I, int8_t* pool, int8_t* A0, int8_t*
             for (int sub = 0; sub < k; ++sub) {
                 const int64_t t = I.t0 + s0 + sub;
                 const DrawStep ds = draw_step(K, t);
-                const int ex = (k - 1 - sub) * r, lo = H - ex, w = kEnsTile + 2 * ex;
+                const int ex = (k - 1 - sub) * r, lo = H - ex, w = TILE + 2 * ex;
                 for (int q = threadIdx.x; q < w * w; q += blockDim.x) {
                     const int lx = lo + q % w, ly = lo + q / w, o = ly * S + lx;
                     const int64_t mx = map_axis(I.bnd0, X0 - H + lx, I.n1), my = map_axis(I.bnd1, Y0 - H + ly, I.n2);
@@ -179,9 +180,9 @@ __device__ int run_tiled(const EnsInstance& I, int8_t* pool, int8_t* A0, int8_t*
                 __syncthreads();
                 int8_t* tmp = A; A = B; B = tmp;
             }
-            for (int q = threadIdx.x; q < kEnsTile * kEnsTile; q += blockDim.x) {
-                const int64_t gx = X0 + q % kEnsTile, gy = Y0 + q / kEnsTile;
-                if (gx < I.n1 && gy < I.n2) dst[gx + gy * I.pitch] = A[(H + q / kEnsTile) * S + H + q % kEnsTile];
+            for (int q = threadIdx.x; q < TILE * TILE; q += blockDim.x) {
+                const int64_t gx = X0 + q % TILE, gy = Y0 + q / TILE;
+                if (gx < I.n1 && gy < I.n2) dst[gx + gy * I.pitch] = A[(H + q / TILE) * S + H + q % TILE];
             }
         }
         __syncthreads();  // the whole pass is written before the next one reads it
@@ -230,20 +231,22 @@ __device__ void run_in_smem_fire(const EnsInstance& I, int8_t* pool, int8_t* A, 
     }
 }
 
-// Forest fire on tiles of kEnsTile^2 through the two global buffers, 8 steps per pass,
-// four cells per work item. Returns the buffer holding the final state.
+// Forest fire on tiles of TILE^2 through the two global buffers, I.depth (<= 8) steps per
+// pass, four cells per work item. Returns the buffer holding the final state.
+template <int TILE>
 __device__ int run_tiled_fire(const EnsInstance& I, int8_t* pool, int8_t* A0, int8_t* B0, const PhiloxKeys& K,
                               const FireGeom& g) {
-    constexpr int HX = kEnsMaxHalo, SX = kEnsTile + 2 * HX, SW = SX / 4;
-    const int ntx = (int)((I.n1 + kEnsTile - 1) / kEnsTile), nty = (int)((I.n2 + kEnsTile - 1) / kEnsTile);
+    constexpr int HX = kEnsMaxHalo, SX = TILE + 2 * HX, SW = SX / 4;
+    const int ntx = (int)((I.n1 + TILE - 1) / TILE), nty = (int)((I.n2 + TILE - 1) / TILE);
+    const int depth = I.depth;
     int cur = I.cur;
-    for (int64_t s0 = 0; s0 < I.nsteps; s0 += kEnsMaxHalo) {
-        const int k = (int)((I.nsteps - s0) < kEnsMaxHalo ? (I.nsteps - s0) : kEnsMaxHalo);
-        const int SY = kEnsTile + 2 * k;
+    for (int64_t s0 = 0; s0 < I.nsteps; s0 += depth) {
+        const int k = (int)((I.nsteps - s0) < depth ? (I.nsteps - s0) : depth);
+        const int SY = TILE + 2 * k;
         const int8_t* src = pool + I.off[cur];
         int8_t* dst = pool + I.off[cur ^ 1];
         for (int tile = 0; tile < ntx * nty; ++tile) {
-            const int64_t X0 = (int64_t)(tile % ntx) * kEnsTile, Y0 = (int64_t)(tile / ntx) * kEnsTile;
+            const int64_t X0 = (int64_t)(tile % ntx) * TILE, Y0 = (int64_t)(tile / ntx) * TILE;
             int8_t* A = A0;
             int8_t* B = B0;
             __syncthreads();
@@ -252,27 +255,27 @@ __device__ int run_tiled_fire(const EnsInstance& I, int8_t* pool, int8_t* A0, in
                 A[q] = boundary_value(I, src, I.pitch, X0 - HX + lx, Y0 - k + ly);
             }
             __syncthreads();
-            const bool interior = X0 - HX >= 0 && X0 + kEnsTile + HX <= I.n1 && Y0 - k >= 0 &&
-                                  Y0 + kEnsTile + k <= I.n2;
+            const bool interior = X0 - HX >= 0 && X0 + TILE + HX <= I.n1 && Y0 - k >= 0 &&
+                                  Y0 + TILE + k <= I.n2;
             for (int sub = 0; sub < k; ++sub) {
                 const DrawStep ds = draw_step(K, I.t0 + s0 + sub);
                 const int ex = k - 1 - sub;
-                const int w_lo = (HX - ex) >> 2, w_hi = (HX + kEnsTile + ex + 3) >> 2;
+                const int w_lo = (HX - ex) >> 2, w_hi = (HX + TILE + ex + 3) >> 2;
                 const bool exact = s0 == 0 && sub == 0;  // the run's first step may read any Int8 value
                 if (interior)
                     fire_substep_words<false>((const uint32_t*)A, (uint32_t*)B, SW, w_lo, w_hi - w_lo, k - ex,
-                                              kEnsTile + 2 * ex, X0 - HX, Y0 - k, g, ds, K, threadIdx.x, blockDim.x,
+                                              TILE + 2 * ex, X0 - HX, Y0 - k, g, ds, K, threadIdx.x, blockDim.x,
                                               exact);
                 else
                     fire_substep_words<true>((const uint32_t*)A, (uint32_t*)B, SW, w_lo, w_hi - w_lo, k - ex,
-                                             kEnsTile + 2 * ex, X0 - HX, Y0 - k, g, ds, K, threadIdx.x, blockDim.x,
+                                             TILE + 2 * ex, X0 - HX, Y0 - k, g, ds, K, threadIdx.x, blockDim.x,
                                              exact);
                 __syncthreads();
                 int8_t* tmp = A; A = B; B = tmp;
             }
-            for (int q = threadIdx.x; q < kEnsTile * kEnsTile; q += blockDim.x) {
-                const int64_t gx = X0 + q % kEnsTile, gy = Y0 + q / kEnsTile;
-                if (gx < I.n1 && gy < I.n2) dst[gx + gy * I.pitch] = A[(k + q / kEnsTile) * SX + HX + q % kEnsTile];
+            for (int q = threadIdx.x; q < TILE * TILE; q += blockDim.x) {
+                const int64_t gx = X0 + q % TILE, gy = Y0 + q / TILE;
+                if (gx < I.n1 && gy < I.n2) dst[gx + gy * I.pitch] = A[(k + q / TILE) * SX + HX + q % TILE];
             }
         }
         __syncthreads();
@@ -323,12 +326,14 @@ __device__ __noinline__ void summarize(const EnsInstance& I, const int8_t* base,
     for (int k = threadIdx.x; k < kEnsSumWords; k += blockDim.x) out->w[k] = (long long)red[k];
 }
 
+template <int TILE>
 __global__ void __launch_bounds__(kEnsThreads) k_ensemble(const EnsInstance* __restrict__ insts,
                                                           const int* __restrict__ order, int n,
                                                           int* __restrict__ counter, int8_t* __restrict__ pool,
                                                           EnsSummary* __restrict__ out, int* __restrict__ final_cur) {
-    __shared__ __align__(16) int8_t sA[kEnsBuf];
-    __shared__ __align__(16) int8_t sB[kEnsBuf];
+    extern __shared__ __align__(16) int8_t ens_smem[];
+    int8_t* sA = ens_smem;
+    int8_t* sB = ens_smem + ens_buf(TILE);
     __shared__ int s_q;
     for (;;) {
         __syncthreads();
@@ -352,11 +357,11 @@ __global__ void __launch_bounds__(kEnsThreads) k_ensemble(const EnsInstance* __r
                 fire_thresholds(I.thr_p, I.thr_f, I.params_f32 != 0, g);
                 g.exact_always = fire_odd_constant(I.bnd0, I.cval0, I.bnd1, I.cval1);
                 if (I.small) run_in_smem_fire(I, pool, sA, sB, K, g);
-                else cur = run_tiled_fire(I, pool, sA, sB, K, g);
+                else cur = run_tiled_fire<TILE>(I, pool, sA, sB, K, g);
             } else if (I.small) {
                 run_in_smem(I, pool, sA, sB, K);
             } else {
-                cur = run_tiled(I, pool, sA, sB, K);
+                cur = run_tiled<TILE>(I, pool, sA, sB, K);
             }
         }
         __syncthreads();
@@ -376,31 +381,66 @@ int efail(int code, const char* fmt, ...) {
     return code;
 }
 
+// The kernel for a tile size, with its shared memory opted in.
+template <int TILE>
+cudaError_t ens_kernel(void (**fn)(const EnsInstance*, const int*, int, int*, int8_t*, EnsSummary*, int*),
+                       size_t* smem) {
+    *fn = k_ensemble<TILE>;
+    *smem = 2 * (size_t)ens_buf(TILE);
+    return cudaFuncSetAttribute(k_ensemble<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+}
+
+cudaError_t ens_select(int tile, void (**fn)(const EnsInstance*, const int*, int, int*, int8_t*, EnsSummary*, int*),
+                       size_t* smem) {
+    switch (tile) {
+        case 64: return ens_kernel<64>(fn, smem);
+        case 192: return ens_kernel<192>(fn, smem);
+        default: return ens_kernel<128>(fn, smem);
+    }
+}
+
 }  // namespace
 
+bool ensemble_tile_ok(int tile) { return tile == 64 || tile == 128 || tile == 192; }
+
 cudaError_t launch_ensemble(const EnsInstance* d_inst, const int* d_order, int n, int* d_counter, int8_t* pool,
-                            EnsSummary* d_out, int* d_cur, int grid, cudaStream_t st) {
+                            EnsSummary* d_out, int* d_cur, int grid, cudaStream_t st, int tile) {
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    k_ensemble<<<grid, kEnsThreads, 0, st>>>(d_inst, d_order, n, d_counter, pool, d_out, d_cur);
+    void (*fn)(const EnsInstance*, const int*, int, int*, int8_t*, EnsSummary*, int*) = nullptr;
+    size_t smem = 0;
+    e = ens_select(tile, &fn, &smem);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, kEnsThreads, smem, st>>>(d_inst, d_order, n, d_counter, pool, d_out, d_cur);
     count_launch();
     return cudaGetLastError();
 }
 
-int ensemble_grid() {
+int ensemble_grid(int tile) {
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ensemble, kEnsThreads, 0);
+    void (*fn)(const EnsInstance*, const int*, int, int*, int8_t*, EnsSummary*, int*) = nullptr;
+    size_t smem = 0;
+    if (ens_select(tile, &fn, &smem) == cudaSuccess)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kEnsThreads, smem);
+    cudaGetLastError();
     return nsm * (per > 0 ? per : 1);
 }
 
-int ensemble_smem_cells() { return kEnsBuf; }
+int ensemble_smem_cells(int tile) { return ens_buf(tile); }
 
-bool ensemble_fits_smem(const gbca_desc& d) {
+bool ensemble_fits_smem(const gbca_desc& d, int tile) {
+    const int buf = ens_buf(tile);
     if (d.rule == GBCA_RULE_FOREST_FIRE && d.nbhd == GBCA_VON_NEUMANN && d.radius == 1)
-        return (d.n1 + 8 + 3) / 4 * 4 * (d.n2 + 2) <= kEnsBuf;
-    return (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= kEnsBuf;
+        return (d.n1 + 8 + 3) / 4 * 4 * (d.n2 + 2) <= buf;
+    return (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= buf;
+}
+
+int ensemble_depth(const gbca_desc& d, int depth) {
+    const int cap = kEnsMaxHalo / d.radius;  // the halo of a pass fits the tile's margin
+    if (depth <= 0 || depth > cap) depth = cap;
+    return depth < 1 ? 1 : depth;
 }
 
 }  // namespace gbca
@@ -423,8 +463,31 @@ struct gbca_ensemble {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t exec = nullptr;
     int grid = 0;
+    int tile = 128;   // the kernel's tile side (gbca_ensemble_set_geometry / gbca_ensemble_tune)
+    int depth = 0;    // steps per pass of the tiled path; 0: the deepest the halo allows
     bool ran = false;
 };
+
+namespace {
+
+// Applies a geometry: the small-lattice split and pass depth of every instance, the grid, and
+// a fresh graph at the next run.
+void apply_geometry(gbca_ensemble* e, int tile, int depth) {
+    e->tile = tile;
+    e->depth = depth;
+    for (int32_t i = 0; i < e->n; ++i) {
+        EnsInstance& I = e->h_inst[(size_t)i];
+        I.small = ensemble_fits_smem(e->descs[(size_t)i], tile) ? 1 : 0;
+        I.depth = ensemble_depth(e->descs[(size_t)i], depth);
+    }
+    e->grid = ensemble_grid(tile);
+    if (e->exec) {
+        cudaGraphExecDestroy(e->exec);
+        e->exec = nullptr;
+    }
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -467,7 +530,8 @@ int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out)
         I.bnd1 = d.boundary[1];
         I.cval0 = d.boundary[0] == GBCA_CONSTANT ? (int32_t)d.constant[0] : 0;
         I.cval1 = d.boundary[1] == GBCA_CONSTANT ? (int32_t)d.constant[1] : 0;
-        I.small = ensemble_fits_smem(d) ? 1 : 0;
+        I.small = ensemble_fits_smem(d, 128) ? 1 : 0;
+        I.depth = ensemble_depth(d, 0);
         I.summarize = 1;
     }
     if (gbca_device_count() < 1) return efail(GBCA_ERR_CUDA, "no CUDA device is visible");
@@ -488,10 +552,6 @@ int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out)
     if (c == cudaSuccess) c = cudaMemsetAsync(e->pool, 0, e->pool_bytes, e->stream);
     if (c == cudaSuccess) c = cudaMemsetAsync(e->d_out, 0, sizeof(EnsSummary) * n, e->stream);
     if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
-    int dev = 0, nsm = 0, per = 0;
-    if (c == cudaSuccess) c = cudaGetDevice(&dev);
-    if (c == cudaSuccess) c = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (c == cudaSuccess) c = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ensemble, kEnsThreads, 0);
     if (c != cudaSuccess) {
         const bool oom = c == cudaErrorMemoryAllocation;
         gbca_ensemble_destroy(e);
@@ -499,7 +559,7 @@ int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out)
         return oom ? efail(GBCA_ERR_OUT_OF_MEMORY, "ensemble allocation of %zu bytes failed", off)
                    : efail(GBCA_ERR_CUDA, "gbca_ensemble_create: %s", cudaGetErrorString(c));
     }
-    e->grid = nsm * (per > 0 ? per : 1);
+    e->grid = ensemble_grid(e->tile);
     *out = e;
     return GBCA_OK;
 }
@@ -568,11 +628,14 @@ int gbca_ensemble_run(gbca_ensemble* e, const int64_t* t0, const int64_t* nsteps
     if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble upload: %s", cudaGetErrorString(c));
     if (!e->exec) {  // capture the run once: reset the work counter, one persistent launch
         cudaGraph_t g = nullptr;
-        c = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+        void (*fn)(const EnsInstance*, const int*, int, int*, int8_t*, EnsSummary*, int*) = nullptr;
+        size_t smem = 0;
+        c = ens_select(e->tile, &fn, &smem);  // sets the kernel's shared-memory limit before capture
+        if (c == cudaSuccess) c = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
         if (c == cudaSuccess) {
             cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream);
-            k_ensemble<<<e->grid, kEnsThreads, 0, e->stream>>>(e->d_inst, e->d_order, e->n, e->d_counter, e->pool,
-                                                               e->d_out, e->d_cur);
+            fn<<<e->grid, kEnsThreads, smem, e->stream>>>(e->d_inst, e->d_order, e->n, e->d_counter, e->pool,
+                                                          e->d_out, e->d_cur);
             c = cudaStreamEndCapture(e->stream, &g);
         }
         if (c == cudaSuccess) c = cudaGraphInstantiate(&e->exec, g, 0);
@@ -621,6 +684,82 @@ int gbca_ensemble_summaries(gbca_ensemble* e, int64_t* counts, int32_t nvals, in
             morans[i] = morans_from_sums(w[kEnsCounts + 1], w[kEnsCounts + 2], w[kEnsCounts + 3], w[kEnsCounts + 4],
                                          w[kEnsCounts + 5], ncell);
     }
+    return GBCA_OK;
+}
+
+int gbca_ensemble_set_geometry(gbca_ensemble* e, int32_t tile, int32_t depth) {
+    if (!e) return efail(GBCA_ERR_ARGUMENT, "null ensemble");
+    if (!ensemble_tile_ok(tile)) return efail(GBCA_ERR_ARGUMENT, "ensemble tiles are 64, 128 or 192 cells, got %d", tile);
+    if (depth < 0 || depth > kEnsMaxHalo)
+        return efail(GBCA_ERR_ARGUMENT, "depth must lie in 0:%d (0: the deepest), got %d", kEnsMaxHalo, depth);
+    int rc = gbca_ensemble_sync(e);
+    if (rc != GBCA_OK) return rc;
+    apply_geometry(e, tile, depth);
+    return GBCA_OK;
+}
+
+int gbca_ensemble_tune(gbca_ensemble* e, int64_t probe_steps, const double* params, int32_t nparams, int32_t* tile,
+                       int32_t* depth) {
+    if (!e) return efail(GBCA_ERR_ARGUMENT, "null ensemble");
+    if (probe_steps < 1) return efail(GBCA_ERR_ARGUMENT, "probe_steps must be positive");
+    int rc = gbca_ensemble_sync(e);
+    if (rc != GBCA_OK) return rc;
+    // keep the states and each instance's current buffer; every candidate starts from them
+    std::vector<int32_t> cur0((size_t)e->n);
+    for (int32_t i = 0; i < e->n; ++i) cur0[(size_t)i] = e->h_inst[(size_t)i].cur;
+    int8_t* saved = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t c = cudaMalloc(&saved, e->pool_bytes);
+    if (c == cudaSuccess) c = cudaMemcpyAsync(saved, e->pool, e->pool_bytes, cudaMemcpyDeviceToDevice, e->stream);
+    if (c == cudaSuccess) c = cudaEventCreate(&ev[0]);
+    if (c == cudaSuccess) c = cudaEventCreate(&ev[1]);
+    const std::vector<int64_t> steps((size_t)e->n, probe_steps);
+    const int tiles[3] = {64, 128, 192}, depths[3] = {2, 4, 0};
+    float best = -1.0f;
+    int best_tile = e->tile, best_depth = e->depth;
+    for (int a = 0; a < 3 && c == cudaSuccess && rc == GBCA_OK; ++a)
+        for (int b = 0; b < 3 && c == cudaSuccess && rc == GBCA_OK; ++b) {
+            apply_geometry(e, tiles[a], depths[b]);
+            float ms_min = -1.0f;
+            for (int rep = 0; rep < 2 && c == cudaSuccess && rc == GBCA_OK; ++rep) {
+                for (int32_t i = 0; i < e->n; ++i) e->h_inst[(size_t)i].cur = cur0[(size_t)i];
+                c = cudaMemcpyAsync(e->pool, saved, e->pool_bytes, cudaMemcpyDeviceToDevice, e->stream);
+                if (c == cudaSuccess) c = cudaEventRecord(ev[0], e->stream);
+                if (c != cudaSuccess) break;
+                rc = gbca_ensemble_run(e, nullptr, steps.data(), params, nparams);
+                if (rc != GBCA_OK) break;
+                c = cudaEventRecord(ev[1], e->stream);
+                if (c == cudaSuccess) rc = gbca_ensemble_sync(e);
+                float ms = 0.0f;
+                if (c == cudaSuccess && rc == GBCA_OK) c = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+                if (ms_min < 0.0f || ms < ms_min) ms_min = ms;
+            }
+            if (c == cudaSuccess && rc == GBCA_OK && (best < 0.0f || ms_min < best)) {
+                best = ms_min;
+                best_tile = tiles[a];
+                best_depth = depths[b];
+            }
+        }
+    for (int32_t i = 0; i < e->n; ++i) e->h_inst[(size_t)i].cur = cur0[(size_t)i];
+    if (saved) {
+        const cudaError_t c2 = cudaMemcpyAsync(e->pool, saved, e->pool_bytes, cudaMemcpyDeviceToDevice, e->stream);
+        const cudaError_t c3 = cudaStreamSynchronize(e->stream);
+        if (c == cudaSuccess) c = c2 != cudaSuccess ? c2 : c3;
+        cudaFree(saved);
+    }
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    apply_geometry(e, best_tile, best_depth);
+    if (rc != GBCA_OK) return rc;
+    if (c != cudaSuccess) {
+        cudaGetLastError();
+        return c == cudaErrorMemoryAllocation
+                   ? efail(GBCA_ERR_OUT_OF_MEMORY, "the tuner's copy of the ensemble (%zu bytes) did not fit",
+                           e->pool_bytes)
+                   : efail(GBCA_ERR_CUDA, "ensemble tuning: %s", cudaGetErrorString(c));
+    }
+    if (tile) *tile = best_tile;
+    if (depth) *depth = best_depth;
     return GBCA_OK;
 }
 

@@ -21,20 +21,27 @@ struct EnsInstance {
     int32_t cur;             // buffer holding the current state
     int32_t small;           // fits in shared memory with its halo
     int32_t summarize;       // reduce the final state to its summaries at the end of the run
+    int32_t depth;           // steps per temporally blocked pass of the tiled path
+    int32_t pad_;
 };
 
 struct EnsSummary {
     long long w[kEnsSumWords];
 };
 
+// The ensemble kernel runs tiles of 64, 128 or 192 cells a side (a template parameter; its
+// shared buffers and the small-lattice threshold follow the tile).
+bool ensemble_tile_ok(int tile);
 // One persistent launch over n instances (order: the queue order); resets the counter first.
 cudaError_t launch_ensemble(const EnsInstance* d_inst, const int* d_order, int n, int* d_counter, int8_t* pool,
-                            EnsSummary* d_out, int* d_cur, int grid, cudaStream_t st);
+                            EnsSummary* d_out, int* d_cur, int grid, cudaStream_t st, int tile = 128);
 // Grid size that fills the current device with resident CTAs.
-int ensemble_grid();
+int ensemble_grid(int tile = 128);
 // Bytes of each of the two shared buffers a CTA of the ensemble kernel has.
-int ensemble_smem_cells();
+int ensemble_smem_cells(int tile = 128);
 // Whether an instance runs with its whole lattice (and halo) in shared memory.
-bool ensemble_fits_smem(const gbca_desc& d);
+bool ensemble_fits_smem(const gbca_desc& d, int tile = 128);
+// Steps per pass of the tiled path for a requested depth (0: the deepest the halo allows).
+int ensemble_depth(const gbca_desc& d, int depth);
 
 }  // namespace gbca

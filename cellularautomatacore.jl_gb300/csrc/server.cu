@@ -229,6 +229,7 @@ EnsInstance small_instance(const Request* r, int64_t steps, bool last) {
     I.cval1 = d.boundary[1] == GBCA_CONSTANT ? (int32_t)d.constant[1] : 0;
     I.cur = r->cur;
     I.small = ensemble_fits_smem(d) ? 1 : 0;
+    I.depth = ensemble_depth(d, 0);
     I.summarize = last ? 1 : 0;
     return I;
 }

@@ -72,6 +72,24 @@ class BatchedEnsemble:
     def sync(self):
         capi.check(capi.lib().gbca_ensemble_sync(self.handle))
 
+    def set_geometry(self, tile: int = 128, depth: int = 0):
+        """The batched kernel's tile side (64, 128, 192) and steps per pass (0: deepest)."""
+        capi.check(capi.lib().gbca_ensemble_set_geometry(self.handle, int(tile), int(depth)))
+
+    def tune(self, probe_steps: int = 16, params=None):
+        """Times every (tile, depth) on this ensemble's instances for probe_steps steps from
+        their current states (restored afterwards), keeps the fastest; returns it."""
+        n = self.n
+        vals = []
+        for i, p in enumerate(self.probs):
+            pv = _params_tuple(p.rule, p.p if params is None else params[i]) if isinstance(p.rule, ForestFire) else ()
+            vals.extend(list(pv) + [0.0] * (2 - len(pv)))
+        P = (ctypes.c_double * (2 * n))(*vals)
+        tile, depth = ctypes.c_int32(), ctypes.c_int32()
+        capi.check(capi.lib().gbca_ensemble_tune(self.handle, int(probe_steps), P, 2, ctypes.byref(tile),
+                                                 ctypes.byref(depth)))
+        return int(tile.value), int(depth.value)
+
     def summaries(self, nvals: int = 3):
         """(counts[n][nvals], other[n], morans[n]) of every instance's state after the last run."""
         n = self.n

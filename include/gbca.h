@@ -253,6 +253,21 @@ int gbca_ensemble_summaries(gbca_ensemble* e, int64_t* counts, int32_t nvals, in
 /* current_state of instance i. */
 int gbca_ensemble_get_state(gbca_ensemble* e, int32_t i, void* host, size_t nbytes);
 
+/* The ensemble kernel's geometry: tiles of `tile` cells a side (64, 128 or 192; the shared
+ * buffers, hence which lattices live whole in shared memory, follow the tile) and `depth`
+ * steps per temporally blocked pass of the tiled path (1..8, 0 = the deepest the halo of 8
+ * cells allows for the instance's radius). Results never depend on it. No counterpart in the
+ * reference. */
+int gbca_ensemble_set_geometry(gbca_ensemble* e, int32_t tile, int32_t depth);
+
+/* The autotuner for the batched path: times every (tile, depth) candidate on the ensemble's
+ * own instances for `probe_steps` steps each from their current states (restored after every
+ * candidate and at the end; params as in gbca_ensemble_run), keeps the fastest and returns it.
+ * It allocates one copy of the ensemble's state pool while it runs; summaries are those of the
+ * last probe until the next gbca_ensemble_run. No counterpart in the reference. */
+int gbca_ensemble_tune(gbca_ensemble* e, int64_t probe_steps, const double* params, int32_t nparams, int32_t* tile,
+                       int32_t* depth);
+
 /* ---- serving: a device-resident request loop with continuous batching. Clients submit
  * simulation requests at any time; a scheduler thread admits them in arrival order while
  * their state buffers fit the HBM budget, advances every admitted request by up to

@@ -138,3 +138,34 @@ def test_abc_batched_equals_serial(ca):
         s = ca.solve(prob.remake(p=proposals[i - 1], seed=prob.seed + i), save_everystep=False)
         assert res.proposal_distances[i - 1] == dist(s, observed)
     assert res.distances == sorted(res.proposal_distances)[:4]
+
+
+def test_batched_geometries_and_tuner(ca):
+    """Every tile side and pass depth of the batched kernel gives the same states and
+    summaries; the tuner restores the states it probes and picks one of the candidates."""
+    probs = mixed_problems(ca, n=20, seed=11)
+    steps = [p.tspan[1] for p in probs]
+    ref = None
+    for tile in (64, 128, 192):
+        for depth in (1, 3, 0):
+            ens = ca.BatchedEnsemble(probs)
+            ens.set_initial_states()
+            ens.set_geometry(tile, depth)
+            ens.run(nsteps=steps)
+            out = [ens.state(i) for i in range(len(probs))], ens.summaries(3)
+            ens.close()
+            if ref is None:
+                ref = out
+                continue
+            assert all(np.array_equal(a, b) for a, b in zip(out[0], ref[0])), (tile, depth)
+            assert np.array_equal(out[1][0], ref[1][0]) and np.array_equal(out[1][1], ref[1][1])
+    ens = ca.BatchedEnsemble(probs)
+    ens.set_initial_states()
+    tile, depth = ens.tune(probe_steps=6)
+    assert tile in (64, 128, 192) and depth in (2, 4, 0)
+    assert all(np.array_equal(ens.state(i), np.asarray(p.u0)) for i, p in enumerate(probs))
+    ens.run(nsteps=steps)
+    assert all(np.array_equal(ens.state(i), ref[0][i]) for i in range(len(probs)))
+    ens.close()
+    with pytest.raises(ca.ArgumentError):
+        ca.BatchedEnsemble(probs).set_geometry(100, 0)
