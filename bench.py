@@ -190,6 +190,10 @@ def cpu_sample(nthreads: int):
             "parts_gcells": {"ltl": r1 / 1e9, "fire": r2 / 1e9}, "seconds": t2 - t0, "cell_updates": cu}
 
 
+WORKLOAD = ("single-instance sweeps: Larger-than-Life Moore(5) B34..45/S34..58 on an 8192^2 Int8 torus x 1000 "
+            "steps + forest fire VonNeumann(1) on a 16384^2 Grid Constant(0) x 500 steps (p=0.03, f=1e-4)")
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -206,8 +210,9 @@ def run_reference(args, rank, world):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int8", "data": "synthetic",
-            "config": {"workload": "single-instance sweeps: LtL Moore(5) 8192^2 torus x1000 + forest fire "
-                                   "16384^2 Grid x500 (bounded CPU samples per step)"},
+            "config": {"workload": WORKLOAD, "cell_updates_per_step": cell_updates(), "parallelism": "replicas x1",
+                       "sample": "each step times a bounded sample of the workload on the host cores (3 LtL steps "
+                                 "on 8192^2 + 1 forest-fire step on 16384^2, weighted 1000:500)"},
             "cpu_baseline": {"value": v, "unit": "Gcell-updates/s", "cores": nthreads, "kind": "port",
                              "sample": "per step: 3 LtL steps on 8192^2 + 1 forest-fire step on 16384^2"},
             "e2e": {"value": v, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -755,9 +760,7 @@ def main():
         line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "int8", "data": "synthetic",
-                "config": {"workload": "single-instance sweeps: Larger-than-Life Moore(5) B34..45/S34..58 on an "
-                                       "8192^2 Int8 torus x 1000 steps + forest fire VonNeumann(1) on a 16384^2 Grid "
-                                       "Constant(0) x 500 steps (p=0.03, f=1e-4)",
+                "config": {"workload": WORKLOAD,
                            "cell_updates_per_step": cell_updates(), "parallelism": f"replicas x{world}",
                            "geometry": {k: {"steps_per_pass": v[0], "tile_rows": v[1]} for k, v in geometry.items()},
                            "l2": "inputs larger than L2: the 16384^2 state is 268 MB, and each step re-copies "

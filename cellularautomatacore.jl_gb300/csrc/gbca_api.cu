@@ -74,6 +74,13 @@ int cuda_fail(cudaError_t e, const char* what) {
     return fail(GBCA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+// A tile-copy wait that gave up leaves its tile unwritten: report it once the work is done.
+int check_timeouts() {
+    const int n = gbca::fire_tma_timeouts_take();
+    if (n) return fail(GBCA_ERR_TIMEOUT, "%d tile copies did not complete within their wait limit", n);
+    return GBCA_OK;
+}
+
 #define GBCA_CUDA(call, what)                          \
     do {                                               \
         cudaError_t e_ = (call);                       \
@@ -450,7 +457,7 @@ int gbca_get_state(gbca_handle* h, void* host, size_t nbytes) {
                                 cudaMemcpyDeviceToHost, h->stream),
               "current_state copy");
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "current_state");
-    return GBCA_OK;
+    return check_timeouts();
 }
 
 int gbca_advance(gbca_handle* h, int64_t t, int64_t nsteps, const double* params, int32_t nparams) {
@@ -631,7 +638,7 @@ int gbca_write_cell(gbca_handle* h, int64_t i, int64_t j, const void* value) {
 int gbca_sync(gbca_handle* h) {
     if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
     GBCA_CUDA(cudaStreamSynchronize(h->stream), "sync");
-    return GBCA_OK;
+    return check_timeouts();
 }
 
 int gbca_set_sparse(gbca_handle* h, int32_t enable, int32_t background, int32_t tilesize) {

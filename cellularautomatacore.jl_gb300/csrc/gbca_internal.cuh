@@ -240,5 +240,7 @@ int life_steps_per_pass(const SweepParams& p);
 bool life_choice_fits(const SweepParams& p, int steps, int rows);
 bool fire_fast_supported(const SweepParams& p);
 cudaError_t launch_fire(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
+// Tiles whose TMA copy did not complete within its wait limit since the last call (cleared).
+int fire_tma_timeouts_take();
 
 }  // namespace gbca

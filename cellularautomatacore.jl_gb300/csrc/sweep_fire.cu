@@ -9,21 +9,72 @@
 // draw_fast() hoists the products that do not depend on the cell out of the cell loop,
 // and temporal blocking (nsub steps per pass, halo nsub) keeps HBM traffic at
 // 2 B / nsub per cell-update.
+//
+// Tile staging: where the tile's loaded region lies inside the lattice, or the lattice is a
+// Grid with Constant(0) edges (the tensor's zero fill is then the boundary value), one TMA
+// copy (cp.async.bulk.tensor) brings the whole halo-padded tile into shared memory (for the
+// zero-fill case n1 must be a multiple of 16, so no box reaches the column padding). The state
+// is viewed as a 3-D tensor (16-byte segments x segments x rows), so a box of
+// 16 x (sx / 16) x sy lands as rows of sx bytes, the tile's own layout. Other tiles load
+// through the boundary map. The copy's completion is awaited on an mbarrier with an
+// iteration limit; on expiry the CTA records a timeout (reported by gbca_sync /
+// gbca_get_state), waits once more with a limit and leaves its tile unwritten.
+#include <cuda.h>
+
+#include <cstring>
+#include <mutex>
+#include <vector>
+
 #include "fire_words.cuh"
 #include "gbca_internal.cuh"
 
 namespace gbca {
 
+__device__ int g_fire_tma_timeouts = 0;
+
 namespace {
 
 constexpr int kFireTX = 256, kFireTY = 128;
 constexpr int kFireThreadsX = 32, kFireThreadsY = 16;
+constexpr int kTmaSpins = 1 << 22;  // try_wait polls before a tile gives up
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase) {
+    for (int it = 0; it < kTmaSpins; ++it)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+
+// One thread: arm the barrier for `bytes` and issue the 3-D tile copy into `dst`.
+__device__ __forceinline__ void tma_tile_load(const CUtensorMap* map, void* dst, uint64_t* bar, int seg0, int row0,
+                                              uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(0), "r"(seg0), "r"(row0), "r"(smem_u32(bar))
+        : "memory");
+}
 
 // Four cells (one 32-bit word of the shared tile) per work item: neighbour tests in byte
 // SIMD, then four independent Philox chains.
 template <bool INTERIOR>
 __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __restrict__ src,
-                                          int8_t* __restrict__ dst, int8_t* A, int8_t* B) {
+                                          int8_t* __restrict__ dst, int8_t* A, int8_t* B, bool staged) {
     const int hx = p.halo_x, hy = p.halo_y;
     const int sx = kFireTX + 2 * hx, sy = kFireTY + 2 * hy;
     const int sw = sx / 4;  // words per shared row
@@ -31,7 +82,8 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
     const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
     const int nthr = kFireThreadsX * kFireThreadsY;
 
-    if (INTERIOR) {  // 16-byte loads: X0 - hx, sx and the pitch are multiples of 16
+    if (staged) {  // the tile arrived by TMA
+    } else if (INTERIOR) {  // 16-byte loads: X0 - hx, sx and the pitch are multiples of 16
         const int qx = sx / 16;
         for (int q = tid; q < qx * sy; q += nthr) {
             const int lq = q % qx, ly = q / qx;
@@ -82,20 +134,112 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
     }
 }
 
-__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY) k_fire(SweepParams p, const int8_t* __restrict__ src,
-                                                                      int8_t* __restrict__ dst) {
-    extern __shared__ __align__(16) int8_t smem_f[];
+// tma: 0 = no tensor map; 1 = stage interior tiles by TMA; 2 = every tile (Constant(0) edges).
+__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
+    k_fire(SweepParams p, const int8_t* __restrict__ src, int8_t* __restrict__ dst,
+           const __grid_constant__ CUtensorMap tmap, int tma) {
+    extern __shared__ __align__(128) int8_t smem_f[];
+    __shared__ __align__(8) uint64_t tma_bar;
     const int sx = kFireTX + 2 * p.halo_x, sy = kFireTY + 2 * p.halo_y;
     int8_t* A = smem_f;
     int8_t* B = smem_f + sx * sy;
     const int64_t X0 = (int64_t)blockIdx.x * kFireTX, Y0 = (int64_t)blockIdx.y * kFireTY;
     const bool interior = X0 - p.halo_x >= 0 && X0 + kFireTX + p.halo_x <= p.n1 && Y0 - p.halo_y >= 0 &&
                           Y0 + kFireTY + p.halo_y <= p.n2;
-    if (interior) fire_tile<true>(p, src, dst, A, B);
-    else fire_tile<false>(p, src, dst, A, B);
+    const bool staged = tma == 2 || (tma == 1 && interior);
+    if (staged) {
+        const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&tma_bar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        __syncthreads();
+        // the region starts at lattice (X0 - halo_x, Y0 - halo_y): segment (X0 - halo_x) / 16,
+        // a whole number since X0 and halo_x are multiples of 16; innermost coordinate 0
+        if (tid == 0)
+            tma_tile_load(&tmap, A, &tma_bar, (int)((X0 - p.halo_x) / 16), (int)(Y0 - p.halo_y),
+                          (uint32_t)(sx * sy));
+        const bool ok = __syncthreads_and(mbar_wait_bounded(&tma_bar, 0));
+        if (!ok) {
+            if (tid == 0) atomicAdd(&g_fire_tma_timeouts, 1);
+            mbar_wait_bounded(&tma_bar, 0);  // let a late copy land before the CTA leaves
+            return;
+        }
+    }
+    if (interior) fire_tile<true>(p, src, dst, A, B, staged);
+    else fire_tile<false>(p, src, dst, A, B, staged);
+}
+
+// Tensor maps of the state buffers, by buffer and box height (the pass depth sets it).
+struct MapKey {
+    const void* base;
+    int64_t n1, n2, pitch;
+    int sx, sy;
+};
+struct MapEntry {
+    MapKey k;
+    CUtensorMap map;
+};
+
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+std::mutex g_map_mu;
+std::vector<MapEntry> g_maps;  // a few entries: two buffers x the depths in use
+EncodeTiled g_encode = nullptr;
+bool g_encode_looked = false;
+
+// The 3-D view (16-byte segments, segment index, row) of a state buffer with a box of one
+// whole tile; false when the driver offers no tensor maps.
+bool tile_map(const void* base, int64_t n1, int64_t n2, int64_t pitch, int sx, int sy, CUtensorMap* out) {
+    std::lock_guard<std::mutex> lock(g_map_mu);
+    for (const MapEntry& m : g_maps)
+        if (m.k.base == base && m.k.n1 == n1 && m.k.n2 == n2 && m.k.pitch == pitch && m.k.sx == sx && m.k.sy == sy) {
+            *out = m.map;
+            return true;
+        }
+    if (!g_encode_looked) {
+        g_encode_looked = true;
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = (EncodeTiled)fn;
+        cudaGetLastError();
+    }
+    if (!g_encode) return false;
+    const cuuint64_t dims[3] = {16, (cuuint64_t)((n1 + 15) / 16), (cuuint64_t)n2};
+    const cuuint64_t strides[2] = {16, (cuuint64_t)pitch};
+    const cuuint32_t box[3] = {16, (cuuint32_t)(sx / 16), (cuuint32_t)sy};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUtensorMap m;
+    if (g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<void*>(base), dims, strides, box, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    if (g_maps.size() >= 16) g_maps.erase(g_maps.begin());
+    g_maps.push_back(MapEntry{MapKey{base, n1, n2, pitch, sx, sy}, m});
+    *out = m;
+    return true;
 }
 
 }  // namespace
+
+int fire_tma_timeouts_take() {
+    int n = 0;
+    if (cudaMemcpyFromSymbol(&n, g_fire_tma_timeouts, sizeof n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (n) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_fire_tma_timeouts, &zero, sizeof zero);
+    }
+    return n;
+}
 
 bool fire_fast_supported(const SweepParams& p) {
     return !p.mask && p.rule == GBCA_RULE_FOREST_FIRE && p.nbhd == GBCA_VON_NEUMANN && p.radius == 1 &&
@@ -109,11 +253,23 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     p.halo_y = p.nsub;
     p.halo_x = (p.nsub + 15) / 16 * 16;
     p.keys = philox_keys(p.seed);
-    const size_t smem = 2 * (size_t)(kFireTX + 2 * p.halo_x) * (size_t)(kFireTY + 2 * p.halo_y);
+    const int sx = kFireTX + 2 * p.halo_x, sy = kFireTY + 2 * p.halo_y;
+    const size_t smem = 2 * (size_t)sx * (size_t)sy;
     cudaError_t e = cudaFuncSetAttribute(k_fire, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    // TMA staging: interior tiles always; every tile when both edges are Constant(0), whose
+    // value the tensor's zero fill reproduces, and n1 is a whole number of 16-byte segments
+    // (so no box reads the column padding past n1)
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    int tma = 0;
+    if (sy <= 256 && sx / 16 <= 256 && ((uintptr_t)src & 15u) == 0 && tile_map(src, p.n1, p.n2, p.pitch, sx, sy, &map)) {
+        const bool zero_edges = p.bnd[0] == GBCA_CONSTANT && p.bnd[1] == GBCA_CONSTANT && p.cval[0] == 0 &&
+                                p.cval[1] == 0 && p.n1 % 16 == 0;
+        tma = zero_edges ? 2 : 1;
+    }
     dim3 grid((unsigned)((p.n1 + kFireTX - 1) / kFireTX), (unsigned)((p.n2 + kFireTY - 1) / kFireTY));
-    k_fire<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(p, src, dst);
+    k_fire<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(p, src, dst, map, tma);
     return cudaGetLastError();
 }
 

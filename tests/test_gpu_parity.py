@@ -98,6 +98,10 @@ CASES = [
     ("forest fire, p = 0, f = 1, Float32", "fire", (300, 260), dict(nb="vn", seed=2, f32=True), 9, 9, (0.0, 1.0)),
     ("forest fire, reflecting edges, tiled", "fire", (700, 300), dict(nb="vn", seed=12, bnd=("r", "p")), 17, 17,
      (0.07, 0.003)),
+    # n1 a multiple of 16 on a Constant(0) grid: every tile, edges included, staged by TMA
+    ("forest fire, TMA-staged grid", "fire", (1024, 600), dict(nb="vn", seed=13, bnd=("c", "c")), 25, 25,
+     (0.05, 0.001)),
+    ("forest fire, TMA-staged interior, torus", "fire", (1536, 520), dict(nb="vn", seed=14), 19, 19, (0.05, 0.002)),
 ]
 
 
