@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--n", type=int, default=4096)
     ap.add_argument("--no-tune", action="store_true", help="keep the kernels' default sweep geometry")
     ap.add_argument("--spp", type=int, default=0, help="--case: pin this many steps per pass (no tuning)")
+    ap.add_argument("--staging", type=int, default=0, help="--case with --spp: 1 stages fire tiles by TMA")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-saves", action="store_true", help="skip the save-path measurement")
     ap.add_argument("--no-sparse", action="store_true", help="skip the active-tile measurement")
@@ -257,7 +258,7 @@ def run_case(args):
     nparams = 2 if params is not None else 0
     geometry = None
     if args.case in ("ltl", "fire") and args.spp > 0:
-        capi.check(lib.gbca_set_geometry(h, args.spp, 0))
+        capi.check(lib.gbca_set_geometry(h, args.spp, 0, args.staging))
         per = args.spp
     elif args.case in ("ltl", "fire") and not args.no_tune:
         geometry = tune(capi, lib, h, params, nparams)
@@ -290,10 +291,10 @@ ENS = dict(n=4096, steps=500, plain_sample=256)
 
 
 def tune(capi, lib, h, params, nparams):
-    """The autotuner's (steps per pass, tile rows) for the handle's shape, timed on its state."""
-    k, rows = ctypes.c_int32(), ctypes.c_int32()
-    capi.check(lib.gbca_tune(h, params, nparams, ctypes.byref(k), ctypes.byref(rows)))
-    return int(k.value), int(rows.value)
+    """The autotuner's (steps per pass, tile rows, staging) for the handle's shape, timed on its state."""
+    k, rows, staging = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    capi.check(lib.gbca_tune(h, params, nparams, ctypes.byref(k), ctypes.byref(rows), ctypes.byref(staging)))
+    return int(k.value), int(rows.value), int(staging.value)
 
 
 SAVES = [dict(name="highlife-128", rule="highlife", n=128, steps=200, saveat=20),
@@ -762,7 +763,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "int8", "data": "synthetic",
                 "config": {"workload": WORKLOAD,
                            "cell_updates_per_step": cell_updates(), "parallelism": f"replicas x{world}",
-                           "geometry": {k: {"steps_per_pass": v[0], "tile_rows": v[1]} for k, v in geometry.items()},
+                           "geometry": {k: {"steps_per_pass": v[0], "tile_rows": v[1], "tma_staging": v[2]}
+                                        for k, v in geometry.items()},
                            "l2": "inputs larger than L2: the 16384^2 state is 268 MB, and each step re-copies "
                                  "335 MB of initial states"},
                 "roofline": roofline, "philox_roof": philox_roof, "parts": parts, "e2e": e2e, "gpu_launches": launches,

@@ -286,16 +286,18 @@ def device_summaries(st: GB300State, nvals: int = 3):
 def tune(st: GB300State, prob=None, p=None):
     """Times the candidate sweep geometries of the state's fast kernel on its current state
     (restored afterwards) and caches the fastest for the problem's shape; returns
-    (steps per pass, tile rows), (0, 0) when the problem runs on the general kernel."""
+    (steps per pass, tile rows, staging), (0, 0, 0) when the problem runs on the general kernel."""
     st.flush()
     vals = _params_tuple(prob.rule, p if p is not None else prob.p) if prob is not None else ()
     arr = (ctypes.c_double * max(1, len(vals)))(*vals)
-    k, rows = ctypes.c_int32(), ctypes.c_int32()
-    capi.check(capi.lib().gbca_tune(st.handle, arr, len(vals), ctypes.byref(k), ctypes.byref(rows)))
-    return int(k.value), int(rows.value)
+    k, rows, staging = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    capi.check(capi.lib().gbca_tune(st.handle, arr, len(vals), ctypes.byref(k), ctypes.byref(rows),
+                                    ctypes.byref(staging)))
+    return int(k.value), int(rows.value), int(staging.value)
 
 
-def set_geometry(st: GB300State, steps_per_pass: int = 0, tile_rows: int = 0) -> None:
-    """Pins the state's sweep geometry; (0, 0) returns it to the tuned or default one."""
+def set_geometry(st: GB300State, steps_per_pass: int = 0, tile_rows: int = 0, staging: int = 0) -> None:
+    """Pins the state's sweep geometry (staging 1: the forest fire's tiles by TMA); (0, 0, 0)
+    returns it to the tuned or default one."""
     st.flush()
-    capi.check(capi.lib().gbca_set_geometry(st.handle, int(steps_per_pass), int(tile_rows)))
+    capi.check(capi.lib().gbca_set_geometry(st.handle, int(steps_per_pass), int(tile_rows), int(staging)))

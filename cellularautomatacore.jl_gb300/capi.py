@@ -70,7 +70,8 @@ SIGNATURES = {
     "gbca_device_state": (ctypes.c_int, [_V, _P(_V), _P(_I64)]),
     "gbca_set_stream": (ctypes.c_int, [_V, _V]),
     "gbca_kernel_launches": (ctypes.c_int64, []),
-    "gbca_tune": (ctypes.c_int, [_V, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_int32), _P(ctypes.c_int32)]),
+    "gbca_tune": (ctypes.c_int, [_V, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_int32), _P(ctypes.c_int32),
+                                 _P(ctypes.c_int32)]),
     "gbca_forget_tuning": (ctypes.c_int, []),
     "gbca_set_mask": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
     "gbca_snapshot": (ctypes.c_int, [_V, _P(_I64)]),
@@ -79,7 +80,7 @@ SIGNATURES = {
     "gbca_set_field": (ctypes.c_int, [_V, ctypes.c_int32, _V, _V, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "gbca_set_covariate": (ctypes.c_int, [_V, _V, _I64, ctypes.c_int32]),
     "gbca_philox_rate": (ctypes.c_int, [_I64, _P(ctypes.c_double)]),
-    "gbca_set_geometry": (ctypes.c_int, [_V, ctypes.c_int32, ctypes.c_int32]),
+    "gbca_set_geometry": (ctypes.c_int, [_V, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "gbca_threshold": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_int32]),
     "gbca_ensemble_create": (ctypes.c_int, [_P(Desc), ctypes.c_int32, _P(_V)]),
     "gbca_ensemble_destroy": (ctypes.c_int, [_V]),

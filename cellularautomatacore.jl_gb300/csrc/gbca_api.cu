@@ -27,7 +27,7 @@ struct gbca_handle {
     gbca::LeniaPlan* lenia = nullptr;
     bool states_valid = true;  // every state is one the rule produces (see scan_states)
     bool forced = false;       // gbca_set_geometry pinned the sweep geometry
-    gbca::SweepChoice force = {0, 0};
+    gbca::SweepChoice force = {0, 0, 0};
     // the environment (gbca_set_mask / gbca_set_field / gbca_set_covariate)
     uint8_t* mask = nullptr;           // pitch bytes between columns
     int2* taps = nullptr;
@@ -470,10 +470,12 @@ int gbca_advance(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
     return advance_int8(h, t, nsteps, params, nparams);
 }
 
-int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* steps_per_pass, int32_t* tile_rows) {
+int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* steps_per_pass, int32_t* tile_rows,
+              int32_t* staging) {
     if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
     if (steps_per_pass) *steps_per_pass = 0;
     if (tile_rows) *tile_rows = 0;
+    if (staging) *staging = 0;
     if (h->d.rule == GBCA_RULE_LENIA || h->d.rule == GBCA_RULE_SI_FIELD) return GBCA_OK;  // nothing to tune
     if (h->d.rule == GBCA_RULE_FOREST_FIRE && (!params || nparams < 2))
         return fail(GBCA_ERR_ARGUMENT, "the forest-fire rule needs parameters (p, f)");
@@ -487,6 +489,7 @@ int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* st
     gbca::store_choice(h->d, best);
     if (steps_per_pass) *steps_per_pass = best.steps_per_pass;
     if (tile_rows) *tile_rows = best.tile_rows;
+    if (staging) *staging = best.staging;
     return GBCA_OK;
 }
 
@@ -495,15 +498,16 @@ int gbca_forget_tuning(void) {
     return GBCA_OK;
 }
 
-int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows) {
+int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows, int32_t staging) {
     if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
-    if (steps_per_pass == 0 && tile_rows == 0) {
+    if (steps_per_pass == 0 && tile_rows == 0 && staging == 0) {
         h->forced = false;
         return GBCA_OK;
     }
-    if (steps_per_pass < 1 || steps_per_pass > 64 || tile_rows < 0)
-        return fail(GBCA_ERR_ARGUMENT, "steps per pass must lie in 1..64 and tile rows be non-negative, got %d, %d",
-                    (int)steps_per_pass, (int)tile_rows);
+    if (steps_per_pass < 1 || steps_per_pass > 64 || tile_rows < 0 || staging < 0 || staging > 1)
+        return fail(GBCA_ERR_ARGUMENT,
+                    "steps per pass must lie in 1..64, tile rows be non-negative and staging 0 or 1, got %d, %d, %d",
+                    (int)steps_per_pass, (int)tile_rows, (int)staging);
     if (h->d.rule == GBCA_RULE_LENIA || h->d.rule == GBCA_RULE_SI_FIELD)
         return fail(GBCA_ERR_UNSUPPORTED, "sweep geometry applies to the Int8 stencil kernels only");
     const int rc = ensure_scanned(h);
@@ -512,6 +516,7 @@ int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows)
     if (gbca::fire_fast_supported(p)) {
         if (tile_rows != 0) return fail(GBCA_ERR_ARGUMENT, "the forest-fire kernel's tile height is fixed; pass 0");
     } else if (gbca::life_simd_supported(p)) {
+        if (staging != 0) return fail(GBCA_ERR_ARGUMENT, "the bit-sliced kernel stages its tiles one way; pass 0");
         if (tile_rows > 0 && !gbca::life_choice_fits(p, steps_per_pass, tile_rows))
             return fail(GBCA_ERR_ARGUMENT, "%d steps per pass on tiles %d rows high exceed shared memory",
                         (int)steps_per_pass, (int)tile_rows);
@@ -520,6 +525,7 @@ int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows)
     }
     h->force.steps_per_pass = steps_per_pass;
     h->force.tile_rows = tile_rows;
+    h->force.staging = staging;
     h->forced = true;
     return GBCA_OK;
 }

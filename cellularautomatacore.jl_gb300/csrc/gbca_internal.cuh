@@ -163,7 +163,7 @@ struct SweepParams {
     PhiloxKeys keys;           // round keys of `seed` (set by the launchers that use them)
     int32_t states_valid;      // every state is known to be one the rule produces (Generations
                                // 0..C-1, forest fire 0..2)
-    int32_t pad_;
+    int32_t staging;           // forest fire: 1 = stage tiles by TMA where the tile fits
     const uint8_t* mask;       // nonzero = the cell updates (pitch bytes between columns), or null
     // active-tile scheduling: the tiles (ty * tiles_x + tx, tiles of tile_x x tile_y cells) to
     // run, *tile_count of them; each run tile writes whether it holds a non-background cell
@@ -196,10 +196,12 @@ int64_t launches_so_far();
 // Kernel selection and temporally blocked passes for an Int8 problem (sweep_dispatch.cu):
 // nsteps steps between bufs[*cur] and bufs[*cur ^ 1], *cur updated.
 SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params);
-// A kernel geometry choice: steps per temporally blocked pass and tile height (0 = default).
+// A kernel geometry choice: steps per temporally blocked pass, tile height (0 = default) and
+// how the forest-fire kernel stages its tiles (0 = vector loads, 1 = TMA where it fits).
 struct SweepChoice {
     int32_t steps_per_pass;
     int32_t tile_rows;
+    int32_t staging;
 };
 
 // states_valid: every state is known to be one the rule produces (Generations: 0..C-1,

@@ -7,16 +7,20 @@
 //  * Admission by HBM budget: request states live in one device arena of a fixed size; a
 //    request is admitted, in arrival order, when its two buffers fit, and its memory is
 //    released the moment it finishes. A request larger than the whole arena is refused.
-//  * Continuous batching: the scheduler works in iterations. In each one every admitted
-//    request advances by up to `chunk_steps` steps: all small requests together in one
-//    persistent ensemble launch (ensemble.cu; one CTA per request), the large ones as
-//    temporally blocked multi-CTA sweeps on their own streams, concurrently with it.
-//    Requests that arrive while an iteration runs join at the next one; finished requests
-//    leave and free their memory for the queue.
+//  * Continuous batching, event driven: large requests each take one of `max_big` stream
+//    lanes and run there from their initial state to their summaries (temporally blocked
+//    multi-CTA sweeps); small requests run together, `chunk_steps` steps at a time, in
+//    persistent ensemble launches (ensemble.cu; one CTA per request) on their own stream,
+//    back to back. Every launch ends with an event and a host callback that wakes the
+//    scheduler, which then collects what finished, frees its memory, admits waiting
+//    requests and refills the idle lane or the small stream at once: no lane waits for
+//    another, and no iteration-wide barrier holds the device.
+//  * A request's initial state is uploaded or generated on the stream that then runs it, so
+//    its first step is ordered after its state.
 //  * Results are exact: a request's steps, draws and summaries are those it would get alone
 //    (the draws depend only on its seed, cell and time).
-// The scheduler never waits on the device inside a kernel: each iteration ends with a
-// stream synchronisation on the host, so there is no device-side spin to bound.
+// The scheduler never waits on the device inside a kernel: it polls events on the host, so
+// there is no device-side spin to bound.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -107,6 +111,7 @@ struct Request {
     int64_t pitch = 0;
     int cur = 0;
     bool big = false;
+    bool fresh = true;  // the initial state is still to be written into the arena
     bool valid = true;  // every initial state is one the rule produces
     double t_submit = 0.0, t_admit = 0.0;
 };
@@ -156,6 +161,9 @@ struct gbca_server {
     unsigned long long* d_acc = nullptr;
     unsigned long long* h_acc = nullptr;
     int grid = 0;
+    std::vector<cudaEvent_t> ev_big;  // end of each lane's request
+    cudaEvent_t ev_small = nullptr;    // end of the small requests' launch in flight
+    std::atomic<uint64_t> signals{0};  // completions reported by host callbacks
 
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
@@ -234,9 +242,10 @@ EnsInstance small_instance(const Request* r, int64_t steps, bool last) {
     return I;
 }
 
-// Admit pending requests in arrival order while the arena has room.
-cudaError_t admit(gbca_server* S, std::deque<Request*>& pending, std::vector<Request*>& active,
-                  std::vector<gbca_result>& done) {
+// Admit pending requests in arrival order while the arena has room; the state is initialised
+// later, on the stream that runs the request.
+void admit(gbca_server* S, std::deque<Request*>& pending, std::vector<Request*>& admitted,
+           std::vector<gbca_result>& done) {
     while (!pending.empty()) {
         Request* r = pending.front();
         const gbca_desc& d = r->d;
@@ -251,65 +260,169 @@ cudaError_t admit(gbca_server* S, std::deque<Request*>& pending, std::vector<Req
             continue;
         }
         if (!S->arena.alloc(r->bytes, &r->off)) break;
-        int8_t* buf = S->arena_base + r->off;
-        cudaError_t e;
-        if (!r->u0.empty()) {
-            e = cudaMemcpy2DAsync(buf, (size_t)r->pitch, r->u0.data(), (size_t)d.n1, (size_t)d.n1, (size_t)d.n2,
-                                  cudaMemcpyHostToDevice, S->s_small);
-            std::vector<int8_t>().swap(r->u0);
-        } else if (r->density > 0.0) {
-            const uint32_t thr = (uint32_t)gbca_threshold(r->density, 1);
-            k_soup<<<S->grid, 256, 0, S->s_small>>>(buf, d.n1, d.n2, r->pitch, r->init_seed, thr);
-            count_launch();
-            e = cudaGetLastError();
-        } else {
-            e = cudaMemsetAsync(buf, 0, one, S->s_small);
-        }
-        if (e != cudaSuccess) return e;
         r->cur = 0;
         r->done = 0;
+        r->fresh = true;
         r->t_admit = S->now();
-        active.push_back(r);
+        admitted.push_back(r);
         pending.pop_front();
     }
-    return cudaSuccess;
+}
+
+// Writes a request's initial state into its first buffer on stream st.
+cudaError_t init_state(gbca_server* S, Request* r, cudaStream_t st) {
+    r->fresh = false;
+    const gbca_desc& d = r->d;
+    int8_t* buf = S->arena_base + r->off;
+    if (!r->u0.empty()) {
+        // a pageable source is staged before the call returns, so it can go at once
+        const cudaError_t e = cudaMemcpy2DAsync(buf, (size_t)r->pitch, r->u0.data(), (size_t)d.n1, (size_t)d.n1,
+                                                (size_t)d.n2, cudaMemcpyHostToDevice, st);
+        std::vector<int8_t>().swap(r->u0);
+        return e;
+    }
+    if (r->density > 0.0) {
+        const uint32_t thr = (uint32_t)gbca_threshold(r->density, 1);
+        k_soup<<<S->grid, 256, 0, st>>>(buf, d.n1, d.n2, r->pitch, r->init_seed, thr);
+        count_launch();
+        return cudaGetLastError();
+    }
+    return cudaMemsetAsync(buf, 0, r->bytes / 2, st);
+}
+
+void CUDART_CB on_done(void* p) {
+    gbca_server* S = (gbca_server*)p;
+    S->signals.fetch_add(1, std::memory_order_release);
+    S->cv.notify_all();
 }
 
 void scheduler(gbca_server* S) {
     cudaSetDevice(S->device);
     std::deque<Request*> pending;
-    std::vector<Request*> active;
+    std::vector<Request*> waiting_big;  // admitted large requests without a lane
+    std::vector<Request*> smalls;       // admitted small requests
+    std::vector<Request*> batch;        // the small requests of the launch in flight
+    std::vector<int64_t> batch_steps;
+    const int nlanes = (int)S->s_big.size();
+    std::vector<Request*> lane((size_t)nlanes, nullptr);
+    bool small_busy = false;
     std::vector<gbca_result> done;
-    const int nbig = (int)S->s_big.size();
+    uint64_t seen = 0;
     for (;;) {
+        const bool busy = small_busy || std::any_of(lane.begin(), lane.end(), [](Request* r) { return r; });
         {
             std::unique_lock<std::mutex> lock(S->mu);
-            while (S->inbox.empty() && pending.empty() && active.empty() && !S->stopping)
+            while (S->inbox.empty() && pending.empty() && waiting_big.empty() && smalls.empty() && !busy &&
+                   !S->stopping)
                 S->cv.wait_for(lock, std::chrono::milliseconds(50));
             while (!S->inbox.empty()) {
                 pending.push_back(S->inbox.front());
                 S->inbox.pop_front();
             }
-            if (S->stopping && pending.empty() && active.empty()) break;
+            if (S->stopping && pending.empty() && waiting_big.empty() && smalls.empty() && !busy) break;
         }
-        cudaError_t e = admit(S, pending, active, done);
-        // one iteration: every small request in one ensemble launch, large ones on their streams
-        std::vector<Request*> smalls, bigs;
-        for (Request* r : active) (r->big ? bigs : smalls).push_back(r);
-        if (bigs.size() > (size_t)nbig) bigs.resize((size_t)nbig);  // the rest wait for a stream
-        std::vector<int64_t> step_small(smalls.size()), step_big(bigs.size());
-        if (e == cudaSuccess && !smalls.empty()) {
-            if (!grow_small(S, (int)smalls.size())) e = cudaErrorMemoryAllocation;
-            std::vector<EnsInstance> inst(smalls.size());
-            std::vector<int64_t> work(smalls.size());
-            for (size_t j = 0; j < smalls.size() && e == cudaSuccess; ++j) {
-                Request* r = smalls[j];
-                const int64_t rem = r->nsteps - r->done;
-                step_small[j] = rem < S->cfg.chunk_steps ? rem : S->cfg.chunk_steps;
-                inst[j] = small_instance(r, step_small[j], step_small[j] == rem);
-                work[j] = r->d.n1 * r->d.n2 * step_small[j];
+        cudaError_t e = cudaSuccess;
+        bool progress = false;
+        const double t = S->now();
+        std::vector<Request*> finished;
+        // 1. lanes whose request is done
+        for (int j = 0; j < nlanes && e == cudaSuccess; ++j) {
+            Request* r = lane[(size_t)j];
+            if (!r) continue;
+            const cudaError_t q = cudaEventQuery(S->ev_big[(size_t)j]);
+            if (q == cudaErrorNotReady) continue;
+            if (q != cudaSuccess) {
+                e = q;
+                break;
             }
-            std::vector<int> order(smalls.size());
+            gbca_result res = make_result(r, GBCA_OK, t);
+            finish_measures(S->h_acc + (size_t)j * kMeasureWords, r->d.n1 * r->d.n2, res.counts, kEnsCounts,
+                            &res.other, &res.morans);
+            done.push_back(res);
+            finished.push_back(r);
+            lane[(size_t)j] = nullptr;
+            progress = true;
+        }
+        // 2. the small requests' launch
+        if (e == cudaSuccess && small_busy) {
+            const cudaError_t q = cudaEventQuery(S->ev_small);
+            if (q == cudaSuccess) {
+                small_busy = false;
+                progress = true;
+                for (size_t j = 0; j < batch.size(); ++j) {
+                    Request* r = batch[j];
+                    r->cur = S->h_cur[j];
+                    r->done += batch_steps[j];
+                    if (r->done < r->nsteps) continue;
+                    gbca_result res = make_result(r, GBCA_OK, t);
+                    const long long* w = S->h_out[j].w;
+                    const int64_t ncell = r->d.n1 * r->d.n2;
+                    int64_t inrange = 0;
+                    for (int v = 0; v < kEnsCounts; ++v) {
+                        res.counts[v] = w[v];
+                        inrange += w[v];
+                    }
+                    res.other = ncell - inrange;
+                    res.morans = morans_from_sums(w[kEnsCounts + 1], w[kEnsCounts + 2], w[kEnsCounts + 3],
+                                                  w[kEnsCounts + 4], w[kEnsCounts + 5], ncell);
+                    done.push_back(res);
+                    finished.push_back(r);
+                    smalls.erase(std::find(smalls.begin(), smalls.end(), r));
+                }
+                batch.clear();
+            } else if (q != cudaErrorNotReady) {
+                e = q;
+            }
+        }
+        for (Request* r : finished) {
+            S->arena.release(r->off, r->bytes);
+            delete r;
+        }
+        // 3. admission into the memory just freed
+        if (e == cudaSuccess) {
+            std::vector<Request*> admitted;
+            admit(S, pending, admitted, done);
+            for (Request* r : admitted) (r->big ? waiting_big : smalls).push_back(r);
+            progress = progress || !admitted.empty();
+        }
+        // 4. idle lanes take the next large request, from its initial state to its summaries
+        for (int j = 0; j < nlanes && e == cudaSuccess && !waiting_big.empty(); ++j) {
+            if (lane[(size_t)j]) continue;
+            Request* r = waiting_big.front();
+            waiting_big.erase(waiting_big.begin());
+            cudaStream_t st = S->s_big[(size_t)j];
+            e = init_state(S, r, st);
+            int8_t* const bufs[2] = {S->arena_base + r->off, S->arena_base + r->off + r->bytes / 2};
+            if (e == cudaSuccess)
+                e = sweep_int8(r->d, r->pitch, bufs, &r->cur, r->t0, r->nsteps, r->params, st, r->valid);
+            unsigned long long* acc = S->d_acc + (size_t)j * kMeasureWords;
+            if (e == cudaSuccess)
+                e = launch_measures(bufs[r->cur], r->d.n1, r->d.n2, r->pitch, r->d.boundary[0], r->d.boundary[1], acc,
+                                    S->grid / 4 > 0 ? S->grid / 4 : 1, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(S->h_acc + (size_t)j * kMeasureWords, acc, kMeasureWords * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaEventRecord(S->ev_big[(size_t)j], st);
+            if (e == cudaSuccess) e = cudaLaunchHostFunc(st, on_done, S);
+            lane[(size_t)j] = r;
+            progress = true;
+        }
+        // 5. the small requests, chunk_steps at a time, in one persistent launch
+        if (e == cudaSuccess && !small_busy && !smalls.empty()) {
+            if (!grow_small(S, (int)smalls.size())) e = cudaErrorMemoryAllocation;
+            batch = smalls;
+            batch_steps.assign(batch.size(), 0);
+            std::vector<EnsInstance> inst(batch.size());
+            std::vector<int64_t> work(batch.size());
+            for (size_t j = 0; j < batch.size() && e == cudaSuccess; ++j) {
+                Request* r = batch[j];
+                if (r->fresh) e = init_state(S, r, S->s_small);
+                const int64_t rem = r->nsteps - r->done;
+                batch_steps[j] = rem < S->cfg.chunk_steps ? rem : S->cfg.chunk_steps;
+                inst[j] = small_instance(r, batch_steps[j], batch_steps[j] == rem);
+                work[j] = r->d.n1 * r->d.n2 * batch_steps[j];
+            }
+            std::vector<int> order(batch.size());
             std::iota(order.begin(), order.end(), 0);
             std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
             if (e == cudaSuccess)
@@ -326,37 +439,29 @@ void scheduler(gbca_server* S) {
                                     S->s_small);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(S->h_cur, S->d_cur, sizeof(int) * inst.size(), cudaMemcpyDeviceToHost, S->s_small);
+            if (e == cudaSuccess) e = cudaEventRecord(S->ev_small, S->s_small);
+            if (e == cudaSuccess) e = cudaLaunchHostFunc(S->s_small, on_done, S);
+            small_busy = e == cudaSuccess;
+            progress = true;
         }
-        for (size_t j = 0; j < bigs.size() && e == cudaSuccess; ++j) {
-            Request* r = bigs[j];
-            const int64_t rem = r->nsteps - r->done;
-            step_big[j] = rem < S->cfg.chunk_steps ? rem : S->cfg.chunk_steps;
-            int8_t* const bufs[2] = {S->arena_base + r->off, S->arena_base + r->off + r->bytes / 2};
-            e = sweep_int8(r->d, r->pitch, bufs, &r->cur, r->t0 + r->done, step_big[j], r->params, S->s_big[j],
-                           r->valid);
-            r->valid = r->valid || r->d.rule == GBCA_RULE_FOREST_FIRE;  // a fire step leaves only 0, 1, 2
-            if (e == cudaSuccess && step_big[j] == rem) {
-                unsigned long long* acc = S->d_acc + (size_t)j * kMeasureWords;
-                e = launch_measures(bufs[r->cur], r->d.n1, r->d.n2, r->pitch, r->d.boundary[0], r->d.boundary[1], acc,
-                                    S->grid / 4 > 0 ? S->grid / 4 : 1, S->s_big[j]);
-                if (e == cudaSuccess)
-                    e = cudaMemcpyAsync(S->h_acc + (size_t)j * kMeasureWords, acc,
-                                        kMeasureWords * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                        S->s_big[j]);
-            }
-        }
-        if (e == cudaSuccess && !smalls.empty()) e = cudaStreamSynchronize(S->s_small);
-        for (size_t j = 0; j < bigs.size() && e == cudaSuccess; ++j) e = cudaStreamSynchronize(S->s_big[j]);
-        const double t = S->now();
-        std::vector<Request*> finished;
         if (e != cudaSuccess) {
             // the device failed: every admitted and queued request fails with it
-            for (Request* r : active) done.push_back(make_result(r, GBCA_ERR_CUDA, t));
-            for (Request* r : pending) done.push_back(make_result(r, GBCA_ERR_CUDA, t));
-            for (Request* r : active) delete r;
-            for (Request* r : pending) delete r;
-            active.clear();
+            cudaGetLastError();
+            std::vector<Request*> all(pending.begin(), pending.end());
+            all.insert(all.end(), waiting_big.begin(), waiting_big.end());
+            all.insert(all.end(), smalls.begin(), smalls.end());
+            for (Request* r : lane)
+                if (r) all.push_back(r);
+            for (Request* r : all) {
+                done.push_back(make_result(r, GBCA_ERR_CUDA, S->now()));
+                delete r;
+            }
             pending.clear();
+            waiting_big.clear();
+            smalls.clear();
+            batch.clear();
+            std::fill(lane.begin(), lane.end(), nullptr);
+            small_busy = false;
             std::lock_guard<std::mutex> lock(S->mu);
             S->dead = true;
             for (auto& res : done) S->outbox.push_back(res);
@@ -364,47 +469,20 @@ void scheduler(gbca_server* S) {
             S->stopping = true;
             continue;
         }
-        for (size_t j = 0; j < smalls.size(); ++j) {
-            Request* r = smalls[j];
-            r->cur = S->h_cur[j];
-            r->done += step_small[j];
-            if (r->done >= r->nsteps) {
-                gbca_result res = make_result(r, GBCA_OK, t);
-                const long long* w = S->h_out[j].w;
-                const int64_t ncell = r->d.n1 * r->d.n2;
-                int64_t inrange = 0;
-                for (int v = 0; v < kEnsCounts; ++v) {
-                    res.counts[v] = w[v];
-                    inrange += w[v];
-                }
-                res.other = ncell - inrange;
-                res.morans = morans_from_sums(w[kEnsCounts + 1], w[kEnsCounts + 2], w[kEnsCounts + 3],
-                                              w[kEnsCounts + 4], w[kEnsCounts + 5], ncell);
-                done.push_back(res);
-                finished.push_back(r);
+        {
+            std::unique_lock<std::mutex> lock(S->mu);
+            for (auto& res : done) S->outbox.push_back(res);
+            done.clear();
+            S->queued = (int64_t)(pending.size() + S->inbox.size());
+            S->active_n = (int64_t)(waiting_big.size() + smalls.size() +
+                                    std::count_if(lane.begin(), lane.end(), [](Request* r) { return r; }));
+            if (!progress) {  // nothing finished or started: sleep until a launch ends or a request arrives
+                const uint64_t now_signals = S->signals.load(std::memory_order_acquire);
+                if (now_signals == seen && S->inbox.empty() && !S->stopping)
+                    S->cv.wait_for(lock, std::chrono::milliseconds(1));
+                seen = S->signals.load(std::memory_order_acquire);
             }
         }
-        for (size_t j = 0; j < bigs.size(); ++j) {
-            Request* r = bigs[j];
-            r->done += step_big[j];
-            if (r->done >= r->nsteps) {
-                gbca_result res = make_result(r, GBCA_OK, t);
-                finish_measures(S->h_acc + (size_t)j * kMeasureWords, r->d.n1 * r->d.n2, res.counts, kEnsCounts,
-                                &res.other, &res.morans);
-                done.push_back(res);
-                finished.push_back(r);
-            }
-        }
-        for (Request* r : finished) {
-            S->arena.release(r->off, r->bytes);
-            active.erase(std::find(active.begin(), active.end(), r));
-            delete r;
-        }
-        std::lock_guard<std::mutex> lock(S->mu);
-        for (auto& res : done) S->outbox.push_back(res);
-        done.clear();
-        S->queued = (int64_t)(pending.size() + S->inbox.size());
-        S->active_n = (int64_t)active.size();
     }
 }
 
@@ -428,6 +506,10 @@ int gbca_server_start(const gbca_server_config* cfg, gbca_server** out) {
     S->s_big.assign((size_t)cfg->max_big, nullptr);
     for (auto& st : S->s_big)
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    S->ev_big.assign((size_t)cfg->max_big, nullptr);
+    for (auto& ev : S->ev_big)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->ev_small, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&S->d_counter, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&S->d_acc, sizeof(unsigned long long) * kMeasureWords * cfg->max_big);
     if (e == cudaSuccess) e = cudaMallocHost(&S->h_acc, sizeof(unsigned long long) * kMeasureWords * cfg->max_big);
@@ -441,6 +523,9 @@ int gbca_server_start(const gbca_server_config* cfg, gbca_server** out) {
         if (S->s_small) cudaStreamDestroy(S->s_small);
         for (auto st : S->s_big)
             if (st) cudaStreamDestroy(st);
+        for (auto ev : S->ev_big)
+            if (ev) cudaEventDestroy(ev);
+        if (S->ev_small) cudaEventDestroy(S->ev_small);
         delete S;
         return oom ? sfail(GBCA_ERR_OUT_OF_MEMORY, "the server's HBM budget of %llu bytes cannot be allocated",
                            (unsigned long long)cfg->hbm_budget)
@@ -547,6 +632,9 @@ int gbca_server_stop(gbca_server* S) {
     if (S->s_small) cudaStreamDestroy(S->s_small);
     for (auto st : S->s_big)
         if (st) cudaStreamDestroy(st);
+    for (auto ev : S->ev_big)
+        if (ev) cudaEventDestroy(ev);
+    if (S->ev_small) cudaEventDestroy(S->ev_small);
     delete S;
     return GBCA_OK;
 }

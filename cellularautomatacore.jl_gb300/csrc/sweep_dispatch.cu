@@ -85,10 +85,11 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
     }
     const bool fire = fire_fast_supported(p);
     const bool life = !fire && life_simd_supported(p);
-    SweepChoice choice = {0, 0};
+    SweepChoice choice = {0, 0, 0};
     if (force) choice = *force;
     else if (fire || life) tuned_choice(d, &choice);  // the autotuner's pick for this shape, if any
     p.tile_y = choice.tile_rows;
+    p.staging = choice.staging;
     while (nsteps > 0) {
         int64_t k;
         cudaError_t e;

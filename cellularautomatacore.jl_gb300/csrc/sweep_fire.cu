@@ -10,8 +10,9 @@
 // and temporal blocking (nsub steps per pass, halo nsub) keeps HBM traffic at
 // 2 B / nsub per cell-update.
 //
-// Tile staging: where the tile's loaded region lies inside the lattice, or the lattice is a
-// Grid with Constant(0) edges (the tensor's zero fill is then the boundary value), one TMA
+// Tile staging (the autotuner's choice, p.staging): where the tile's loaded region lies inside
+// the lattice, or the lattice is a Grid with Constant(0) edges (the tensor's zero fill is then
+// the boundary value), one TMA
 // copy (cp.async.bulk.tensor) brings the whole halo-padded tile into shared memory (for the
 // zero-fill case n1 must be a multiple of 16, so no box reaches the column padding). The state
 // is viewed as a 3-D tensor (16-byte segments x segments x rows), so a box of
@@ -263,7 +264,8 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     int tma = 0;
-    if (sy <= 256 && sx / 16 <= 256 && ((uintptr_t)src & 15u) == 0 && tile_map(src, p.n1, p.n2, p.pitch, sx, sy, &map)) {
+    if (p.staging && sy <= 256 && sx / 16 <= 256 && ((uintptr_t)src & 15u) == 0 &&
+        tile_map(src, p.n1, p.n2, p.pitch, sx, sy, &map)) {
         const bool zero_edges = p.bnd[0] == GBCA_CONSTANT && p.bnd[1] == GBCA_CONSTANT && p.cval[0] == 0 &&
                                 p.cval[1] == 0 && p.n1 % 16 == 0;
         tma = zero_edges ? 2 : 1;

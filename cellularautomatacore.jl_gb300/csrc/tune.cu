@@ -1,8 +1,9 @@
 // tune.cu — the sweep autotuner's candidate geometries and its per-shape cache.
 //
-// A geometry is (steps per temporally blocked pass, tile height). Deeper passes re-read HBM
-// less often but redo more halo work; taller tiles cut halo overhead but change how many
-// tiles fill the 152 SMs' slots. The best pair depends on the lattice size, the radius and
+// A geometry is (steps per temporally blocked pass, tile height, tile staging). Deeper passes
+// re-read HBM less often but redo more halo work; taller tiles cut halo overhead but change how
+// many tiles fill the 152 SMs' slots; the forest fire's tiles arrive by vector loads or by one
+// TMA copy each. The best pair depends on the lattice size, the radius and
 // the rule, so gbca_tune (gbca_api.cu) times the candidates below on the handle's own data and
 // stores the fastest here; sweep_int8 then uses it for every later call on that shape (single
 // handles and the server's large requests alike). Every geometry gives identical results: a
@@ -53,8 +54,10 @@ void forget_choices() {
 std::vector<SweepChoice> sweep_candidates(const SweepParams& p) {
     std::vector<SweepChoice> out;
     if (fire_fast_supported(p)) {
-        // the tile height is fixed by the kernel's word layout; only the pass depth varies
-        for (int k : {2, 4, 6, 8, 12}) out.push_back({k, 0});
+        // the tile height is fixed by the kernel's word layout; the pass depth and the tile
+        // staging (vector loads or TMA) vary
+        for (int staging : {0, 1})
+            for (int k : {2, 4, 6, 8, 12}) out.push_back({k, 0, staging});
         return out;
     }
     if (!life_simd_supported(p)) return out;
@@ -63,7 +66,7 @@ std::vector<SweepChoice> sweep_candidates(const SweepParams& p) {
     const int* per = kPer[p.radius - 1];
     for (int i = 0; i < 5; ++i)
         for (int ty : {64, 96, 128, 144, 176, 216, 256})
-            if (life_choice_fits(p, per[i], ty)) out.push_back({per[i], ty});
+            if (life_choice_fits(p, per[i], ty)) out.push_back({per[i], ty, 0});
     return out;
 }
 

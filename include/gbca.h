@@ -205,23 +205,26 @@ int64_t gbca_kernel_launches(void);
 int gbca_philox_rate(int64_t draws, double* draws_per_s);
 
 /* ---- sweep autotuning. No counterpart in the reference (its kernels have one geometry).
- * A sweep geometry is (steps per temporally blocked pass, tile rows). gbca_tune times every
- * candidate geometry of the handle's fast kernel (forest fire: pass depth; bit-sliced
- * Life/Generations: pass depth x tile height) on the handle's current state, about 48 steps
- * each, restores the state, and caches the fastest for the problem's shape (rule,
- * neighbourhood, size, boundaries, scheme, device): every later sweep of that shape, on any
- * handle or in the server, uses it. The chosen pair is returned ((0, 0): the problem runs
- * on the general kernel, nothing to tune). Results never depend on the geometry.
- * It allocates one copy of the state while it runs; params as in gbca_advance. */
-int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* steps_per_pass, int32_t* tile_rows);
+ * A sweep geometry is (steps per temporally blocked pass, tile rows, tile staging). gbca_tune
+ * times every candidate geometry of the handle's fast kernel (forest fire: pass depth x
+ * staging by vector loads or by TMA; bit-sliced Life/Generations: pass depth x tile height) on
+ * the handle's current state, about 48 steps each, restores the state, and caches the fastest
+ * for the problem's shape (rule, neighbourhood, size, boundaries, scheme, device): every later
+ * sweep of that shape, on any handle or in the server, uses it. The chosen geometry is
+ * returned ((0, 0, 0): the problem runs on the general kernel, nothing to tune; staging may be
+ * NULL). Results never depend on the geometry. It allocates one copy of the state while it
+ * runs; params as in gbca_advance. */
+int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* steps_per_pass, int32_t* tile_rows,
+              int32_t* staging);
 
 /* Clears the tuning cache (all shapes). */
 int gbca_forget_tuning(void);
 
-/* Pins this handle's sweep geometry ((0, 0) unpins it). The forest-fire kernel takes
- * tile_rows = 0; the bit-sliced kernel takes tile_rows 0 (its default) or any height whose
- * tiles fit shared memory; the general kernel takes none (GBCA_ERR_UNSUPPORTED). */
-int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows);
+/* Pins this handle's sweep geometry ((0, 0, 0) unpins it). The forest-fire kernel takes
+ * tile_rows = 0 and staging 0 (vector loads) or 1 (TMA where the tile fits); the bit-sliced
+ * kernel takes tile_rows 0 (its default) or any height whose tiles fit shared memory, and
+ * staging 0; the general kernel takes none (GBCA_ERR_UNSUPPORTED). */
+int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows, int32_t staging);
 
 /* ---- batched ensembles: many problems advanced by one persistent, graph-captured launch.
  * Replaces solving an EnsembleProblem one trajectory at a time (src/problem.jl:571-589 with

@@ -71,15 +71,16 @@ def test_generations_geometries(ca, oracle, steps, rows):
     st.close()
 
 
-@pytest.mark.parametrize("steps", [1, 2, 5, 12, 16])
-def test_fire_geometries(ca, oracle, steps):
-    """Forest fire on a 900 x 410 grid from t = 3, 29 steps."""
-    u0 = np.random.default_rng(steps).integers(0, 3, (900, 410)).astype(np.int8)
-    prob = ca.CAProblem.new(ca.ForestFire(), u0, 40, {"p": 0.05, "f": 0.002}, space=ca.Grid(900, 410), seed=7)
+@pytest.mark.parametrize("steps,staging,n1", [(1, 0, 900), (2, 1, 900), (5, 0, 1024), (12, 1, 1024), (16, 1, 912)])
+def test_fire_geometries(ca, oracle, steps, staging, n1):
+    """Forest fire on an n1 x 410 grid from t = 3, 29 steps; staging 1 stages tiles by TMA
+    (interior tiles for n1 = 900, every tile for the multiples of 16)."""
+    u0 = np.random.default_rng(steps).integers(0, 3, (n1, 410)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 40, {"p": 0.05, "f": 0.002}, space=ca.Grid(n1, 410), seed=7)
     st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
-    ca.set_geometry(st, steps, 0)
+    ca.set_geometry(st, steps, 0, staging)
     got = _run(ca, prob, st, 3, 29, prob.p)
-    P = oracle.Problem(oracle.RULE_FOREST_FIRE, 900, 410, nbhd=oracle.VON_NEUMANN, seed=7,
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, n1, 410, nbhd=oracle.VON_NEUMANN, seed=7,
                        boundary=(oracle.CONSTANT, oracle.CONSTANT))
     assert np.array_equal(got, oracle.run_array(P, u0, 3, 29, (0.05, 0.002), nthreads=8))
     st.close()
@@ -92,8 +93,8 @@ def test_tune_keeps_state_and_results(ca, oracle):
     prob = ca.CAProblem.new(ca.Life(":conway"), u0, 40)
     B = ca.GB300Backend()
     st = ca.allocate_state(B, prob, ca.Synchronous())
-    k, rows = ca.tune(st, prob)
-    assert k in (8, 12, 16, 24, 32) and rows in (64, 96, 128, 144, 176, 216, 256)
+    k, rows, staging = ca.tune(st, prob)
+    assert k in (8, 12, 16, 24, 32) and rows in (64, 96, 128, 144, 176, 216, 256) and staging == 0
     assert np.array_equal(ca.current_state(B, st), u0)
     got = _run(ca, prob, st, 0, 40)
     P = oracle.Problem(oracle.RULE_LIFE, 1536, 1280, birth=oracle.mask([3]), survive=oracle.mask([2, 3]))
@@ -111,8 +112,8 @@ def test_tune_fire_and_general(ca, oracle):
     prob = ca.CAProblem.new(ca.ForestFire(), u0, 20, {"p": 0.05, "f": 0.002}, space=ca.Grid(1000, 600), seed=3)
     B = ca.GB300Backend()
     st = ca.allocate_state(B, prob, ca.Synchronous())
-    k, rows = ca.tune(st, prob)
-    assert k in (2, 4, 6, 8, 12) and rows == 0
+    k, rows, staging = ca.tune(st, prob)
+    assert k in (2, 4, 6, 8, 12) and rows == 0 and staging in (0, 1)
     assert np.array_equal(ca.current_state(B, st), u0)
     got = _run(ca, prob, st, 0, 20, prob.p)
     P = oracle.Problem(oracle.RULE_FOREST_FIRE, 1000, 600, nbhd=oracle.VON_NEUMANN, seed=3,
@@ -123,7 +124,7 @@ def test_tune_fire_and_general(ca, oracle):
     prob2 = ca.CAProblem.new(ca.Life([2, 3], [1, 2], neighbourhood=ca.VonNeumann(1)),
                              np.zeros((64, 64), np.int8), 5)
     st2 = ca.allocate_state(B, prob2, ca.Synchronous())
-    assert ca.tune(st2, prob2) == (0, 0)
+    assert ca.tune(st2, prob2) == (0, 0, 0)
     with pytest.raises(ca.UnsupportedCombinationError):
         ca.set_geometry(st2, 4, 0)
     st2.close()
@@ -140,6 +141,8 @@ def test_geometry_refusals(ca):
         ca.set_geometry(st, 0, 16)
     with pytest.raises(ca.ArgumentError):
         ca.set_geometry(st, 65, 0)
+    with pytest.raises(ca.ArgumentError):
+        ca.set_geometry(st, 4, 0, 2)  # staging is 0 or 1
     st.close()
     ltl = ca.CAProblem.new(ca.Life(LTL["birth"], LTL["survive"], neighbourhood=ca.Moore(5)),
                            np.zeros((4096, 4096), np.int8), 5)
