@@ -504,7 +504,8 @@ def serve_desc(capi, kind, side, seed):
 
 def run_stream(capi, lib, n, rate, seed):
     """Submit n requests of the served stream at Poisson rate `rate` into a fresh server and
-    collect every result; returns (results {id: (status, t_submit, t_done)}, requests, wall)."""
+    collect every result; returns (results {id: (status, t_submit, t_done, counts, other, morans)},
+    requests, wall)."""
     arrivals, kinds, sides, steps, ps, fs, seeds = serve_requests(n, seed)
     arrivals = arrivals * (SERVE["rate"] / rate)
     cfg = capi.ServerConfig()
@@ -522,7 +523,8 @@ def run_stream(capi, lib, n, rate, seed):
         capi.check(lib.gbca_server_poll(srv, res_buf, 4096, ctypes.byref(nres)))
         for k in range(nres.value):
             r = res_buf[k]
-            got[int(r.id)] = (r.status, r.t_submit, r.t_done)
+            got[int(r.id)] = (r.status, r.t_submit, r.t_done, tuple(r.counts[k] for k in range(8)), r.other,
+                              r.morans)
 
     t0 = time.perf_counter()
     for i in range(n):
@@ -545,9 +547,11 @@ def bench_served(capi, lib):
     server (far above what one GPU completes, so latency is mostly queueing), then a stream at
     half the measured capacity (latency of the loop itself); latency = result time - submit
     time. Then the plain path: the same kind of requests one at a time through a handle each
-    (create, upload, advance, summaries, destroy), on a sample."""
+    (create, the same device soup, advance, summaries, destroy), on a sample, whose summaries
+    must equal the served ones exactly."""
     n = int(SERVE["rate"] * SERVE["seconds"])
     got, reqs, wall = run_stream(capi, lib, n, SERVE["rate"], 2000)
+    ids = sorted(got)  # ids are given in submission order
     arrivals, kinds, sides, steps, ps, fs, seeds, descs = reqs
     lat = np.array([v[2] - v[1] for v in got.values()])
     t_first = min(v[1] for v in got.values())
@@ -564,16 +568,15 @@ def bench_served(capi, lib):
     # the plain per-request path on a random sample, one request at a time
     rng = np.random.Generator(np.random.PCG64(5))
     sample = rng.choice(n, SERVE["plain_sample"], replace=False)
-    lat_plain, t_sum = [], 0.0
+    lat_plain, t_sum, exact = [], 0.0, 0
     for i in sample:
-        u0 = (rng.random(int(sides[i]) ** 2) < 0.5).astype(np.int8) if kinds[i] != 2 else \
-            np.zeros(int(sides[i]) ** 2, np.int8)
         d = descs[i]
         P = (ctypes.c_double * 2)(ps[i], fs[i])
         ts = time.perf_counter()
         h = ctypes.c_void_p()
         capi.check(lib.gbca_create(ctypes.byref(d), ctypes.byref(h)))
-        capi.check(lib.gbca_set_state(h, u0.ctypes.data, u0.nbytes))
+        if kinds[i] != 2:  # the server's initial state: the same device soup from the same seed
+            capi.check(lib.gbca_set_state_soup(h, 0.5, int(seeds[i])))
         capi.check(lib.gbca_advance(h, 0, int(steps[i]), P, 2 if kinds[i] == 2 else 0))
         c8 = (ctypes.c_int64 * 8)()
         o1 = ctypes.c_int64()
@@ -583,6 +586,9 @@ def bench_served(capi, lib):
         dt = time.perf_counter() - ts
         t_sum += dt
         lat_plain.append(dt)
+        srv = got[ids[i]]
+        same_m = srv[5] == m1.value or (np.isnan(srv[5]) and np.isnan(m1.value))
+        exact += int(srv[0] == 0 and tuple(c8) == srv[3] and srv[4] == o1.value and same_m)
     # a stream at half the measured capacity, for the loop's latency when it keeps up
     rate2 = 0.5 * served["sims_per_s"]
     n2 = max(50, int(rate2 * 3.0))
@@ -596,6 +602,7 @@ def bench_served(capi, lib):
     served["plain_sims_per_s"] = len(sample) / t_sum
     served["plain_sample"] = len(sample)
     served["plain_service_p50_s"] = float(np.percentile(lat_plain, 50))
+    served["exact_matches_in_sample"] = exact
     served["speedup_vs_plain"] = served["sims_per_s"] / served["plain_sims_per_s"]
     return served
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "gbca_forget_tuning": (ctypes.c_int, []),
     "gbca_set_mask": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
     "gbca_snapshot": (ctypes.c_int, [_V, _P(_I64)]),
+    "gbca_set_state_soup": (ctypes.c_int, [_V, ctypes.c_double, ctypes.c_uint64]),
     "gbca_set_sparse": (ctypes.c_int, [_V, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "gbca_snapshot_fetch": (ctypes.c_int, [_V, _I64, _V, ctypes.c_size_t]),
     "gbca_set_field": (ctypes.c_int, [_V, ctypes.c_int32, _V, _V, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),

@@ -448,6 +448,18 @@ int gbca_set_state_device(gbca_handle* h, const void* dptr, int64_t src_pitch) {
     return GBCA_OK;
 }
 
+int gbca_set_state_soup(gbca_handle* h, double density, uint64_t seed) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (h->esize != 1) return fail(GBCA_ERR_UNSUPPORTED, "a soup is an Int8 state");
+    if (!(density >= 0.0 && density <= 1.0)) return fail(GBCA_ERR_ARGUMENT, "density must be in [0, 1]");
+    GBCA_CUDA(gbca::launch_soup((int8_t*)h->buf[h->cur], h->d.n1, h->d.n2, h->pitch, density, seed, h->nsm * 8,
+                                h->stream),
+              "set_state_soup");
+    h->states_valid = false;
+    h->sparse_dirty = true;
+    return GBCA_OK;
+}
+
 int gbca_get_state(gbca_handle* h, void* host, size_t nbytes) {
     if (!h || !host) return fail(GBCA_ERR_ARGUMENT, "null handle or state");
     const size_t row = (size_t)h->d.n1 * h->esize;

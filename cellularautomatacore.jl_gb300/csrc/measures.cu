@@ -69,6 +69,26 @@ __global__ void __launch_bounds__(256) k_measures(const int8_t* __restrict__ u, 
 
 }  // namespace
 
+namespace {
+
+__global__ void k_soup(int8_t* __restrict__ buf, int64_t n1, int64_t n2, int64_t pitch, uint64_t seed, uint32_t thr24) {
+    const int64_t n = n1 * n2;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint2 w = cell_draw(seed, (uint64_t)q + 1u, (int64_t)0xFFFFFFFFu, 0xFFFFFFFEu);
+        buf[(q % n1) + (q / n1) * pitch] = (int8_t)((w.x >> 8) < thr24 ? 1 : 0);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_soup(int8_t* buf, int64_t n1, int64_t n2, int64_t pitch, double density, uint64_t seed, int grid,
+                        cudaStream_t st) {
+    const uint32_t thr = (uint32_t)gbca_threshold(density, 1);
+    k_soup<<<grid, 256, 0, st>>>(buf, n1, n2, pitch, seed, thr);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t b1, int32_t b2,
                             unsigned long long* acc, int nsm, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(acc, 0, kMeasureWords * sizeof(unsigned long long), st);

@@ -8,6 +8,12 @@ namespace gbca {
 // Accumulator layout: [0, 256) histogram of value + 128; then S, S2, P, Q, W.
 constexpr int kMeasureWords = 261;
 
+// A Bernoulli(density) soup of 0/1 from a seed, on the device: cell id's draw is
+// (seed; id, 0, 0xFFFFFFFF, 0xFFFFFFFE), a counter the rules never use, compared as a Float32
+// uniform. The synthetic initial state of requests and handles that are given none.
+cudaError_t launch_soup(int8_t* buf, int64_t n1, int64_t n2, int64_t pitch, double density, uint64_t seed, int grid,
+                        cudaStream_t st);
+
 cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t b1, int32_t b2,
                             unsigned long long* acc, int nsm, cudaStream_t st);
 

@@ -44,16 +44,6 @@ namespace gbca {
 
 namespace {
 
-// Bernoulli(density) soup of 0/1 from a seed: draw (seed; cell id, 0, 0xFFFFFFFF, 0xFFFFFFFE),
-// a counter the rules never use. A synthetic-input generator for requests without a state.
-__global__ void k_soup(int8_t* __restrict__ buf, int64_t n1, int64_t n2, int64_t pitch, uint64_t seed, uint32_t thr24) {
-    const int64_t n = n1 * n2;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const uint2 w = cell_draw(seed, (uint64_t)q + 1u, (int64_t)0xFFFFFFFFu, 0xFFFFFFFEu);
-        buf[(q % n1) + (q / n1) * pitch] = (int8_t)((w.x >> 8) < thr24 ? 1 : 0);
-    }
-}
-
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 // First-fit allocator over a device arena (offsets only; the host owns the books).
@@ -282,10 +272,7 @@ cudaError_t init_state(gbca_server* S, Request* r, cudaStream_t st) {
         return e;
     }
     if (r->density > 0.0) {
-        const uint32_t thr = (uint32_t)gbca_threshold(r->density, 1);
-        k_soup<<<S->grid, 256, 0, st>>>(buf, d.n1, d.n2, r->pitch, r->init_seed, thr);
-        count_launch();
-        return cudaGetLastError();
+        return launch_soup(buf, d.n1, d.n2, r->pitch, r->density, r->init_seed, S->grid, st);
     }
     return cudaMemsetAsync(buf, 0, r->bytes / 2, st);
 }

@@ -105,6 +105,12 @@ int gbca_set_state(gbca_handle* h, const void* host, size_t nbytes);
  * copy is queued on the handle's stream. */
 int gbca_set_state_device(gbca_handle* h, const void* dptr, int64_t src_pitch);
 
+/* set_state! with a Bernoulli(density) soup of 0/1 generated on the device from `seed` (cell
+ * id's draw (seed; id, 0, 0xFFFFFFFF, 0xFFFFFFFE) as a Float32 uniform), the same generator
+ * gbca_server_submit uses for requests without a state. Queued on the handle's stream.
+ * No counterpart in the reference (its initial states come from the host). */
+int gbca_set_state_soup(gbca_handle* h, double density, uint64_t seed);
+
 /* Replaces current_state(b, st) (src/backends.jl:132-139; KA ext :126-130): waits for
  * pending work and copies the whole state to host memory. */
 int gbca_get_state(gbca_handle* h, void* host, size_t nbytes);
