@@ -322,7 +322,8 @@ void scheduler(gbca_server* S) {
                 e = q;
                 break;
             }
-            gbca_result res = make_result(r, GBCA_OK, t);
+            // a tile copy that gave up its wait left a tile unwritten: the result is not valid
+            gbca_result res = make_result(r, fire_tma_timeouts_take() ? GBCA_ERR_TIMEOUT : GBCA_OK, t);
             finish_measures(S->h_acc + (size_t)j * kMeasureWords, r->d.n1 * r->d.n2, res.counts, kEnsCounts,
                             &res.other, &res.morans);
             done.push_back(res);

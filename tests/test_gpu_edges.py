@@ -1,0 +1,115 @@
+"""Edge cases of the sweep on the GPU: degenerate and ragged lattices (1 x 1, single rows and
+columns, sides just off the kernels' word and tile sizes), zero-step advances, and a lattice of
+more than 2^32 cells, whose cell ids need the Philox counter's high word
+(src/random.jl:102-107: ctr = (id % 2^32, id >> 32, t, k))."""
+import ctypes
+import zlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ca():
+    import __graft_entry__ as ge
+    ge.build()
+    m = ge.load_package()
+    if m.capi.lib().gbca_device_count() < 1:
+        pytest.fail("no CUDA device visible")
+    return m
+
+
+SHAPES = [(1, 1), (1, 50), (50, 1), (2, 2), (31, 33), (33, 31), (32, 1), (257, 129), (1025, 3)]
+
+
+def _pair(ca, o, kind, n1, n2, bnd):
+    kinds = {"p": (ca.Periodic(), o.PERIODIC), "r": (ca.Reflecting(), o.REFLECTING), "c": (ca.Constant(0), o.CONSTANT)}
+    space = ca.Lattice((n1, n2), (kinds[bnd[0]][0], kinds[bnd[1]][0]))
+    ob = (kinds[bnd[0]][1], kinds[bnd[1]][1])
+    if kind == "life":
+        return ca.Life(":highlife"), space, o.Problem(o.RULE_LIFE, n1, n2, birth=o.mask([3, 6]),
+                                                    survive=o.mask([2, 3]), boundary=ob), 2, None
+    if kind == "ltl":
+        r = ca.Life(list(range(5, 9)), list(range(4, 10)), neighbourhood=ca.Moore(3))
+        return r, space, o.Problem(o.RULE_LIFE, n1, n2, radius=3, birth=o.mask(range(5, 9)),
+                                   survive=o.mask(range(4, 10)), boundary=ob), 2, None
+    if kind == "gen":
+        return ca.Generations(":star_wars"), space, o.Problem(o.RULE_GENERATIONS, n1, n2, birth=o.mask([2]),
+                                                             survive=o.mask([3, 4, 5]), states=4, boundary=ob), 4, None
+    return (ca.ForestFire(), space, o.Problem(o.RULE_FOREST_FIRE, n1, n2, nbhd=o.VON_NEUMANN, boundary=ob, seed=5),
+            3, (0.2, 0.01))
+
+
+@pytest.mark.parametrize("kind", ["life", "ltl", "gen", "fire"])
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}" for a, b in SHAPES])
+def test_degenerate_and_ragged_lattices(ca, oracle, kind, shape):
+    n1, n2 = shape
+    for bnd in ("pp", "rc"):
+        rule, space, P, C, params = _pair(ca, oracle, kind, n1, n2, bnd)
+        P.seed = 5
+        rng = np.random.default_rng(zlib.crc32(f"{kind}{shape}{bnd}".encode()))
+        u0 = rng.integers(0, C, (n1, n2)).astype(np.int8)
+        pd = None if params is None else {"p": params[0], "f": params[1]}
+        prob = ca.CAProblem.new(rule, u0, 13, pd, space=space, seed=5)
+        sol = ca.solve(prob, ca.Synchronous(), backend=ca.GB300Backend(), saveat=13)
+        want = oracle.run_array(P, u0, 0, 13, params)
+        assert np.array_equal(sol.u[-1], want), (kind, shape, bnd)
+
+
+def test_zero_steps_and_repeated_reads(ca):
+    u0 = np.random.default_rng(1).integers(0, 2, (40, 30)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.Life(":conway"), u0, 0)
+    sol = ca.solve(prob, ca.Synchronous(), backend=ca.GB300Backend())
+    assert sol.t == [0] and np.array_equal(sol.u[0], u0)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    capi = ca.capi
+    capi.check(capi.lib().gbca_advance(st.handle, 0, 0, None, 0))
+    assert np.array_equal(ca.current_state(B, st), u0) and np.array_equal(ca.current_state(B, st), u0)
+    st.close()
+
+
+def test_more_than_2_to_32_cells(ca, oracle):
+    """A forest fire on a 65541 x 65539 grid (4.295e9 cells, ids past 2^32): the general
+    kernel's 64-bit ids. The state is a device soup; chosen cells and their neighbours are
+    read before one step, and each cell's next state is checked against the rule with the
+    oracle's draws for its 64-bit id."""
+    n1, n2 = 65541, 65539
+    assert n1 * n2 > 2 ** 32
+    # the problem without a host u0 (4.3 GB): only its shape and element type reach the library
+    prob = ca.CAProblem(rule=ca.ForestFire(), u0=np.zeros(0, np.int8), tspan=(0, 1), p={"p": 0.4, "f": 0.3},
+                        space=ca.Grid(n1, n2), seed=77, neighbours=ca.VonNeumann(1))
+    B = ca.GB300Backend()
+    d = ca.backend.make_desc(prob, ca.Synchronous())
+    st = ca.GB300State(d, np.int8)
+    capi = ca.capi
+    # a soup of trees (1) and empty cells (0); then a few fires (2) written near the chosen cells
+    capi.check(capi.lib().gbca_set_state_soup(st.handle, 0.6, 12345))
+    cells = [(1, 1), (n1, n2), (n1 // 2, n2 - 1), (n1 - 7, n2 - 2), (5, n2), (n1 - 1, 65536), (300, 65535)]
+    for i, j in cells[:3]:
+        if j + 1 <= n2:
+            ca.write_cell(B, st, (i, j + 1), 2)
+
+    def read(i, j):
+        if 1 <= i <= n1 and 1 <= j <= n2:
+            return int(ca.read_cell(B, st, (i, j)))
+        return 0  # Constant(0) edge
+
+    before = {c: (read(*c), [read(c[0] + di, c[1] + dj) for di, dj in ((0, -1), (-1, 0), (1, 0), (0, 1))])
+              for c in cells}
+    capi.check(capi.lib().gbca_advance(st.handle, 0, 1, (ctypes.c_double * 2)(0.4, 0.3), 2))
+    for (i, j), (c, nb) in before.items():
+        cid = (i - 1) + (j - 1) * n1 + 1
+        if c == 2:
+            want = 0
+        elif c == 0:
+            want = 1 if oracle.uniform(77, cid, 0, 1) < 0.4 else 0
+        elif 2 in nb:
+            want = 2
+        else:
+            want = 2 if oracle.uniform(77, cid, 0, 2) < 0.3 else 1
+        assert read(i, j) == want, ((i, j), cid, c, nb)
+    assert any((i - 1) + (j - 1) * n1 + 1 > 2 ** 32 for i, j in cells)
+    st.close()
