@@ -133,4 +133,79 @@ __device__ __forceinline__ void fire_substep_words(const uint32_t* __restrict__ 
     }
 }
 
+// The same sub-step with threads on word columns: thread t takes column w_lo + t % nw and
+// a contiguous run of rows (the rows split into nthr / nw runs), walking down it so each row
+// reuses the two row words it loaded for the row above (3 shared loads per word instead of
+// 5) and steps its addresses and cell ids by one row each. Needs nw <= nthr; threads past
+// the last whole run stay idle.
+template <bool MAPPED>
+__device__ __forceinline__ void fire_substep_rows(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw,
+                                                  int w_lo, int nw, int y_lo, int nrows, int64_t gx0, int64_t gy0,
+                                                  const FireGeom& g, const DrawStep& ds, const PhiloxKeys& K, int tid,
+                                                  int nthr, bool exact) {
+    const int nseg = nthr / nw, seg = tid / nw;
+    if (seg >= nseg) return;
+    const int r0 = y_lo + (int)(((int64_t)seg * nrows) / nseg), r1 = y_lo + (int)(((int64_t)(seg + 1) * nrows) / nseg);
+    if (r0 >= r1) return;
+    const int lw = w_lo + tid % nw;
+    const uint32_t n1 = (uint32_t)g.n1;
+    const int64_t gx = gx0 + 4 * lw;
+    // the column's cells: their lattice x (mapped) and which lie beyond a Constant edge
+    uint32_t mx[4];
+    uint32_t xout = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        if (MAPPED) {
+            const int64_t mb = map_axis(g.bnd0, gx + b, g.n1);
+            mx[b] = (uint32_t)mb;
+            if (mb < 0) xout |= 0xFFu << (8 * b);
+        } else {
+            mx[b] = (uint32_t)gx + b;
+        }
+    }
+    int o = r0 * sw + lw;
+    uint32_t Up = A[o - sw], C = A[o];
+    int64_t gy = gy0 + r0;
+    for (int ly = r0; ly < r1; ++ly, o += sw, ++gy) {
+        const uint32_t Dn = A[o + sw], Wl = A[o - 1], Wr = A[o + 1];
+        const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
+        const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
+        uint32_t E4, F4, N4;
+        if (!exact && !g.exact_always) {
+            E4 = gather4(~(C | (C >> 1)) & 0x01010101u);
+            F4 = gather4((C >> 1) & 0x01010101u);
+            N4 = gather4(((Lf | Rt | Up | Dn) >> 1) & 0x01010101u);
+        } else {
+            E4 = gather4(bytes_eq(C, 0u) >> 7);
+            F4 = gather4(bytes_eq(C, 0x02020202u) >> 7);
+            N4 = gather4((bytes_eq(Lf, 0x02020202u) | bytes_eq(Rt, 0x02020202u) | bytes_eq(Up, 0x02020202u) |
+                          bytes_eq(Dn, 0x02020202u)) >> 7);
+        }
+        uint32_t my = (uint32_t)gy;
+        bool rowout = false;
+        if (MAPPED) {
+            const int64_t m = map_axis(g.bnd1, gy, g.n2);
+            rowout = m < 0;
+            my = (uint32_t)m;
+        }
+        const uint32_t base = my * n1 + 1u;
+        uint2 w[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) w[b] = draw_fast(ds, K, base + mx[b], 2u - ((E4 >> b) & 1u));
+        uint32_t H4 = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) H4 |= (uint32_t)fire_hit(w[b], (E4 >> b) & 1u, g) << b;
+        const uint32_t T4 = ~(E4 | F4) & 0xFu;
+        const uint32_t one = (E4 & H4) | (T4 & ~(N4 | H4)), two = T4 & (N4 | H4);
+        uint32_t res = spread4(one) | (spread4(two) << 1);
+        if (MAPPED) {
+            if (rowout) res = g.cst1;
+            else res = (res & ~xout) | (g.cst0 & xout);
+        }
+        B[o] = res;
+        Up = C;
+        C = Dn;
+    }
+}
+
 }  // namespace gbca

@@ -113,9 +113,9 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
         const DrawStep ds = draw_step(p.keys, p.t0 + s);
         const int ex = p.nsub - 1 - s;
         const int w_lo = (hx - ex) >> 2, w_hi = (hx + kFireTX + ex + 3) >> 2;  // words covering the region
-        fire_substep_words<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
-                                      kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
-                                      s == 0 && !p.states_valid);
+        fire_substep_rows<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
+                                     kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
+                                     s == 0 && !p.states_valid);
         __syncthreads();
         int8_t* t = A; A = B; B = t;
     }

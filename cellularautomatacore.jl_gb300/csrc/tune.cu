@@ -57,7 +57,7 @@ std::vector<SweepChoice> sweep_candidates(const SweepParams& p) {
         // the tile height is fixed by the kernel's word layout; the pass depth and the tile
         // staging (vector loads or TMA) vary
         for (int staging : {0, 1})
-            for (int k : {2, 4, 6, 8, 12}) out.push_back({k, 0, staging});
+            for (int k : {1, 2, 3, 4, 6, 8}) out.push_back({k, 0, staging});
         return out;
     }
     if (!life_simd_supported(p)) return out;

@@ -113,7 +113,7 @@ def test_tune_fire_and_general(ca, oracle):
     B = ca.GB300Backend()
     st = ca.allocate_state(B, prob, ca.Synchronous())
     k, rows, staging = ca.tune(st, prob)
-    assert k in (2, 4, 6, 8, 12) and rows == 0 and staging in (0, 1)
+    assert k in (1, 2, 3, 4, 6, 8) and rows == 0 and staging in (0, 1)
     assert np.array_equal(ca.current_state(B, st), u0)
     got = _run(ca, prob, st, 0, 20, prob.p)
     P = oracle.Problem(oracle.RULE_FOREST_FIRE, 1000, 600, nbhd=oracle.VON_NEUMANN, seed=3,
