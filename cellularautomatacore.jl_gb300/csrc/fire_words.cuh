@@ -137,12 +137,15 @@ __device__ __forceinline__ void fire_substep_words(const uint32_t* __restrict__ 
 // a contiguous run of rows (the rows split into nthr / nw runs), walking down it so each row
 // reuses the two row words it loaded for the row above (3 shared loads per word instead of
 // 5) and steps its addresses and cell ids by one row each. Needs nw <= nthr; threads past
-// the last whole run stay idle.
+// the last whole run stay idle. With gdst set (a sweep's last sub-step, whose region is the
+// output tile), results go straight to the lattice state (pitch bytes between columns), only
+// the cells inside the lattice, instead of to B.
 template <bool MAPPED>
 __device__ __forceinline__ void fire_substep_rows(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw,
                                                   int w_lo, int nw, int y_lo, int nrows, int64_t gx0, int64_t gy0,
                                                   const FireGeom& g, const DrawStep& ds, const PhiloxKeys& K, int tid,
-                                                  int nthr, bool exact) {
+                                                  int nthr, bool exact, int8_t* __restrict__ gdst = nullptr,
+                                                  int64_t gpitch = 0) {
     const int nseg = nthr / nw, seg = tid / nw;
     if (seg >= nseg) return;
     const int r0 = y_lo + (int)(((int64_t)seg * nrows) / nseg), r1 = y_lo + (int)(((int64_t)(seg + 1) * nrows) / nseg);
@@ -198,11 +201,22 @@ __device__ __forceinline__ void fire_substep_rows(const uint32_t* __restrict__ A
         const uint32_t T4 = ~(E4 | F4) & 0xFu;
         const uint32_t one = (E4 & H4) | (T4 & ~(N4 | H4)), two = T4 & (N4 | H4);
         uint32_t res = spread4(one) | (spread4(two) << 1);
-        if (MAPPED) {
-            if (rowout) res = g.cst1;
-            else res = (res & ~xout) | (g.cst0 & xout);
+        if (gdst) {  // cells of the output tile: never beyond a lower edge
+            if (gy < g.n2 && gx < g.n1) {
+                int8_t* q = gdst + gx + gy * gpitch;
+                if (gx + 4 <= g.n1) {
+                    *(uint32_t*)q = res;
+                } else {
+                    for (int b = 0; gx + b < g.n1; ++b) q[b] = (int8_t)(res >> (8 * b));
+                }
+            }
+        } else {
+            if (MAPPED) {
+                if (rowout) res = g.cst1;
+                else res = (res & ~xout) | (g.cst0 & xout);
+            }
+            B[o] = res;
         }
-        B[o] = res;
         Up = C;
         C = Dn;
     }

@@ -113,25 +113,14 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
         const DrawStep ds = draw_step(p.keys, p.t0 + s);
         const int ex = p.nsub - 1 - s;
         const int w_lo = (hx - ex) >> 2, w_hi = (hx + kFireTX + ex + 3) >> 2;  // words covering the region
+        // the last sub-step writes the tile straight to the lattice state
+        const bool last = s == p.nsub - 1;
         fire_substep_rows<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
                                      kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
-                                     s == 0 && !p.states_valid);
+                                     s == 0 && !p.states_valid, last ? dst : nullptr, p.pitch);
+        if (last) return;
         __syncthreads();
         int8_t* t = A; A = B; B = t;
-    }
-
-    if (INTERIOR) {
-        const int qx = kFireTX / 16;
-        for (int q = tid; q < qx * kFireTY; q += nthr) {
-            const int lq = q % qx, oy = q / qx;
-            *(int4*)(dst + (X0 + 16 * lq) + (Y0 + oy) * p.pitch) = *(const int4*)(A + (hy + oy) * sx + hx + 16 * lq);
-        }
-    } else {
-        for (int idx = tid; idx < kFireTX * kFireTY; idx += nthr) {
-            const int ox = idx % kFireTX, oy = idx / kFireTX;
-            const int64_t gx = X0 + ox, gy = Y0 + oy;
-            if (gx < p.n1 && gy < p.n2) dst[gx + gy * p.pitch] = A[(hy + oy) * sx + hx + ox];
-        }
     }
 }
 
