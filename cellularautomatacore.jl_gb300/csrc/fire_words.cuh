@@ -169,7 +169,10 @@ __device__ __forceinline__ void fire_substep_rows(const uint32_t* __restrict__ A
     int o = r0 * sw + lw;
     uint32_t Up = A[o - sw], C = A[o];
     int64_t gy = gy0 + r0;
-    for (int ly = r0; ly < r1; ++ly, o += sw, ++gy) {
+    // direct stores: the column's first cell and how many of its 4 cells lie inside the lattice
+    int8_t* q = gdst ? gdst + gx + gy * gpitch : nullptr;
+    const int64_t xin = g.n1 - gx;
+    for (int ly = r0; ly < r1; ++ly, o += sw, ++gy, q += gpitch) {
         const uint32_t Dn = A[o + sw], Wl = A[o - 1], Wr = A[o + 1];
         const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
         const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
@@ -202,13 +205,12 @@ __device__ __forceinline__ void fire_substep_rows(const uint32_t* __restrict__ A
         const uint32_t one = (E4 & H4) | (T4 & ~(N4 | H4)), two = T4 & (N4 | H4);
         uint32_t res = spread4(one) | (spread4(two) << 1);
         if (gdst) {  // cells of the output tile: never beyond a lower edge
-            if (gy < g.n2 && gx < g.n1) {
-                int8_t* q = gdst + gx + gy * gpitch;
-                if (gx + 4 <= g.n1) {
-                    *(uint32_t*)q = res;
-                } else {
-                    for (int b = 0; gx + b < g.n1; ++b) q[b] = (int8_t)(res >> (8 * b));
-                }
+            if (!MAPPED) {
+                *(uint32_t*)q = res;  // an interior tile: every cell is a lattice cell
+            } else if (gy < g.n2 && xin > 0) {
+                if (xin >= 4) *(uint32_t*)q = res;
+                else
+                    for (int b = 0; b < xin; ++b) q[b] = (int8_t)(res >> (8 * b));
             }
         } else {
             if (MAPPED) {

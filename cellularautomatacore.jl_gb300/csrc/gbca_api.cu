@@ -516,9 +516,9 @@ int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows,
         h->forced = false;
         return GBCA_OK;
     }
-    if (steps_per_pass < 1 || steps_per_pass > 64 || tile_rows < 0 || staging < 0 || staging > 1)
+    if (steps_per_pass < 1 || steps_per_pass > 64 || tile_rows < 0 || staging < 0 || staging > 2)
         return fail(GBCA_ERR_ARGUMENT,
-                    "steps per pass must lie in 1..64, tile rows be non-negative and staging 0 or 1, got %d, %d, %d",
+                    "steps per pass must lie in 1..64, tile rows be non-negative and staging 0..2, got %d, %d, %d",
                     (int)steps_per_pass, (int)tile_rows, (int)staging);
     if (h->d.rule == GBCA_RULE_LENIA || h->d.rule == GBCA_RULE_SI_FIELD)
         return fail(GBCA_ERR_UNSUPPORTED, "sweep geometry applies to the Int8 stencil kernels only");

@@ -10,7 +10,9 @@
 // and temporal blocking (nsub steps per pass, halo nsub) keeps HBM traffic at
 // 2 B / nsub per cell-update.
 //
-// Tile staging (the autotuner's choice, p.staging): where the tile's loaded region lies inside
+// Tile staging (the autotuner's choice, p.staging: 0 vector loads, 1 a TMA copy per tile, 2 the
+// same from a persistent kernel that prefetches each CTA's next tile): where the tile's loaded
+// region lies inside
 // the lattice, or the lattice is a Grid with Constant(0) edges (the tensor's zero fill is then
 // the boundary value), one TMA
 // copy (cp.async.bulk.tensor) brings the whole halo-padded tile into shared memory (for the
@@ -161,6 +163,108 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     else fire_tile<false>(p, src, dst, A, B, staged);
 }
 
+// One step per pass with TMA staging, persistent: each CTA walks the tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... While it computes one tile from one shared buffer, the TMA copy
+// of its next tile fills the other, so the copy's latency hides behind the Philox work; the
+// last (only) sub-step stores straight to HBM, so no third buffer is needed. Tiles that TMA
+// cannot stage (beyond an edge that is not Constant(0)) load through the boundary map.
+__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
+    k_fire_stream(SweepParams p, const int8_t* __restrict__ src, int8_t* __restrict__ dst,
+                  const __grid_constant__ CUtensorMap tmap, int tma, int tiles_x, int ntiles) {
+    extern __shared__ __align__(128) int8_t smem_f[];
+    __shared__ __align__(8) uint64_t bars[2];
+    const int hx = p.halo_x, hy = p.halo_y;  // halo_y = 1: one step per pass
+    const int sx = kFireTX + 2 * hx, sy = kFireTY + 2 * hy, sw = sx / 4;
+    int8_t* const buf0 = smem_f;
+    int8_t* const buf1 = smem_f + sx * sy;  // sx * sy is a multiple of 16
+    const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
+    const int nthr = kFireThreadsX * kFireThreadsY;
+    FireGeom g;
+    g.n1 = p.n1;
+    g.n2 = p.n2;
+    g.bnd0 = p.bnd[0];
+    g.bnd1 = p.bnd[1];
+    g.cst0 = (uint32_t)(uint8_t)p.cval[0] * 0x01010101u;
+    g.cst1 = (uint32_t)(uint8_t)p.cval[1] * 0x01010101u;
+    fire_thresholds(p.thr_p, p.thr_f, p.params_f32 != 0, g);
+    g.exact_always = fire_odd_constant(p.bnd[0], p.cval[0], p.bnd[1], p.cval[1]);
+    const DrawStep ds = draw_step(p.keys, p.t0);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    auto origin = [&](int tile, int64_t* X0, int64_t* Y0) {
+        *X0 = (int64_t)(tile % tiles_x) * kFireTX;
+        *Y0 = (int64_t)(tile / tiles_x) * kFireTY;
+        return *X0 - hx >= 0 && *X0 + kFireTX + hx <= p.n1 && *Y0 - hy >= 0 && *Y0 + kFireTY + hy <= p.n2;
+    };
+    auto staged = [&](bool interior) { return tma == 2 || (tma == 1 && interior); };
+    auto issue = [&](int tile, int k) {  // one thread: the tile's copy into buffer k
+        int64_t X0, Y0;
+        origin(tile, &X0, &Y0);
+        tma_tile_load(&tmap, k ? buf1 : buf0, &bars[k], (int)((X0 - hx) / 16), (int)(Y0 - hy), (uint32_t)(sx * sy));
+    };
+    uint32_t phase = 0u;  // bit k: the parity buffer k's barrier completes next
+    uint32_t pend = 0u;   // bit k: a copy was issued into buffer k and not yet awaited
+    int tile = blockIdx.x, b = 0;
+    if (tile < ntiles) {
+        int64_t X0, Y0;
+        if (staged(origin(tile, &X0, &Y0))) {
+            if (tid == 0) issue(tile, 0);
+            pend |= 1u;
+        }
+    }
+    bool failed = false;
+    for (; tile < ntiles; tile += gridDim.x, b ^= 1) {
+        const int next = tile + (int)gridDim.x;
+        if (next < ntiles) {  // buffer b ^ 1 was last read before the previous iteration's barrier
+            int64_t X1, Y1;
+            if (staged(origin(next, &X1, &Y1))) {
+                if (tid == 0) issue(next, b ^ 1);
+                pend |= 1u << (b ^ 1);
+            }
+        }
+        int64_t X0, Y0;
+        const bool interior = origin(tile, &X0, &Y0);
+        int8_t* const cur = b ? buf1 : buf0;
+        if ((pend >> b) & 1u) {
+            const bool ok = __syncthreads_and(mbar_wait_bounded(&bars[b], (phase >> b) & 1u));
+            phase ^= 1u << b;
+            pend &= ~(1u << b);
+            if (!ok) {
+                failed = true;
+                break;
+            }
+        } else {  // beyond an edge TMA cannot reproduce: the boundary map
+            int8_t* A = cur;
+            for (int idx = tid; idx < sx * sy; idx += nthr) {
+                const int lx = idx % sx, ly = idx / sx;
+                const int64_t mx = map_axis(p.bnd[0], X0 - hx + lx, p.n1), my = map_axis(p.bnd[1], Y0 - hy + ly, p.n2);
+                A[idx] = my < 0 ? (int8_t)p.cval[1] : (mx < 0 ? (int8_t)p.cval[0] : src[mx + my * p.pitch]);
+            }
+            __syncthreads();
+        }
+        const uint32_t* A = (const uint32_t*)cur;
+        if (interior)
+            fire_substep_rows<false>(A, nullptr, sw, hx >> 2, kFireTX / 4, hy, kFireTY, X0 - hx, Y0 - hy, g, ds,
+                                     p.keys, tid, nthr, !p.states_valid, dst, p.pitch);
+        else
+            fire_substep_rows<true>(A, nullptr, sw, hx >> 2, kFireTX / 4, hy, kFireTY, X0 - hx, Y0 - hy, g, ds,
+                                    p.keys, tid, nthr, !p.states_valid, dst, p.pitch);
+        __syncthreads();
+    }
+    if (failed) {
+        if (tid == 0) atomicAdd(&g_fire_tma_timeouts, 1);
+        // let the copies in flight land before the CTA leaves: the one that timed out
+        // (its parity was flipped above) and a prefetch still pending
+        mbar_wait_bounded(&bars[b], ((phase >> b) & 1u) ^ 1u);
+        if ((pend >> (b ^ 1)) & 1u) mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
+    }
+}
+
 // Tensor maps of the state buffers, by buffer and box height (the pass depth sets it).
 struct MapKey {
     const void* base;
@@ -259,7 +363,21 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
                                 p.cval[1] == 0 && p.n1 % 16 == 0;
         tma = zero_edges ? 2 : 1;
     }
-    dim3 grid((unsigned)((p.n1 + kFireTX - 1) / kFireTX), (unsigned)((p.n2 + kFireTY - 1) / kFireTY));
+    const int tiles_x = (int)((p.n1 + kFireTX - 1) / kFireTX), tiles_y = (int)((p.n2 + kFireTY - 1) / kFireTY);
+    if (p.nsub == 1 && tma && p.staging == 2) {  // one step per pass: the persistent, double-buffered kernel
+        e = cudaFuncSetAttribute(k_fire_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fire_stream, kFireThreadsX * kFireThreadsY, smem);
+        const int ntiles = tiles_x * tiles_y;
+        int grid = nsm * (per > 0 ? per : 1);
+        if (grid > ntiles) grid = ntiles;
+        k_fire_stream<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(p, src, dst, map, tma, tiles_x, ntiles);
+        return cudaGetLastError();
+    }
+    dim3 grid((unsigned)tiles_x, (unsigned)tiles_y);
     k_fire<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(p, src, dst, map, tma);
     return cudaGetLastError();
 }

@@ -58,6 +58,7 @@ std::vector<SweepChoice> sweep_candidates(const SweepParams& p) {
         // staging (vector loads or TMA) vary
         for (int staging : {0, 1})
             for (int k : {1, 2, 3, 4, 6, 8}) out.push_back({k, 0, staging});
+        out.push_back({1, 0, 2});  // one step per pass from the persistent prefetching kernel
         return out;
     }
     if (!life_simd_supported(p)) return out;

@@ -71,7 +71,8 @@ def test_generations_geometries(ca, oracle, steps, rows):
     st.close()
 
 
-@pytest.mark.parametrize("steps,staging,n1", [(1, 0, 900), (2, 1, 900), (5, 0, 1024), (12, 1, 1024), (16, 1, 912)])
+@pytest.mark.parametrize("steps,staging,n1", [(1, 0, 900), (2, 1, 900), (5, 0, 1024), (12, 1, 1024), (16, 1, 912),
+                                               (1, 2, 900), (1, 2, 1024), (1, 1, 912)])
 def test_fire_geometries(ca, oracle, steps, staging, n1):
     """Forest fire on an n1 x 410 grid from t = 3, 29 steps; staging 1 stages tiles by TMA
     (interior tiles for n1 = 900, every tile for the multiples of 16)."""
@@ -113,7 +114,7 @@ def test_tune_fire_and_general(ca, oracle):
     B = ca.GB300Backend()
     st = ca.allocate_state(B, prob, ca.Synchronous())
     k, rows, staging = ca.tune(st, prob)
-    assert k in (1, 2, 3, 4, 6, 8) and rows == 0 and staging in (0, 1)
+    assert k in (1, 2, 3, 4, 6, 8) and rows == 0 and staging in (0, 1, 2)
     assert np.array_equal(ca.current_state(B, st), u0)
     got = _run(ca, prob, st, 0, 20, prob.p)
     P = oracle.Problem(oracle.RULE_FOREST_FIRE, 1000, 600, nbhd=oracle.VON_NEUMANN, seed=3,
@@ -142,7 +143,7 @@ def test_geometry_refusals(ca):
     with pytest.raises(ca.ArgumentError):
         ca.set_geometry(st, 65, 0)
     with pytest.raises(ca.ArgumentError):
-        ca.set_geometry(st, 4, 0, 2)  # staging is 0 or 1
+        ca.set_geometry(st, 4, 0, 3)  # staging is 0, 1 or 2
     st.close()
     ltl = ca.CAProblem.new(ca.Life(LTL["birth"], LTL["survive"], neighbourhood=ca.Moore(5)),
                            np.zeros((4096, 4096), np.int8), 5)
