@@ -138,7 +138,8 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     const int64_t X0 = (int64_t)blockIdx.x * kFireTX, Y0 = (int64_t)blockIdx.y * kFireTY;
     const bool interior = X0 - p.halo_x >= 0 && X0 + kFireTX + p.halo_x <= p.n1 && Y0 - p.halo_y >= 0 &&
                           Y0 + kFireTY + p.halo_y <= p.n2;
-    const bool staged = tma == 2 || (tma == 1 && interior);
+    // a tensor copy's shared destination must be 128-byte aligned (the dynamic base is)
+    const bool staged = (smem_u32(A) & 127u) == 0u && (tma == 2 || (tma == 1 && interior));
     if (staged) {
         const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
         if (tid == 0) {
@@ -175,8 +176,11 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     __shared__ __align__(8) uint64_t bars[2];
     const int hx = p.halo_x, hy = p.halo_y;  // halo_y = 1: one step per pass
     const int sx = kFireTX + 2 * hx, sy = kFireTY + 2 * hy, sw = sx / 4;
+    // a tensor copy's shared destination must be 128-byte aligned: buffers start on 128 bytes
+    const int stride = (sx * sy + 127) / 128 * 128;
     int8_t* const buf0 = smem_f;
-    int8_t* const buf1 = smem_f + sx * sy;  // sx * sy is a multiple of 16
+    int8_t* const buf1 = smem_f + stride;
+    const bool aligned = ((smem_u32(buf0) | smem_u32(buf1)) & 127u) == 0u;
     const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
     const int nthr = kFireThreadsX * kFireThreadsY;
     FireGeom g;
@@ -201,10 +205,13 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
         *Y0 = (int64_t)(tile / tiles_x) * kFireTY;
         return *X0 - hx >= 0 && *X0 + kFireTX + hx <= p.n1 && *Y0 - hy >= 0 && *Y0 + kFireTY + hy <= p.n2;
     };
-    auto staged = [&](bool interior) { return tma == 2 || (tma == 1 && interior); };
+    auto staged = [&](bool interior) { return aligned && (tma == 2 || (tma == 1 && interior)); };
     auto issue = [&](int tile, int k) {  // one thread: the tile's copy into buffer k
         int64_t X0, Y0;
         origin(tile, &X0, &Y0);
+        // order the buffer's earlier generic-proxy reads and writes (finished at the last
+        // barrier) before the async-proxy copy that overwrites it
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tma_tile_load(&tmap, k ? buf1 : buf0, &bars[k], (int)((X0 - hx) / 16), (int)(Y0 - hy), (uint32_t)(sx * sy));
     };
     uint32_t phase = 0u;  // bit k: the parity buffer k's barrier completes next
@@ -365,16 +372,17 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     }
     const int tiles_x = (int)((p.n1 + kFireTX - 1) / kFireTX), tiles_y = (int)((p.n2 + kFireTY - 1) / kFireTY);
     if (p.nsub == 1 && tma && p.staging == 2) {  // one step per pass: the persistent, double-buffered kernel
-        e = cudaFuncSetAttribute(k_fire_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const size_t smem2 = 2 * (((size_t)sx * sy + 127) / 128 * 128);  // two 128-byte-aligned buffers
+        e = cudaFuncSetAttribute(k_fire_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
         if (e != cudaSuccess) return e;
         int dev = 0, nsm = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fire_stream, kFireThreadsX * kFireThreadsY, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fire_stream, kFireThreadsX * kFireThreadsY, smem2);
         const int ntiles = tiles_x * tiles_y;
         int grid = nsm * (per > 0 ? per : 1);
         if (grid > ntiles) grid = ntiles;
-        k_fire_stream<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(p, src, dst, map, tma, tiles_x, ntiles);
+        k_fire_stream<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem2, st>>>(p, src, dst, map, tma, tiles_x, ntiles);
         return cudaGetLastError();
     }
     dim3 grid((unsigned)tiles_x, (unsigned)tiles_y);

@@ -152,3 +152,22 @@ def test_geometry_refusals(ca):
         ca.set_geometry(st, 6, 4000)  # far beyond shared memory
     ca.set_geometry(st, 0, 0)
     st.close()
+
+
+@pytest.mark.parametrize("space", ["grid", "torus"])
+def test_fire_persistent_multi_tile(ca, oracle, space):
+    """The persistent prefetching kernel (staging 2) with more tiles than CTAs, so each CTA
+    runs several tiles through both of its shared buffers: a 4096 x 4096 lattice (512 tiles),
+    on a Constant(0) grid (every tile a TMA copy) and on a torus (edge tiles through the
+    boundary map), 6 steps."""
+    n = 4096
+    u0 = np.random.default_rng(99).integers(0, 3, (n, n)).astype(np.int8)
+    sp = ca.Grid(n, n) if space == "grid" else ca.Torus(n, n)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 6, {"p": 0.05, "f": 0.002}, space=sp, seed=21)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, 1, 0, 2)
+    got = _run(ca, prob, st, 0, 6, prob.p)
+    bnd = (oracle.CONSTANT, oracle.CONSTANT) if space == "grid" else (oracle.PERIODIC, oracle.PERIODIC)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, n, n, nbhd=oracle.VON_NEUMANN, seed=21, boundary=bnd)
+    assert np.array_equal(got, oracle.run_array(P, u0, 0, 6, (0.05, 0.002), nthreads=16))
+    st.close()
