@@ -607,6 +607,21 @@ def bench_served(capi, lib):
     return served
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The largest of every rank's x (a time): the whole job is as slow as its slowest replica."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world: int, cell_updates_per_rank: float, ms_per_step: float) -> float:
+    """Whole-job Gcell-updates/s of `world` replicas that each run the workload per step."""
+    return world * cell_updates_per_rank / (ms_per_step * 1e-3) / 1e9
+
+
 def main():
     args = parse()
     if args.case:
@@ -687,12 +702,9 @@ def main():
     launches = lib.gbca_kernel_launches() - launches0
     ms_total = start.elapsed_time(stop)
     part_ms = [sum(e[0].elapsed_time(e[1]) for e in ev), sum(e[2].elapsed_time(e[3]) for e in ev)]
-    if dist is not None:
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(ms_total, dist, "cuda")
     ms_per_step = ms_total / args.steps
-    value = world * cell_updates() / (ms_per_step * 1e-3) / 1e9
+    value = replica_value(world, cell_updates(), ms_per_step)
 
     # ---- roofline of the dominant kernel
     per_pass = {"ltl": geometry.get("ltl", (0, 0))[0] or 4, "fire": geometry.get("fire", (0, 0))[0] or 8}
@@ -744,12 +756,9 @@ def main():
         step_e2e()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     nbytes = sum(x.numel() for x in host_in)
-    e2e = {"value": world * cell_updates() / (e2e_s / args.steps) / 1e9, "unit": "Gcell-updates/s",
+    e2e = {"value": replica_value(world, cell_updates(), e2e_s / args.steps * 1e3), "unit": "Gcell-updates/s",
            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3}
 
     batched = None
