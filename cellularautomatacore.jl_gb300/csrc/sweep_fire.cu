@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
 // of its next tile fills the other, so the copy's latency hides behind the Philox work; the
 // last (only) sub-step stores straight to HBM, so no third buffer is needed. Tiles that TMA
 // cannot stage (beyond an edge that is not Constant(0)) load through the boundary map.
-__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
+__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY, 2)  // two CTAs per SM: <= 64 registers
     k_fire_stream(SweepParams p, const int8_t* __restrict__ src, int8_t* __restrict__ dst,
                   const __grid_constant__ CUtensorMap tmap, int tma, int tiles_x, int ntiles) {
     extern __shared__ __align__(128) int8_t smem_f[];
