@@ -89,9 +89,9 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
     if (force) choice = *force;
     else if ((fire || life) && !tuned_choice(d, &choice) && fire) {
         // untuned forest fire: on large lattices one step per pass from the persistent TMA
-        // kernel (the compute-bound optimum); on small ones 4 steps per pass, a quarter of the
-        // launches for a launch-bound grid
-        choice = d.n1 * d.n2 >= ((int64_t)1 << 24) ? SweepChoice{1, 0, 2} : SweepChoice{4, 0, 1};
+        // kernel (the compute-bound optimum); on small ones 8 steps per pass with vector
+        // loads, an eighth of the launches for a launch-bound grid
+        choice = d.n1 * d.n2 >= ((int64_t)1 << 24) ? SweepChoice{1, 0, 2} : SweepChoice{8, 0, 0};
     }
     p.tile_y = choice.tile_rows;
     p.staging = choice.staging;

@@ -115,14 +115,35 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
         const DrawStep ds = draw_step(p.keys, p.t0 + s);
         const int ex = p.nsub - 1 - s;
         const int w_lo = (hx - ex) >> 2, w_hi = (hx + kFireTX + ex + 3) >> 2;  // words covering the region
-        // the last sub-step writes the tile straight to the lattice state
-        const bool last = s == p.nsub - 1;
-        fire_substep_rows<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
-                                     kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
-                                     s == 0 && !p.states_valid, last ? dst : nullptr, p.pitch);
-        if (last) return;
+        const bool exact = s == 0 && !p.states_valid;
+        if (p.nsub == 1) {
+            // one step: the region is the tile itself (64 words, all 512 threads busy walking
+            // rows), stored straight to the lattice state
+            fire_substep_rows<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
+                                         kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr, exact, dst,
+                                         p.pitch);
+            return;
+        }
+        // deeper passes: the region is wider than the tile in early sub-steps, so the flat
+        // word x row split keeps every thread busy
+        fire_substep_words<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
+                                      kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr, exact);
         __syncthreads();
         int8_t* t = A; A = B; B = t;
+    }
+
+    if (INTERIOR) {  // 16-byte stores: X0, the tile width and the pitch are multiples of 16
+        const int qx = kFireTX / 16;
+        for (int q = tid; q < qx * kFireTY; q += nthr) {
+            const int lq = q % qx, oy = q / qx;
+            *(int4*)(dst + (X0 + 16 * lq) + (Y0 + oy) * p.pitch) = *(const int4*)(A + (hy + oy) * sx + hx + 16 * lq);
+        }
+    } else {
+        for (int idx = tid; idx < kFireTX * kFireTY; idx += nthr) {
+            const int ox = idx % kFireTX, oy = idx / kFireTX;
+            const int64_t gx = X0 + ox, gy = Y0 + oy;
+            if (gx < p.n1 && gy < p.n2) dst[gx + gy * p.pitch] = A[(hy + oy) * sx + hx + ox];
+        }
     }
 }
 
@@ -169,7 +190,7 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
 // of its next tile fills the other, so the copy's latency hides behind the Philox work; the
 // last (only) sub-step stores straight to HBM, so no third buffer is needed. Tiles that TMA
 // cannot stage (beyond an edge that is not Constant(0)) load through the boundary map.
-__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY, 2)  // two CTAs per SM: <= 64 registers
+__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     k_fire_stream(SweepParams p, const int8_t* __restrict__ src, int8_t* __restrict__ dst,
                   const __grid_constant__ CUtensorMap tmap, int tma, int tiles_x, int ntiles) {
     extern __shared__ __align__(128) int8_t smem_f[];
