@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-saves", action="store_true", help="skip the save-path measurement")
     ap.add_argument("--no-sparse", action="store_true", help="skip the active-tile measurement")
+    ap.add_argument("--pin", default="", help="pin the sweeps' geometry instead of tuning, e.g. "
+                    "'ltl=6,216,0;fire=1,0,1' (steps per pass, tile rows, staging), for profiling runs")
     return ap.parse_args()
 
 
@@ -677,9 +679,14 @@ def main():
 
     # the autotuner picks each sweep's geometry on the initial states (untimed, like warm-up)
     geometry = {}
+    pins = dict(kv.split("=") for kv in args.pin.split(";") if kv) if args.pin else {}
     for name, h, d0, (n1, n2) in zip(("ltl", "fire"), handles, dev0, sizes):
         capi.check(lib.gbca_set_state_device(h, ctypes.c_void_p(d0.data_ptr()), n1))
-        if not args.no_tune:
+        if name in pins:
+            k, rows, staging = (int(x) for x in pins[name].split(","))
+            capi.check(lib.gbca_set_geometry(h, k, rows, staging))
+            geometry[name] = (k, rows, staging)
+        elif not args.no_tune:
             geometry[name] = tune(capi, lib, h, params_fire if name == "fire" else None, 2 if name == "fire" else 0)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
