@@ -81,6 +81,7 @@ SIGNATURES = {
     "gbca_set_field": (ctypes.c_int, [_V, ctypes.c_int32, _V, _V, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "gbca_set_covariate": (ctypes.c_int, [_V, _V, _I64, ctypes.c_int32]),
     "gbca_philox_rate": (ctypes.c_int, [_I64, _P(ctypes.c_double)]),
+    "gbca_selftest_wait": (ctypes.c_int, [ctypes.c_int32]),
     "gbca_set_geometry": (ctypes.c_int, [_V, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "gbca_threshold": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_int32]),
     "gbca_ensemble_create": (ctypes.c_int, [_P(Desc), ctypes.c_int32, _P(_V)]),

@@ -448,6 +448,13 @@ int gbca_set_state_device(gbca_handle* h, const void* dptr, int64_t src_pitch) {
     return GBCA_OK;
 }
 
+int gbca_selftest_wait(int32_t polls) {
+    if (polls < 1 || polls > (1 << 20)) return fail(GBCA_ERR_ARGUMENT, "polls must lie in 1..2^20, got %d", (int)polls);
+    GBCA_CUDA(gbca::launch_wait_probe(polls, nullptr), "wait probe");
+    GBCA_CUDA(cudaDeviceSynchronize(), "wait probe");
+    return check_timeouts();
+}
+
 int gbca_set_state_soup(gbca_handle* h, double density, uint64_t seed) {
     if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
     if (h->esize != 1) return fail(GBCA_ERR_UNSUPPORTED, "a soup is an Int8 state");

@@ -244,5 +244,7 @@ bool fire_fast_supported(const SweepParams& p);
 cudaError_t launch_fire(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 // Tiles whose TMA copy did not complete within its wait limit since the last call (cleared).
 int fire_tma_timeouts_take();
+// One bounded wait (`polls` polls) on a barrier nothing completes: exercises the timeout path.
+cudaError_t launch_wait_probe(int polls, cudaStream_t st);
 
 }  // namespace gbca

@@ -55,10 +55,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
     return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase) {
-    for (int it = 0; it < kTmaSpins; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, int limit = kTmaSpins) {
+    for (int it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
+}
+
+// The timeout path on purpose: one bounded wait on a barrier that nothing completes (no copy is
+// issued), recorded like a tile copy that gave up. Nothing is in flight when the CTA leaves.
+__global__ void k_wait_probe(int polls) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool ok = __syncthreads_and(mbar_wait_bounded(&bar, 0, polls));
+    if (!ok && threadIdx.x == 0) atomicAdd(&g_fire_tma_timeouts, 1);
 }
 
 // One thread: arm the barrier for `bytes` and issue the 3-D tile copy into `dst`.
@@ -349,6 +362,12 @@ bool tile_map(const void* base, int64_t n1, int64_t n2, int64_t pitch, int sx, i
 }
 
 }  // namespace
+
+cudaError_t launch_wait_probe(int polls, cudaStream_t st) {
+    k_wait_probe<<<1, 32, 0, st>>>(polls);
+    count_launch();
+    return cudaGetLastError();
+}
 
 int fire_tma_timeouts_take() {
     int n = 0;

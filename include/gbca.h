@@ -210,6 +210,12 @@ int64_t gbca_kernel_launches(void);
  * draw per cell-update. A diagnostic with no counterpart in the reference. */
 int gbca_philox_rate(int64_t draws, double* draws_per_s);
 
+/* Self-test of the failure path of the device-side waits: one kernel waits, at most `polls`
+ * polls (1..2^20), on a barrier that nothing completes, and records the timeout as a tile copy
+ * that gave up would. Returns GBCA_ERR_TIMEOUT, read on the host; the context stays usable.
+ * Nothing faults, traps or hangs. No counterpart in the reference. */
+int gbca_selftest_wait(int32_t polls);
+
 /* ---- sweep autotuning. No counterpart in the reference (its kernels have one geometry).
  * A sweep geometry is (steps per temporally blocked pass, tile rows, tile staging). gbca_tune
  * times every candidate geometry of the handle's fast kernel (forest fire: pass depth x

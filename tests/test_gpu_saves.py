@@ -76,3 +76,15 @@ def test_save_everystep_and_callbacks(ca, oracle):
     u[0:5, 0:5] = 1
     u = oracle.run_array(P, u, 7, 13)
     assert sol.t == [0, 5, 10, 15, 20] and np.array_equal(sol.u[-1], u)
+
+
+def test_bounded_wait_reports_timeout(ca):
+    """The failure path of the device-side waits, without a fault: a kernel waits (at most
+    256 polls) on a barrier nothing completes; the host reads GBCA_ERR_TIMEOUT and the context
+    stays usable."""
+    with pytest.raises(ca.errors.DeviceTimeout):
+        ca.capi.check(ca.capi.lib().gbca_selftest_wait(256))
+    u0 = np.random.default_rng(2).integers(0, 2, (64, 64)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.Life(":conway"), u0, 5)
+    sol = ca.solve(prob, ca.Synchronous(), backend=ca.GB300Backend())
+    assert len(sol.u) == 6
