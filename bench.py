@@ -714,7 +714,13 @@ def main():
     value = replica_value(world, cell_updates(), ms_per_step)
 
     # ---- roofline of the dominant kernel
-    per_pass = {"ltl": geometry.get("ltl", (0, 0))[0] or 4, "fire": geometry.get("fire", (0, 0))[0] or 8}
+    per_pass = {}
+    for name, h in zip(("ltl", "fire"), handles):  # the geometry the sweeps ran with
+        k, rows, staging = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        capi.check(lib.gbca_geometry(h, params_fire if name == "fire" else None, ctypes.byref(k), ctypes.byref(rows),
+                                     ctypes.byref(staging)))
+        per_pass[name] = max(1, k.value)
+        geometry.setdefault(name, (k.value, rows.value, staging.value))
     parts = {}
     for name, cfg, ms in (("ltl", LTL, part_ms[0]), ("fire", FIRE, part_ms[1])):
         launches_part = -(-cfg["steps"] // per_pass[name])

@@ -73,6 +73,8 @@ SIGNATURES = {
     "gbca_tune": (ctypes.c_int, [_V, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_int32), _P(ctypes.c_int32),
                                  _P(ctypes.c_int32)]),
     "gbca_forget_tuning": (ctypes.c_int, []),
+    "gbca_geometry": (ctypes.c_int, [_V, _P(ctypes.c_double), _P(ctypes.c_int32), _P(ctypes.c_int32),
+                                     _P(ctypes.c_int32)]),
     "gbca_set_mask": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
     "gbca_snapshot": (ctypes.c_int, [_V, _P(_I64)]),
     "gbca_set_state_soup": (ctypes.c_int, [_V, ctypes.c_double, ctypes.c_uint64]),

@@ -512,6 +512,21 @@ int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* st
     return GBCA_OK;
 }
 
+int gbca_geometry(gbca_handle* h, const double* params, int32_t* steps_per_pass, int32_t* tile_rows,
+                  int32_t* staging) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    gbca::SweepChoice c = {0, 0, 0};
+    if (h->d.rule != GBCA_RULE_LENIA && h->d.rule != GBCA_RULE_SI_FIELD && !h->sparse_on) {
+        const gbca::SweepParams p = handle_params(h, params);
+        const bool fire = gbca::fire_fast_supported(p), life = !fire && gbca::life_simd_supported(p);
+        if (fire || life) c = gbca::sweep_choice(h->d, fire, life, h->forced ? &h->force : nullptr);
+    }
+    if (steps_per_pass) *steps_per_pass = c.steps_per_pass;
+    if (tile_rows) *tile_rows = c.tile_rows;
+    if (staging) *staging = c.staging;
+    return GBCA_OK;
+}
+
 int gbca_forget_tuning(void) {
     gbca::forget_choices();
     return GBCA_OK;

@@ -221,6 +221,10 @@ cudaError_t launch_tile_flags(const int8_t* u, int64_t n1, int64_t n2, int64_t p
 // Whether a background cell whose neighbours are all background stays background.
 bool rule_quiescent(const gbca_desc& d, const double* params, int32_t background);
 
+// The geometry the next sweep of a problem uses: the pinned one, the tuned one, or the kernel's
+// default (steps per pass filled in for the fast kernels).
+SweepChoice sweep_choice(const gbca_desc& d, bool fire, bool life, const SweepChoice* force);
+
 // The autotuner's cached choice for a problem shape (tune.cu); false when it has none.
 bool tuned_choice(const gbca_desc& d, SweepChoice* out);
 void store_choice(const gbca_desc& d, const SweepChoice& c);

@@ -37,6 +37,23 @@ SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params
     return p;
 }
 
+SweepChoice sweep_choice(const gbca_desc& d, bool fire, bool life, const SweepChoice* force) {
+    SweepChoice choice = {0, 0, 0};
+    if (force) return *force;
+    if ((fire || life) && !tuned_choice(d, &choice) && fire) {
+        // untuned forest fire: on large lattices one step per pass from the persistent TMA
+        // kernel (the compute-bound optimum); on small ones 8 steps per pass with vector
+        // loads, an eighth of the launches for a launch-bound grid
+        choice = d.n1 * d.n2 >= ((int64_t)1 << 24) ? SweepChoice{1, 0, 2} : SweepChoice{8, 0, 0};
+    }
+    if (life && choice.steps_per_pass == 0) {
+        SweepParams p = sweep_params(d, 0, nullptr);
+        p.radius = d.radius;
+        choice.steps_per_pass = life_steps_per_pass(p);
+    }
+    return choice;
+}
+
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
                        const double* params, cudaStream_t st, bool states_valid, const SweepChoice* force,
                        const uint8_t* mask, const SparseTiles* sparse) {
@@ -85,14 +102,7 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
     }
     const bool fire = fire_fast_supported(p);
     const bool life = !fire && life_simd_supported(p);
-    SweepChoice choice = {0, 0, 0};
-    if (force) choice = *force;
-    else if ((fire || life) && !tuned_choice(d, &choice) && fire) {
-        // untuned forest fire: on large lattices one step per pass from the persistent TMA
-        // kernel (the compute-bound optimum); on small ones 8 steps per pass with vector
-        // loads, an eighth of the launches for a launch-bound grid
-        choice = d.n1 * d.n2 >= ((int64_t)1 << 24) ? SweepChoice{1, 0, 2} : SweepChoice{8, 0, 0};
-    }
+    const SweepChoice choice = sweep_choice(d, fire, life, force);
     p.tile_y = choice.tile_rows;
     p.staging = choice.staging;
     while (nsteps > 0) {

@@ -229,6 +229,12 @@ int gbca_selftest_wait(int32_t polls);
 int gbca_tune(gbca_handle* h, const double* params, int32_t nparams, int32_t* steps_per_pass, int32_t* tile_rows,
               int32_t* staging);
 
+/* The geometry the handle's next sweep uses (pinned, tuned or the kernel's default), (0, 0, 0)
+ * for the general kernel, Lenia, the SI rule and active-tile sweeps. params as in gbca_advance
+ * (the forest fire's decide whether its fast kernel applies). */
+int gbca_geometry(gbca_handle* h, const double* params, int32_t* steps_per_pass, int32_t* tile_rows,
+                  int32_t* staging);
+
 /* Clears the tuning cache (all shapes). */
 int gbca_forget_tuning(void);
 
