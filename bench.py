@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
-    ap.add_argument("--case", choices=["ltl", "fire", "lenia", "lenia-fft"], default=None,
+    ap.add_argument("--case", choices=["ltl", "fire", "lenia", "lenia-fft", "ensemble"], default=None,
                     help="time single passes of one kernel on an n x n lattice (for profiling)")
     ap.add_argument("--n", type=int, default=4096)
     ap.add_argument("--no-tune", action="store_true", help="keep the kernels' default sweep geometry")
@@ -222,6 +222,39 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_ensemble_case(capi, lib, args):
+    """`steps` timed runs of a batched forest-fire ensemble of `n` instances (the batched
+    workload's size distribution and parameters, 100 steps each), after `warmup` runs."""
+    sides, ps, fs, seeds = ensemble_instances()
+    n = min(args.n, len(sides))
+    descs = (capi.Desc * n)()
+    for i in range(n):
+        descs[i] = fire_desc(capi, sides[i], seeds[i])
+    e = ctypes.c_void_p()
+    capi.check(lib.gbca_ensemble_create(descs, n, ctypes.byref(e)))
+    if args.spp:
+        capi.check(lib.gbca_ensemble_set_geometry(e, 128, args.spp))
+    T0 = (ctypes.c_int64 * n)()
+    S = (ctypes.c_int64 * n)(*([100] * n))
+    P = (ctypes.c_double * (2 * n))(*np.column_stack([ps[:n], fs[:n]]).ravel().tolist())
+
+    def run():
+        capi.check(lib.gbca_ensemble_fill(e, 0))
+        capi.check(lib.gbca_ensemble_run(e, T0, S, P, 2))
+        capi.check(lib.gbca_ensemble_sync(e))
+
+    for _ in range(args.warmup):
+        run()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run()
+    dt = (time.perf_counter() - t0) / args.steps
+    cu = float((sides[:n].astype(np.float64) ** 2).sum() * 100)
+    print(json.dumps({"case": "ensemble", "instances": n, "s_per_run": dt, "sims_per_s": n / dt,
+                      "gcell_updates_s": cu / dt / 1e9}))
+    lib.gbca_ensemble_destroy(e)
+
+
 def run_case(args):
     """`steps` timed passes (one kernel launch each for the sweeps, one step for Lenia) of
     one workload on an n x n lattice after `warmup` untimed ones."""
@@ -230,6 +263,8 @@ def run_case(args):
     ge.build()
     ca = ge.load_package()
     capi, lib = ca.capi, ca.capi.lib()
+    if args.case == "ensemble":
+        return run_ensemble_case(capi, lib, args)
     n = args.n
     d1, d2 = descs(capi)
     rng = np.random.Generator(np.random.PCG64(2))
