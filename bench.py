@@ -59,6 +59,10 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-saves", action="store_true", help="skip the save-path measurement")
     ap.add_argument("--no-sparse", action="store_true", help="skip the active-tile measurement")
+    ap.add_argument("--large", default=None, help="ensemble case: 'min_cells,steps_per_pass' of the batched "
+                    "large-instance passes (0,1: none)")
+    ap.add_argument("--side-range", default="", help="ensemble case: keep the instances with lo <= side < hi "
+                    "('lo,hi')")
     ap.add_argument("--pin", default="", help="pin the sweeps' geometry instead of tuning, e.g. "
                     "'ltl=6,216,0;fire=1,0,1' (steps per pass, tile rows, staging), for profiling runs")
     return ap.parse_args()
@@ -226,6 +230,10 @@ def run_ensemble_case(capi, lib, args):
     """`steps` timed runs of a batched forest-fire ensemble of `n` instances (the batched
     workload's size distribution and parameters, 100 steps each), after `warmup` runs."""
     sides, ps, fs, seeds = ensemble_instances()
+    if args.side_range:
+        lo, hi = (int(x) for x in args.side_range.split(","))
+        keep = (sides >= lo) & (sides < hi)
+        sides, ps, fs, seeds = sides[keep], ps[keep], fs[keep], seeds[keep]
     n = min(args.n, len(sides))
     descs = (capi.Desc * n)()
     for i in range(n):
@@ -234,6 +242,9 @@ def run_ensemble_case(capi, lib, args):
     capi.check(lib.gbca_ensemble_create(descs, n, ctypes.byref(e)))
     if args.spp:
         capi.check(lib.gbca_ensemble_set_geometry(e, 128, args.spp))
+    if args.large is not None:
+        cells, k = (int(x) for x in args.large.split(","))
+        capi.check(lib.gbca_ensemble_set_large(e, cells, k))
     T0 = (ctypes.c_int64 * n)()
     S = (ctypes.c_int64 * n)(*([100] * n))
     P = (ctypes.c_double * (2 * n))(*np.column_stack([ps[:n], fs[:n]]).ravel().tolist())
@@ -250,8 +261,11 @@ def run_ensemble_case(capi, lib, args):
         run()
     dt = (time.perf_counter() - t0) / args.steps
     cu = float((sides[:n].astype(np.float64) ** 2).sum() * 100)
+    geo = [ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()]
+    capi.check(lib.gbca_ensemble_geometry(e, *[ctypes.byref(x) for x in geo]))
     print(json.dumps({"case": "ensemble", "instances": n, "s_per_run": dt, "sims_per_s": n / dt,
-                      "gcell_updates_s": cu / dt / 1e9}))
+                      "gcell_updates_s": cu / dt / 1e9, "large_cells": geo[2].value, "large_steps": geo[3].value,
+                      "large_instances": geo[4].value}))
     lib.gbca_ensemble_destroy(e)
 
 
@@ -460,10 +474,14 @@ def bench_batched(capi, lib, warmup: int, steps: int):
     capi.check(lib.gbca_ensemble_tune(e, 16, P, 2, ctypes.byref(tile), ctypes.byref(depth)))
     for _ in range(warmup):
         run()
+    geo = [ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()]
+    capi.check(lib.gbca_ensemble_geometry(e, *[ctypes.byref(x) for x in geo]))
+    l0 = lib.gbca_kernel_launches()
     t0 = time.perf_counter()
     for _ in range(steps):
         run()
     t_batched = (time.perf_counter() - t0) / steps
+    launches = (lib.gbca_kernel_launches() - l0) / steps
     C = (ctypes.c_int64 * (3 * n))()
     O = (ctypes.c_int64 * n)()
     M = (ctypes.c_double * n)()
@@ -501,8 +519,10 @@ def bench_batched(capi, lib, warmup: int, steps: int):
             "plain_sims_per_s": plain_sims, "plain_sample": len(sample),
             "plain_gcell_updates_s": sample_cu / t_plain / 1e9,
             "speedup_vs_plain": (n / t_batched) / plain_sims,
-            "exact_matches_in_sample": exact, "launches_per_run": 1,
-            "geometry": {"tile": tile.value, "depth": depth.value, "picked_by": "gbca_ensemble_tune"}}
+            "exact_matches_in_sample": exact, "graph_launches_per_run": 1, "kernels_per_run": launches,
+            "geometry": {"tile": tile.value, "depth": depth.value, "large_cells": geo[2].value,
+                         "large_steps_per_pass": geo[3].value, "large_instances": geo[4].value,
+                         "picked_by": "gbca_ensemble_tune"}}
 
 
 SERVE = dict(rate=2000.0, seconds=2.0, plain_sample=48, hbm_budget=8 << 30, chunk_steps=100,

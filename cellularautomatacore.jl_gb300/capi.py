@@ -95,6 +95,9 @@ SIGNATURES = {
     "gbca_ensemble_summaries": (ctypes.c_int, [_V, _P(_I64), ctypes.c_int32, _P(_I64), _P(ctypes.c_double)]),
     "gbca_ensemble_get_state": (ctypes.c_int, [_V, ctypes.c_int32, _V, ctypes.c_size_t]),
     "gbca_ensemble_set_geometry": (ctypes.c_int, [_V, ctypes.c_int32, ctypes.c_int32]),
+    "gbca_ensemble_set_large": (ctypes.c_int, [_V, _I64, ctypes.c_int32]),
+    "gbca_ensemble_geometry": (ctypes.c_int, [_V, _P(ctypes.c_int32), _P(ctypes.c_int32), _P(_I64),
+                                              _P(ctypes.c_int32), _P(ctypes.c_int32)]),
     "gbca_ensemble_tune": (ctypes.c_int, [_V, _I64, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_int32),
                                           _P(ctypes.c_int32)]),
     "gbca_server_start": (ctypes.c_int, [_P(ServerConfig), _P(_V)]),

@@ -19,6 +19,15 @@
 // At the end the CTA reduces the final state to the exact integers behind state_counts and
 // Moran's I (src/measures.jl:14-20,91-107) — the same sums, hence the same bits, as
 // gbca_summaries on a single handle.
+//
+// Large forest-fire instances (2^18 cells or more by default) would each hold one CTA for far
+// longer than the rest of the ensemble takes. They run instead as batched multi-lattice passes
+// (launch_fire_batch: every tile of every large instance in one launch, one launch per pass of
+// K steps) on a second stream forked off the same CUDA graph, then a batched reduction writes
+// their summaries; the persistent kernel runs the rest meanwhile. Their buffers use a 128-byte
+// pitch for the fire kernel's 16-byte vector loads. The per-run data of both paths (start
+// buffer, t0, steps, thresholds) is uploaded before each graph launch; the graph is captured
+// again only when its shape changes (the large set, the number of passes, the geometry).
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
@@ -284,6 +293,43 @@ __device__ int run_tiled_fire(const EnsInstance& I, int8_t* pool, int8_t* A0, in
     return cur;
 }
 
+// Cell (i, j)'s share of the summary words: its value counted (0..7, else "other"), S, S2, and
+// its VonNeumann(1) pairs' P, Q and W (a neighbour beyond a Constant edge is no neighbour).
+__device__ __forceinline__ void summary_cell(const int8_t* base, int64_t pitch, int64_t n1, int64_t n2, int32_t bnd0,
+                                             int32_t bnd1, int64_t i, int64_t j, long long* acc) {
+    const int x = base[i + j * pitch];
+    if (x >= 0 && x < kEnsCounts) {
+#pragma unroll
+        for (int v = 0; v < kEnsCounts; ++v) acc[v] += (x == v);
+    } else {
+        acc[kEnsCounts] += 1;
+    }
+    acc[kEnsCounts + 1] += x;
+    acc[kEnsCounts + 2] += x * x;
+    const int di[4] = {0, -1, 1, 0}, dj[4] = {-1, 0, 0, 1};
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        const int64_t a = map_axis(bnd0, i + di[d], n1), b = map_axis(bnd1, j + dj[d], n2);
+        if (a < 0 || b < 0) continue;
+        const int y = base[a + b * pitch];
+        acc[kEnsCounts + 3] += x * y;
+        acc[kEnsCounts + 4] += x + y;
+        acc[kEnsCounts + 5] += 1;
+    }
+}
+
+// The block's summary words, reduced into red[] (zeroed by the caller before a barrier).
+__device__ __forceinline__ void summary_reduce(const long long* acc, unsigned long long* red) {
+#pragma unroll
+    for (int k = 0; k < kEnsSumWords; ++k) {
+        long long v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&red[k], (unsigned long long)v);
+    }
+    __syncthreads();
+}
+
 // Integer summaries of a state (values 0..7 counted, Moran's I sums over VonNeumann(1)).
 __device__ __noinline__ void summarize(const EnsInstance& I, const int8_t* base, int64_t pitch, EnsSummary* out) {
     __shared__ unsigned long long red[kEnsSumWords];
@@ -293,37 +339,38 @@ __device__ __noinline__ void summarize(const EnsInstance& I, const int8_t* base,
 #pragma unroll
     for (int k = 0; k < kEnsSumWords; ++k) acc[k] = 0;
     const int64_t n = I.n1 * I.n2;
-    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
-        const int64_t i = q % I.n1, j = q / I.n1;
-        const int x = base[i + j * pitch];
-        if (x >= 0 && x < kEnsCounts) {
-#pragma unroll
-            for (int v = 0; v < kEnsCounts; ++v) acc[v] += (x == v);
-        } else {
-            acc[kEnsCounts] += 1;
-        }
-        acc[kEnsCounts + 1] += x;
-        acc[kEnsCounts + 2] += x * x;
-        const int di[4] = {0, -1, 1, 0}, dj[4] = {-1, 0, 0, 1};
-#pragma unroll
-        for (int d = 0; d < 4; ++d) {
-            const int64_t a = map_axis(I.bnd0, i + di[d], I.n1), b = map_axis(I.bnd1, j + dj[d], I.n2);
-            if (a < 0 || b < 0) continue;
-            const int y = base[a + b * pitch];
-            acc[kEnsCounts + 3] += x * y;
-            acc[kEnsCounts + 4] += x + y;
-            acc[kEnsCounts + 5] += 1;
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < kEnsSumWords; ++k) {
-        long long v = acc[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&red[k], (unsigned long long)v);
-    }
-    __syncthreads();
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x)
+        summary_cell(base, pitch, I.n1, I.n2, I.bnd0, I.bnd1, q % I.n1, q / I.n1, acc);
+    summary_reduce(acc, red);
     for (int k = threadIdx.x; k < kEnsSumWords; k += blockDim.x) out->w[k] = (long long)red[k];
+}
+
+// Summaries of the large instances after their batched passes: block b reduces output tile b
+// of the jobs' concatenated tile order (launch_fire_batch's tiles) of the final buffer and adds
+// its integers to the instance's summary words, zeroed earlier in the same graph. Integer sums
+// in any order: the same words as summarize() on one CTA.
+__global__ void __launch_bounds__(kEnsThreads) k_ens_measures(const FireJob* __restrict__ jobs,
+                                                              const int32_t* __restrict__ tile_job, int K,
+                                                              EnsSummary* __restrict__ out) {
+    __shared__ unsigned long long red[kEnsSumWords];
+    const FireJob& J = jobs[tile_job[blockIdx.x]];
+    const int64_t passes = J.nsteps > 0 ? (J.nsteps + K - 1) / K : 0;
+    const int8_t* base = J.buf[J.cur0 ^ (int)(passes & 1)];
+    const int64_t n1 = J.p.n1, n2 = J.p.n2, pitch = J.p.pitch;
+    const int local = (int)blockIdx.x - J.tile0;
+    const int64_t X0 = (int64_t)(local % J.tiles_x) * kFireTileCols, Y0 = (int64_t)(local / J.tiles_x) * kFireTileRows;
+    for (int k = threadIdx.x; k < kEnsSumWords; k += blockDim.x) red[k] = 0ull;
+    __syncthreads();
+    long long acc[kEnsSumWords];
+#pragma unroll
+    for (int k = 0; k < kEnsSumWords; ++k) acc[k] = 0;
+    for (int q = threadIdx.x; q < kFireTileCols * kFireTileRows; q += blockDim.x) {
+        const int64_t i = X0 + q % kFireTileCols, j = Y0 + q / kFireTileCols;
+        if (i < n1 && j < n2) summary_cell(base, pitch, n1, n2, J.p.bnd[0], J.p.bnd[1], i, j, acc);
+    }
+    summary_reduce(acc, red);
+    if (threadIdx.x < kEnsSumWords && red[threadIdx.x])
+        atomicAdd((unsigned long long*)&out[J.inst].w[threadIdx.x], red[threadIdx.x]);
 }
 
 template <int TILE>
@@ -437,6 +484,11 @@ bool ensemble_fits_smem(const gbca_desc& d, int tile) {
     return (d.n1 + 2 * d.radius) * (d.n2 + 2 * d.radius) <= buf;
 }
 
+bool ensemble_large_capable(const gbca_desc& d) {
+    return d.rule == GBCA_RULE_FOREST_FIRE && d.nbhd == GBCA_VON_NEUMANN && d.radius == 1 &&
+           d.scheme == GBCA_SYNCHRONOUS;
+}
+
 int ensemble_depth(const gbca_desc& d, int depth) {
     const int cap = kEnsMaxHalo / d.radius;  // the halo of a pass fits the tile's margin
     if (depth <= 0 || depth > cap) depth = cap;
@@ -466,6 +518,19 @@ struct gbca_ensemble {
     int tile = 128;   // the kernel's tile side (gbca_ensemble_set_geometry / gbca_ensemble_tune)
     int depth = 0;    // steps per pass of the tiled path; 0: the deepest the halo allows
     bool ran = false;
+    // large instances: batched multi-lattice fire passes on a forked stream of the same graph
+    int64_t large_cells = (int64_t)1 << 18;  // smallest large instance (cells); 0: none is large
+    int large_k = 1;                          // steps per batched pass
+    std::vector<int> big;                     // the large instances (create order)
+    std::vector<int> big_final;               // their buffer after the last run
+    std::vector<gbca::FireJob> h_jobs;
+    gbca::FireJob* d_jobs = nullptr;
+    int32_t* d_tile_job = nullptr;
+    int cap_jobs = 0, cap_tiles = 0;
+    int graph_kernels = 0;                    // kernel launches one replay of the graph makes
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    std::vector<int64_t> graph_sig;           // the shape the captured graph runs
 };
 
 namespace {
@@ -485,6 +550,93 @@ void apply_geometry(gbca_ensemble* e, int tile, int depth) {
         cudaGraphExecDestroy(e->exec);
         e->exec = nullptr;
     }
+}
+
+// Whether instance i runs as batched multi-CTA passes under the current settings.
+bool is_large(const gbca_ensemble* e, int32_t i) {
+    const gbca_desc& d = e->descs[(size_t)i];
+    const EnsInstance& I = e->h_inst[(size_t)i];
+    return e->large_cells > 0 && ensemble_large_capable(d) && I.n1 * I.n2 >= e->large_cells &&
+           I.n1 * I.n2 >= kEnsLargeFloor && I.pitch % 16 == 0;
+}
+
+// Captures one run: zero the work counter and the summaries; fork the batched passes of the
+// large instances (one launch per pass, then their summaries) onto the second stream while the
+// persistent kernel runs the others; join. Waits for the previous run first (its graph and job
+// table are replaced).
+cudaError_t capture_run(gbca_ensemble* e, const std::vector<int>& big, int ntiles, int n_small, int passes, int K) {
+    cudaError_t c = cudaStreamSynchronize(e->stream);
+    if (c != cudaSuccess) return c;
+    if (e->exec) {
+        cudaGraphExecDestroy(e->exec);
+        e->exec = nullptr;
+    }
+    if (!big.empty()) {
+        if (!e->aux) c = cudaStreamCreateWithFlags(&e->aux, cudaStreamNonBlocking);
+        if (c == cudaSuccess && !e->ev_fork) c = cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming);
+        if (c == cudaSuccess && !e->ev_join) c = cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming);
+        if (c == cudaSuccess && (size_t)e->cap_jobs < big.size()) {
+            cudaFree(e->d_jobs);
+            e->d_jobs = nullptr;
+            c = cudaMalloc(&e->d_jobs, sizeof(FireJob) * big.size());
+            e->cap_jobs = c == cudaSuccess ? (int)big.size() : 0;
+        }
+        if (c == cudaSuccess && e->cap_tiles < ntiles) {
+            cudaFree(e->d_tile_job);
+            e->d_tile_job = nullptr;
+            c = cudaMalloc(&e->d_tile_job, sizeof(int32_t) * ntiles);
+            e->cap_tiles = c == cudaSuccess ? ntiles : 0;
+        }
+        if (c == cudaSuccess) {  // block -> job map of the concatenated tile order
+            std::vector<int32_t> tj((size_t)ntiles);
+            for (size_t b = 0; b < big.size(); ++b) {
+                const FireJob& J = e->h_jobs[b];
+                const int end = b + 1 < big.size() ? e->h_jobs[b + 1].tile0 : ntiles;
+                for (int t = J.tile0; t < end; ++t) tj[(size_t)t] = (int32_t)b;
+            }
+            c = cudaMemcpy(e->d_tile_job, tj.data(), sizeof(int32_t) * ntiles, cudaMemcpyHostToDevice);
+        }
+        if (c != cudaSuccess) return c;
+    }
+    void (*fn)(const EnsInstance*, const int*, int, int*, int8_t*, EnsSummary*, int*) = nullptr;
+    size_t smem = 0;
+    c = ens_select(e->tile, &fn, &smem);  // sets the kernel's shared-memory limit before capture
+    if (c != cudaSuccess) return c;
+    cudaGraph_t g = nullptr;
+    c = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeRelaxed);
+    if (c != cudaSuccess) return c;
+    cudaError_t err = cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(e->d_out, 0, sizeof(EnsSummary) * e->n, e->stream);
+    if (err == cudaSuccess && !big.empty()) {
+        err = cudaEventRecord(e->ev_fork, e->stream);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(e->aux, e->ev_fork, 0);
+    }
+    int kernels = 0;
+    if (err == cudaSuccess && n_small > 0) {
+        fn<<<e->grid, kEnsThreads, smem, e->stream>>>(e->d_inst, e->d_order, n_small, e->d_counter, e->pool, e->d_out,
+                                                      e->d_cur);
+        err = cudaGetLastError();
+        ++kernels;
+    }
+    if (err == cudaSuccess && !big.empty()) {
+        for (int q = 0; q < passes && err == cudaSuccess; ++q, ++kernels)
+            err = launch_fire_batch(e->d_jobs, e->d_tile_job, ntiles, q, K, e->aux);
+        if (err == cudaSuccess) {
+            k_ens_measures<<<ntiles, kEnsThreads, 0, e->aux>>>(e->d_jobs, e->d_tile_job, K, e->d_out);
+            err = cudaGetLastError();
+            ++kernels;
+        }
+        // the join is recorded even after an error, so the capture ends with one stream
+        const cudaError_t j1 = cudaEventRecord(e->ev_join, e->aux);
+        const cudaError_t j2 = cudaStreamWaitEvent(e->stream, e->ev_join, 0);
+        if (err == cudaSuccess) err = j1 != cudaSuccess ? j1 : j2;
+    }
+    c = cudaStreamEndCapture(e->stream, &g);
+    if (err == cudaSuccess) err = c;
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&e->exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    e->graph_kernels = kernels;
+    return err;
 }
 
 }  // namespace
@@ -513,11 +665,12 @@ int gbca_ensemble_create(const gbca_desc* descs, int32_t n, gbca_ensemble** out)
         std::memset(&I, 0, sizeof I);
         I.n1 = d.n1;
         I.n2 = d.n2;
-        I.pitch = d.n1;
+        // instances that may run as batched multi-CTA passes get a 128-byte pitch
+        I.pitch = ensemble_large_capable(d) && d.n1 * d.n2 >= kEnsLargeFloor ? (d.n1 + 127) / 128 * 128 : d.n1;
         I.off[0] = (int64_t)off;
-        off += (size_t)(d.n1 * d.n2 + 255) / 256 * 256;
+        off += (size_t)(I.pitch * d.n2 + 255) / 256 * 256;
         I.off[1] = (int64_t)off;
-        off += (size_t)(d.n1 * d.n2 + 255) / 256 * 256;
+        off += (size_t)(I.pitch * d.n2 + 255) / 256 * 256;
         I.rule = d.rule;
         I.nbhd = d.nbhd;
         I.radius = d.radius;
@@ -576,6 +729,11 @@ int gbca_ensemble_destroy(gbca_ensemble* e) {
     cudaFree(e->d_out);
     if (e->h_out) cudaFreeHost(e->h_out);
     if (e->h_cur) cudaFreeHost(e->h_cur);
+    cudaFree(e->d_jobs);
+    cudaFree(e->d_tile_job);
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
+    if (e->aux) cudaStreamDestroy(e->aux);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
     return GBCA_OK;
@@ -587,7 +745,8 @@ int gbca_ensemble_set_state(gbca_ensemble* e, int32_t i, const void* host, size_
     if (nbytes != (size_t)(I.n1 * I.n2))
         return efail(GBCA_ERR_STATE, "instance %d has %lld cells, the state %zu bytes", i, (long long)(I.n1 * I.n2),
                      nbytes);
-    cudaError_t c = cudaMemcpyAsync(e->pool + I.off[I.cur], host, nbytes, cudaMemcpyHostToDevice, e->stream);
+    cudaError_t c = cudaMemcpy2DAsync(e->pool + I.off[I.cur], (size_t)I.pitch, host, (size_t)I.n1, (size_t)I.n1,
+                                      (size_t)I.n2, cudaMemcpyHostToDevice, e->stream);
     if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
     if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble set_state: %s", cudaGetErrorString(c));
     return GBCA_OK;
@@ -618,33 +777,68 @@ int gbca_ensemble_run(gbca_ensemble* e, const int64_t* t0, const int64_t* nsteps
         }
         work[(size_t)i] = I.n1 * I.n2 * (I.nsteps > 0 ? I.nsteps : 0);
     }
-    std::vector<int> order((size_t)e->n);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[(size_t)a] > work[(size_t)b]; });
-    cudaError_t c = cudaMemcpyAsync(e->d_inst, e->h_inst.data(), sizeof(EnsInstance) * e->n, cudaMemcpyHostToDevice,
-                                    e->stream);
-    if (c == cudaSuccess)
-        c = cudaMemcpyAsync(e->d_order, order.data(), sizeof(int) * e->n, cudaMemcpyHostToDevice, e->stream);
-    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble upload: %s", cudaGetErrorString(c));
-    if (!e->exec) {  // capture the run once: reset the work counter, one persistent launch
-        cudaGraph_t g = nullptr;
-        void (*fn)(const EnsInstance*, const int*, int, int*, int8_t*, EnsSummary*, int*) = nullptr;
-        size_t smem = 0;
-        c = ens_select(e->tile, &fn, &smem);  // sets the kernel's shared-memory limit before capture
-        if (c == cudaSuccess) c = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
-        if (c == cudaSuccess) {
-            cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream);
-            fn<<<e->grid, kEnsThreads, smem, e->stream>>>(e->d_inst, e->d_order, e->n, e->d_counter, e->pool,
-                                                          e->d_out, e->d_cur);
-            c = cudaStreamEndCapture(e->stream, &g);
+    // the large instances run as batched passes of K steps; the rest on the persistent kernel
+    const int K = e->large_k;
+    std::vector<int> big, order;
+    int64_t passes = 0;
+    for (int32_t i = 0; i < e->n; ++i) {
+        if (is_large(e, i)) {
+            big.push_back(i);
+            const int64_t q = (e->h_inst[(size_t)i].nsteps + K - 1) / K;
+            if (q > passes) passes = q;
+        } else {
+            order.push_back(i);
         }
-        if (c == cudaSuccess) c = cudaGraphInstantiate(&e->exec, g, 0);
-        if (g) cudaGraphDestroy(g);
-        if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble graph capture: %s", cudaGetErrorString(c));
     }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[(size_t)a] > work[(size_t)b]; });
+    const int n_small = (int)order.size();
+    // this run's jobs: the structure follows the large set, the rest the run's arguments
+    e->h_jobs.resize(big.size());
+    e->big_final.resize(big.size());
+    int ntiles = 0;
+    for (size_t b = 0; b < big.size(); ++b) {
+        const int i = big[b];
+        const EnsInstance& I = e->h_inst[(size_t)i];
+        FireJob& J = e->h_jobs[b];
+        std::memset(&J, 0, sizeof J);
+        J.p = sweep_params(e->descs[(size_t)i], I.pitch, nullptr);
+        J.p.thr_p = I.thr_p;
+        J.p.thr_f = I.thr_f;
+        J.p.keys = philox_keys(I.seed);
+        J.p.t0 = I.t0;
+        J.buf[0] = e->pool + I.off[0];
+        J.buf[1] = e->pool + I.off[1];
+        J.nsteps = I.nsteps;
+        J.cur0 = I.cur;
+        J.tiles_x = (int32_t)((I.n1 + kFireTileCols - 1) / kFireTileCols);
+        J.tile0 = ntiles;
+        J.inst = i;
+        ntiles += J.tiles_x * (int32_t)((I.n2 + kFireTileRows - 1) / kFireTileRows);
+        e->big_final[b] = I.cur ^ (int)(((I.nsteps + K - 1) / K) & 1);
+    }
+    std::vector<int64_t> sig = {e->tile, e->grid, K, n_small, passes, (int64_t)big.size()};
+    sig.insert(sig.end(), big.begin(), big.end());
+    cudaError_t c = cudaSuccess;
+    if (!e->exec || sig != e->graph_sig) {
+        c = capture_run(e, big, ntiles, n_small, (int)passes, K);
+        if (c != cudaSuccess) {
+            e->graph_sig.clear();
+            cudaGetLastError();
+            return efail(GBCA_ERR_CUDA, "ensemble graph capture: %s", cudaGetErrorString(c));
+        }
+        e->graph_sig = sig;
+    }
+    e->big = big;
+    c = cudaMemcpyAsync(e->d_inst, e->h_inst.data(), sizeof(EnsInstance) * e->n, cudaMemcpyHostToDevice, e->stream);
+    if (c == cudaSuccess && n_small > 0)
+        c = cudaMemcpyAsync(e->d_order, order.data(), sizeof(int) * n_small, cudaMemcpyHostToDevice, e->stream);
+    if (c == cudaSuccess && !big.empty())
+        c = cudaMemcpyAsync(e->d_jobs, e->h_jobs.data(), sizeof(FireJob) * big.size(), cudaMemcpyHostToDevice,
+                            e->stream);
+    if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble upload: %s", cudaGetErrorString(c));
     c = cudaGraphLaunch(e->exec, e->stream);
     if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble launch: %s", cudaGetErrorString(c));
-    count_launch();
+    count_launch(e->graph_kernels);
     // results come back with the summaries; the buffer holding each final state too
     c = cudaMemcpyAsync(e->h_cur, e->d_cur, sizeof(int) * e->n, cudaMemcpyDeviceToHost, e->stream);
     if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble result copy: %s", cudaGetErrorString(c));
@@ -657,7 +851,13 @@ int gbca_ensemble_sync(gbca_ensemble* e) {
     cudaError_t c = cudaStreamSynchronize(e->stream);
     if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble sync: %s", cudaGetErrorString(c));
     if (e->ran) {
-        for (int32_t i = 0; i < e->n; ++i) e->h_inst[(size_t)i].cur = e->h_cur[i];
+        std::vector<uint8_t> is_big((size_t)e->n, 0);
+        for (size_t b = 0; b < e->big.size(); ++b) {
+            e->h_inst[(size_t)e->big[b]].cur = e->big_final[b];
+            is_big[(size_t)e->big[b]] = 1;
+        }
+        for (int32_t i = 0; i < e->n; ++i)
+            if (!is_big[(size_t)i]) e->h_inst[(size_t)i].cur = e->h_cur[i];
         e->ran = false;
     }
     return GBCA_OK;
@@ -698,6 +898,35 @@ int gbca_ensemble_set_geometry(gbca_ensemble* e, int32_t tile, int32_t depth) {
     return GBCA_OK;
 }
 
+int gbca_ensemble_set_large(gbca_ensemble* e, int64_t min_cells, int32_t steps_per_pass) {
+    if (!e) return efail(GBCA_ERR_ARGUMENT, "null ensemble");
+    if (min_cells != 0 && min_cells < kEnsLargeFloor)
+        return efail(GBCA_ERR_ARGUMENT, "min_cells is 0 (none) or at least %lld, got %lld", (long long)kEnsLargeFloor,
+                     (long long)min_cells);
+    if (steps_per_pass < 1 || steps_per_pass > 16)
+        return efail(GBCA_ERR_ARGUMENT, "steps_per_pass must lie in 1:16, got %d", steps_per_pass);
+    int rc = gbca_ensemble_sync(e);
+    if (rc != GBCA_OK) return rc;
+    e->large_cells = min_cells;
+    e->large_k = steps_per_pass;
+    return GBCA_OK;
+}
+
+int gbca_ensemble_geometry(gbca_ensemble* e, int32_t* tile, int32_t* depth, int64_t* large_cells,
+                           int32_t* large_steps, int32_t* n_large) {
+    if (!e) return efail(GBCA_ERR_ARGUMENT, "null ensemble");
+    if (tile) *tile = e->tile;
+    if (depth) *depth = e->depth;
+    if (large_cells) *large_cells = e->large_cells;
+    if (large_steps) *large_steps = e->large_k;
+    if (n_large) {
+        int32_t k = 0;
+        for (int32_t i = 0; i < e->n; ++i) k += is_large(e, i) ? 1 : 0;
+        *n_large = k;
+    }
+    return GBCA_OK;
+}
+
 int gbca_ensemble_tune(gbca_ensemble* e, int64_t probe_steps, const double* params, int32_t nparams, int32_t* tile,
                        int32_t* depth) {
     if (!e) return efail(GBCA_ERR_ARGUMENT, "null ensemble");
@@ -714,32 +943,71 @@ int gbca_ensemble_tune(gbca_ensemble* e, int64_t probe_steps, const double* para
     if (c == cudaSuccess) c = cudaEventCreate(&ev[0]);
     if (c == cudaSuccess) c = cudaEventCreate(&ev[1]);
     const std::vector<int64_t> steps((size_t)e->n, probe_steps);
+    struct Cand {
+        int tile, depth;
+        int64_t large_cells;
+        int large_k;
+    };
+    // one candidate: restore the states, time the fastest of two probe runs
+    auto probe = [&](const Cand& k, float* ms_min) {
+        apply_geometry(e, k.tile, k.depth);
+        e->large_cells = k.large_cells;
+        e->large_k = k.large_k;
+        *ms_min = -1.0f;
+        for (int rep = 0; rep < 2 && c == cudaSuccess && rc == GBCA_OK; ++rep) {
+            for (int32_t i = 0; i < e->n; ++i) e->h_inst[(size_t)i].cur = cur0[(size_t)i];
+            c = cudaMemcpyAsync(e->pool, saved, e->pool_bytes, cudaMemcpyDeviceToDevice, e->stream);
+            if (c == cudaSuccess) c = cudaEventRecord(ev[0], e->stream);
+            if (c != cudaSuccess) break;
+            rc = gbca_ensemble_run(e, nullptr, steps.data(), params, nparams);
+            if (rc != GBCA_OK) break;
+            c = cudaEventRecord(ev[1], e->stream);
+            if (c == cudaSuccess) rc = gbca_ensemble_sync(e);
+            float ms = 0.0f;
+            if (c == cudaSuccess && rc == GBCA_OK) c = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            if (*ms_min < 0.0f || ms < *ms_min) *ms_min = ms;
+        }
+        return c == cudaSuccess && rc == GBCA_OK;
+    };
+    // first the persistent kernel's tile and depth (large instances at the current split), then
+    // the split: which instances run as batched passes, and the passes' depth
     const int tiles[3] = {64, 128, 192}, depths[3] = {2, 4, 0};
     float best = -1.0f;
-    int best_tile = e->tile, best_depth = e->depth;
-    for (int a = 0; a < 3 && c == cudaSuccess && rc == GBCA_OK; ++a)
-        for (int b = 0; b < 3 && c == cudaSuccess && rc == GBCA_OK; ++b) {
-            apply_geometry(e, tiles[a], depths[b]);
-            float ms_min = -1.0f;
-            for (int rep = 0; rep < 2 && c == cudaSuccess && rc == GBCA_OK; ++rep) {
-                for (int32_t i = 0; i < e->n; ++i) e->h_inst[(size_t)i].cur = cur0[(size_t)i];
-                c = cudaMemcpyAsync(e->pool, saved, e->pool_bytes, cudaMemcpyDeviceToDevice, e->stream);
-                if (c == cudaSuccess) c = cudaEventRecord(ev[0], e->stream);
-                if (c != cudaSuccess) break;
-                rc = gbca_ensemble_run(e, nullptr, steps.data(), params, nparams);
-                if (rc != GBCA_OK) break;
-                c = cudaEventRecord(ev[1], e->stream);
-                if (c == cudaSuccess) rc = gbca_ensemble_sync(e);
-                float ms = 0.0f;
-                if (c == cudaSuccess && rc == GBCA_OK) c = cudaEventElapsedTime(&ms, ev[0], ev[1]);
-                if (ms_min < 0.0f || ms < ms_min) ms_min = ms;
-            }
-            if (c == cudaSuccess && rc == GBCA_OK && (best < 0.0f || ms_min < best)) {
-                best = ms_min;
-                best_tile = tiles[a];
-                best_depth = depths[b];
+    Cand win = {e->tile, e->depth, e->large_cells, e->large_k};
+    const int64_t cells0 = e->large_cells;
+    const int k0 = e->large_k;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            const Cand k = {tiles[a], depths[b], cells0, k0};
+            float ms = 0.0f;
+            if (!probe(k, &ms)) break;
+            if (best < 0.0f || ms < best) {
+                best = ms;
+                win = k;
             }
         }
+    bool capable = false;
+    for (int32_t i = 0; i < e->n; ++i)
+        capable = capable || (ensemble_large_capable(e->descs[(size_t)i]) &&
+                              e->h_inst[(size_t)i].n1 * e->h_inst[(size_t)i].n2 >= kEnsLargeFloor);
+    if (capable && c == cudaSuccess && rc == GBCA_OK) {
+        const int64_t splits[5] = {(int64_t)1 << 16, (int64_t)1 << 17, (int64_t)1 << 18, (int64_t)1 << 20, 0};
+        const int ks[3] = {1, 2, 4};
+        for (int a = 0; a < 5; ++a)
+            for (int b = 0; b < 3; ++b) {
+                if (splits[a] == 0 && b > 0) break;  // nothing runs as batched passes
+                const Cand k = {win.tile, win.depth, splits[a], ks[b]};
+                float ms = 0.0f;
+                if (!probe(k, &ms)) break;
+                if (ms < best) {
+                    best = ms;
+                    win = k;
+                }
+            }
+    }
+    e->large_cells = win.large_cells;
+    e->large_k = win.large_k;
+    const int best_tile = win.tile, best_depth = win.depth;
     for (int32_t i = 0; i < e->n; ++i) e->h_inst[(size_t)i].cur = cur0[(size_t)i];
     if (saved) {
         const cudaError_t c2 = cudaMemcpyAsync(e->pool, saved, e->pool_bytes, cudaMemcpyDeviceToDevice, e->stream);
@@ -771,7 +1039,8 @@ int gbca_ensemble_get_state(gbca_ensemble* e, int32_t i, void* host, size_t nbyt
     if (nbytes != (size_t)(I.n1 * I.n2))
         return efail(GBCA_ERR_STATE, "instance %d has %lld cells, the buffer %zu bytes", i, (long long)(I.n1 * I.n2),
                      nbytes);
-    cudaError_t c = cudaMemcpyAsync(host, e->pool + I.off[I.cur], nbytes, cudaMemcpyDeviceToHost, e->stream);
+    cudaError_t c = cudaMemcpy2DAsync(host, (size_t)I.n1, e->pool + I.off[I.cur], (size_t)I.pitch, (size_t)I.n1,
+                                      (size_t)I.n2, cudaMemcpyDeviceToHost, e->stream);
     if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
     if (c != cudaSuccess) return efail(GBCA_ERR_CUDA, "ensemble get_state: %s", cudaGetErrorString(c));
     return GBCA_OK;

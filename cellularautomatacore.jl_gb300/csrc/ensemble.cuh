@@ -43,5 +43,10 @@ int ensemble_smem_cells(int tile = 128);
 bool ensemble_fits_smem(const gbca_desc& d, int tile = 128);
 // Steps per pass of the tiled path for a requested depth (0: the deepest the halo allows).
 int ensemble_depth(const gbca_desc& d, int depth);
+// Whether an instance's rule has the batched multi-CTA pass (launch_fire_batch); such an
+// instance of at least the ensemble's large-cell threshold runs there instead of on one CTA of
+// the persistent kernel. Instances below kEnsLargeFloor cells never do.
+bool ensemble_large_capable(const gbca_desc& d);
+constexpr int64_t kEnsLargeFloor = (int64_t)1 << 14;
 
 }  // namespace gbca

@@ -246,6 +246,26 @@ int life_steps_per_pass(const SweepParams& p);
 bool life_choice_fits(const SweepParams& p, int steps, int rows);
 bool fire_fast_supported(const SweepParams& p);
 cudaError_t launch_fire(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
+
+// The forest-fire kernel's output tile (cells along axis 1 x axis 2).
+constexpr int kFireTileCols = 256, kFireTileRows = 128;
+
+// One lattice of a batched forest-fire sweep (many lattices per launch, one pass each).
+struct FireJob {
+    SweepParams p;       // its sweep: t0 = time of its first step; keys and thresholds set
+    int8_t* buf[2];      // its two state buffers (pitch p.pitch, 16-byte aligned)
+    int64_t nsteps;      // steps of this run
+    int32_t cur0;        // buffer holding the state before the first pass
+    int32_t tiles_x;     // output tiles along axis 1
+    int32_t tile0;       // its first tile in the launch's tile order
+    int32_t inst;        // the caller's index of the lattice
+};
+// Pass `pass` (steps pass*K .. pass*K + K - 1 of every job, fewer where a job ends) over all
+// jobs' tiles: block b runs tile b of the concatenated order, tile_job[b] naming its job.
+// Jobs whose steps are all done leave their blocks idle. 1 <= K <= 16. Not counted in
+// gbca_kernel_launches (the batched ensemble counts its graph's kernels per replay).
+cudaError_t launch_fire_batch(const FireJob* jobs, const int32_t* tile_job, int ntiles, int pass, int K,
+                              cudaStream_t st);
 // Tiles whose TMA copy did not complete within its wait limit since the last call (cleared).
 int fire_tma_timeouts_take();
 // One bounded wait (`polls` polls) on a barrier nothing completes: exercises the timeout path.

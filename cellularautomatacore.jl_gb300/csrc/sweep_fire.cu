@@ -37,7 +37,7 @@ __device__ int g_fire_tma_timeouts = 0;
 
 namespace {
 
-constexpr int kFireTX = 256, kFireTY = 128;
+constexpr int kFireTX = kFireTileCols, kFireTY = kFireTileRows;
 constexpr int kFireThreadsX = 32, kFireThreadsY = 16;
 constexpr int kTmaSpins = 1 << 22;  // try_wait polls before a tile gives up
 
@@ -86,15 +86,65 @@ __device__ __forceinline__ void tma_tile_load(const CUtensorMap* map, void* dst,
         : "memory");
 }
 
+// The halo-padded region of a tile that reaches past the lattice's edges: sx x sy bytes from
+// lattice (X0 - hx, Y0 - hy) through the boundary map (a row beyond a Constant edge of axis 2
+// holds its constant; else a cell beyond a Constant edge of axis 1 holds that constant). First
+// by 16-byte segments (X0 - hx, sx and the pitch are multiples of 16): a segment inside the
+// lattice's columns is one vector load, a row or segment wholly beyond a Constant edge one
+// vector fill. The remaining columns — a segment straddling column n1, or beyond a Periodic or
+// Reflecting edge — then map byte by byte, one byte per thread, so no warp waits on a few
+// lanes' byte loops.
+__device__ __forceinline__ void load_region_mapped(const SweepParams& p, const int8_t* __restrict__ src, int8_t* A,
+                                                   int64_t X0, int64_t Y0, int hx, int hy, int sx, int sy, int tid,
+                                                   int nthr) {
+    const int qx = sx / 16;
+    const int64_t gx0 = X0 - hx;
+    const bool cst0 = p.bnd[0] == GBCA_CONSTANT;
+    const uint32_t c0 = (uint32_t)(uint8_t)p.cval[0] * 0x01010101u, c1 = (uint32_t)(uint8_t)p.cval[1] * 0x01010101u;
+    for (int q = tid; q < qx * sy; q += nthr) {
+        const int lq = q % qx, ly = q / qx;
+        const int64_t gx = gx0 + 16 * lq;
+        const int64_t my = map_axis(p.bnd[1], Y0 - hy + ly, p.n2);
+        int4* out = (int4*)(A + ly * sx + 16 * lq);
+        if (my < 0) {
+            *out = make_int4((int)c1, (int)c1, (int)c1, (int)c1);
+        } else if (gx >= 0 && gx + 16 <= p.n1) {
+            *out = *(const int4*)(src + gx + my * p.pitch);
+        } else if (cst0 && (gx + 16 <= 0 || gx >= p.n1)) {
+            *out = make_int4((int)c0, (int)c0, (int)c0, (int)c0);
+        }
+    }
+    // the byte-mapped columns: [0, nl) before the lattice (beyond a Periodic or Reflecting
+    // edge), and [r0, r1) from the first segment not wholly inside it: with a Constant axis 1
+    // the straddling segment only (the ones beyond were filled above), else every column on
+    const int nl = (!cst0 && gx0 < 0) ? (int)(-gx0 < (int64_t)sx ? -gx0 : (int64_t)sx) : 0;
+    const int64_t a = p.n1 - gx0;  // region columns from its left edge to column n1 (> 0)
+    int r0 = sx, r1 = sx;
+    if (a < sx) {
+        r0 = (int)(a / 16 * 16);
+        r1 = cst0 ? (a % 16 ? r0 + 16 : r0) : sx;
+    }
+    const int ncols = nl + (r1 - r0);
+    if (ncols == 0) return;
+    for (int idx = tid; idx < ncols * sy; idx += nthr) {
+        const int k = idx % ncols, ly = idx / ncols;
+        const int lx = k < nl ? k : r0 + (k - nl);
+        const int64_t my = map_axis(p.bnd[1], Y0 - hy + ly, p.n2);
+        if (my < 0) continue;  // the row's constant is already in place
+        const int64_t mx = map_axis(p.bnd[0], gx0 + lx, p.n1);
+        A[ly * sx + lx] = mx < 0 ? (int8_t)p.cval[0] : src[mx + my * p.pitch];
+    }
+}
+
 // Four cells (one 32-bit word of the shared tile) per work item: neighbour tests in byte
 // SIMD, then four independent Philox chains.
 template <bool INTERIOR>
 __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __restrict__ src,
-                                          int8_t* __restrict__ dst, int8_t* A, int8_t* B, bool staged) {
+                                          int8_t* __restrict__ dst, int8_t* A, int8_t* B, bool staged,
+                                          int64_t X0, int64_t Y0) {
     const int hx = p.halo_x, hy = p.halo_y;
     const int sx = kFireTX + 2 * hx, sy = kFireTY + 2 * hy;
     const int sw = sx / 4;  // words per shared row
-    const int64_t X0 = (int64_t)blockIdx.x * kFireTX, Y0 = (int64_t)blockIdx.y * kFireTY;
     const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
     const int nthr = kFireThreadsX * kFireThreadsY;
 
@@ -107,11 +157,7 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
             *(int4*)(A + ly * sx + 16 * lq) = v;
         }
     } else {
-        for (int idx = tid; idx < sx * sy; idx += nthr) {
-            const int lx = idx % sx, ly = idx / sx;
-            const int64_t mx = map_axis(p.bnd[0], X0 - hx + lx, p.n1), my = map_axis(p.bnd[1], Y0 - hy + ly, p.n2);
-            A[idx] = my < 0 ? (int8_t)p.cval[1] : (mx < 0 ? (int8_t)p.cval[0] : src[mx + my * p.pitch]);
-        }
+        load_region_mapped(p, src, A, X0, Y0, hx, hy, sx, sy, tid, nthr);
     }
     __syncthreads();
 
@@ -131,10 +177,15 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
         const bool exact = s == 0 && !p.states_valid;
         if (p.nsub == 1) {
             // one step: the region is the tile itself (64 words, all 512 threads busy walking
-            // rows), stored straight to the lattice state
-            fire_substep_rows<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
-                                         kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr, exact, dst,
-                                         p.pitch);
+            // rows), stored straight to the lattice state; a ragged last tile spreads the
+            // threads over the words and rows inside the lattice only
+            int nw = kFireTX / 4, nrows = kFireTY;
+            if (!INTERIOR) {
+                if (p.n1 - X0 < kFireTX) nw = (int)((p.n1 - X0 + 3) / 4);
+                if (p.n2 - Y0 < kFireTY) nrows = (int)(p.n2 - Y0);
+            }
+            fire_substep_rows<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, hx >> 2, nw, hy, nrows, X0 - hx,
+                                         Y0 - hy, g, ds, p.keys, tid, nthr, exact, dst, p.pitch);
             return;
         }
         // deeper passes: the region is wider than the tile in early sub-steps, so the flat
@@ -194,8 +245,47 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
             return;
         }
     }
-    if (interior) fire_tile<true>(p, src, dst, A, B, staged);
-    else fire_tile<false>(p, src, dst, A, B, staged);
+    if (interior) fire_tile<true>(p, src, dst, A, B, staged, X0, Y0);
+    else fire_tile<false>(p, src, dst, A, B, staged, X0, Y0);
+}
+
+// Many lattices per launch (a batched ensemble's large instances): one pass of up to K steps
+// over every tile of every job, block b running tile b of the concatenated tile order. Pass q
+// of a job reads buffer cur0 ^ (q & 1) and writes the other, so a job's passes ping-pong as a
+// single lattice's do; a job with no steps left at pass q leaves its blocks idle. Tiles load
+// with 16-byte vector loads inside the lattice and through the boundary map at its edges.
+__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY, 2)
+    k_fire_batch(const FireJob* __restrict__ jobs, const int32_t* __restrict__ tile_job, int pass, int K) {
+    extern __shared__ __align__(128) int8_t smem_f[];
+    __shared__ SweepParams sp;
+    const FireJob& J = jobs[tile_job[blockIdx.x]];
+    const int64_t done = (int64_t)pass * K;
+    if (done >= J.nsteps) return;  // the whole block: the job ended in an earlier pass
+    const int nsub = (int)(J.nsteps - done < K ? J.nsteps - done : K);
+    const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
+    for (int k = tid; k < (int)(sizeof(SweepParams) / 4); k += kFireThreadsX * kFireThreadsY)
+        ((uint32_t*)&sp)[k] = ((const uint32_t*)&J.p)[k];
+    __syncthreads();
+    if (tid == 0) {
+        sp.nsub = nsub;
+        sp.t0 = J.p.t0 + done;
+        sp.halo_y = nsub;
+        sp.halo_x = (nsub + 15) / 16 * 16;
+        if (pass > 0) sp.states_valid = 1;  // a pass leaves only 0, 1 and 2
+    }
+    __syncthreads();
+    const int local = (int)blockIdx.x - J.tile0;
+    const int64_t X0 = (int64_t)(local % J.tiles_x) * kFireTX, Y0 = (int64_t)(local / J.tiles_x) * kFireTY;
+    const int c = J.cur0 ^ (pass & 1);
+    const int8_t* src = J.buf[c];
+    int8_t* dst = J.buf[c ^ 1];
+    const int sx = kFireTX + 2 * sp.halo_x, sy = kFireTY + 2 * sp.halo_y;
+    int8_t* A = smem_f;
+    int8_t* B = smem_f + sx * sy;
+    const bool interior = X0 - sp.halo_x >= 0 && X0 + kFireTX + sp.halo_x <= sp.n1 && Y0 - sp.halo_y >= 0 &&
+                          Y0 + kFireTY + sp.halo_y <= sp.n2;
+    if (interior) fire_tile<true>(sp, src, dst, A, B, false, X0, Y0);
+    else fire_tile<false>(sp, src, dst, A, B, false, X0, Y0);
 }
 
 // One step per pass with TMA staging, persistent: each CTA walks the tiles blockIdx.x,
@@ -280,21 +370,19 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
                 break;
             }
         } else {  // beyond an edge TMA cannot reproduce: the boundary map
-            int8_t* A = cur;
-            for (int idx = tid; idx < sx * sy; idx += nthr) {
-                const int lx = idx % sx, ly = idx / sx;
-                const int64_t mx = map_axis(p.bnd[0], X0 - hx + lx, p.n1), my = map_axis(p.bnd[1], Y0 - hy + ly, p.n2);
-                A[idx] = my < 0 ? (int8_t)p.cval[1] : (mx < 0 ? (int8_t)p.cval[0] : src[mx + my * p.pitch]);
-            }
+            load_region_mapped(p, src, cur, X0, Y0, hx, hy, sx, sy, tid, nthr);
             __syncthreads();
         }
         const uint32_t* A = (const uint32_t*)cur;
-        if (interior)
+        if (interior) {
             fire_substep_rows<false>(A, nullptr, sw, hx >> 2, kFireTX / 4, hy, kFireTY, X0 - hx, Y0 - hy, g, ds,
                                      p.keys, tid, nthr, !p.states_valid, dst, p.pitch);
-        else
-            fire_substep_rows<true>(A, nullptr, sw, hx >> 2, kFireTX / 4, hy, kFireTY, X0 - hx, Y0 - hy, g, ds,
-                                    p.keys, tid, nthr, !p.states_valid, dst, p.pitch);
+        } else {  // a ragged last tile: the words and rows inside the lattice only
+            const int nw = p.n1 - X0 < kFireTX ? (int)((p.n1 - X0 + 3) / 4) : kFireTX / 4;
+            const int nrows = p.n2 - Y0 < kFireTY ? (int)(p.n2 - Y0) : kFireTY;
+            fire_substep_rows<true>(A, nullptr, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds, p.keys, tid,
+                                    nthr, !p.states_valid, dst, p.pitch);
+        }
         __syncthreads();
     }
     if (failed) {
@@ -380,6 +468,17 @@ int fire_tma_timeouts_take() {
         cudaMemcpyToSymbol(g_fire_tma_timeouts, &zero, sizeof zero);
     }
     return n;
+}
+
+cudaError_t launch_fire_batch(const FireJob* jobs, const int32_t* tile_job, int ntiles, int pass, int K,
+                              cudaStream_t st) {
+    if (K < 1 || K > 16 || ntiles < 1) return cudaErrorInvalidValue;
+    const int hx = (K + 15) / 16 * 16;
+    const size_t smem = 2 * (size_t)(kFireTX + 2 * hx) * (size_t)(kFireTY + 2 * K);
+    cudaError_t e = cudaFuncSetAttribute(k_fire_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_fire_batch<<<ntiles, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(jobs, tile_job, pass, K);
+    return cudaGetLastError();
 }
 
 bool fire_fast_supported(const SweepParams& p) {

@@ -76,6 +76,17 @@ class BatchedEnsemble:
         """The batched kernel's tile side (64, 128, 192) and steps per pass (0: deepest)."""
         capi.check(capi.lib().gbca_ensemble_set_geometry(self.handle, int(tile), int(depth)))
 
+    def set_large(self, min_cells: int = 1 << 18, steps_per_pass: int = 1):
+        """Forest-fire instances of at least min_cells cells (0: none) run as batched multi-CTA
+        passes of steps_per_pass steps instead of on one CTA of the persistent kernel."""
+        capi.check(capi.lib().gbca_ensemble_set_large(self.handle, int(min_cells), int(steps_per_pass)))
+
+    def geometry(self):
+        """dict(tile, depth, large_cells, large_steps, n_large) of the next run."""
+        v = [ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()]
+        capi.check(capi.lib().gbca_ensemble_geometry(self.handle, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("tile", "depth", "large_cells", "large_steps", "n_large"), (int(x.value) for x in v)))
+
     def tune(self, probe_steps: int = 16, params=None):
         """Times every (tile, depth) on this ensemble's instances for probe_steps steps from
         their current states (restored afterwards), keeps the fastest; returns it."""

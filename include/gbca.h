@@ -282,11 +282,26 @@ int gbca_ensemble_get_state(gbca_ensemble* e, int32_t i, void* host, size_t nbyt
  * reference. */
 int gbca_ensemble_set_geometry(gbca_ensemble* e, int32_t tile, int32_t depth);
 
+/* Which instances leave the persistent kernel: forest-fire instances (VonNeumann(1)) of at
+ * least min_cells cells (0 = none; else at least 2^14) run as batched multi-CTA passes — every
+ * tile of every such instance in one launch, steps_per_pass (1..16) steps per launch — on a
+ * second stream of the same graph, and their summaries by a batched reduction. Default 2^18
+ * cells, 1 step per pass. Results never depend on it. No counterpart in the reference. */
+int gbca_ensemble_set_large(gbca_ensemble* e, int64_t min_cells, int32_t steps_per_pass);
+
+/* The geometry the next run uses (any pointer may be NULL); n_large = instances that run as
+ * batched passes. */
+int gbca_ensemble_geometry(gbca_ensemble* e, int32_t* tile, int32_t* depth, int64_t* large_cells,
+                           int32_t* large_steps, int32_t* n_large);
+
 /* The autotuner for the batched path: times every (tile, depth) candidate on the ensemble's
  * own instances for `probe_steps` steps each from their current states (restored after every
- * candidate and at the end; params as in gbca_ensemble_run), keeps the fastest and returns it.
- * It allocates one copy of the ensemble's state pool while it runs; summaries are those of the
- * last probe until the next gbca_ensemble_run. No counterpart in the reference. */
+ * candidate and at the end; params as in gbca_ensemble_run), keeps the fastest, then times the
+ * large-instance split (min_cells 2^16, 2^17, 2^18, 2^20 or none x 1, 2 or 4 steps per pass)
+ * where an instance could take it, and keeps the fastest of all; returns tile and depth
+ * (gbca_ensemble_geometry gives the rest). It allocates one copy of the ensemble's state pool
+ * while it runs; summaries are those of the last probe until the next gbca_ensemble_run. No
+ * counterpart in the reference. */
 int gbca_ensemble_tune(gbca_ensemble* e, int64_t probe_steps, const double* params, int32_t nparams, int32_t* tile,
                        int32_t* depth);
 

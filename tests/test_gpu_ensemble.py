@@ -169,3 +169,69 @@ def test_batched_geometries_and_tuner(ca):
     ens.close()
     with pytest.raises(ca.ArgumentError):
         ca.BatchedEnsemble(probs).set_geometry(100, 0)
+
+
+def large_split_problems(ca):
+    """Forest fires on both sides of the 2^14-cell floor, ragged sides (not multiples of the
+    256 x 128 output tile), every boundary kind the fire kernel maps, and a Life instance that
+    always stays on the persistent kernel."""
+    rng = np.random.default_rng(2024)
+    shapes = [(130, 140), (300, 257), (1000, 20), (513, 129), (64, 300), (40, 50), (260, 600), (129, 127)]
+    spaces = [lambda a, b: ca.Grid(a, b), lambda a, b: ca.Torus(a, b),
+              lambda a, b: ca.Lattice((a, b), (ca.Reflecting(), ca.Constant(1))),
+              lambda a, b: ca.Lattice((a, b), (ca.Constant(2), ca.Periodic()))]
+    probs = []
+    for i, (a, b) in enumerate(shapes):
+        u0 = rng.integers(0, 3, (a, b)).astype(np.int8)
+        p = {"p": float(rng.uniform(0.02, 0.2)), "f": float(rng.uniform(1e-4, 1e-2))}
+        probs.append(ca.CAProblem.new(ca.ForestFire(), u0, 20, p, space=spaces[i % 4](a, b), seed=300 + i))
+    probs.append(ca.CAProblem.new(ca.Life("B3/S23"), rng.integers(0, 2, (200, 180)).astype(np.int8), 20,
+                                  space=ca.Torus(200, 180), seed=9))
+    return probs
+
+
+@pytest.mark.parametrize("k", [1, 3, 16])
+def test_large_instances_as_batched_passes(ca, k):
+    """Instances of at least 2^14 cells run as batched multi-CTA passes of k steps: states and
+    summaries equal one solve per instance, over two runs with step counts that are not
+    multiples of k (0 included), from t0 != 0."""
+    probs = large_split_problems(ca)
+    ens = ca.BatchedEnsemble(probs)
+    ens.set_initial_states()
+    ens.set_large(1 << 14, k)
+    g = ens.geometry()
+    assert g["large_cells"] == 1 << 14 and g["large_steps"] == k
+    assert g["n_large"] == sum(isinstance(p.rule, ca.ForestFire) and np.prod(p.space.dims) >= 1 << 14 for p in probs)
+    states = [np.asarray(p.u0) for p in probs]
+    t0 = [3 + i for i in range(len(probs))]
+    for rnd in range(2):
+        steps = [(0, 1, 5, 13, 29, 2, 17, 8, 11)[(i + rnd) % 9] for i in range(len(probs))]
+        ens.run(t0=t0, nsteps=steps)
+        counts, other, morans = ens.summaries(3)
+        for i, p in enumerate(probs):
+            got = ens.state(i)
+            want, c1, o1, m1 = single(ca, p, t0[i], steps[i], states[i])
+            assert np.array_equal(got, want), f"instance {i} ({p.space.dims}) run {rnd} k {k}"
+            assert list(counts[i]) == c1 and other[i] == o1, (i, rnd)
+            assert (morans[i] == m1) or (np.isnan(morans[i]) and np.isnan(m1)), (i, morans[i], m1)
+            states[i] = got
+            t0[i] += steps[i]
+    ens.close()
+
+
+def test_large_split_tuner_and_refusals(ca):
+    probs = large_split_problems(ca)
+    ens = ca.BatchedEnsemble(probs)
+    ens.set_initial_states()
+    tile, depth = ens.tune(probe_steps=4)
+    g = ens.geometry()
+    assert (tile, depth) == (g["tile"], g["depth"])
+    assert g["large_cells"] in (0, 1 << 16, 1 << 17, 1 << 18, 1 << 20) and g["large_steps"] in (1, 2, 4)
+    assert all(np.array_equal(ens.state(i), np.asarray(p.u0)) for i, p in enumerate(probs))
+    with pytest.raises(ca.ArgumentError):
+        ens.set_large(1000, 1)  # below the floor
+    with pytest.raises(ca.ArgumentError):
+        ens.set_large(1 << 18, 17)
+    ens.set_large(0, 1)
+    assert ens.geometry()["n_large"] == 0
+    ens.close()
