@@ -184,8 +184,8 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
                 if (p.n1 - X0 < kFireTX) nw = (int)((p.n1 - X0 + 3) / 4);
                 if (p.n2 - Y0 < kFireTY) nrows = (int)(p.n2 - Y0);
             }
-            fire_substep_rows<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, hx >> 2, nw, hy, nrows, X0 - hx,
-                                         Y0 - hy, g, ds, p.keys, tid, nthr, exact, dst, p.pitch);
+            fire_substep_rows<!INTERIOR>((const uint32_t*)A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds,
+                                         p.keys, tid, nthr, exact, dst, p.pitch);
             return;
         }
         // deeper passes: the region is wider than the tile in early sub-steps, so the flat
@@ -375,13 +375,13 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
         }
         const uint32_t* A = (const uint32_t*)cur;
         if (interior) {
-            fire_substep_rows<false>(A, nullptr, sw, hx >> 2, kFireTX / 4, hy, kFireTY, X0 - hx, Y0 - hy, g, ds,
-                                     p.keys, tid, nthr, !p.states_valid, dst, p.pitch);
+            fire_substep_rows<false>(A, sw, hx >> 2, kFireTX / 4, hy, kFireTY, X0 - hx, Y0 - hy, g, ds, p.keys, tid,
+                                     nthr, !p.states_valid, dst, p.pitch);
         } else {  // a ragged last tile: the words and rows inside the lattice only
             const int nw = p.n1 - X0 < kFireTX ? (int)((p.n1 - X0 + 3) / 4) : kFireTX / 4;
             const int nrows = p.n2 - Y0 < kFireTY ? (int)(p.n2 - Y0) : kFireTY;
-            fire_substep_rows<true>(A, nullptr, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds, p.keys, tid,
-                                    nthr, !p.states_valid, dst, p.pitch);
+            fire_substep_rows<true>(A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
+                                    !p.states_valid, dst, p.pitch);
         }
         __syncthreads();
     }
