@@ -19,8 +19,10 @@ struct FireGeom {
     int64_t n1, n2;
     int32_t bnd0, bnd1;
     uint32_t cst0, cst1;   // Constant value of each axis, replicated in every byte
-    uint64_t Up, Uf;       // thresholds against the raw words (w.x:w.y) of a draw
-    bool all_p, all_f;     // p >= 1, f >= 1 (every draw hits)
+    // thresholds against a draw's raw words (w.x:w.y): Ua + k dU for draw index k (mod 2^64),
+    // which is Up for k = 1 (an empty cell) and Uf for k = 2 (a tree)
+    uint64_t Ua, dU;
+    uint32_t allp, allf;   // 0x01010101 if p >= 1 (resp. f >= 1: every draw hits), else 0
     bool exact_always;     // a Constant edge holds a value other than 0, 1, 2
 };
 
@@ -36,19 +38,28 @@ __host__ __device__ inline bool fire_odd_constant(int32_t b0, int32_t c0, int32_
 __host__ __device__ inline void fire_thresholds(uint64_t thr_p, uint64_t thr_f, bool f32, FireGeom& g) {
     const uint64_t full = f32 ? ((uint64_t)1 << 24) : ((uint64_t)1 << 53);
     const int shift = f32 ? 40 : 11;
-    g.all_p = thr_p >= full;
-    g.all_f = thr_f >= full;
-    g.Up = g.all_p ? 0 : thr_p << shift;
-    g.Uf = g.all_f ? 0 : thr_f << shift;
+    const bool all_p = thr_p >= full, all_f = thr_f >= full;
+    g.allp = all_p ? 0x01010101u : 0u;
+    g.allf = all_f ? 0x01010101u : 0u;
+    const uint64_t Up = all_p ? 0 : thr_p << shift, Uf = all_f ? 0 : thr_f << shift;
+    g.dU = Uf - Up;
+    g.Ua = Up - g.dU;
 }
 
-// bernoulli(p) (empty cell) or bernoulli(f) (tree) of a draw, without a branch, so the four
-// draws of a word interleave.
-__device__ __forceinline__ bool fire_hit(uint2 w, bool empty, const FireGeom& g) {
-    const uint64_t U = empty ? g.Up : g.Uf;
-    const bool all = empty ? g.all_p : g.all_f;
+// Whether a draw with index k falls below its cell's threshold: bernoulli(p) for an empty cell
+// (k = 1), bernoulli(f) for a tree (k = 2), without a branch, so the four draws of a word
+// interleave. The threshold Ua + k dU is formed by integer multiply-adds rather than selects:
+// the sweep's limit is the ALU pipe (the Philox XORs and the rule's byte logic), and the
+// multiply-adds issue to the FMA pipe beside it. A saturated p or f (>= 1) is applied per
+// word (fire_next).
+__device__ __forceinline__ bool fire_below(uint2 w, uint32_t k, const FireGeom& g) {
+    uint64_t t;
+    uint32_t hi;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(t) : "r"(k), "r"((uint32_t)g.dU), "l"(g.Ua));
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(hi) : "r"(k), "r"((uint32_t)(g.dU >> 32)), "r"((uint32_t)(t >> 32)));
+    const uint64_t U = ((uint64_t)hi << 32) | (uint32_t)t;
     const uint64_t x = ((uint64_t)w.x << 32) | (uint64_t)w.y;
-    return (x < U) | all;
+    return x < U;
 }
 
 // Byte masks of a word of four cells (bit 0 of byte b for cell b): empty, burning, and next to
@@ -76,12 +87,14 @@ __device__ __forceinline__ void fire_masks(uint32_t C, uint32_t Lf, uint32_t Rt,
 // hit, else 1. Byte arithmetic throughout: each cell's code lands in its own byte.
 __device__ __forceinline__ uint32_t fire_next(uint32_t E, uint32_t F, uint32_t N, uint32_t base, const uint32_t* mx,
                                               const FireGeom& g, const DrawStep& ds, const PhiloxKeys& K) {
-    uint32_t H = 0;
+    // hits: a saturated probability hits every cell of its kind (byte select of allp / allf)
+    uint32_t H = (E & g.allp) | (~E & g.allf);
+    const uint32_t Kw = 0x02020202u - E;  // byte b: cell b's draw index, 1 if empty else 2
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const uint32_t e = (E >> (8 * b)) & 1u;
-        const uint2 w = draw_fast(ds, K, base + mx[b], 2u - e);
-        H |= (uint32_t)fire_hit(w, e, g) << (8 * b);
+        const uint32_t k = __byte_perm(Kw, 0u, 0x4440u | b);
+        const uint2 w = draw_fast(ds, K, base + mx[b], k);
+        if (fire_below(w, k, g)) H |= 1u << (8 * b);
     }
     const uint32_t T = ~(E | F) & 0x01010101u, NH = N | H;
     return ((E & H) | (T & ~NH)) | ((T & NH) << 1);
