@@ -151,15 +151,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel: str):
-    """Per-launch DRAM bytes of `kernel` from its committed ncu summary, when there is one
+def profiled_traffic(summary: str):
+    """Per-launch DRAM bytes from a committed ncu summary under profiles/, when it has them
     (a line 'traffic_bytes_per_launch: N')."""
-    for name in os.listdir(os.path.join(ROOT, "profiles")) if os.path.isdir(os.path.join(ROOT, "profiles")) else []:
-        if name.startswith(kernel) and name.endswith(".md"):
-            with open(os.path.join(ROOT, "profiles", name)) as f:
-                for line in f:
-                    if line.strip().startswith("traffic_bytes_per_launch:"):
-                        return float(line.split(":", 1)[1])
+    path = os.path.join(ROOT, "profiles", summary)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
     return None
 
 
@@ -790,7 +791,9 @@ def main():
     peak, peak_src = measured_peaks()
     achieved = parts[dom]["achieved_gbs"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": peak_src, "kernel": kernel, "traffic": profiled_traffic(kernel)}
+                "peak_source": peak_src, "kernel": kernel,
+                "traffic": profiled_traffic({"k_life": "k_life_ltl_moore5_8192.md",
+                                             "k_fire": "k_fire_forest_fire_16384.md"}[kernel])}
     for name in parts:
         parts[name]["hbm_frac_per_effective_step"] = parts[name]["achieved_gbs"] / peak
     # the forest fire's compute roof: one Philox4x32-10 draw per cell-update, measured alone
