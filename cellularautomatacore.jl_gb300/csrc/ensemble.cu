@@ -434,7 +434,7 @@ cudaError_t ens_kernel(void (**fn)(const EnsInstance*, const int*, int, int*, in
                        size_t* smem) {
     *fn = k_ensemble<TILE>;
     *smem = 2 * (size_t)ens_buf(TILE);
-    return cudaFuncSetAttribute(k_ensemble<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+    return ensure_dynamic_smem((const void*)k_ensemble<TILE>, *smem);
 }
 
 cudaError_t ens_select(int tile, void (**fn)(const EnsInstance*, const int*, int, int*, int8_t*, EnsSummary*, int*),

@@ -206,6 +206,13 @@ struct SparseTiles {
 // The message gbca_last_error() returns on this thread.
 void set_last_error(const char* msg);
 
+// Per-device launch facts, looked up once (launch_cache.cu): raise a kernel's dynamic
+// shared-memory limit to at least `bytes` (the runtime is called only when the limit set
+// before is lower), the SM count, and resident blocks per SM.
+cudaError_t ensure_dynamic_smem(const void* fn, size_t bytes);
+int device_sms();
+int blocks_per_sm(const void* fn, int threads, size_t smem);
+
 // Process-wide count of kernel launches (gbca_kernel_launches).
 void count_launch(int64_t n = 1);
 int64_t launches_so_far();
@@ -219,6 +226,7 @@ struct SweepChoice {
     int32_t steps_per_pass;
     int32_t tile_rows;
     int32_t staging;
+    int32_t tile_words = 0;  // bit-sliced kernel: tile width in 32-cell words (0: up to 32)
 };
 
 // states_valid: every state is known to be one the rule produces (Generations: 0..C-1,
@@ -254,6 +262,8 @@ cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst,
 // The general kernel over the tiles of p.tile_list (grid: the number of tiles of the lattice).
 cudaError_t launch_generic_tiles(const SweepParams& p, int ntiles, const int8_t* src, int8_t* dst, cudaStream_t st);
 bool life_simd_supported(const SweepParams& p);
+// The bit-sliced kernel's geometry for a lattice with no tuned or pinned one (sweep_life.cu).
+SweepChoice life_default_choice(const SweepParams& p);
 cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 // The bit-sliced kernel over the tiles of p.tile_list (tiles of tile_w x tile_h cells).
 cudaError_t launch_life_tiles(const SweepParams& p, const SparseTiles& sp, const int8_t* src, int8_t* dst,

@@ -370,7 +370,7 @@ int advance_t(LeniaPlan* P, int64_t nsteps, cudaStream_t st, int* cur, void* con
         } else if (P->box13) {
             constexpr int sx = kDirTX + 2 * kR13, sy = kDirTY + 2 * kR13, sp = (sx + 3 + 4) / 4 * 4;
             const size_t smem = sizeof(T) * sp * sy;
-            e = cudaFuncSetAttribute(k_lenia13<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            e = ensure_dynamic_smem((const void*)k_lenia13<T>, smem);
             if (e != cudaSuccess) return fail_to(err, GBCA_ERR_CUDA, cudaGetErrorString(e));
             dim3 grid((unsigned)((P->n1 + kDirTX - 1) / kDirTX), (unsigned)((P->n2 + kDirTY - 1) / kDirTY));
             const Box13<T>* wb;
@@ -382,7 +382,7 @@ int advance_t(LeniaPlan* P, int64_t nsteps, cudaStream_t st, int* cur, void* con
         } else {
             const int R = P->d.lenia_R, tile = 32;
             const size_t smem = sizeof(T) * (tile + 2 * R) * (tile + 2 * R);
-            e = cudaFuncSetAttribute(k_lenia_taps<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            e = ensure_dynamic_smem((const void*)k_lenia_taps<T>, smem);
             if (e != cudaSuccess) return fail_to(err, GBCA_ERR_CUDA, cudaGetErrorString(e));
             dim3 grid((unsigned)((P->n1 + tile - 1) / tile), (unsigned)((P->n2 + tile - 1) / tile));
             k_lenia_taps<T><<<grid, 256, smem, st>>>(u, out, P->n1, P->n2, P->pe, b1, b2, P->d_off, (const T*)P->d_w,

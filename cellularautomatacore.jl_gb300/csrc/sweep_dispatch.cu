@@ -47,9 +47,9 @@ SweepChoice sweep_choice(const gbca_desc& d, bool fire, bool life, const SweepCh
         choice = d.n1 * d.n2 >= ((int64_t)1 << 24) ? SweepChoice{1, 0, 2} : SweepChoice{8, 0, 0};
     }
     if (life && choice.steps_per_pass == 0) {
-        SweepParams p = sweep_params(d, 0, nullptr);
-        p.radius = d.radius;
-        choice.steps_per_pass = life_steps_per_pass(p);
+        const SweepParams p = sweep_params(d, 0, nullptr);
+        if (choice.tile_rows == 0) choice = life_default_choice(p);  // neither tuned nor pinned
+        else choice.steps_per_pass = life_steps_per_pass(p);
     }
     return choice;
 }
@@ -105,6 +105,7 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
     const SweepChoice choice = sweep_choice(d, fire, life, force);
     p.tile_y = choice.tile_rows;
     p.staging = choice.staging;
+    if (life) p.tile_x = choice.tile_words;
     while (nsteps > 0) {
         int64_t k;
         cudaError_t e;

@@ -475,7 +475,7 @@ cudaError_t launch_fire_batch(const FireJob* jobs, const int32_t* tile_job, int 
     if (K < 1 || K > 16 || ntiles < 1) return cudaErrorInvalidValue;
     const int hx = (K + 15) / 16 * 16;
     const size_t smem = 2 * (size_t)(kFireTX + 2 * hx) * (size_t)(kFireTY + 2 * K);
-    cudaError_t e = cudaFuncSetAttribute(k_fire_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_fire_batch, smem);
     if (e != cudaSuccess) return e;
     k_fire_batch<<<ntiles, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(jobs, tile_job, pass, K);
     return cudaGetLastError();
@@ -495,7 +495,7 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     p.keys = philox_keys(p.seed);
     const int sx = kFireTX + 2 * p.halo_x, sy = kFireTY + 2 * p.halo_y;
     const size_t smem = 2 * (size_t)sx * (size_t)sy;
-    cudaError_t e = cudaFuncSetAttribute(k_fire, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_fire, smem);
     if (e != cudaSuccess) return e;
     // TMA staging: interior tiles always; every tile when both edges are Constant(0), whose
     // value the tensor's zero fill reproduces, and n1 is a whole number of 16-byte segments
@@ -512,14 +512,10 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     const int tiles_x = (int)((p.n1 + kFireTX - 1) / kFireTX), tiles_y = (int)((p.n2 + kFireTY - 1) / kFireTY);
     if (p.nsub == 1 && tma && p.staging == 2) {  // one step per pass: the persistent, double-buffered kernel
         const size_t smem2 = 2 * (((size_t)sx * sy + 127) / 128 * 128);  // two 128-byte-aligned buffers
-        e = cudaFuncSetAttribute(k_fire_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+        e = ensure_dynamic_smem((const void*)k_fire_stream, smem2);
         if (e != cudaSuccess) return e;
-        int dev = 0, nsm = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fire_stream, kFireThreadsX * kFireThreadsY, smem2);
         const int ntiles = tiles_x * tiles_y;
-        int grid = nsm * (per > 0 ? per : 1);
+        int grid = device_sms() * blocks_per_sm((const void*)k_fire_stream, kFireThreadsX * kFireThreadsY, smem2);
         if (grid > ntiles) grid = ntiles;
         k_fire_stream<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem2, st>>>(p, src, dst, map, tma, tiles_x, ntiles);
         return cudaGetLastError();

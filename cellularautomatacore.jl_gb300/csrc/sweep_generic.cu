@@ -159,7 +159,7 @@ cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst,
     const int sx = p.tile_x + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
     const size_t smem = 2 * (size_t)sx * (size_t)sy;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_generic<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = ensure_dynamic_smem((const void*)k_generic<false>, smem);
         if (e != cudaSuccess) return e;
     }
     dim3 grid((unsigned)((p.n1 + p.tile_x - 1) / p.tile_x), (unsigned)((p.n2 + p.tile_y - 1) / p.tile_y));
@@ -171,7 +171,7 @@ cudaError_t launch_generic_tiles(const SweepParams& p, int ntiles, const int8_t*
     const int sx = p.tile_x + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
     const size_t smem = 2 * (size_t)sx * (size_t)sy;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_generic<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = ensure_dynamic_smem((const void*)k_generic<true>, smem);
         if (e != cudaSuccess) return e;
     }
     k_generic<true><<<(unsigned)ntiles, 256, smem, st>>>(p, src, dst);

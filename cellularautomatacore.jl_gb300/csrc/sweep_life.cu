@@ -461,7 +461,8 @@ LifeGeom life_geometry(const SweepParams& p, int K, int rows) {
     g.hy = g.K * p.radius;
     g.hw = (g.hy + 31) / 32;
     const int64_t words = (p.n1 + 31) / 32;
-    g.tw = words < 32 ? (int)words : 32;
+    const int tw = p.tile_x > 0 ? p.tile_x : 32;  // the default choice's width, or 32 words
+    g.tw = words < tw ? (int)words : tw;
     int ty = p.rule == GBCA_RULE_GENERATIONS ? 96 : 216;  // two planes: half the rows
     if (rows > 0) ty = rows;
     g.ty = p.n2 < ty ? (int)p.n2 : ty;
@@ -479,7 +480,7 @@ template <int R, int NI, int PL>
 cudaError_t launch_rn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                       cudaStream_t st, int ntiles) {
     const size_t smem = life_smem_bytes(p, g);
-    cudaError_t e = cudaFuncSetAttribute(k_life<R, NI, PL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_life<R, NI, PL>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((p.n1 + 32 * g.tw - 1) / (32 * g.tw)), (unsigned)((p.n2 + g.ty - 1) / g.ty));
     if (ntiles > 0) grid = dim3((unsigned)ntiles, 1u);  // one CTA per listed tile
@@ -524,6 +525,62 @@ int life_steps_per_pass(const SweepParams& p) {
         case 4: return 5;
         default: return 4;
     }
+}
+
+// The geometry for a lattice that has no tuned or pinned one: the steps per pass, tile height
+// and tile width that minimise a cost model of one pass per cell-update. A pass costs the
+// busiest SM's CTAs (ceil(CTAs / SMs)) times the cells one CTA computes — its tile plus the
+// halo each sub-step recomputes, ex = (K - 1 - s) r rows on each side and one word on each
+// side while ex > 0 — at a per-SM rate, plus a fixed launch cost. Wide tiles and deep passes
+// waste least on halos on large lattices; narrower, shorter tiles fill the GPU on medium ones
+// (a 2048^2 lattice has 20 CTAs of 1024 x 216 cells), and shallow passes on tiny ones cost
+// launches. The rates need only be right relative to the launch cost.
+SweepChoice life_default_choice(const SweepParams& p0) {
+    SweepParams p = p0;
+    const int Kmax = life_steps_per_pass(p);
+    const int PL = p.rule == GBCA_RULE_GENERATIONS ? 2 : 1;
+    const double rate = 60e9 / (p.radius * PL);  // cell-updates per second per SM (model)
+    const double t_launch = 4e-6;
+    const int nsm = device_sms();
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        optin = 227 * 1024;
+    }
+    const int64_t words = (p.n1 + 31) / 32;
+    SweepChoice best = {Kmax, 0, 0};
+    double best_cost = -1.0;
+    const int Ks[3] = {Kmax, Kmax / 2, Kmax / 4};
+    const int tws[3] = {32, 16, 8};
+    const int tys[5] = {216, 128, 96, 64, 32};
+    for (int K : Ks) {
+        if (K < 1) continue;
+        for (int tw : tws) {
+            const int twe = words < tw ? (int)words : tw;
+            if (twe < tw && tw != tws[0] && words < tws[0]) continue;  // narrower than the lattice already
+            for (int ty : tys) {
+                const int tye = p.n2 < ty ? (int)p.n2 : ty;
+                p.tile_x = twe;
+                const LifeGeom g = life_geometry(p, K, tye);
+                if (life_smem_bytes(p, g) > (size_t)optin) continue;
+                const int64_t ctas = ((words + twe - 1) / twe) * ((p.n2 + tye - 1) / tye);
+                double work = 0.0;  // cells one CTA computes over the pass
+                for (int s = 0; s < K; ++s) {
+                    const int ex = (K - 1 - s) * p.radius;
+                    work += 32.0 * (twe + 2 * ((ex + 31) / 32)) * (tye + 2 * ex);
+                }
+                const double t = (double)((ctas + nsm - 1) / nsm) * work / rate + t_launch;
+                const double cost = t / ((double)p.n1 * (double)p.n2 * K);
+                if (best_cost < 0.0 || cost < best_cost) {
+                    best_cost = cost;
+                    best = SweepChoice{K, tye, 0};
+                    best.tile_words = twe;
+                }
+            }
+        }
+    }
+    return best;
 }
 
 bool life_choice_fits(const SweepParams& p, int steps, int rows) {
