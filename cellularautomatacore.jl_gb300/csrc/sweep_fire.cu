@@ -143,7 +143,8 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
                                           int8_t* __restrict__ dst, int8_t* A, int8_t* B, bool staged,
                                           int64_t X0, int64_t Y0) {
     const int hx = p.halo_x, hy = p.halo_y;
-    const int sx = kFireTX + 2 * hx, sy = kFireTY + 2 * hy;
+    const int TY = p.tile_y;  // the tile's rows (the launcher's choice)
+    const int sx = kFireTX + 2 * hx, sy = TY + 2 * hy;
     const int sw = sx / 4;  // words per shared row
     const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
     const int nthr = kFireThreadsX * kFireThreadsY;
@@ -179,10 +180,10 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
             // one step: the region is the tile itself (64 words, all 512 threads busy walking
             // rows), stored straight to the lattice state; a ragged last tile spreads the
             // threads over the words and rows inside the lattice only
-            int nw = kFireTX / 4, nrows = kFireTY;
+            int nw = kFireTX / 4, nrows = TY;
             if (!INTERIOR) {
                 if (p.n1 - X0 < kFireTX) nw = (int)((p.n1 - X0 + 3) / 4);
-                if (p.n2 - Y0 < kFireTY) nrows = (int)(p.n2 - Y0);
+                if (p.n2 - Y0 < TY) nrows = (int)(p.n2 - Y0);
             }
             fire_substep_rows<!INTERIOR>((const uint32_t*)A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds,
                                          p.keys, tid, nthr, exact, dst, p.pitch);
@@ -191,19 +192,19 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
         // deeper passes: the region is wider than the tile in early sub-steps, so the flat
         // word x row split keeps every thread busy
         fire_substep_words<!INTERIOR>((const uint32_t*)A, (uint32_t*)B, sw, w_lo, w_hi - w_lo, hy - ex,
-                                      kFireTY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr, exact);
+                                      TY + 2 * ex, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr, exact);
         __syncthreads();
         int8_t* t = A; A = B; B = t;
     }
 
     if (INTERIOR) {  // 16-byte stores: X0, the tile width and the pitch are multiples of 16
         const int qx = kFireTX / 16;
-        for (int q = tid; q < qx * kFireTY; q += nthr) {
+        for (int q = tid; q < qx * TY; q += nthr) {
             const int lq = q % qx, oy = q / qx;
             *(int4*)(dst + (X0 + 16 * lq) + (Y0 + oy) * p.pitch) = *(const int4*)(A + (hy + oy) * sx + hx + 16 * lq);
         }
     } else {
-        for (int idx = tid; idx < kFireTX * kFireTY; idx += nthr) {
+        for (int idx = tid; idx < kFireTX * TY; idx += nthr) {
             const int ox = idx % kFireTX, oy = idx / kFireTX;
             const int64_t gx = X0 + ox, gy = Y0 + oy;
             if (gx < p.n1 && gy < p.n2) dst[gx + gy * p.pitch] = A[(hy + oy) * sx + hx + ox];
@@ -217,12 +218,12 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
            const __grid_constant__ CUtensorMap tmap, int tma) {
     extern __shared__ __align__(128) int8_t smem_f[];
     __shared__ __align__(8) uint64_t tma_bar;
-    const int sx = kFireTX + 2 * p.halo_x, sy = kFireTY + 2 * p.halo_y;
+    const int sx = kFireTX + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
     int8_t* A = smem_f;
     int8_t* B = smem_f + sx * sy;
-    const int64_t X0 = (int64_t)blockIdx.x * kFireTX, Y0 = (int64_t)blockIdx.y * kFireTY;
+    const int64_t X0 = (int64_t)blockIdx.x * kFireTX, Y0 = (int64_t)blockIdx.y * p.tile_y;
     const bool interior = X0 - p.halo_x >= 0 && X0 + kFireTX + p.halo_x <= p.n1 && Y0 - p.halo_y >= 0 &&
-                          Y0 + kFireTY + p.halo_y <= p.n2;
+                          Y0 + p.tile_y + p.halo_y <= p.n2;
     // a tensor copy's shared destination must be 128-byte aligned (the dynamic base is)
     const bool staged = (smem_u32(A) & 127u) == 0u && (tma == 2 || (tma == 1 && interior));
     if (staged) {
@@ -267,6 +268,7 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY, 2)
         ((uint32_t*)&sp)[k] = ((const uint32_t*)&J.p)[k];
     __syncthreads();
     if (tid == 0) {
+        sp.tile_y = kFireTY;
         sp.nsub = nsub;
         sp.t0 = J.p.t0 + done;
         sp.halo_y = nsub;
@@ -299,7 +301,8 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     extern __shared__ __align__(128) int8_t smem_f[];
     __shared__ __align__(8) uint64_t bars[2];
     const int hx = p.halo_x, hy = p.halo_y;  // halo_y = 1: one step per pass
-    const int sx = kFireTX + 2 * hx, sy = kFireTY + 2 * hy, sw = sx / 4;
+    const int TY = p.tile_y;                   // the tile's rows (the launcher's choice)
+    const int sx = kFireTX + 2 * hx, sy = TY + 2 * hy, sw = sx / 4;
     // a tensor copy's shared destination must be 128-byte aligned: buffers start on 128 bytes
     const int stride = (sx * sy + 127) / 128 * 128;
     int8_t* const buf0 = smem_f;
@@ -326,8 +329,8 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     __syncthreads();
     auto origin = [&](int tile, int64_t* X0, int64_t* Y0) {
         *X0 = (int64_t)(tile % tiles_x) * kFireTX;
-        *Y0 = (int64_t)(tile / tiles_x) * kFireTY;
-        return *X0 - hx >= 0 && *X0 + kFireTX + hx <= p.n1 && *Y0 - hy >= 0 && *Y0 + kFireTY + hy <= p.n2;
+        *Y0 = (int64_t)(tile / tiles_x) * TY;
+        return *X0 - hx >= 0 && *X0 + kFireTX + hx <= p.n1 && *Y0 - hy >= 0 && *Y0 + TY + hy <= p.n2;
     };
     auto staged = [&](bool interior) { return aligned && (tma == 2 || (tma == 1 && interior)); };
     auto issue = [&](int tile, int k) {  // one thread: the tile's copy into buffer k
@@ -375,11 +378,11 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
         }
         const uint32_t* A = (const uint32_t*)cur;
         if (interior) {
-            fire_substep_rows<false>(A, sw, hx >> 2, kFireTX / 4, hy, kFireTY, X0 - hx, Y0 - hy, g, ds, p.keys, tid,
+            fire_substep_rows<false>(A, sw, hx >> 2, kFireTX / 4, hy, TY, X0 - hx, Y0 - hy, g, ds, p.keys, tid,
                                      nthr, !p.states_valid, dst, p.pitch);
         } else {  // a ragged last tile: the words and rows inside the lattice only
             const int nw = p.n1 - X0 < kFireTX ? (int)((p.n1 - X0 + 3) / 4) : kFireTX / 4;
-            const int nrows = p.n2 - Y0 < kFireTY ? (int)(p.n2 - Y0) : kFireTY;
+            const int nrows = p.n2 - Y0 < TY ? (int)(p.n2 - Y0) : TY;
             fire_substep_rows<true>(A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
                                     !p.states_valid, dst, p.pitch);
         }
@@ -489,11 +492,17 @@ bool fire_fast_supported(const SweepParams& p) {
 cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, cudaStream_t st) {
     SweepParams p = p0;
     p.tile_x = kFireTX;
+    // tile rows: 128, or 64 / 32 when the lattice has fewer than two tiles per CTA slot
+    // (two CTAs per SM), so a medium lattice still spreads over every SM
     p.tile_y = kFireTY;
+    {
+        const int64_t tx = (p.n1 + kFireTX - 1) / kFireTX, slots = 2 * (int64_t)device_sms();
+        while (p.tile_y > 32 && tx * ((p.n2 + p.tile_y - 1) / p.tile_y) < 2 * slots) p.tile_y /= 2;
+    }
     p.halo_y = p.nsub;
     p.halo_x = (p.nsub + 15) / 16 * 16;
     p.keys = philox_keys(p.seed);
-    const int sx = kFireTX + 2 * p.halo_x, sy = kFireTY + 2 * p.halo_y;
+    const int sx = kFireTX + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
     const size_t smem = 2 * (size_t)sx * (size_t)sy;
     cudaError_t e = ensure_dynamic_smem((const void*)k_fire, smem);
     if (e != cudaSuccess) return e;
@@ -509,7 +518,7 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
                                 p.cval[1] == 0 && p.n1 % 16 == 0;
         tma = zero_edges ? 2 : 1;
     }
-    const int tiles_x = (int)((p.n1 + kFireTX - 1) / kFireTX), tiles_y = (int)((p.n2 + kFireTY - 1) / kFireTY);
+    const int tiles_x = (int)((p.n1 + kFireTX - 1) / kFireTX), tiles_y = (int)((p.n2 + p.tile_y - 1) / p.tile_y);
     if (p.nsub == 1 && tma && p.staging == 2) {  // one step per pass: the persistent, double-buffered kernel
         const size_t smem2 = 2 * (((size_t)sx * sy + 127) / 128 * 128);  // two 128-byte-aligned buffers
         e = ensure_dynamic_smem((const void*)k_fire_stream, smem2);

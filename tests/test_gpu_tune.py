@@ -171,3 +171,20 @@ def test_fire_persistent_multi_tile(ca, oracle, space):
     P = oracle.Problem(oracle.RULE_FOREST_FIRE, n, n, nbhd=oracle.VON_NEUMANN, seed=21, boundary=bnd)
     assert np.array_equal(got, oracle.run_array(P, u0, 0, 6, (0.05, 0.002), nthreads=16))
     st.close()
+
+
+@pytest.mark.parametrize("staging", [0, 1, 2])
+def test_fire_full_height_tiles(ca, oracle, staging):
+    """A lattice with enough 256 x 128 tiles to fill every CTA slot twice keeps full-height
+    tiles (smaller lattices take 64- or 32-row tiles): 4096 x 5120 (640 tiles), 3 steps of
+    each staging method, against the oracle."""
+    n1, n2 = 4096, 5120
+    u0 = np.random.default_rng(31 + staging).integers(0, 3, (n1, n2)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 3, {"p": 0.05, "f": 0.002}, space=ca.Grid(n1, n2), seed=17)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, 1, 0, staging)
+    got = _run(ca, prob, st, 0, 3, prob.p)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, n1, n2, nbhd=oracle.VON_NEUMANN, seed=17,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    assert np.array_equal(got, oracle.run_array(P, u0, 0, 3, (0.05, 0.002), nthreads=16))
+    st.close()
