@@ -41,10 +41,11 @@ SweepChoice sweep_choice(const gbca_desc& d, bool fire, bool life, const SweepCh
     SweepChoice choice = {0, 0, 0};
     if (force) return *force;
     if ((fire || life) && !tuned_choice(d, &choice) && fire) {
-        // untuned forest fire: on large lattices one step per pass from the persistent TMA
-        // kernel (the compute-bound optimum); on small ones 8 steps per pass with vector
-        // loads, an eighth of the launches for a launch-bound grid
-        choice = d.n1 * d.n2 >= ((int64_t)1 << 24) ? SweepChoice{1, 0, 2} : SweepChoice{8, 0, 0};
+        // untuned forest fire: from 2^22 cells one step per pass, each tile staged by TMA (the
+        // compute-bound optimum: 221, 311, 376 and 406 Gcell-updates/s at 2048^2, 4096^2,
+        // 8192^2 and 16384^2 on GB300); below, 8 steps per pass with vector loads, an eighth
+        // of the launches for a launch-bound grid (156 against 120 at 1024^2)
+        choice = d.n1 * d.n2 >= ((int64_t)1 << 22) ? SweepChoice{1, 0, 1} : SweepChoice{8, 0, 0};
     }
     if (life && choice.steps_per_pass == 0) {
         const SweepParams p = sweep_params(d, 0, nullptr);

@@ -492,12 +492,22 @@ bool fire_fast_supported(const SweepParams& p) {
 cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, cudaStream_t st) {
     SweepParams p = p0;
     p.tile_x = kFireTX;
-    // tile rows: 128, or 64 / 32 when the lattice has fewer than two tiles per CTA slot
-    // (two CTAs per SM), so a medium lattice still spreads over every SM
-    p.tile_y = kFireTY;
+    // tile rows: 128, 64 or 32, whichever keeps the most of the GPU busy. The tiles run in
+    // rounds of one per CTA slot (two CTAs per SM), so a lattice of t tiles fills
+    // (t / slots) / ceil(t / slots) of the last round's share; a shorter tile recomputes a
+    // larger share of halo rows, TY / (TY + 2 halo) useful.
     {
         const int64_t tx = (p.n1 + kFireTX - 1) / kFireTX, slots = 2 * (int64_t)device_sms();
-        while (p.tile_y > 32 && tx * ((p.n2 + p.tile_y - 1) / p.tile_y) < 2 * slots) p.tile_y /= 2;
+        double best = -1.0;
+        for (int ty = kFireTY; ty >= 32; ty /= 2) {
+            const int64_t t = tx * ((p.n2 + ty - 1) / ty);
+            const double rounds = (double)((t + slots - 1) / slots);
+            const double eff = ((double)t / (double)slots) / rounds * (double)ty / (double)(ty + 2 * p.nsub);
+            if (eff > best + 1e-9) {
+                best = eff;
+                p.tile_y = ty;
+            }
+        }
     }
     p.halo_y = p.nsub;
     p.halo_x = (p.nsub + 15) / 16 * 16;
