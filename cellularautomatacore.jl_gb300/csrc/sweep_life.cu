@@ -39,6 +39,7 @@ namespace {
 
 constexpr int kMaxIntervals = 8;
 constexpr int kLifeThreads = 256;
+constexpr double kLifeIoCost = 6.0;  // cell-steps per loaded cell of a pass (the default's cost model)
 
 struct LifeTables {
     int32_t n[2];                                // interval counts: [0] dead cells, [1] live cells
@@ -529,12 +530,15 @@ int life_steps_per_pass(const SweepParams& p) {
 
 // The geometry for a lattice that has no tuned or pinned one: the steps per pass, tile height
 // and tile width that minimise a cost model of one pass per cell-update. A pass costs the
-// busiest SM's CTAs (ceil(CTAs / SMs)) times the cells one CTA computes — its tile plus the
-// halo each sub-step recomputes, ex = (K - 1 - s) r rows on each side and one word on each
-// side while ex > 0 — at a per-SM rate, plus a fixed launch cost. Wide tiles and deep passes
-// waste least on halos on large lattices; narrower, shorter tiles fill the GPU on medium ones
-// (a 2048^2 lattice has 20 CTAs of 1024 x 216 cells), and shallow passes on tiny ones cost
-// launches. The rates need only be right relative to the launch cost.
+// busiest SM's CTAs (ceil(CTAs / SMs)) times the work of one CTA, at a per-SM rate, plus a
+// fixed launch cost. A CTA's work is the cells it computes — its tile plus the halo each
+// sub-step recomputes, ex = (K - 1 - s) r rows on each side and one word on each side while
+// ex > 0 — plus its loaded region (tile and full halo) at kLifeIoCost cell-steps per cell for
+// packing bytes into bits and unpacking the results; that term favours deep passes. Wide tiles
+// and deep passes waste least on large lattices; narrower, shorter tiles fill the GPU on
+// medium ones (a 2048^2 lattice has 20 CTAs of 1024 x 216 cells). kLifeIoCost = 6 fits the
+// measured rates of Life B3/S23 on a 16384^2 torus at 16 and at 4 steps per pass (8.5 and
+// 5.0 Tcell-updates/s at 1024 x 216-cell tiles).
 SweepChoice life_default_choice(const SweepParams& p0) {
     SweepParams p = p0;
     const int Kmax = life_steps_per_pass(p);
@@ -565,11 +569,12 @@ SweepChoice life_default_choice(const SweepParams& p0) {
                 const LifeGeom g = life_geometry(p, K, tye);
                 if (life_smem_bytes(p, g) > (size_t)optin) continue;
                 const int64_t ctas = ((words + twe - 1) / twe) * ((p.n2 + tye - 1) / tye);
-                double work = 0.0;  // cells one CTA computes over the pass
+                double work = 0.0;  // cell-steps of one CTA over the pass
                 for (int s = 0; s < K; ++s) {
                     const int ex = (K - 1 - s) * p.radius;
                     work += 32.0 * (twe + 2 * ((ex + 31) / 32)) * (tye + 2 * ex);
                 }
+                work += kLifeIoCost * 32.0 * (twe + 2 * g.hw) * (tye + 2 * g.hy);
                 const double t = (double)((ctas + nsm - 1) / nsm) * work / rate + t_launch;
                 const double cost = t / ((double)p.n1 * (double)p.n2 * K);
                 if (best_cost < 0.0 || cost < best_cost) {
