@@ -62,21 +62,21 @@ __device__ __forceinline__ bool fire_below(uint2 w, uint32_t k, const FireGeom& 
     return x < U;
 }
 
-// Byte masks of a word of four cells (bit 0 of byte b for cell b): empty, burning, and next to
-// a burning cell, from the word C and its neighbour words (Lf, Rt: the cells left and right;
+// Byte masks of a word of four cells (bit 0 of byte b for cell b): empty, tree, and next to a
+// burning cell, from the word C and its neighbour words (Lf, Rt: the cells left and right;
 // Up, Dn: the rows above and below). EXACT compares whole bytes, for tiles that may hold
-// states other than 0, 1, 2 (other values are trees); otherwise 2 is bit 1 and 0 is neither
-// bit.
+// states other than 0, 1, 2 (other values are trees); otherwise a tree is bit 0, a fire bit 1
+// and an empty cell neither bit.
 template <bool EXACT>
 __device__ __forceinline__ void fire_masks(uint32_t C, uint32_t Lf, uint32_t Rt, uint32_t Up, uint32_t Dn,
-                                           uint32_t& E, uint32_t& F, uint32_t& N) {
+                                           uint32_t& E, uint32_t& T, uint32_t& N) {
     if (!EXACT) {
         E = ~(C | (C >> 1)) & 0x01010101u;
-        F = (C >> 1) & 0x01010101u;
+        T = C & 0x01010101u;
         N = ((Lf | Rt | Up | Dn) >> 1) & 0x01010101u;
     } else {
         E = bytes_eq(C, 0u) >> 7;
-        F = bytes_eq(C, 0x02020202u) >> 7;
+        T = ~(E | (bytes_eq(C, 0x02020202u) >> 7)) & 0x01010101u;
         N = (bytes_eq(Lf, 0x02020202u) | bytes_eq(Rt, 0x02020202u) | bytes_eq(Up, 0x02020202u) |
              bytes_eq(Dn, 0x02020202u)) >> 7;
     }
@@ -84,8 +84,9 @@ __device__ __forceinline__ void fire_masks(uint32_t C, uint32_t Lf, uint32_t Rt,
 
 // The next states of a word of four cells from its byte masks: cell b (id base + mx[b]) draws
 // once, k = 1 if empty else 2; empty -> 1 on a hit, fire -> 0, tree -> 2 next to a fire or on a
-// hit, else 1. Byte arithmetic throughout: each cell's code lands in its own byte.
-__device__ __forceinline__ uint32_t fire_next(uint32_t E, uint32_t F, uint32_t N, uint32_t base, const uint32_t* mx,
+// hit, else 1. Byte arithmetic throughout, each cell's code in its own byte: the next state is
+// T + (T & (N | H)) + (E & H), no byte above 2, so no carry crosses a byte.
+__device__ __forceinline__ uint32_t fire_next(uint32_t E, uint32_t T, uint32_t N, uint32_t base, const uint32_t* mx,
                                               const FireGeom& g, const DrawStep& ds, const PhiloxKeys& K) {
     // hits: a saturated probability hits every cell of its kind (byte select of allp / allf)
     uint32_t H = (E & g.allp) | (~E & g.allf);
@@ -96,8 +97,7 @@ __device__ __forceinline__ uint32_t fire_next(uint32_t E, uint32_t F, uint32_t N
         const uint2 w = draw_fast(ds, K, base + mx[b], k);
         if (fire_below(w, k, g)) H |= 1u << (8 * b);
     }
-    const uint32_t T = ~(E | F) & 0x01010101u, NH = N | H;
-    return ((E & H) | (T & ~NH)) | ((T & NH) << 1);
+    return T + (T & (N | H)) + (E & H);
 }
 
 // Words [w_lo, w_lo + nw) x rows [y_lo, y_lo + nrows) of a tile with row pitch sw words; byte
@@ -130,8 +130,8 @@ __device__ __forceinline__ void fire_substep_words_t(const uint32_t* __restrict_
         const uint32_t C = A[o], Wl = A[o - 1], Wr = A[o + 1], Up = A[o - sw], Dn = A[o + sw];
         const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
         const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
-        uint32_t E, F, N;
-        fire_masks<EXACT>(C, Lf, Rt, Up, Dn, E, F, N);
+        uint32_t E, T, N;
+        fire_masks<EXACT>(C, Lf, Rt, Up, Dn, E, T, N);
         const int64_t gy = gy0 + ly, gx = gx0 + 4 * lw;
         uint32_t outmask = 0, my = (uint32_t)gy;
         uint32_t mx[4];
@@ -150,7 +150,7 @@ __device__ __forceinline__ void fire_substep_words_t(const uint32_t* __restrict_
 #pragma unroll
             for (int b = 0; b < 4; ++b) mx[b] = (uint32_t)gx + b;
         }
-        uint32_t res = fire_next(E, F, N, my * n1 + 1u, mx, g, ds, K);
+        uint32_t res = fire_next(E, T, N, my * n1 + 1u, mx, g, ds, K);
         if (MAPPED) {
             if (rowout) res = g.cst1;
             else res = (res & ~outmask) | (g.cst0 & outmask);
@@ -207,9 +207,9 @@ __device__ __forceinline__ void fire_substep_rows_t(const uint32_t* __restrict__
         const uint32_t Dn = A[o + sw], Wl = A[o - 1], Wr = A[o + 1];
         const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
         const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
-        uint32_t E, F, N;
-        fire_masks<EXACT>(C, Lf, Rt, Up, Dn, E, F, N);
-        const uint32_t res = fire_next(E, F, N, base, mx, g, ds, K);
+        uint32_t E, T, N;
+        fire_masks<EXACT>(C, Lf, Rt, Up, Dn, E, T, N);
+        const uint32_t res = fire_next(E, T, N, base, mx, g, ds, K);
         if (!CHECKED || xin >= 4) {
             *(uint32_t*)q = res;
         } else {
