@@ -413,7 +413,10 @@ typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, v
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 std::mutex g_map_mu;
-std::vector<MapEntry> g_maps;  // a few entries: two buffers x the depths in use
+// two buffers x the depths and tile heights in use, per lattice: 128 entries cover a server's
+// lanes (16 lattices at a time) without one lane evicting another's maps
+constexpr size_t kMaxMaps = 128;
+std::vector<MapEntry> g_maps;
 EncodeTiled g_encode = nullptr;
 bool g_encode_looked = false;
 
@@ -421,11 +424,13 @@ bool g_encode_looked = false;
 // whole tile; false when the driver offers no tensor maps.
 bool tile_map(const void* base, int64_t n1, int64_t n2, int64_t pitch, int sx, int sy, CUtensorMap* out) {
     std::lock_guard<std::mutex> lock(g_map_mu);
-    for (const MapEntry& m : g_maps)
+    for (auto it = g_maps.rbegin(); it != g_maps.rend(); ++it) {  // the most recent first
+        const MapEntry& m = *it;
         if (m.k.base == base && m.k.n1 == n1 && m.k.n2 == n2 && m.k.pitch == pitch && m.k.sx == sx && m.k.sy == sy) {
             *out = m.map;
             return true;
         }
+    }
     if (!g_encode_looked) {
         g_encode_looked = true;
         void* fn = nullptr;
@@ -446,7 +451,7 @@ bool tile_map(const void* base, int64_t n1, int64_t n2, int64_t pitch, int sx, i
                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return false;
-    if (g_maps.size() >= 16) g_maps.erase(g_maps.begin());
+    if (g_maps.size() >= kMaxMaps) g_maps.erase(g_maps.begin());
     g_maps.push_back(MapEntry{MapKey{base, n1, n2, pitch, sx, sy}, m});
     *out = m;
     return true;
