@@ -991,9 +991,10 @@ int gbca_ensemble_tune(gbca_ensemble* e, int64_t probe_steps, const double* para
         capable = capable || (ensemble_large_capable(e->descs[(size_t)i]) &&
                               e->h_inst[(size_t)i].n1 * e->h_inst[(size_t)i].n2 >= kEnsLargeFloor);
     if (capable && c == cudaSuccess && rc == GBCA_OK) {
-        const int64_t splits[5] = {(int64_t)1 << 16, (int64_t)1 << 17, (int64_t)1 << 18, (int64_t)1 << 20, 0};
+        const int64_t splits[7] = {kEnsLargeFloor,     (int64_t)1 << 15, (int64_t)1 << 16, (int64_t)1 << 17,
+                                   (int64_t)1 << 18, (int64_t)1 << 20, 0};
         const int ks[3] = {1, 2, 4};
-        for (int a = 0; a < 5; ++a)
+        for (int a = 0; a < 7; ++a)
             for (int b = 0; b < 3; ++b) {
                 if (splits[a] == 0 && b > 0) break;  // nothing runs as batched passes
                 const Cand k = {win.tile, win.depth, splits[a], ks[b]};

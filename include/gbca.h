@@ -297,7 +297,7 @@ int gbca_ensemble_geometry(gbca_ensemble* e, int32_t* tile, int32_t* depth, int6
 /* The autotuner for the batched path: times every (tile, depth) candidate on the ensemble's
  * own instances for `probe_steps` steps each from their current states (restored after every
  * candidate and at the end; params as in gbca_ensemble_run), keeps the fastest, then times the
- * large-instance split (min_cells 2^16, 2^17, 2^18, 2^20 or none x 1, 2 or 4 steps per pass)
+ * large-instance split (min_cells 2^14 .. 2^18, 2^20 or none x 1, 2 or 4 steps per pass)
  * where an instance could take it, and keeps the fastest of all; returns tile and depth
  * (gbca_ensemble_geometry gives the rest). It allocates one copy of the ensemble's state pool
  * while it runs; summaries are those of the last probe until the next gbca_ensemble_run. No

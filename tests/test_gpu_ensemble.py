@@ -226,7 +226,8 @@ def test_large_split_tuner_and_refusals(ca):
     tile, depth = ens.tune(probe_steps=4)
     g = ens.geometry()
     assert (tile, depth) == (g["tile"], g["depth"])
-    assert g["large_cells"] in (0, 1 << 16, 1 << 17, 1 << 18, 1 << 20) and g["large_steps"] in (1, 2, 4)
+    assert g["large_cells"] in (0, 1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18, 1 << 20)
+    assert g["large_steps"] in (1, 2, 4)
     assert all(np.array_equal(ens.state(i), np.asarray(p.u0)) for i, p in enumerate(probs))
     with pytest.raises(ca.ArgumentError):
         ens.set_large(1000, 1)  # below the floor
