@@ -165,7 +165,7 @@ cudaError_t scan_states(gbca_handle* h, bool* valid) {
         e = cudaMemcpyAsync(h->acc_host, h->acc, 256 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return e;
-    const int nv = h->d.rule == GBCA_RULE_GENERATIONS ? h->d.states : 3;
+    const int nv = h->d.rule == GBCA_RULE_GENERATIONS ? h->d.states : (h->d.rule == GBCA_RULE_LIFE ? 2 : 3);
     unsigned long long inside = 0;
     for (int v = 0; v < nv && v < 128; ++v) inside += h->acc_host[128 + v];
     *valid = inside == (unsigned long long)(h->d.n1 * h->d.n2);
@@ -173,7 +173,9 @@ cudaError_t scan_states(gbca_handle* h, bool* valid) {
 }
 
 bool scanned_rule(const gbca_handle* h) {
-    return h->d.rule == GBCA_RULE_GENERATIONS || h->d.rule == GBCA_RULE_FOREST_FIRE;
+    // gated Life keeps closed cells' values, which its bit-sliced kernel holds only for 0 and 1
+    return h->d.rule == GBCA_RULE_GENERATIONS || h->d.rule == GBCA_RULE_FOREST_FIRE ||
+           (h->d.rule == GBCA_RULE_LIFE && h->d.scheme != GBCA_SYNCHRONOUS);
 }
 
 // A state written by the caller may hold values the rule never produces; the fast paths

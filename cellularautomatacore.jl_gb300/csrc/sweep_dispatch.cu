@@ -72,7 +72,8 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
             int64_t per;
             if (life) {
                 per = life_steps_per_pass(p);
-                const int64_t cap = sparse->tile_h / (2 * p.radius);  // halo no deeper than half a tile
+                // halo (steps x gates x r) no deeper than half a tile
+                const int64_t cap = sparse->tile_h / (2 * p.radius * p.ngates);
                 if (per > cap) per = cap > 0 ? cap : 1;
             } else {
                 per = 32 / (p.radius * p.ngates);
@@ -122,7 +123,7 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
         } else if (life) {
             const int64_t per = choice.steps_per_pass > 0 ? choice.steps_per_pass : life_steps_per_pass(p);
             k = nsteps < per ? nsteps : per;
-            p.nsub = (int32_t)k;
+            p.nsub = (int32_t)(k * p.ngates);  // sub-steps: two half-steps per Checkerboard step
             e = launch_life_simd(p, src, dst, st);
         } else {
             int64_t per = 32 / (p.radius * p.ngates);

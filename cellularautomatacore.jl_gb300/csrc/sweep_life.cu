@@ -31,6 +31,15 @@
 // Temporal blocking: K sub-steps per HBM pass; the computed region shrinks by r per
 // sub-step. Periodic and reflecting halos are images of lattice cells and evolve like
 // them; cells beyond a Constant edge are reset to the constant after every sub-step.
+//
+// Gated schemes (src/schemes.jl:84-93): a sub-step's new bits are blended with the old ones
+// through a gate mask, so a closed cell keeps its state. Checkerboard runs two half-steps per
+// step, the cells with (x + y) even and then odd (0-based): the mask alternates by bit and row,
+// which matches the mapped cells' parity for halos beyond a Constant edge (reset anyway) or a
+// Periodic edge of even length, the only boundaries it runs here. Stochastic(p) opens cell
+// (x, y) when its draw k = 0 at time t falls below p, the draw keyed by the mapped cell's id as
+// in the rule's own draws. A closed Life cell keeps its value, which the indicator bits hold
+// only for states 0 and 1, so gated Life needs every state in {0, 1} (the host scans it).
 #include "gbca_internal.cuh"
 
 namespace gbca {
@@ -39,7 +48,9 @@ namespace {
 
 constexpr int kMaxIntervals = 8;
 constexpr int kLifeThreads = 256;
-constexpr double kLifeIoCost = 6.0;  // cell-steps per loaded cell of a pass (the default's cost model)
+constexpr double kLifeIoCost = 6.0;   // cell-steps per loaded cell of a pass (the default's cost model)
+constexpr double kLifeSatCtas = 2.0;       // CTAs per SM the default's cost model takes to fill an SM,
+constexpr double kLifeSatCtasDraws = 3.0;  // and with a Philox gate draw per cell-step
 
 struct LifeTables {
     int32_t n[2];                                // interval counts: [0] dead cells, [1] live cells
@@ -53,6 +64,49 @@ struct LifeGeom {
     int32_t sw, sy;   // smem row pitch in words (tw + 2hw + 2 guards), rows (ty + 2hy)
     int32_t K;        // sub-steps
 };
+
+// A sub-step's gate (mode 0: every cell updates, 1: Checkerboard parity `gate`, 2: the
+// Stochastic draws at the sub-step's time), with the lattice position of local cell 0.
+struct LifeGate {
+    int32_t mode, gate;
+    int64_t X0, Y0;
+    DrawStep ds;
+};
+
+// The Stochastic gate of the 32 cells x = gx .. gx + 31 of lattice row y: bit b open when the
+// draw k = 0 of the mapped cell falls below p. Cells beyond a Constant edge get a closed bit
+// (the Constant reset overwrites them after the sub-step anyway).
+__device__ __forceinline__ uint32_t stochastic_gate(const SweepParams& p, const DrawStep& ds, int64_t gx, int64_t y) {
+    uint32_t G = 0;
+    const int64_t my = map_axis(p.bnd[1], y, p.n2);
+    if (my < 0) return 0u;
+    if (gx >= 0 && gx + 32 <= p.n1) {
+        const uint32_t base = (uint32_t)(gx + my * p.n1) + 1u;
+#pragma unroll 4
+        for (int b = 0; b < 32; ++b)
+            G |= (uint32_t)draw_below(draw_fast(ds, p.keys, base + (uint32_t)b, 0u), p.gate_thr, p.gate_f32 != 0) << b;
+        return G;
+    }
+    if (p.bnd[0] == GBCA_PERIODIC && p.n1 >= 32) {  // a word across the wrap: one modulo, then steps
+        int64_t m = gx % p.n1;
+        if (m < 0) m += p.n1;
+        uint32_t mx = (uint32_t)m;
+        const uint32_t row = (uint32_t)(my * p.n1) + 1u, n1 = (uint32_t)p.n1;
+#pragma unroll 4
+        for (int b = 0; b < 32; ++b) {
+            G |= (uint32_t)draw_below(draw_fast(ds, p.keys, row + mx, 0u), p.gate_thr, p.gate_f32 != 0) << b;
+            mx = mx + 1u == n1 ? 0u : mx + 1u;
+        }
+        return G;
+    }
+    for (int b = 0; b < 32; ++b) {
+        const int64_t mx = map_axis(p.bnd[0], gx + b, p.n1);
+        if (mx < 0) continue;
+        const uint32_t id = (uint32_t)(mx + my * p.n1) + 1u;
+        G |= (uint32_t)draw_below(draw_fast(ds, p.keys, id, 0u), p.gate_thr, p.gate_f32 != 0) << b;
+    }
+    return G;
+}
 
 template <int R>
 struct LifeBits {
@@ -192,9 +246,10 @@ __device__ __forceinline__ void rule_hits(const uint32_t* v, const LifeTables& t
     }
 }
 
-template <int R, int NI, int PL>
+template <int R, int NI, int PL, bool GATED>
 __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw, int ps,
-                                            int w, int r0, int r1, const LifeTables& tb) {
+                                            int w, int r0, int r1, const LifeTables& tb, const SweepParams& p,
+                                            const LifeGate& gt) {
     constexpr int N = LifeBits<R>::N, BH = LifeBits<R>::H, BV = LifeBits<R>::V;
     const uint32_t* ca = A + 1 + w;
     uint32_t* cb = B + 1 + w;
@@ -214,14 +269,20 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
             if (y < r1) {
                 uint32_t dead, live;
                 rule_hits<BV, NI>(v, tb, dead, live);
+                // the gate: open cells take the rule's state, closed ones keep theirs
+                uint32_t G = 0xFFFFFFFFu;
+                if constexpr (GATED) {
+                    if (gt.mode == 1) G = ((gt.Y0 + y + gt.gate) & 1) ? 0xAAAAAAAAu : 0x55555555u;
+                    else if (gt.mode == 2) G = stochastic_gate(p, gt.ds, gt.X0 + 32 * w, gt.Y0 + y);
+                }
                 if constexpr (PL == 1) {
                     const uint32_t c = ca[y * sw];
-                    cb[y * sw] = (c & live) | (~c & dead);
+                    cb[y * sw] = (((c & live) | (~c & dead)) & G) | (c & ~G);
                 } else {  // Generations, state = lo + 2 hi
                     const uint32_t lo = ca[y * sw], hi = ca[y * sw + ps];
                     const uint32_t is0 = ~lo & ~hi, is1 = lo & ~hi, is2 = ~lo & hi;
-                    cb[y * sw] = (is0 & dead) | (is1 & live) | (is2 & tb.c4);
-                    cb[y * sw + ps] = (is1 & ~live & tb.c3) | (is2 & tb.c4);
+                    cb[y * sw] = (((is0 & dead) | (is1 & live) | (is2 & tb.c4)) & G) | (lo & ~G);
+                    cb[y * sw + ps] = (((is1 & ~live & tb.c3) | (is2 & tb.c4)) & G) | (hi & ~G);
                 }
                 if (y + 1 < r1) {
                     vsub<BH, BV>(v, ring[k]);
@@ -300,7 +361,7 @@ __device__ __forceinline__ uint32_t load_plane32(const SweepParams& p, const int
     return bits;
 }
 
-template <int R, int NI, int PL>
+template <int R, int NI, int PL, bool GATED>
 __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g, LifeTables tb,
                                                        const int8_t* __restrict__ src, int8_t* __restrict__ dst) {
     extern __shared__ __align__(16) uint32_t smw[];
@@ -350,7 +411,17 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
                      (p.bnd[1] == GBCA_CONSTANT && (Y0 < 0 || Y0 + g.sy > p.n2));
     __syncthreads();
 
+    LifeGate gt;  // a gated scheme's sub-step gate (the synchronous kernel has none)
+    gt.mode = 0;
+    gt.gate = 0;
+    gt.X0 = X0;
+    gt.Y0 = Y0;
+    if constexpr (GATED) gt.mode = p.scheme == GBCA_CHECKERBOARD ? 1 : (p.scheme == GBCA_STOCHASTIC ? 2 : 0);
     for (int s = 0; s < g.K; ++s) {
+        if constexpr (GATED) {
+            gt.gate = (p.sub0 + s) % p.ngates;
+            if (gt.mode == 2) gt.ds = draw_step(p.keys, p.t0 + (p.sub0 + s) / p.ngates);
+        }
         const int ex = (g.K - 1 - s) * R;
         const int y_lo = g.hy - ex, y_hi = g.hy + g.ty + ex;
         const int w_lo = (32 * g.hw - ex) >> 5, w_hi = (32 * (g.hw + g.tw) + ex + 31) >> 5;
@@ -360,7 +431,7 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
         if (seg < nseg) {
             const int rows = y_hi - y_lo;
             const int r0 = y_lo + (seg * rows) / nseg, r1 = y_lo + ((seg + 1) * rows) / nseg;
-            if (r1 > r0) life_column<R, NI, PL>(A, B, g.sw, ps, w_lo + threadIdx.x % nw, r0, r1, tb);
+            if (r1 > r0) life_column<R, NI, PL, GATED>(A, B, g.sw, ps, w_lo + threadIdx.x % nw, r0, r1, tb, p, gt);
         }
         __syncthreads();
         if (fix) {
@@ -477,15 +548,15 @@ size_t life_smem_bytes(const SweepParams& p, const LifeGeom& g) {
     return 2 * PL * (size_t)g.sw * (size_t)g.sy * 4;
 }
 
-template <int R, int NI, int PL>
+template <int R, int NI, int PL, bool GATED>
 cudaError_t launch_rn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                       cudaStream_t st, int ntiles) {
     const size_t smem = life_smem_bytes(p, g);
-    cudaError_t e = ensure_dynamic_smem((const void*)k_life<R, NI, PL>, smem);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_life<R, NI, PL, GATED>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((p.n1 + 32 * g.tw - 1) / (32 * g.tw)), (unsigned)((p.n2 + g.ty - 1) / g.ty));
     if (ntiles > 0) grid = dim3((unsigned)ntiles, 1u);  // one CTA per listed tile
-    k_life<R, NI, PL><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
+    k_life<R, NI, PL, GATED><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
     return cudaGetLastError();
 }
 
@@ -493,16 +564,39 @@ template <int R, int PL>
 cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                      cudaStream_t st, int ntiles = 0) {
     const int ni = tb.n[0] > tb.n[1] ? tb.n[0] : tb.n[1];
-    if (ni <= 1) return launch_rn<R, 1, PL>(p, g, tb, src, dst, st, ntiles);
-    if (ni <= 2) return launch_rn<R, 2, PL>(p, g, tb, src, dst, st, ntiles);
-    return launch_rn<R, kMaxIntervals, PL>(p, g, tb, src, dst, st, ntiles);
+    if (p.scheme != GBCA_SYNCHRONOUS) {  // gated variants exist for r <= 2 (life_simd_supported)
+        if constexpr (R <= 2) {
+            if (ni <= 1) return launch_rn<R, 1, PL, true>(p, g, tb, src, dst, st, ntiles);
+            if (ni <= 2) return launch_rn<R, 2, PL, true>(p, g, tb, src, dst, st, ntiles);
+            return launch_rn<R, kMaxIntervals, PL, true>(p, g, tb, src, dst, st, ntiles);
+        } else {
+            return cudaErrorNotSupported;
+        }
+    }
+    if (ni <= 1) return launch_rn<R, 1, PL, false>(p, g, tb, src, dst, st, ntiles);
+    if (ni <= 2) return launch_rn<R, 2, PL, false>(p, g, tb, src, dst, st, ntiles);
+    return launch_rn<R, kMaxIntervals, PL, false>(p, g, tb, src, dst, st, ntiles);
 }
 
 }  // namespace
 
 bool life_simd_supported(const SweepParams& p) {
     if (p.mask) return false;
-    if (p.nbhd != GBCA_MOORE || p.radius < 1 || p.scheme != GBCA_SYNCHRONOUS || p.pitch % 16 != 0) return false;
+    if (p.nbhd != GBCA_MOORE || p.radius < 1 || p.pitch % 16 != 0) return false;
+    if (p.scheme == GBCA_CHECKERBOARD) {
+        // the parity mask is the mapped cells' parity only across Constant and even Periodic edges
+        for (int a = 0; a < 2; ++a) {
+            const int64_t n = a == 0 ? p.n1 : p.n2;
+            if (!(p.bnd[a] == GBCA_CONSTANT || (p.bnd[a] == GBCA_PERIODIC && n % 2 == 0))) return false;
+        }
+    } else if (p.scheme == GBCA_STOCHASTIC) {
+        if (p.n1 * p.n2 >= ((int64_t)1 << 32) - 1) return false;  // gate ids in the draws' 32-bit form
+    } else if (p.scheme != GBCA_SYNCHRONOUS) {
+        return false;
+    }
+    if (p.scheme != GBCA_SYNCHRONOUS && p.radius > 2) return false;  // gated kernels: r <= 2
+    // a closed Life cell keeps its value: the indicator bits hold it only for 0 and 1
+    if (p.scheme != GBCA_SYNCHRONOUS && p.rule == GBCA_RULE_LIFE && !p.states_valid) return false;
     if (p.rule == GBCA_RULE_LIFE) {
         if (p.radius > 5) return false;
     } else if (p.rule == GBCA_RULE_GENERATIONS) {
@@ -530,8 +624,8 @@ int life_steps_per_pass(const SweepParams& p) {
 
 // The geometry for a lattice that has no tuned or pinned one: the steps per pass, tile height
 // and tile width that minimise a cost model of one pass per cell-update. A pass costs the
-// busiest SM's CTAs (ceil(CTAs / SMs)) times the work of one CTA, at a per-SM rate, plus a
-// fixed launch cost. A CTA's work is the cells it computes — its tile plus the halo each
+// busiest SM's CTAs (ceil(CTAs / SMs), at least kLifeSatCtas: one 8-warp CTA does not keep an
+// SM busy) times the work of one CTA, at a per-SM rate, plus a fixed launch cost. A CTA's work is the cells it computes — its tile plus the halo each
 // sub-step recomputes, ex = (K - 1 - s) r rows on each side and one word on each side while
 // ex > 0 — plus its loaded region (tile and full halo) at kLifeIoCost cell-steps per cell for
 // packing bytes into bits and unpacking the results; that term favours deep passes. Wide tiles
@@ -543,7 +637,13 @@ SweepChoice life_default_choice(const SweepParams& p0) {
     SweepParams p = p0;
     const int Kmax = life_steps_per_pass(p);
     const int PL = p.rule == GBCA_RULE_GENERATIONS ? 2 : 1;
-    const double rate = 60e9 / (p.radius * PL);  // cell-updates per second per SM (model)
+    // seconds per SM: a cell-step of the bit-sliced rule, plus a Philox gate draw per cell-step
+    // under Stochastic (about 3.3e9 draws per second per SM), and a loaded cell's packing
+    const double rate = 60e9 / (p.radius * PL);
+    const double c_step = 1.0 / rate + (p.scheme == GBCA_STOCHASTIC ? 1.0 / 3.3e9 : 0.0);
+    const double c_io = kLifeIoCost / rate;
+    // CTAs an SM needs to reach that rate: more when each cell-step waits on a draw's long chain
+    const double sat = p.scheme == GBCA_STOCHASTIC ? kLifeSatCtasDraws : kLifeSatCtas;
     const double t_launch = 4e-6;
     const int nsm = device_sms();
     int dev = 0, optin = 0;
@@ -566,16 +666,19 @@ SweepChoice life_default_choice(const SweepParams& p0) {
             for (int ty : tys) {
                 const int tye = p.n2 < ty ? (int)p.n2 : ty;
                 p.tile_x = twe;
-                const LifeGeom g = life_geometry(p, K, tye);
+                const int KS = K * p.ngates;  // sub-steps (two half-steps per Checkerboard step)
+                const LifeGeom g = life_geometry(p, KS, tye);
                 if (life_smem_bytes(p, g) > (size_t)optin) continue;
                 const int64_t ctas = ((words + twe - 1) / twe) * ((p.n2 + tye - 1) / tye);
-                double work = 0.0;  // cell-steps of one CTA over the pass
-                for (int s = 0; s < K; ++s) {
-                    const int ex = (K - 1 - s) * p.radius;
-                    work += 32.0 * (twe + 2 * ((ex + 31) / 32)) * (tye + 2 * ex);
+                double steps = 0.0;  // cell-steps of one CTA over the pass
+                for (int s = 0; s < KS; ++s) {
+                    const int ex = (KS - 1 - s) * p.radius;
+                    steps += 32.0 * (twe + 2 * ((ex + 31) / 32)) * (tye + 2 * ex);
                 }
-                work += kLifeIoCost * 32.0 * (twe + 2 * g.hw) * (tye + 2 * g.hy);
-                const double t = (double)((ctas + nsm - 1) / nsm) * work / rate + t_launch;
+                const double loaded = 32.0 * (twe + 2 * g.hw) * (tye + 2 * g.hy);
+                // an SM reaches its rate with about kLifeSatCtas CTAs resident: fewer leave it idle
+                const double per_sm = (double)((ctas + nsm - 1) / nsm);
+                const double t = (per_sm > sat ? per_sm : sat) * (steps * c_step + loaded * c_io) + t_launch;
                 const double cost = t / ((double)p.n1 * (double)p.n2 * K);
                 if (best_cost < 0.0 || cost < best_cost) {
                     best_cost = cost;
@@ -596,10 +699,12 @@ bool life_choice_fits(const SweepParams& p, int steps, int rows) {
         cudaGetLastError();
         optin = 227 * 1024;
     }
-    return life_smem_bytes(p, life_geometry(p, steps, rows)) <= (size_t)optin;
+    return life_smem_bytes(p, life_geometry(p, steps * p.ngates, rows)) <= (size_t)optin;
 }
 
-cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st) {
+cudaError_t launch_life_simd(const SweepParams& p0, const int8_t* src, int8_t* dst, cudaStream_t st) {
+    SweepParams p = p0;
+    if (p.scheme == GBCA_STOCHASTIC) p.keys = philox_keys(p.seed);  // the gate draws
     LifeTables tb;
     if (!make_tables(p, &tb)) return cudaErrorNotSupported;
     const LifeGeom g = life_geometry(p, p.nsub, p.tile_y);  // tile_y: the autotuner's pick, or 0
@@ -620,8 +725,10 @@ cudaError_t launch_life_simd(const SweepParams& p, const int8_t* src, int8_t* ds
 
 namespace gbca {
 
-cudaError_t launch_life_tiles(const SweepParams& p, const SparseTiles& sp, const int8_t* src, int8_t* dst,
+cudaError_t launch_life_tiles(const SweepParams& p0, const SparseTiles& sp, const int8_t* src, int8_t* dst,
                               cudaStream_t st) {
+    SweepParams p = p0;
+    if (p.scheme == GBCA_STOCHASTIC) p.keys = philox_keys(p.seed);  // the gate draws
     LifeTables tb;
     if (!make_tables(p, &tb)) return cudaErrorNotSupported;
     LifeGeom g;

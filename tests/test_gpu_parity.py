@@ -76,6 +76,28 @@ CASES = [
      dict(nb="vn", birth=[5, 6, 7, 8], survive=[4, 5, 6, 7, 8], scheme="check"), 10, 1, None),
     ("Checkerboard odd torus", "life", (19, 17), dict(nb="vn", birth=[2, 3], survive=[1, 2], scheme="check"), 12, 4,
      None),
+    # gated schemes in the bit-sliced kernel: Checkerboard across Constant and even Periodic edges,
+    # Stochastic on every boundary (gate draws keyed by the mapped cells' ids at the edges)
+    ("Checkerboard Life, even torus, tiled", "life", (200, 150), dict(birth=[3], survive=[2, 3], scheme="check"), 40,
+     8, None),
+    ("Checkerboard Life, Constant grid, odd sides", "life", (75, 61),
+     dict(birth=[3], survive=[2, 3], scheme="check", bnd=("c", "c")), 30, 10, None),
+    ("Checkerboard Life, odd torus (general kernel)", "life", (51, 40),
+     dict(birth=[3], survive=[2, 3], scheme="check"), 20, 5, None),
+    ("Checkerboard Moore(2), even torus x Constant(1)", "life", (128, 90),
+     dict(r=2, birth=[5, 6, 7], survive=[4, 5, 6, 7, 8], scheme="check", bnd=("p", "c"), const=(0, 1)), 25, 25, None),
+    ("Stochastic(0.3) Moore(2) Life, reflecting", "life", (90, 70),
+     dict(r=2, birth=[5, 6, 7], survive=[4, 5, 6, 7, 8], seed=21, scheme="stoch", sp=0.3, bnd=("r", "r")), 30, 6,
+     None),
+    ("Stochastic(0.6f0) Life, tiled torus", "life", (257, 129),
+     dict(birth=[3], survive=[2, 3], seed=22, scheme="stoch", sp=0.6, sp32=True), 40, 40, None),
+    ("Stochastic(0.6) Brian's Brain, tiled torus", "gen", (300, 200),
+     dict(birth=[2], survive=[], states=3, seed=23, scheme="stoch", sp=0.6), 30, 10, None),
+    ("Checkerboard Generations C=4, Constant edges", "gen", (130, 100),
+     dict(birth=[2], survive=[3, 4, 5], states=4, scheme="check", bnd=("c", "c"), const=(1, 2)), 24, 6, None),
+    ("Stochastic(0.5) Generations Moore(2), cylinder", "gen", (160, 96),
+     dict(r=2, birth=[3, 4, 5], survive=[2, 3, 4, 5, 6], states=4, seed=24, scheme="stoch", sp=0.5,
+          bnd=("p", "c"), const=(0, 3)), 20, 4, None),
     ("forest fire, small grid", "fire", (40, 30), dict(nb="vn", seed=3, bnd=("c", "c")), 30, 3, (0.3, 0.01)),
     ("forest fire, Float32 parameters, torus", "fire", (33, 21), dict(nb="vn", seed=5, f32=True), 30, 10,
      (0.3, 0.01)),
@@ -156,6 +178,27 @@ def test_generations_states_outside_range(ca, oracle):
         ca.advance(B, st, prob, ca.Synchronous(), None, t)
     got = ca.current_state(B, st)
     P = oracle.Problem(oracle.RULE_GENERATIONS, 64, 96, birth=oracle.mask([2]), survive=0, states=3)
+    assert np.array_equal(got, oracle.run_array(P, odd, 0, 12))
+    st.close()
+
+
+@pytest.mark.parametrize("scheme", ["stoch", "check"])
+def test_gated_life_states_outside_range(ca, oracle, scheme):
+    """Gated Life on a state holding values other than 0 and 1: a closed cell keeps its value
+    (which the bit-sliced kernel's indicator bits cannot hold), so the sweep runs the general
+    kernel until every state is 0 or 1; the result equals the oracle's throughout."""
+    rng = np.random.default_rng(10)
+    odd = rng.integers(-2, 4, (96, 64)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.Life(":conway"), np.zeros((96, 64), np.int8), 12, seed=31)
+    sch = ca.Stochastic(0.5) if scheme == "stoch" else ca.Checkerboard()
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, sch)
+    ca.set_state(B, st, odd)
+    for t in range(12):
+        ca.advance(B, st, prob, sch, None, t)
+    got = ca.current_state(B, st)
+    P = oracle.Problem(oracle.RULE_LIFE, 96, 64, birth=oracle.mask([3]), survive=oracle.mask([2, 3]), seed=31,
+                       scheme=oracle.STOCHASTIC if scheme == "stoch" else oracle.CHECKERBOARD, scheme_p=0.5)
     assert np.array_equal(got, oracle.run_array(P, odd, 0, 12))
     st.close()
 
