@@ -157,15 +157,27 @@ uint64_t threshold(double p, bool f32) {
 }
 
 // Whether every cell of the current state is one the rule produces — 0..C-1 for Generations,
-// 0..2 for the forest fire — from a device histogram of the state.
+// 0..2 for the forest fire, 0..1 for gated Life — by one byte-compare pass over the state
+// (an HBM-speed read), or from a device histogram where the buffer layout does not allow it.
 cudaError_t scan_states(gbca_handle* h, bool* valid) {
-    cudaError_t e = gbca::launch_measures((const int8_t*)h->buf[h->cur], h->d.n1, h->d.n2, h->pitch,
-                                          h->d.boundary[0], h->d.boundary[1], h->acc, h->nsm, h->stream);
+    const int nv = h->d.rule == GBCA_RULE_GENERATIONS ? h->d.states : (h->d.rule == GBCA_RULE_LIFE ? 2 : 3);
+    const int8_t* u = (const int8_t*)h->buf[h->cur];
+    if (h->pitch % 16 == 0 && ((uintptr_t)u & 15u) == 0) {
+        unsigned int* bad = (unsigned int*)h->acc;
+        cudaError_t e = gbca::launch_states_in_range(u, h->d.n1, h->d.n2, h->pitch, nv, bad, h->nsm, h->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h->acc_host, bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return e;
+        *valid = *(const unsigned int*)h->acc_host == 0u;
+        return cudaSuccess;
+    }
+    cudaError_t e = gbca::launch_measures(u, h->d.n1, h->d.n2, h->pitch, h->d.boundary[0], h->d.boundary[1], h->acc,
+                                          h->nsm, h->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h->acc_host, h->acc, 256 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return e;
-    const int nv = h->d.rule == GBCA_RULE_GENERATIONS ? h->d.states : (h->d.rule == GBCA_RULE_LIFE ? 2 : 3);
     unsigned long long inside = 0;
     for (int v = 0; v < nv && v < 128; ++v) inside += h->acc_host[128 + v];
     *valid = inside == (unsigned long long)(h->d.n1 * h->d.n2);

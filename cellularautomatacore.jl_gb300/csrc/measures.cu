@@ -104,7 +104,48 @@ cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pit
 }
 
 namespace {
+
+// Whether every cell of an Int8 state lies in 0 .. nv - 1: 16-byte chunks of each column,
+// compared byte by byte as unsigned (a negative value is >= 128), the bytes past n1 ignored.
+// Any thread that finds a value outside sets *bad; a warp votes first, so one atomic per warp.
+__global__ void __launch_bounds__(256) k_states_in_range(const int8_t* __restrict__ u, int64_t n1, int64_t n2,
+                                                         int64_t pitch, uint32_t nv, unsigned int* __restrict__ bad) {
+    const int64_t chunks = (n1 + 15) / 16, total = chunks * n2;
+    const uint32_t lim = nv * 0x01010101u;
+    bool found = false;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = q % chunks, j = q / chunks;
+        const int4 v = *(const int4*)(u + j * pitch + 16 * c);
+        const uint32_t w[4] = {(uint32_t)v.x, (uint32_t)v.y, (uint32_t)v.z, (uint32_t)v.w};
+        const int64_t inside = n1 - 16 * c;  // bytes of this chunk inside the lattice (>= 1)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            uint32_t ok = __vcmpltu4(w[k], lim);  // 0xFF in each byte below nv
+            const int64_t nb = inside - 4 * k;    // bytes of this word inside the lattice
+            if (nb < 4) ok |= nb <= 0 ? 0xFFFFFFFFu : (0xFFFFFFFFu << (8 * nb));
+            found = found || ok != 0xFFFFFFFFu;
+        }
+    }
+    if (__any_sync(0xFFFFFFFFu, found) && (threadIdx.x & 31) == 0) atomicOr(bad, 1u);
+}
+
 std::atomic<int64_t> g_launches{0};
+
+}  // namespace
+
+cudaError_t launch_states_in_range(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t nv,
+                                   unsigned int* bad, int nsm, cudaStream_t st) {
+    if (pitch % 16 != 0 || ((uintptr_t)u & 15u) != 0 || nv < 1 || nv > 255) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+    const int64_t total = (n1 + 15) / 16 * n2;
+    int64_t blocks = (total + 255) / 256;
+    const int64_t cap = (int64_t)nsm * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_states_in_range<<<(unsigned)blocks, 256, 0, st>>>(u, n1, n2, pitch, (uint32_t)nv, bad);
+    count_launch();
+    return cudaGetLastError();
 }
 
 void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }

@@ -17,6 +17,12 @@ cudaError_t launch_soup(int8_t* buf, int64_t n1, int64_t n2, int64_t pitch, doub
 cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t b1, int32_t b2,
                             unsigned long long* acc, int nsm, cudaStream_t st);
 
+// *bad = 0 when every cell of the state lies in 0 .. nv - 1 (nv in 1..255), else nonzero.
+// Needs a 16-byte-aligned buffer and pitch; the bytes between n1 and the pitch are not read
+// as cells.
+cudaError_t launch_states_in_range(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t nv,
+                                   unsigned int* bad, int nsm, cudaStream_t st);
+
 // counts[v] for v < nvals, *other = cells outside, *morans from the integer sums
 // (NaN for a constant field). Any output pointer may be null.
 void finish_measures(const unsigned long long* acc, int64_t n, int64_t* counts, int32_t nvals, int64_t* other,
