@@ -257,6 +257,12 @@ void forget_choices();
 // The geometries the autotuner times for a problem (empty: the general kernel, nothing to tune).
 std::vector<SweepChoice> sweep_candidates(const SweepParams& p);
 
+// Sub-steps per pass of the general kernel (steps = this / (r x gates), at least 1): the kernel
+// is compute-bound (shared-memory neighbour reads, per-cell rule), so deep passes, whose halos
+// grow by r per sub-step around a 64 x 64 tile, cost more in recomputed halo than they save in
+// HBM traffic.
+constexpr int kGenericSubsteps = 4;
+
 // Launchers (one translation unit each).
 cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 // The general kernel over the tiles of p.tile_list (grid: the number of tiles of the lattice).

@@ -140,7 +140,7 @@ extern "C" int gbca_advance_noalloc(const gbca_desc* desc, void* state, int64_t 
             p.nsub = (int32_t)k;
             e = launch_life_simd(p, src, dst, st);
         } else {
-            int64_t per = 32 / (p.radius * p.ngates);
+            int64_t per = kGenericSubsteps / (p.radius * p.ngates);
             if (per < 1) per = 1;
             k = nsteps < per ? nsteps : per;
             p.nsub = (int32_t)(k * p.ngates);

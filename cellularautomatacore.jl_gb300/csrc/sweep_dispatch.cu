@@ -76,7 +76,7 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
                 const int64_t cap = sparse->tile_h / (2 * p.radius * p.ngates);
                 if (per > cap) per = cap > 0 ? cap : 1;
             } else {
-                per = 32 / (p.radius * p.ngates);
+                per = kGenericSubsteps / (p.radius * p.ngates);
                 if (per < 1) per = 1;
             }
             const int64_t k = nsteps < per ? nsteps : per;
@@ -126,7 +126,7 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
             p.nsub = (int32_t)(k * p.ngates);  // sub-steps: two half-steps per Checkerboard step
             e = launch_life_simd(p, src, dst, st);
         } else {
-            int64_t per = 32 / (p.radius * p.ngates);
+            int64_t per = kGenericSubsteps / (p.radius * p.ngates);
             if (per < 1) per = 1;
             k = nsteps < per ? nsteps : per;
             p.nsub = (int32_t)(k * p.ngates);

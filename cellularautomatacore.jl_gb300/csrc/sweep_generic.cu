@@ -87,19 +87,24 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
     const bool interior = X0 - hx >= 0 && X0 + p.tile_x + hx <= p.n1 && Y0 - hy >= 0 &&
                           Y0 + p.tile_y + hy <= p.n2;
 
-    for (int idx = threadIdx.x; idx < sx * sy; idx += blockDim.x) {
-        const int lx = idx % sx, ly = idx / sx;
-        const int64_t gx = X0 - hx + lx, gy = Y0 - hy + ly;
-        int8_t v;
-        if (interior) {
-            v = src[gx + gy * p.pitch];
-        } else {
-            const int64_t mx = map_axis(p.bnd[0], gx, p.n1), my = map_axis(p.bnd[1], gy, p.n2);
-            if (my < 0) v = (int8_t)p.cval[1];
-            else if (mx < 0) v = (int8_t)p.cval[0];
-            else v = src[mx + my * p.pitch];
+    // rows to warps, cells of a row to lanes: no division per cell
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int ly = warp; ly < sy; ly += nwarps) {
+        const int64_t gy = Y0 - hy + ly;
+        const int64_t my = interior ? gy : map_axis(p.bnd[1], gy, p.n2);
+        for (int lx = lane; lx < sx; lx += 32) {
+            const int64_t gx = X0 - hx + lx;
+            int8_t v;
+            if (interior) {
+                v = src[gx + gy * p.pitch];
+            } else {
+                const int64_t mx = map_axis(p.bnd[0], gx, p.n1);
+                if (my < 0) v = (int8_t)p.cval[1];
+                else if (mx < 0) v = (int8_t)p.cval[0];
+                else v = src[mx + my * p.pitch];
+            }
+            A[ly * sx + lx] = v;
         }
-        A[idx] = v;
     }
     __syncthreads();
 
@@ -109,8 +114,9 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
         const int ex = (p.nsub - 1 - s) * p.radius;  // margin still needed after this sub-step
         const int x_lo = hx - ex, y_lo = hy - ex;
         const int w = p.tile_x + 2 * ex, h = p.tile_y + 2 * ex;
-        for (int idx = threadIdx.x; idx < w * h; idx += blockDim.x) {
-            const int lx = x_lo + idx % w, ly = y_lo + idx / w;
+        for (int j = warp; j < h; j += nwarps)
+        for (int i = lane; i < w; i += 32) {
+            const int lx = x_lo + i, ly = y_lo + j;
             int64_t mx = X0 - hx + lx, my = Y0 - hy + ly;
             if (!interior) {
                 mx = map_axis(p.bnd[0], mx, p.n1);
@@ -138,15 +144,15 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
     }
 
     int active = 0;
-    for (int idx = threadIdx.x; idx < p.tile_x * p.tile_y; idx += blockDim.x) {
-        const int ox = idx % p.tile_x, oy = idx / p.tile_x;
-        const int64_t gx = X0 + ox, gy = Y0 + oy;
-        if (gx < p.n1 && gy < p.n2) {
-            const int8_t v = A[(hy + oy) * sx + hx + ox];
-            dst[gx + gy * p.pitch] = v;
-            if (TILES) active |= v != (int8_t)p.background;
+    for (int oy = warp; oy < p.tile_y; oy += nwarps)
+        for (int ox = lane; ox < p.tile_x; ox += 32) {
+            const int64_t gx = X0 + ox, gy = Y0 + oy;
+            if (gx < p.n1 && gy < p.n2) {
+                const int8_t v = A[(hy + oy) * sx + hx + ox];
+                dst[gx + gy * p.pitch] = v;
+                if (TILES) active |= v != (int8_t)p.background;
+            }
         }
-    }
     if (TILES) {
         active = __syncthreads_or(active);
         if (threadIdx.x == 0) p.flags_out[tile] = (uint8_t)active;
