@@ -17,9 +17,12 @@ namespace gbca {
 
 namespace {
 
+// RC: the radius when it is known at compile time (1, the common neighbourhoods, whose loops
+// then unroll), 0 to read it from p.
+template <int RC>
 __device__ __forceinline__ int8_t generic_rule(const SweepParams& p, const int8_t* A, int sx, int lx, int ly,
                                                int8_t c, uint64_t id, int64_t t) {
-    const int r = p.radius;
+    const int r = RC > 0 ? RC : p.radius;
     int n = 0;
     bool fire = false;
     if (p.nbhd == GBCA_MOORE) {
@@ -65,7 +68,7 @@ __device__ __forceinline__ int8_t generic_rule(const SweepParams& p, const int8_
     return draw_below(cell_draw(p.seed, id, t, 2), p.thr_f, p.params_f32) ? 2 : 1;
 }
 
-template <bool TILES>
+template <bool TILES, int RC>
 __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __restrict__ src,
                                                  int8_t* __restrict__ dst) {
     extern __shared__ int8_t smem_g[];
@@ -137,7 +140,7 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
                 open = draw_below(cell_draw(p.seed, id, t, 0), p.gate_thr, p.gate_f32);
             else if (p.scheme == GBCA_CHECKERBOARD)
                 open = (((mx + my + 2) & 1) == (gate == 1 ? 1 : 0));
-            B[ly * sx + lx] = open ? generic_rule(p, A, sx, lx, ly, c, id, t) : c;
+            B[ly * sx + lx] = open ? generic_rule<RC>(p, A, sx, lx, ly, c, id, t) : c;
         }
         __syncthreads();
         int8_t* tmp = A; A = B; B = tmp;
@@ -161,27 +164,30 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
 
 }  // namespace
 
-cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st) {
+namespace {
+
+template <bool TILES>
+cudaError_t launch_generic_as(const SweepParams& p, dim3 grid, const int8_t* src, int8_t* dst, cudaStream_t st) {
     const int sx = p.tile_x + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
     const size_t smem = 2 * (size_t)sx * (size_t)sy;
+    void (*fn)(SweepParams, const int8_t*, int8_t*) = p.radius == 1 ? k_generic<TILES, 1> : k_generic<TILES, 0>;
     if (smem > 48 * 1024) {
-        cudaError_t e = ensure_dynamic_smem((const void*)k_generic<false>, smem);
+        cudaError_t e = ensure_dynamic_smem((const void*)fn, smem);
         if (e != cudaSuccess) return e;
     }
-    dim3 grid((unsigned)((p.n1 + p.tile_x - 1) / p.tile_x), (unsigned)((p.n2 + p.tile_y - 1) / p.tile_y));
-    k_generic<false><<<grid, 256, smem, st>>>(p, src, dst);
+    fn<<<grid, 256, smem, st>>>(p, src, dst);
     return cudaGetLastError();
 }
 
+}  // namespace
+
+cudaError_t launch_generic(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st) {
+    const dim3 grid((unsigned)((p.n1 + p.tile_x - 1) / p.tile_x), (unsigned)((p.n2 + p.tile_y - 1) / p.tile_y));
+    return launch_generic_as<false>(p, grid, src, dst, st);
+}
+
 cudaError_t launch_generic_tiles(const SweepParams& p, int ntiles, const int8_t* src, int8_t* dst, cudaStream_t st) {
-    const int sx = p.tile_x + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
-    const size_t smem = 2 * (size_t)sx * (size_t)sy;
-    if (smem > 48 * 1024) {
-        cudaError_t e = ensure_dynamic_smem((const void*)k_generic<true>, smem);
-        if (e != cudaSuccess) return e;
-    }
-    k_generic<true><<<(unsigned)ntiles, 256, smem, st>>>(p, src, dst);
-    return cudaGetLastError();
+    return launch_generic_as<true>(p, dim3((unsigned)ntiles), src, dst, st);
 }
 
 }  // namespace gbca
