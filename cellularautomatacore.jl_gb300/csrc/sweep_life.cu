@@ -1,6 +1,7 @@
 // sweep_life.cu — Life-like and Larger-than-Life rules (src/rules.jl:354-389) on Moore(r),
-// r = 1..5, and Generations rules with up to 4 states on Moore(1..2), Synchronous, as a
-// bit-sliced, temporally blocked sweep.
+// r = 1..5, and von Neumann(1), and Generations rules with up to 4 states on Moore(1..2) and
+// von Neumann(1), Synchronous, Stochastic(p) or Checkerboard (r <= 2), as a bit-sliced,
+// temporally blocked sweep.
 //
 // Layout. Global memory keeps the user's Int8 column-major state. A CTA stages its tile
 // plus a halo of K*r cells in shared memory as ONE BIT PER CELL: bit b of word w of a
@@ -14,7 +15,8 @@
 // neighbour words) and adds them with a full-adder tree into a bit-sliced count Hx
 // (2-4 bit planes); a register ring keeps the last 2r+1 Hx rows and a bit-sliced running
 // sum V = sum of Hx over rows y-r..y+r is updated by one add and one subtract per row.
-// V is the Moore box count including the centre.
+// V is the Moore box count including the centre. Von Neumann(1) needs no ring: a row's count
+// is its 3-cell horizontal count plus the words above and below.
 //
 // Rule. A dead cell is born when V lies in one of the birth intervals, a live cell
 // survives when V - 1 lies in a survive interval, i.e. V in the interval shifted by one.
@@ -246,13 +248,64 @@ __device__ __forceinline__ void rule_hits(const uint32_t* v, const LifeTables& t
     }
 }
 
-template <int R, int NI, int PL, bool GATED>
+// The next state of word column w, row y, from its bit-sliced count v (centre included): the
+// rule's birth / survival tests, the gate, and the write to B.
+template <int BV, int NI, int PL, bool GATED>
+__device__ __forceinline__ void life_emit(const uint32_t* v, const uint32_t* ca, uint32_t* cb, int y, int sw, int ps,
+                                          int w, const LifeTables& tb, const SweepParams& p, const LifeGate& gt) {
+    uint32_t dead, live;
+    rule_hits<BV, NI>(v, tb, dead, live);
+    // the gate: open cells take the rule's state, closed ones keep theirs
+    uint32_t G = 0xFFFFFFFFu;
+    if constexpr (GATED) {
+        if (gt.mode == 1) G = ((gt.Y0 + y + gt.gate) & 1) ? 0xAAAAAAAAu : 0x55555555u;
+        else if (gt.mode == 2) G = stochastic_gate(p, gt.ds, gt.X0 + 32 * w, gt.Y0 + y);
+    }
+    if constexpr (PL == 1) {
+        const uint32_t c = ca[y * sw];
+        cb[y * sw] = (((c & live) | (~c & dead)) & G) | (c & ~G);
+    } else {  // Generations, state = lo + 2 hi
+        const uint32_t lo = ca[y * sw], hi = ca[y * sw + ps];
+        const uint32_t is0 = ~lo & ~hi, is1 = lo & ~hi, is2 = ~lo & hi;
+        cb[y * sw] = (((is0 & dead) | (is1 & live) | (is2 & tb.c4)) & G) | (lo & ~G);
+        cb[y * sw + ps] = (((is1 & ~live & tb.c3) | (is2 & tb.c4)) & G) | (hi & ~G);
+    }
+}
+
+// The alive bits of a word (Life: the indicator; Generations: state 1, lo & ~hi).
+template <int PL>
+__device__ __forceinline__ uint32_t alive_word(const uint32_t* q, int ps) {
+    if constexpr (PL == 1) return q[0];
+    else return q[0] & ~q[ps];
+}
+
+// One sub-step of word column w over rows [r0, r1). Moore(R): a ring of the last 2R+1 rows'
+// horizontal counts and their running vertical sum. VN (von Neumann(1)): each row's count is its
+// 3-cell horizontal count plus the cells above and below.
+template <int R, int NI, int PL, bool GATED, bool VN>
 __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw, int ps,
                                             int w, int r0, int r1, const LifeTables& tb, const SweepParams& p,
                                             const LifeGate& gt) {
     constexpr int N = LifeBits<R>::N, BH = LifeBits<R>::H, BV = LifeBits<R>::V;
     const uint32_t* ca = A + 1 + w;
     uint32_t* cb = B + 1 + w;
+    if constexpr (VN) {
+        static_assert(R == 1, "von Neumann: radius 1");
+        for (int y = r0; y < r1; ++y) {
+            uint32_t h[2];
+            hrow<1, PL>(ca + y * sw, ps, h);  // cells x - 1, x, x + 1: h0 + 2 h1
+            const uint32_t up = alive_word<PL>(ca + (y - 1) * sw, ps), dn = alive_word<PL>(ca + (y + 1) * sw, ps);
+            const uint32_t s1 = up ^ dn, c1 = up & dn, k0 = h[0] & s1;
+            uint32_t v[BV];
+            v[0] = h[0] ^ s1;
+            v[1] = h[1] ^ c1 ^ k0;
+            v[2] = maj3(h[1], c1, k0);
+#pragma unroll
+            for (int i = 3; i < BV; ++i) v[i] = 0u;
+            life_emit<BV, NI, PL, GATED>(v, ca, cb, y, sw, ps, w, tb, p, gt);
+        }
+        return;
+    }
     uint32_t ring[N][BH];
     uint32_t v[BV];
 #pragma unroll
@@ -267,23 +320,7 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
         for (int k = 0; k < N; ++k) {
             const int y = y0 + k;
             if (y < r1) {
-                uint32_t dead, live;
-                rule_hits<BV, NI>(v, tb, dead, live);
-                // the gate: open cells take the rule's state, closed ones keep theirs
-                uint32_t G = 0xFFFFFFFFu;
-                if constexpr (GATED) {
-                    if (gt.mode == 1) G = ((gt.Y0 + y + gt.gate) & 1) ? 0xAAAAAAAAu : 0x55555555u;
-                    else if (gt.mode == 2) G = stochastic_gate(p, gt.ds, gt.X0 + 32 * w, gt.Y0 + y);
-                }
-                if constexpr (PL == 1) {
-                    const uint32_t c = ca[y * sw];
-                    cb[y * sw] = (((c & live) | (~c & dead)) & G) | (c & ~G);
-                } else {  // Generations, state = lo + 2 hi
-                    const uint32_t lo = ca[y * sw], hi = ca[y * sw + ps];
-                    const uint32_t is0 = ~lo & ~hi, is1 = lo & ~hi, is2 = ~lo & hi;
-                    cb[y * sw] = (((is0 & dead) | (is1 & live) | (is2 & tb.c4)) & G) | (lo & ~G);
-                    cb[y * sw + ps] = (((is1 & ~live & tb.c3) | (is2 & tb.c4)) & G) | (hi & ~G);
-                }
+                life_emit<BV, NI, PL, GATED>(v, ca, cb, y, sw, ps, w, tb, p, gt);
                 if (y + 1 < r1) {
                     vsub<BH, BV>(v, ring[k]);
                     hrow<R, PL>(ca + (y + R + 1) * sw, ps, ring[k]);
@@ -293,7 +330,6 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
         }
     }
 }
-
 // Indicator bits (byte == 1) of 4 bytes, in bits 0..3.
 __device__ __forceinline__ uint32_t ones4(uint32_t w) {
     const uint32_t t = w ^ 0x01010101u;
@@ -361,7 +397,7 @@ __device__ __forceinline__ uint32_t load_plane32(const SweepParams& p, const int
     return bits;
 }
 
-template <int R, int NI, int PL, bool GATED>
+template <int R, int NI, int PL, bool GATED, bool VN>
 __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g, LifeTables tb,
                                                        const int8_t* __restrict__ src, int8_t* __restrict__ dst) {
     extern __shared__ __align__(16) uint32_t smw[];
@@ -431,7 +467,8 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
         if (seg < nseg) {
             const int rows = y_hi - y_lo;
             const int r0 = y_lo + (seg * rows) / nseg, r1 = y_lo + ((seg + 1) * rows) / nseg;
-            if (r1 > r0) life_column<R, NI, PL, GATED>(A, B, g.sw, ps, w_lo + threadIdx.x % nw, r0, r1, tb, p, gt);
+            if (r1 > r0)
+                life_column<R, NI, PL, GATED, VN>(A, B, g.sw, ps, w_lo + threadIdx.x % nw, r0, r1, tb, p, gt);
         }
         __syncthreads();
         if (fix) {
@@ -548,41 +585,42 @@ size_t life_smem_bytes(const SweepParams& p, const LifeGeom& g) {
     return 2 * PL * (size_t)g.sw * (size_t)g.sy * 4;
 }
 
-template <int R, int NI, int PL, bool GATED>
+template <int R, int NI, int PL, bool GATED, bool VN>
 cudaError_t launch_rn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                       cudaStream_t st, int ntiles) {
     const size_t smem = life_smem_bytes(p, g);
-    cudaError_t e = ensure_dynamic_smem((const void*)k_life<R, NI, PL, GATED>, smem);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_life<R, NI, PL, GATED, VN>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((p.n1 + 32 * g.tw - 1) / (32 * g.tw)), (unsigned)((p.n2 + g.ty - 1) / g.ty));
     if (ntiles > 0) grid = dim3((unsigned)ntiles, 1u);  // one CTA per listed tile
-    k_life<R, NI, PL, GATED><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
+    k_life<R, NI, PL, GATED, VN><<<grid, kLifeThreads, smem, st>>>(p, g, tb, src, dst);
     return cudaGetLastError();
 }
 
-template <int R, int PL>
+template <int R, int PL, bool VN = false>
 cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                      cudaStream_t st, int ntiles = 0) {
     const int ni = tb.n[0] > tb.n[1] ? tb.n[0] : tb.n[1];
     if (p.scheme != GBCA_SYNCHRONOUS) {  // gated variants exist for r <= 2 (life_simd_supported)
         if constexpr (R <= 2) {
-            if (ni <= 1) return launch_rn<R, 1, PL, true>(p, g, tb, src, dst, st, ntiles);
-            if (ni <= 2) return launch_rn<R, 2, PL, true>(p, g, tb, src, dst, st, ntiles);
-            return launch_rn<R, kMaxIntervals, PL, true>(p, g, tb, src, dst, st, ntiles);
+            if (ni <= 1) return launch_rn<R, 1, PL, true, VN>(p, g, tb, src, dst, st, ntiles);
+            if (ni <= 2) return launch_rn<R, 2, PL, true, VN>(p, g, tb, src, dst, st, ntiles);
+            return launch_rn<R, kMaxIntervals, PL, true, VN>(p, g, tb, src, dst, st, ntiles);
         } else {
             return cudaErrorNotSupported;
         }
     }
-    if (ni <= 1) return launch_rn<R, 1, PL, false>(p, g, tb, src, dst, st, ntiles);
-    if (ni <= 2) return launch_rn<R, 2, PL, false>(p, g, tb, src, dst, st, ntiles);
-    return launch_rn<R, kMaxIntervals, PL, false>(p, g, tb, src, dst, st, ntiles);
+    if (ni <= 1) return launch_rn<R, 1, PL, false, VN>(p, g, tb, src, dst, st, ntiles);
+    if (ni <= 2) return launch_rn<R, 2, PL, false, VN>(p, g, tb, src, dst, st, ntiles);
+    return launch_rn<R, kMaxIntervals, PL, false, VN>(p, g, tb, src, dst, st, ntiles);
 }
 
 }  // namespace
 
 bool life_simd_supported(const SweepParams& p) {
     if (p.mask) return false;
-    if (p.nbhd != GBCA_MOORE || p.radius < 1 || p.pitch % 16 != 0) return false;
+    if (p.radius < 1 || p.pitch % 16 != 0) return false;
+    if (p.nbhd != GBCA_MOORE && !(p.nbhd == GBCA_VON_NEUMANN && p.radius == 1)) return false;
     if (p.scheme == GBCA_CHECKERBOARD) {
         // the parity mask is the mapped cells' parity only across Constant and even Periodic edges
         for (int a = 0; a < 2; ++a) {
@@ -708,6 +746,10 @@ cudaError_t launch_life_simd(const SweepParams& p0, const int8_t* src, int8_t* d
     LifeTables tb;
     if (!make_tables(p, &tb)) return cudaErrorNotSupported;
     const LifeGeom g = life_geometry(p, p.nsub, p.tile_y);  // tile_y: the autotuner's pick, or 0
+    if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1 (life_simd_supported)
+        if (p.rule == GBCA_RULE_GENERATIONS) return launch_r<1, 2, true>(p, g, tb, src, dst, st);
+        return launch_r<1, 1, true>(p, g, tb, src, dst, st);
+    }
     if (p.rule == GBCA_RULE_GENERATIONS) {
         if (p.radius == 1) return launch_r<1, 2>(p, g, tb, src, dst, st);
         return launch_r<2, 2>(p, g, tb, src, dst, st);
@@ -740,6 +782,10 @@ cudaError_t launch_life_tiles(const SweepParams& p0, const SparseTiles& sp, cons
     g.sw = g.tw + 2 * g.hw + 2;
     g.sy = g.ty + 2 * g.hy;
     const int n = sp.tiles_x * sp.tiles_y;
+    if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1 (life_simd_supported)
+        if (p.rule == GBCA_RULE_GENERATIONS) return launch_r<1, 2, true>(p, g, tb, src, dst, st, n);
+        return launch_r<1, 1, true>(p, g, tb, src, dst, st, n);
+    }
     if (p.rule == GBCA_RULE_GENERATIONS) {
         if (p.radius == 1) return launch_r<1, 2>(p, g, tb, src, dst, st, n);
         return launch_r<2, 2>(p, g, tb, src, dst, st, n);

@@ -98,6 +98,15 @@ CASES = [
     ("Stochastic(0.5) Generations Moore(2), cylinder", "gen", (160, 96),
      dict(r=2, birth=[3, 4, 5], survive=[2, 3, 4, 5, 6], states=4, seed=24, scheme="stoch", sp=0.5,
           bnd=("p", "c"), const=(0, 3)), 20, 4, None),
+    # von Neumann(1) in the bit-sliced kernel: the row's 3-cell count plus the cells above and below
+    ("von Neumann(1) Life-like, tiled torus", "life", (300, 200), dict(nb="vn", birth=[2], survive=[1, 2]), 40, 8,
+     None),
+    ("von Neumann(1) majority, Checkerboard, Constant grid", "life", (129, 77),
+     dict(nb="vn", birth=[3, 4], survive=[2, 3, 4], scheme="check", bnd=("c", "c"), const=(0, 1)), 30, 10, None),
+    ("von Neumann(1) Generations C=3, reflecting", "gen", (150, 90),
+     dict(nb="vn", birth=[2], survive=[1], states=3, bnd=("r", "r")), 30, 10, None),
+    ("von Neumann(1) Stochastic(0.4), cylinder", "life", (200, 64),
+     dict(nb="vn", birth=[1, 3], survive=[2, 3], seed=41, scheme="stoch", sp=0.4, bnd=("p", "c")), 25, 5, None),
     ("forest fire, small grid", "fire", (40, 30), dict(nb="vn", seed=3, bnd=("c", "c")), 30, 3, (0.3, 0.01)),
     ("forest fire, Float32 parameters, torus", "fire", (33, 21), dict(nb="vn", seed=5, f32=True), 30, 10,
      (0.3, 0.01)),
