@@ -36,9 +36,9 @@
 //
 // Gated schemes (src/schemes.jl:84-93): a sub-step's new bits are blended with the old ones
 // through a gate mask, so a closed cell keeps its state. Checkerboard runs two half-steps per
-// step, the cells with (x + y) even and then odd (0-based): the mask alternates by bit and row,
-// which matches the mapped cells' parity for halos beyond a Constant edge (reset anyway) or a
-// Periodic edge of even length, the only boundaries it runs here. Stochastic(p) opens cell
+// step, the cells with (x + y) even and then odd (0-based): the mask alternates by bit and row
+// inside the lattice, and halo words take the parity of the cells they image (a Reflecting
+// edge or a Periodic one of odd length flips it). Stochastic(p) opens cell
 // (x, y) when its draw k = 0 at time t falls below p, the draw keyed by the mapped cell's id as
 // in the rule's own draws. A closed Life cell keeps its value, which the indicator bits hold
 // only for states 0 and 1, so gated Life needs every state in {0, 1} (the host scans it).
@@ -71,16 +71,29 @@ struct LifeGeom {
 // Stochastic draws at the sub-step's time), with the lattice position of local cell 0.
 struct LifeGate {
     int32_t mode, gate;
+    bool rows_plain;  // Checkerboard: rows need no mapping for their parity (checker_gate)
     int64_t X0, Y0;
     DrawStep ds;
 };
+
+// map_axis for an index at most one lattice length beyond an edge (the halo of a pass), without
+// a division: one wrap (Periodic) or one reflection; anything farther goes to map_axis.
+__device__ __forceinline__ int64_t map_near(int32_t b, int64_t g, int64_t n) {
+    if ((uint64_t)g < (uint64_t)n) return g;
+    if (b == GBCA_CONSTANT) return -1;
+    if (g >= -n && g < 2 * n) {
+        if (b == GBCA_PERIODIC) return g < 0 ? g + n : g - n;
+        return g < 0 ? -g - 1 : 2 * n - 1 - g;  // Reflecting
+    }
+    return map_axis(b, g, n);
+}
 
 // The Stochastic gate of the 32 cells x = gx .. gx + 31 of lattice row y: bit b open when the
 // draw k = 0 of the mapped cell falls below p. Cells beyond a Constant edge get a closed bit
 // (the Constant reset overwrites them after the sub-step anyway).
 __device__ __forceinline__ uint32_t stochastic_gate(const SweepParams& p, const DrawStep& ds, int64_t gx, int64_t y) {
     uint32_t G = 0;
-    const int64_t my = map_axis(p.bnd[1], y, p.n2);
+    const int64_t my = map_near(p.bnd[1], y, p.n2);
     if (my < 0) return 0u;
     if (gx >= 0 && gx + 32 <= p.n1) {
         const uint32_t base = (uint32_t)(gx + my * p.n1) + 1u;
@@ -102,12 +115,61 @@ __device__ __forceinline__ uint32_t stochastic_gate(const SweepParams& p, const 
         return G;
     }
     for (int b = 0; b < 32; ++b) {
-        const int64_t mx = map_axis(p.bnd[0], gx + b, p.n1);
+        const int64_t mx = map_near(p.bnd[0], gx + b, p.n1);
         if (mx < 0) continue;
         const uint32_t id = (uint32_t)(mx + my * p.n1) + 1u;
         G |= (uint32_t)draw_below(draw_fast(ds, p.keys, id, 0u), p.gate_thr, p.gate_f32 != 0) << b;
     }
     return G;
+}
+
+// The Checkerboard gate of the 32 cells x = gx .. gx + 31 (gx a multiple of 32) of lattice row
+// y in half-step `gate`: bit b open when the mapped cell's (x + y) is even for gate 0, odd for
+// gate 1 (0-based, as isodd(i + j) with 1-based indices, src/schemes.jl:89). Inside the lattice
+// the mask alternates by bit. A cell one lattice length or less beyond an edge images a cell of
+// the same parity across a Periodic edge of even length, of the other parity across a Periodic
+// edge of odd length or a Reflecting edge (x and -x-1, or 2n-1-x); beyond a Constant edge its
+// bit is closed (the cell is reset to the constant after the sub-step). So a word column's gate
+// is the alternating mask with fixed bits flipped (`flip`) and cleared (`keep`), set once per
+// column; a row only maps its y and picks the mask by parity.
+struct CheckerCol {
+    uint32_t keep, flip;
+    bool exact;  // a lattice narrower than the halo: map cell by cell (checker_gate_exact)
+};
+
+__device__ __forceinline__ CheckerCol checker_col(const SweepParams& p, int64_t gx) {
+    CheckerCol c{0xFFFFFFFFu, 0u, false};
+    if (gx >= 0 && gx + 32 <= p.n1) return c;
+    uint32_t out = 0;  // bits of cells beyond either edge
+    if (gx < 0) out |= -gx >= 32 ? 0xFFFFFFFFu : ((1u << (int)(-gx)) - 1u);
+    if (gx + 32 > p.n1) out |= p.n1 - gx <= 0 ? 0xFFFFFFFFu : (0xFFFFFFFFu << (int)(p.n1 - gx));
+    if (p.bnd[0] == GBCA_CONSTANT) c.keep = ~out;
+    else if (gx >= -p.n1 && gx + 32 <= 2 * p.n1) c.flip = (p.bnd[0] == GBCA_REFLECTING || (p.n1 & 1)) ? out : 0u;
+    else c.exact = true;
+    return c;
+}
+
+__device__ __noinline__ uint32_t checker_gate_exact(int32_t b0, int64_t n1, int64_t gx, int64_t my, int gate) {
+    uint32_t G = 0;
+    for (int b = 0; b < 32; ++b) {
+        const int64_t mx = map_axis(b0, gx + b, n1);
+        if (mx >= 0 && ((mx + my) & 1) == gate) G |= 1u << b;
+    }
+    return G;
+}
+
+// rows_plain: every row images a row of its own parity or lies beyond a Constant edge (axis 2
+// Constant, or Periodic of even length), so a row's parity is its own and needs no mapping.
+__device__ __forceinline__ uint32_t checker_gate(const SweepParams& p, const CheckerCol& c, bool rows_plain,
+                                                 int64_t gx, int64_t y, int gate) {
+    int64_t my = y;
+    if (!rows_plain) {
+        my = map_near(p.bnd[1], y, p.n2);
+        if (my < 0) return 0u;
+    }
+    if (c.exact) return checker_gate_exact(p.bnd[0], p.n1, gx, my, gate);
+    const uint32_t base = ((my + gate) & 1) ? 0xAAAAAAAAu : 0x55555555u;  // gx is even
+    return (base ^ c.flip) & c.keep;
 }
 
 template <int R>
@@ -252,13 +314,14 @@ __device__ __forceinline__ void rule_hits(const uint32_t* v, const LifeTables& t
 // rule's birth / survival tests, the gate, and the write to B.
 template <int BV, int NI, int PL, bool GATED>
 __device__ __forceinline__ void life_emit(const uint32_t* v, const uint32_t* ca, uint32_t* cb, int y, int sw, int ps,
-                                          int w, const LifeTables& tb, const SweepParams& p, const LifeGate& gt) {
+                                          int w, const LifeTables& tb, const SweepParams& p, const LifeGate& gt,
+                                          const CheckerCol& cc) {
     uint32_t dead, live;
     rule_hits<BV, NI>(v, tb, dead, live);
     // the gate: open cells take the rule's state, closed ones keep theirs
     uint32_t G = 0xFFFFFFFFu;
     if constexpr (GATED) {
-        if (gt.mode == 1) G = ((gt.Y0 + y + gt.gate) & 1) ? 0xAAAAAAAAu : 0x55555555u;
+        if (gt.mode == 1) G = checker_gate(p, cc, gt.rows_plain, gt.X0 + 32 * w, gt.Y0 + y, gt.gate);
         else if (gt.mode == 2) G = stochastic_gate(p, gt.ds, gt.X0 + 32 * w, gt.Y0 + y);
     }
     if constexpr (PL == 1) {
@@ -289,6 +352,10 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
     constexpr int N = LifeBits<R>::N, BH = LifeBits<R>::H, BV = LifeBits<R>::V;
     const uint32_t* ca = A + 1 + w;
     uint32_t* cb = B + 1 + w;
+    CheckerCol cc{0xFFFFFFFFu, 0u, false};  // the column's Checkerboard mask adjustments
+    if constexpr (GATED) {
+        if (gt.mode == 1) cc = checker_col(p, gt.X0 + 32 * w);
+    }
     if constexpr (VN) {
         static_assert(R == 1, "von Neumann: radius 1");
         for (int y = r0; y < r1; ++y) {
@@ -302,7 +369,7 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
             v[2] = maj3(h[1], c1, k0);
 #pragma unroll
             for (int i = 3; i < BV; ++i) v[i] = 0u;
-            life_emit<BV, NI, PL, GATED>(v, ca, cb, y, sw, ps, w, tb, p, gt);
+            life_emit<BV, NI, PL, GATED>(v, ca, cb, y, sw, ps, w, tb, p, gt, cc);
         }
         return;
     }
@@ -320,7 +387,7 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
         for (int k = 0; k < N; ++k) {
             const int y = y0 + k;
             if (y < r1) {
-                life_emit<BV, NI, PL, GATED>(v, ca, cb, y, sw, ps, w, tb, p, gt);
+                life_emit<BV, NI, PL, GATED>(v, ca, cb, y, sw, ps, w, tb, p, gt, cc);
                 if (y + 1 < r1) {
                     vsub<BH, BV>(v, ring[k]);
                     hrow<R, PL>(ca + (y + R + 1) * sw, ps, ring[k]);
@@ -450,6 +517,7 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
     LifeGate gt;  // a gated scheme's sub-step gate (the synchronous kernel has none)
     gt.mode = 0;
     gt.gate = 0;
+    gt.rows_plain = p.bnd[1] == GBCA_CONSTANT || (p.bnd[1] == GBCA_PERIODIC && (p.n2 & 1) == 0);
     gt.X0 = X0;
     gt.Y0 = Y0;
     if constexpr (GATED) gt.mode = p.scheme == GBCA_CHECKERBOARD ? 1 : (p.scheme == GBCA_STOCHASTIC ? 2 : 0);
@@ -622,11 +690,7 @@ bool life_simd_supported(const SweepParams& p) {
     if (p.radius < 1 || p.pitch % 16 != 0) return false;
     if (p.nbhd != GBCA_MOORE && !(p.nbhd == GBCA_VON_NEUMANN && p.radius == 1)) return false;
     if (p.scheme == GBCA_CHECKERBOARD) {
-        // the parity mask is the mapped cells' parity only across Constant and even Periodic edges
-        for (int a = 0; a < 2; ++a) {
-            const int64_t n = a == 0 ? p.n1 : p.n2;
-            if (!(p.bnd[a] == GBCA_CONSTANT || (p.bnd[a] == GBCA_PERIODIC && n % 2 == 0))) return false;
-        }
+        // any boundary: the gate maps halo cells to the cells they image (checker_gate)
     } else if (p.scheme == GBCA_STOCHASTIC) {
         if (p.n1 * p.n2 >= ((int64_t)1 << 32) - 1) return false;  // gate ids in the draws' 32-bit form
     } else if (p.scheme != GBCA_SYNCHRONOUS) {

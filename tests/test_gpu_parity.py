@@ -82,8 +82,11 @@ CASES = [
      8, None),
     ("Checkerboard Life, Constant grid, odd sides", "life", (75, 61),
      dict(birth=[3], survive=[2, 3], scheme="check", bnd=("c", "c")), 30, 10, None),
-    ("Checkerboard Life, odd torus (general kernel)", "life", (51, 40),
-     dict(birth=[3], survive=[2, 3], scheme="check"), 20, 5, None),
+    ("Checkerboard Life, odd torus", "life", (51, 40), dict(birth=[3], survive=[2, 3], scheme="check"), 20, 5, None),
+    ("Checkerboard Life, odd x reflecting, tiled", "life", (301, 133),
+     dict(birth=[3], survive=[2, 3], scheme="check", bnd=("p", "r")), 30, 10, None),
+    ("Checkerboard Generations Moore(2), reflecting x odd torus", "gen", (96, 75),
+     dict(r=2, birth=[3, 4], survive=[2, 3, 4, 5], states=3, scheme="check", bnd=("r", "p")), 20, 5, None),
     ("Checkerboard Moore(2), even torus x Constant(1)", "life", (128, 90),
      dict(r=2, birth=[5, 6, 7], survive=[4, 5, 6, 7, 8], scheme="check", bnd=("p", "c"), const=(0, 1)), 25, 25, None),
     ("Stochastic(0.3) Moore(2) Life, reflecting", "life", (90, 70),
