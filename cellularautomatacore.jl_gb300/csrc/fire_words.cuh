@@ -181,11 +181,30 @@ __device__ __forceinline__ void fire_substep_words(const uint32_t* __restrict__ 
 // nw <= nthr; threads past the last whole run stay idle. Every word's first cell lies inside
 // the lattice; with CHECKED the last word of a row may reach past column n1, and only its
 // cells inside are stored.
-template <bool CHECKED, bool EXACT>
+// A one-step sweep's gate and mask (src/schemes.jl:84-93, src/environment.jl:123-130): a closed
+// or masked cell keeps its state. mode 0: every cell updates; 1: Checkerboard half-step `gate`
+// (cells with (x + y) even for gate 0, odd for gate 1); 2: Stochastic, a cell opens when its draw
+// k = 0 falls below the raw threshold Ug (or always, allg). mask: nonzero bytes update (pitch
+// mpitch between columns), or null.
+struct FireGate {
+    int32_t mode, gate;
+    uint64_t Ug;
+    bool allg;
+    const uint8_t* mask;
+    int64_t mpitch;
+};
+
+// Bytes of w that are nonzero, as 0xFF bytes.
+__device__ __forceinline__ uint32_t bytes_nonzero(uint32_t w) {
+    const uint32_t hi = (w | ((w & 0x7F7F7F7Fu) + 0x7F7F7F7Fu)) & 0x80808080u;
+    return (hi >> 7) * 0xFFu;
+}
+
+template <bool CHECKED, bool EXACT, bool GATED>
 __device__ __forceinline__ void fire_substep_rows_t(const uint32_t* __restrict__ A, int sw, int w_lo, int nw, int y_lo,
                                                     int nrows, int64_t gx0, int64_t gy0, const FireGeom& g,
                                                     const DrawStep& ds, const PhiloxKeys& K, int tid, int nthr,
-                                                    int8_t* __restrict__ gdst, int64_t gpitch) {
+                                                    int8_t* __restrict__ gdst, int64_t gpitch, const FireGate* fg) {
     const int nseg = nthr / nw, seg = tid / nw;
     if (seg >= nseg) return;
     const int r0 = y_lo + (int)(((int64_t)seg * nrows) / nseg), r1 = y_lo + (int)(((int64_t)(seg + 1) * nrows) / nseg);
@@ -199,17 +218,32 @@ __device__ __forceinline__ void fire_substep_rows_t(const uint32_t* __restrict__
     for (int b = 0; b < 4; ++b) mx[b] = (uint32_t)gx + b;
     int o = r0 * sw + lw;
     uint32_t Up = A[o - sw], C = A[o];
-    const int64_t gy = gy0 + r0;
+    int64_t gy = gy0 + r0;
     uint32_t base = (uint32_t)gy * n1 + 1u;  // id of the row's cell 0
     int8_t* q = gdst + gx + gy * gpitch;
     const int64_t xin = g.n1 - gx;  // cells of this word inside the lattice (>= 1)
-    for (int ly = r0; ly < r1; ++ly, o += sw, q += gpitch, base += n1) {
+    for (int ly = r0; ly < r1; ++ly, o += sw, q += gpitch, base += n1, ++gy) {
         const uint32_t Dn = A[o + sw], Wl = A[o - 1], Wr = A[o + 1];
         const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
         const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
         uint32_t E, T, N;
         fire_masks<EXACT>(C, Lf, Rt, Up, Dn, E, T, N);
-        const uint32_t res = fire_next(E, T, N, base, mx, g, ds, K);
+        uint32_t res = fire_next(E, T, N, base, mx, g, ds, K);
+        if constexpr (GATED) {  // open bytes take the rule's state, closed and masked ones keep theirs
+            uint32_t Gb = 0xFFFFFFFFu;
+            if (fg->mode == 1) {
+                Gb = ((gy + fg->gate) & 1) ? 0xFF00FF00u : 0x00FF00FFu;  // gx is even
+            } else if (fg->mode == 2 && !fg->allg) {
+                Gb = 0u;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const uint2 w = draw_fast(ds, K, base + mx[b], 0u);
+                    if ((((uint64_t)w.x << 32) | (uint64_t)w.y) < fg->Ug) Gb |= 0xFFu << (8 * b);
+                }
+            }
+            if (fg->mask) Gb &= bytes_nonzero(*(const uint32_t*)(fg->mask + gx + gy * fg->mpitch));
+            res = (res & Gb) | (C & ~Gb);
+        }
         if (!CHECKED || xin >= 4) {
             *(uint32_t*)q = res;
         } else {
@@ -220,15 +254,33 @@ __device__ __forceinline__ void fire_substep_rows_t(const uint32_t* __restrict__
     }
 }
 
-template <bool CHECKED>
+// GATED: the sweep has a gate or a mask (fg), compiled apart from the synchronous, unmasked one.
+template <bool CHECKED, bool GATED = false>
 __device__ __forceinline__ void fire_substep_rows(const uint32_t* __restrict__ A, int sw, int w_lo, int nw, int y_lo,
                                                   int nrows, int64_t gx0, int64_t gy0, const FireGeom& g,
                                                   const DrawStep& ds, const PhiloxKeys& K, int tid, int nthr,
-                                                  bool exact, int8_t* __restrict__ gdst, int64_t gpitch) {
+                                                  bool exact, int8_t* __restrict__ gdst, int64_t gpitch,
+                                                  const FireGate* fg = nullptr) {
     if (exact || g.exact_always)
-        fire_substep_rows_t<CHECKED, true>(A, sw, w_lo, nw, y_lo, nrows, gx0, gy0, g, ds, K, tid, nthr, gdst, gpitch);
+        fire_substep_rows_t<CHECKED, true, GATED>(A, sw, w_lo, nw, y_lo, nrows, gx0, gy0, g, ds, K, tid, nthr, gdst,
+                                                  gpitch, fg);
     else
-        fire_substep_rows_t<CHECKED, false>(A, sw, w_lo, nw, y_lo, nrows, gx0, gy0, g, ds, K, tid, nthr, gdst, gpitch);
+        fire_substep_rows_t<CHECKED, false, GATED>(A, sw, w_lo, nw, y_lo, nrows, gx0, gy0, g, ds, K, tid, nthr, gdst,
+                                                   gpitch, fg);
+}
+
+// The gate of a one-step sweep from its parameters (gate = the sub-step's half, 0 or 1), and
+// whether the sweep has one.
+__device__ __forceinline__ bool fire_gate(int32_t scheme, int32_t gate, uint64_t gate_thr, int32_t gate_f32,
+                                          const uint8_t* mask, int64_t pitch, FireGate& fg) {
+    fg.mode = scheme == GBCA_CHECKERBOARD ? 1 : (scheme == GBCA_STOCHASTIC ? 2 : 0);
+    fg.gate = gate;
+    // bernoulli(p) of the gate draw against its raw words, as fire_thresholds does for p and f
+    fg.allg = gate_f32 ? gate_thr >= ((uint64_t)1 << 24) : gate_thr >= ((uint64_t)1 << 53);
+    fg.Ug = fg.allg ? 0 : gate_thr << (gate_f32 ? 40 : 11);
+    fg.mask = mask;
+    fg.mpitch = pitch;
+    return fg.mode != 0 || mask != nullptr;
 }
 
 }  // namespace gbca

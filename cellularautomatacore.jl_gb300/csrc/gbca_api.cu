@@ -264,7 +264,8 @@ int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
     const cudaError_t e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, t, nsteps, params, h->stream,
                                            scanned_rule(h) && h->states_valid, h->forced ? &h->force : nullptr,
                                            h->mask, h->sparse_on ? &h->sparse : nullptr);
-    if (h->d.rule == GBCA_RULE_FOREST_FIRE) h->states_valid = true;  // a step leaves only 0, 1 and 2
+    // a synchronous, unmasked step leaves only 0, 1 and 2; a closed or masked cell keeps its value
+    if (h->d.rule == GBCA_RULE_FOREST_FIRE && h->d.scheme == GBCA_SYNCHRONOUS && !h->mask) h->states_valid = true;
     if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
     return GBCA_OK;
 }
@@ -563,6 +564,7 @@ int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows,
     const gbca::SweepParams p = handle_params(h, nullptr);
     if (gbca::fire_fast_supported(p)) {
         if (tile_rows != 0) return fail(GBCA_ERR_ARGUMENT, "the forest-fire kernel's tile height is fixed; pass 0");
+        // (a gated or masked fire runs one sub-step per launch whatever steps_per_pass says)
     } else if (gbca::life_simd_supported(p)) {
         if (staging != 0) return fail(GBCA_ERR_ARGUMENT, "the bit-sliced kernel stages its tiles one way; pass 0");
         if (tile_rows > 0 && !gbca::life_choice_fits(p, steps_per_pass, tile_rows))

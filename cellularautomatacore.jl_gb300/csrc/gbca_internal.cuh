@@ -278,6 +278,11 @@ int life_steps_per_pass(const SweepParams& p);
 // Whether a pass of `steps` steps on tiles `rows` high fits the bit-sliced kernel's shared memory.
 bool life_choice_fits(const SweepParams& p, int steps, int rows);
 bool fire_fast_supported(const SweepParams& p);
+// A forest-fire sweep with a gate (Stochastic, Checkerboard) or a mask: one sub-step per launch.
+bool fire_gated(const SweepParams& p);
+// One step of a gated or masked forest fire at time t: a launch per sub-step (Checkerboard's two
+// halves in turn), *cur updated after each. Counts its launches.
+cudaError_t fire_gated_step(SweepParams& p, int8_t* const bufs[2], int* cur, int64_t t, cudaStream_t st);
 cudaError_t launch_fire(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 
 // The forest-fire kernel's output tile (cells along axis 1 x axis 2).

@@ -125,6 +125,12 @@ extern "C" int gbca_advance_noalloc(const gbca_desc* desc, void* state, int64_t 
     const bool life = !fire && life_simd_supported(p);
     int8_t* bufs[2] = {(int8_t*)state, (int8_t*)scratch};
     int cur = 0;
+    if (fire && fire_gated(p)) {  // a gate or a mask: one sub-step per launch
+        for (; nsteps > 0; ++t, --nsteps) {
+            e = fire_gated_step(p, bufs, &cur, t, st);
+            if (e != cudaSuccess) return nfail(GBCA_ERR_CUDA, "sweep launch: %s", cudaGetErrorString(e));
+        }
+    }
     while (nsteps > 0) {
         int64_t k;
         const int8_t* src = bufs[cur];
@@ -137,7 +143,7 @@ extern "C" int gbca_advance_noalloc(const gbca_desc* desc, void* state, int64_t 
         } else if (life) {
             const int64_t per = life_steps_per_pass(p);
             k = nsteps < per ? nsteps : per;
-            p.nsub = (int32_t)k;
+            p.nsub = (int32_t)(k * p.ngates);  // sub-steps: two half-steps per Checkerboard step
             e = launch_life_simd(p, src, dst, st);
         } else {
             int64_t per = kGenericSubsteps / (p.radius * p.ngates);

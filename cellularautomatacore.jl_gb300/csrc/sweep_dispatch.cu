@@ -55,6 +55,20 @@ SweepChoice sweep_choice(const gbca_desc& d, bool fire, bool life, const SweepCh
     return choice;
 }
 
+cudaError_t fire_gated_step(SweepParams& p, int8_t* const bufs[2], int* cur, int64_t t, cudaStream_t st) {
+    p.nsub = 1;
+    p.t0 = t;
+    for (int gate = 0; gate < p.ngates; ++gate) {
+        p.sub0 = gate;
+        const cudaError_t e = launch_fire(p, bufs[*cur], bufs[*cur ^ 1], st);
+        if (e != cudaSuccess) return e;
+        count_launch();
+        *cur ^= 1;
+    }
+    p.sub0 = 0;
+    return cudaSuccess;
+}
+
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
                        const double* params, cudaStream_t st, bool states_valid, const SweepChoice* force,
                        const uint8_t* mask, const SparseTiles* sparse) {
@@ -108,6 +122,13 @@ cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2],
     p.tile_y = choice.tile_rows;
     p.staging = choice.staging;
     if (life) p.tile_x = choice.tile_words;
+    if (fire && fire_gated(p)) {  // a gate or a mask: one sub-step per launch, states kept as valid as given
+        for (; nsteps > 0; ++t, --nsteps) {
+            const cudaError_t e = fire_gated_step(p, bufs, cur, t, st);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
     while (nsteps > 0) {
         int64_t k;
         cudaError_t e;

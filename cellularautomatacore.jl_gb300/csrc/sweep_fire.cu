@@ -138,7 +138,7 @@ __device__ __forceinline__ void load_region_mapped(const SweepParams& p, const i
 
 // Four cells (one 32-bit word of the shared tile) per work item: neighbour tests in byte
 // SIMD, then four independent Philox chains.
-template <bool INTERIOR>
+template <bool INTERIOR, bool GATED>
 __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __restrict__ src,
                                           int8_t* __restrict__ dst, int8_t* A, int8_t* B, bool staged,
                                           int64_t X0, int64_t Y0) {
@@ -185,8 +185,10 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
                 if (p.n1 - X0 < kFireTX) nw = (int)((p.n1 - X0 + 3) / 4);
                 if (p.n2 - Y0 < TY) nrows = (int)(p.n2 - Y0);
             }
-            fire_substep_rows<!INTERIOR>((const uint32_t*)A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds,
-                                         p.keys, tid, nthr, exact, dst, p.pitch);
+            FireGate fg;  // a gated or masked sweep runs one sub-step per launch, half p.sub0
+            if constexpr (GATED) fire_gate(p.scheme, p.sub0 % p.ngates, p.gate_thr, p.gate_f32, p.mask, p.pitch, fg);
+            fire_substep_rows<!INTERIOR, GATED>((const uint32_t*)A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g,
+                                                ds, p.keys, tid, nthr, exact, dst, p.pitch, &fg);
             return;
         }
         // deeper passes: the region is wider than the tile in early sub-steps, so the flat
@@ -213,6 +215,9 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
 }
 
 // tma: 0 = no tensor map; 1 = stage interior tiles by TMA; 2 = every tile (Constant(0) edges).
+// GATED: a one-step sweep with a gate or a mask (compiled apart, so the synchronous kernel keeps
+// its registers).
+template <bool GATED>
 __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     k_fire(SweepParams p, const int8_t* __restrict__ src, int8_t* __restrict__ dst,
            const __grid_constant__ CUtensorMap tmap, int tma) {
@@ -246,8 +251,8 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
             return;
         }
     }
-    if (interior) fire_tile<true>(p, src, dst, A, B, staged, X0, Y0);
-    else fire_tile<false>(p, src, dst, A, B, staged, X0, Y0);
+    if (interior) fire_tile<true, GATED>(p, src, dst, A, B, staged, X0, Y0);
+    else fire_tile<false, GATED>(p, src, dst, A, B, staged, X0, Y0);
 }
 
 // Many lattices per launch (a batched ensemble's large instances): one pass of up to K steps
@@ -286,8 +291,8 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY, 2)
     int8_t* B = smem_f + sx * sy;
     const bool interior = X0 - sp.halo_x >= 0 && X0 + kFireTX + sp.halo_x <= sp.n1 && Y0 - sp.halo_y >= 0 &&
                           Y0 + kFireTY + sp.halo_y <= sp.n2;
-    if (interior) fire_tile<true>(sp, src, dst, A, B, false, X0, Y0);
-    else fire_tile<false>(sp, src, dst, A, B, false, X0, Y0);
+    if (interior) fire_tile<true, false>(sp, src, dst, A, B, false, X0, Y0);
+    else fire_tile<false, false>(sp, src, dst, A, B, false, X0, Y0);
 }
 
 // One step per pass with TMA staging, persistent: each CTA walks the tiles blockIdx.x,
@@ -295,6 +300,7 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY, 2)
 // of its next tile fills the other, so the copy's latency hides behind the Philox work; the
 // last (only) sub-step stores straight to HBM, so no third buffer is needed. Tiles that TMA
 // cannot stage (beyond an edge that is not Constant(0)) load through the boundary map.
+template <bool GATED>
 __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     k_fire_stream(SweepParams p, const int8_t* __restrict__ src, int8_t* __restrict__ dst,
                   const __grid_constant__ CUtensorMap tmap, int tma, int tiles_x, int ntiles) {
@@ -320,6 +326,8 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     fire_thresholds(p.thr_p, p.thr_f, p.params_f32 != 0, g);
     g.exact_always = fire_odd_constant(p.bnd[0], p.cval[0], p.bnd[1], p.cval[1]);
     const DrawStep ds = draw_step(p.keys, p.t0);
+    FireGate fg;  // a gated or masked sweep: one sub-step, half p.sub0
+    if constexpr (GATED) fire_gate(p.scheme, p.sub0 % p.ngates, p.gate_thr, p.gate_f32, p.mask, p.pitch, fg);
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[0])) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[1])) : "memory");
@@ -378,13 +386,13 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
         }
         const uint32_t* A = (const uint32_t*)cur;
         if (interior) {
-            fire_substep_rows<false>(A, sw, hx >> 2, kFireTX / 4, hy, TY, X0 - hx, Y0 - hy, g, ds, p.keys, tid,
-                                     nthr, !p.states_valid, dst, p.pitch);
+            fire_substep_rows<false, GATED>(A, sw, hx >> 2, kFireTX / 4, hy, TY, X0 - hx, Y0 - hy, g, ds, p.keys,
+                                            tid, nthr, !p.states_valid, dst, p.pitch, &fg);
         } else {  // a ragged last tile: the words and rows inside the lattice only
             const int nw = p.n1 - X0 < kFireTX ? (int)((p.n1 - X0 + 3) / 4) : kFireTX / 4;
             const int nrows = p.n2 - Y0 < TY ? (int)(p.n2 - Y0) : TY;
-            fire_substep_rows<true>(A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
-                                    !p.states_valid, dst, p.pitch);
+            fire_substep_rows<true, GATED>(A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g, ds, p.keys, tid, nthr,
+                                           !p.states_valid, dst, p.pitch, &fg);
         }
         __syncthreads();
     }
@@ -490,9 +498,13 @@ cudaError_t launch_fire_batch(const FireJob* jobs, const int32_t* tile_job, int 
 }
 
 bool fire_fast_supported(const SweepParams& p) {
-    return !p.mask && p.rule == GBCA_RULE_FOREST_FIRE && p.nbhd == GBCA_VON_NEUMANN && p.radius == 1 &&
-           p.scheme == GBCA_SYNCHRONOUS && p.n1 * p.n2 < ((int64_t)1 << 32) - 1 && p.pitch % 16 == 0;
+    // every scheme and masks: a gated or masked sweep runs one sub-step per launch (fire_gated)
+    return p.rule == GBCA_RULE_FOREST_FIRE && p.nbhd == GBCA_VON_NEUMANN && p.radius == 1 &&
+           (p.scheme == GBCA_SYNCHRONOUS || p.scheme == GBCA_STOCHASTIC || p.scheme == GBCA_CHECKERBOARD) &&
+           p.n1 * p.n2 < ((int64_t)1 << 32) - 1 && p.pitch % 16 == 0;
 }
+
+bool fire_gated(const SweepParams& p) { return p.scheme != GBCA_SYNCHRONOUS || p.mask != nullptr; }
 
 cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, cudaStream_t st) {
     SweepParams p = p0;
@@ -519,7 +531,10 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     p.keys = philox_keys(p.seed);
     const int sx = kFireTX + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
     const size_t smem = 2 * (size_t)sx * (size_t)sy;
-    cudaError_t e = ensure_dynamic_smem((const void*)k_fire, smem);
+    const bool gated = fire_gated(p);  // one sub-step per launch (p.nsub == 1), compiled apart
+    auto* fire_fn = gated ? k_fire<true> : k_fire<false>;
+    auto* stream_fn = gated ? k_fire_stream<true> : k_fire_stream<false>;
+    cudaError_t e = ensure_dynamic_smem((const void*)fire_fn, smem);
     if (e != cudaSuccess) return e;
     // TMA staging: interior tiles always; every tile when both edges are Constant(0), whose
     // value the tensor's zero fill reproduces, and n1 is a whole number of 16-byte segments
@@ -536,16 +551,16 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     const int tiles_x = (int)((p.n1 + kFireTX - 1) / kFireTX), tiles_y = (int)((p.n2 + p.tile_y - 1) / p.tile_y);
     if (p.nsub == 1 && tma && p.staging == 2) {  // one step per pass: the persistent, double-buffered kernel
         const size_t smem2 = 2 * (((size_t)sx * sy + 127) / 128 * 128);  // two 128-byte-aligned buffers
-        e = ensure_dynamic_smem((const void*)k_fire_stream, smem2);
+        e = ensure_dynamic_smem((const void*)stream_fn, smem2);
         if (e != cudaSuccess) return e;
         const int ntiles = tiles_x * tiles_y;
-        int grid = device_sms() * blocks_per_sm((const void*)k_fire_stream, kFireThreadsX * kFireThreadsY, smem2);
+        int grid = device_sms() * blocks_per_sm((const void*)stream_fn, kFireThreadsX * kFireThreadsY, smem2);
         if (grid > ntiles) grid = ntiles;
-        k_fire_stream<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem2, st>>>(p, src, dst, map, tma, tiles_x, ntiles);
+        stream_fn<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem2, st>>>(p, src, dst, map, tma, tiles_x, ntiles);
         return cudaGetLastError();
     }
     dim3 grid((unsigned)tiles_x, (unsigned)tiles_y);
-    k_fire<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(p, src, dst, map, tma);
+    fire_fn<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(p, src, dst, map, tma);
     return cudaGetLastError();
 }
 

@@ -54,6 +54,10 @@ void forget_choices() {
 std::vector<SweepChoice> sweep_candidates(const SweepParams& p) {
     std::vector<SweepChoice> out;
     if (fire_fast_supported(p)) {
+        if (fire_gated(p)) {  // one sub-step per launch: only the staging varies
+            for (int staging : {0, 1, 2}) out.push_back({1, 0, staging});
+            return out;
+        }
         // the tile height is fixed by the kernel's word layout; the pass depth and the tile
         // staging (vector loads or TMA) vary
         for (int staging : {0, 1})

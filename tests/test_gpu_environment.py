@@ -159,6 +159,8 @@ MASK_CASES = [
      "sync", (0, 0), 20),
     ("Brian's Brain", "gen", (120, 90), dict(birth=[2], survive=[], states=3), "sync", (0, 0), 25),
     ("forest fire grid", "fire", (300, 200), dict(nb="vn"), "sync", (0.05, 0.001), 30),
+    ("forest fire, Stochastic(0.5), tiled", "fire", (600, 300), dict(nb="vn"), "stoch", (0.05, 0.001), 20),
+    ("forest fire, Checkerboard, TMA-staged", "fire", (256, 512), dict(nb="vn"), "check", (0.1, 0.01), 16),
     ("Stochastic(0.5) Life", "life", (64, 80), dict(birth=[3], survive=[2, 3]), "stoch", (0, 0), 15),
     ("Checkerboard majority", "life", (70, 50), dict(nb="vn", birth=[3, 4], survive=[2, 3, 4]), "check", (0, 0), 12),
 ]

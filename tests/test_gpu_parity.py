@@ -110,6 +110,15 @@ CASES = [
      dict(nb="vn", birth=[2], survive=[1], states=3, bnd=("r", "r")), 30, 10, None),
     ("von Neumann(1) Stochastic(0.4), cylinder", "life", (200, 64),
      dict(nb="vn", birth=[1, 3], survive=[2, 3], seed=41, scheme="stoch", sp=0.4, bnd=("p", "c")), 25, 5, None),
+    # gated forest fires in the fire kernel, one sub-step per launch
+    ("forest fire, Checkerboard, Constant grid", "fire", (257, 190),
+     dict(nb="vn", seed=51, bnd=("c", "c"), scheme="check"), 20, 5, (0.1, 0.01)),
+    ("forest fire, Stochastic(0.3f0), tiled torus", "fire", (700, 300),
+     dict(nb="vn", seed=52, scheme="stoch", sp=0.3, sp32=True), 20, 10, (0.05, 0.002)),
+    ("forest fire, Checkerboard, reflecting x odd torus, tiled", "fire", (513, 301),
+     dict(nb="vn", seed=53, bnd=("r", "p"), scheme="check"), 16, 4, (0.05, 0.002)),
+    ("forest fire, Stochastic(1.0), TMA-staged grid", "fire", (1024, 300),
+     dict(nb="vn", seed=54, bnd=("c", "c"), scheme="stoch", sp=1.0), 10, 10, (0.05, 0.002)),
     ("forest fire, small grid", "fire", (40, 30), dict(nb="vn", seed=3, bnd=("c", "c")), 30, 3, (0.3, 0.01)),
     ("forest fire, Float32 parameters, torus", "fire", (33, 21), dict(nb="vn", seed=5, f32=True), 30, 10,
      (0.3, 0.01)),
@@ -172,6 +181,28 @@ def test_fire_states_outside_range(ca, oracle):
     P = oracle.Problem(oracle.RULE_FOREST_FIRE, 600, 300, nbhd=oracle.VON_NEUMANN, seed=4,
                        boundary=(oracle.CONSTANT, oracle.CONSTANT))
     assert np.array_equal(got, oracle.run_array(P, odd, 0, 20, (0.1, 0.01)))
+    st.close()
+
+
+@pytest.mark.parametrize("scheme", ["stoch", "check"])
+def test_gated_fire_states_outside_range(ca, oracle, scheme):
+    """A gated forest fire keeps closed cells' values, so a state written with values other than
+    0, 1, 2 stays exact (byte compares) for as long as such values remain."""
+    rng = np.random.default_rng(19)
+    prob = ca.CAProblem.new(ca.ForestFire(), np.zeros((300, 280), np.int8), 12, {"p": 0.1, "f": 0.01},
+                            space=ca.Grid(300, 280), seed=6)
+    sch = ca.Stochastic(0.4) if scheme == "stoch" else ca.Checkerboard()
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, sch)
+    odd = rng.integers(-4, 8, (300, 280)).astype(np.int8)
+    ca.set_state(B, st, odd)
+    for t in range(12):
+        ca.advance(B, st, prob, sch, prob.p, t)
+    got = ca.current_state(B, st)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, 300, 280, nbhd=oracle.VON_NEUMANN, seed=6,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT),
+                       scheme=oracle.STOCHASTIC if scheme == "stoch" else oracle.CHECKERBOARD, scheme_p=0.4)
+    assert np.array_equal(got, oracle.run_array(P, odd, 0, 12, (0.1, 0.01)))
     st.close()
 
 
