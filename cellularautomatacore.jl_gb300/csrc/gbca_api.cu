@@ -185,9 +185,9 @@ cudaError_t scan_states(gbca_handle* h, bool* valid) {
 }
 
 bool scanned_rule(const gbca_handle* h) {
-    // gated Life keeps closed cells' values, which its bit-sliced kernel holds only for 0 and 1
+    // gated or masked Life keeps closed cells' values, which its bit-sliced kernel holds only for 0 and 1
     return h->d.rule == GBCA_RULE_GENERATIONS || h->d.rule == GBCA_RULE_FOREST_FIRE ||
-           (h->d.rule == GBCA_RULE_LIFE && h->d.scheme != GBCA_SYNCHRONOUS);
+           (h->d.rule == GBCA_RULE_LIFE && (h->d.scheme != GBCA_SYNCHRONOUS || h->mask));
 }
 
 // A state written by the caller may hold values the rule never produces; the fast paths

@@ -313,9 +313,9 @@ __device__ __forceinline__ void rule_hits(const uint32_t* v, const LifeTables& t
 // The next state of word column w, row y, from its bit-sliced count v (centre included): the
 // rule's birth / survival tests, the gate, and the write to B.
 template <int BV, int NI, int PL, bool GATED>
-__device__ __forceinline__ void life_emit(const uint32_t* v, const uint32_t* ca, uint32_t* cb, int y, int sw, int ps,
-                                          int w, const LifeTables& tb, const SweepParams& p, const LifeGate& gt,
-                                          const CheckerCol& cc) {
+__device__ __forceinline__ void life_emit(const uint32_t* v, const uint32_t* ca, uint32_t* cb, const uint32_t* cm, int y,
+                                          int sw, int ps, int w, const LifeTables& tb, const SweepParams& p,
+                                          const LifeGate& gt, const CheckerCol& cc) {
     uint32_t dead, live;
     rule_hits<BV, NI>(v, tb, dead, live);
     // the gate: open cells take the rule's state, closed ones keep theirs
@@ -323,6 +323,7 @@ __device__ __forceinline__ void life_emit(const uint32_t* v, const uint32_t* ca,
     if constexpr (GATED) {
         if (gt.mode == 1) G = checker_gate(p, cc, gt.rows_plain, gt.X0 + 32 * w, gt.Y0 + y, gt.gate);
         else if (gt.mode == 2) G = stochastic_gate(p, gt.ds, gt.X0 + 32 * w, gt.Y0 + y);
+        if (cm) G &= cm[y * sw];  // masked cells keep their state (src/environment.jl:123-130)
     }
     if constexpr (PL == 1) {
         const uint32_t c = ca[y * sw];
@@ -346,12 +347,13 @@ __device__ __forceinline__ uint32_t alive_word(const uint32_t* q, int ps) {
 // horizontal counts and their running vertical sum. VN (von Neumann(1)): each row's count is its
 // 3-cell horizontal count plus the cells above and below.
 template <int R, int NI, int PL, bool GATED, bool VN>
-__device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B, int sw, int ps,
-                                            int w, int r0, int r1, const LifeTables& tb, const SweepParams& p,
-                                            const LifeGate& gt) {
+__device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B,
+                                            const uint32_t* __restrict__ M, int sw, int ps, int w, int r0, int r1,
+                                            const LifeTables& tb, const SweepParams& p, const LifeGate& gt) {
     constexpr int N = LifeBits<R>::N, BH = LifeBits<R>::H, BV = LifeBits<R>::V;
     const uint32_t* ca = A + 1 + w;
     uint32_t* cb = B + 1 + w;
+    const uint32_t* cm = M ? M + 1 + w : nullptr;  // the column's mask bits, or none
     CheckerCol cc{0xFFFFFFFFu, 0u, false};  // the column's Checkerboard mask adjustments
     if constexpr (GATED) {
         if (gt.mode == 1) cc = checker_col(p, gt.X0 + 32 * w);
@@ -369,7 +371,7 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
             v[2] = maj3(h[1], c1, k0);
 #pragma unroll
             for (int i = 3; i < BV; ++i) v[i] = 0u;
-            life_emit<BV, NI, PL, GATED>(v, ca, cb, y, sw, ps, w, tb, p, gt, cc);
+            life_emit<BV, NI, PL, GATED>(v, ca, cb, cm, y, sw, ps, w, tb, p, gt, cc);
         }
         return;
     }
@@ -387,7 +389,7 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
         for (int k = 0; k < N; ++k) {
             const int y = y0 + k;
             if (y < r1) {
-                life_emit<BV, NI, PL, GATED>(v, ca, cb, y, sw, ps, w, tb, p, gt, cc);
+                life_emit<BV, NI, PL, GATED>(v, ca, cb, cm, y, sw, ps, w, tb, p, gt, cc);
                 if (y + 1 < r1) {
                     vsub<BH, BV>(v, ring[k]);
                     hrow<R, PL>(ca + (y + R + 1) * sw, ps, ring[k]);
@@ -431,14 +433,14 @@ __device__ __forceinline__ int4 bytes16(uint32_t b) {
 __device__ __forceinline__ uint32_t load_bits32(const SweepParams& p, const int8_t* __restrict__ row, int64_t gx) {
     int64_t a = -1;
     if (gx >= 0 && gx + 32 <= p.n1) a = gx;
-    else if (p.bnd[0] == GBCA_PERIODIC && (p.n1 & 31) == 0) a = map_axis(GBCA_PERIODIC, gx, p.n1);
+    else if (p.bnd[0] == GBCA_PERIODIC && (p.n1 & 31) == 0) a = map_near(GBCA_PERIODIC, gx, p.n1);
     if (a >= 0) {
         const int4* q = (const int4*)(row + a);
         return ones16(q[0]) | (ones16(q[1]) << 16);
     }
     uint32_t bits = 0;
     for (int b = 0; b < 32; ++b) {
-        const int64_t mx = map_axis(p.bnd[0], gx + b, p.n1);
+        const int64_t mx = map_near(p.bnd[0], gx + b, p.n1);
         const int v = mx < 0 ? p.cval[0] : row[mx];
         bits |= (uint32_t)(v == 1) << b;
     }
@@ -450,16 +452,45 @@ __device__ __forceinline__ uint32_t load_plane32(const SweepParams& p, const int
                                                  int bit) {
     int64_t a = -1;
     if (gx >= 0 && gx + 32 <= p.n1) a = gx;
-    else if (p.bnd[0] == GBCA_PERIODIC && (p.n1 & 31) == 0) a = map_axis(GBCA_PERIODIC, gx, p.n1);
+    else if (p.bnd[0] == GBCA_PERIODIC && (p.n1 & 31) == 0) a = map_near(GBCA_PERIODIC, gx, p.n1);
     if (a >= 0) {
         const int4* q = (const int4*)(row + a);
         return plane16(q[0], bit) | (plane16(q[1], bit) << 16);
     }
     uint32_t bits = 0;
     for (int b = 0; b < 32; ++b) {
-        const int64_t mx = map_axis(p.bnd[0], gx + b, p.n1);
+        const int64_t mx = map_near(p.bnd[0], gx + b, p.n1);
         const int v = mx < 0 ? p.cval[0] : row[mx];
         bits |= (uint32_t)((v >> bit) & 1) << b;
+    }
+    return bits;
+}
+
+// Nonzero bytes of 4 bytes, in bits 0..3.
+__device__ __forceinline__ uint32_t nonzero4(uint32_t w) {
+    const uint32_t hi = (w | ((w & 0x7F7F7F7Fu) + 0x7F7F7F7Fu)) & 0x80808080u;
+    return ((hi >> 7) * 0x10204080u) >> 28;
+}
+
+__device__ __forceinline__ uint32_t nonzero16(int4 q) {
+    return nonzero4((uint32_t)q.x) | (nonzero4((uint32_t)q.y) << 4) | (nonzero4((uint32_t)q.z) << 8) |
+           (nonzero4((uint32_t)q.w) << 12);
+}
+
+// Mask bits (the cell updates: nonzero byte) of the cells gx .. gx+31 of an already mapped mask
+// row; a cell beyond a Constant edge gets 0 (it is reset to the constant anyway).
+__device__ __forceinline__ uint32_t load_mask32(const SweepParams& p, const uint8_t* __restrict__ row, int64_t gx) {
+    int64_t a = -1;
+    if (gx >= 0 && gx + 32 <= p.n1) a = gx;
+    else if (p.bnd[0] == GBCA_PERIODIC && (p.n1 & 31) == 0) a = map_near(GBCA_PERIODIC, gx, p.n1);
+    if (a >= 0) {
+        const int4* q = (const int4*)(row + a);
+        return nonzero16(q[0]) | (nonzero16(q[1]) << 16);
+    }
+    uint32_t bits = 0;
+    for (int b = 0; b < 32; ++b) {
+        const int64_t mx = map_near(p.bnd[0], gx + b, p.n1);
+        if (mx >= 0 && row[mx]) bits |= 1u << b;
     }
     return bits;
 }
@@ -471,6 +502,7 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
     const int ps = g.sw * g.sy;  // words between the planes of one buffer
     uint32_t* A = smw;
     uint32_t* B = smw + PL * ps;
+    uint32_t* M = smw + 2 * PL * ps;  // the mask plane (masked sweeps only)
     const int W = g.tw + 2 * g.hw;
     int bx = blockIdx.x, by = blockIdx.y, tile = 0;
     if (p.tile_list) {  // active-tile sweeps: one CTA per listed tile, the rest has nothing to do
@@ -491,7 +523,7 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
 
     for (int q = threadIdx.x; q < W * g.sy; q += blockDim.x) {
         const int lw = q % W, ly = q / W;
-        const int64_t my = map_axis(p.bnd[1], Y0 + ly, p.n2);
+        const int64_t my = map_near(p.bnd[1], Y0 + ly, p.n2);
 #pragma unroll
         for (int pl = 0; pl < PL; ++pl) {
             uint32_t bits;
@@ -500,6 +532,9 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
             else bits = load_plane32(p, src + my * p.pitch, X0 + 32 * lw, pl);
             A[pl * ps + ly * g.sw + 1 + lw] = bits;
             B[pl * ps + ly * g.sw + 1 + lw] = bits;
+        }
+        if constexpr (GATED) {  // the mask's bits, mapped like the state (a masked cell keeps its state)
+            if (p.mask) M[ly * g.sw + 1 + lw] = my < 0 ? 0u : load_mask32(p, p.mask + my * p.pitch, X0 + 32 * lw);
         }
     }
     for (int ly = threadIdx.x; ly < g.sy; ly += blockDim.x) {
@@ -536,7 +571,8 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
             const int rows = y_hi - y_lo;
             const int r0 = y_lo + (seg * rows) / nseg, r1 = y_lo + ((seg + 1) * rows) / nseg;
             if (r1 > r0)
-                life_column<R, NI, PL, GATED, VN>(A, B, g.sw, ps, w_lo + threadIdx.x % nw, r0, r1, tb, p, gt);
+                life_column<R, NI, PL, GATED, VN>(A, B, GATED && p.mask ? M : nullptr, g.sw, ps,
+                                                  w_lo + threadIdx.x % nw, r0, r1, tb, p, gt);
         }
         __syncthreads();
         if (fix) {
@@ -650,7 +686,8 @@ LifeGeom life_geometry(const SweepParams& p, int K, int rows) {
 
 size_t life_smem_bytes(const SweepParams& p, const LifeGeom& g) {
     const int PL = p.rule == GBCA_RULE_GENERATIONS ? 2 : 1;
-    return 2 * PL * (size_t)g.sw * (size_t)g.sy * 4;
+    const int planes = 2 * PL + (p.mask ? 1 : 0);  // two buffers of PL planes, and the mask's bits
+    return (size_t)planes * (size_t)g.sw * (size_t)g.sy * 4;
 }
 
 template <int R, int NI, int PL, bool GATED, bool VN>
@@ -669,7 +706,7 @@ template <int R, int PL, bool VN = false>
 cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                      cudaStream_t st, int ntiles = 0) {
     const int ni = tb.n[0] > tb.n[1] ? tb.n[0] : tb.n[1];
-    if (p.scheme != GBCA_SYNCHRONOUS) {  // gated variants exist for r <= 2 (life_simd_supported)
+    if (p.scheme != GBCA_SYNCHRONOUS || p.mask) {  // gated variants (gates, masks) exist for r <= 2
         if constexpr (R <= 2) {
             if (ni <= 1) return launch_rn<R, 1, PL, true, VN>(p, g, tb, src, dst, st, ntiles);
             if (ni <= 2) return launch_rn<R, 2, PL, true, VN>(p, g, tb, src, dst, st, ntiles);
@@ -686,8 +723,8 @@ cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& 
 }  // namespace
 
 bool life_simd_supported(const SweepParams& p) {
-    if (p.mask) return false;
     if (p.radius < 1 || p.pitch % 16 != 0) return false;
+    if (p.mask && (((uintptr_t)p.mask & 15u) != 0 || p.radius > 2)) return false;  // the gated kernels: r <= 2
     if (p.nbhd != GBCA_MOORE && !(p.nbhd == GBCA_VON_NEUMANN && p.radius == 1)) return false;
     if (p.scheme == GBCA_CHECKERBOARD) {
         // any boundary: the gate maps halo cells to the cells they image (checker_gate)
@@ -697,8 +734,8 @@ bool life_simd_supported(const SweepParams& p) {
         return false;
     }
     if (p.scheme != GBCA_SYNCHRONOUS && p.radius > 2) return false;  // gated kernels: r <= 2
-    // a closed Life cell keeps its value: the indicator bits hold it only for 0 and 1
-    if (p.scheme != GBCA_SYNCHRONOUS && p.rule == GBCA_RULE_LIFE && !p.states_valid) return false;
+    // a closed or masked Life cell keeps its value: the indicator bits hold it only for 0 and 1
+    if ((p.scheme != GBCA_SYNCHRONOUS || p.mask) && p.rule == GBCA_RULE_LIFE && !p.states_valid) return false;
     if (p.rule == GBCA_RULE_LIFE) {
         if (p.radius > 5) return false;
     } else if (p.rule == GBCA_RULE_GENERATIONS) {
@@ -809,7 +846,19 @@ cudaError_t launch_life_simd(const SweepParams& p0, const int8_t* src, int8_t* d
     if (p.scheme == GBCA_STOCHASTIC) p.keys = philox_keys(p.seed);  // the gate draws
     LifeTables tb;
     if (!make_tables(p, &tb)) return cudaErrorNotSupported;
-    const LifeGeom g = life_geometry(p, p.nsub, p.tile_y);  // tile_y: the autotuner's pick, or 0
+    LifeGeom g = life_geometry(p, p.nsub, p.tile_y);  // tile_y: the autotuner's pick, or 0
+    if (p.mask) {  // the mask's plane: a pick made for the unmasked rule may need shorter tiles
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+            cudaGetLastError();
+            optin = 227 * 1024;
+        }
+        for (int ty = g.ty; life_smem_bytes(p, g) > (size_t)optin && ty > 8;) {
+            ty /= 2;
+            g = life_geometry(p, p.nsub, ty);
+        }
+    }
     if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1 (life_simd_supported)
         if (p.rule == GBCA_RULE_GENERATIONS) return launch_r<1, 2, true>(p, g, tb, src, dst, st);
         return launch_r<1, 1, true>(p, g, tb, src, dst, st);

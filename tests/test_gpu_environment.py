@@ -204,3 +204,93 @@ def test_masks(ca, oracle, case):
     want = o.run_array_env(P, o.Env(mask=mask), u0, 0, steps, params if kind == "fire" else None, nthreads=8)
     assert np.array_equal(got, want), f"{name}: {(got != want).sum()} cells differ"
     assert np.array_equal(got[~mask], u0[~mask]) and not np.array_equal(got, u0)
+
+
+def _geometry(ca, st):
+    import ctypes
+    k, rows, staging = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    ca.capi.check(ca.capi.lib().gbca_geometry(st.handle, None, ctypes.byref(k), ctypes.byref(rows),
+                                              ctypes.byref(staging)))
+    return int(k.value), int(rows.value), int(staging.value)
+
+
+BITSLICED_MASK_CASES = [
+    # name, rule kind, dims, boundary kinds, scheme, steps
+    ("Life on a 512 x 256 torus, three passes", "life", (512, 256), "pp", "sync", 40),
+    ("Life Moore(2) on a 300 x 200 grid", "life2", (300, 200), "cc", "sync", 20),
+    ("Life on a reflecting 200 x 130 lattice", "life", (200, 130), "rr", "sync", 25),
+    ("Brian's Brain, Checkerboard, 256 x 128 torus", "gen", (256, 128), "pp", "check", 10),
+    ("von Neumann majority, Stochastic(0.5), 320 x 96 torus", "vn", (320, 96), "pp", "stoch", 12),
+]
+
+
+@pytest.mark.parametrize("case", BITSLICED_MASK_CASES, ids=[c[0] for c in BITSLICED_MASK_CASES])
+def test_masks_bit_sliced(ca, oracle, case):
+    """Masked Life and Generations on the bit-sliced kernel (its gated form, with the mask's
+    bits in shared memory): the geometry query names a fast-kernel geometry, and the state
+    equals the oracle's after every step."""
+    name, kind, (n1, n2), bk, scheme, steps = case
+    o = oracle
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
+    bnd, obnd = _bnd(ca, o, bk)
+    if kind == "gen":
+        rule = ca.Generations(":brians_brain")
+        P = o.Problem(o.RULE_GENERATIONS, n1, n2, birth=o.mask([2]), survive=0, states=3)
+        C = 3
+    else:
+        r = 2 if kind == "life2" else 1
+        birth, survive = ([3, 4], [2, 3, 4]) if kind == "vn" else ((range(5, 8), range(4, 9)) if r == 2 else
+                                                                  ([3], [2, 3]))
+        nb = ca.VonNeumann(1) if kind == "vn" else ca.Moore(r)
+        rule = ca.Life(list(birth), list(survive), neighbourhood=nb)
+        P = o.Problem(o.RULE_LIFE, n1, n2, nbhd=o.VON_NEUMANN if kind == "vn" else o.MOORE, radius=r,
+                      birth=o.mask(birth), survive=o.mask(survive))
+        C = 2
+    P.boundary = obnd
+    P.seed = 6
+    if scheme == "stoch":
+        P.scheme, P.scheme_p = o.STOCHASTIC, 0.5
+    elif scheme == "check":
+        P.scheme = o.CHECKERBOARD
+    sch = {"sync": ca.Synchronous(), "stoch": ca.Stochastic(0.5), "check": ca.Checkerboard()}[scheme]
+    u0 = rng.integers(0, C, (n1, n2)).astype(np.int8)
+    mask = rng.random((n1, n2)) < 0.8
+    prob = ca.CAProblem.new(rule, u0, steps, space=ca.Lattice((n1, n2), bnd), seed=6, mask=mask)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, sch)
+    ca.set_state(B, st, u0)
+    want = u0
+    for t in range(steps):
+        ca.advance(B, st, prob, sch, None, t)
+        want = o.run_array_env(P, o.Env(mask=mask), want, t, 1, None, nthreads=8)
+        if t in (0, steps // 2, steps - 1):
+            got = ca.current_state(B, st)
+            assert np.array_equal(got, want), f"{name}, step {t + 1}: {(got != want).sum()} cells differ"
+    assert _geometry(ca, st)[0] > 0, "the masked sweep fell back to the general kernel"
+    for t in range(steps, 2 * steps):  # queued steps run as whole passes
+        ca.advance(B, st, prob, sch, None, t)
+    want = o.run_array_env(P, o.Env(mask=mask), want, steps, steps, None, nthreads=8)
+    assert np.array_equal(ca.current_state(B, st), want)
+    assert np.array_equal(want[~mask], u0[~mask])
+    st.close()
+
+
+def test_masked_life_states_outside_range(ca, oracle):
+    """Masked Life on a state holding values other than 0 and 1: a masked cell keeps its value,
+    which the bit-sliced kernel's indicator bits cannot hold, so the sweep stays on the general
+    kernel; the result equals the oracle's."""
+    rng = np.random.default_rng(12)
+    n1, n2 = 128, 96
+    odd = rng.integers(-2, 4, (n1, n2)).astype(np.int8)
+    mask = rng.random((n1, n2)) < 0.7
+    prob = ca.CAProblem.new(ca.Life(":conway"), np.zeros((n1, n2), np.int8), 10, mask=mask)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    ca.set_state(B, st, odd)
+    for t in range(10):
+        ca.advance(B, st, prob, ca.Synchronous(), None, t)
+    P = oracle.Problem(oracle.RULE_LIFE, n1, n2, birth=oracle.mask([3]), survive=oracle.mask([2, 3]))
+    want = oracle.run_array_env(P, oracle.Env(mask=mask), odd, 0, 10, None, nthreads=8)
+    assert np.array_equal(ca.current_state(B, st), want)
+    assert _geometry(ca, st) == (0, 0, 0)
+    st.close()
