@@ -563,7 +563,10 @@ int gbca_set_geometry(gbca_handle* h, int32_t steps_per_pass, int32_t tile_rows,
     if (rc != GBCA_OK) return rc;
     const gbca::SweepParams p = handle_params(h, nullptr);
     if (gbca::fire_fast_supported(p)) {
-        if (tile_rows != 0) return fail(GBCA_ERR_ARGUMENT, "the forest-fire kernel's tile height is fixed; pass 0");
+        if (tile_rows != 0 && !gbca::fire_rows_fit(steps_per_pass, tile_rows, staging))
+            return fail(GBCA_ERR_ARGUMENT,
+                        "forest-fire tiles take %d..%d rows within shared memory; got %d rows at %d steps per pass",
+                        gbca::kFireRowsMin, gbca::kFireRowsMax, (int)tile_rows, (int)steps_per_pass);
         // (a gated or masked fire runs one sub-step per launch whatever steps_per_pass says)
     } else if (gbca::life_simd_supported(p)) {
         if (staging != 0) return fail(GBCA_ERR_ARGUMENT, "the bit-sliced kernel stages its tiles one way; pass 0");

@@ -283,10 +283,15 @@ bool fire_gated(const SweepParams& p);
 // One step of a gated or masked forest fire at time t: a launch per sub-step (Checkerboard's two
 // halves in turn), *cur updated after each. Counts its launches.
 cudaError_t fire_gated_step(SweepParams& p, int8_t* const bufs[2], int* cur, int64_t t, cudaStream_t st);
+// p.tile_y: a pinned tile height, or 0 for the launcher's model.
 cudaError_t launch_fire(const SweepParams& p, const int8_t* src, int8_t* dst, cudaStream_t st);
 
-// The forest-fire kernel's output tile (cells along axis 1 x axis 2).
+// The forest-fire kernel's output tile (cells along axis 1 x axis 2; the launcher picks the
+// height of one-step passes, kFireTileRows is the persistent ensemble pass's).
 constexpr int kFireTileCols = 256, kFireTileRows = 128;
+constexpr int kFireRowsMin = 8, kFireRowsMax = 240;  // heights gbca_set_geometry accepts for the fire kernel
+// Whether tiles of `rows` rows fit shared memory at `steps` steps per pass and that staging.
+bool fire_rows_fit(int steps, int rows, int staging);
 
 // One lattice of a batched forest-fire sweep (many lattices per launch, one pass each).
 struct FireJob {

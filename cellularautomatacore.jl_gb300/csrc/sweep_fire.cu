@@ -39,6 +39,8 @@ namespace {
 
 constexpr int kFireTX = kFireTileCols, kFireTY = kFireTileRows;
 constexpr int kFireThreadsX = 32, kFireThreadsY = 16;
+constexpr int kFireRowsOneStep = 160;  // the tallest tile the one-step model considers
+constexpr int kFireTileCost = 16;      // a tile's fixed cost in rows (see launch_fire)
 constexpr int kTmaSpins = 1 << 22;  // try_wait polls before a tile gives up
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -506,6 +508,19 @@ bool fire_fast_supported(const SweepParams& p) {
 
 bool fire_gated(const SweepParams& p) { return p.scheme != GBCA_SYNCHRONOUS || p.mask != nullptr; }
 
+bool fire_rows_fit(int steps, int rows, int staging) {
+    if (rows < kFireRowsMin || rows > kFireRowsMax || steps < 1) return false;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        optin = 227 * 1024;
+    }
+    const size_t sx = kFireTX + 2 * (size_t)((steps + 15) / 16 * 16), sy = (size_t)rows + 2 * (size_t)steps;
+    const size_t smem = staging == 2 && steps == 1 ? 2 * ((sx * sy + 127) / 128 * 128) : 2 * sx * sy;
+    return smem <= (size_t)optin;
+}
+
 cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, cudaStream_t st) {
     SweepParams p = p0;
     p.tile_x = kFireTX;
@@ -513,7 +528,25 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     // rounds of one per CTA slot (two CTAs per SM), so a lattice of t tiles fills
     // (t / slots) / ceil(t / slots) of the last round's share; a shorter tile recomputes a
     // larger share of halo rows, TY / (TY + 2 halo) useful.
-    {
+    if (p0.tile_y > 0) {  // pinned (gbca_set_geometry checked that it fits)
+        p.tile_y = p0.tile_y;
+    } else if (p.nsub == 1) {
+        // one step per pass: the busiest SM's tiles, ceil(tiles / SMs), times the cost of a
+        // tile, its rows plus kFireTileCost rows' worth of halo, staging and set-up. Fitted to
+        // Gcell-updates/s measured by height on 2048^2, 4096^2 and 8192^2 grids: the minimum
+        // falls on 108, 108 and 160 rows (255, 329, 384 against 227, 292, 375 for the best
+        // power of two), and the model ranks the other heights as measured.
+        const int64_t tx = (p.n1 + kFireTX - 1) / kFireTX, nsm = device_sms();
+        int64_t best = -1;
+        for (int ty = kFireRowsOneStep; ty >= 32; --ty) {
+            const int64_t t = tx * ((p.n2 + ty - 1) / ty);
+            const int64_t cost = (t + nsm - 1) / nsm * (ty + kFireTileCost);
+            if (best < 0 || cost < best) {
+                best = cost;
+                p.tile_y = ty;
+            }
+        }
+    } else {
         const int64_t tx = (p.n1 + kFireTX - 1) / kFireTX, slots = 2 * (int64_t)device_sms();
         double best = -1.0;
         for (int ty = kFireTY; ty >= 32; ty /= 2) {

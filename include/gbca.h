@@ -239,7 +239,8 @@ int gbca_geometry(gbca_handle* h, const double* params, int32_t* steps_per_pass,
 int gbca_forget_tuning(void);
 
 /* Pins this handle's sweep geometry ((0, 0, 0) unpins it). The forest-fire kernel takes
- * tile_rows = 0 and staging 0 (vector loads), 1 (a TMA copy per tile where the tile fits) or
+ * tile_rows 0 (its launcher's model) or 8..240 rows whose tiles fit shared memory, and
+ * staging 0 (vector loads), 1 (a TMA copy per tile where the tile fits) or
  * 2 (the same, prefetched by a persistent kernel; one step per pass only); the bit-sliced
  * kernel takes tile_rows 0 (its default) or any height whose tiles fit shared memory, and
  * staging 0; the general kernel takes none (GBCA_ERR_UNSUPPORTED). */

@@ -137,7 +137,9 @@ def test_geometry_refusals(ca):
     fire = ca.CAProblem.new(ca.ForestFire(), np.zeros((64, 64), np.int8), 5, {"p": 0.1, "f": 0.0})
     st = ca.allocate_state(B, fire, ca.Synchronous())
     with pytest.raises(ca.ArgumentError):
-        ca.set_geometry(st, 4, 128)  # the fire kernel's tile height is fixed
+        ca.set_geometry(st, 4, 300)  # fire tiles take 8..240 rows
+    with pytest.raises(ca.ArgumentError):
+        ca.set_geometry(st, 64, 240)  # beyond shared memory at 64 steps per pass
     with pytest.raises(ca.ArgumentError):
         ca.set_geometry(st, 0, 16)
     with pytest.raises(ca.ArgumentError):
@@ -170,6 +172,37 @@ def test_fire_persistent_multi_tile(ca, oracle, space):
     bnd = (oracle.CONSTANT, oracle.CONSTANT) if space == "grid" else (oracle.PERIODIC, oracle.PERIODIC)
     P = oracle.Problem(oracle.RULE_FOREST_FIRE, n, n, nbhd=oracle.VON_NEUMANN, seed=21, boundary=bnd)
     assert np.array_equal(got, oracle.run_array(P, u0, 0, 6, (0.05, 0.002), nthreads=16))
+    st.close()
+
+
+@pytest.mark.parametrize("steps,rows,staging", [(1, 108, 1), (1, 72, 2), (1, 37, 0), (3, 200, 1), (8, 8, 0)])
+def test_fire_pinned_tile_rows(ca, oracle, steps, rows, staging):
+    """Pinned forest-fire tile heights that divide nothing (a 1000 x 770 grid: ragged tiles on
+    both axes), each staging method, one and several steps per pass, from t = 2, 11 steps."""
+    n1, n2 = 1000, 770
+    u0 = np.random.default_rng(rows).integers(0, 3, (n1, n2)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 20, {"p": 0.05, "f": 0.002}, space=ca.Grid(n1, n2), seed=19)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, steps, rows, staging)
+    got = _run(ca, prob, st, 2, 11, prob.p)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, n1, n2, nbhd=oracle.VON_NEUMANN, seed=19,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    assert np.array_equal(got, oracle.run_array(P, u0, 2, 11, (0.05, 0.002), nthreads=16))
+    st.close()
+
+
+@pytest.mark.parametrize("side", [2048, 4096])
+def test_fire_one_step_model_heights(ca, oracle, side):
+    """The one-step model's tile heights (108 rows on 2048^2 and 4096^2 grids, whose tiles
+    then spread evenly over the SMs), 3 steps from an oracle-checked state."""
+    u0 = np.random.default_rng(side).integers(0, 3, (side, side)).astype(np.int8)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 3, {"p": 0.05, "f": 0.002}, space=ca.Grid(side, side), seed=23)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, 1, 0, 1)
+    got = _run(ca, prob, st, 0, 3, prob.p)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, side, side, nbhd=oracle.VON_NEUMANN, seed=23,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    assert np.array_equal(got, oracle.run_array(P, u0, 0, 3, (0.05, 0.002), nthreads=16))
     st.close()
 
 
