@@ -11,7 +11,9 @@ One bench step runs both from their initial states. Metric: Gcell-updates/s
   value : device-resident — initial states are copied device-to-device into the handles,
           then advanced; CUDA events on the stream the library launches on.
   e2e   : the same through the C ABI with host buffers — set_state from pinned host memory,
-          advance, current_state back to pinned host memory, every step.
+          advance, current_state back to pinned host memory, every step. Each handle runs on
+          its own stream, and both inputs and both sweeps are issued before either result is
+          read, so one lattice's copies overlap the other's sweep.
   roofline: the dominant kernel (by device time), algorithmic bytes 2 B per cell-update
           (Int8 read + write) over its average launch duration, against the measured HBM copy
           bandwidth in MEASURED_PEAKS.json.
@@ -810,14 +812,16 @@ def main():
         capi.check(lib.gbca_set_stream(h, None))
 
     def step_e2e():
-        for k, (h, hi, ho) in enumerate(zip(handles, host_in, host_out)):
-            nb = hi.numel()
-            capi.check(lib.gbca_set_state(h, ctypes.c_void_p(hi.data_ptr()), nb))
+        # inputs and sweeps first (each handle on its own stream), results after: the forest
+        # fire's input copy overlaps the Larger-than-Life sweep, whose result copy overlaps the fire
+        for k, (h, hi) in enumerate(zip(handles, host_in)):
+            capi.check(lib.gbca_set_state(h, ctypes.c_void_p(hi.data_ptr()), hi.numel()))
             if k == 0:
                 capi.check(lib.gbca_advance(h, 0, LTL["steps"], None, 0))
             else:
                 capi.check(lib.gbca_advance(h, 0, FIRE["steps"], params_fire, 2))
-            capi.check(lib.gbca_get_state(h, ctypes.c_void_p(ho.data_ptr()), nb))
+        for h, ho in zip(handles, host_out):
+            capi.check(lib.gbca_get_state(h, ctypes.c_void_p(ho.data_ptr()), ho.numel()))
 
     step_e2e()
     barrier()
