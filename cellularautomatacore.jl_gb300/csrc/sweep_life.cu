@@ -1,7 +1,7 @@
 // sweep_life.cu — Life-like and Larger-than-Life rules (src/rules.jl:354-389) on Moore(r),
-// r = 1..5, and von Neumann(1), and Generations rules with up to 4 states on Moore(1..2) and
-// von Neumann(1), Synchronous, Stochastic(p) or Checkerboard (r <= 2), as a bit-sliced,
-// temporally blocked sweep.
+// r = 1..7, and von Neumann(1), and Generations rules with up to 4 states on Moore(1..2) and
+// von Neumann(1), Synchronous, Stochastic(p) or Checkerboard and masks (r <= 2), as a
+// bit-sliced, temporally blocked sweep.
 //
 // Layout. Global memory keeps the user's Int8 column-major state. A CTA stages its tile
 // plus a halo of K*r cells in shared memory as ONE BIT PER CELL: bit b of word w of a
@@ -176,7 +176,8 @@ template <int R>
 struct LifeBits {
     static constexpr int N = 2 * R + 1;
     static constexpr int H = N < 4 ? 2 : (N < 8 ? 3 : 4);                        // planes of Hx
-    static constexpr int V = N * N < 16 ? 4 : (N * N < 32 ? 5 : (N * N < 64 ? 6 : 7));  // planes of V
+    static constexpr int V = N * N < 16 ? 4 : (N * N < 32 ? 5 : (N * N < 64 ? 6 : (N * N < 128 ? 7 : 8)));  // of V
+    static_assert(N * N < 256, "the comparator tables hold 8 planes: r <= 7");
 };
 
 __device__ __forceinline__ uint32_t maj3(uint32_t a, uint32_t b, uint32_t c) { return (a & b) | (a & c) | (b & c); }
@@ -214,8 +215,7 @@ __device__ __forceinline__ void hcount(const uint32_t* x, uint32_t* h) {
         m2 = t & k4;
         h[2] = m1 ^ m2;
         h[3] = m1 & m2;
-    } else {
-        static_assert(R == 5, "r = 1..5");
+    } else if constexpr (R == 5) {
         uint32_t s1, k1, s2, k2, s3, k3, s4, k4, k5, t1, m1, m2;
         fa(x[0], x[1], x[2], s1, k1);
         fa(x[3], x[4], x[5], s2, k2);
@@ -226,6 +226,33 @@ __device__ __forceinline__ void hcount(const uint32_t* x, uint32_t* h) {
         fa(k4, k5, t1, h[1], m2);
         h[2] = m1 ^ m2;
         h[3] = m1 & m2;
+    } else if constexpr (R == 6) {  // 13 inputs: weight-1 sums, then weight-2 and weight-4 carries
+        uint32_t s1, k1, s2, k2, s3, k3, s4, k4, t1, c1, c2, d1, e1, d2, e2, e3;
+        fa(x[0], x[1], x[2], s1, k1);
+        fa(x[3], x[4], x[5], s2, k2);
+        fa(x[6], x[7], x[8], s3, k3);
+        fa(x[9], x[10], x[11], s4, k4);
+        fa(s1, s2, s3, t1, c1);
+        fa(t1, s4, x[12], h[0], c2);
+        fa(k1, k2, k3, d1, e1);
+        fa(k4, c1, c2, d2, e2);
+        h[1] = d1 ^ d2;
+        e3 = d1 & d2;
+        fa(e1, e2, e3, h[2], h[3]);
+    } else {
+        static_assert(R == 7, "r = 1..7");
+        uint32_t s1, k1, s2, k2, s3, k3, s4, k4, s5, k5, t1, c1, c2, d1, e1, d2, e2, e3;
+        fa(x[0], x[1], x[2], s1, k1);
+        fa(x[3], x[4], x[5], s2, k2);
+        fa(x[6], x[7], x[8], s3, k3);
+        fa(x[9], x[10], x[11], s4, k4);
+        fa(x[12], x[13], x[14], s5, k5);
+        fa(s1, s2, s3, t1, c1);
+        fa(t1, s4, s5, h[0], c2);
+        fa(k1, k2, k3, d1, e1);
+        fa(k4, k5, c1, d2, e2);
+        fa(d1, d2, c2, h[1], e3);
+        fa(e1, e2, e3, h[2], h[3]);
     }
 }
 
@@ -716,7 +743,9 @@ cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& 
         }
     }
     if (ni <= 1) return launch_rn<R, 1, PL, false, VN>(p, g, tb, src, dst, st, ntiles);
-    if (ni <= 2) return launch_rn<R, 2, PL, false, VN>(p, g, tb, src, dst, st, ntiles);
+    if constexpr (R <= 5) {  // radii 6 and 7 compile one- and eight-interval forms only
+        if (ni <= 2) return launch_rn<R, 2, PL, false, VN>(p, g, tb, src, dst, st, ntiles);
+    }
     return launch_rn<R, kMaxIntervals, PL, false, VN>(p, g, tb, src, dst, st, ntiles);
 }
 
@@ -737,7 +766,7 @@ bool life_simd_supported(const SweepParams& p) {
     // a closed or masked Life cell keeps its value: the indicator bits hold it only for 0 and 1
     if ((p.scheme != GBCA_SYNCHRONOUS || p.mask) && p.rule == GBCA_RULE_LIFE && !p.states_valid) return false;
     if (p.rule == GBCA_RULE_LIFE) {
-        if (p.radius > 5) return false;
+        if (p.radius > 7) return false;  // counts up to 15^2 = 225 in 8 bit planes
     } else if (p.rule == GBCA_RULE_GENERATIONS) {
         // two planes hold states 0..3; every state (and Constant value) must lie in 0..C-1
         if (p.radius > 2 || p.states > 4 || !p.states_valid) return false;
@@ -872,7 +901,9 @@ cudaError_t launch_life_simd(const SweepParams& p0, const int8_t* src, int8_t* d
         case 2: return launch_r<2, 1>(p, g, tb, src, dst, st);
         case 3: return launch_r<3, 1>(p, g, tb, src, dst, st);
         case 4: return launch_r<4, 1>(p, g, tb, src, dst, st);
-        default: return launch_r<5, 1>(p, g, tb, src, dst, st);
+        case 5: return launch_r<5, 1>(p, g, tb, src, dst, st);
+        case 6: return launch_r<6, 1>(p, g, tb, src, dst, st);
+        default: return launch_r<7, 1>(p, g, tb, src, dst, st);
     }
 }
 
@@ -908,7 +939,9 @@ cudaError_t launch_life_tiles(const SweepParams& p0, const SparseTiles& sp, cons
         case 2: return launch_r<2, 1>(p, g, tb, src, dst, st, n);
         case 3: return launch_r<3, 1>(p, g, tb, src, dst, st, n);
         case 4: return launch_r<4, 1>(p, g, tb, src, dst, st, n);
-        default: return launch_r<5, 1>(p, g, tb, src, dst, st, n);
+        case 5: return launch_r<5, 1>(p, g, tb, src, dst, st, n);
+        case 6: return launch_r<6, 1>(p, g, tb, src, dst, st, n);
+        default: return launch_r<7, 1>(p, g, tb, src, dst, st, n);
     }
 }
 

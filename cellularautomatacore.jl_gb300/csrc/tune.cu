@@ -58,16 +58,16 @@ std::vector<SweepChoice> sweep_candidates(const SweepParams& p) {
             for (int staging : {0, 1, 2}) out.push_back({1, 0, staging});
             return out;
         }
-        // the tile height is fixed by the kernel's word layout; the pass depth and the tile
-        // staging (vector loads or TMA) vary
+        // the tile height comes from the launcher's model; the pass depth and the tile staging
+        // (vector loads or TMA) vary
         for (int staging : {0, 1})
             for (int k : {1, 2, 3, 4, 6, 8}) out.push_back({k, 0, staging});
         out.push_back({1, 0, 2});  // one step per pass from the persistent prefetching kernel
         return out;
     }
     if (!life_simd_supported(p)) return out;
-    static const int kPer[5][5] = {{8, 12, 16, 24, 32}, {4, 6, 8, 12, 16}, {3, 4, 6, 8, 10},
-                                   {3, 4, 5, 6, 8},     {2, 3, 4, 5, 6}};
+    static const int kPer[7][5] = {{8, 12, 16, 24, 32}, {4, 6, 8, 12, 16}, {3, 4, 6, 8, 10}, {3, 4, 5, 6, 8},
+                                   {2, 3, 4, 5, 6},     {2, 3, 4, 5, 6},   {1, 2, 3, 4, 5}};
     const int* per = kPer[p.radius - 1];
     for (int i = 0; i < 5; ++i)
         for (int ty : {64, 96, 128, 144, 176, 216, 256})

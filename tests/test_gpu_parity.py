@@ -165,6 +165,55 @@ def test_conformance(ca, oracle, case):
     assert not np.array_equal(us[-1], u0)
 
 
+LTL_WIDE = [
+    # name, r, dims, boundaries, density, birth, survive, steps
+    ("Moore(6) torus, one interval each", 6, (230, 170), ("p", "p"), 0.25, range(38, 51), range(36, 56), 24),
+    ("Moore(7) grid, Constant(1) edges", 7, (300, 200), ("c", "c"), 0.2, range(40, 53), range(38, 59), 16),
+    ("Moore(7) reflecting x torus, several intervals", 7, (250, 180), ("r", "p"), 0.2,
+     [40, 41, 42, 43, 47, 48, 49, 50], [38, 39, 40, 41, 44, 45, 46, 47, 48, 49, 50, 51, 52, 53, 54, 55, 60], 16),
+    ("Moore(6) lattice narrower than a halo word", 6, (40, 33), ("p", "p"), 0.25, range(38, 51), range(36, 56), 12),
+]
+
+
+@pytest.mark.parametrize("case", LTL_WIDE, ids=[c[0] for c in LTL_WIDE])
+def test_larger_than_life_radius_6_7(ca, oracle, case):
+    """Larger than Life on Moore(6) and Moore(7) (169 and 225 cells: eight count planes) runs
+    the bit-sliced kernel, its one- and eight-interval forms, on every boundary kind: the
+    state equals the oracle's after the first, middle and last steps and after whole queued
+    passes, and the geometry query names a bit-sliced geometry. Sparse soups keep the first
+    steps' counts near the intervals (the reference's count masks stop at 63, so a denser
+    lattice dies at once): step 1 births most cells and step 2 kills most of them, counts
+    spanning every interval and the gaps between them."""
+    import ctypes
+    name, r, (n1, n2), bnd, dens, birth, survive, steps = case
+    const = (1, 1) if "Constant(1)" in name else (0, 0)
+    rule, space, scheme, P = spec_pair(ca, oracle, "life", n1, n2, r=r, birth=birth, survive=survive, bnd=bnd,
+                                       const=const)
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
+    u0 = (rng.random((n1, n2)) < dens).astype(np.int8)
+    prob = ca.CAProblem.new(rule, u0, 2 * steps, space=space)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, scheme)
+    want = u0
+    for t in range(steps):
+        ca.advance(B, st, prob, scheme, None, t)
+        want = oracle.run_array(P, want, t, 1, nthreads=8)
+        if t == 0:
+            assert (want != u0).sum() > 0.05 * want.size
+        if t in (0, 1, steps // 2, steps - 1):
+            got = ca.current_state(B, st)
+            assert np.array_equal(got, want), f"{name}, step {t + 1}: {(got != want).sum()} cells differ"
+    k, rows, staging = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    ca.capi.check(ca.capi.lib().gbca_geometry(st.handle, None, ctypes.byref(k), ctypes.byref(rows),
+                                              ctypes.byref(staging)))
+    assert k.value > 0, "Moore(r <= 7) Life fell back to the general kernel"
+    for t in range(steps, 2 * steps):
+        ca.advance(B, st, prob, scheme, None, t)
+    want = oracle.run_array(P, want, steps, steps, nthreads=8)
+    assert np.array_equal(ca.current_state(B, st), want)
+    st.close()
+
+
 def test_fire_states_outside_range(ca, oracle):
     """A forest-fire state written with values other than 0, 1, 2 (trees in the rule) takes
     exact byte compares on the first step and bit tests after it."""
