@@ -324,16 +324,18 @@ __device__ __forceinline__ uint32_t ge(const uint32_t* v, const uint32_t* m) {
     return g;
 }
 
-// NI interval tests per kind, unrolled with no branches; the tables fill unused intervals
-// with an empty one (lo = 1, hi + 1 = 0), which never matches.
+// NI interval tests per kind, unrolled; the tables fill unused intervals with an empty one
+// (lo = 1, hi + 1 = 0), which never matches. The one- and two-interval forms test every
+// interval with no branch; the eight-interval form skips the empty ones by the rule's
+// interval counts (a uniform branch), so a three-interval rule pays for three.
 template <int BV, int NI>
 __device__ __forceinline__ void rule_hits(const uint32_t* v, const LifeTables& tb, uint32_t& dead, uint32_t& live) {
     dead = 0u;
     live = 0u;
 #pragma unroll
     for (int k = 0; k < NI; ++k) {
-        dead |= ge<BV>(v, tb.m[0][k][0]) & ~ge<BV>(v, tb.m[0][k][1]);
-        live |= ge<BV>(v, tb.m[1][k][0]) & ~ge<BV>(v, tb.m[1][k][1]);
+        if (NI <= 2 || k < tb.n[0]) dead |= ge<BV>(v, tb.m[0][k][0]) & ~ge<BV>(v, tb.m[0][k][1]);
+        if (NI <= 2 || k < tb.n[1]) live |= ge<BV>(v, tb.m[1][k][0]) & ~ge<BV>(v, tb.m[1][k][1]);
     }
 }
 

@@ -66,6 +66,12 @@ CASES = [
      None),
     ("Larger than Life Moore(5) torus", "life", (97, 83), dict(r=5, birth=range(34, 46), survive=range(34, 59)), 40,
      10, None),
+    # rules of three and four count intervals: the eight-interval comparator form
+    ("Replicator B1357/S1357, reflecting", "life", (150, 70), dict(birth=[1, 3, 5, 7], survive=[1, 3, 5, 7],
+                                                                     bnd=("r", "r")), 20, 5, None),
+    ("Morley B368/S245 torus", "life", (200, 96), dict(birth=[3, 6, 8], survive=[2, 4, 5]), 30, 10, None),
+    ("Moore(2) three intervals, Constant(1) edges", "life", (130, 77),
+     dict(r=2, birth=[4, 7, 8, 12], survive=[3, 5, 6, 10, 11], bnd=("c", "c"), const=(1, 1)), 20, 4, None),
     ("Larger than Life Moore(3) grid", "life", (70, 90),
      dict(r=3, birth=range(9, 15), survive=range(8, 20), bnd=("c", "c")), 30, 10, None),
     ("Stochastic(0.4) Life", "life", (20, 20), dict(birth=[3], survive=[2, 3], seed=2, scheme="stoch", sp=0.4), 15,
