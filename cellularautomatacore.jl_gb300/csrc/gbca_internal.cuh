@@ -208,9 +208,10 @@ void set_last_error(const char* msg);
 
 // Per-device launch facts, looked up once (launch_cache.cu): raise a kernel's dynamic
 // shared-memory limit to at least `bytes` (the runtime is called only when the limit set
-// before is lower), the SM count, and resident blocks per SM.
+// before is lower), the SM count, the opt-in shared memory per block, and resident blocks per SM.
 cudaError_t ensure_dynamic_smem(const void* fn, size_t bytes);
 int device_sms();
+int smem_optin();
 int blocks_per_sm(const void* fn, int threads, size_t smem);
 
 // Process-wide count of kernel launches (gbca_kernel_launches).

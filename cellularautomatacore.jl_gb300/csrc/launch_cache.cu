@@ -16,6 +16,7 @@ namespace {
 std::mutex g_mu;
 std::map<std::pair<const void*, int>, size_t> g_smem;                      // limit set per kernel, device
 std::map<int, int> g_sms;                                                  // SMs per device
+std::map<int, int> g_optin;                                                // opt-in shared memory per block
 std::map<std::tuple<const void*, int, int, size_t>, int> g_blocks;         // resident blocks per SM
 
 int current_device() {
@@ -48,6 +49,20 @@ int device_sms() {
     }
     g_sms[dev] = nsm;
     return nsm;
+}
+
+int smem_optin() {
+    const int dev = current_device();
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_optin.find(dev);
+    if (it != g_optin.end()) return it->second;
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || optin < 1) {
+        cudaGetLastError();
+        optin = 227 * 1024;  // GB300's opt-in limit
+    }
+    g_optin[dev] = optin;
+    return optin;
 }
 
 int blocks_per_sm(const void* fn, int threads, size_t smem) {

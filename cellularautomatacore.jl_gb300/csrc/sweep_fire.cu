@@ -510,12 +510,7 @@ bool fire_gated(const SweepParams& p) { return p.scheme != GBCA_SYNCHRONOUS || p
 
 bool fire_rows_fit(int steps, int rows, int staging) {
     if (rows < kFireRowsMin || rows > kFireRowsMax || steps < 1) return false;
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
-        cudaGetLastError();
-        optin = 227 * 1024;
-    }
+    const int optin = smem_optin();
     const size_t sx = kFireTX + 2 * (size_t)((steps + 15) / 16 * 16), sy = (size_t)rows + 2 * (size_t)steps;
     const size_t smem = staging == 2 && steps == 1 ? 2 * ((sx * sy + 127) / 128 * 128) : 2 * sx * sy;
     return smem <= (size_t)optin;

@@ -402,27 +402,27 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
             for (int i = 3; i < BV; ++i) v[i] = 0u;
             life_emit<BV, NI, PL, GATED>(v, ca, cb, cm, y, sw, ps, w, tb, p, gt, cc);
         }
-        return;
-    }
-    uint32_t ring[N][BH];
-    uint32_t v[BV];
+    } else {
+        uint32_t ring[N][BH];
+        uint32_t v[BV];
 #pragma unroll
-    for (int i = 0; i < BV; ++i) v[i] = 0u;
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-        hrow<R, PL>(ca + (r0 - R + k) * sw, ps, ring[k]);
-        vadd<BH, BV>(v, ring[k]);
-    }
-    for (int y0 = r0; y0 < r1; y0 += N) {
+        for (int i = 0; i < BV; ++i) v[i] = 0u;
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-            const int y = y0 + k;
-            if (y < r1) {
-                life_emit<BV, NI, PL, GATED>(v, ca, cb, cm, y, sw, ps, w, tb, p, gt, cc);
-                if (y + 1 < r1) {
-                    vsub<BH, BV>(v, ring[k]);
-                    hrow<R, PL>(ca + (y + R + 1) * sw, ps, ring[k]);
-                    vadd<BH, BV>(v, ring[k]);
+            hrow<R, PL>(ca + (r0 - R + k) * sw, ps, ring[k]);
+            vadd<BH, BV>(v, ring[k]);
+        }
+        for (int y0 = r0; y0 < r1; y0 += N) {
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                const int y = y0 + k;
+                if (y < r1) {
+                    life_emit<BV, NI, PL, GATED>(v, ca, cb, cm, y, sw, ps, w, tb, p, gt, cc);
+                    if (y + 1 < r1) {
+                        vsub<BH, BV>(v, ring[k]);
+                        hrow<R, PL>(ca + (y + R + 1) * sw, ps, ring[k]);
+                        vadd<BH, BV>(v, ring[k]);
+                    }
                 }
             }
         }
@@ -816,12 +816,7 @@ SweepChoice life_default_choice(const SweepParams& p0) {
     const double sat = p.scheme == GBCA_STOCHASTIC ? kLifeSatCtasDraws : kLifeSatCtas;
     const double t_launch = 4e-6;
     const int nsm = device_sms();
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
-        cudaGetLastError();
-        optin = 227 * 1024;
-    }
+    const int optin = smem_optin();
     const int64_t words = (p.n1 + 31) / 32;
     SweepChoice best = {Kmax, 0, 0};
     double best_cost = -1.0;
@@ -863,12 +858,7 @@ SweepChoice life_default_choice(const SweepParams& p0) {
 
 bool life_choice_fits(const SweepParams& p, int steps, int rows) {
     if (steps < 1 || rows < 1) return false;
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
-        cudaGetLastError();
-        optin = 227 * 1024;
-    }
+    const int optin = smem_optin();
     return life_smem_bytes(p, life_geometry(p, steps * p.ngates, rows)) <= (size_t)optin;
 }
 
@@ -879,12 +869,7 @@ cudaError_t launch_life_simd(const SweepParams& p0, const int8_t* src, int8_t* d
     if (!make_tables(p, &tb)) return cudaErrorNotSupported;
     LifeGeom g = life_geometry(p, p.nsub, p.tile_y);  // tile_y: the autotuner's pick, or 0
     if (p.mask) {  // the mask's plane: a pick made for the unmasked rule may need shorter tiles
-        int dev = 0, optin = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
-            cudaGetLastError();
-            optin = 227 * 1024;
-        }
+        const int optin = smem_optin();
         for (int ty = g.ty; life_smem_bytes(p, g) > (size_t)optin && ty > 8;) {
             ty /= 2;
             g = life_geometry(p, p.nsub, ty);
