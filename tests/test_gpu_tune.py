@@ -206,6 +206,25 @@ def test_fire_one_step_model_heights(ca, oracle, side):
     st.close()
 
 
+@pytest.mark.parametrize("n1,n2,space,staging", [(4000, 2999, "grid", 1), (4000, 2999, "grid", 2),
+                                                 (2050, 2100, "torus", 1), (2050, 2100, "grid", 0)])
+def test_fire_one_step_model_ragged(ca, oracle, n1, n2, space, staging):
+    """The one-step model's heights on ragged lattices (158 rows on 4000 x 2999, a last tile
+    of 155 rows and a last tile column of 160 cells; 132 rows on 2050 x 2100, two cells in the
+    last tile column), TMA, persistent and vector-load staging, on a grid and a torus (edge
+    tiles through the boundary map): 3 steps from t = 5 against the oracle."""
+    u0 = np.random.default_rng(n1 + staging).integers(0, 3, (n1, n2)).astype(np.int8)
+    sp = ca.Grid(n1, n2) if space == "grid" else ca.Torus(n1, n2)
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 8, {"p": 0.05, "f": 0.002}, space=sp, seed=29)
+    st = ca.allocate_state(ca.GB300Backend(), prob, ca.Synchronous())
+    ca.set_geometry(st, 1, 0, staging)
+    got = _run(ca, prob, st, 5, 3, prob.p)
+    bnd = (oracle.CONSTANT, oracle.CONSTANT) if space == "grid" else (oracle.PERIODIC, oracle.PERIODIC)
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, n1, n2, nbhd=oracle.VON_NEUMANN, seed=29, boundary=bnd)
+    assert np.array_equal(got, oracle.run_array(P, u0, 5, 3, (0.05, 0.002), nthreads=16))
+    st.close()
+
+
 @pytest.mark.parametrize("staging", [0, 1, 2])
 def test_fire_full_height_tiles(ca, oracle, staging):
     """A lattice with enough 256 x 128 tiles to fill every CTA slot twice keeps full-height
