@@ -751,6 +751,28 @@ cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& 
     return launch_rn<R, kMaxIntervals, PL, false, VN>(p, g, tb, src, dst, st, ntiles);
 }
 
+// The kernel of the problem's rule, neighbourhood and radius (life_simd_supported holds).
+cudaError_t launch_by_rule(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
+                           int8_t* dst, cudaStream_t st, int ntiles) {
+    if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1
+        if (p.rule == GBCA_RULE_GENERATIONS) return launch_r<1, 2, true>(p, g, tb, src, dst, st, ntiles);
+        return launch_r<1, 1, true>(p, g, tb, src, dst, st, ntiles);
+    }
+    if (p.rule == GBCA_RULE_GENERATIONS) {  // radius 1 or 2
+        if (p.radius == 1) return launch_r<1, 2>(p, g, tb, src, dst, st, ntiles);
+        return launch_r<2, 2>(p, g, tb, src, dst, st, ntiles);
+    }
+    switch (p.radius) {
+        case 1: return launch_r<1, 1>(p, g, tb, src, dst, st, ntiles);
+        case 2: return launch_r<2, 1>(p, g, tb, src, dst, st, ntiles);
+        case 3: return launch_r<3, 1>(p, g, tb, src, dst, st, ntiles);
+        case 4: return launch_r<4, 1>(p, g, tb, src, dst, st, ntiles);
+        case 5: return launch_r<5, 1>(p, g, tb, src, dst, st, ntiles);
+        case 6: return launch_r<6, 1>(p, g, tb, src, dst, st, ntiles);
+        default: return launch_r<7, 1>(p, g, tb, src, dst, st, ntiles);
+    }
+}
+
 }  // namespace
 
 bool life_simd_supported(const SweepParams& p) {
@@ -875,23 +897,7 @@ cudaError_t launch_life_simd(const SweepParams& p0, const int8_t* src, int8_t* d
             g = life_geometry(p, p.nsub, ty);
         }
     }
-    if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1 (life_simd_supported)
-        if (p.rule == GBCA_RULE_GENERATIONS) return launch_r<1, 2, true>(p, g, tb, src, dst, st);
-        return launch_r<1, 1, true>(p, g, tb, src, dst, st);
-    }
-    if (p.rule == GBCA_RULE_GENERATIONS) {
-        if (p.radius == 1) return launch_r<1, 2>(p, g, tb, src, dst, st);
-        return launch_r<2, 2>(p, g, tb, src, dst, st);
-    }
-    switch (p.radius) {
-        case 1: return launch_r<1, 1>(p, g, tb, src, dst, st);
-        case 2: return launch_r<2, 1>(p, g, tb, src, dst, st);
-        case 3: return launch_r<3, 1>(p, g, tb, src, dst, st);
-        case 4: return launch_r<4, 1>(p, g, tb, src, dst, st);
-        case 5: return launch_r<5, 1>(p, g, tb, src, dst, st);
-        case 6: return launch_r<6, 1>(p, g, tb, src, dst, st);
-        default: return launch_r<7, 1>(p, g, tb, src, dst, st);
-    }
+    return launch_by_rule(p, g, tb, src, dst, st, 0);
 }
 
 }  // namespace gbca
@@ -912,24 +918,7 @@ cudaError_t launch_life_tiles(const SweepParams& p0, const SparseTiles& sp, cons
     g.ty = sp.tile_h;
     g.sw = g.tw + 2 * g.hw + 2;
     g.sy = g.ty + 2 * g.hy;
-    const int n = sp.tiles_x * sp.tiles_y;
-    if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1 (life_simd_supported)
-        if (p.rule == GBCA_RULE_GENERATIONS) return launch_r<1, 2, true>(p, g, tb, src, dst, st, n);
-        return launch_r<1, 1, true>(p, g, tb, src, dst, st, n);
-    }
-    if (p.rule == GBCA_RULE_GENERATIONS) {
-        if (p.radius == 1) return launch_r<1, 2>(p, g, tb, src, dst, st, n);
-        return launch_r<2, 2>(p, g, tb, src, dst, st, n);
-    }
-    switch (p.radius) {
-        case 1: return launch_r<1, 1>(p, g, tb, src, dst, st, n);
-        case 2: return launch_r<2, 1>(p, g, tb, src, dst, st, n);
-        case 3: return launch_r<3, 1>(p, g, tb, src, dst, st, n);
-        case 4: return launch_r<4, 1>(p, g, tb, src, dst, st, n);
-        case 5: return launch_r<5, 1>(p, g, tb, src, dst, st, n);
-        case 6: return launch_r<6, 1>(p, g, tb, src, dst, st, n);
-        default: return launch_r<7, 1>(p, g, tb, src, dst, st, n);
-    }
+    return launch_by_rule(p, g, tb, src, dst, st, sp.tiles_x * sp.tiles_y);
 }
 
 }  // namespace gbca
