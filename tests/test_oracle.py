@@ -71,6 +71,69 @@ def test_life_generations_against_definition(oracle, b, s, C):
         assert np.array_equal(oracle.run_array(P, u, 0, 1, nthreads=3), naive_generations(b, s, C, u))
 
 
+def _axis_images(oracle, kind, n, r):
+    """0-based images of cells -r .. n+r-1 along one axis (src/spaces.jl:46-51): Periodic
+    wraps, Reflecting mirrors with the edge cell repeated (period 2n), -1 beyond Constant."""
+    j = np.arange(-r, n + r)
+    if kind == oracle.PERIODIC:
+        return j % n
+    if kind == oracle.REFLECTING:
+        m = j % (2 * n)
+        return np.where(m < n, m, 2 * n - 1 - m)
+    return np.where((j >= 0) & (j < n), j, -1)
+
+
+def naive_life(oracle, u, r, nbhd, birth, survive, bnd, const):
+    """Life / Larger than Life by definition (src/rules.jl:377-389): n counts the neighbours
+    equal to 1 over Moore(r) or von Neumann(r) (centre excluded), read through the boundary
+    images (beyond two Constant edges the second axis's value wins, src/backends.jl:177-184);
+    the next state is bit n of the survival mask for a cell equal to 1, of the birth mask
+    otherwise, and 0 when n >= 64 (UInt64 masks)."""
+    n1, n2 = u.shape
+    ix, iy = _axis_images(oracle, bnd[0], n1, r), _axis_images(oracle, bnd[1], n2, r)
+    pad = u[np.clip(ix, 0, None)][:, np.clip(iy, 0, None)].astype(np.int64)
+    if bnd[0] == oracle.CONSTANT:
+        pad[ix < 0, :] = const[0]
+    if bnd[1] == oracle.CONSTANT:
+        pad[:, iy < 0] = const[1]
+    alive = (pad == 1).astype(np.int64)
+    n = np.zeros((n1, n2), np.int64)
+    for a in range(-r, r + 1):
+        for b in range(-r, r + 1):
+            if (a, b) == (0, 0) or (nbhd == oracle.VON_NEUMANN and abs(a) + abs(b) > r):
+                continue
+            n += alive[r + a:r + a + n1, r + b:r + b + n2]
+    masks = np.where(u == 1, np.uint64(survive), np.uint64(birth)).astype(np.uint64)
+    bit = (masks >> np.minimum(n, 63).astype(np.uint64)) & np.uint64(1)
+    return np.where(n < 64, bit, 0).astype(np.int8)
+
+
+@pytest.mark.parametrize("nb,r,dims,bnd,const", [
+    ("moore", 2, (20, 17), "pp", (0, 0)), ("moore", 5, (30, 24), "cc", (1, 0)), ("moore", 6, (5, 9), "pr", (0, 0)),
+    ("moore", 7, (33, 40), "rc", (0, 1)), ("moore", 7, (16, 16), "cp", (1, 0)), ("vn", 1, (11, 13), "rr", (0, 0)),
+    ("vn", 3, (14, 9), "cp", (1, 0)), ("vn", 7, (6, 20), "pc", (0, 1))])
+def test_larger_than_life_against_definition(oracle, nb, r, dims, bnd, const):
+    """The oracle's Life on Moore(r) and von Neumann(r) up to r = 7 against a numpy
+    restatement of the definition, on every boundary kind (lattices smaller than the radius
+    included), random 64-bit count masks and states holding values other than 0 and 1."""
+    kinds = {"p": oracle.PERIODIC, "r": oracle.REFLECTING, "c": oracle.CONSTANT}
+    bounds = (kinds[bnd[0]], kinds[bnd[1]])
+    nbhd = oracle.MOORE if nb == "moore" else oracle.VON_NEUMANN
+    rng = np.random.default_rng(1000 * r + dims[0])
+    n1, n2 = dims
+    for trial in range(3):
+        birth = int(rng.integers(0, 2 ** 63)) | (int(rng.integers(0, 2)) << 63)
+        survive = int(rng.integers(0, 2 ** 63))
+        u = (rng.random((n1, n2)) < (0.15, 0.35, 0.6)[trial]).astype(np.int8)
+        u[rng.random((n1, n2)) < 0.05] = 2
+        u[rng.random((n1, n2)) < 0.02] = -1
+        P = oracle.Problem(oracle.RULE_LIFE, n1, n2, nbhd=nbhd, radius=r, birth=birth, survive=survive,
+                           boundary=bounds, constant=const)
+        want = naive_life(oracle, u, r, nbhd, birth, survive, bounds, const)
+        assert np.array_equal(oracle.step_reference(P, u, 0), want)
+        assert np.array_equal(oracle.run_array(P, u, 0, 1, nthreads=3), want)
+
+
 def test_classic_patterns(oracle):
     """Blinker, block and glider (test/test_rules.jl:109-122)."""
     life = oracle.Problem(oracle.RULE_LIFE, 5, 5, birth=oracle.mask([3]), survive=oracle.mask([2, 3]))
