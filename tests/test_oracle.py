@@ -134,6 +134,77 @@ def test_larger_than_life_against_definition(oracle, nb, r, dims, bnd, const):
         assert np.array_equal(oracle.run_array(P, u, 0, 1, nthreads=3), want)
 
 
+def _neighbour_images(oracle, u, nbhd, bnd, const):
+    """The radius-1 neighbour values of every cell, read through the boundary images (as
+    naive_life does), as a list of arrays in the neighbourhood's offset order."""
+    n1, n2 = u.shape
+    ix, iy = _axis_images(oracle, bnd[0], n1, 1), _axis_images(oracle, bnd[1], n2, 1)
+    pad = u[np.clip(ix, 0, None)][:, np.clip(iy, 0, None)].astype(np.int64)
+    if bnd[0] == oracle.CONSTANT:
+        pad[ix < 0, :] = const[0]
+    if bnd[1] == oracle.CONSTANT:
+        pad[:, iy < 0] = const[1]
+    offs = [(a, b) for b in (-1, 0, 1) for a in (-1, 0, 1) if (a, b) != (0, 0)
+            and (nbhd == oracle.MOORE or abs(a) + abs(b) == 1)]
+    return [pad[1 + a:1 + a + n1, 1 + b:1 + b + n2] for a, b in offs]
+
+
+@pytest.mark.parametrize("nb,bnd,const,dims", [("vn", "cc", (0, 0), (12, 9)), ("vn", "pp", (0, 0), (10, 11)),
+                                               ("moore", "rc", (0, 2), (9, 13)), ("vn", "cp", (2, 0), (7, 8))])
+def test_forest_fire_against_definition(oracle, nb, bnd, const, dims):
+    """One forest-fire step by definition (the package README's rule on Int8 codes), with
+    draws from the oracle's Philox uniform (pinned by the known answers above) keyed by the
+    1-based column-major cell id (i - 1) + (j - 1) n1 + 1, the time of the state read, and
+    draw index 1 (empty -> tree) or 2 (lightning): 2 -> 0; 0 -> 1 iff u < p; any other state
+    -> 2 next to a fire, else 2 iff u < f, else 1."""
+    kinds = {"p": oracle.PERIODIC, "r": oracle.REFLECTING, "c": oracle.CONSTANT}
+    bounds = (kinds[bnd[0]], kinds[bnd[1]])
+    nbhd = oracle.MOORE if nb == "moore" else oracle.VON_NEUMANN
+    n1, n2 = dims
+    rng = np.random.default_rng(n1 * n2)
+    p, f, seed = 0.4, 0.2, 17
+    for t in (0, 5):
+        u = rng.integers(0, 3, (n1, n2)).astype(np.int8)
+        u[rng.random((n1, n2)) < 0.05] = 4
+        fire_near = np.zeros((n1, n2), bool)
+        for v in _neighbour_images(oracle, u, nbhd, bounds, const):
+            fire_near |= v == 2
+        want = np.zeros((n1, n2), np.int8)
+        for i in range(n1):
+            for j in range(n2):
+                cid = i + j * n1 + 1
+                c = u[i, j]
+                if c == 2:
+                    want[i, j] = 0
+                elif c == 0:
+                    want[i, j] = 1 if oracle.uniform(seed, cid, t, 1) < p else 0
+                elif fire_near[i, j]:
+                    want[i, j] = 2
+                else:
+                    want[i, j] = 2 if oracle.uniform(seed, cid, t, 2) < f else 1
+        P = oracle.Problem(oracle.RULE_FOREST_FIRE, n1, n2, nbhd=nbhd, seed=seed, boundary=bounds, constant=const)
+        assert np.array_equal(oracle.step_reference(P, u, t, (p, f)), want)
+        assert np.array_equal(oracle.run_array(P, u, t, 1, (p, f), nthreads=2), want)
+
+
+def test_stochastic_gate_against_definition(oracle):
+    """Stochastic(p) (src/schemes.jl:84-89): a cell updates iff draw 0 of its id at the step's
+    time falls below p, else keeps its state; the update is the synchronous rule's."""
+    n1, n2, seed, p = 14, 11, 23, 0.45
+    rng = np.random.default_rng(5)
+    B3S23 = dict(birth=oracle.mask([3]), survive=oracle.mask([2, 3]))
+    for t in (0, 3):
+        u = (rng.random((n1, n2)) < 0.4).astype(np.int8)
+        sync = naive_life(oracle, u, 1, oracle.MOORE, B3S23["birth"], B3S23["survive"],
+                          (oracle.PERIODIC, oracle.PERIODIC), (0, 0))
+        open_ = np.array([[oracle.uniform(seed, i + j * n1 + 1, t, 0) < p for j in range(n2)] for i in range(n1)])
+        want = np.where(open_, sync, u).astype(np.int8)
+        P = oracle.Problem(oracle.RULE_LIFE, n1, n2, seed=seed, scheme=oracle.STOCHASTIC, scheme_p=p, **B3S23)
+        assert np.array_equal(oracle.step_reference(P, u, t), want)
+        assert np.array_equal(oracle.run_array(P, u, t, 1, nthreads=2), want)
+        assert 0 < open_.sum() < open_.size
+
+
 def test_classic_patterns(oracle):
     """Blinker, block and glider (test/test_rules.jl:109-122)."""
     life = oracle.Problem(oracle.RULE_LIFE, 5, 5, birth=oracle.mask([3]), survive=oracle.mask([2, 3]))
