@@ -134,6 +134,43 @@ def test_larger_than_life_against_definition(oracle, nb, r, dims, bnd, const):
         assert np.array_equal(oracle.run_array(P, u, 0, 1, nthreads=3), want)
 
 
+@pytest.mark.parametrize("nb,r,C,bnd,const", [("moore", 2, 3, "rc", (0, 2)), ("moore", 2, 4, "cc", (1, 3)),
+                                              ("vn", 1, 4, "pr", (0, 0)), ("moore", 1, 3, "cp", (2, 0))])
+def test_generations_radius_and_edges_against_definition(oracle, nb, r, C, bnd, const):
+    """Generations (src/rules.jl:446-456) on Moore(2) and von Neumann(1) with Reflecting and
+    Constant edges, by definition: the count of neighbours equal to 1 (naive_life's count),
+    0 -> 1 on a birth count, 1 -> 1 on a survival count else 2 (or 0 when C = 2), s >= 2 ->
+    s + 1 below C, else 0."""
+    kinds = {"p": oracle.PERIODIC, "r": oracle.REFLECTING, "c": oracle.CONSTANT}
+    bounds = (kinds[bnd[0]], kinds[bnd[1]])
+    nbhd = oracle.MOORE if nb == "moore" else oracle.VON_NEUMANN
+    rng = np.random.default_rng(100 * r + C)
+    n1, n2 = 17, 12
+    birth, survive = oracle.mask([2, 3, 7]), oracle.mask([1, 3, 4, 5, 9])
+    for _ in range(3):
+        u = rng.integers(0, C, (n1, n2)).astype(np.int8)
+        # n: the neighbours equal to 1, read through the boundary images
+        ix, iy = _axis_images(oracle, bounds[0], n1, r), _axis_images(oracle, bounds[1], n2, r)
+        pad = u[np.clip(ix, 0, None)][:, np.clip(iy, 0, None)].astype(np.int64)
+        if bounds[0] == oracle.CONSTANT:
+            pad[ix < 0, :] = const[0]
+        if bounds[1] == oracle.CONSTANT:
+            pad[:, iy < 0] = const[1]
+        n = np.zeros((n1, n2), np.int64)
+        for a in range(-r, r + 1):
+            for b in range(-r, r + 1):
+                if (a, b) != (0, 0) and (nbhd == oracle.MOORE or abs(a) + abs(b) <= r):
+                    n += pad[r + a:r + a + n1, r + b:r + b + n2] == 1
+        bit = lambda m: ((np.uint64(m) >> n.astype(np.uint64)) & np.uint64(1)).astype(bool)
+        want = np.where(u == 0, bit(birth).astype(np.int8),
+                        np.where(u == 1, np.where(bit(survive), 1, 2 if C > 2 else 0),
+                                 np.where(u + 1 < C, u + 1, 0))).astype(np.int8)
+        P = oracle.Problem(oracle.RULE_GENERATIONS, n1, n2, nbhd=nbhd, radius=r, birth=birth, survive=survive,
+                           states=C, boundary=bounds, constant=const)
+        assert np.array_equal(oracle.step_reference(P, u, 0), want)
+        assert np.array_equal(oracle.run_array(P, u, 0, 1, nthreads=2), want)
+
+
 def _neighbour_images(oracle, u, nbhd, bnd, const):
     """The radius-1 neighbour values of every cell, read through the boundary images (as
     naive_life does), as a list of arrays in the neighbourhood's offset order."""
