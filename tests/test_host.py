@@ -40,6 +40,29 @@ def test_library_exports_every_declared_symbol(ca):
     assert lib.gbca_version() >= 100
 
 
+def declared_parameter_counts():
+    """{function: number of parameters} from the prototypes in include/*.h."""
+    counts = {}
+    for name in os.listdir(os.path.join(ROOT, "include")):
+        if name.endswith(".h"):
+            with open(os.path.join(ROOT, "include", name)) as f:
+                src = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+            for fn, params in re.findall(r"\b(gbca_[a-z0-9_]+)\s*\(([^;{)]*)\)\s*;", src):
+                params = params.strip()
+                counts[fn] = 0 if params in ("", "void") else params.count(",") + 1
+    return counts
+
+
+def test_bindings_match_prototypes(ca):
+    """Every function the Python binding calls takes as many arguments as include/gbca.h
+    declares (a changed prototype without a changed binding would pass garbage through ctypes)."""
+    counts = declared_parameter_counts()
+    assert len(counts) >= 40
+    assert set(counts) == declared_symbols()  # every prototype parsed
+    for fn, (_, argtypes) in ca.capi.SIGNATURES.items():
+        assert len(argtypes) == counts[fn], (fn, len(argtypes), counts[fn])
+
+
 def test_thresholds_equal_float_compares(ca, oracle):
     """uniform < p (random.jl:116-120, FP64; :109-114, FP32) <=> x < T for the draw's integer x."""
     rng = np.random.default_rng(7)
