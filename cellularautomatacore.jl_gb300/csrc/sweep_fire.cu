@@ -519,18 +519,16 @@ bool fire_rows_fit(int steps, int rows, int staging) {
 cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, cudaStream_t st) {
     SweepParams p = p0;
     p.tile_x = kFireTX;
-    // tile rows: 128, 64 or 32, whichever keeps the most of the GPU busy. The tiles run in
-    // rounds of one per CTA slot (two CTAs per SM), so a lattice of t tiles fills
-    // (t / slots) / ceil(t / slots) of the last round's share; a shorter tile recomputes a
-    // larger share of halo rows, TY / (TY + 2 halo) useful.
+    // tile rows: pinned, or a model's pick
     if (p0.tile_y > 0) {  // pinned (gbca_set_geometry checked that it fits)
         p.tile_y = p0.tile_y;
     } else if (p.nsub == 1) {
-        // one step per pass: the busiest SM's tiles, ceil(tiles / SMs), times the cost of a
-        // tile, its rows plus kFireTileCost rows' worth of halo, staging and set-up. Fitted to
-        // Gcell-updates/s measured by height on 2048^2, 4096^2 and 8192^2 grids: the minimum
-        // falls on 108, 108 and 160 rows (255, 329, 384 against 227, 292, 375 for the best
-        // power of two), and the model ranks the other heights as measured.
+        // one step per pass, any height of 32..160 rows: minimise the busiest SM's tiles,
+        // ceil(tiles / SMs), times the cost of a tile, its rows plus kFireTileCost rows' worth
+        // of halo, staging and set-up. The constant is fitted to Gcell-updates/s measured by
+        // height on 2048^2, 4096^2 and 8192^2 grids; the model's picks there (108, 147 and 158
+        // rows) ran fastest of the heights measured, 255, 336 and 387 against 227, 292 and 376
+        // for the best of 128, 64 and 32 rows.
         const int64_t tx = (p.n1 + kFireTX - 1) / kFireTX, nsm = device_sms();
         int64_t best = -1;
         for (int ty = kFireRowsOneStep; ty >= 32; --ty) {
@@ -542,6 +540,10 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
             }
         }
     } else {
+        // deeper passes: 128, 64 or 32 rows, whichever keeps the most of the GPU busy. The
+        // tiles run in rounds of one per CTA slot (two CTAs per SM), so a lattice of t tiles
+        // fills (t / slots) / ceil(t / slots) of the last round's share; a shorter tile
+        // recomputes a larger share of halo rows, TY / (TY + 2 halo) useful.
         const int64_t tx = (p.n1 + kFireTX - 1) / kFireTX, slots = 2 * (int64_t)device_sms();
         double best = -1.0;
         for (int ty = kFireTY; ty >= 32; ty /= 2) {
