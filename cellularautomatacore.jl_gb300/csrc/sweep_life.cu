@@ -42,6 +42,11 @@
 // (x, y) when its draw k = 0 at time t falls below p, the draw keyed by the mapped cell's id as
 // in the rule's own draws. A closed Life cell keeps its value, which the indicator bits hold
 // only for states 0 and 1, so gated Life needs every state in {0, 1} (the host scans it).
+//
+// Masks (src/environment.jl:123-130) use the gated form too: the loader packs the mask's
+// nonzero bytes into one more bit plane, mapped through the boundary like the state, and a
+// sub-step's gate is ANDed with it, so a masked cell, and each halo image of one, keeps its
+// state.
 #include "gbca_internal.cuh"
 
 namespace gbca {
