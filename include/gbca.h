@@ -138,7 +138,9 @@ int gbca_write_cell(gbca_handle* h, int64_t i, int64_t j, const void* value);
  * Replaces CAProblem's `mask` (problem.jl:20-27, environment.jl:123-130): cells whose byte is
  * 0 never update, though their neighbours still read them (backends.jl:448-450). `host` holds
  * n1*n2 bytes, column-major, nonzero = the cell updates; NULL removes the mask. Int8 rules
- * only (GBCA_ERR_UNSUPPORTED for Lenia). A masked problem runs on the general kernel. */
+ * only (GBCA_ERR_UNSUPPORTED for Lenia). A masked forest fire runs its fast kernel one step per
+ * launch; masked Life and Generations of radius <= 2 (Moore) or von Neumann(1) run the
+ * bit-sliced kernel with the mask as a bit plane; other masked problems the general kernel. */
 int gbca_set_mask(gbca_handle* h, const uint8_t* host, size_t nbytes);
 
 /* Replaces the resolved KernelField of a GBCA_RULE_SI_FIELD problem (environment.jl:53-69):
