@@ -329,6 +329,31 @@ def test_checkerboard_against_definition(oracle):
     assert np.array_equal(o.step_reference(P, u, 0), v)
 
 
+@pytest.mark.parametrize("nb,r,dims,bnd,const", [("moore", 1, (9, 11), "rr", (0, 0)), ("moore", 2, (13, 10), "cp", (1, 0)),
+                                                ("vn", 1, (7, 7), "pc", (0, 1)), ("moore", 2, (11, 9), "pp", (0, 0))])
+def test_checkerboard_edges_against_definition(oracle, nb, r, dims, bnd, const):
+    """Checkerboard (src/schemes.jl:42-51) on Reflecting, Constant and odd Periodic edges: the
+    cells of even 1-based index sum take the synchronous rule's value (naive_life) from the
+    current state, then the odd cells from the state the first half left; halo cells read
+    through the boundary images, so they carry their images' states."""
+    kinds = {"p": oracle.PERIODIC, "r": oracle.REFLECTING, "c": oracle.CONSTANT}
+    bounds = (kinds[bnd[0]], kinds[bnd[1]])
+    nbhd = oracle.MOORE if nb == "moore" else oracle.VON_NEUMANN
+    n1, n2 = dims
+    birth, survive = oracle.mask([2, 3, 6]), oracle.mask([1, 2, 4, 5])
+    rng = np.random.default_rng(n1 * 31 + n2)
+    i, j = np.meshgrid(np.arange(1, n1 + 1), np.arange(1, n2 + 1), indexing="ij")
+    for _ in range(2):
+        u = (rng.random((n1, n2)) < 0.4).astype(np.int8)
+        v = u
+        for odd in (0, 1):
+            v = np.where((i + j) % 2 == odd, naive_life(oracle, v, r, nbhd, birth, survive, bounds, const), v)
+        P = oracle.Problem(oracle.RULE_LIFE, n1, n2, nbhd=nbhd, radius=r, birth=birth, survive=survive,
+                           boundary=bounds, constant=const, scheme=oracle.CHECKERBOARD)
+        assert np.array_equal(oracle.step_reference(P, u, 0), v)
+        assert np.array_equal(oracle.run_array(P, u, 0, 1, nthreads=2), v)
+
+
 def test_forest_fire_rates(oracle):
     """bernoulli(p) hits at rate p (test/test_random.jl:51-56) through the rule."""
     o = oracle
