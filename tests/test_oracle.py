@@ -354,6 +354,33 @@ def test_checkerboard_edges_against_definition(oracle, nb, r, dims, bnd, const):
         assert np.array_equal(oracle.run_array(P, u, 0, 1, nthreads=2), v)
 
 
+@pytest.mark.parametrize("scheme,bnd,const", [("sync", "rr", (0, 0)), ("stoch", "cp", (1, 0))])
+def test_mask_against_definition(oracle, scheme, bnd, const):
+    """A mask (src/environment.jl:123-130, src/backends.jl:448-450): a cell whose mask is
+    false keeps its state in every step, while its neighbours still read it; the others take
+    the scheme's update (Moore(2) Life here, the Stochastic gate as draw 0 below p)."""
+    kinds = {"p": oracle.PERIODIC, "r": oracle.REFLECTING, "c": oracle.CONSTANT}
+    bounds = (kinds[bnd[0]], kinds[bnd[1]])
+    n1, n2, seed, p = 15, 12, 8, 0.6
+    birth, survive = oracle.mask([4, 5, 6, 7]), oracle.mask([3, 4, 5, 6, 8])
+    rng = np.random.default_rng(len(scheme) + n1)
+    for t in (0, 2):
+        u = (rng.random((n1, n2)) < 0.35).astype(np.int8)
+        mask = rng.random((n1, n2)) < 0.7
+        upd = naive_life(oracle, u, 2, oracle.MOORE, birth, survive, bounds, const)
+        if scheme == "stoch":
+            gate = np.array([[oracle.uniform(seed, i + j * n1 + 1, t, 0) < p for j in range(n2)] for i in range(n1)])
+            upd = np.where(gate, upd, u)
+        want = np.where(mask, upd, u).astype(np.int8)
+        P = oracle.Problem(oracle.RULE_LIFE, n1, n2, radius=2, birth=birth, survive=survive, boundary=bounds,
+                           constant=const, seed=seed, scheme=oracle.STOCHASTIC if scheme == "stoch" else
+                           oracle.SYNCHRONOUS, scheme_p=p if scheme == "stoch" else 1.0)
+        E = oracle.Env(mask=mask)
+        assert np.array_equal(oracle.step_reference_env(P, E, u, t), want)
+        assert np.array_equal(oracle.run_array_env(P, E, u, t, 1, nthreads=2), want)
+        assert np.array_equal(want[~mask], u[~mask]) and not np.array_equal(want, u)
+
+
 def test_forest_fire_rates(oracle):
     """bernoulli(p) hits at rate p (test/test_random.jl:51-56) through the rule."""
     o = oracle
