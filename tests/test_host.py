@@ -182,3 +182,35 @@ def test_problem_validation(ca):
     with pytest.raises(ca.ArgumentError):
         ca.check_problem(B, ca.CAProblem.new(ca.Lenia(method="fft", precision="Float32"), np.zeros((8, 8), np.float32), 1,
                                              space=ca.Grid(8, 8)), ca.Synchronous())
+
+
+def test_no_device_fails_loudly(ca):
+    """Without a visible GPU the library refuses to create a handle (a CUDA error naming the
+    missing device) instead of running anywhere else, and the no-alloc entry point refuses a
+    sweep it cannot run; its argument checks come first and touch no memory."""
+    import ctypes
+    lib = ca.capi.lib()
+    if lib.gbca_device_count() > 0:
+        pytest.skip("a GPU is visible: the refusal applies to machines without one")
+    h = ctypes.c_void_p()
+    rc = lib.gbca_create(ctypes.byref(desc_for(ca)), ctypes.byref(h))
+    assert rc == ca.capi.ERR_CUDA and not h.value
+    assert "device" in lib.gbca_last_error().decode()
+    buf = np.zeros(8 * 1024 + 64, np.int8)
+    addr = buf.ctypes.data + (-buf.ctypes.data) % 16  # a 16-byte aligned host address, never written
+    big = desc_for(ca, n1=4096, n2=4097)  # one column more than the scratch array holds
+    with pytest.raises(ca.ArgumentError, match="scratch"):
+        ca.capi.check(lib.gbca_advance_noalloc(ctypes.byref(big), ctypes.c_void_p(addr), 4096, 0, 1, None, 0, None))
+    with pytest.raises(ca.ArgumentError, match="aligned"):
+        ca.capi.check(lib.gbca_advance_noalloc(ctypes.byref(desc_for(ca)), ctypes.c_void_p(addr + 1), 16, 0, 1, None,
+                                               0, None))
+    with pytest.raises(ca.ArgumentError):
+        ca.capi.check(lib.gbca_advance_noalloc(ctypes.byref(desc_for(ca)), ctypes.c_void_p(addr), 4, 0, 1, None, 0,
+                                               None))  # pitch below n1
+    with pytest.raises(ca.UnsupportedCombinationError):
+        ca.capi.check(lib.gbca_advance_noalloc(ctypes.byref(desc_for(ca, rule=ca.capi.RULE_LENIA)),
+                                               ctypes.c_void_p(addr), 32, 0, 1, None, 0, None))
+    assert lib.gbca_advance_noalloc(ctypes.byref(desc_for(ca)), ctypes.c_void_p(addr), 16, 0, 0, None, 0,
+                                    None) == ca.capi.OK  # zero steps: nothing to run
+    rc = lib.gbca_advance_noalloc(ctypes.byref(desc_for(ca)), ctypes.c_void_p(addr), 16, 0, 1, None, 0, None)
+    assert rc == ca.capi.ERR_CUDA and not buf.any()
