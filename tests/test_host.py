@@ -214,3 +214,7 @@ def test_no_device_fails_loudly(ca):
                                     None) == ca.capi.OK  # zero steps: nothing to run
     rc = lib.gbca_advance_noalloc(ctypes.byref(desc_for(ca)), ctypes.c_void_p(addr), 16, 0, 1, None, 0, None)
     assert rc == ca.capi.ERR_CUDA and not buf.any()
+    # the reference-facing call raises too
+    prob = ca.CAProblem.new(ca.Life(), np.zeros((8, 8), np.int8), 2)
+    with pytest.raises(ca.errors.GPUError, match="no CUDA device"):
+        ca.solve(prob, backend=ca.GB300Backend())
