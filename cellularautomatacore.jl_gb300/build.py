@@ -6,6 +6,7 @@ import glob
 import os
 import shutil
 import subprocess
+import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -43,6 +44,7 @@ def _stale() -> bool:
 def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     """Compile and link; returns the path of libgbca.so."""
     if not force and not _stale():
+        print(f"libgbca.so: up to date, reused ({LIB})", file=sys.stderr)
         return LIB
     os.makedirs(os.path.join(OUT, "obj"), exist_ok=True)
     cc = nvcc()
@@ -65,10 +67,10 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    print(f"libgbca.so: compiled from source ({len(objs)} translation units)", file=sys.stderr)
     return LIB
 
 
 if __name__ == "__main__":
-    import sys
     print(build(force="--force" in sys.argv, verbose=True,
                 extra_flags=["-Xptxas", "-v"] if "--ptxas" in sys.argv else []))

@@ -1,0 +1,7 @@
+// sweep_life_r1.cu — the bit-sliced sweep's kernels for Moore(1) (life_kernel.cuh).
+#include "life_kernel.cuh"
+
+namespace gbca {
+template cudaError_t launch_life_radius<1>(const SweepParams&, const LifeGeom&, const LifeTables&, const int8_t*,
+                                             int8_t*, cudaStream_t, int);
+}  // namespace gbca

@@ -7,7 +7,7 @@ reference checkout; the fixtures are committed so that nothing reads it at test 
 * ``rule_strings.json`` — the rule-string presets of ``src/rules.jl:249-265`` (names and
   B/S strings), extracted the same way, for the host-side rule parser tests.
 
-Usage: python tests/golden/make_golden.py [path-to-reference-checkout]
+Usage: python tests/golden/make_golden.py <path-to-reference-checkout>
 """
 import json
 import os
@@ -48,4 +48,6 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path-to-reference-checkout>")
+    main(sys.argv[1])
