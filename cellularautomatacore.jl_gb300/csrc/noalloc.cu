@@ -17,13 +17,24 @@
 // or from different host threads) race on the array. Serialise them.
 //
 // Set-up: the first call on each device looks up the array's device address with
-// cudaGetSymbolAddress, with that device current, and caches it. That first call should come
-// before any stream capture on the device.
+// cudaGetSymbolAddress, with that device current, and caches it under the identity of the
+// current CUDA context (cuCtxGetId), so a context that was destroyed and created again (after
+// cudaDeviceReset, say, when the module reloads and the array may move) gets a fresh lookup
+// rather than a stale address. That first call should come before any stream capture on the
+// device.
+//
+// The sweep itself is the one gbca_advance runs (sweep_int8: the same kernels, tuned or
+// pinned geometry and TMA staging), between the caller's state and the array, so results
+// are gbca_advance's bit for bit. The states are not scanned first (that would need a device
+// flag of its own): Generations, and Life under a gate or a mask, run the general kernel,
+// which reads any state; the forest fire compares whole bytes on its first step only.
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+
+#include <cuda.h>
 
 #include "gbca_internal.cuh"
 
@@ -33,9 +44,42 @@ namespace {
 
 static __device__ __align__(256) int8_t g_noalloc_scratch[GBCA_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
+// Looked-up addresses by (device, context id): a handful of contexts per process at most.
+constexpr int kMaxContexts = 64;
+struct ScratchEntry {
+    int dev;
+    unsigned long long ctx_id;
+    void* addr;
+};
 std::mutex g_scratch_mutex;
-void* g_scratch_addr[kMaxDevices] = {nullptr};
+ScratchEntry g_scratch[kMaxContexts];
+int g_scratch_n = 0;
+
+typedef CUresult (*CtxGetCurrent)(CUcontext*);
+typedef CUresult (*CtxGetId)(CUcontext, unsigned long long*);
+CtxGetCurrent g_ctx_current = nullptr;
+CtxGetId g_ctx_id = nullptr;
+bool g_ctx_looked = false;
+
+// The id of the calling thread's current context, or false when there is none yet (the
+// runtime creates the device's primary context on its first call that needs one).
+bool current_context_id(unsigned long long* id) {
+    if (!g_ctx_looked) {
+        g_ctx_looked = true;
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_current = (CtxGetCurrent)fn;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_id = (CtxGetId)fn;
+        cudaGetLastError();
+    }
+    CUcontext ctx = nullptr;
+    if (!g_ctx_current || !g_ctx_id || g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return g_ctx_id(ctx, id) == CUDA_SUCCESS;
+}
 
 int nfail(int code, const char* fmt, ...) {
     char msg[512];
@@ -47,20 +91,29 @@ int nfail(int code, const char* fmt, ...) {
     return code;
 }
 
-// The device address of the scratch array on the current device (looked up once per device).
+// The device address of the scratch array in the current context of the current device
+// (looked up once per context).
 cudaError_t scratch_address(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_addr[dev] = p;
+    unsigned long long id = 0;
+    const bool have_id = current_context_id(&id);
+    if (have_id)
+        for (int i = 0; i < g_scratch_n; ++i)
+            if (g_scratch[i].dev == dev && g_scratch[i].ctx_id == id) {
+                *out = g_scratch[i].addr;
+                return cudaSuccess;
+            }
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // creates the primary context if needed
+    if (e != cudaSuccess) return e;
+    if (have_id || current_context_id(&id)) {
+        ScratchEntry& slot = g_scratch[g_scratch_n < kMaxContexts ? g_scratch_n++ : (int)(id % kMaxContexts)];
+        slot = ScratchEntry{dev, id, p};
     }
-    *out = g_scratch_addr[dev];
+    *out = p;
     return cudaSuccess;
 }
 
@@ -95,71 +148,10 @@ extern "C" int gbca_advance_noalloc(const gbca_desc* desc, void* state, int64_t 
     cudaError_t e = scratch_address(&scratch);
     if (e != cudaSuccess) return nfail(GBCA_ERR_CUDA, "scratch address: %s", cudaGetErrorString(e));
     cudaStream_t st = (cudaStream_t)stream;
-
-    SweepParams p;
-    std::memset(&p, 0, sizeof p);
-    p.n1 = desc->n1;
-    p.n2 = desc->n2;
-    p.pitch = pitch;
-    for (int a = 0; a < 2; ++a) {
-        p.bnd[a] = desc->boundary[a];
-        p.cval[a] = desc->boundary[a] == GBCA_CONSTANT ? (int32_t)desc->constant[a] : 0;
-    }
-    p.rule = desc->rule;
-    p.nbhd = desc->nbhd;
-    p.radius = desc->radius;
-    p.states = desc->states;
-    p.birth = desc->birth;
-    p.survive = desc->survive;
-    p.seed = desc->seed;
-    p.scheme = desc->scheme;
-    p.gate_f32 = desc->scheme_p_f32;
-    p.gate_thr = desc->scheme == GBCA_STOCHASTIC ? gbca_threshold(desc->scheme_p, desc->scheme_p_f32) : 0;
-    p.params_f32 = desc->params_f32;
-    p.ngates = desc->scheme == GBCA_CHECKERBOARD ? 2 : 1;
-    if (desc->rule == GBCA_RULE_FOREST_FIRE) {
-        p.thr_p = gbca_threshold(params[0], desc->params_f32);
-        p.thr_f = gbca_threshold(params[1], desc->params_f32);
-    }
-    const bool fire = fire_fast_supported(p);
-    const bool life = !fire && life_simd_supported(p);
     int8_t* bufs[2] = {(int8_t*)state, (int8_t*)scratch};
     int cur = 0;
-    if (fire && fire_gated(p)) {  // a gate or a mask: one sub-step per launch
-        for (; nsteps > 0; ++t, --nsteps) {
-            e = fire_gated_step(p, bufs, &cur, t, st);
-            if (e != cudaSuccess) return nfail(GBCA_ERR_CUDA, "sweep launch: %s", cudaGetErrorString(e));
-        }
-    }
-    while (nsteps > 0) {
-        int64_t k;
-        const int8_t* src = bufs[cur];
-        int8_t* dst = bufs[cur ^ 1];
-        p.t0 = t;
-        if (fire) {
-            k = nsteps < 8 ? nsteps : 8;
-            p.nsub = (int32_t)k;
-            e = launch_fire(p, src, dst, st);
-        } else if (life) {
-            const int64_t per = life_steps_per_pass(p);
-            k = nsteps < per ? nsteps : per;
-            p.nsub = (int32_t)(k * p.ngates);  // sub-steps: two half-steps per Checkerboard step
-            e = launch_life_simd(p, src, dst, st);
-        } else {
-            int64_t per = kGenericSubsteps / (p.radius * p.ngates);
-            if (per < 1) per = 1;
-            k = nsteps < per ? nsteps : per;
-            p.nsub = (int32_t)(k * p.ngates);
-            p.tile_x = p.tile_y = 64;
-            p.halo_x = p.halo_y = p.nsub * p.radius;
-            e = launch_generic(p, src, dst, st);
-        }
-        if (e != cudaSuccess) return nfail(GBCA_ERR_CUDA, "sweep launch: %s", cudaGetErrorString(e));
-        count_launch();
-        cur ^= 1;
-        t += k;
-        nsteps -= k;
-    }
+    e = sweep_int8(*desc, pitch, bufs, &cur, t, nsteps, params, st);
+    if (e != cudaSuccess) return nfail(GBCA_ERR_CUDA, "sweep launch: %s", cudaGetErrorString(e));
     if (cur == 1) {  // the result is in the scratch array: copy it back into the caller's state
         e = cudaMemcpy2DAsync(state, (size_t)pitch, scratch, (size_t)pitch, (size_t)desc->n1, (size_t)desc->n2,
                               cudaMemcpyDeviceToDevice, st);

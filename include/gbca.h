@@ -373,9 +373,15 @@ int gbca_server_stop(gbca_server* s);
  * Lenia (whose FFT plans allocate) with GBCA_ERR_UNSUPPORTED. Results are those of
  * gbca_advance, bit for bit. The work is queued; the call returns before it finishes.
  *
- * The first call on a device looks up the scratch array's address there (make it before
- * any stream capture on that device). All calls share the array and it keeps the last
- * call's contents: calls that overlap on the GPU race on it, so serialise them. */
+ * The sweep is gbca_advance's own (same kernels, geometry and staging). The state is not
+ * scanned first, so Generations, and Life under a gate or a mask, take the general kernel
+ * (slower than the bit-sliced one it would reach on a handle, same results).
+ *
+ * The first call on a device looks up the scratch array's address in the calling thread's
+ * current CUDA context (make it before any stream capture on that device); the address is
+ * kept per context, and a context created anew (after cudaDeviceReset) is looked up again.
+ * All calls share the array and it keeps the last call's contents: calls that overlap on
+ * the GPU race on it, so serialise them. */
 int gbca_advance_noalloc(const gbca_desc* desc, void* state, int64_t pitch, int64_t t, int64_t nsteps,
                          const double* params, int32_t nparams, void* stream);
 

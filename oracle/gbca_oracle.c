@@ -448,6 +448,12 @@ void or_state_counts(const int8_t* u, int64_t n, int64_t* counts, int32_t nvals,
     if (other) *other = o;
 }
 
+void or_soup(uint64_t seed, int64_t n1, int64_t n2, double density, int8_t* out) {
+    const float p = (float)density;
+    for (int64_t q = 0; q < n1 * n2; ++q)
+        out[q] = (int8_t)(or_uniform32(seed, (uint64_t)q + 1u, (int64_t)0xFFFFFFFFu, 0xFFFFFFFEu) < p);
+}
+
 double or_morans_i(const or_problem* P, const int8_t* u) {
     static const int vn[4][2] = {{0, -1}, {-1, 0}, {1, 0}, {0, 1}};
     int64_t n1 = P->n1, n2 = P->n2, n = n1 * n2;

@@ -112,6 +112,12 @@ void or_state_counts(const int8_t* u, int64_t n, int64_t* counts, int32_t nvals,
  * (boundaries from P). Returns NaN for a constant field (the reference raises). */
 double or_morans_i(const or_problem* P, const int8_t* u);
 
+/* The Bernoulli(density) soup of 0/1 the backend generates on the device for a state it is
+ * not given (no counterpart in the reference): cell q (1-based column-major id) is 1 when the
+ * Float32 uniform of its draw (seed; q, 0, 0xFFFFFFFF, 0xFFFFFFFE) (random.jl:102-114) lies
+ * below Float32(density), as bernoulli(Float32) compares (random.jl:130). */
+void or_soup(uint64_t seed, int64_t n1, int64_t n2, double density, int8_t* out);
+
 /* Lenia (lenia.jl:42-47, environment.jl:151-169, kernels.jl:87-104,174-189).
  * or_lenia_weights: offsets to read (negated kernel offsets, column-major order)
  * and FP64-normalised weights; returns the tap count (room for (2R+1)^2). */

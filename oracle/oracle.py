@@ -81,6 +81,7 @@ def lib():
                                       P(ctypes.c_int64)]
         L.or_morans_i.argtypes = [P(OrProblem), ctypes.c_void_p]
         L.or_morans_i.restype = ctypes.c_double
+        L.or_soup.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p]
         L.or_step_reference_env.argtypes = [P(OrProblem), P(OrEnv), ctypes.c_void_p, ctypes.c_int64,
                                             P(ctypes.c_double)]
         L.or_run_array_env.argtypes = [P(OrProblem), P(OrEnv), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
@@ -312,6 +313,13 @@ def state_counts(u: np.ndarray, nvals: int = 3):
 def morans_i(prob: Problem, u: np.ndarray) -> float:
     a = _u8(u)
     return lib().or_morans_i(ctypes.byref(prob.c()), a.ctypes.data)
+
+
+def soup(seed: int, n1: int, n2: int, density: float) -> np.ndarray:
+    """The backend's device-generated Bernoulli(density) soup of 0/1 (an n1 x n2 Int8 state)."""
+    a = np.zeros((n1, n2), dtype=np.int8, order="F")
+    lib().or_soup(seed % (1 << 64), n1, n2, density, a.ctypes.data)
+    return a
 
 
 # ----------------------------------------------------------------- Lenia

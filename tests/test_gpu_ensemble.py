@@ -236,3 +236,62 @@ def test_large_split_tuner_and_refusals(ca):
     ens.set_large(0, 1)
     assert ens.geometry()["n_large"] == 0
     ens.close()
+
+
+def test_config_sample_of_the_bench_ensemble_against_the_oracle(ca, oracle):
+    """The bench's batched workload (4096 forest-fire instances from its own generator, all empty
+    at t = 0, 500 steps, seeds 1..4096) run whole, under the bench's tuned geometry (64-cell
+    tiles, 4 steps per pass, instances of 2^14 cells and more as batched one-step passes) and
+    under the default one; 16 instances checked against the oracle: the smallest, the largest,
+    the instances just below and at the large-instance split, and 12 at random. Final states are
+    equal, state counts equal and Moran's I equal to 1e-12 (src/measures.jl:14-20,91-107)."""
+    import ctypes
+    import os
+
+    import bench
+
+    o = oracle
+    capi, lib = ca.capi, ca.capi.lib()
+    sides, ps, fs, seeds = bench.ensemble_instances()
+    n, steps = len(sides), bench.ENS["steps"]
+    order = np.argsort(sides, kind="stable")
+    below = int(order[np.searchsorted(sides[order], 128) - 1])  # largest side under 128 (< 2^14 cells)
+    at = int(order[np.searchsorted(sides[order], 128)])          # first side of 128 or more
+    rng = np.random.default_rng(12)
+    pick = [int(order[0]), int(order[-1]), below, at] + [int(x) for x in rng.choice(n, 12, replace=False)]
+    want = {}
+    for i in pick:
+        P = o.Problem(o.RULE_FOREST_FIRE, int(sides[i]), int(sides[i]), nbhd=o.VON_NEUMANN, seed=int(seeds[i]),
+                      boundary=(o.CONSTANT, o.CONSTANT))
+        u = o.run_array(P, np.zeros((sides[i], sides[i]), np.int8), 0, steps, (ps[i], fs[i]), os.cpu_count() or 1)
+        want[i] = (u, o.state_counts(u, 3), o.morans_i(P, u))
+    descs = (capi.Desc * n)()
+    for i in range(n):
+        descs[i] = bench.fire_desc(capi, sides[i], seeds[i])
+    T0 = (ctypes.c_int64 * n)()
+    S = (ctypes.c_int64 * n)(*([steps] * n))
+    Par = (ctypes.c_double * (2 * n))(*np.column_stack([ps, fs]).ravel().tolist())
+    for geometry in ("bench", "default"):
+        e = ctypes.c_void_p()
+        capi.check(lib.gbca_ensemble_create(descs, n, ctypes.byref(e)))
+        try:
+            if geometry == "bench":
+                capi.check(lib.gbca_ensemble_set_geometry(e, 64, 4))
+                capi.check(lib.gbca_ensemble_set_large(e, 1 << 14, 1))
+            capi.check(lib.gbca_ensemble_fill(e, 0))
+            capi.check(lib.gbca_ensemble_run(e, T0, S, Par, 2))
+            capi.check(lib.gbca_ensemble_sync(e))
+            C = (ctypes.c_int64 * (3 * n))()
+            O = (ctypes.c_int64 * n)()
+            M = (ctypes.c_double * n)()
+            capi.check(lib.gbca_ensemble_summaries(e, C, 3, O, M))
+            for i in pick:
+                u, (c3, other), mi = want[i]
+                got = np.empty((sides[i], sides[i]), np.int8, order="F")
+                capi.check(lib.gbca_ensemble_get_state(e, i, got.ctypes.data, got.nbytes))
+                assert np.array_equal(got, u), f"{geometry}: instance {i} (side {sides[i]}) differs from the oracle"
+                assert [C[3 * i + k] for k in range(3)] == c3 and O[i] == other == 0, (geometry, i)
+                assert M[i] == pytest.approx(mi, rel=1e-12, abs=1e-15), (geometry, i, M[i], mi)
+        finally:
+            lib.gbca_ensemble_destroy(e)
+    assert sum(want[i][1][0][1] for i in pick) > 0  # trees grew: the comparison means something

@@ -83,3 +83,49 @@ def test_oversized_request_is_refused(ca):
         got = srv.wait([i, j])
     assert got[i]["status"] == ca.capi.ERR_OOM and got[j]["status"] == 0
     assert got[j]["counts"][0] == 64 * 64
+
+
+def test_served_mix_against_the_oracle(ca, oracle):
+    """Twelve requests of the served stream's three rules (Life B3/S23 and Generations B2/S/C3
+    from the server's device soups, the forest fire from empty, p ~ U(0.01, 0.1),
+    f ~ LogU(1e-5, 1e-3)), sides log-uniform in 64..1024 and 50..400 steps, submitted together
+    to a server with the bench's configuration: each result's state counts equal the oracle's
+    and its Moran's I agrees to 1e-12 (src/measures.jl:14-20,91-107), the oracle running the
+    same soup (seed; id, 0, 0xFFFFFFFF, 0xFFFFFFFE) through the reference's ArrayBackend sweep."""
+    import os
+
+    o = oracle
+    rng = np.random.Generator(np.random.PCG64(1212))
+    reqs, want = [], []
+    for k in range(12):
+        kind = k % 3
+        side = int(np.round(np.exp(rng.uniform(np.log(64), np.log(1024)))))
+        steps = int(rng.integers(50, 401))
+        seed, init_seed = int(rng.integers(1, 2 ** 62)), int(rng.integers(1, 2 ** 62))
+        if kind == 0:
+            rule, space, p, dens = ca.Life("B3/S23"), ca.Torus(side, side), None, 0.5
+            P = o.Problem(o.RULE_LIFE, side, side, birth=o.mask([3]), survive=o.mask([2, 3]), seed=seed)
+        elif kind == 1:
+            rule, space, p, dens = ca.Generations("B2/S/C3"), ca.Torus(side, side), None, 0.5
+            P = o.Problem(o.RULE_GENERATIONS, side, side, birth=o.mask([2]), survive=0, states=3, seed=seed)
+        else:
+            rule, space, dens = ca.ForestFire(), ca.Grid(side, side), None
+            p = {"p": float(rng.uniform(0.01, 0.1)), "f": float(np.exp(rng.uniform(np.log(1e-5), np.log(1e-3))))}
+            P = o.Problem(o.RULE_FOREST_FIRE, side, side, nbhd=o.VON_NEUMANN, seed=seed,
+                          boundary=(o.CONSTANT, o.CONSTANT))
+        prob = ca.CAProblem.new(rule, np.zeros((side, side), np.int8), steps, p, space=space, seed=seed)
+        reqs.append((prob, dens, init_seed))
+        u0 = o.soup(init_seed, side, side, dens) if dens else np.zeros((side, side), np.int8)
+        u = o.run_array(P, u0, 0, steps, (p["p"], p["f"]) if p else None, os.cpu_count() or 1)
+        want.append((o.state_counts(u, 8), o.morans_i(P, u)))
+    with ca.serving.Server(hbm_budget=8 << 30, chunk_steps=100, big_cells=1 << 16, max_big=16) as srv:
+        ids = [srv.submit(prob, density=dens, init_seed=s) for prob, dens, s in reqs]
+        got = srv.wait(ids)
+    for (prob, dens, s), i, ((counts, other), mi) in zip(reqs, ids, want):
+        r = got[i]
+        assert r["status"] == 0
+        assert r["counts"] == counts and r["other"] == other, (prob.rule, prob.space.dims)
+        if np.isnan(mi):
+            assert np.isnan(r["morans"])
+        else:
+            assert r["morans"] == pytest.approx(mi, rel=1e-12, abs=1e-15), (prob.rule, prob.space.dims)
