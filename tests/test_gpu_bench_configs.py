@@ -84,7 +84,8 @@ def test_ltl_8192_torus_full_size(env, ltl_case, geometry):
     assert used[0] >= 1, "the bit-sliced kernel must run this problem"
     bad = int((got != want).sum())
     assert bad == 0, f"{bad} of {got.size} cells differ from the oracle after 10 steps (geometry {used})"
-    assert 0.2 < want.mean() < 0.8  # the soup is still alive: the comparison means something
+    # the soup is still alive and has moved: the comparison means something
+    assert 0.01 < want.mean() < 0.9 and (want != ltl0).mean() > 0.05
 
 
 @pytest.fixture(scope="module")
