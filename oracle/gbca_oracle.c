@@ -454,13 +454,24 @@ void or_soup(uint64_t seed, int64_t n1, int64_t n2, double density, int8_t* out)
         out[q] = (int8_t)(or_uniform32(seed, (uint64_t)q + 1u, (int64_t)0xFFFFFFFFu, 0xFFFFFFFEu) < p);
 }
 
+/* Neumaier-compensated running sum: the sums of measures.jl:95-104 over millions of cells,
+ * accurate to a few ulps whatever their order (the reference's own sum is pairwise, so no
+ * order reproduces it bit for bit; an accurate sum is the fixed point both approximate). */
+typedef struct { double s, c; } or_ksum;
+static void or_ksum_add(or_ksum* k, double x) {
+    double t = k->s + x;
+    if (fabs(k->s) >= fabs(x)) k->c += (k->s - t) + x;
+    else k->c += (x - t) + k->s;
+    k->s = t;
+}
+
 double or_morans_i(const or_problem* P, const int8_t* u) {
     static const int vn[4][2] = {{0, -1}, {-1, 0}, {1, 0}, {0, 1}};
     int64_t n1 = P->n1, n2 = P->n2, n = n1 * n2;
     int64_t s = 0;
     for (int64_t k = 0; k < n; ++k) s += u[k];
     double m = (double)s / (double)n;
-    double num = 0.0;
+    or_ksum num = {0.0, 0.0};
     int64_t W = 0;
     for (int64_t j = 1; j <= n2; ++j)
         for (int64_t i = 1; i <= n1; ++i) {
@@ -470,17 +481,18 @@ double or_morans_i(const or_problem* P, const int8_t* u) {
                 int64_t a = or_map_axis(P->boundary[0], i + vn[k][0], n1, &o1);
                 int64_t b = or_map_axis(P->boundary[1], j + vn[k][1], n2, &o2);
                 if (o1 || o2) continue; /* beyond a Constant edge: not a neighbour */
-                num += xi * ((double)u[(a - 1) + (b - 1) * n1] - m);
+                or_ksum_add(&num, xi * ((double)u[(a - 1) + (b - 1) * n1] - m));
                 W += 1;
             }
         }
-    double den = 0.0;
+    or_ksum den = {0.0, 0.0};
     for (int64_t k = 0; k < n; ++k) {
         double d = (double)u[k] - m;
-        den += d * d;
+        or_ksum_add(&den, d * d);
     }
-    if (den == 0.0) return NAN;
-    return (double)n / (double)W * num / den;
+    double dsum = den.s + den.c;
+    if (dsum == 0.0) return NAN;
+    return (double)n / (double)W * (num.s + num.c) / dsum;
 }
 
 /* ------------------------------------------------------------------ Lenia */
