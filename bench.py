@@ -598,8 +598,16 @@ def run_stream(capi, lib, n, rate, seed):
         drain()
         time.sleep(0.001)
     wall = time.perf_counter() - t0
+    busy = (ctypes.c_double * 64)()
+    nl, small, clock, chunks = ctypes.c_int32(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
+    capi.check(lib.gbca_server_stats(srv, busy, 64, ctypes.byref(nl), ctypes.byref(small), ctypes.byref(clock),
+                                     ctypes.byref(chunks)))
     lib.gbca_server_stop(srv)
-    return got, (arrivals, kinds, sides, steps, ps, fs, seeds, descs), wall
+    lanes = [busy[k] / clock.value for k in range(min(nl.value, 64))]
+    occupancy = {"lanes": nl.value, "lane_busy_frac": [round(x, 3) for x in lanes],
+                 "mean_lanes_busy": sum(lanes), "small_stream_busy_frac": small.value / clock.value,
+                 "large_chunks": chunks.value}
+    return got, (arrivals, kinds, sides, steps, ps, fs, seeds, descs), wall, occupancy
 
 
 def bench_served(capi, lib):
@@ -610,7 +618,7 @@ def bench_served(capi, lib):
     (create, the same device soup, advance, summaries, destroy), on a sample, whose summaries
     must equal the served ones exactly."""
     n = int(SERVE["rate"] * SERVE["seconds"])
-    got, reqs, wall = run_stream(capi, lib, n, SERVE["rate"], 2000)
+    got, reqs, wall, occ = run_stream(capi, lib, n, SERVE["rate"], 2000)
     ids = sorted(got)  # ids are given in submission order
     arrivals, kinds, sides, steps, ps, fs, seeds, descs = reqs
     lat = np.array([v[2] - v[1] for v in got.values()])
@@ -623,7 +631,8 @@ def bench_served(capi, lib):
               "sims_per_s": n / (t_last - t_first), "gcell_updates_s": cu / (t_last - t_first) / 1e9,
               "offered_gcell_updates_s": cu / arrivals[-1] / 1e9,
               "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
-              "wall_s": wall, "config": {k: SERVE[k] for k in ("hbm_budget", "chunk_steps", "big_cells", "max_big")}}
+              "wall_s": wall, "config": {k: SERVE[k] for k in ("hbm_budget", "chunk_steps", "big_cells", "max_big")},
+              "occupancy": occ}
 
     # the plain per-request path on a random sample, one request at a time
     rng = np.random.Generator(np.random.PCG64(5))
@@ -652,13 +661,13 @@ def bench_served(capi, lib):
     # a stream at half the measured capacity, for the loop's latency when it keeps up
     rate2 = 0.5 * served["sims_per_s"]
     n2 = max(50, int(rate2 * 3.0))
-    got2, reqs2, _ = run_stream(capi, lib, n2, rate2, 2001)
+    got2, reqs2, _, occ2 = run_stream(capi, lib, n2, rate2, 2001)
     lat2 = np.array([v[2] - v[1] for v in got2.values()])
     t2a, t2b = min(v[1] for v in got2.values()), max(v[2] for v in got2.values())
     served["at_half_capacity"] = {"rate_per_s": rate2, "requests": n2,
                                   "ok": int(sum(1 for v in got2.values() if v[0] == 0)),
                                   "sims_per_s": n2 / (t2b - t2a), "latency_p50_s": float(np.percentile(lat2, 50)),
-                                  "latency_p99_s": float(np.percentile(lat2, 99))}
+                                  "latency_p99_s": float(np.percentile(lat2, 99)), "occupancy": occ2}
     served["plain_sims_per_s"] = len(sample) / t_sum
     served["plain_sample"] = len(sample)
     served["plain_service_p50_s"] = float(np.percentile(lat_plain, 50))

@@ -38,7 +38,7 @@ class Desc(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     """gbca_server_config."""
     _fields_ = [("hbm_budget", ctypes.c_uint64), ("chunk_steps", ctypes.c_int32), ("big_cells", ctypes.c_int32),
-                ("max_big", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("max_big", ctypes.c_int32), ("big_chunk_us", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):
@@ -105,6 +105,8 @@ SIGNATURES = {
                                           _I64, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_uint64)]),
     "gbca_server_poll": (ctypes.c_int, [_V, _P(Result), ctypes.c_int32, _P(ctypes.c_int32)]),
     "gbca_server_status": (ctypes.c_int, [_V, _P(_I64), _P(_I64), _P(ctypes.c_double)]),
+    "gbca_server_stats": (ctypes.c_int, [_V, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_int32),
+                                         _P(ctypes.c_double), _P(ctypes.c_double), _P(_I64)]),
     "gbca_server_stop": (ctypes.c_int, [_V]),
     "gbca_advance_noalloc": (ctypes.c_int, [_P(Desc), _V, _I64, _I64, _I64, _P(ctypes.c_double), ctypes.c_int32, _V]),
 }

@@ -7,14 +7,19 @@
 //  * Admission by HBM budget: request states live in one device arena of a fixed size; a
 //    request is admitted, in arrival order, when its two buffers fit, and its memory is
 //    released the moment it finishes. A request larger than the whole arena is refused.
-//  * Continuous batching, event driven: large requests each take one of `max_big` stream
-//    lanes and run there from their initial state to their summaries (temporally blocked
-//    multi-CTA sweeps); small requests run together, `chunk_steps` steps at a time, in
-//    persistent ensemble launches (ensemble.cu; one CTA per request) on their own stream,
-//    back to back. Every launch ends with an event and a host callback that wakes the
-//    scheduler, which then collects what finished, frees its memory, admits waiting
-//    requests and refills the idle lane or the small stream at once: no lane waits for
-//    another, and no iteration-wide barrier holds the device.
+//  * Continuous batching, event driven: large requests run on `max_big` stream lanes in chunks
+//    of about big_chunk_us (default kChunkSeconds) of estimated GPU time (temporally blocked multi-CTA sweeps; the
+//    last chunk ends with the request's summaries); small requests run together,
+//    `chunk_steps` steps at a time, in persistent ensemble launches (ensemble.cu; one CTA per
+//    request) on their own stream, back to back. Every launch ends with an event and a host
+//    callback that wakes the scheduler, which then collects what finished, frees its memory,
+//    admits waiting requests and refills the idle lane or the small stream at once: no lane
+//    waits for another, and no iteration-wide barrier holds the device.
+//  * Large requests are picked shortest estimated remaining time first, aged by their time in
+//    the system (so none starves), and lanes are filled only while the chunks in flight
+//    occupy at most kFillCap GPUs' worth of tiles: a long forest fire no longer holds a lane
+//    from start to end while short requests queue behind it, and a dozen lattices that each
+//    fill the GPU no longer share it sixteen ways.
 //  * A request's initial state is uploaded or generated on the stream that then runs it, so
 //    its first step is ordered after its state.
 //  * Results are exact: a request's steps, draws and summaries are those it would get alone
@@ -106,6 +111,11 @@ struct Request {
     double t_submit = 0.0, t_admit = 0.0;
 };
 
+// Chunks of large requests: about this much estimated GPU time each unless the configuration
+// says otherwise, and chunks in flight holding at most this many GPUs' worth of tiles.
+constexpr double kChunkSeconds = 4e-3;
+constexpr double kFillCap = 2.0;
+
 int sfail(int code, const char* fmt, ...) {
     char msg[512];
     va_list ap;
@@ -154,6 +164,10 @@ struct gbca_server {
     std::vector<cudaEvent_t> ev_big;  // end of each lane's request
     cudaEvent_t ev_small = nullptr;    // end of the small requests' launch in flight
     std::atomic<uint64_t> signals{0};  // completions reported by host callbacks
+    // occupancy (under mu): seconds each lane and the small stream had work in flight, chunks run
+    std::vector<double> lane_busy;
+    double small_busy = 0.0;
+    int64_t chunks = 0;
 
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
@@ -232,6 +246,30 @@ EnsInstance small_instance(const Request* r, int64_t steps, bool last) {
     return I;
 }
 
+// Estimated sweep rate of a large request (cell-updates per second on one GB300): the forest
+// fire is bound by its Philox draws, the bit-sliced Life and Generations kernels by their
+// counting (by r), the general kernel by its per-cell loads.
+double est_rate(const gbca_desc& d) {
+    if (d.rule == GBCA_RULE_FOREST_FIRE) return d.nbhd == GBCA_VON_NEUMANN && d.radius == 1 ? 3.5e11 : 5e10;
+    if (d.rule == GBCA_RULE_LIFE && d.nbhd == GBCA_MOORE && d.radius <= 7) return 4e12 / d.radius;
+    if (d.rule == GBCA_RULE_GENERATIONS && d.nbhd == GBCA_MOORE && d.radius <= 2 && d.states <= 4)
+        return 2e12 / d.radius;
+    return 1e11 / (d.radius * d.radius);
+}
+
+// The share of the GPU one sweep of the request occupies (its tiles over the resident CTA
+// slots), at most 1: a forest-fire tile is 256 x ~158 cells, two per SM; a bit-sliced tile up
+// to 1024 x 216 cells.
+double est_fill(const gbca_desc& d) {
+    const double cells = (double)d.n1 * (double)d.n2;
+    const double full = d.rule == GBCA_RULE_FOREST_FIRE ? 1.2e7 : 6e7;
+    return cells >= full ? 1.0 : cells / full;
+}
+
+double est_remaining_s(const Request* r) {
+    return (double)r->d.n1 * (double)r->d.n2 * (double)(r->nsteps - r->done) / est_rate(r->d);
+}
+
 // Admit pending requests in arrival order while the arena has room; the state is initialised
 // later, on the stream that runs the request.
 void admit(gbca_server* S, std::deque<Request*>& pending, std::vector<Request*>& admitted,
@@ -286,12 +324,17 @@ void CUDART_CB on_done(void* p) {
 void scheduler(gbca_server* S) {
     cudaSetDevice(S->device);
     std::deque<Request*> pending;
-    std::vector<Request*> waiting_big;  // admitted large requests without a lane
+    std::vector<Request*> waiting_big;  // admitted large requests between chunks (or not started)
     std::vector<Request*> smalls;       // admitted small requests
     std::vector<Request*> batch;        // the small requests of the launch in flight
     std::vector<int64_t> batch_steps;
     const int nlanes = (int)S->s_big.size();
     std::vector<Request*> lane((size_t)nlanes, nullptr);
+    std::vector<int64_t> lane_steps((size_t)nlanes, 0);
+    std::vector<double> lane_start((size_t)nlanes, 0.0), lane_fill((size_t)nlanes, 0.0);
+    std::vector<double> busy_add((size_t)nlanes, 0.0);
+    double small_start = 0.0, small_add = 0.0;
+    int64_t chunks_add = 0;
     bool small_busy = false;
     std::vector<gbca_result> done;
     uint64_t seen = 0;
@@ -312,7 +355,7 @@ void scheduler(gbca_server* S) {
         bool progress = false;
         const double t = S->now();
         std::vector<Request*> finished;
-        // 1. lanes whose request is done
+        // 1. lanes whose chunk is done: the request goes back to the queue, or its summaries out
         for (int j = 0; j < nlanes && e == cudaSuccess; ++j) {
             Request* r = lane[(size_t)j];
             if (!r) continue;
@@ -322,20 +365,28 @@ void scheduler(gbca_server* S) {
                 e = q;
                 break;
             }
+            lane[(size_t)j] = nullptr;
+            busy_add[(size_t)j] += t - lane_start[(size_t)j];
+            progress = true;
+            r->done += lane_steps[(size_t)j];
+            r->valid = true;  // the rule's own states from here on
+            if (r->done < r->nsteps) {
+                waiting_big.push_back(r);
+                continue;
+            }
             // a tile copy that gave up its wait left a tile unwritten: the result is not valid
             gbca_result res = make_result(r, fire_tma_timeouts_take() ? GBCA_ERR_TIMEOUT : GBCA_OK, t);
             finish_measures(S->h_acc + (size_t)j * kMeasureWords, r->d.n1 * r->d.n2, res.counts, kEnsCounts,
                             &res.other, &res.morans);
             done.push_back(res);
             finished.push_back(r);
-            lane[(size_t)j] = nullptr;
-            progress = true;
         }
         // 2. the small requests' launch
         if (e == cudaSuccess && small_busy) {
             const cudaError_t q = cudaEventQuery(S->ev_small);
             if (q == cudaSuccess) {
                 small_busy = false;
+                small_add += t - small_start;
                 progress = true;
                 for (size_t j = 0; j < batch.size(); ++j) {
                     Request* r = batch[j];
@@ -373,26 +424,48 @@ void scheduler(gbca_server* S) {
             for (Request* r : admitted) (r->big ? waiting_big : smalls).push_back(r);
             progress = progress || !admitted.empty();
         }
-        // 4. idle lanes take the next large request, from its initial state to its summaries
+        // 4. idle lanes take the next chunk of the large request with the shortest estimated
+        //    remaining time (aged by its time in the system), while the chunks in flight fill at
+        //    most kFillCap GPUs
         for (int j = 0; j < nlanes && e == cudaSuccess && !waiting_big.empty(); ++j) {
             if (lane[(size_t)j]) continue;
-            Request* r = waiting_big.front();
-            waiting_big.erase(waiting_big.begin());
+            double fill = 0.0;
+            for (int k = 0; k < nlanes; ++k)
+                if (lane[(size_t)k]) fill += lane_fill[(size_t)k];
+            const double now = S->now();
+            auto key = [&](const Request* r) { return est_remaining_s(r) - (now - r->t_admit); };
+            auto best = std::min_element(waiting_big.begin(), waiting_big.end(),
+                                         [&](const Request* a, const Request* b) { return key(a) < key(b); });
+            Request* r = *best;
+            if (fill > 0.0 && fill + est_fill(r->d) > kFillCap) break;
+            waiting_big.erase(best);
+            const double cells = (double)r->d.n1 * (double)r->d.n2;
+            const int64_t rem = r->nsteps - r->done;
+            const double chunk_s = S->cfg.big_chunk_us > 0 ? S->cfg.big_chunk_us * 1e-6 : kChunkSeconds;
+            int64_t steps = (int64_t)(est_rate(r->d) * chunk_s / cells);
+            if (steps < S->cfg.chunk_steps) steps = S->cfg.chunk_steps;
+            if (steps > rem) steps = rem;
             cudaStream_t st = S->s_big[(size_t)j];
-            e = init_state(S, r, st);
+            if (r->fresh) e = init_state(S, r, st);
             int8_t* const bufs[2] = {S->arena_base + r->off, S->arena_base + r->off + r->bytes / 2};
             if (e == cudaSuccess)
-                e = sweep_int8(r->d, r->pitch, bufs, &r->cur, r->t0, r->nsteps, r->params, st, r->valid);
-            unsigned long long* acc = S->d_acc + (size_t)j * kMeasureWords;
-            if (e == cudaSuccess)
-                e = launch_measures(bufs[r->cur], r->d.n1, r->d.n2, r->pitch, r->d.boundary[0], r->d.boundary[1], acc,
-                                    S->grid / 4 > 0 ? S->grid / 4 : 1, st);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(S->h_acc + (size_t)j * kMeasureWords, acc, kMeasureWords * sizeof(unsigned long long),
-                                    cudaMemcpyDeviceToHost, st);
+                e = sweep_int8(r->d, r->pitch, bufs, &r->cur, r->t0 + r->done, steps, r->params, st, r->valid);
+            if (steps == rem) {  // the last chunk: the request's summaries
+                unsigned long long* acc = S->d_acc + (size_t)j * kMeasureWords;
+                if (e == cudaSuccess)
+                    e = launch_measures(bufs[r->cur], r->d.n1, r->d.n2, r->pitch, r->d.boundary[0], r->d.boundary[1],
+                                        acc, S->grid / 4 > 0 ? S->grid / 4 : 1, st);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(S->h_acc + (size_t)j * kMeasureWords, acc,
+                                        kMeasureWords * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+            }
             if (e == cudaSuccess) e = cudaEventRecord(S->ev_big[(size_t)j], st);
             if (e == cudaSuccess) e = cudaLaunchHostFunc(st, on_done, S);
             lane[(size_t)j] = r;
+            lane_steps[(size_t)j] = steps;
+            lane_start[(size_t)j] = now;
+            lane_fill[(size_t)j] = est_fill(r->d);
+            ++chunks_add;
             progress = true;
         }
         // 5. the small requests, chunk_steps at a time, in one persistent launch
@@ -430,6 +503,7 @@ void scheduler(gbca_server* S) {
             if (e == cudaSuccess) e = cudaEventRecord(S->ev_small, S->s_small);
             if (e == cudaSuccess) e = cudaLaunchHostFunc(S->s_small, on_done, S);
             small_busy = e == cudaSuccess;
+            small_start = S->now();
             progress = true;
         }
         if (e != cudaSuccess) {
@@ -461,6 +535,14 @@ void scheduler(gbca_server* S) {
             std::unique_lock<std::mutex> lock(S->mu);
             for (auto& res : done) S->outbox.push_back(res);
             done.clear();
+            for (int j = 0; j < nlanes; ++j) {
+                S->lane_busy[(size_t)j] += busy_add[(size_t)j];
+                busy_add[(size_t)j] = 0.0;
+            }
+            S->small_busy += small_add;
+            small_add = 0.0;
+            S->chunks += chunks_add;
+            chunks_add = 0;
             S->queued = (int64_t)(pending.size() + S->inbox.size());
             S->active_n = (int64_t)(waiting_big.size() + smalls.size() +
                                     std::count_if(lane.begin(), lane.end(), [](Request* r) { return r; }));
@@ -482,7 +564,7 @@ int gbca_server_start(const gbca_server_config* cfg, gbca_server** out) {
     if (!cfg || !out) return sfail(GBCA_ERR_ARGUMENT, "null configuration or output");
     *out = nullptr;
     if (cfg->hbm_budget < 4096 || cfg->chunk_steps < 1 || cfg->max_big < 1 || cfg->max_big > 64 ||
-        cfg->big_cells < 0)
+        cfg->big_cells < 0 || cfg->big_chunk_us < 0)
         return sfail(GBCA_ERR_ARGUMENT, "server configuration out of range");
     if (gbca_device_count() < 1) return sfail(GBCA_ERR_CUDA, "no CUDA device is visible");
     gbca_server* S = new gbca_server();
@@ -520,6 +602,7 @@ int gbca_server_start(const gbca_server_config* cfg, gbca_server** out) {
                    : sfail(GBCA_ERR_CUDA, "server start: %s", cudaGetErrorString(e));
     }
     S->arena.reset((size_t)cfg->hbm_budget);
+    S->lane_busy.assign((size_t)cfg->max_big, 0.0);
     S->grid = ensemble_grid();
     S->th = std::thread(scheduler, S);
     *out = S;
@@ -596,6 +679,19 @@ int gbca_server_status(gbca_server* S, int64_t* queued, int64_t* active, double*
     if (active) *active = S->active_n;
     if (clock) *clock = S->now();
     return S->dead ? sfail(GBCA_ERR_CUDA, "the server stopped after a device failure") : GBCA_OK;
+}
+
+int gbca_server_stats(gbca_server* S, double* lane_busy_s, int32_t max_lanes, int32_t* nlanes, double* small_busy_s,
+                      double* wall_s, int64_t* chunks) {
+    if (!S || (max_lanes > 0 && !lane_busy_s)) return sfail(GBCA_ERR_ARGUMENT, "null server or output");
+    std::lock_guard<std::mutex> lock(S->mu);
+    const int32_t n = (int32_t)S->lane_busy.size();
+    for (int32_t j = 0; j < n && j < max_lanes; ++j) lane_busy_s[j] = S->lane_busy[(size_t)j];
+    if (nlanes) *nlanes = n;
+    if (small_busy_s) *small_busy_s = S->small_busy;
+    if (wall_s) *wall_s = S->now();
+    if (chunks) *chunks = S->chunks;
+    return GBCA_OK;
 }
 
 int gbca_server_stop(gbca_server* S) {

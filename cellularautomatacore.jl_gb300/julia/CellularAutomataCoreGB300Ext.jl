@@ -95,7 +95,7 @@ struct GbcaServerConfig
     chunk_steps::Int32
     big_cells::Int32
     max_big::Int32
-    reserved::Int32
+    big_chunk_us::Int32
 end
 
 # gbca_result
@@ -519,7 +519,7 @@ end
 # ------------------------------------------------------------------ serving
 
 """
-    GB300Server(; hbm_budget=8 << 30, chunk_steps=64, big_cells=1 << 20, max_big=8)
+    GB300Server(; hbm_budget=8 << 30, chunk_steps=64, big_cells=1 << 20, max_big=8, big_chunk_us=0)
 
 The continuous-batching request loop of libgbca.so: `submit(srv, prob)` queues a simulation
 (Int8 rules, Synchronous) and returns its id at once; `poll(srv)` returns finished requests'
@@ -529,8 +529,8 @@ mutable struct GB300Server
     ptr::Ptr{Cvoid}
 end
 function GB300Server(; hbm_budget::Integer=8 << 30, chunk_steps::Integer=64, big_cells::Integer=1 << 20,
-                     max_big::Integer=8)
-    cfg = GbcaServerConfig(hbm_budget, chunk_steps, big_cells, max_big, 0)
+                     max_big::Integer=8, big_chunk_us::Integer=0)
+    cfg = GbcaServerConfig(hbm_budget, chunk_steps, big_cells, max_big, big_chunk_us)
     p = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:gbca_server_start, libgbca), Cint, (Ref{GbcaServerConfig}, Ref{Ptr{Cvoid}}), cfg, p))
     srv = GB300Server(p[])
@@ -570,6 +570,16 @@ function status(srv::GB300Server)
     check(ccall((:gbca_server_status, libgbca), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ref{Float64}),
                 srv.ptr, q, a, c))
     return (queued=q[], active=a[], clock=c[])
+end
+
+# seconds each large-request lane and the small stream had work in flight, clock, chunks run
+function stats(srv::GB300Server)
+    busy = zeros(Float64, 64)
+    n, small, wall, chunks = Ref{Int32}(0), Ref{Float64}(0.0), Ref{Float64}(0.0), Ref{Int64}(0)
+    check(ccall((:gbca_server_stats, libgbca), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Int32, Ref{Int32}, Ref{Float64}, Ref{Float64}, Ref{Int64}),
+                srv.ptr, busy, 64, n, small, wall, chunks))
+    return (lane_busy_s=busy[1:min(n[], 64)], small_busy_s=small[], wall_s=wall[], chunks=chunks[])
 end
 
 function stop!(srv::GB300Server)

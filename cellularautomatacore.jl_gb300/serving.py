@@ -17,10 +17,12 @@ from .model import ForestFire, Synchronous
 class Server:
     """A running request loop on the current GPU."""
 
-    def __init__(self, hbm_budget: int = 8 << 30, chunk_steps: int = 64, big_cells: int = 1 << 20, max_big: int = 8):
+    def __init__(self, hbm_budget: int = 8 << 30, chunk_steps: int = 64, big_cells: int = 1 << 20, max_big: int = 8,
+                 big_chunk_us: int = 0):
         cfg = capi.ServerConfig()
         cfg.hbm_budget, cfg.chunk_steps, cfg.big_cells, cfg.max_big = int(hbm_budget), int(chunk_steps), \
             int(big_cells), int(max_big)
+        cfg.big_chunk_us = int(big_chunk_us)
         self.handle = ctypes.c_void_p()
         capi.check(capi.lib().gbca_server_start(ctypes.byref(cfg), ctypes.byref(self.handle)))
 
@@ -60,6 +62,16 @@ class Server:
         q, a, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
         capi.check(capi.lib().gbca_server_status(self.handle, ctypes.byref(q), ctypes.byref(a), ctypes.byref(c)))
         return int(q.value), int(a.value), float(c.value)
+
+    def stats(self):
+        """Occupancy so far: seconds each large-request lane and the small requests' stream had
+        work in flight, the server's clock, and the number of large-request chunks run."""
+        busy = (ctypes.c_double * 64)()
+        n, small, wall, chunks = ctypes.c_int32(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
+        capi.check(capi.lib().gbca_server_stats(self.handle, busy, 64, ctypes.byref(n), ctypes.byref(small),
+                                                ctypes.byref(wall), ctypes.byref(chunks)))
+        return {"lane_busy_s": [float(busy[k]) for k in range(min(n.value, 64))], "small_busy_s": float(small.value),
+                "wall_s": float(wall.value), "chunks": int(chunks.value)}
 
     def wait(self, ids, timeout: float = 600.0):
         """Poll until every id in `ids` has a result; returns {id: result}."""

@@ -310,11 +310,14 @@ int gbca_ensemble_tune(gbca_ensemble* e, int64_t probe_steps, const double* para
 
 /* ---- serving: a device-resident request loop with continuous batching. Clients submit
  * simulation requests at any time; a scheduler thread admits them in arrival order while
- * their state buffers fit the HBM budget, advances every admitted request by up to
- * chunk_steps steps per iteration (small requests together in one persistent launch, large
- * ones as multi-CTA sweeps on their own streams), and returns each request's state counts and
- * Moran's I as soon as it finishes. A request's result does not depend on what else runs.
- * No counterpart in the reference (its unit of work is one solve at a time). */
+ * their state buffers fit the HBM budget and returns each request's state counts and Moran's
+ * I as soon as it finishes. Small requests advance together, chunk_steps steps per persistent
+ * launch; large ones (above big_cells cells) run as multi-CTA sweeps on up to max_big stream
+ * lanes, in chunks of big_chunk_us of estimated GPU time (at least chunk_steps steps),
+ * the request with the shortest estimated remaining time (less its time in the system) first,
+ * while the chunks in flight fill at most two GPUs' worth of tiles. A request's result does
+ * not depend on what else runs. No counterpart in the reference (its unit of work is one
+ * solve at a time). */
 typedef struct gbca_server gbca_server;
 
 typedef struct gbca_server_config {
@@ -322,7 +325,8 @@ typedef struct gbca_server_config {
     int32_t chunk_steps;   /* steps per request per iteration */
     int32_t big_cells;     /* requests above this many cells run as their own multi-CTA sweeps */
     int32_t max_big;       /* large requests advanced concurrently (one stream each), 1..64 */
-    int32_t reserved;
+    int32_t big_chunk_us;  /* a large request's chunk, in microseconds of estimated GPU time (at least
+                              chunk_steps steps); 0 = 4000 */
 } gbca_server_config;
 
 typedef struct gbca_result {
@@ -350,6 +354,14 @@ int gbca_server_poll(gbca_server* s, gbca_result* out, int32_t max, int32_t* n);
 
 /* Requests waiting for admission, requests admitted, and the server's clock (seconds). */
 int gbca_server_status(gbca_server* s, int64_t* queued, int64_t* active, double* clock);
+
+/* Occupancy so far: the seconds each large-request lane had a chunk in flight
+ * (lane_busy_s[0 .. min(max_lanes, lanes) - 1]; *nlanes gets the number of lanes), the seconds
+ * the small requests' stream had a launch in flight, the server's clock, and the number of
+ * large-request chunks run. Any output but lane_busy_s may be NULL. No counterpart in the
+ * reference. */
+int gbca_server_stats(gbca_server* s, double* lane_busy_s, int32_t max_lanes, int32_t* nlanes, double* small_busy_s,
+                      double* wall_s, int64_t* chunks);
 
 /* Stop accepting requests, finish every queued and admitted one, free everything.
  * Results not yet polled are lost. */

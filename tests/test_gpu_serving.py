@@ -48,15 +48,21 @@ def key(r):
 
 def test_same_alone_and_in_the_mix(ca):
     reqs = mixed_requests(ca)
-    # the mix: a small budget (forces admission waits), small chunks, a low large-request threshold
-    with ca.serving.Server(hbm_budget=6 << 20, chunk_steps=16, big_cells=40000, max_big=3) as srv:
+    # the mix: a small budget (forces admission waits), small chunks (large requests too: a 1 us
+    # chunk target leaves chunk_steps steps per chunk, so they interleave and resume), a low
+    # large-request threshold
+    with ca.serving.Server(hbm_budget=6 << 20, chunk_steps=16, big_cells=40000, max_big=3, big_chunk_us=1) as srv:
         ids = []
         for k, (prob, dens, s) in enumerate(reqs):
             ids.append(srv.submit(prob, density=dens, init_seed=s))
             if k % 7 == 3:
                 time.sleep(0.003)  # staggered arrivals join running iterations
         mix = srv.wait(ids)
+        occ = srv.stats()
     assert all(mix[i]["status"] == 0 for i in ids)
+    big = [p for p, _, _ in reqs if p.space.dims[0] * p.space.dims[1] > 40000]
+    assert occ["chunks"] > len(big) > 0  # large requests ran in several chunks each
+    assert len(occ["lane_busy_s"]) == 3 and all(0.0 <= b <= occ["wall_s"] for b in occ["lane_busy_s"])
     # each request alone in its own server
     for (prob, dens, s), i in zip(reqs, ids):
         with ca.serving.Server(hbm_budget=8 << 20, chunk_steps=1000, big_cells=40000, max_big=1) as one:
