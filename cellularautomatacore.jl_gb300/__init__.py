@@ -6,7 +6,8 @@ model types (spaces, neighbourhoods, rules, schemes), the backend contract
 (GB300Backend and its functions) and the SciML-style problem / solve layer."""
 from . import backend, capi, ensemble, errors, model, problem, serving
 from .backend import (GB300Backend, GB300State, advance, allocate_state, check_problem, current_state,
-                      device_summaries, read_cell, set_geometry, set_state, supports, tune, write_cell)
+                      device_summaries, read_cell, set_geometry, set_state, supports, tune, update_cell,
+                      write_cell)
 from .errors import (ArgumentError, GPUError, IncompatibleSpaceError, InvalidStateError, RuleParseError,
                      StateShapeError, UnsupportedCombinationError)
 from .model import (GENERATIONS_PRESETS, LIFE_PRESETS, AnisotropicKernel, Checkerboard, Constant, EmpiricalKernel,

@@ -17,6 +17,7 @@ rules (draws keyed as src/random.jl:102-107)."""
 from __future__ import annotations
 
 import ctypes
+import hashlib
 
 import numpy as np
 
@@ -254,6 +255,53 @@ def write_cell(backend, st: GB300State, I, v) -> None:
     i, j = I
     val = np.array([v], dtype=st.dtype)
     capi.check(capi.lib().gbca_write_cell(st.handle, int(i), int(j), val.ctypes.data))
+
+
+# the last lattice update_cell stepped: (problem, time, parameters, digest of the state) and
+# the stepped state, so a loop over every cell of one state costs one sweep
+_UPDATE_CELL_CACHE: dict = {}
+
+
+def update_cell(prob, u, I, t: int, p=None):
+    """The new state of cell I when the whole state u (in the layout of prob.u0) is updated
+    synchronously at time t with parameters p (default prob.p), without changing u: the rule
+    applied to the cell and its neighbours under the space's boundaries, with the problem's
+    mask and the draws every backend makes (src/backends.jl:281-307). I is a 1-based (i, j)
+    or a 1-based column-major linear index.
+
+    Computed on the GPU: u goes through one Synchronous sweep of this backend's kernels and
+    cell I is read back. The stepped lattice is kept for the next call with the same problem,
+    time, parameters and state, so asking for every cell costs one sweep. As in the
+    reference, problems with kernel fields (the SI rule, Lenia) are refused."""
+    if prob.fields or isinstance(prob.rule, (KernelSI, Lenia)):
+        raise ArgumentError("update_cell does not compute kernel fields; use GB300Backend's sweep")
+    a = np.asarray(u)
+    n1, n2 = prob.space.dims
+    if a.shape != (n1, n2):
+        raise StateShapeError(f"the state has size {a.shape}, the space {(n1, n2)}")
+    if isinstance(I, (int, np.integer)):
+        if not 1 <= int(I) <= n1 * n2:
+            raise ArgumentError(f"cell index {I} is outside 1:{n1 * n2}")
+        i, j = (int(I) - 1) % n1 + 1, (int(I) - 1) // n1 + 1
+    else:
+        i, j = (int(x) for x in I)
+        if not (1 <= i <= n1 and 1 <= j <= n2):
+            raise ArgumentError(f"cell index ({i}, {j}) is outside the {n1} x {n2} lattice")
+    params = prob.p if p is None else p
+    a8 = np.asfortranarray(a.astype(np.int8, copy=False))
+    key = (id(prob), int(t), _params_tuple(prob.rule, params), hashlib.blake2b(a8.tobytes(order="F")).hexdigest())
+    hit = _UPDATE_CELL_CACHE.get("key")
+    if hit != key:
+        st = allocate_state(GB300Backend(), prob, Synchronous())
+        try:
+            set_state(None, st, a8)
+            advance(None, st, prob, Synchronous(), params, int(t))
+            stepped = current_state(None, st)
+        finally:
+            st.close()
+        _UPDATE_CELL_CACHE.clear()
+        _UPDATE_CELL_CACHE.update(key=key, state=stepped, prob=prob)  # prob kept alive: its id stays unique
+    return _UPDATE_CELL_CACHE["state"][i - 1, j - 1]
 
 
 def snapshot(st: GB300State) -> int:
