@@ -14,6 +14,7 @@ struct LifeTables {
     int32_t n[2];                                // interval counts: [0] dead cells, [1] live cells
     uint32_t m[2][kMaxIntervals][2][8];          // [kind][interval][lo, hi+1][bit] majority masks
     uint32_t c3, c4;                             // Generations: ~0 when C > 2, when C == 4
+    uint32_t cb[3];                              // Generations, three planes: C's bits as masks
 };
 
 struct LifeGeom {
@@ -25,14 +26,19 @@ struct LifeGeom {
 
 // A sub-step's gate (mode 0: every cell updates, 1: Checkerboard parity `gate`, 2: the
 size_t life_smem_bytes(const SweepParams& p, const LifeGeom& g);
+// Bit planes per cell: 1 for Life, 2 for Generations with C <= 4, 3 up to C = 8.
+inline int life_planes(const SweepParams& p) {
+    return p.rule != GBCA_RULE_GENERATIONS ? 1 : (p.states <= 4 ? 2 : 3);
+}
 
 // The bit-sliced kernel for Moore(R) (Life-like, and Generations for R <= 2), one per
 // translation unit sweep_life_rR.cu; ntiles > 0 runs the listed tiles of p.tile_list.
 template <int R>
 cudaError_t launch_life_radius(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
                                int8_t* dst, cudaStream_t st, int ntiles);
-// The same for von Neumann(1) (sweep_life_vn1.cu).
-cudaError_t launch_life_vn1(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
-                            int8_t* dst, cudaStream_t st, int ntiles);
+// The same for von Neumann(R), R = 1..3 (sweep_life_vnR.cu).
+template <int R>
+cudaError_t launch_life_vn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
+                           int8_t* dst, cudaStream_t st, int ntiles);
 
 }  // namespace gbca

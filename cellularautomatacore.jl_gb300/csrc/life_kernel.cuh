@@ -1,7 +1,7 @@
 // life_kernel.cuh — the bit-sliced sweep kernel: Life-like and Larger-than-Life rules
-// (src/rules.jl:354-389) on Moore(r), r = 1..7, and von Neumann(1), and Generations rules
-// with up to 4 states on Moore(1..2) and von Neumann(1), Synchronous, Stochastic(p) or Checkerboard and masks (r <= 2), as a
-// bit-sliced, temporally blocked sweep.
+// (src/rules.jl:354-389) on Moore(r), r = 1..7, and von Neumann(r), r = 1..3, and Generations
+// rules with up to 8 states on Moore(1..2) and von Neumann(1..3), Synchronous, Stochastic(p) or
+// Checkerboard and masks (r <= 5), as a bit-sliced, temporally blocked sweep.
 //
 // Layout. Global memory keeps the user's Int8 column-major state. A CTA stages its tile
 // plus a halo of K*r cells in shared memory as ONE BIT PER CELL: bit b of word w of a
@@ -16,7 +16,8 @@
 // (2-4 bit planes); a register ring keeps the last 2r+1 Hx rows and a bit-sliced running
 // sum V = sum of Hx over rows y-r..y+r is updated by one add and one subtract per row.
 // V is the Moore box count including the centre. Von Neumann(1) needs no ring: a row's count
-// is its 3-cell horizontal count plus the words above and below.
+// is its 3-cell horizontal count plus the words above and below; von Neumann(2) and (3) add
+// the diamond's 13 or 25 shifted words with the same adder trees.
 //
 // Rule. A dead cell is born when V lies in one of the birth intervals, a live cell
 // survives when V - 1 lies in a survive interval, i.e. V in the interval shifted by one.
@@ -24,11 +25,13 @@
 // L is a chain of majority gates, g = maj(v_i, g, m_i) with m_i = 0 where bit i of L is 1
 // and ~0 where it is 0 — one LOP3 per bit with m_i read from the parameter bank.
 //
-// Generations (src/rules.jl:446-456) with C <= 4 states runs in the same kernel with two
-// bit planes per cell (state = lo + 2 hi): the count reads the alive plane lo & ~hi, and the
-// next state is 1 for a born dead cell or a surviving live one, 2 for a live cell that does
-// not survive (C > 2), 3 for a state-2 cell when C = 4, else 0. The host guarantees that
-// every state lies in 0..C-1 (it scans the state on the device after the user writes it).
+// Generations (src/rules.jl:446-456) with C <= 8 states runs in the same kernel with two bit
+// planes per cell for C <= 4 (state = lo + 2 hi) and three for C <= 8 (b0 + 2 b1 + 4 b2): the
+// count reads the alive plane (state 1), and the next state is 1 for a born dead cell or a
+// surviving live one, 2 for a live cell that does not survive (C > 2), s + 1 for a dying cell
+// s >= 2 unless s + 1 == C, which goes to 0 (a three-bit increment compared with C's bits).
+// The host guarantees that every state lies in 0..C-1 (it scans the state on the device
+// after the user writes it).
 //
 // Temporal blocking: K sub-steps per HBM pass; the computed region shrinks by r per
 // sub-step. Periodic and reflecting halos are images of lattice cells and evolve like
@@ -257,13 +260,16 @@ __device__ __forceinline__ void hrow_words(uint32_t l, uint32_t c, uint32_t r, u
 }
 
 // Hx of one row: p points at the thread's word of plane 0 (guards make p[-1] and p[1]
-// valid); with two planes the counted cells are the alive ones, lo & ~hi.
+// valid); with two or three planes the counted cells are the alive ones (state 1).
 template <int R, int PL>
 __device__ __forceinline__ void hrow(const uint32_t* p, int ps, uint32_t* h) {
     if constexpr (PL == 1) {
         hrow_words<R>(p[-1], p[0], p[1], h);
-    } else {
+    } else if constexpr (PL == 2) {
         hrow_words<R>(p[-1] & ~p[ps - 1], p[0] & ~p[ps], p[1] & ~p[ps + 1], h);
+    } else {  // state 1: lo set, both higher planes clear
+        hrow_words<R>(p[-1] & ~(p[ps - 1] | p[2 * ps - 1]), p[0] & ~(p[ps] | p[2 * ps]),
+                      p[1] & ~(p[ps + 1] | p[2 * ps + 1]), h);
     }
 }
 
@@ -344,24 +350,80 @@ __device__ __forceinline__ void life_emit(const uint32_t* v, const uint32_t* ca,
     if constexpr (PL == 1) {
         const uint32_t c = ca[y * sw];
         cb[y * sw] = (((c & live) | (~c & dead)) & G) | (c & ~G);
-    } else {  // Generations, state = lo + 2 hi
+    } else if constexpr (PL == 2) {  // Generations, state = lo + 2 hi
         const uint32_t lo = ca[y * sw], hi = ca[y * sw + ps];
         const uint32_t is0 = ~lo & ~hi, is1 = lo & ~hi, is2 = ~lo & hi;
         cb[y * sw] = (((is0 & dead) | (is1 & live) | (is2 & tb.c4)) & G) | (lo & ~G);
         cb[y * sw + ps] = (((is1 & ~live & tb.c3) | (is2 & tb.c4)) & G) | (hi & ~G);
+    } else {  // Generations, state = b0 + 2 b1 + 4 b2 (C <= 8)
+        const uint32_t b0 = ca[y * sw], b1 = ca[y * sw + ps], b2 = ca[y * sw + 2 * ps];
+        const uint32_t hi = b1 | b2, is0 = ~b0 & ~hi, is1 = b0 & ~hi;
+        // a dying cell (s >= 2) moves to s + 1, or to 0 when s + 1 == C (three-bit increment, and
+        // C's bits as masks: n == C when no bit differs)
+        const uint32_t n0 = ~b0, n1 = b1 ^ b0, n2 = b2 ^ (b1 & b0);
+        const uint32_t wrap = ~((n0 ^ tb.cb[0]) | (n1 ^ tb.cb[1]) | (n2 ^ tb.cb[2]));
+        const uint32_t dying = hi & ~wrap;
+        cb[y * sw] = (((is0 & dead) | (is1 & live) | (dying & n0)) & G) | (b0 & ~G);
+        cb[y * sw + ps] = (((is1 & ~live & tb.c3) | (dying & n1)) & G) | (b1 & ~G);
+        cb[y * sw + 2 * ps] = ((dying & n2) & G) | (b2 & ~G);
     }
 }
 
-// The alive bits of a word (Life: the indicator; Generations: state 1, lo & ~hi).
+// The alive bits of a word (Life: the indicator; Generations: state 1, lo & ~hi [& ~top]).
 template <int PL>
 __device__ __forceinline__ uint32_t alive_word(const uint32_t* q, int ps) {
     if constexpr (PL == 1) return q[0];
-    else return q[0] & ~q[ps];
+    else if constexpr (PL == 2) return q[0] & ~q[ps];
+    else return q[0] & ~(q[ps] | q[2 * ps]);
+}
+
+// First input of row offset dy in the von Neumann(R) input list (rows -R..R contribute
+// 2(R - |dy|) + 1 horizontally shifted words each).
+__host__ __device__ constexpr int vn_base(int R, int dy) {
+    int n = 0;
+    for (int d = -R; d < dy; ++d) n += 2 * (R - (d < 0 ? -d : d)) + 1;
+    return n;
+}
+
+// Bit-sliced von Neumann(R) count (centre included) of word column `ca` at row y, R = 2 or 3:
+// the diamond's 2R^2 + 2R + 1 shifted alive words (13 or 25) through the full-adder trees of the
+// Moore kernel (13 inputs: the 13-input tree; 25: the 15- and 9-input trees, then a ripple add
+// with the last input as the carry-in).
+template <int R, int PL, int BV>
+__device__ __forceinline__ void vn_count(const uint32_t* ca, int y, int sw, int ps, uint32_t* v) {
+    static_assert(R == 2 || R == 3, "von Neumann(2) or (3)");
+    constexpr int NIN = 2 * R * R + 2 * R + 1;
+    uint32_t x[NIN];
+#pragma unroll
+    for (int dy = -R; dy <= R; ++dy) {
+        const uint32_t* row = ca + (y + dy) * sw;
+        const uint32_t l = alive_word<PL>(row - 1, ps), c = alive_word<PL>(row, ps), r = alive_word<PL>(row + 1, ps);
+        const int k = R - (dy < 0 ? -dy : dy), b = vn_base(R, dy);
+        x[b] = c;
+#pragma unroll
+        for (int d = 1; d <= k; ++d) {
+            x[b + 2 * d - 1] = __funnelshift_l(l, c, d);  // cell x - d
+            x[b + 2 * d] = __funnelshift_r(c, r, d);      // cell x + d
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < BV; ++i) v[i] = 0u;
+    if constexpr (R == 2) {
+        hcount<6>(x, v);  // 13 inputs, four planes
+    } else {
+        uint32_t a[4], bb[4], c = x[24];
+        hcount<7>(x, a);        // inputs 0..14
+        hcount<4>(x + 15, bb);  // inputs 15..23
+#pragma unroll
+        for (int i = 0; i < 4; ++i) fa(a[i], bb[i], c, v[i], c);
+        v[4] = c;
+    }
 }
 
 // One sub-step of word column w over rows [r0, r1). Moore(R): a ring of the last 2R+1 rows'
-// horizontal counts and their running vertical sum. VN (von Neumann(1)): each row's count is its
-// 3-cell horizontal count plus the cells above and below.
+// horizontal counts and their running vertical sum. VN, von Neumann(1): each row's count is its
+// 3-cell horizontal count plus the cells above and below; von Neumann(2, 3): the diamond's
+// shifted words through an adder tree (vn_count).
 template <int R, int NI, int PL, bool GATED, bool VN>
 __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B,
                                             const uint32_t* __restrict__ M, int sw, int ps, int w, int r0, int r1,
@@ -374,8 +436,13 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
     if constexpr (GATED) {
         if (gt.mode == 1) cc = checker_col(p, gt.X0 + 32 * w);
     }
-    if constexpr (VN) {
-        static_assert(R == 1, "von Neumann: radius 1");
+    if constexpr (VN && R > 1) {
+        for (int y = r0; y < r1; ++y) {
+            uint32_t v[BV];
+            vn_count<R, PL, BV>(ca, y, sw, ps, v);
+            life_emit<BV, NI, PL, GATED>(v, ca, cb, cm, y, sw, ps, w, tb, p, gt, cc);
+        }
+    } else if constexpr (VN) {
         for (int y = r0; y < r1; ++y) {
             uint32_t h[2];
             hrow<1, PL>(ca + y * sw, ps, h);  // cells x - 1, x, x + 1: h0 + 2 h1
@@ -613,29 +680,40 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
     }
 
     int active = 0;  // a written cell differs from the background (active-tile sweeps)
-    const uint32_t bg0 = (p.background & 1) ? 0xFFFFFFFFu : 0u;                // the background's
-    const uint32_t bg1 = PL == 2 && (p.background & 2) ? 0xFFFFFFFFu : 0u;     // plane bits
+    uint32_t bgp[PL];  // the background's plane bits
+#pragma unroll
+    for (int pl = 0; pl < PL; ++pl) bgp[pl] = ((p.background >> pl) & 1) ? 0xFFFFFFFFu : 0u;
     for (int q = threadIdx.x; q < g.tw * g.ty; q += blockDim.x) {
         const int lw = g.hw + q % g.tw, ly = g.hy + q / g.tw;
         const int64_t gy = Y0 + ly, gx = X0 + 32 * lw;
         if (gy >= p.n2 || gx >= p.n1) continue;
-        const uint32_t bits = A[ly * g.sw + 1 + lw];
-        const uint32_t hib = PL == 2 ? A[ps + ly * g.sw + 1 + lw] : 0u;
+        uint32_t pw[PL];
+        uint32_t diff = 0u;
+#pragma unroll
+        for (int pl = 0; pl < PL; ++pl) {
+            pw[pl] = A[pl * ps + ly * g.sw + 1 + lw];
+            diff |= pw[pl] ^ bgp[pl];
+        }
         const uint32_t valid = gx + 32 <= p.n1 ? 0xFFFFFFFFu : ((1u << (p.n1 - gx)) - 1u);
-        active |= (((bits ^ bg0) | (PL == 2 ? hib ^ bg1 : 0u)) & valid) != 0u;
+        active |= (diff & valid) != 0u;
         int8_t* out = dst + gy * p.pitch + gx;
         if (gx + 32 <= p.n1) {
-            int4 q0 = bytes16(bits), q1 = bytes16(bits >> 16);
-            if (PL == 2) {
-                const int4 h0 = bytes16(hib), h1 = bytes16(hib >> 16);
-                q0 = make_int4(q0.x | (h0.x << 1), q0.y | (h0.y << 1), q0.z | (h0.z << 1), q0.w | (h0.w << 1));
-                q1 = make_int4(q1.x | (h1.x << 1), q1.y | (h1.y << 1), q1.z | (h1.z << 1), q1.w | (h1.w << 1));
+            int4 q0 = bytes16(pw[0]), q1 = bytes16(pw[0] >> 16);
+#pragma unroll
+            for (int pl = 1; pl < PL; ++pl) {
+                const int4 h0 = bytes16(pw[pl]), h1 = bytes16(pw[pl] >> 16);
+                q0 = make_int4(q0.x | (h0.x << pl), q0.y | (h0.y << pl), q0.z | (h0.z << pl), q0.w | (h0.w << pl));
+                q1 = make_int4(q1.x | (h1.x << pl), q1.y | (h1.y << pl), q1.z | (h1.z << pl), q1.w | (h1.w << pl));
             }
             ((int4*)out)[0] = q0;
             ((int4*)out)[1] = q1;
         } else {
-            for (int b = 0; gx + b < p.n1; ++b)
-                out[b] = (int8_t)(((bits >> b) & 1u) | (PL == 2 ? ((hib >> b) & 1u) << 1 : 0u));
+            for (int b = 0; gx + b < p.n1; ++b) {
+                uint32_t v = 0;
+#pragma unroll
+                for (int pl = 0; pl < PL; ++pl) v |= ((pw[pl] >> b) & 1u) << pl;
+                out[b] = (int8_t)v;
+            }
         }
     }
     if (p.tile_list) {
@@ -660,8 +738,8 @@ template <int R, int PL, bool VN = false>
 cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src, int8_t* dst,
                      cudaStream_t st, int ntiles = 0) {
     const int ni = tb.n[0] > tb.n[1] ? tb.n[0] : tb.n[1];
-    if (p.scheme != GBCA_SYNCHRONOUS || p.mask) {  // gated variants (gates, masks) exist for r <= 2
-        if constexpr (R <= 2) {
+    if (p.scheme != GBCA_SYNCHRONOUS || p.mask) {  // gated variants (gates, masks) exist for r <= 5
+        if constexpr (R <= 5) {
             if (ni <= 1) return launch_rn<R, 1, PL, true, VN>(p, g, tb, src, dst, st, ntiles);
             if (ni <= 2) return launch_rn<R, 2, PL, true, VN>(p, g, tb, src, dst, st, ntiles);
             return launch_rn<R, kMaxIntervals, PL, true, VN>(p, g, tb, src, dst, st, ntiles);
@@ -679,14 +757,28 @@ cudaError_t launch_r(const SweepParams& p, const LifeGeom& g, const LifeTables& 
 
 }  // namespace
 
-// Moore(R): Life-like rules, and Generations (two planes) for R <= 2.
+// Moore(R): Life-like rules, and Generations (two planes up to C = 4, three up to 8) for R <= 2.
 template <int R>
 cudaError_t launch_life_radius(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
                                int8_t* dst, cudaStream_t st, int ntiles) {
     if constexpr (R <= 2) {
-        if (p.rule == GBCA_RULE_GENERATIONS) return launch_r<R, 2>(p, g, tb, src, dst, st, ntiles);
+        if (p.rule == GBCA_RULE_GENERATIONS) {
+            if (p.states <= 4) return launch_r<R, 2>(p, g, tb, src, dst, st, ntiles);
+            return launch_r<R, 3>(p, g, tb, src, dst, st, ntiles);
+        }
     }
     return launch_r<R, 1>(p, g, tb, src, dst, st, ntiles);
+}
+
+// von Neumann(R): Life-like rules and Generations (two or three planes).
+template <int R>
+cudaError_t launch_life_vn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
+                           int8_t* dst, cudaStream_t st, int ntiles) {
+    if (p.rule == GBCA_RULE_GENERATIONS) {
+        if (p.states <= 4) return launch_r<R, 2, true>(p, g, tb, src, dst, st, ntiles);
+        return launch_r<R, 3, true>(p, g, tb, src, dst, st, ntiles);
+    }
+    return launch_r<R, 1, true>(p, g, tb, src, dst, st, ntiles);
 }
 
 }  // namespace gbca

@@ -252,7 +252,7 @@ EnsInstance small_instance(const Request* r, int64_t steps, bool last) {
 double est_rate(const gbca_desc& d) {
     if (d.rule == GBCA_RULE_FOREST_FIRE) return d.nbhd == GBCA_VON_NEUMANN && d.radius == 1 ? 3.5e11 : 5e10;
     if (d.rule == GBCA_RULE_LIFE && d.nbhd == GBCA_MOORE && d.radius <= 7) return 4e12 / d.radius;
-    if (d.rule == GBCA_RULE_GENERATIONS && d.nbhd == GBCA_MOORE && d.radius <= 2 && d.states <= 4)
+    if (d.rule == GBCA_RULE_GENERATIONS && d.nbhd == GBCA_MOORE && d.radius <= 2 && d.states <= 8)
         return 2e12 / d.radius;
     return 1e11 / (d.radius * d.radius);
 }

@@ -1,6 +1,6 @@
 // sweep_dispatch.cu — picks the sweep kernel for an Int8 problem and runs nsteps steps as
 // temporally blocked passes: the forest-fire kernel (VonNeumann(1), Synchronous), the
-// bit-sliced kernel (Life-like on Moore(r <= 7); Generations with C <= 4 on Moore(r <= 2)
+// bit-sliced kernel (Life-like on Moore(r <= 7); Generations with C <= 8 on Moore(r <= 2)
 // when every state is known to lie in 0..C-1), else the general kernel.
 #include <cstring>
 

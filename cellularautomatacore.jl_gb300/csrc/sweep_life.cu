@@ -1,7 +1,7 @@
 // sweep_life.cu — host side of the bit-sliced Life-like / Larger-than-Life / Generations sweep
 // (the kernel and its layout are described in life_kernel.cuh): the rule's comparator tables,
 // tile geometry and its cost model, and the dispatch to the per-radius kernels
-// (sweep_life_r1.cu .. sweep_life_r7.cu, sweep_life_vn1.cu).
+// (sweep_life_r1.cu .. sweep_life_r7.cu, sweep_life_vn1.cu .. sweep_life_vn3.cu).
 #include "life_common.cuh"
 
 namespace gbca {
@@ -48,6 +48,7 @@ bool make_tables(const SweepParams& p, LifeTables* tb) {
     }
     tb->c3 = p.states > 2 ? 0xFFFFFFFFu : 0u;
     tb->c4 = p.states == 4 ? 0xFFFFFFFFu : 0u;
+    for (int i = 0; i < 3; ++i) tb->cb[i] = ((p.states >> i) & 1) ? 0xFFFFFFFFu : 0u;
     return true;
 }
 
@@ -60,7 +61,8 @@ LifeGeom life_geometry(const SweepParams& p, int K, int rows) {
     const int64_t words = (p.n1 + 31) / 32;
     const int tw = p.tile_x > 0 ? p.tile_x : 32;  // the default choice's width, or 32 words
     g.tw = words < tw ? (int)words : tw;
-    int ty = p.rule == GBCA_RULE_GENERATIONS ? 96 : 216;  // two planes: half the rows
+    const int PL = life_planes(p);
+    int ty = PL == 1 ? 216 : (PL == 2 ? 96 : 64);  // more planes: fewer rows
     if (rows > 0) ty = rows;
     g.ty = p.n2 < ty ? (int)p.n2 : ty;
     g.sw = g.tw + 2 * g.hw + 2;
@@ -71,7 +73,7 @@ LifeGeom life_geometry(const SweepParams& p, int K, int rows) {
 }  // namespace
 
 size_t life_smem_bytes(const SweepParams& p, const LifeGeom& g) {
-    const int PL = p.rule == GBCA_RULE_GENERATIONS ? 2 : 1;
+    const int PL = life_planes(p);
     const int planes = 2 * PL + (p.mask ? 1 : 0);  // two buffers of PL planes, and the mask's bits
     return (size_t)planes * (size_t)g.sw * (size_t)g.sy * 4;
 }
@@ -81,7 +83,11 @@ namespace {
 // The kernel of the problem's rule, neighbourhood and radius (life_simd_supported holds).
 cudaError_t launch_by_rule(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
                            int8_t* dst, cudaStream_t st, int ntiles) {
-    if (p.nbhd == GBCA_VON_NEUMANN) return launch_life_vn1(p, g, tb, src, dst, st, ntiles);  // radius 1
+    if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1..3
+        if (p.radius == 1) return launch_life_vn<1>(p, g, tb, src, dst, st, ntiles);
+        if (p.radius == 2) return launch_life_vn<2>(p, g, tb, src, dst, st, ntiles);
+        return launch_life_vn<3>(p, g, tb, src, dst, st, ntiles);
+    }
     switch (p.radius) {
         case 1: return launch_life_radius<1>(p, g, tb, src, dst, st, ntiles);
         case 2: return launch_life_radius<2>(p, g, tb, src, dst, st, ntiles);
@@ -97,8 +103,8 @@ cudaError_t launch_by_rule(const SweepParams& p, const LifeGeom& g, const LifeTa
 
 bool life_simd_supported(const SweepParams& p) {
     if (p.radius < 1 || p.pitch % 16 != 0) return false;
-    if (p.mask && (((uintptr_t)p.mask & 15u) != 0 || p.radius > 2)) return false;  // the gated kernels: r <= 2
-    if (p.nbhd != GBCA_MOORE && !(p.nbhd == GBCA_VON_NEUMANN && p.radius == 1)) return false;
+    if (p.mask && (((uintptr_t)p.mask & 15u) != 0 || p.radius > 5)) return false;  // the gated kernels: r <= 5
+    if (p.nbhd != GBCA_MOORE && !(p.nbhd == GBCA_VON_NEUMANN && p.radius <= 3)) return false;
     if (p.scheme == GBCA_CHECKERBOARD) {
         // any boundary: the gate maps halo cells to the cells they image (checker_gate)
     } else if (p.scheme == GBCA_STOCHASTIC) {
@@ -106,14 +112,15 @@ bool life_simd_supported(const SweepParams& p) {
     } else if (p.scheme != GBCA_SYNCHRONOUS) {
         return false;
     }
-    if (p.scheme != GBCA_SYNCHRONOUS && p.radius > 2) return false;  // gated kernels: r <= 2
+    if (p.scheme != GBCA_SYNCHRONOUS && p.radius > 5) return false;  // gated kernels: r <= 5
     // a closed or masked Life cell keeps its value: the indicator bits hold it only for 0 and 1
     if ((p.scheme != GBCA_SYNCHRONOUS || p.mask) && p.rule == GBCA_RULE_LIFE && !p.states_valid) return false;
     if (p.rule == GBCA_RULE_LIFE) {
         if (p.radius > 7) return false;  // counts up to 15^2 = 225 in 8 bit planes
     } else if (p.rule == GBCA_RULE_GENERATIONS) {
-        // two planes hold states 0..3; every state (and Constant value) must lie in 0..C-1
-        if (p.radius > 2 || p.states > 4 || !p.states_valid) return false;
+        // two planes hold states 0..3, three 0..7; every state (and Constant value) must lie in 0..C-1;
+        // Moore(1, 2) and von Neumann(1..3)
+        if (p.radius > (p.nbhd == GBCA_VON_NEUMANN ? 3 : 2) || p.states > 8 || !p.states_valid) return false;
         for (int a = 0; a < 2; ++a)
             if (p.bnd[a] == GBCA_CONSTANT && (p.cval[a] < 0 || p.cval[a] >= p.states)) return false;
     } else {
@@ -137,8 +144,8 @@ int life_steps_per_pass(const SweepParams& p) {
 // The geometry for a lattice that has no tuned or pinned one: the steps per pass, tile height
 // and tile width that minimise a cost model of one pass per cell-update. A pass costs the
 // busiest SM's CTAs (ceil(CTAs / SMs), at least kLifeSatCtas: one 8-warp CTA does not keep an
-// SM busy) times the work of one CTA, at a per-SM rate, plus a fixed launch cost. A CTA's work is the cells it computes — its tile plus the halo each
-// sub-step recomputes, ex = (K - 1 - s) r rows on each side and one word on each side while
+// SM busy) times the work of one CTA, at a per-SM rate, plus a fixed launch cost. A CTA's
+// work is the cells it computes — its tile plus the halo each sub-step recomputes, ex = (K - 1 - s) r rows on each side and one word on each side while
 // ex > 0 — plus its loaded region (tile and full halo) at kLifeIoCost cell-steps per cell for
 // packing bytes into bits and unpacking the results; that term favours deep passes. Wide tiles
 // and deep passes waste least on large lattices; narrower, shorter tiles fill the GPU on
@@ -148,7 +155,7 @@ int life_steps_per_pass(const SweepParams& p) {
 SweepChoice life_default_choice(const SweepParams& p0) {
     SweepParams p = p0;
     const int Kmax = life_steps_per_pass(p);
-    const int PL = p.rule == GBCA_RULE_GENERATIONS ? 2 : 1;
+    const int PL = life_planes(p);
     // seconds per SM: a cell-step of the bit-sliced rule, plus a Philox gate draw per cell-step
     // under Stochastic (about 3.3e9 draws per second per SM), and a loaded cell's packing
     const double rate = 60e9 / (p.radius * PL);

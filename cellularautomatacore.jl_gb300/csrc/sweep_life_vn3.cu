@@ -1,0 +1,8 @@
+// sweep_life_vn3.cu — the bit-sliced sweep's kernels for von Neumann(3) (life_kernel.cuh): Life-like
+// rules and Generations with up to 8 states.
+#include "life_kernel.cuh"
+
+namespace gbca {
+template cudaError_t launch_life_vn<3>(const SweepParams&, const LifeGeom&, const LifeTables&, const int8_t*, int8_t*,
+                                       cudaStream_t, int);
+}  // namespace gbca

@@ -375,3 +375,129 @@ def test_device_summaries(ca, oracle):
     checker = np.array([[(i + j) % 2 for j in range(6)] for i in range(6)], np.int8)
     st = ca.allocate_state(ca.GB300Backend(), ca.CAProblem.new(ca.Life(), checker, 1), ca.Synchronous())
     assert abs(ca.device_summaries(st, 2)[2] + 1.0) < 1e-15  # test/test_extras.jl:140-141
+
+
+GEN_WIDE = [
+    # name, dims, kwargs, steps, saveat
+    ("C=5 Moore(1) torus", (300, 200), dict(birth=[2], survive=[3, 4], states=5), 30, 10),
+    ("C=6 Moore(2), Constant(4) and Constant(1) edges", (150, 170),
+     dict(r=2, birth=[3, 4, 5], survive=[2, 3, 4, 5, 6], states=6, bnd=("c", "c"), const=(4, 1)), 20, 5),
+    ("C=7 reflecting x torus, tiled", (400, 130), dict(birth=[2, 3], survive=[3, 4, 5], states=7, bnd=("r", "p")),
+     25, 25),
+    ("C=8 Moore(1) torus (a dying 7 wraps to 0)", (200, 96), dict(birth=[2], survive=[2, 3], states=8), 30, 6),
+    ("C=5 von Neumann(1), reflecting", (150, 90), dict(nb="vn", birth=[1], survive=[1, 2], states=5,
+                                                       bnd=("r", "r")), 30, 10),
+    ("C=8 von Neumann(1) Checkerboard, Constant grid", (129, 77),
+     dict(nb="vn", birth=[2], survive=[1, 2], states=8, scheme="check", bnd=("c", "c"), const=(0, 5)), 24, 6),
+    ("C=6 Stochastic(0.6) Moore(2), cylinder", (160, 96),
+     dict(r=2, birth=[3, 4, 5], survive=[2, 3, 4, 5, 6], states=6, seed=24, scheme="stoch", sp=0.6,
+          bnd=("p", "c"), const=(0, 3)), 20, 4),
+    ("C=7 Checkerboard Moore(1), odd torus", (51, 40), dict(birth=[2], survive=[3], states=7, scheme="check"), 20, 5),
+]
+
+
+@pytest.mark.parametrize("case", GEN_WIDE, ids=[c[0] for c in GEN_WIDE])
+def test_generations_three_planes(ca, oracle, case):
+    """Generations with 5..8 states (src/rules.jl:424-456) in the bit-sliced kernel's three-plane
+    form, on every boundary kind and scheme: every save equals the oracle's, and the geometry
+    query names a bit-sliced geometry (not the general kernel)."""
+    import ctypes
+    name, (n1, n2), kw, steps, saveat = case
+    rule, space, scheme, P = spec_pair(ca, oracle, "gen", n1, n2, **kw)
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
+    u0 = rng.integers(0, P.states, (n1, n2)).astype(np.int8)
+    prob = ca.CAProblem.new(rule, u0, steps, space=space, seed=kw.get("seed", 0))
+    sol = ca.solve(prob, scheme, backend=ca.GB300Backend(), saveat=saveat)
+    ts, us = oracle.solve(P, u0, steps, saveat=saveat, nthreads=8)
+    assert sol.t == ts
+    for k, (a, b) in enumerate(zip(sol.u, us)):
+        assert np.array_equal(a, b), f"{name}: save {k} (t = {ts[k]}) differs in {(a != b).sum()} cells"
+    assert not np.array_equal(us[-1], u0) and (us[-1] >= 3).any()
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, scheme)
+    ca.advance(B, st, prob, scheme, None, 0)
+    ca.current_state(B, st)  # the state scan has run
+    k, rows, staging = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    ca.capi.check(ca.capi.lib().gbca_geometry(st.handle, None, ctypes.byref(k), ctypes.byref(rows),
+                                              ctypes.byref(staging)))
+    assert k.value > 0, f"{name} fell back to the general kernel"
+    st.close()
+
+
+WIDENED = [
+    # name, kind, dims, kwargs, steps, saveat — von Neumann(2, 3) and gated / masked Moore(3..5), which
+    # the bit-sliced kernel runs
+    ("von Neumann(2) Life-like torus", "life", (300, 200), dict(nb="vn", r=2, birth=[3, 4], survive=[2, 3, 4]), 30,
+     10),
+    ("von Neumann(3) Life-like, Constant(1) grid", "life", (257, 190),
+     dict(nb="vn", r=3, birth=[5, 6, 7, 8], survive=[4, 5, 6, 7, 8, 9], bnd=("c", "c"), const=(1, 1)), 24, 8),
+    ("von Neumann(3), reflecting x odd torus", "life", (129, 77),
+     dict(nb="vn", r=3, birth=[6, 7, 8, 12], survive=[5, 6, 7, 8, 9, 10], bnd=("r", "p")), 20, 5),
+    ("von Neumann(2) Generations C=4, reflecting", "gen", (150, 90),
+     dict(nb="vn", r=2, birth=[3, 4], survive=[2, 3, 4, 5], states=4, bnd=("r", "r")), 30, 10),
+    ("von Neumann(3) Generations C=6, torus", "gen", (200, 96),
+     dict(nb="vn", r=3, birth=[4, 5, 6], survive=[3, 4, 5, 6, 7], states=6), 30, 6),
+    ("von Neumann(2) Stochastic(0.5), cylinder", "life", (200, 64),
+     dict(nb="vn", r=2, birth=[3, 4], survive=[2, 3, 4], seed=41, scheme="stoch", sp=0.5, bnd=("p", "c")), 25, 5),
+    ("von Neumann(3) Checkerboard, Constant grid", "life", (131, 97),
+     dict(nb="vn", r=3, birth=[5, 6, 7, 8], survive=[4, 5, 6, 7, 8, 9], scheme="check", bnd=("c", "c")), 20, 5),
+    ("Checkerboard Moore(3), odd torus", "life", (151, 103),
+     dict(r=3, birth=range(9, 15), survive=range(8, 20), scheme="check"), 20, 5),
+    ("Stochastic(0.4) Moore(4), reflecting", "life", (180, 150),
+     dict(r=4, birth=range(14, 25), survive=range(12, 30), seed=44, scheme="stoch", sp=0.4, bnd=("r", "r")), 20, 4),
+    ("Checkerboard Larger than Life Moore(5), Constant grid", "life", (230, 170),
+     dict(r=5, birth=range(34, 46), survive=range(34, 59), scheme="check", bnd=("c", "c")), 16, 4),
+    ("Stochastic(0.7f0) Moore(5), torus, several intervals", "life", (200, 180),
+     dict(r=5, birth=[34, 35, 36, 40, 41, 42], survive=range(34, 59), seed=45, scheme="stoch", sp=0.7, sp32=True),
+     16, 8),
+]
+
+
+@pytest.mark.parametrize("case", WIDENED, ids=[c[0] for c in WIDENED])
+def test_widened_bit_sliced(ca, oracle, case):
+    """von Neumann(2) and (3) (13 and 25 cells, src/neighbourhoods.jl:33-42,148-153) and the
+    gated schemes on Moore(3..5) run the bit-sliced kernel: every save equals the oracle's, and
+    the geometry query names a bit-sliced geometry."""
+    import ctypes
+    name, kind, (n1, n2), kw, steps, saveat = case
+    rule, space, scheme, P = spec_pair(ca, oracle, kind, n1, n2, **kw)
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
+    u0 = rng.integers(0, P.states, (n1, n2)).astype(np.int8)
+    prob = ca.CAProblem.new(rule, u0, steps, space=space, seed=kw.get("seed", 0))
+    sol = ca.solve(prob, scheme, backend=ca.GB300Backend(), saveat=saveat)
+    ts, us = oracle.solve(P, u0, steps, saveat=saveat, nthreads=8)
+    assert sol.t == ts
+    for k, (a, b) in enumerate(zip(sol.u, us)):
+        assert np.array_equal(a, b), f"{name}: save {k} (t = {ts[k]}) differs in {(a != b).sum()} cells"
+    assert not np.array_equal(us[-1], u0) and 0 < (us[-1] == 1).sum() < us[-1].size
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, scheme)
+    ca.advance(B, st, prob, scheme, None, 0)
+    ca.current_state(B, st)
+    k, rows, staging = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    ca.capi.check(ca.capi.lib().gbca_geometry(st.handle, None, ctypes.byref(k), ctypes.byref(rows),
+                                              ctypes.byref(staging)))
+    assert k.value > 0, f"{name} fell back to the general kernel"
+    st.close()
+
+
+@pytest.mark.parametrize("r", [3, 5])
+def test_masked_moore_bit_sliced(ca, oracle, r):
+    """A masked Larger-than-Life sweep on Moore(3) and Moore(5) (src/environment.jl:123-130): masked
+    cells keep their state though their neighbours read them; equal to the oracle step by step."""
+    n1, n2 = 170, 130
+    birth, survive = (range(9, 15), range(8, 20)) if r == 3 else (range(34, 46), range(34, 59))
+    rule, space, scheme, P = spec_pair(ca, oracle, "life", n1, n2, r=r, birth=birth, survive=survive, bnd=("p", "r"))
+    rng = np.random.default_rng(70 + r)
+    u0 = rng.integers(0, 2, (n1, n2)).astype(np.int8)
+    mask = np.ones((n1, n2), bool)
+    mask[40:90, 20:70] = False
+    mask[::7, :] = False
+    prob = ca.CAProblem.new(rule, u0, 12, space=space, mask=mask)
+    sol = ca.solve(prob, scheme, backend=ca.GB300Backend(), saveat=4)
+    env = oracle.Env(mask=mask)
+    want = u0
+    for k, t in enumerate(range(0, 12, 4)):
+        want = oracle.run_array_env(P, env, want, t, 4, nthreads=8)
+        assert np.array_equal(sol.u[k + 1], want), f"Moore({r}) masked, t = {t + 4}"
+    assert np.array_equal(sol.u[-1][~mask], u0[~mask]) and not np.array_equal(sol.u[-1], u0)
