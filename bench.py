@@ -529,7 +529,7 @@ def bench_batched(capi, lib, warmup: int, steps: int):
 
 
 SERVE = dict(rate=2000.0, seconds=2.0, plain_sample=48, hbm_budget=8 << 30, chunk_steps=100,
-             big_cells=1 << 16, max_big=16)
+             big_cells=1 << 14, max_big=16)
 
 
 def serve_requests(n: int, seed: int = 2000):

@@ -9,9 +9,10 @@
 //    released the moment it finishes. A request larger than the whole arena is refused.
 //  * Continuous batching, event driven: large requests run on `max_big` stream lanes in chunks
 //    of about big_chunk_us (default kChunkSeconds) of estimated GPU time (temporally blocked multi-CTA sweeps; the
-//    last chunk ends with the request's summaries); small requests run together,
-//    `chunk_steps` steps at a time, in persistent ensemble launches (ensemble.cu; one CTA per
-//    request) on their own stream, back to back. Every launch ends with an event and a host
+//    last chunk ends with the request's summaries); small requests run together, each up to
+//    `chunk_steps` steps (fewer for larger lattices, so that no launch outlasts about
+//    kSmallLaunchSeconds of one CTA's work) in persistent ensemble launches (ensemble.cu; one
+//    CTA per request) on their own stream, back to back. Every launch ends with an event and a host
 //    callback that wakes the scheduler, which then collects what finished, frees its memory,
 //    admits waiting requests and refills the idle lane or the small stream at once: no lane
 //    waits for another, and no iteration-wide barrier holds the device.
@@ -115,6 +116,10 @@ struct Request {
 // says otherwise, and chunks in flight holding at most this many GPUs' worth of tiles.
 constexpr double kChunkSeconds = 4e-3;
 constexpr double kFillCap = 2.0;
+// A persistent launch of small requests lasts as long as its slowest instance (one CTA each), and
+// requests arriving meanwhile wait for it: each instance takes about this much of its CTA's time
+// per launch (at most chunk_steps steps).
+constexpr double kSmallLaunchSeconds = 1.5e-3;
 
 int sfail(int code, const char* fmt, ...) {
     char msg[512];
@@ -264,6 +269,15 @@ double est_fill(const gbca_desc& d) {
     const double cells = (double)d.n1 * (double)d.n2;
     const double full = d.rule == GBCA_RULE_FOREST_FIRE ? 1.2e7 : 6e7;
     return cells >= full ? 1.0 : cells / full;
+}
+
+// Steps of a small request per persistent launch: kSmallLaunchSeconds of one CTA at its
+// estimated rate (the forest fire's Philox draws, the other rules' byte-per-cell updates), at
+// least 1 and at most chunk_steps.
+int64_t small_chunk(const gbca_desc& d, int64_t chunk_steps) {
+    const double cta_rate = d.rule == GBCA_RULE_FOREST_FIRE ? 3e8 : 6e8;
+    const int64_t s = (int64_t)(kSmallLaunchSeconds * cta_rate / ((double)d.n1 * (double)d.n2));
+    return s < 1 ? 1 : (s > chunk_steps ? chunk_steps : s);
 }
 
 double est_remaining_s(const Request* r) {
@@ -478,8 +492,8 @@ void scheduler(gbca_server* S) {
             for (size_t j = 0; j < batch.size() && e == cudaSuccess; ++j) {
                 Request* r = batch[j];
                 if (r->fresh) e = init_state(S, r, S->s_small);
-                const int64_t rem = r->nsteps - r->done;
-                batch_steps[j] = rem < S->cfg.chunk_steps ? rem : S->cfg.chunk_steps;
+                const int64_t rem = r->nsteps - r->done, cap = small_chunk(r->d, S->cfg.chunk_steps);
+                batch_steps[j] = rem < cap ? rem : cap;
                 inst[j] = small_instance(r, batch_steps[j], batch_steps[j] == rem);
                 work[j] = r->d.n1 * r->d.n2 * batch_steps[j];
             }

@@ -311,8 +311,8 @@ int gbca_ensemble_tune(gbca_ensemble* e, int64_t probe_steps, const double* para
 /* ---- serving: a device-resident request loop with continuous batching. Clients submit
  * simulation requests at any time; a scheduler thread admits them in arrival order while
  * their state buffers fit the HBM budget and returns each request's state counts and Moran's
- * I as soon as it finishes. Small requests advance together, chunk_steps steps per persistent
- * launch; large ones (above big_cells cells) run as multi-CTA sweeps on up to max_big stream
+ * I as soon as it finishes. Small requests advance together in persistent launches, up to
+ * chunk_steps steps each per launch (fewer on larger lattices, so a launch stays short); large ones (above big_cells cells) run as multi-CTA sweeps on up to max_big stream
  * lanes, in chunks of big_chunk_us of estimated GPU time (at least chunk_steps steps),
  * the request with the shortest estimated remaining time (less its time in the system) first,
  * while the chunks in flight fill at most two GPUs' worth of tiles. A request's result does
