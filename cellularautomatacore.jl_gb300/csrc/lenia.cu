@@ -9,9 +9,10 @@
 // Direct field: a fused kernel per step. The CTA stages a tile of u plus a halo of R
 // cells in shared memory (periodic / reflecting / Constant(0) through the boundary map);
 // each thread computes 16 consecutive cells of a row, sliding a 16+2R register window
-// over every kernel row, so each shared-memory value feeds up to 16 fused multiply-adds.
+// over the kernel rows, so each shared-memory value feeds up to 16 fused multiply-adds.
 // R = 13 (the standard Lenia radius) is specialised with the disk taps unrolled at
-// compile time and the weights in the parameter bank; other radii loop over a tap list.
+// compile time, the weights in the parameter bank, and the rows dj and -dj (equal weights)
+// summed before the multiply-adds; other radii loop over a tap list.
 //
 // FFT field (periodic lattices, the FFTW extension's convention
 // ext/CellularAutomataCoreFFTWExt.jl:17-30): U = irfft(rfft(u) .* conj(rfft(kpad))) with
@@ -62,27 +63,78 @@ __device__ __forceinline__ void load_tile(const T* __restrict__ u, int64_t n1, i
     }
 }
 
+// 16 bytes of a 16-byte-aligned shared-memory row into consecutive registers.
+template <typename T>
+__device__ __forceinline__ void load16(const T* p, T* dst) {
+    if constexpr (sizeof(T) == 4) {
+        const float4 v = *(const float4*)p;
+        dst[0] = v.x;
+        dst[1] = v.y;
+        dst[2] = v.z;
+        dst[3] = v.w;
+    } else {
+        const double2 v = *(const double2*)p;
+        dst[0] = v.x;
+        dst[1] = v.y;
+    }
+}
+
+// Shared row pitch of k_lenia13's tile, in elements: room for the last thread's 16-byte-aligned
+// window (cells lx0 - R .. lx0 + 15 + R rounded up to whole 16-byte loads), and a row length of
+// 16 bytes modulo 128, so that eight consecutive rows start in eight different groups of four
+// banks and a quarter-warp's eight 16-byte loads (one per row) meet no bank conflict.
+template <typename T>
+constexpr int lenia13_pitch() {
+    constexpr int V = 16 / (int)sizeof(T);
+    constexpr int need = kDirTX - kDirCells + (kDirCells + 2 * kR13 + V - 1) / V * V;
+    int sp = need;
+    while ((sp * (int)sizeof(T)) % 128 != 16) ++sp;
+    return sp;
+}
+
+// R = 13. The Lenia kernel depends on the distance only, so rows dj and -dj carry the same
+// weights: each thread adds the two rows' windows first (one add per window cell) and then
+// runs one fused multiply-add per tap of the pair for each of its 16 cells, 271 per cell for
+// the 516 taps. Windows arrive by 16-byte shared-memory loads. Thread layout: the eight lanes
+// of a quarter-warp take eight consecutive output rows at the same 16 columns (lanes 8q..8q+7,
+// column block 4 (warp / 4) + q), so with lenia13_pitch each of their loads is conflict-free.
 template <typename T>
 __global__ void __launch_bounds__(256) k_lenia13(const T* __restrict__ u, T* __restrict__ out, int64_t n1, int64_t n2,
                                                  int64_t pe, int b1, int b2, Box13<T> wb, T mu, T sigma, T dt) {
     extern __shared__ __align__(16) unsigned char lsm[];
     T* s = (T*)lsm;
     constexpr int sx = kDirTX + 2 * kR13, sy = kDirTY + 2 * kR13;
-    constexpr int sp = (sx + 3 + 4) / 4 * 4;  // row pitch, room for the last aligned window
+    constexpr int sp = lenia13_pitch<T>();
+    constexpr int V = 16 / sizeof(T);          // elements per 16-byte load
+    constexpr int W = kDirCells + 2 * kR13;    // window: cells x - R .. x + 15 + R
+    constexpr int WL = (W + V - 1) / V * V;    // loaded window
+    static_assert(kDirTX / kDirCells == 8 && kDirTY == 32, "thread layout: 8 column blocks x 32 rows");
     const int64_t X0 = (int64_t)blockIdx.x * kDirTX, Y0 = (int64_t)blockIdx.y * kDirTY;
     load_tile<T>(u, n1, n2, pe, b1, b2, X0 - kR13, Y0 - kR13, sx, sy, sp, s);
     __syncthreads();
-    const int tx = threadIdx.x % (kDirTX / kDirCells), ty = threadIdx.x / (kDirTX / kDirCells);
-    const int lx0 = tx * kDirCells;  // local x of the first output (tile coords), halo-shifted below
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tx = 4 * (warp >> 2) + (lane >> 3), ty = 8 * (warp & 3) + (lane & 7);
+    const int lx0 = tx * kDirCells;                // local x of the first output (tile coords)
+    const T* centre = s + (ty + kR13) * sp + lx0;  // the thread's row, from cell lx0 - R
     T acc[kDirCells];
 #pragma unroll
     for (int k = 0; k < kDirCells; ++k) acc[k] = T(0);
 #pragma unroll
-    for (int dj = -kR13; dj <= kR13; ++dj) {
-        const T* row = s + (ty + kR13 + dj) * sp + lx0;  // cell x = lx0 - R .. lx0 + 15 + R
-        T win[kDirCells + 2 * kR13];
+    for (int dj = 0; dj <= kR13; ++dj) {
+        T win[WL];
+        if (dj == 0) {
 #pragma unroll
-        for (int k = 0; k < kDirCells + 2 * kR13; ++k) win[k] = row[k];
+            for (int k = 0; k < WL; k += V) load16<T>(centre + k, win + k);
+        } else {
+            T lo[WL];
+#pragma unroll
+            for (int k = 0; k < WL; k += V) {
+                load16<T>(centre + dj * sp + k, win + k);
+                load16<T>(centre - dj * sp + k, lo + k);
+            }
+#pragma unroll
+            for (int k = 0; k < W; ++k) win[k] += lo[k];
+        }
 #pragma unroll
         for (int di = -kR13; di <= kR13; ++di) {
             if (!in_disk13(di, dj)) continue;
@@ -96,10 +148,7 @@ __global__ void __launch_bounds__(256) k_lenia13(const T* __restrict__ u, T* __r
 #pragma unroll
     for (int k = 0; k < kDirCells; ++k) {
         const int64_t gx = X0 + lx0 + k;
-        if (gx < n1) {
-            const T c = s[(ty + kR13) * sp + lx0 + k + kR13];
-            out[gx + gy * pe] = growth_step<T>(c, acc[k], mu, sigma, dt);
-        }
+        if (gx < n1) out[gx + gy * pe] = growth_step<T>(centre[k + kR13], acc[k], mu, sigma, dt);
     }
 }
 
@@ -307,6 +356,11 @@ int lenia_create(const gbca_desc& d, int64_t pitch_bytes, cudaStream_t st, Lenia
             P->b32.w[(dj + kR13) * kBox13 + di + kR13] = (float)P->w[k];
             P->b64.w[(dj + kR13) * kBox13 + di + kR13] = P->w[k];
         }
+        // the kernel pairs rows dj and -dj: their weights must be equal (a radial kernel's are)
+        for (int dj = 1; dj <= kR13 && P->box13; ++dj)
+            for (int di = -kR13; di <= kR13; ++di)
+                if (P->b64.w[(dj + kR13) * kBox13 + di + kR13] != P->b64.w[(kR13 - dj) * kBox13 + di + kR13])
+                    P->box13 = false;
     }
     cudaError_t e = cudaMalloc(&P->d_off, sizeof(int2) * ntaps);
     if (e == cudaSuccess) e = cudaMalloc(&P->d_w, (size_t)es * ntaps);
@@ -368,7 +422,7 @@ int advance_t(LeniaPlan* P, int64_t nsteps, cudaStream_t st, int* cur, void* con
                                                     dt);
             count_launch(2);
         } else if (P->box13) {
-            constexpr int sx = kDirTX + 2 * kR13, sy = kDirTY + 2 * kR13, sp = (sx + 3 + 4) / 4 * 4;
+            constexpr int sy = kDirTY + 2 * kR13, sp = lenia13_pitch<T>();
             const size_t smem = sizeof(T) * sp * sy;
             e = ensure_dynamic_smem((const void*)k_lenia13<T>, smem);
             if (e != cudaSuccess) return fail_to(err, GBCA_ERR_CUDA, cudaGetErrorString(e));

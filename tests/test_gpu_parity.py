@@ -392,7 +392,8 @@ GEN_WIDE = [
     ("C=6 Stochastic(0.6) Moore(2), cylinder", (160, 96),
      dict(r=2, birth=[3, 4, 5], survive=[2, 3, 4, 5, 6], states=6, seed=24, scheme="stoch", sp=0.6,
           bnd=("p", "c"), const=(0, 3)), 20, 4),
-    ("C=7 Checkerboard Moore(1), odd torus", (51, 40), dict(birth=[2], survive=[3], states=7, scheme="check"), 20, 5),
+    ("C=7 Checkerboard Moore(1), odd torus", (51, 40), dict(birth=[2, 3], survive=[3, 4, 5], states=7, scheme="check"),
+     20, 5),
 ]
 
 
@@ -501,3 +502,80 @@ def test_masked_moore_bit_sliced(ca, oracle, r):
         want = oracle.run_array_env(P, env, want, t, 4, nthreads=8)
         assert np.array_equal(sol.u[k + 1], want), f"Moore({r}) masked, t = {t + 4}"
     assert np.array_equal(sol.u[-1][~mask], u0[~mask]) and not np.array_equal(sol.u[-1], u0)
+
+
+def _tie_cells(oracle, seed, n1, n2, u0, t):
+    """Forest-fire parameters on the edge of chosen cells' draws (random.jl:116-120,129): p one
+    unit (2^-53) above an empty cell's 53-bit draw (a hit), f equal to a tree's (no hit), so each
+    draw agrees with its threshold in the first 32 bits and differs only in the last 21."""
+    def x53(i, j, k):
+        r = oracle.philox4x32(((i + j * n1 + 1) & 0xFFFFFFFF, 0, t, k), (seed & 0xFFFFFFFF, seed >> 32))
+        return ((r[0] << 32) | r[1]) >> 11
+
+    empties = [(i, j) for i, j in zip(*np.nonzero(u0 == 0))]
+    trees = [(i, j) for i, j in zip(*np.nonzero(u0 == 1))]
+    xe = next(x for x in (x53(i, j, 1) for i, j in empties[len(empties) // 3:]) if (x + 1) >> 21 == x >> 21)
+    xt = x53(*trees[len(trees) // 2], 2)
+    return (xe + 1) / 2.0**53, xt / 2.0**53
+
+
+def test_fire_threshold_ties(ca, oracle):
+    """Draws on the edge of their thresholds (see _tie_cells): every cell of the single-lattice
+    sweep (one and several tiles) and of the batched engine (persistent and multi-lattice passes)
+    equals the oracle, step by step."""
+    n1, n2, seed = 600, 300, 11
+    rng = np.random.default_rng(5)
+    u0 = (rng.random((n1, n2)) < 0.5).astype(np.int8)  # empty and trees, no fire: every cell draws
+    p, f = _tie_cells(oracle, seed, n1, n2, u0, 0)
+    assert 0 < p < 1 and 0 < f < 1
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, n1, n2, nbhd=oracle.VON_NEUMANN, seed=seed,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    want = oracle.run_array(P, u0, 0, 1, (p, f))
+    prob = ca.CAProblem.new(ca.ForestFire(), u0, 4, {"p": p, "f": f}, space=ca.Grid(n1, n2), seed=seed)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    ca.advance(B, st, prob, ca.Synchronous(), prob.p, 0)
+    assert np.array_equal(ca.current_state(B, st), want)
+    for t in range(1, 4):
+        ca.advance(B, st, prob, ca.Synchronous(), prob.p, t)
+    assert np.array_equal(ca.current_state(B, st), oracle.run_array(P, want, 1, 3, (p, f)))
+    st.close()
+    # the batched engine: the same lattice as a large instance (multi-lattice passes) and as a
+    # small one (the persistent kernel), beside a second instance
+    small = u0[:90, :70].copy()
+    ps, fs = _tie_cells(oracle, seed + 1, 90, 70, small, 0)
+    Ps = oracle.Problem(oracle.RULE_FOREST_FIRE, 90, 70, nbhd=oracle.VON_NEUMANN, seed=seed + 1,
+                        boundary=(oracle.CONSTANT, oracle.CONSTANT))
+    probs = [prob, ca.CAProblem.new(ca.ForestFire(), small, 4, {"p": ps, "f": fs}, space=ca.Grid(90, 70),
+                                    seed=seed + 1)]
+    for min_cells in (1 << 14, 1 << 30):
+        ens = ca.BatchedEnsemble(probs)
+        ens.set_large(min_cells, 1)
+        ens.set_initial_states()
+        ens.run(t0=[0, 0], nsteps=[1, 1])
+        assert np.array_equal(ens.state(0), want)
+        assert np.array_equal(ens.state(1), oracle.run_array(Ps, small, 0, 1, (ps, fs)))
+        ens.close()
+
+
+def test_fire_threshold_ties_float32(ca, oracle):
+    """Float32 parameters: p equal to a draw's 24-bit value (r1 >> 8) * 2^-24 (random.jl:109-114,
+    130), for a draw whose word 1 has a zero low byte: no hit, as the reference's compare gives."""
+    n1, n2, seed = 300, 200, 21
+    u0 = np.zeros((n1, n2), np.int8)
+    cand = [q for q in range(n1 * n2) if oracle.philox4x32((q + 1, 0, 0, 1), (seed, 0))[0] & 0xFF == 0]
+    assert cand
+    r1 = oracle.philox4x32((cand[0] + 1, 0, 0, 1), (seed, 0))[0]
+    p = np.float32((r1 >> 8) / 2.0**24)
+    assert float(p) * 2**24 == r1 >> 8
+    P = oracle.Problem(oracle.RULE_FOREST_FIRE, n1, n2, nbhd=oracle.VON_NEUMANN, seed=seed,
+                       boundary=(oracle.CONSTANT, oracle.CONSTANT), params_f32=True)
+    want = oracle.run_array(P, u0, 0, 2, (float(p), 1e-3))
+    prob = ca.CAProblem.new(ca.ForestFire(float32=True), u0, 2, {"p": float(p), "f": 1e-3}, space=ca.Grid(n1, n2),
+                            seed=seed)
+    B = ca.GB300Backend()
+    st = ca.allocate_state(B, prob, ca.Synchronous())
+    for t in range(2):
+        ca.advance(B, st, prob, ca.Synchronous(), prob.p, t)
+    assert np.array_equal(ca.current_state(B, st), want)
+    st.close()

@@ -54,7 +54,7 @@ def test_update_cell_over_every_cell_is_one_synchronous_step(gbca, oracle):
         assert np.array_equal(stepped, states[t + 1]), t
         assert not np.array_equal(states[t + 1], states[t])
     assert ca.update_cell(prob, u0, (2, 5), 0) == u0[1, 4]  # masked: unchanged
-    k = 7 + 4 * n1  # the linear index of (8, 5)
+    k = 8 + 4 * n1  # the 1-based linear index of (8, 5)
     assert ca.update_cell(prob, u0, k, 0) == ca.update_cell(prob, u0, (8, 5), 0)
     assert ca.update_cell(prob, u0, (8, 5), 0, {"p": 0.3, "f": 0.05}) == states[1][7, 4]
 

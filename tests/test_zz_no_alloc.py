@@ -6,7 +6,7 @@ caller's own device buffer must give exactly what the allocating entry points
 what the oracle gives; Int8 results are compared bit for bit, the tolerance of every Int8
 parity test here. The cases reach every branch of the sweep dispatch the entry point uses:
 the forest-fire kernel (plain and gated), the bit-sliced kernel, and the general kernel
-(Generations with more than four states, a pitch that is not a multiple of 16, Checkerboard
+(Generations with more than eight states, a pitch that is not a multiple of 16, Checkerboard
 Life on an unscanned state), plus a state of exactly the scratch array's size. Oversized and
 misaligned states are refused. The file sorts last so that a run stopping at its first
 failure has run every other test first; it also passes alone in a fresh process."""
@@ -71,7 +71,7 @@ CASES = [
      "stoch", None, 7, None),
     ("Life, Checkerboard, odd steps", lambda ca: ca.Life(), lambda ca: ca.Torus(96, 64), "check", None, 7, None),
     ("Life, pitch not a multiple of 16", lambda ca: ca.Life(), lambda ca: ca.Torus(100, 70), "sync", None, 6, 100),
-    ("Generations C = 6, reflecting", lambda ca: ca.Generations("B2/S34/C6"),
+    ("Generations C = 10, reflecting", lambda ca: ca.Generations("B2/S34/C10"),
      lambda ca: ca.Lattice((70, 50), (ca.Reflecting(), ca.Reflecting())), "sync", None, 5, None),
 ]
 
