@@ -4,7 +4,7 @@ The compute path is libgbca.so (hand-written sm_103a CUDA, C ABI in include/gbca
 this package is the host-side mirror of the reference's interface over it:
 model types (spaces, neighbourhoods, rules, schemes), the backend contract
 (GB300Backend and its functions) and the SciML-style problem / solve layer."""
-from . import backend, capi, ensemble, errors, model, problem, serving
+from . import backend, capi, ensemble, errors, model, problem, serving, slabs
 from .backend import (GB300Backend, GB300State, advance, allocate_state, check_problem, current_state,
                       device_summaries, read_cell, set_geometry, set_state, supports, tune, update_cell,
                       write_cell)

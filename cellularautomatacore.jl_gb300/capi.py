@@ -68,6 +68,8 @@ SIGNATURES = {
     "gbca_sync": (ctypes.c_int, [_V]),
     "gbca_summaries": (ctypes.c_int, [_V, _P(_I64), ctypes.c_int32, _P(_I64), _P(ctypes.c_double)]),
     "gbca_device_state": (ctypes.c_int, [_V, _P(_V), _P(_I64)]),
+    "gbca_set_slab": (ctypes.c_int, [_V, _I64, _I64]),
+    "gbca_slab_sums": (ctypes.c_int, [_V, _I64, _I64, _P(_I64)]),
     "gbca_set_stream": (ctypes.c_int, [_V, _V]),
     "gbca_kernel_launches": (ctypes.c_int64, []),
     "gbca_tune": (ctypes.c_int, [_V, _P(ctypes.c_double), ctypes.c_int32, _P(ctypes.c_int32), _P(ctypes.c_int32),

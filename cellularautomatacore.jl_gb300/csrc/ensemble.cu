@@ -403,6 +403,8 @@ __global__ void __launch_bounds__(kEnsThreads) k_ensemble(const EnsInstance* __r
                 g.cst1 = (uint32_t)(uint8_t)I.cval1 * 0x01010101u;
                 fire_thresholds(I.thr_p, I.thr_f, I.params_f32 != 0, g);
                 g.exact_always = fire_odd_constant(I.bnd0, I.cval0, I.bnd1, I.cval1);
+                g.col0 = 0;
+                g.n2g = I.n2;
                 if (I.small) run_in_smem_fire(I, pool, sA, sB, K, g);
                 else cur = run_tiled_fire<TILE>(I, pool, sA, sB, K, g);
             } else if (I.small) {

@@ -24,7 +24,17 @@ struct FireGeom {
     uint64_t Ua, dU;
     uint32_t allp, allf;   // 0x01010101 if p >= 1 (resp. f >= 1: every draw hits), else 0
     bool exact_always;     // a Constant edge holds a value other than 0, 1, 2
+    int64_t col0, n2g;     // the lattice as a slab of a larger one (SweepParams::col0, n2g)
 };
+
+// The global column of local lattice column my (0 <= my < n2): the column of its cells' ids
+// and Checkerboard parities.
+__device__ __forceinline__ int64_t fire_gcol(const FireGeom& g, int64_t my) {
+    int64_t c = my + g.col0;
+    if (c < 0) c += g.n2g;
+    else if (c >= g.n2g) c -= g.n2g;
+    return c;
+}
 
 // Whether a Constant edge value is one the bit tests cannot read (anything but 0, 1, 2).
 __host__ __device__ inline bool fire_odd_constant(int32_t b0, int32_t c0, int32_t b1, int32_t c1) {
@@ -150,7 +160,8 @@ __device__ __forceinline__ void fire_substep_words_t(const uint32_t* __restrict_
 #pragma unroll
             for (int b = 0; b < 4; ++b) mx[b] = (uint32_t)gx + b;
         }
-        uint32_t res = fire_next(E, T, N, my * n1 + 1u, mx, g, ds, K);
+        const uint32_t gc = (uint32_t)fire_gcol(g, rowout ? 0 : (int64_t)my);
+        uint32_t res = fire_next(E, T, N, gc * n1 + 1u, mx, g, ds, K);
         if (MAPPED) {
             if (rowout) res = g.cst1;
             else res = (res & ~outmask) | (g.cst0 & outmask);
@@ -219,10 +230,11 @@ __device__ __forceinline__ void fire_substep_rows_t(const uint32_t* __restrict__
     int o = r0 * sw + lw;
     uint32_t Up = A[o - sw], C = A[o];
     int64_t gy = gy0 + r0;
-    uint32_t base = (uint32_t)gy * n1 + 1u;  // id of the row's cell 0
+    int64_t gg = fire_gcol(g, gy);            // the row's global column
+    uint32_t base = (uint32_t)gg * n1 + 1u;  // id of the row's cell 0
     int8_t* q = gdst + gx + gy * gpitch;
     const int64_t xin = g.n1 - gx;  // cells of this word inside the lattice (>= 1)
-    for (int ly = r0; ly < r1; ++ly, o += sw, q += gpitch, base += n1, ++gy) {
+    for (int ly = r0; ly < r1; ++ly, o += sw, q += gpitch, ++gy) {
         const uint32_t Dn = A[o + sw], Wl = A[o - 1], Wr = A[o + 1];
         const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
         const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
@@ -232,7 +244,7 @@ __device__ __forceinline__ void fire_substep_rows_t(const uint32_t* __restrict__
         if constexpr (GATED) {  // open bytes take the rule's state, closed and masked ones keep theirs
             uint32_t Gb = 0xFFFFFFFFu;
             if (fg->mode == 1) {
-                Gb = ((gy + fg->gate) & 1) ? 0xFF00FF00u : 0x00FF00FFu;  // gx is even
+                Gb = ((gg + fg->gate) & 1) ? 0xFF00FF00u : 0x00FF00FFu;  // gx is even
             } else if (fg->mode == 2 && !fg->allg) {
                 Gb = 0u;
 #pragma unroll
@@ -251,6 +263,12 @@ __device__ __forceinline__ void fire_substep_rows_t(const uint32_t* __restrict__
         }
         Up = C;
         C = Dn;
+        if (++gg == g.n2g) {  // the next row's global column wraps to 0
+            gg = 0;
+            base = 1u;
+        } else {
+            base += n1;
+        }
     }
 }
 

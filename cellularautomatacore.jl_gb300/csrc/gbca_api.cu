@@ -54,6 +54,9 @@ struct gbca_handle {
     bool sparse_on = false;
     bool sparse_dirty = true;  // the state changed outside a sweep: flags and buffers to rebuild
     gbca::SparseTiles sparse = {};
+    // the lattice as a slab of a larger one (gbca_set_slab)
+    bool slab_on = false;
+    gbca::SlabPlace slab = {0, 0};
 };
 
 namespace {
@@ -263,7 +266,8 @@ int advance_int8(gbca_handle* h, int64_t t, int64_t nsteps, const double* params
     }
     const cudaError_t e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, t, nsteps, params, h->stream,
                                            scanned_rule(h) && h->states_valid, h->forced ? &h->force : nullptr,
-                                           h->mask, h->sparse_on ? &h->sparse : nullptr);
+                                           h->mask, h->sparse_on ? &h->sparse : nullptr,
+                                           h->slab_on ? &h->slab : nullptr);
     // a synchronous, unmasked step leaves only 0, 1 and 2; a closed or masked cell keeps its value
     if (h->d.rule == GBCA_RULE_FOREST_FIRE && h->d.scheme == GBCA_SYNCHRONOUS && !h->mask) h->states_valid = true;
     if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
@@ -275,6 +279,10 @@ gbca::SweepParams handle_params(const gbca_handle* h, const double* params) {
     gbca::SweepParams p = gbca::sweep_params(h->d, h->pitch, params);
     p.states_valid = scanned_rule(h) && h->states_valid ? 1 : 0;
     p.mask = h->mask;
+    if (h->slab_on) {
+        p.col0 = h->slab.col0;
+        p.n2g = h->slab.n2g;
+    }
     return p;
 }
 
@@ -304,7 +312,7 @@ int time_candidates(gbca_handle* h, const std::vector<gbca::SweepChoice>& cands,
             if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
             if (e == cudaSuccess)
                 e = gbca::sweep_int8(h->d, h->pitch, bufs, &h->cur, 1, nsteps, params, h->stream, valid, &cands[c],
-                                     h->mask);
+                                     h->mask, nullptr, h->slab_on ? &h->slab : nullptr);
             if (e == cudaSuccess) e = cudaEventRecord(ev[1], h->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
             float ms = 0.0f;
@@ -711,6 +719,7 @@ int gbca_set_sparse(gbca_handle* h, int32_t enable, int32_t background, int32_t 
         return fail(GBCA_ERR_ARGUMENT, "active-tile sweeps run rules without kernel fields (Life, Generations, forest fire)");
     if (h->d.scheme == GBCA_CHECKERBOARD)
         return fail(GBCA_ERR_UNSUPPORTED, "active-tile sweeps run Synchronous() and Stochastic(p)");
+    if (h->slab_on) return fail(GBCA_ERR_UNSUPPORTED, "a slab of a larger lattice runs dense sweeps only");
     if (background < -128 || background > 127) return fail(GBCA_ERR_ARGUMENT, "the background must be an Int8 value");
     if (tilesize <= 0) tilesize = 64;
     if (tilesize < 8 || tilesize > 128)
@@ -828,6 +837,41 @@ int gbca_set_stream(gbca_handle* h, void* stream) {
 }
 
 int64_t gbca_kernel_launches(void) { return gbca::launches_so_far(); }
+
+int gbca_set_slab(gbca_handle* h, int64_t col0, int64_t n2_global) {
+    if (!h) return fail(GBCA_ERR_ARGUMENT, "null handle");
+    if (h->d.rule == GBCA_RULE_LENIA || h->d.rule == GBCA_RULE_SI_FIELD)
+        return fail(GBCA_ERR_UNSUPPORTED, "slabs run rules without kernel fields (Life, Generations, forest fire)");
+    if (h->sparse_on) return fail(GBCA_ERR_UNSUPPORTED, "a slab of a larger lattice runs dense sweeps only");
+    if (n2_global < h->d.n2)
+        return fail(GBCA_ERR_ARGUMENT, "the larger lattice (%lld columns) must hold the slab's %lld",
+                    (long long)n2_global, (long long)h->d.n2);
+    if (col0 <= -n2_global || col0 >= n2_global)
+        return fail(GBCA_ERR_ARGUMENT, "the slab's first column %lld must lie in (-%lld, %lld)", (long long)col0,
+                    (long long)n2_global, (long long)n2_global);
+    if (h->d.n1 > INT64_MAX / n2_global) return fail(GBCA_ERR_ARGUMENT, "the larger lattice is too large");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "set_slab");
+    h->slab_on = !(col0 == 0 && n2_global == h->d.n2);
+    h->slab = gbca::SlabPlace{col0, n2_global};
+    return GBCA_OK;
+}
+
+int gbca_slab_sums(gbca_handle* h, int64_t j_lo, int64_t j_hi, int64_t* sums) {
+    if (!h || !sums) return fail(GBCA_ERR_ARGUMENT, "null handle or output");
+    if (h->d.rule == GBCA_RULE_LENIA) return fail(GBCA_ERR_UNSUPPORTED, "summaries need an Int8 state");
+    if (j_lo < 0 || j_hi > h->d.n2 || j_lo > j_hi)
+        return fail(GBCA_ERR_ARGUMENT, "columns %lld:%lld lie outside 0:%lld", (long long)j_lo, (long long)j_hi,
+                    (long long)h->d.n2);
+    GBCA_CUDA(gbca::launch_measures((const int8_t*)h->buf[h->cur], h->d.n1, h->d.n2, h->pitch, h->d.boundary[0],
+                                    h->d.boundary[1], h->acc, h->nsm, h->stream, j_lo, j_hi),
+              "slab sums launch");
+    GBCA_CUDA(cudaMemcpyAsync(h->acc_host, h->acc, gbca::kMeasureWords * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, h->stream),
+              "slab sums copy");
+    GBCA_CUDA(cudaStreamSynchronize(h->stream), "slab sums");
+    for (int k = 0; k < gbca::kMeasureWords; ++k) sums[k] = (int64_t)h->acc_host[k];
+    return GBCA_OK;
+}
 
 int gbca_device_state(gbca_handle* h, void** dptr, int64_t* pitch) {
     if (!h || !dptr) return fail(GBCA_ERR_ARGUMENT, "null handle or output");

@@ -189,6 +189,24 @@ struct SweepParams {
     uint8_t* flags_out;
     int32_t tiles_x;
     int32_t background;
+    // the lattice as a slab of a larger one (gbca_set_slab): local column j is global column
+    // (j + col0) mod n2g, whose cell ids and Checkerboard parities the sweep uses. col0 = 0 and
+    // n2g = n2 for a lattice of its own.
+    int64_t col0, n2g;
+};
+
+// The global column of mapped local column `my` (0 <= my < n2): one wrap at most, since
+// |col0| < n2g and n2 <= n2g.
+__host__ __device__ __forceinline__ int64_t global_col(const SweepParams& p, int64_t my) {
+    int64_t g = my + p.col0;
+    if (g < 0) g += p.n2g;
+    else if (g >= p.n2g) g -= p.n2g;
+    return g;
+}
+
+// Where a lattice lies in a larger one along axis 2 (gbca_set_slab).
+struct SlabPlace {
+    int64_t col0, n2g;
 };
 
 // Active-tile scheduling state of a handle (sweep_sparse.cu): only tiles holding a cell
@@ -238,7 +256,7 @@ struct SweepChoice {
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
                        const double* params, cudaStream_t st, bool states_valid = false,
                        const SweepChoice* force = nullptr, const uint8_t* mask = nullptr,
-                       const SparseTiles* sparse = nullptr);
+                       const SparseTiles* sparse = nullptr, const SlabPlace* slab = nullptr);
 
 // Active-tile scheduling (sweep_sparse.cu).
 cudaError_t launch_candidates(const SweepParams& p, const SparseTiles& sp, int cur, int halo, cudaStream_t st);

@@ -85,8 +85,9 @@ __device__ __forceinline__ uint32_t stochastic_gate(const SweepParams& p, const 
     uint32_t G = 0;
     const int64_t my = map_near(p.bnd[1], y, p.n2);
     if (my < 0) return 0u;
+    const int64_t gy = global_col(p, my);  // the row's global column: its cells' ids
     if (gx >= 0 && gx + 32 <= p.n1) {
-        const uint32_t base = (uint32_t)(gx + my * p.n1) + 1u;
+        const uint32_t base = (uint32_t)(gx + gy * p.n1) + 1u;
 #pragma unroll 4
         for (int b = 0; b < 32; ++b)
             G |= (uint32_t)draw_below(draw_fast(ds, p.keys, base + (uint32_t)b, 0u), p.gate_thr, p.gate_f32 != 0) << b;
@@ -96,7 +97,7 @@ __device__ __forceinline__ uint32_t stochastic_gate(const SweepParams& p, const 
         int64_t m = gx % p.n1;
         if (m < 0) m += p.n1;
         uint32_t mx = (uint32_t)m;
-        const uint32_t row = (uint32_t)(my * p.n1) + 1u, n1 = (uint32_t)p.n1;
+        const uint32_t row = (uint32_t)(gy * p.n1) + 1u, n1 = (uint32_t)p.n1;
 #pragma unroll 4
         for (int b = 0; b < 32; ++b) {
             G |= (uint32_t)draw_below(draw_fast(ds, p.keys, row + mx, 0u), p.gate_thr, p.gate_f32 != 0) << b;
@@ -107,7 +108,7 @@ __device__ __forceinline__ uint32_t stochastic_gate(const SweepParams& p, const 
     for (int b = 0; b < 32; ++b) {
         const int64_t mx = map_near(p.bnd[0], gx + b, p.n1);
         if (mx < 0) continue;
-        const uint32_t id = (uint32_t)(mx + my * p.n1) + 1u;
+        const uint32_t id = (uint32_t)(mx + gy * p.n1) + 1u;
         G |= (uint32_t)draw_below(draw_fast(ds, p.keys, id, 0u), p.gate_thr, p.gate_f32 != 0) << b;
     }
     return G;
@@ -149,13 +150,15 @@ __device__ __noinline__ uint32_t checker_gate_exact(int32_t b0, int64_t n1, int6
 }
 
 // rows_plain: every row images a row of its own parity or lies beyond a Constant edge (axis 2
-// Constant, or Periodic of even length), so a row's parity is its own and needs no mapping.
+// Constant, or Periodic of even length), so a row's parity is its own and needs no mapping
+// (a lattice of its own only: a slab's rows take their global columns' parities).
 __device__ __forceinline__ uint32_t checker_gate(const SweepParams& p, const CheckerCol& c, bool rows_plain,
                                                  int64_t gx, int64_t y, int gate) {
     int64_t my = y;
     if (!rows_plain) {
         my = map_near(p.bnd[1], y, p.n2);
         if (my < 0) return 0u;
+        my = global_col(p, my);  // parity of the global column (a slab of a larger lattice)
     }
     if (c.exact) return checker_gate_exact(p.bnd[0], p.n1, gx, my, gate);
     const uint32_t base = ((my + gate) & 1) ? 0xAAAAAAAAu : 0x55555555u;  // gx is even
@@ -635,7 +638,8 @@ __global__ void __launch_bounds__(kLifeThreads) k_life(SweepParams p, LifeGeom g
     LifeGate gt;  // a gated scheme's sub-step gate (the synchronous kernel has none)
     gt.mode = 0;
     gt.gate = 0;
-    gt.rows_plain = p.bnd[1] == GBCA_CONSTANT || (p.bnd[1] == GBCA_PERIODIC && (p.n2 & 1) == 0);
+    gt.rows_plain = (p.col0 == 0 && p.n2g == p.n2) &&
+                    (p.bnd[1] == GBCA_CONSTANT || (p.bnd[1] == GBCA_PERIODIC && (p.n2 & 1) == 0));
     gt.X0 = X0;
     gt.Y0 = Y0;
     if constexpr (GATED) gt.mode = p.scheme == GBCA_CHECKERBOARD ? 1 : (p.scheme == GBCA_STOCHASTIC ? 2 : 0);

@@ -18,7 +18,7 @@ namespace gbca {
 namespace {
 
 __global__ void __launch_bounds__(256) k_measures(const int8_t* __restrict__ u, int64_t n1, int64_t n2,
-                                                  int64_t pitch, int32_t b1, int32_t b2,
+                                                  int64_t pitch, int32_t b1, int32_t b2, int64_t j_lo, int64_t j_hi,
                                                   unsigned long long* __restrict__ acc) {
     __shared__ unsigned int hist[256];
     __shared__ long long sums[5];
@@ -26,9 +26,9 @@ __global__ void __launch_bounds__(256) k_measures(const int8_t* __restrict__ u, 
     if (threadIdx.x < 5) sums[threadIdx.x] = 0;
     __syncthreads();
     long long S = 0, S2 = 0, P = 0, Q = 0, W = 0;
-    const int64_t n = n1 * n2;
+    const int64_t n = n1 * (j_hi - j_lo);  // the cells of columns j_lo .. j_hi - 1
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = k % n1, j = k / n1;
+        const int64_t i = k % n1, j = j_lo + k / n1;
         const int x = u[i + j * pitch];
         atomicAdd(&hist[x + 128], 1u);
         S += x;
@@ -90,15 +90,16 @@ cudaError_t launch_soup(int8_t* buf, int64_t n1, int64_t n2, int64_t pitch, doub
 }
 
 cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t b1, int32_t b2,
-                            unsigned long long* acc, int nsm, cudaStream_t st) {
+                            unsigned long long* acc, int nsm, cudaStream_t st, int64_t j_lo, int64_t j_hi) {
     cudaError_t e = cudaMemsetAsync(acc, 0, kMeasureWords * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    const int64_t n = n1 * n2;
+    if (j_hi < 0) j_hi = n2;
+    const int64_t n = n1 * (j_hi - j_lo);
     int64_t blocks = (n + 255) / 256;
     const int64_t cap = (int64_t)nsm * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    k_measures<<<(unsigned)blocks, 256, 0, st>>>(u, n1, n2, pitch, b1, b2, acc);
+    k_measures<<<(unsigned)blocks, 256, 0, st>>>(u, n1, n2, pitch, b1, b2, j_lo, j_hi, acc);
     count_launch();
     return cudaGetLastError();
 }

@@ -14,8 +14,10 @@ constexpr int kMeasureWords = 261;
 cudaError_t launch_soup(int8_t* buf, int64_t n1, int64_t n2, int64_t pitch, double density, uint64_t seed, int grid,
                         cudaStream_t st);
 
+// The sums over the cells of columns j_lo .. j_hi - 1 (j_hi < 0: through column n2 - 1), their
+// neighbours read through the lattice's boundaries: a slab's share of a larger lattice's sums.
 cudaError_t launch_measures(const int8_t* u, int64_t n1, int64_t n2, int64_t pitch, int32_t b1, int32_t b2,
-                            unsigned long long* acc, int nsm, cudaStream_t st);
+                            unsigned long long* acc, int nsm, cudaStream_t st, int64_t j_lo = 0, int64_t j_hi = -1);
 
 // *bad = 0 when every cell of the state lies in 0 .. nv - 1 (nv in 1..255), else nonzero.
 // Needs a 16-byte-aligned buffer and pitch; the bytes between n1 and the pitch are not read

@@ -30,6 +30,8 @@ SweepParams sweep_params(const gbca_desc& d, int64_t pitch, const double* params
     p.gate_thr = d.scheme == GBCA_STOCHASTIC ? gbca_threshold(d.scheme_p, d.scheme_p_f32) : 0;
     p.params_f32 = d.params_f32;
     p.ngates = d.scheme == GBCA_CHECKERBOARD ? 2 : 1;
+    p.col0 = 0;
+    p.n2g = d.n2;
     if (d.rule == GBCA_RULE_FOREST_FIRE && params) {
         p.thr_p = gbca_threshold(params[0], d.params_f32);
         p.thr_f = gbca_threshold(params[1], d.params_f32);
@@ -71,8 +73,12 @@ cudaError_t fire_gated_step(SweepParams& p, int8_t* const bufs[2], int* cur, int
 
 cudaError_t sweep_int8(const gbca_desc& d, int64_t pitch, int8_t* const bufs[2], int* cur, int64_t t, int64_t nsteps,
                        const double* params, cudaStream_t st, bool states_valid, const SweepChoice* force,
-                       const uint8_t* mask, const SparseTiles* sparse) {
+                       const uint8_t* mask, const SparseTiles* sparse, const SlabPlace* slab) {
     SweepParams p = sweep_params(d, pitch, params);
+    if (slab) {
+        p.col0 = slab->col0;
+        p.n2g = slab->n2g;
+    }
     p.states_valid = states_valid ? 1 : 0;
     p.mask = mask;
     if (sparse) {  // active tiles only: the bit-sliced kernel where it applies, else the general one

@@ -173,6 +173,8 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
     g.cst1 = (uint32_t)(uint8_t)p.cval[1] * 0x01010101u;
     fire_thresholds(p.thr_p, p.thr_f, p.params_f32 != 0, g);
     g.exact_always = fire_odd_constant(p.bnd[0], p.cval[0], p.bnd[1], p.cval[1]);
+    g.col0 = p.col0;
+    g.n2g = p.n2g;
     for (int s = 0; s < p.nsub; ++s) {
         const DrawStep ds = draw_step(p.keys, p.t0 + s);
         const int ex = p.nsub - 1 - s;
@@ -327,6 +329,8 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
     g.cst1 = (uint32_t)(uint8_t)p.cval[1] * 0x01010101u;
     fire_thresholds(p.thr_p, p.thr_f, p.params_f32 != 0, g);
     g.exact_always = fire_odd_constant(p.bnd[0], p.cval[0], p.bnd[1], p.cval[1]);
+    g.col0 = p.col0;
+    g.n2g = p.n2g;
     const DrawStep ds = draw_step(p.keys, p.t0);
     FireGate fg;  // a gated or masked sweep: one sub-step, half p.sub0
     if constexpr (GATED) fire_gate(p.scheme, p.sub0 % p.ngates, p.gate_thr, p.gate_f32, p.mask, p.pitch, fg);
@@ -503,7 +507,7 @@ bool fire_fast_supported(const SweepParams& p) {
     // every scheme and masks: a gated or masked sweep runs one sub-step per launch (fire_gated)
     return p.rule == GBCA_RULE_FOREST_FIRE && p.nbhd == GBCA_VON_NEUMANN && p.radius == 1 &&
            (p.scheme == GBCA_SYNCHRONOUS || p.scheme == GBCA_STOCHASTIC || p.scheme == GBCA_CHECKERBOARD) &&
-           p.n1 * p.n2 < ((int64_t)1 << 32) - 1 && p.pitch % 16 == 0;
+           p.n1 * p.n2g < ((int64_t)1 << 32) - 1 && p.pitch % 16 == 0;
 }
 
 bool fire_gated(const SweepParams& p) { return p.scheme != GBCA_SYNCHRONOUS || p.mask != nullptr; }

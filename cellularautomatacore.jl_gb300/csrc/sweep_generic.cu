@@ -134,12 +134,13 @@ __global__ void __launch_bounds__(256) k_generic(SweepParams p, const int8_t* __
                 B[ly * sx + lx] = c;
                 continue;
             }
-            const uint64_t id = (uint64_t)mx + (uint64_t)my * (uint64_t)p.n1 + 1u;
+            const int64_t gc = global_col(p, my);  // the global column: ids and parities
+            const uint64_t id = (uint64_t)mx + (uint64_t)gc * (uint64_t)p.n1 + 1u;
             bool open = true;  // src/schemes.jl:84-89
             if (p.scheme == GBCA_STOCHASTIC)
                 open = draw_below(cell_draw(p.seed, id, t, 0), p.gate_thr, p.gate_f32);
             else if (p.scheme == GBCA_CHECKERBOARD)
-                open = (((mx + my + 2) & 1) == (gate == 1 ? 1 : 0));
+                open = (((mx + gc + 2) & 1) == (gate == 1 ? 1 : 0));
             B[ly * sx + lx] = open ? generic_rule<RC>(p, A, sx, lx, ly, c, id, t) : c;
         }
         __syncthreads();

@@ -108,7 +108,7 @@ bool life_simd_supported(const SweepParams& p) {
     if (p.scheme == GBCA_CHECKERBOARD) {
         // any boundary: the gate maps halo cells to the cells they image (checker_gate)
     } else if (p.scheme == GBCA_STOCHASTIC) {
-        if (p.n1 * p.n2 >= ((int64_t)1 << 32) - 1) return false;  // gate ids in the draws' 32-bit form
+        if (p.n1 * p.n2g >= ((int64_t)1 << 32) - 1) return false;  // gate ids in the draws' 32-bit form
     } else if (p.scheme != GBCA_SYNCHRONOUS) {
         return false;
     }

@@ -196,6 +196,25 @@ int gbca_summaries(gbca_handle* h, int64_t* counts, int32_t nvals, int64_t* othe
  * valid until the next gbca_advance / gbca_destroy. For callers that keep inputs in HBM. */
 int gbca_device_state(gbca_handle* h, void** dptr, int64_t* pitch);
 
+/* The handle's lattice (n1 x n2) as columns col0 .. col0 + n2 - 1, taken modulo n2_global, of a
+ * lattice of n1 x n2_global cells: the slab one rank holds when the single sweep is split along
+ * its last axis, as ArrayBackend's threads split it (src/backends.jl:457-479). Cell ids (hence
+ * every draw, random.jl:102-107) and Checkerboard parities (schemes.jl:89) become the larger
+ * lattice's; neighbours are still read from the handle's own lattice through its boundaries, so
+ * a caller that pads the slab with h = r x steps x gates columns on each side the larger lattice
+ * continues and refreshes them every `steps` steps gets exact owned columns. col0 = 0 with
+ * n2_global = n2 restores a lattice of its own. Int8 rules only (Life, Generations, forest fire),
+ * dense sweeps only (no gbca_set_sparse); needs -n2_global < col0 < n2_global. */
+int gbca_set_slab(gbca_handle* h, int64_t col0, int64_t n2_global);
+
+/* The exact integer sums behind state_counts and Moran's I (src/measures.jl:14-20,91-107) over
+ * the cells of columns j_lo .. j_hi - 1 of the current state, neighbours read through the
+ * handle's boundaries: sums[0..255] count the values -128..127, then S = sum x, S2 = sum x^2,
+ * P = sum over VonNeumann(1) neighbour pairs of x_i x_j, Q = sum over pairs of x_i + x_j, and
+ * W = the number of pairs (261 values). Slabs' sums add up to the whole lattice's, from which
+ * Moran's I = (n^2 P - n S Q + W S^2) / (W (n S2 - S^2)). */
+int gbca_slab_sums(gbca_handle* h, int64_t j_lo, int64_t j_hi, int64_t* sums);
+
 /* Run the handle's work on `stream` (a cudaStream_t; NULL restores the handle's own
  * stream) from the next call on, after waiting for what was queued before. Lets a caller
  * order the sweep with its own work and time it with events on the same stream.
