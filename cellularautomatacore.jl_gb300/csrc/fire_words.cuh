@@ -234,41 +234,43 @@ __device__ __forceinline__ void fire_substep_rows_t(const uint32_t* __restrict__
     uint32_t base = (uint32_t)gg * n1 + 1u;  // id of the row's cell 0
     int8_t* q = gdst + gx + gy * gpitch;
     const int64_t xin = g.n1 - gx;  // cells of this word inside the lattice (>= 1)
-    for (int ly = r0; ly < r1; ++ly, o += sw, q += gpitch, ++gy) {
-        const uint32_t Dn = A[o + sw], Wl = A[o - 1], Wr = A[o + 1];
-        const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
-        const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
-        uint32_t E, T, N;
-        fire_masks<EXACT>(C, Lf, Rt, Up, Dn, E, T, N);
-        uint32_t res = fire_next(E, T, N, base, mx, g, ds, K);
-        if constexpr (GATED) {  // open bytes take the rule's state, closed and masked ones keep theirs
-            uint32_t Gb = 0xFFFFFFFFu;
-            if (fg->mode == 1) {
-                Gb = ((gg + fg->gate) & 1) ? 0xFF00FF00u : 0x00FF00FFu;  // gx is even
-            } else if (fg->mode == 2 && !fg->allg) {
-                Gb = 0u;
+    int ly = r0;
+    while (ly < r1) {
+        // the rows before the global column wraps to 0 (all of them but on a slab of a torus whose
+        // halo crosses the lattice's edge), ids stepped by n1 a row
+        const int seg_end = (int64_t)(r1 - ly) <= g.n2g - gg ? r1 : ly + (int)(g.n2g - gg);
+        for (; ly < seg_end; ++ly, o += sw, q += gpitch, ++gy, ++gg, base += n1) {
+            const uint32_t Dn = A[o + sw], Wl = A[o - 1], Wr = A[o + 1];
+            const uint32_t Lf = __funnelshift_l(Wl, C, 8);  // byte b = cell x - 1
+            const uint32_t Rt = __funnelshift_r(C, Wr, 8);  // byte b = cell x + 1
+            uint32_t E, T, N;
+            fire_masks<EXACT>(C, Lf, Rt, Up, Dn, E, T, N);
+            uint32_t res = fire_next(E, T, N, base, mx, g, ds, K);
+            if constexpr (GATED) {  // open bytes take the rule's state, closed and masked ones keep theirs
+                uint32_t Gb = 0xFFFFFFFFu;
+                if (fg->mode == 1) {
+                    Gb = ((gg + fg->gate) & 1) ? 0xFF00FF00u : 0x00FF00FFu;  // gx is even
+                } else if (fg->mode == 2 && !fg->allg) {
+                    Gb = 0u;
 #pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const uint2 w = draw_fast(ds, K, base + mx[b], 0u);
-                    if ((((uint64_t)w.x << 32) | (uint64_t)w.y) < fg->Ug) Gb |= 0xFFu << (8 * b);
+                    for (int b = 0; b < 4; ++b) {
+                        const uint2 w = draw_fast(ds, K, base + mx[b], 0u);
+                        if ((((uint64_t)w.x << 32) | (uint64_t)w.y) < fg->Ug) Gb |= 0xFFu << (8 * b);
+                    }
                 }
+                if (fg->mask) Gb &= bytes_nonzero(*(const uint32_t*)(fg->mask + gx + gy * fg->mpitch));
+                res = (res & Gb) | (C & ~Gb);
             }
-            if (fg->mask) Gb &= bytes_nonzero(*(const uint32_t*)(fg->mask + gx + gy * fg->mpitch));
-            res = (res & Gb) | (C & ~Gb);
+            if (!CHECKED || xin >= 4) {
+                *(uint32_t*)q = res;
+            } else {
+                for (int b = 0; b < xin; ++b) q[b] = (int8_t)(res >> (8 * b));
+            }
+            Up = C;
+            C = Dn;
         }
-        if (!CHECKED || xin >= 4) {
-            *(uint32_t*)q = res;
-        } else {
-            for (int b = 0; b < xin; ++b) q[b] = (int8_t)(res >> (8 * b));
-        }
-        Up = C;
-        C = Dn;
-        if (++gg == g.n2g) {  // the next row's global column wraps to 0
-            gg = 0;
-            base = 1u;
-        } else {
-            base += n1;
-        }
+        gg = 0;  // the next row is global column 0
+        base = 1u;
     }
 }
 

@@ -16,8 +16,9 @@
 //
 // FFT field (periodic lattices, the FFTW extension's convention
 // ext/CellularAutomataCoreFFTWExt.jl:17-30): U = irfft(rfft(u) .* conj(rfft(kpad))) with
-// kpad the kernel wrapped onto the lattice. cuFFT does the transforms (a library call);
-// the spectral product and the growth/clamp are this file's kernels.
+// kpad the kernel wrapped onto the lattice. Sides that are products of 2, 3 and 5 run this
+// library's own transforms with the growth fused into the last one (spectral.cu: three launches
+// a step); other sides run cuFFT (a library call) with this file's spectral product and growth.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -26,6 +27,7 @@
 
 #include "gbca_internal.cuh"
 #include "lenia.cuh"
+#include "spectral.cuh"
 
 namespace gbca {
 
@@ -231,6 +233,7 @@ struct LeniaPlan {
     void* kspec = nullptr;  // conj(rfft(kpad)) / (n1 n2)
     void* spec = nullptr;   // work spectrum
     void* field = nullptr;  // real field, packed n1 x n2
+    SpecConv* sc = nullptr;  // this library's transforms (sides of 2, 3 and 5), else cuFFT
     int nsm = 148;
 };
 
@@ -377,7 +380,20 @@ int lenia_create(const gbca_desc& d, int64_t pitch_bytes, cudaStream_t st, Lenia
         return fail_to(err, GBCA_ERR_CUDA, cudaGetErrorString(e));
     }
 
-    if (P->fft) {
+    if (P->fft && specconv_supported(P->n1, P->n2, P->f64)) {
+        // kpad at 0-based (o mod n) per axis, each weight in the state's precision (environment.jl:63)
+        std::vector<double> kpad((size_t)(P->n1 * P->n2), 0.0);
+        for (int k = 0; k < ntaps; ++k) {
+            const int64_t a = map_axis(GBCA_PERIODIC, P->off[2 * k], P->n1);
+            const int64_t b = map_axis(GBCA_PERIODIC, P->off[2 * k + 1], P->n2);
+            kpad[(size_t)(a + b * P->n1)] += P->f64 ? P->w[k] : (double)(float)P->w[k];
+        }
+        const int rc = specconv_create(P->n1, P->n2, P->f64, kpad.data(), st, &P->sc, err);
+        if (rc != GBCA_OK) {
+            lenia_destroy(P);
+            return rc;
+        }
+    } else if (P->fft) {
         const int rc = P->f64 ? fft_setup<double>(P, st, err) : fft_setup<float>(P, st, err);
         if (rc != GBCA_OK) {
             lenia_destroy(P);
@@ -392,6 +408,7 @@ void lenia_destroy(LeniaPlan* P) {
     if (!P) return;
     if (P->fwd) cufftDestroy(P->fwd);
     if (P->inv) cufftDestroy(P->inv);
+    specconv_destroy(P->sc);
     cudaFree(P->d_off);
     cudaFree(P->d_w);
     cudaFree(P->kspec);
@@ -410,7 +427,9 @@ int advance_t(LeniaPlan* P, int64_t nsteps, cudaStream_t st, int* cur, void* con
         const T* u = (const T*)bufs[*cur];
         T* out = (T*)bufs[*cur ^ 1];
         cudaError_t e = cudaSuccess;
-        if (P->fft) {
+        if (P->sc) {
+            e = specconv_lenia_step(P->sc, u, out, P->pe, P->d.lenia_mu, P->d.lenia_sigma, P->d.lenia_dt, st);
+        } else if (P->fft) {
             const int64_t nc = P->n1 / 2 + 1;
             if (cufftSetStream(P->fwd, st) != CUFFT_SUCCESS || cufftSetStream(P->inv, st) != CUFFT_SUCCESS ||
                 F::fwd(P->fwd, u, (C*)P->spec) != CUFFT_SUCCESS)

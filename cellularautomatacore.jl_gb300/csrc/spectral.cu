@@ -1,0 +1,561 @@
+// spectral.cu — this library's FFTs for the periodic kernel fields of Lenia and KernelField
+// dispersal: U = irfft(rfft(src) .* conj(rfft(kpad))) (ext/CellularAutomataCoreFFTWExt.jl:17-30),
+// kpad the kernel's weights wrapped onto the lattice at 0-based (offset mod n) per axis.
+//
+// Three launches per field, each line of the lattice transformed inside one CTA's shared memory
+// by a mixed-radix Stockham FFT (radix 4, 2, 3, 5; self-sorting, so no bit reversal), twiddles
+// from a table computed in FP64 on the host:
+//   1. axis 1 (the contiguous axis): two real lines per CTA packed as one complex line,
+//      transformed, split into the two half spectra (n1/2 + 1 frequencies each), and written
+//      transposed, frequency-major, so that axis-2 lines are contiguous;
+//   2. axis 2, one CTA per axis-1 frequency: forward transform, product with the kernel's
+//      spectrum (conjugated, with the inverse's 1/(n1 n2) folded in), inverse transform, in place;
+//   3. axis 1 inverse, two lines per CTA: the Hermitian halves rebuilt into one complex line
+//      whose inverse transform holds the two real fields, then the epilogue (Lenia's growth and
+//      clamp, or the field stored for the kernel-field sweep).
+// The kernel's spectrum is made once by the same launches in FP64 (steps 1 and 2, forward only).
+#include <cmath>
+#include <vector>
+
+#include "gbca_internal.cuh"
+#include "spectral.cuh"
+
+namespace gbca {
+
+namespace {
+
+template <typename T> struct CxOf;
+template <> struct CxOf<float> { using type = float2; };
+template <> struct CxOf<double> { using type = double2; };
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+// a * (DIR i): DIR = +1 multiplies by i, -1 by -i
+template <int DIR, typename C> __device__ __forceinline__ C cmul_i(C a) {
+    return DIR > 0 ? C{-a.y, a.x} : C{a.y, -a.x};
+}
+
+constexpr int kMaxStages = 16;
+struct FftFactors {
+    int n, nst;
+    uint64_t code;  // stage s has radix (code >> 4 s) & 15
+    __host__ __device__ int radix(int s) const { return (int)((code >> (4 * s)) & 15u); }
+};
+
+// n as radices 8, then 4, 2, 3, 5; nst = -1 when n has another prime factor.
+FftFactors factorize(int64_t n) {
+    FftFactors f;
+    f.n = (int)n;
+    f.nst = 0;
+    f.code = 0;
+    int64_t m = n;
+    for (int r : {8, 4, 2, 3, 5})
+        while (n >= 1 && m % r == 0 && f.nst < kMaxStages) {
+            f.code |= (uint64_t)r << (4 * f.nst++);
+            m /= r;
+        }
+    if (m != 1 || n < 1) f.nst = -1;
+    return f;
+}
+
+// Threads that transform one n-point line: at most 8 points each.
+__host__ __device__ inline int line_threads(int n) {
+    const int t = (n + 7) / 8;
+    return t < 32 ? 32 : (t + 31) / 32 * 32;
+}
+
+// The DFT of R points in place (R = 2, 3, 4, 5, 8), exponent sign DIR.
+template <int R, int DIR, typename C>
+__device__ __forceinline__ void dft_small(C* v) {
+    using T = decltype(v[0].x);
+    if constexpr (R == 2) {
+        const C a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    } else if constexpr (R == 4) {
+        const C a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]), a2 = cadd(v[1], v[3]);
+        const C a3 = cmul_i<DIR>(csub(v[1], v[3]));
+        v[0] = cadd(a0, a2);
+        v[1] = cadd(a1, a3);
+        v[2] = csub(a0, a2);
+        v[3] = csub(a1, a3);
+    } else if constexpr (R == 8) {  // two 4-point DFTs (even and odd points) and 4 radix-2 pairs
+        C e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+        dft_small<4, DIR>(e);
+        dft_small<4, DIR>(o);
+        const T r = T(0.70710678118654752440);  // 1 / sqrt(2)
+        const C o1 = C{r * (o[1].x - DIR * o[1].y), r * (o[1].y + DIR * o[1].x)};    // (1 + DIR i)/sqrt2 o1
+        const C o2 = cmul_i<DIR>(o[2]);                                                  // DIR i o2
+        const C o3 = C{r * (-o[3].x - DIR * o[3].y), r * (-o[3].y + DIR * o[3].x)};  // (-1 + DIR i)/sqrt2 o3
+        v[0] = cadd(e[0], o[0]);
+        v[4] = csub(e[0], o[0]);
+        v[1] = cadd(e[1], o1);
+        v[5] = csub(e[1], o1);
+        v[2] = cadd(e[2], o2);
+        v[6] = csub(e[2], o2);
+        v[3] = cadd(e[3], o3);
+        v[7] = csub(e[3], o3);
+    } else if constexpr (R == 3) {
+        const T s3 = T(0.86602540378443864676);  // sin(2 pi / 3)
+        const C t = cadd(v[1], v[2]);
+        const C d = cmul_i<DIR>(csub(v[1], v[2]));
+        const C m = C{v[0].x - T(0.5) * t.x, v[0].y - T(0.5) * t.y};
+        v[0] = cadd(v[0], t);
+        v[1] = C{m.x + s3 * d.x, m.y + s3 * d.y};
+        v[2] = C{m.x - s3 * d.x, m.y - s3 * d.y};
+    } else {  // R == 5
+        const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);  // cos(2 pi / 5), cos(4 pi / 5)
+        const T s1 = T(0.95105651629515357212), s2 = T(0.58778525229247312917);   // sin(2 pi / 5), sin(4 pi / 5)
+        const C t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+        const C d1 = cmul_i<DIR>(csub(v[1], v[4])), d2 = cmul_i<DIR>(csub(v[2], v[3]));
+        const C a1 = C{v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y};
+        const C a2 = C{v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y};
+        const C b1 = C{s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y};
+        const C b2 = C{s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y};
+        v[0] = cadd(v[0], cadd(t1, t2));
+        v[1] = cadd(a1, b1);
+        v[4] = csub(a1, b1);
+        v[2] = cadd(a2, b2);
+        v[3] = csub(a2, b2);
+    }
+}
+
+// One Stockham stage of radix R with sub-transform length l over the n-point line x, in place:
+// butterfly j (< n/R) reads x[j + q n/R] (q < R), turns the inputs by W(k, R l)^q with
+// k = j mod l (tw[q] = exp(-2 pi i q / n), conjugated for DIR = +1), and writes their R-point
+// DFT to x[(j - k) R + k + m l]. Thread t of the line's T (>= n/8) threads takes butterflies
+// t, t + T, ...: at most ceil(8 / R), held in registers between a barrier after the reads and
+// the writes, so one buffer serves. Every thread of the CTA must call it (two barriers).
+template <int R, int DIR, typename C>
+__device__ __forceinline__ void fft_stage(C* x, int n, int l, const C* __restrict__ tw, int t, int T) {
+    constexpr int B = (8 + R - 1) / R;
+    const int nR = n / R, step = n / (R * l);
+    const bool l2 = (l & (l - 1)) == 0;
+    C v[B][R];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = t + b * T;
+        if (j < nR) {
+            const int k = l2 ? (j & (l - 1)) : j % l;
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                C a = x[j + q * nR];
+                if (q > 0 && k > 0) {
+                    C w = __ldg(&tw[k * q * step]);
+                    if (DIR > 0) w.y = -w.y;
+                    a = cmul(a, w);
+                }
+                v[b][q] = a;
+            }
+            dft_small<R, DIR>(v[b]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = t + b * T;
+        if (j < nR) {
+            const int k = l2 ? (j & (l - 1)) : j % l;
+            const int base = (j - k) * R + k;
+#pragma unroll
+            for (int m = 0; m < R; ++m) x[base + m * l] = v[b][m];
+        }
+    }
+    __syncthreads();
+}
+
+// One line's DFT (exponent sign DIR) in place in shared memory, by the line's T threads (this
+// thread is t); every thread of the CTA calls it the same number of times. MIX compiles the
+// radix-3 and radix-5 stages too (their butterflies hold more registers); without it the line's
+// length is a power of two.
+template <int DIR, bool MIX, typename C>
+__device__ void fft_line(C* x, const FftFactors& f, const C* __restrict__ tw, int t, int T) {
+    int l = 1;
+    for (int s = 0; s < f.nst; ++s) {
+        const int R = f.radix(s);
+        if (R == 8) fft_stage<8, DIR>(x, f.n, l, tw, t, T);
+        else if (R == 4) fft_stage<4, DIR>(x, f.n, l, tw, t, T);
+        else if (!MIX || R == 2) fft_stage<2, DIR>(x, f.n, l, tw, t, T);
+        else if constexpr (MIX) {
+            if (R == 3) fft_stage<3, DIR>(x, f.n, l, tw, t, T);
+            else fft_stage<5, DIR>(x, f.n, l, tw, t, T);
+        }
+        l *= R;
+    }
+}
+
+// Launch bounds of the transform kernels: up to 1024 threads, registers capped at 64 (so two
+// 512-thread CTAs share an SM).
+constexpr int kFftMaxThreads = 1024;
+
+template <typename T>
+__device__ __forceinline__ T load_source(const void* u, int64_t pitch, int x, int64_t y, int src) {
+    if (src == kSpecReal) return ((const T*)u)[x + y * pitch];
+    const int8_t v = ((const int8_t*)u)[x + y * pitch];
+    if (src == kSpecIsOne) return v == 1 ? T(1) : T(0);
+    return T(v);
+}
+
+// The work spectrum and the kernel's spectrum are stored line by line along axis 2: row y holds
+// the axis-1 frequencies k = 0 .. n1/2 of line y, padded to ncp (a multiple of 4) values, so
+// that axis-1 kernels read and write whole rows and the axis-2 kernel reads four consecutive
+// frequencies of a row as one 32-byte (Float32) piece.
+__host__ __device__ inline int spec_pitch(int n1) { return (n1 / 2 + 1 + 3) / 4 * 4; }
+
+// Axis-1 kernels take four real lines (y = 4 b .. 4 b + 3) a CTA, as two complex lines of
+// n1 points (lines 4b, 4b+1 and 4b+2, 4b+3), each transformed by T = line_threads(n1) threads.
+constexpr int kAxis1Lines = 4;
+// The axis-2 kernel takes up to four frequencies a CTA (fewer when four lines would need more
+// than kFftMaxThreads threads).
+__host__ __device__ inline int axis2_lines(int n2) {
+    const int t = line_threads(n2);
+    return t * 4 <= kFftMaxThreads ? 4 : (t * 2 <= kFftMaxThreads ? 2 : 1);
+}
+
+// Step 1: the four lines along axis 1 into rows y of spec.
+template <typename T, bool MIX>
+__global__ void __launch_bounds__(kFftMaxThreads, 1)
+    k_axis1_forward(const void* __restrict__ u, int64_t pitch, int src, int n1, int n2, FftFactors f,
+                    const typename CxOf<T>::type* __restrict__ tw, typename CxOf<T>::type* __restrict__ spec) {
+    using C = typename CxOf<T>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int TL = line_threads(n1);
+    const int li = threadIdx.x / TL, t = threadIdx.x - li * TL;  // complex line 0 or 1
+    C* a = (C*)smem + li * n1;
+    const int64_t ya = (int64_t)kAxis1Lines * blockIdx.x + 2 * li;
+    const bool h0 = ya < n2, h1 = ya + 1 < n2;
+    for (int x = t; x < n1; x += TL)
+        a[x] = C{h0 ? load_source<T>(u, pitch, x, ya, src) : T(0), h1 ? load_source<T>(u, pitch, x, ya + 1, src) : T(0)};
+    __syncthreads();
+    fft_line<-1, MIX>(a, f, tw, t, TL);
+    const int ncp = spec_pitch(n1);
+    C* ra = spec + ya * ncp;
+    for (int k = t; k <= n1 / 2; k += TL) {
+        const C zk = a[k], zm = a[k == 0 ? 0 : n1 - k];
+        // zc = conj(Z[n1 - k]); Xa = (Zk + zc) / 2, Xb = (Zk - zc) / (2 i)
+        if (h0) ra[k] = C{T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y)};
+        if (h1) ra[ncp + k] = C{T(0.5) * (zk.y + zm.y), T(0.5) * (zm.x - zk.x)};
+    }
+}
+
+// Step 2: frequencies k0 .. k0 + L - 1 (k0 = L blockIdx.x, L = axis2_lines(n2)) along axis 2,
+// line kk by threads kk T .. kk T + T - 1. MUL: forward, times ks, inverse, in place; otherwise
+// forward only, into out. Loads and stores go row by row, lanes over the L frequencies first.
+template <typename T, bool MUL, bool MIX>
+__global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis2(typename CxOf<T>::type* __restrict__ spec,
+                                                             const typename CxOf<T>::type* __restrict__ ks,
+                                                             typename CxOf<T>::type* __restrict__ out, int n1, int n2,
+                                                             FftFactors f, const typename CxOf<T>::type* __restrict__ tw) {
+    using C = typename CxOf<T>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    C* lines = (C*)smem;  // line kk at lines + kk n2
+    const int L = axis2_lines(n2), TL = line_threads(n2), ncp = spec_pitch(n1), nc = n1 / 2 + 1;
+    const int k0 = L * blockIdx.x;
+    const int kk = threadIdx.x / TL, t = threadIdx.x - kk * TL;
+    const int nthr = L * TL;
+    for (int q = threadIdx.x; q < L * n2; q += nthr) {
+        const int y = q / L, j = q - y * L;
+        if (k0 + j < nc) lines[j * n2 + y] = spec[(int64_t)y * ncp + k0 + j];
+    }
+    __syncthreads();
+    C* a = lines + kk * n2;
+    fft_line<-1, MIX>(a, f, tw, t, TL);
+    if (MUL) {
+        for (int q = threadIdx.x; q < L * n2; q += nthr) {
+            const int y = q / L, j = q - y * L;
+            if (k0 + j < nc) lines[j * n2 + y] = cmul(lines[j * n2 + y], ks[(int64_t)y * ncp + k0 + j]);
+        }
+        __syncthreads();
+        fft_line<1, MIX>(a, f, tw, t, TL);
+    }
+    C* dst = MUL ? spec : out;
+    for (int q = threadIdx.x; q < L * n2; q += nthr) {
+        const int y = q / L, j = q - y * L;
+        if (k0 + j < nc) dst[(int64_t)y * ncp + k0 + j] = lines[j * n2 + y];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T growth(T u, T U, T mu, T sigma, T dt) {
+    const T d = U - mu;
+    const T g = T(2) * exp(-(d * d) / (T(2) * (sigma * sigma))) - T(1);
+    T v = u + dt * g;
+    v = v < T(0) ? T(0) : v;
+    return v > T(1) ? T(1) : v;
+}
+
+// Step 3: four lines back along axis 1. Each complex line reads its two lines' rows of half
+// spectra, made Hermitian (the imaginary parts of frequencies 0 and n1/2 dropped), as Fa + i Fb
+// over all n1 frequencies; its inverse transform holds the two real fields. Then LENIA:
+// out = growth(u, U) (pitch pe); else out = U (packed).
+template <typename T, bool LENIA, bool MIX>
+__global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis1_inverse(const typename CxOf<T>::type* __restrict__ spec, int n1, int n2, FftFactors f,
+                                const typename CxOf<T>::type* __restrict__ tw, const T* __restrict__ u,
+                                T* __restrict__ out, int64_t pe, T mu, T sigma, T dt) {
+    using C = typename CxOf<T>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int TL = line_threads(n1);
+    const int li = threadIdx.x / TL, t = threadIdx.x - li * TL;
+    const int64_t ya = (int64_t)kAxis1Lines * blockIdx.x + 2 * li;
+    const bool h0 = ya < n2, h1 = ya + 1 < n2;
+    const int ncp = spec_pitch(n1);
+    C* a = (C*)smem + li * n1;
+    {
+        const C* ra = spec + ya * ncp;
+        for (int k = t; k < n1; k += TL) {
+            const bool lo = 2 * k <= n1;
+            const int m = lo ? k : n1 - k;
+            C fa = h0 ? ra[m] : C{T(0), T(0)}, fb = h1 ? ra[ncp + m] : C{T(0), T(0)};
+            if (!lo) {
+                fa.y = -fa.y;
+                fb.y = -fb.y;
+            }
+            if (k == 0 || 2 * k == n1) {
+                fa.y = T(0);
+                fb.y = T(0);
+            }
+            a[k] = C{fa.x - fb.y, fa.y + fb.x};  // Fa + i Fb
+        }
+    }
+    __syncthreads();
+    fft_line<1, MIX>(a, f, tw, t, TL);
+    for (int x = t; x < n1; x += TL) {
+        const C v = a[x];
+        if (LENIA) {
+            if (h0) out[x + ya * pe] = growth<T>(u[x + ya * pe], v.x, mu, sigma, dt);
+            if (h1) out[x + (ya + 1) * pe] = growth<T>(u[x + (ya + 1) * pe], v.y, mu, sigma, dt);
+        } else {
+            if (h0) out[x + ya * n1] = v.x;
+            if (h1) out[x + (ya + 1) * n1] = v.y;
+        }
+    }
+}
+
+// The kernel's spectrum for the per-step product: conj(S) / (n1 n2) in the plan's precision.
+template <typename C>
+__global__ void k_finish_kspec(const double2* __restrict__ s, C* __restrict__ ks, int64_t n, double scale) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = s[i];
+        ks[i] = C{(decltype(C{}.x))(v.x * scale), (decltype(C{}.x))(-v.y * scale)};
+    }
+}
+
+template <typename C>
+std::vector<C> twiddles(int n) {
+    std::vector<C> t((size_t)n);
+    const double pi = 3.14159265358979323846;
+    for (int q = 0; q < n; ++q) {
+        const double a = -2.0 * pi * (double)q / (double)n;
+        t[(size_t)q] = C{(decltype(C{}.x))std::cos(a), (decltype(C{}.x))std::sin(a)};
+    }
+    return t;
+}
+
+}  // namespace
+
+struct SpecConv {
+    int64_t n1 = 0, n2 = 0;
+    bool f64 = false;
+    FftFactors f1{}, f2{};
+    void* tw1 = nullptr;  // twiddles of axis 1 and 2 in the plan's precision
+    void* tw2 = nullptr;
+    void* ks = nullptr;    // conj(rfft2(kpad)) / (n1 n2), frequency-major: [k][ky]
+    void* spec = nullptr;  // work spectrum, the same layout
+};
+
+bool specconv_supported(int64_t n1, int64_t n2, bool f64) {
+    // a CTA transforms two axis-1 lines (2 x line_threads(n1) <= 1024) or one axis-2 line
+    // (line_threads(n2) <= 1024); shared memory holds them (at most 128 KB)
+    if (n1 < 1 || n2 < 1 || 2 * line_threads((int)(n1 < 8192 ? n1 : 8192)) > kFftMaxThreads || n1 > 4096 ||
+        n2 > 8192)
+        return false;
+    (void)f64;
+    return factorize(n1).nst >= 0 && factorize(n2).nst >= 0;
+}
+
+void specconv_destroy(SpecConv* p) {
+    if (!p) return;
+    cudaFree(p->tw1);
+    cudaFree(p->tw2);
+    cudaFree(p->ks);
+    cudaFree(p->spec);
+    delete p;
+}
+
+namespace {
+
+bool pow2(int64_t n) { return n > 0 && (n & (n - 1)) == 0; }
+
+template <typename T, bool MIX>
+cudaError_t launch_axis1_forward(SpecConv* p, const void* u, int64_t pitch, int src, const void* tw, void* spec,
+                                 cudaStream_t st) {
+    using C = typename CxOf<T>::type;
+    const int n1 = (int)p->n1, n2 = (int)p->n2;
+    const size_t smem = 2 * sizeof(C) * (size_t)n1;
+    cudaError_t e = ensure_dynamic_smem((const void*)k_axis1_forward<T, MIX>, smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)((n2 + kAxis1Lines - 1) / kAxis1Lines);
+    k_axis1_forward<T, MIX><<<grid, 2 * line_threads(n1), smem, st>>>(u, pitch, src, n1, n2, p->f1, (const C*)tw,
+                                                                       (C*)spec);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T, bool MUL, bool MIX>
+cudaError_t launch_axis2(SpecConv* p, void* spec, const void* ks, void* out, const void* tw, cudaStream_t st) {
+    using C = typename CxOf<T>::type;
+    const int n1 = (int)p->n1, n2 = (int)p->n2, L = axis2_lines(n2);
+    const size_t smem = sizeof(C) * (size_t)n2 * L;
+    cudaError_t e = ensure_dynamic_smem((const void*)k_axis2<T, MUL, MIX>, smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)((n1 / 2 + 1 + L - 1) / L);
+    k_axis2<T, MUL, MIX><<<grid, L * line_threads(n2), smem, st>>>((C*)spec, (const C*)ks, (C*)out, n1, n2, p->f2,
+                                                                   (const C*)tw);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T, bool LENIA, bool MIX>
+cudaError_t launch_axis1_inverse(SpecConv* p, const T* u, T* out, int64_t pe, double mu, double sigma, double dt,
+                                 cudaStream_t st) {
+    using C = typename CxOf<T>::type;
+    const int n1 = (int)p->n1, n2 = (int)p->n2;
+    const size_t smem = 2 * sizeof(C) * (size_t)n1;
+    cudaError_t e = ensure_dynamic_smem((const void*)k_axis1_inverse<T, LENIA, MIX>, smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)((n2 + kAxis1Lines - 1) / kAxis1Lines);
+    k_axis1_inverse<T, LENIA, MIX><<<grid, 2 * line_threads(n1), smem, st>>>(
+        (const C*)p->spec, n1, n2, p->f1, (const C*)p->tw1, u, out, pe, (T)mu, (T)sigma, (T)dt);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// Steps 1 and 2: with mul, the spectral product and the inverse along axis 2 in spec; without,
+// the forward spectrum into out.
+template <typename T>
+cudaError_t run_forward(SpecConv* p, const void* u, int64_t pitch, int src, const void* tw1, const void* tw2,
+                        void* spec, const void* ks, void* out, bool mul, cudaStream_t st) {
+    const bool m1 = !pow2(p->n1), m2 = !pow2(p->n2);
+    cudaError_t e = m1 ? launch_axis1_forward<T, true>(p, u, pitch, src, tw1, spec, st)
+                       : launch_axis1_forward<T, false>(p, u, pitch, src, tw1, spec, st);
+    if (e != cudaSuccess) return e;
+    if (mul) return m2 ? launch_axis2<T, true, true>(p, spec, ks, nullptr, tw2, st)
+                       : launch_axis2<T, true, false>(p, spec, ks, nullptr, tw2, st);
+    return m2 ? launch_axis2<T, false, true>(p, spec, nullptr, out, tw2, st)
+              : launch_axis2<T, false, false>(p, spec, nullptr, out, tw2, st);
+}
+
+// Step 3: Lenia's growth into out (pitch pe), or the field into out (packed).
+template <typename T>
+cudaError_t run_inverse(SpecConv* p, const T* u, T* out, int64_t pe, bool lenia, double mu, double sigma, double dt,
+                        cudaStream_t st) {
+    const bool m1 = !pow2(p->n1);
+    if (lenia)
+        return m1 ? launch_axis1_inverse<T, true, true>(p, u, out, pe, mu, sigma, dt, st)
+                  : launch_axis1_inverse<T, true, false>(p, u, out, pe, mu, sigma, dt, st);
+    return m1 ? launch_axis1_inverse<T, false, true>(p, u, out, pe, mu, sigma, dt, st)
+              : launch_axis1_inverse<T, false, false>(p, u, out, pe, mu, sigma, dt, st);
+}
+
+}  // namespace
+
+int specconv_create(int64_t n1, int64_t n2, bool f64, const double* kpad, cudaStream_t st, SpecConv** out,
+                    std::string& err) {
+    *out = nullptr;
+    if (!specconv_supported(n1, n2, f64)) {
+        err = "the lattice's sides are not products of 2, 3 and 5 that fit the transform";
+        return GBCA_ERR_UNSUPPORTED;
+    }
+    SpecConv* p = new SpecConv();
+    p->n1 = n1;
+    p->n2 = n2;
+    p->f64 = f64;
+    p->f1 = factorize(n1);
+    p->f2 = factorize(n2);
+    const int64_t nc = spec_pitch((int)n1), ncell = n1 * n2;  // nc: the spectra's row pitch
+    const size_t cs = f64 ? sizeof(double2) : sizeof(float2);
+    // FP64 twiddles for the kernel's spectrum; the plan's own in its precision
+    const std::vector<double2> t1d = twiddles<double2>((int)n1), t2d = twiddles<double2>((int)n2);
+    double2 *d_t1 = nullptr, *d_t2 = nullptr, *d_s = nullptr, *d_o = nullptr;
+    double* d_k = nullptr;
+    cudaError_t e = cudaMalloc(&p->ks, cs * (size_t)(nc * n2));
+    if (e == cudaSuccess) e = cudaMalloc(&p->spec, cs * (size_t)(nc * n2));
+    if (e == cudaSuccess) e = cudaMalloc(&p->tw1, cs * (size_t)n1);
+    if (e == cudaSuccess) e = cudaMalloc(&p->tw2, cs * (size_t)n2);
+    if (e == cudaSuccess) e = cudaMalloc(&d_t1, sizeof(double2) * (size_t)n1);
+    if (e == cudaSuccess) e = cudaMalloc(&d_t2, sizeof(double2) * (size_t)n2);
+    if (e == cudaSuccess) e = cudaMalloc(&d_s, sizeof(double2) * (size_t)(nc * n2));
+    if (e == cudaSuccess) e = cudaMalloc(&d_o, sizeof(double2) * (size_t)(nc * n2));
+    if (e == cudaSuccess) e = cudaMalloc(&d_k, sizeof(double) * (size_t)ncell);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_t1, t1d.data(), sizeof(double2) * n1, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_t2, t2d.data(), sizeof(double2) * n2, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_k, kpad, sizeof(double) * ncell, cudaMemcpyHostToDevice, st);
+    std::vector<float2> t1f, t2f;
+    if (e == cudaSuccess) {
+        if (f64) {
+            e = cudaMemcpyAsync(p->tw1, t1d.data(), sizeof(double2) * n1, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(p->tw2, t2d.data(), sizeof(double2) * n2, cudaMemcpyHostToDevice, st);
+        } else {
+            t1f = twiddles<float2>((int)n1);
+            t2f = twiddles<float2>((int)n2);
+            e = cudaMemcpyAsync(p->tw1, t1f.data(), sizeof(float2) * n1, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(p->tw2, t2f.data(), sizeof(float2) * n2, cudaMemcpyHostToDevice, st);
+        }
+    }
+    if (e == cudaSuccess) e = run_forward<double>(p, d_k, n1, kSpecReal, d_t1, d_t2, d_s, nullptr, d_o, false, st);
+    if (e == cudaSuccess) {
+        const double scale = 1.0 / (double)ncell;
+        if (f64) k_finish_kspec<double2><<<256, 256, 0, st>>>(d_o, (double2*)p->ks, nc * n2, scale);
+        else k_finish_kspec<float2><<<256, 256, 0, st>>>(d_o, (float2*)p->ks, nc * n2, scale);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host vectors and temporaries go out of scope
+    cudaFree(d_t1);
+    cudaFree(d_t2);
+    cudaFree(d_s);
+    cudaFree(d_o);
+    cudaFree(d_k);
+    if (e != cudaSuccess) {
+        err = cudaGetErrorString(e);
+        const bool oom = e == cudaErrorMemoryAllocation;
+        specconv_destroy(p);
+        cudaGetLastError();
+        return oom ? GBCA_ERR_OUT_OF_MEMORY : GBCA_ERR_CUDA;
+    }
+    *out = p;
+    return GBCA_OK;
+}
+
+cudaError_t specconv_lenia_step(SpecConv* p, const void* u, void* out, int64_t pe, double mu, double sigma, double dt,
+                                cudaStream_t st) {
+    cudaError_t e;
+    if (p->f64) {
+        e = run_forward<double>(p, u, pe, kSpecReal, p->tw1, p->tw2, p->spec, p->ks, nullptr, true, st);
+        if (e == cudaSuccess) e = run_inverse<double>(p, (const double*)u, (double*)out, pe, true, mu, sigma, dt, st);
+    } else {
+        e = run_forward<float>(p, u, pe, kSpecReal, p->tw1, p->tw2, p->spec, p->ks, nullptr, true, st);
+        if (e == cudaSuccess) e = run_inverse<float>(p, (const float*)u, (float*)out, pe, true, mu, sigma, dt, st);
+    }
+    return e;
+}
+
+cudaError_t specconv_field(SpecConv* p, const int8_t* u, int64_t pitch, SpecSource src, void* field,
+                           cudaStream_t st) {
+    cudaError_t e;
+    if (p->f64) {
+        e = run_forward<double>(p, u, pitch, src, p->tw1, p->tw2, p->spec, p->ks, nullptr, true, st);
+        if (e == cudaSuccess) e = run_inverse<double>(p, nullptr, (double*)field, 0, false, 0, 0, 0, st);
+    } else {
+        e = run_forward<float>(p, u, pitch, src, p->tw1, p->tw2, p->spec, p->ks, nullptr, true, st);
+        if (e == cudaSuccess) e = run_inverse<float>(p, nullptr, (float*)field, 0, false, 0, 0, 0, st);
+    }
+    return e;
+}
+
+}  // namespace gbca

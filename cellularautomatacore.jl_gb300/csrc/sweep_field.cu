@@ -16,14 +16,16 @@
 // region holds no nonzero source has every field exactly 0, hence no infection, and skips
 // the tap loop. The rule never reads its neighbours directly and the field is fixed for the
 // whole step, so Checkerboard's two half-sweeps update every cell once from the start-of-step
-// values: one pass covers both. With method = :fft the field comes from cuFFT instead
-// (ext/CellularAutomataCoreFFTWExt.jl:17-30) and the tile needs no halo.
+// values: one pass covers both. With method = :fft the field comes from a spectral product
+// instead (ext/CellularAutomataCoreFFTWExt.jl:17-30) and the tile needs no halo: this
+// library's transforms (spectral.cu) where both sides are products of 2, 3 and 5, cuFFT else.
 #include <cmath>
 #include <vector>
 
 #include <cufft.h>
 
 #include "field.cuh"
+#include "spectral.cuh"
 #include "gbca_internal.cuh"
 
 namespace gbca {
@@ -176,12 +178,14 @@ struct FieldFFT {
     void* spec = nullptr;   // its spectrum
     void* kspec = nullptr;  // conj(rfft(kpad)) / (n1 n2)
     void* field = nullptr;  // the real field, packed n1 x n2
+    SpecConv* sc = nullptr;  // this library's transforms (sides of 2, 3 and 5); else the cuFFT plans
 };
 
 void field_fft_destroy(FieldFFT* F) {
     if (!F) return;
     if (F->fwd) cufftDestroy(F->fwd);
     if (F->inv) cufftDestroy(F->inv);
+    specconv_destroy(F->sc);
     cudaFree(F->src);
     cudaFree(F->spec);
     cudaFree(F->kspec);
@@ -191,7 +195,7 @@ void field_fft_destroy(FieldFFT* F) {
 
 // The FFTW extension's product (ext/CellularAutomataCoreFFTWExt.jl:17-30): the weight of
 // offset o added to kpad at 0-based (o mod n) on each axis, transformed once, conjugated,
-// with the 1/(n1 n2) that cuFFT's inverse leaves out folded in.
+// with the inverse's 1/(n1 n2) folded in; by spectral.cu where the sides allow, else by cuFFT.
 int field_fft_create(int64_t n1, int64_t n2, const std::vector<int>& taps, const std::vector<double>& w, bool f32,
                      cudaStream_t st, FieldFFT** out, std::string& err) {
     *out = nullptr;
@@ -201,6 +205,25 @@ int field_fft_create(int64_t n1, int64_t n2, const std::vector<int>& taps, const
     F->n2 = n2;
     const int64_t nc = n1 / 2 + 1, n = n1 * n2;
     const size_t es = f32 ? sizeof(float) : sizeof(double), cs = 2 * es;
+    if (specconv_supported(n1, n2, !f32)) {  // kpad in FP64, each weight in the field's precision
+        std::vector<double> kpad((size_t)n, 0.0);
+        for (size_t k = 0; k < w.size(); ++k) {
+            const int64_t a = map_axis(GBCA_PERIODIC, taps[2 * k], n1), b = map_axis(GBCA_PERIODIC, taps[2 * k + 1], n2);
+            kpad[(size_t)(a + b * n1)] += f32 ? (double)(float)w[k] : w[k];
+        }
+        int rc = specconv_create(n1, n2, !f32, kpad.data(), st, &F->sc, err);
+        if (rc == GBCA_OK && cudaMalloc(&F->field, es * n) != cudaSuccess) {
+            err = "out of device memory for the field";
+            rc = GBCA_ERR_OUT_OF_MEMORY;
+        }
+        if (rc != GBCA_OK) {
+            field_fft_destroy(F);
+            cudaGetLastError();
+            return rc;
+        }
+        *out = F;
+        return GBCA_OK;
+    }
     int dims[2] = {(int)n2, (int)n1};
     int rembed[2] = {(int)n2, (int)n1};
     int cembed[2] = {(int)n2, (int)nc};
@@ -270,6 +293,8 @@ int field_fft_create(int64_t n1, int64_t n2, const std::vector<int>& taps, const
 
 // The field of the current state into F->field.
 static cudaError_t field_fft_run(FieldFFT* F, const int8_t* u, int64_t pitch, int source, int nsm, cudaStream_t st) {
+    if (F->sc)
+        return specconv_field(F->sc, u, pitch, source == kSourceIdentity ? kSpecValue : kSpecIsOne, F->field, st);
     const int64_t nc = F->n1 / 2 + 1;
     const int grid = nsm * 8;
     // the handle's stream may have changed since the plans were made

@@ -116,8 +116,9 @@ def test_si_field_direct(ca, oracle, case):
 
 
 def test_si_field_fft_float64(ca, oracle):
-    """method=:fft on a torus: cuFFT's Float64 field differs from the direct sum by rounding
-    (~1e-16), which changes an outcome with probability ~1e-16 per draw."""
+    """method=:fft on a torus (this library's transforms: 384 = 2^7 3, 256 = 2^8): the Float64
+    field differs from the direct sum by rounding (~1e-16), which changes an outcome with
+    probability ~1e-16 per draw."""
     case = ("FFT Float64, 384 x 256 torus", (384, 256), "pp", ("exp", 2.0, 0, 0), "Float64", 2, True, "sync", 2.0,
             31, 20)
     prob, sch, P, E, u0, beta, steps = _si_pair(ca, oracle, case, method="fft")

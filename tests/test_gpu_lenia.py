@@ -125,3 +125,24 @@ def test_config_2048_float64_within_1e5_after_100_steps(ca, oracle):
         e = np.abs(g32.astype(np.float64) - want)
         print(f"Float32 {method} after 100 steps: max-abs {e.max():.3e}, L2 {np.sqrt((e ** 2).mean()):.3e}")
         assert np.isfinite(e).all() and g32.min() >= 0 and g32.max() <= 1
+
+
+@pytest.mark.parametrize("dims", [(360, 150), (250, 96), (112, 98)])
+def test_fft_on_mixed_radix_and_other_sides(ca, oracle, dims):
+    """The FFT field on sides that are products of 2, 3 and 5 (this library's transforms: 360 =
+    2^3 3^2 5, 150 = 2 3 5^2, 250 = 2 5^3) and on a side with a factor 7 (98, the cuFFT path):
+    Float64 steps within 1e-10 of the FP64 oracle's FFT, Float32 steps within the per-step
+    tolerance, on a soup that fills the torus."""
+    n1, n2 = dims
+    rng = np.random.default_rng(n1 * 1000 + n2)
+    u = rng.random((n1, n2))
+    fft = oracle.LeniaFFT(n1, n2)
+    space = ca.Torus(n1, n2)
+    g64 = gpu_step(ca, *gpu_state(ca, ca.Lenia(method="fft", precision="Float64"), u, space), u, 3)
+    want = u.copy()
+    for _ in range(3):
+        want = fft.step(want)
+    assert np.max(np.abs(g64 - want)) < 1e-10
+    u32 = u.astype(np.float32)
+    g32 = gpu_step(ca, *gpu_state(ca, ca.Lenia(method="fft", precision="Float32"), u32, space), u32, 1)
+    assert np.max(np.abs(g32.astype(np.float64) - fft.step(u32.astype(np.float64)))) < PER_STEP_TOL_F32
