@@ -123,16 +123,34 @@ __device__ __forceinline__ void dft_small(C* v) {
     }
 }
 
-// One Stockham stage of radix R with sub-transform length l over the n-point line x, in place:
-// butterfly j (< n/R) reads x[j + q n/R] (q < R), turns the inputs by W(k, R l)^q with
-// k = j mod l (tw[q] = exp(-2 pi i q / n), conjugated for DIR = +1), and writes their R-point
-// DFT to x[(j - k) R + k + m l]. Thread t of the line's T (>= n/8) threads takes butterflies
-// t, t + T, ...: at most ceil(8 / R), held in registers between a barrier after the reads and
-// the writes, so one buffer serves. Every thread of the CTA must call it (two barriers).
+// Shared-memory slot of point e of a line: one pad slot every 16 points, so that the early
+// stages' writes (points 8 apart) and the axis-2 kernel's row loads meet few bank conflicts.
+__host__ __device__ __forceinline__ int pad16(int e) { return e + (e >> 4); }
+__host__ __device__ inline int padded_len(int n) { return pad16(n - 1) + 1; }
+
+// Twiddles of every stage, stage after stage: for a stage of radix R after sub-transforms of
+// length l, W(k, R l)^q = exp(-2 pi i k q / (R l)) at [(q - 1) l + k], q = 1 .. R - 1, k < l:
+// consecutive butterflies read consecutive entries. twiddle_count(f) entries in all.
+int twiddle_count(const FftFactors& f) {
+    int l = 1, c = 0;
+    for (int s = 0; s < f.nst; ++s) {
+        c += (f.radix(s) - 1) * l;
+        l *= f.radix(s);
+    }
+    return c;
+}
+
+// One Stockham stage of radix R with sub-transform length l over the n-point line x (padded
+// slots), in place: butterfly j (< n/R) reads points j + q n/R (q < R), turns the inputs by
+// W(k, R l)^q with k = j mod l (tw: the stage's table, conjugated for DIR = +1), and writes
+// their R-point DFT to points (j - k) R + k + m l. Thread t of the line's T (>= n/8) threads
+// takes butterflies t, t + T, ...: at most ceil(8 / R), held in registers between a barrier
+// after the reads and the writes, so one buffer serves. Every thread of the CTA must call it
+// (two barriers).
 template <int R, int DIR, typename C>
-__device__ __forceinline__ void fft_stage(C* x, int n, int l, const C* __restrict__ tw, int t, int T) {
+__device__ __forceinline__ void fft_stage(C* x, int n, int l, const C* tw, int t, int T) {
     constexpr int B = (8 + R - 1) / R;
-    const int nR = n / R, step = n / (R * l);
+    const int nR = n / R;
     const bool l2 = (l & (l - 1)) == 0;
     C v[B][R];
 #pragma unroll
@@ -142,9 +160,9 @@ __device__ __forceinline__ void fft_stage(C* x, int n, int l, const C* __restric
             const int k = l2 ? (j & (l - 1)) : j % l;
 #pragma unroll
             for (int q = 0; q < R; ++q) {
-                C a = x[j + q * nR];
-                if (q > 0 && k > 0) {
-                    C w = __ldg(&tw[k * q * step]);
+                C a = x[pad16(j + q * nR)];
+                if (q > 0) {
+                    C w = tw[(q - 1) * l + k];
                     if (DIR > 0) w.y = -w.y;
                     a = cmul(a, w);
                 }
@@ -161,18 +179,18 @@ __device__ __forceinline__ void fft_stage(C* x, int n, int l, const C* __restric
             const int k = l2 ? (j & (l - 1)) : j % l;
             const int base = (j - k) * R + k;
 #pragma unroll
-            for (int m = 0; m < R; ++m) x[base + m * l] = v[b][m];
+            for (int m = 0; m < R; ++m) x[pad16(base + m * l)] = v[b][m];
         }
     }
     __syncthreads();
 }
 
-// One line's DFT (exponent sign DIR) in place in shared memory, by the line's T threads (this
-// thread is t); every thread of the CTA calls it the same number of times. MIX compiles the
-// radix-3 and radix-5 stages too (their butterflies hold more registers); without it the line's
-// length is a power of two.
+// One line's DFT (exponent sign DIR) in place in shared memory (padded slots), by the line's T
+// threads (this thread is t), twiddles from the per-stage table tw (shared memory); every thread
+// of the CTA calls it the same number of times. MIX compiles the radix-3 and radix-5 stages too
+// (their butterflies hold more registers); without it the line's length is a power of two.
 template <int DIR, bool MIX, typename C>
-__device__ void fft_line(C* x, const FftFactors& f, const C* __restrict__ tw, int t, int T) {
+__device__ void fft_line(C* x, const FftFactors& f, const C* tw, int t, int T) {
     int l = 1;
     for (int s = 0; s < f.nst; ++s) {
         const int R = f.radix(s);
@@ -183,8 +201,16 @@ __device__ void fft_line(C* x, const FftFactors& f, const C* __restrict__ tw, in
             if (R == 3) fft_stage<3, DIR>(x, f.n, l, tw, t, T);
             else fft_stage<5, DIR>(x, f.n, l, tw, t, T);
         }
+        tw += (R - 1) * l;
         l *= R;
     }
+}
+
+// The per-stage twiddle table into shared memory (by all threads of the CTA; a barrier follows
+// before use).
+template <typename C>
+__device__ __forceinline__ void stage_twiddles(C* dst, const C* __restrict__ src, int count) {
+    for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = src[i];
 }
 
 // Launch bounds of the transform kernels: up to 1024 threads, registers capped at 64 (so two
@@ -214,27 +240,34 @@ __host__ __device__ inline int axis2_lines(int n2) {
     const int t = line_threads(n2);
     return t * 4 <= kFftMaxThreads ? 4 : (t * 2 <= kFftMaxThreads ? 2 : 1);
 }
+// Shared-memory stride between the axis-2 kernel's lines: 4 slots (32 bytes in Float32) modulo
+// 16, so that one row's four frequencies land in different banks.
+__host__ __device__ inline int axis2_line_stride(int n2) { return (padded_len(n2) + 15) / 16 * 16 + 4; }
 
 // Step 1: the four lines along axis 1 into rows y of spec.
 template <typename T, bool MIX>
 __global__ void __launch_bounds__(kFftMaxThreads, 1)
     k_axis1_forward(const void* __restrict__ u, int64_t pitch, int src, int n1, int n2, FftFactors f,
-                    const typename CxOf<T>::type* __restrict__ tw, typename CxOf<T>::type* __restrict__ spec) {
+                    const typename CxOf<T>::type* __restrict__ tw, int ntw, typename CxOf<T>::type* __restrict__ spec) {
     using C = typename CxOf<T>::type;
     extern __shared__ __align__(16) unsigned char smem[];
+    C* tws = (C*)smem;  // the twiddles, then the two lines
+    stage_twiddles(tws, tw, ntw);
     const int TL = line_threads(n1);
     const int li = threadIdx.x / TL, t = threadIdx.x - li * TL;  // complex line 0 or 1
-    C* a = (C*)smem + li * n1;
+    C* a = tws + ntw + li * padded_len(n1);
     const int64_t ya = (int64_t)kAxis1Lines * blockIdx.x + 2 * li;
     const bool h0 = ya < n2, h1 = ya + 1 < n2;
+#pragma unroll 4
     for (int x = t; x < n1; x += TL)
-        a[x] = C{h0 ? load_source<T>(u, pitch, x, ya, src) : T(0), h1 ? load_source<T>(u, pitch, x, ya + 1, src) : T(0)};
+        a[pad16(x)] = C{h0 ? load_source<T>(u, pitch, x, ya, src) : T(0),
+                        h1 ? load_source<T>(u, pitch, x, ya + 1, src) : T(0)};
     __syncthreads();
-    fft_line<-1, MIX>(a, f, tw, t, TL);
+    fft_line<-1, MIX>(a, f, tws, t, TL);
     const int ncp = spec_pitch(n1);
     C* ra = spec + ya * ncp;
     for (int k = t; k <= n1 / 2; k += TL) {
-        const C zk = a[k], zm = a[k == 0 ? 0 : n1 - k];
+        const C zk = a[pad16(k)], zm = a[pad16(k == 0 ? 0 : n1 - k)];
         // zc = conj(Z[n1 - k]); Xa = (Zk + zc) / 2, Xb = (Zk - zc) / (2 i)
         if (h0) ra[k] = C{T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y)};
         if (h1) ra[ncp + k] = C{T(0.5) * (zk.y + zm.y), T(0.5) * (zm.x - zk.x)};
@@ -248,33 +281,40 @@ template <typename T, bool MUL, bool MIX>
 __global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis2(typename CxOf<T>::type* __restrict__ spec,
                                                              const typename CxOf<T>::type* __restrict__ ks,
                                                              typename CxOf<T>::type* __restrict__ out, int n1, int n2,
-                                                             FftFactors f, const typename CxOf<T>::type* __restrict__ tw) {
+                                                             FftFactors f, const typename CxOf<T>::type* __restrict__ tw,
+                                                             int ntw) {
     using C = typename CxOf<T>::type;
     extern __shared__ __align__(16) unsigned char smem[];
-    C* lines = (C*)smem;  // line kk at lines + kk n2
+    C* tws = (C*)smem;
+    stage_twiddles(tws, tw, ntw);
+    C* lines = tws + ntw;  // line kk at lines + kk LP
     const int L = axis2_lines(n2), TL = line_threads(n2), ncp = spec_pitch(n1), nc = n1 / 2 + 1;
+    const int LP = axis2_line_stride(n2);
     const int k0 = L * blockIdx.x;
     const int kk = threadIdx.x / TL, t = threadIdx.x - kk * TL;
     const int nthr = L * TL;
+    const int lsh = L == 4 ? 2 : (L == 2 ? 1 : 0);
+#pragma unroll 4
     for (int q = threadIdx.x; q < L * n2; q += nthr) {
-        const int y = q / L, j = q - y * L;
-        if (k0 + j < nc) lines[j * n2 + y] = spec[(int64_t)y * ncp + k0 + j];
+        const int y = q >> lsh, j = q & (L - 1);
+        if (k0 + j < nc) lines[j * LP + pad16(y)] = spec[(int64_t)y * ncp + k0 + j];
     }
     __syncthreads();
-    C* a = lines + kk * n2;
-    fft_line<-1, MIX>(a, f, tw, t, TL);
+    C* a = lines + kk * LP;
+    fft_line<-1, MIX>(a, f, tws, t, TL);
     if (MUL) {
+#pragma unroll 4
         for (int q = threadIdx.x; q < L * n2; q += nthr) {
-            const int y = q / L, j = q - y * L;
-            if (k0 + j < nc) lines[j * n2 + y] = cmul(lines[j * n2 + y], ks[(int64_t)y * ncp + k0 + j]);
+            const int y = q >> lsh, j = q & (L - 1);
+            if (k0 + j < nc) lines[j * LP + pad16(y)] = cmul(lines[j * LP + pad16(y)], ks[(int64_t)y * ncp + k0 + j]);
         }
         __syncthreads();
-        fft_line<1, MIX>(a, f, tw, t, TL);
+        fft_line<1, MIX>(a, f, tws, t, TL);
     }
     C* dst = MUL ? spec : out;
     for (int q = threadIdx.x; q < L * n2; q += nthr) {
-        const int y = q / L, j = q - y * L;
-        if (k0 + j < nc) dst[(int64_t)y * ncp + k0 + j] = lines[j * n2 + y];
+        const int y = q >> lsh, j = q & (L - 1);
+        if (k0 + j < nc) dst[(int64_t)y * ncp + k0 + j] = lines[j * LP + pad16(y)];
     }
 }
 
@@ -293,18 +333,21 @@ __device__ __forceinline__ T growth(T u, T U, T mu, T sigma, T dt) {
 // out = growth(u, U) (pitch pe); else out = U (packed).
 template <typename T, bool LENIA, bool MIX>
 __global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis1_inverse(const typename CxOf<T>::type* __restrict__ spec, int n1, int n2, FftFactors f,
-                                const typename CxOf<T>::type* __restrict__ tw, const T* __restrict__ u,
+                                const typename CxOf<T>::type* __restrict__ tw, int ntw, const T* __restrict__ u,
                                 T* __restrict__ out, int64_t pe, T mu, T sigma, T dt) {
     using C = typename CxOf<T>::type;
     extern __shared__ __align__(16) unsigned char smem[];
+    C* tws = (C*)smem;
+    stage_twiddles(tws, tw, ntw);
     const int TL = line_threads(n1);
     const int li = threadIdx.x / TL, t = threadIdx.x - li * TL;
     const int64_t ya = (int64_t)kAxis1Lines * blockIdx.x + 2 * li;
     const bool h0 = ya < n2, h1 = ya + 1 < n2;
     const int ncp = spec_pitch(n1);
-    C* a = (C*)smem + li * n1;
+    C* a = tws + ntw + li * padded_len(n1);
     {
         const C* ra = spec + ya * ncp;
+#pragma unroll 4
         for (int k = t; k < n1; k += TL) {
             const bool lo = 2 * k <= n1;
             const int m = lo ? k : n1 - k;
@@ -317,13 +360,13 @@ __global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis1_inverse(const typen
                 fa.y = T(0);
                 fb.y = T(0);
             }
-            a[k] = C{fa.x - fb.y, fa.y + fb.x};  // Fa + i Fb
+            a[pad16(k)] = C{fa.x - fb.y, fa.y + fb.x};  // Fa + i Fb
         }
     }
     __syncthreads();
-    fft_line<1, MIX>(a, f, tw, t, TL);
+    fft_line<1, MIX>(a, f, tws, t, TL);
     for (int x = t; x < n1; x += TL) {
-        const C v = a[x];
+        const C v = a[pad16(x)];
         if (LENIA) {
             if (h0) out[x + ya * pe] = growth<T>(u[x + ya * pe], v.x, mu, sigma, dt);
             if (h1) out[x + (ya + 1) * pe] = growth<T>(u[x + (ya + 1) * pe], v.y, mu, sigma, dt);
@@ -344,12 +387,18 @@ __global__ void k_finish_kspec(const double2* __restrict__ s, C* __restrict__ ks
 }
 
 template <typename C>
-std::vector<C> twiddles(int n) {
-    std::vector<C> t((size_t)n);
+std::vector<C> stage_table(const FftFactors& f) {
+    std::vector<C> t;
     const double pi = 3.14159265358979323846;
-    for (int q = 0; q < n; ++q) {
-        const double a = -2.0 * pi * (double)q / (double)n;
-        t[(size_t)q] = C{(decltype(C{}.x))std::cos(a), (decltype(C{}.x))std::sin(a)};
+    int l = 1;
+    for (int s = 0; s < f.nst; ++s) {
+        const int R = f.radix(s);
+        for (int q = 1; q < R; ++q)
+            for (int k = 0; k < l; ++k) {
+                const double a = -2.0 * pi * (double)k * (double)q / (double)(R * l);
+                t.push_back(C{(decltype(C{}.x))std::cos(a), (decltype(C{}.x))std::sin(a)});
+            }
+        l *= R;
     }
     return t;
 }
@@ -360,6 +409,7 @@ struct SpecConv {
     int64_t n1 = 0, n2 = 0;
     bool f64 = false;
     FftFactors f1{}, f2{};
+    int ntw1 = 0, ntw2 = 0;  // entries of the per-stage twiddle tables
     void* tw1 = nullptr;  // twiddles of axis 1 and 2 in the plan's precision
     void* tw2 = nullptr;
     void* ks = nullptr;    // conj(rfft2(kpad)) / (n1 n2), frequency-major: [k][ky]
@@ -367,13 +417,15 @@ struct SpecConv {
 };
 
 bool specconv_supported(int64_t n1, int64_t n2, bool f64) {
-    // a CTA transforms two axis-1 lines (2 x line_threads(n1) <= 1024) or one axis-2 line
-    // (line_threads(n2) <= 1024); shared memory holds them (at most 128 KB)
-    if (n1 < 1 || n2 < 1 || 2 * line_threads((int)(n1 < 8192 ? n1 : 8192)) > kFftMaxThreads || n1 > 4096 ||
-        n2 > 8192)
-        return false;
-    (void)f64;
-    return factorize(n1).nst >= 0 && factorize(n2).nst >= 0;
+    // a CTA transforms two axis-1 lines (2 x line_threads(n1) <= 1024 threads) or up to four
+    // axis-2 lines (line_threads(n2) <= 1024); shared memory holds them and their twiddles
+    if (n1 < 1 || n2 < 1 || n1 > 4096 || n2 > 8192) return false;
+    const FftFactors f1 = factorize(n1), f2 = factorize(n2);
+    if (f1.nst < 0 || f2.nst < 0) return false;
+    const size_t cs = f64 ? sizeof(double2) : sizeof(float2);
+    const size_t s1 = cs * (size_t)(twiddle_count(f1) + 2 * padded_len((int)n1));
+    const size_t s2 = cs * (size_t)(twiddle_count(f2) + axis2_lines((int)n2) * axis2_line_stride((int)n2));
+    return s1 <= (size_t)smem_optin() && s2 <= (size_t)smem_optin();
 }
 
 void specconv_destroy(SpecConv* p) {
@@ -394,12 +446,12 @@ cudaError_t launch_axis1_forward(SpecConv* p, const void* u, int64_t pitch, int 
                                  cudaStream_t st) {
     using C = typename CxOf<T>::type;
     const int n1 = (int)p->n1, n2 = (int)p->n2;
-    const size_t smem = 2 * sizeof(C) * (size_t)n1;
+    const size_t smem = sizeof(C) * (size_t)(p->ntw1 + 2 * padded_len(n1));
     cudaError_t e = ensure_dynamic_smem((const void*)k_axis1_forward<T, MIX>, smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)((n2 + kAxis1Lines - 1) / kAxis1Lines);
     k_axis1_forward<T, MIX><<<grid, 2 * line_threads(n1), smem, st>>>(u, pitch, src, n1, n2, p->f1, (const C*)tw,
-                                                                       (C*)spec);
+                                                                       p->ntw1, (C*)spec);
     count_launch();
     return cudaGetLastError();
 }
@@ -408,12 +460,12 @@ template <typename T, bool MUL, bool MIX>
 cudaError_t launch_axis2(SpecConv* p, void* spec, const void* ks, void* out, const void* tw, cudaStream_t st) {
     using C = typename CxOf<T>::type;
     const int n1 = (int)p->n1, n2 = (int)p->n2, L = axis2_lines(n2);
-    const size_t smem = sizeof(C) * (size_t)n2 * L;
+    const size_t smem = sizeof(C) * (size_t)(p->ntw2 + L * axis2_line_stride(n2));
     cudaError_t e = ensure_dynamic_smem((const void*)k_axis2<T, MUL, MIX>, smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)((n1 / 2 + 1 + L - 1) / L);
     k_axis2<T, MUL, MIX><<<grid, L * line_threads(n2), smem, st>>>((C*)spec, (const C*)ks, (C*)out, n1, n2, p->f2,
-                                                                   (const C*)tw);
+                                                                   (const C*)tw, p->ntw2);
     count_launch();
     return cudaGetLastError();
 }
@@ -423,12 +475,12 @@ cudaError_t launch_axis1_inverse(SpecConv* p, const T* u, T* out, int64_t pe, do
                                  cudaStream_t st) {
     using C = typename CxOf<T>::type;
     const int n1 = (int)p->n1, n2 = (int)p->n2;
-    const size_t smem = 2 * sizeof(C) * (size_t)n1;
+    const size_t smem = sizeof(C) * (size_t)(p->ntw1 + 2 * padded_len(n1));
     cudaError_t e = ensure_dynamic_smem((const void*)k_axis1_inverse<T, LENIA, MIX>, smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)((n2 + kAxis1Lines - 1) / kAxis1Lines);
     k_axis1_inverse<T, LENIA, MIX><<<grid, 2 * line_threads(n1), smem, st>>>(
-        (const C*)p->spec, n1, n2, p->f1, (const C*)p->tw1, u, out, pe, (T)mu, (T)sigma, (T)dt);
+        (const C*)p->spec, n1, n2, p->f1, (const C*)p->tw1, p->ntw1, u, out, pe, (T)mu, (T)sigma, (T)dt);
     count_launch();
     return cudaGetLastError();
 }
@@ -478,33 +530,35 @@ int specconv_create(int64_t n1, int64_t n2, bool f64, const double* kpad, cudaSt
     const int64_t nc = spec_pitch((int)n1), ncell = n1 * n2;  // nc: the spectra's row pitch
     const size_t cs = f64 ? sizeof(double2) : sizeof(float2);
     // FP64 twiddles for the kernel's spectrum; the plan's own in its precision
-    const std::vector<double2> t1d = twiddles<double2>((int)n1), t2d = twiddles<double2>((int)n2);
+    p->ntw1 = twiddle_count(p->f1);
+    p->ntw2 = twiddle_count(p->f2);
+    const std::vector<double2> t1d = stage_table<double2>(p->f1), t2d = stage_table<double2>(p->f2);
     double2 *d_t1 = nullptr, *d_t2 = nullptr, *d_s = nullptr, *d_o = nullptr;
     double* d_k = nullptr;
     cudaError_t e = cudaMalloc(&p->ks, cs * (size_t)(nc * n2));
     if (e == cudaSuccess) e = cudaMalloc(&p->spec, cs * (size_t)(nc * n2));
-    if (e == cudaSuccess) e = cudaMalloc(&p->tw1, cs * (size_t)n1);
-    if (e == cudaSuccess) e = cudaMalloc(&p->tw2, cs * (size_t)n2);
-    if (e == cudaSuccess) e = cudaMalloc(&d_t1, sizeof(double2) * (size_t)n1);
-    if (e == cudaSuccess) e = cudaMalloc(&d_t2, sizeof(double2) * (size_t)n2);
+    if (e == cudaSuccess) e = cudaMalloc(&p->tw1, cs * (size_t)(p->ntw1 + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&p->tw2, cs * (size_t)(p->ntw2 + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&d_t1, sizeof(double2) * (size_t)(p->ntw1 + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&d_t2, sizeof(double2) * (size_t)(p->ntw2 + 1));
     if (e == cudaSuccess) e = cudaMalloc(&d_s, sizeof(double2) * (size_t)(nc * n2));
     if (e == cudaSuccess) e = cudaMalloc(&d_o, sizeof(double2) * (size_t)(nc * n2));
     if (e == cudaSuccess) e = cudaMalloc(&d_k, sizeof(double) * (size_t)ncell);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_t1, t1d.data(), sizeof(double2) * n1, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_t2, t2d.data(), sizeof(double2) * n2, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_t1, t1d.data(), sizeof(double2) * p->ntw1, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_t2, t2d.data(), sizeof(double2) * p->ntw2, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_k, kpad, sizeof(double) * ncell, cudaMemcpyHostToDevice, st);
     std::vector<float2> t1f, t2f;
     if (e == cudaSuccess) {
         if (f64) {
-            e = cudaMemcpyAsync(p->tw1, t1d.data(), sizeof(double2) * n1, cudaMemcpyHostToDevice, st);
+            e = cudaMemcpyAsync(p->tw1, t1d.data(), sizeof(double2) * p->ntw1, cudaMemcpyHostToDevice, st);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(p->tw2, t2d.data(), sizeof(double2) * n2, cudaMemcpyHostToDevice, st);
+                e = cudaMemcpyAsync(p->tw2, t2d.data(), sizeof(double2) * p->ntw2, cudaMemcpyHostToDevice, st);
         } else {
-            t1f = twiddles<float2>((int)n1);
-            t2f = twiddles<float2>((int)n2);
-            e = cudaMemcpyAsync(p->tw1, t1f.data(), sizeof(float2) * n1, cudaMemcpyHostToDevice, st);
+            t1f = stage_table<float2>(p->f1);
+            t2f = stage_table<float2>(p->f2);
+            e = cudaMemcpyAsync(p->tw1, t1f.data(), sizeof(float2) * p->ntw1, cudaMemcpyHostToDevice, st);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(p->tw2, t2f.data(), sizeof(float2) * n2, cudaMemcpyHostToDevice, st);
+                e = cudaMemcpyAsync(p->tw2, t2f.data(), sizeof(float2) * p->ntw2, cudaMemcpyHostToDevice, st);
         }
     }
     if (e == cudaSuccess) e = run_forward<double>(p, d_k, n1, kSpecReal, d_t1, d_t2, d_s, nullptr, d_o, false, st);
