@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-saves", action="store_true", help="skip the save-path measurement")
     ap.add_argument("--no-sparse", action="store_true", help="skip the active-tile measurement")
+    ap.add_argument("--no-lenia", action="store_true", help="skip the Lenia measurement")
     ap.add_argument("--large", default=None, help="ensemble case: 'min_cells,steps_per_pass' of the batched "
                     "large-instance passes (0,1: none)")
     ap.add_argument("--side-range", default="", help="ensemble case: keep the instances with lo <= side < hi "
@@ -429,6 +430,52 @@ def bench_sparse(ca):
     out["equal"] = bool(np.array_equal(finals["dense"], finals["active_tiles"]))
     out["speedup"] = out["dense"]["ms"] / out["active_tiles"]["ms"]
     out["config"] = f"Life B3/S23 on a {n}^2 torus, {m}^2 soup in the centre, {steps} steps"
+    return out
+
+
+FIRE_FMAHEAVY_CYCLES_PER_WARP = 81.33  # k_fire: fmaheavy pipe cycles per 32 cell-updates (ncu)
+
+
+def bench_lenia(capi, lib, reps: int = 3):
+    """Lenia in Float32 on a 2048^2 torus (R = 13, one bump, mu = 0.15, sigma = 0.015, dt = 0.1,
+    Uniform[0,1] in the central 256^2 patch from seed 4), 100 steps, by the direct field and by
+    the FFT field: time per step with CUDA events on the handle's stream, the best of `reps`
+    runs from the initial state."""
+    import torch
+    n, steps = 2048, 100
+    rng = np.random.default_rng(4)
+    u0 = np.zeros((n, n), np.float32)
+    c = n // 2
+    u0[c - 128:c + 128, c - 128:c + 128] = rng.random((256, 256)).astype(np.float32)
+    a = np.asfortranarray(u0)
+    stream = torch.cuda.Stream()
+    out = {"workload": "Lenia Float32, 2048^2 torus, R = 13, 100 steps from a 256^2 soup", "paths": {}}
+    for name, method in (("direct", capi.DIRECT), ("fft", capi.FFT)):
+        d = capi.Desc()
+        d.rule, d.lenia_R, d.lenia_npeaks, d.lenia_peaks[0] = capi.RULE_LENIA, 13, 1, 1.0
+        d.lenia_mu, d.lenia_sigma, d.lenia_dt, d.lenia_method = 0.15, 0.015, 0.1, method
+        d.n1 = d.n2 = n
+        h = ctypes.c_void_p()
+        capi.check(lib.gbca_create(ctypes.byref(d), ctypes.byref(h)))
+        capi.check(lib.gbca_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+        best = None
+        for r in range(reps + 1):  # the first run warms up
+            capi.check(lib.gbca_set_state(h, a.ctypes.data, a.nbytes))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            capi.check(lib.gbca_advance(h, 0, steps, None, 0))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r > 0:
+                ms = e0.elapsed_time(e1) / steps
+                best = ms if best is None else min(best, ms)
+        lib.gbca_destroy(h)
+        tflops = n * n * 516 * 2 / (best * 1e-3) / 1e12
+        out["paths"][name] = {"ms_per_step": best, "gcell_updates_s": n * n / (best * 1e-3) / 1e9,
+                              "direct_equivalent_tflops": tflops}
+    out["fp32_fma_peak_tflops"] = 152 * 128 * 2 * 2.07e9 / 1e12
+    out["paths"]["direct"]["frac_of_fp32_fma_peak"] = out["paths"]["direct"]["direct_equivalent_tflops"] / \
+        out["fp32_fma_peak_tflops"]
     return out
 
 
@@ -813,6 +860,13 @@ def main():
     fire_draws = parts["fire"]["gcell_updates_s"] * 1e9
     philox_roof = {"kernel": "k_fire", "achieved": fire_draws / 1e9, "peak": rate.value / 1e9, "unit": "Gdraws/s",
                    "frac": fire_draws / rate.value, "peak_source": "measured in this run (draw-only kernel)"}
+    # the kernel's own pipe roof: its fmaheavy cycles per 32 cell-updates (ncu, profiles/
+    # k_fire_forest_fire_16384.md) on every SM sub-partition at the SM clock seen in the timed region
+    sm_mhz = clocks.summary().get("sm_mhz") or 2070.0
+    pipe_roof = 32 * 4 * 152 * sm_mhz * 1e6 / FIRE_FMAHEAVY_CYCLES_PER_WARP / 1e9
+    philox_roof["pipe_roof"] = {"pipe": "fmaheavy (integer multiplies)", "cycles_per_32_cells": FIRE_FMAHEAVY_CYCLES_PER_WARP,
+                                "gcell_updates_s": pipe_roof, "frac": fire_draws / 1e9 / pipe_roof,
+                                "source": "instruction mix from ncu pipe counters x SM clock"}
 
     # ---- end to end through the C ABI with host buffers
     host_in = [torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory() for a in (ltl0, fire0)]
@@ -850,6 +904,7 @@ def main():
         batched = bench_batched(capi, lib, max(1, args.warmup // 2), max(1, args.steps // 2))
     saves = bench_saves(ca) if rank == 0 and not args.no_saves else None
     sparse = bench_sparse(ca) if rank == 0 and not args.no_sparse else None
+    lenia = bench_lenia(capi, lib) if rank == 0 and not args.no_lenia else None
     served = bench_served(capi, lib) if rank == 0 and not args.no_serve else None
 
     cpu = None
@@ -869,7 +924,7 @@ def main():
                                  "335 MB of initial states"},
                 "roofline": roofline, "philox_roof": philox_roof, "parts": parts, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks.summary(), "cpu_baseline": cpu, "batched": batched, "served": served,
-                "saves": saves, "sparse": sparse}
+                "saves": saves, "sparse": sparse, "lenia": lenia}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

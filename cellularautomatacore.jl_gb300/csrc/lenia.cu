@@ -423,13 +423,16 @@ int advance_t(LeniaPlan* P, int64_t nsteps, cudaStream_t st, int* cur, void* con
     using C = typename F::C;
     const T mu = (T)P->d.lenia_mu, sigma = (T)P->d.lenia_sigma, dt = (T)P->d.lenia_dt;
     const int b1 = P->d.boundary[0], b2 = P->d.boundary[1];
+    if (P->sc) {  // this library's transforms: the whole run, steps chained
+        const cudaError_t e = specconv_lenia_run(P->sc, bufs, cur, nsteps, P->pe, P->d.lenia_mu, P->d.lenia_sigma,
+                                                 P->d.lenia_dt, st);
+        return e == cudaSuccess ? GBCA_OK : fail_to(err, GBCA_ERR_CUDA, cudaGetErrorString(e));
+    }
     for (int64_t s = 0; s < nsteps; ++s) {
         const T* u = (const T*)bufs[*cur];
         T* out = (T*)bufs[*cur ^ 1];
         cudaError_t e = cudaSuccess;
-        if (P->sc) {
-            e = specconv_lenia_step(P->sc, u, out, P->pe, P->d.lenia_mu, P->d.lenia_sigma, P->d.lenia_dt, st);
-        } else if (P->fft) {
+        if (P->fft) {
             const int64_t nc = P->n1 / 2 + 1;
             if (cufftSetStream(P->fwd, st) != CUFFT_SUCCESS || cufftSetStream(P->inv, st) != CUFFT_SUCCESS ||
                 F::fwd(P->fwd, u, (C*)P->spec) != CUFFT_SUCCESS)

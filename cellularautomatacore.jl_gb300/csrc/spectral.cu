@@ -244,6 +244,18 @@ __host__ __device__ inline int axis2_lines(int n2) {
 // 16, so that one row's four frequencies land in different banks.
 __host__ __device__ inline int axis2_line_stride(int n2) { return (padded_len(n2) + 15) / 16 * 16 + 4; }
 
+// A transformed complex line (Z = DFT(line ya + i line ya + 1), padded slots) split into the two
+// lines' half spectra, stored as rows ya and ya + 1 of spec (row pitch ncp).
+template <typename T, typename C>
+__device__ __forceinline__ void split_rows(const C* a, int n1, C* ra, int ncp, bool h0, bool h1, int t, int TL) {
+    for (int k = t; k <= n1 / 2; k += TL) {
+        const C zk = a[pad16(k)], zm = a[pad16(k == 0 ? 0 : n1 - k)];
+        // zc = conj(Z[n1 - k]); Xa = (Zk + zc) / 2, Xb = (Zk - zc) / (2 i)
+        if (h0) ra[k] = C{T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y)};
+        if (h1) ra[ncp + k] = C{T(0.5) * (zk.y + zm.y), T(0.5) * (zm.x - zk.x)};
+    }
+}
+
 // Step 1: the four lines along axis 1 into rows y of spec.
 template <typename T, bool MIX>
 __global__ void __launch_bounds__(kFftMaxThreads, 1)
@@ -265,13 +277,7 @@ __global__ void __launch_bounds__(kFftMaxThreads, 1)
     __syncthreads();
     fft_line<-1, MIX>(a, f, tws, t, TL);
     const int ncp = spec_pitch(n1);
-    C* ra = spec + ya * ncp;
-    for (int k = t; k <= n1 / 2; k += TL) {
-        const C zk = a[pad16(k)], zm = a[pad16(k == 0 ? 0 : n1 - k)];
-        // zc = conj(Z[n1 - k]); Xa = (Zk + zc) / 2, Xb = (Zk - zc) / (2 i)
-        if (h0) ra[k] = C{T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y)};
-        if (h1) ra[ncp + k] = C{T(0.5) * (zk.y + zm.y), T(0.5) * (zm.x - zk.x)};
-    }
+    split_rows<T>(a, n1, spec + ya * ncp, ncp, h0, h1, t, TL);
 }
 
 // Step 2: frequencies k0 .. k0 + L - 1 (k0 = L blockIdx.x, L = axis2_lines(n2)) along axis 2,
@@ -330,11 +336,13 @@ __device__ __forceinline__ T growth(T u, T U, T mu, T sigma, T dt) {
 // Step 3: four lines back along axis 1. Each complex line reads its two lines' rows of half
 // spectra, made Hermitian (the imaginary parts of frequencies 0 and n1/2 dropped), as Fa + i Fb
 // over all n1 frequencies; its inverse transform holds the two real fields. Then LENIA:
-// out = growth(u, U) (pitch pe); else out = U (packed).
+// out = growth(u, U) (pitch pe), and with `next` the new state's lines are transformed at once
+// (step 1 of the next step, on the same lines, in the same shared memory) into the same rows of
+// spec; else out = U (packed).
 template <typename T, bool LENIA, bool MIX>
-__global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis1_inverse(const typename CxOf<T>::type* __restrict__ spec, int n1, int n2, FftFactors f,
+__global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis1_inverse(typename CxOf<T>::type* __restrict__ spec, int n1, int n2, FftFactors f,
                                 const typename CxOf<T>::type* __restrict__ tw, int ntw, const T* __restrict__ u,
-                                T* __restrict__ out, int64_t pe, T mu, T sigma, T dt) {
+                                T* __restrict__ out, int64_t pe, T mu, T sigma, T dt, bool next) {
     using C = typename CxOf<T>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     C* tws = (C*)smem;
@@ -368,12 +376,20 @@ __global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis1_inverse(const typen
     for (int x = t; x < n1; x += TL) {
         const C v = a[pad16(x)];
         if (LENIA) {
-            if (h0) out[x + ya * pe] = growth<T>(u[x + ya * pe], v.x, mu, sigma, dt);
-            if (h1) out[x + (ya + 1) * pe] = growth<T>(u[x + (ya + 1) * pe], v.y, mu, sigma, dt);
+            const T g0 = h0 ? growth<T>(u[x + ya * pe], v.x, mu, sigma, dt) : T(0);
+            const T g1 = h1 ? growth<T>(u[x + (ya + 1) * pe], v.y, mu, sigma, dt) : T(0);
+            if (h0) out[x + ya * pe] = g0;
+            if (h1) out[x + (ya + 1) * pe] = g1;
+            a[pad16(x)] = C{g0, g1};  // this thread's own slot: the next step's input line
         } else {
             if (h0) out[x + ya * n1] = v.x;
             if (h1) out[x + (ya + 1) * n1] = v.y;
         }
+    }
+    if (LENIA && next) {  // uniform over the CTA
+        __syncthreads();
+        fft_line<-1, MIX>(a, f, tws, t, TL);
+        split_rows<T>(a, n1, spec + ya * ncp, ncp, h0, h1, t, TL);
     }
 }
 
@@ -472,7 +488,7 @@ cudaError_t launch_axis2(SpecConv* p, void* spec, const void* ks, void* out, con
 
 template <typename T, bool LENIA, bool MIX>
 cudaError_t launch_axis1_inverse(SpecConv* p, const T* u, T* out, int64_t pe, double mu, double sigma, double dt,
-                                 cudaStream_t st) {
+                                 bool next, cudaStream_t st) {
     using C = typename CxOf<T>::type;
     const int n1 = (int)p->n1, n2 = (int)p->n2;
     const size_t smem = sizeof(C) * (size_t)(p->ntw1 + 2 * padded_len(n1));
@@ -480,36 +496,57 @@ cudaError_t launch_axis1_inverse(SpecConv* p, const T* u, T* out, int64_t pe, do
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)((n2 + kAxis1Lines - 1) / kAxis1Lines);
     k_axis1_inverse<T, LENIA, MIX><<<grid, 2 * line_threads(n1), smem, st>>>(
-        (const C*)p->spec, n1, n2, p->f1, (const C*)p->tw1, p->ntw1, u, out, pe, (T)mu, (T)sigma, (T)dt);
+        (C*)p->spec, n1, n2, p->f1, (const C*)p->tw1, p->ntw1, u, out, pe, (T)mu, (T)sigma, (T)dt, next);
     count_launch();
     return cudaGetLastError();
 }
 
-// Steps 1 and 2: with mul, the spectral product and the inverse along axis 2 in spec; without,
-// the forward spectrum into out.
+// Step 1 alone: the lines of u along axis 1 into spec.
 template <typename T>
-cudaError_t run_forward(SpecConv* p, const void* u, int64_t pitch, int src, const void* tw1, const void* tw2,
-                        void* spec, const void* ks, void* out, bool mul, cudaStream_t st) {
-    const bool m1 = !pow2(p->n1), m2 = !pow2(p->n2);
-    cudaError_t e = m1 ? launch_axis1_forward<T, true>(p, u, pitch, src, tw1, spec, st)
-                       : launch_axis1_forward<T, false>(p, u, pitch, src, tw1, spec, st);
-    if (e != cudaSuccess) return e;
+cudaError_t run_axis1(SpecConv* p, const void* u, int64_t pitch, int src, const void* tw1, void* spec, cudaStream_t st) {
+    return pow2(p->n1) ? launch_axis1_forward<T, false>(p, u, pitch, src, tw1, spec, st)
+                       : launch_axis1_forward<T, true>(p, u, pitch, src, tw1, spec, st);
+}
+
+// Step 2: with mul, the spectral product and the inverse along axis 2 in spec; without, the
+// forward spectrum into out.
+template <typename T>
+cudaError_t run_axis2(SpecConv* p, void* spec, const void* ks, void* out, const void* tw2, bool mul, cudaStream_t st) {
+    const bool m2 = !pow2(p->n2);
     if (mul) return m2 ? launch_axis2<T, true, true>(p, spec, ks, nullptr, tw2, st)
                        : launch_axis2<T, true, false>(p, spec, ks, nullptr, tw2, st);
     return m2 ? launch_axis2<T, false, true>(p, spec, nullptr, out, tw2, st)
               : launch_axis2<T, false, false>(p, spec, nullptr, out, tw2, st);
 }
 
-// Step 3: Lenia's growth into out (pitch pe), or the field into out (packed).
+// Step 3: Lenia's growth into out (pitch pe; with next, the new state's step 1 too), or the
+// field into out (packed).
 template <typename T>
 cudaError_t run_inverse(SpecConv* p, const T* u, T* out, int64_t pe, bool lenia, double mu, double sigma, double dt,
-                        cudaStream_t st) {
+                        bool next, cudaStream_t st) {
     const bool m1 = !pow2(p->n1);
     if (lenia)
-        return m1 ? launch_axis1_inverse<T, true, true>(p, u, out, pe, mu, sigma, dt, st)
-                  : launch_axis1_inverse<T, true, false>(p, u, out, pe, mu, sigma, dt, st);
-    return m1 ? launch_axis1_inverse<T, false, true>(p, u, out, pe, mu, sigma, dt, st)
-              : launch_axis1_inverse<T, false, false>(p, u, out, pe, mu, sigma, dt, st);
+        return m1 ? launch_axis1_inverse<T, true, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                  : launch_axis1_inverse<T, true, false>(p, u, out, pe, mu, sigma, dt, next, st);
+    return m1 ? launch_axis1_inverse<T, false, true>(p, u, out, pe, mu, sigma, dt, false, st)
+              : launch_axis1_inverse<T, false, false>(p, u, out, pe, mu, sigma, dt, false, st);
+}
+
+// nsteps Lenia steps: step 1 of the first, then per step the axis-2 product and the inverse
+// with the growth, which also runs step 1 of the following step (all but the last).
+template <typename T>
+cudaError_t lenia_run(SpecConv* p, void* const bufs[2], int* cur, int64_t nsteps, int64_t pe, double mu,
+                      double sigma, double dt, cudaStream_t st) {
+    if (nsteps <= 0) return cudaSuccess;
+    cudaError_t e = run_axis1<T>(p, bufs[*cur], pe, kSpecReal, p->tw1, p->spec, st);
+    for (int64_t s = 0; s < nsteps && e == cudaSuccess; ++s) {
+        e = run_axis2<T>(p, p->spec, p->ks, nullptr, p->tw2, true, st);
+        if (e == cudaSuccess)
+            e = run_inverse<T>(p, (const T*)bufs[*cur], (T*)bufs[*cur ^ 1], pe, true, mu, sigma, dt, s + 1 < nsteps,
+                               st);
+        if (e == cudaSuccess) *cur ^= 1;
+    }
+    return e;
 }
 
 }  // namespace
@@ -561,7 +598,8 @@ int specconv_create(int64_t n1, int64_t n2, bool f64, const double* kpad, cudaSt
                 e = cudaMemcpyAsync(p->tw2, t2f.data(), sizeof(float2) * p->ntw2, cudaMemcpyHostToDevice, st);
         }
     }
-    if (e == cudaSuccess) e = run_forward<double>(p, d_k, n1, kSpecReal, d_t1, d_t2, d_s, nullptr, d_o, false, st);
+    if (e == cudaSuccess) e = run_axis1<double>(p, d_k, n1, kSpecReal, d_t1, d_s, st);
+    if (e == cudaSuccess) e = run_axis2<double>(p, d_s, nullptr, d_o, d_t2, false, st);
     if (e == cudaSuccess) {
         const double scale = 1.0 / (double)ncell;
         if (f64) k_finish_kspec<double2><<<256, 256, 0, st>>>(d_o, (double2*)p->ks, nc * n2, scale);
@@ -586,28 +624,23 @@ int specconv_create(int64_t n1, int64_t n2, bool f64, const double* kpad, cudaSt
     return GBCA_OK;
 }
 
-cudaError_t specconv_lenia_step(SpecConv* p, const void* u, void* out, int64_t pe, double mu, double sigma, double dt,
-                                cudaStream_t st) {
-    cudaError_t e;
-    if (p->f64) {
-        e = run_forward<double>(p, u, pe, kSpecReal, p->tw1, p->tw2, p->spec, p->ks, nullptr, true, st);
-        if (e == cudaSuccess) e = run_inverse<double>(p, (const double*)u, (double*)out, pe, true, mu, sigma, dt, st);
-    } else {
-        e = run_forward<float>(p, u, pe, kSpecReal, p->tw1, p->tw2, p->spec, p->ks, nullptr, true, st);
-        if (e == cudaSuccess) e = run_inverse<float>(p, (const float*)u, (float*)out, pe, true, mu, sigma, dt, st);
-    }
-    return e;
+cudaError_t specconv_lenia_run(SpecConv* p, void* const bufs[2], int* cur, int64_t nsteps, int64_t pe, double mu,
+                               double sigma, double dt, cudaStream_t st) {
+    return p->f64 ? lenia_run<double>(p, bufs, cur, nsteps, pe, mu, sigma, dt, st)
+                  : lenia_run<float>(p, bufs, cur, nsteps, pe, mu, sigma, dt, st);
 }
 
 cudaError_t specconv_field(SpecConv* p, const int8_t* u, int64_t pitch, SpecSource src, void* field,
                            cudaStream_t st) {
     cudaError_t e;
     if (p->f64) {
-        e = run_forward<double>(p, u, pitch, src, p->tw1, p->tw2, p->spec, p->ks, nullptr, true, st);
-        if (e == cudaSuccess) e = run_inverse<double>(p, nullptr, (double*)field, 0, false, 0, 0, 0, st);
+        e = run_axis1<double>(p, u, pitch, src, p->tw1, p->spec, st);
+        if (e == cudaSuccess) e = run_axis2<double>(p, p->spec, p->ks, nullptr, p->tw2, true, st);
+        if (e == cudaSuccess) e = run_inverse<double>(p, nullptr, (double*)field, 0, false, 0, 0, 0, false, st);
     } else {
-        e = run_forward<float>(p, u, pitch, src, p->tw1, p->tw2, p->spec, p->ks, nullptr, true, st);
-        if (e == cudaSuccess) e = run_inverse<float>(p, nullptr, (float*)field, 0, false, 0, 0, 0, st);
+        e = run_axis1<float>(p, u, pitch, src, p->tw1, p->spec, st);
+        if (e == cudaSuccess) e = run_axis2<float>(p, p->spec, p->ks, nullptr, p->tw2, true, st);
+        if (e == cudaSuccess) e = run_inverse<float>(p, nullptr, (float*)field, 0, false, 0, 0, 0, false, st);
     }
     return e;
 }

@@ -24,10 +24,11 @@ int specconv_create(int64_t n1, int64_t n2, bool f64, const double* kpad, cudaSt
                     std::string& err);
 void specconv_destroy(SpecConv* p);
 
-// One Lenia step from state u (pitch pe elements) into out: the field by the plan, then
-// clamp(u + dt (2 exp(-(U - mu)^2 / (2 sigma^2)) - 1), 0, 1) (src/lenia.jl:42-47).
-cudaError_t specconv_lenia_step(SpecConv* p, const void* u, void* out, int64_t pe, double mu, double sigma, double dt,
-                                cudaStream_t st);
+// nsteps Lenia steps between bufs[*cur] and bufs[*cur ^ 1] (pitch pe elements), *cur updated:
+// each the field by the plan, then clamp(u + dt (2 exp(-(U - mu)^2 / (2 sigma^2)) - 1), 0, 1)
+// (src/lenia.jl:42-47); a step's last launch also transforms the new state for the next.
+cudaError_t specconv_lenia_run(SpecConv* p, void* const bufs[2], int* cur, int64_t nsteps, int64_t pe, double mu,
+                               double sigma, double dt, cudaStream_t st);
 
 // The field of an Int8 state (pitch bytes between columns) into `field` (n1 x n2 packed, the
 // plan's precision).

@@ -454,6 +454,34 @@ function fetch_snapshot(st::GB300State{T}, ticket::Integer) where {T}
     return u
 end
 
+# ------------------------------------------------------------------ slabs of one lattice
+
+"""
+    set_slab!(st, col0, n2_global)
+
+Places the state's n1 x n2 lattice as columns col0 .. col0 + n2 - 1 (mod n2_global) of a lattice
+of n2_global columns: cell ids, hence draws, and Checkerboard parities become the larger
+lattice's (src/backends.jl:457-479 splits that lattice among threads; here among ranks). The
+caller pads each rank's slab with h = r K gates columns on each side and refreshes them from its
+neighbours every K steps (columns are contiguous in `device_state`'s buffer).
+"""
+set_slab!(st::GB300State, col0::Integer, n2_global::Integer) =
+    check(ccall((:gbca_set_slab, libgbca), Cint, (Ptr{Cvoid}, Int64, Int64), st.handle, col0, n2_global))
+
+"""
+    slab_sums(st, j_lo, j_hi) -> Vector{Int64}
+
+The exact integer sums behind state_counts and morans_i (src/measures.jl:14-20,91-107) over
+columns j_lo:j_hi-1 (0-based) of the current state: 256 value counts, then S, S2, P, Q, W. Summed
+over the ranks' owned columns (an MPI Allreduce), they are the whole lattice's.
+"""
+function slab_sums(st::GB300State{Int8}, j_lo::Integer, j_hi::Integer)
+    flush!(st)
+    sums = zeros(Int64, 261)
+    check(ccall((:gbca_slab_sums, libgbca), Cint, (Ptr{Cvoid}, Int64, Int64, Ptr{Int64}), st.handle, j_lo, j_hi, sums))
+    return sums
+end
+
 # ------------------------------------------------------------------ batched ensembles
 
 """
