@@ -198,6 +198,11 @@ class DeviceSlab:
         """Work queued inside runs on the slab's stream."""
         return self.torch.cuda.stream(self.stream)
 
+    def set_state_device(self, cols) -> None:
+        """The padded slab's state from a device tensor holding its width columns of n1 bytes
+        (contiguous), queued on the slab's stream."""
+        capi.check(capi.lib().gbca_set_state_device(self.handle, ctypes.c_void_p(cols.data_ptr()), self.n1))
+
     def step(self, t: int, k: int, params) -> None:
         vals = tuple(params or ())
         arr = (ctypes.c_double * max(1, len(vals)))(*vals)
