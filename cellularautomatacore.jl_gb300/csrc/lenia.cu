@@ -10,9 +10,10 @@
 // cells in shared memory (periodic / reflecting / Constant(0) through the boundary map);
 // each thread computes 16 consecutive cells of a row, sliding a 16+2R register window
 // over the kernel rows, so each shared-memory value feeds up to 16 fused multiply-adds.
-// R = 13 (the standard Lenia radius) is specialised with the disk taps unrolled at
-// compile time, the weights in the parameter bank, and the rows dj and -dj (equal weights)
-// summed before the multiply-adds; other radii loop over a tap list.
+// R = 13 (the standard Lenia radius) is specialised: the rows dj and -dj (equal weights) summed
+// before the multiply-adds, the taps of a row unrolled at compile time, rows of equal extent
+// sharing one loop body (a quarter of the code of a fully unrolled disk), the weights in the
+// parameter bank; other radii loop over a tap list.
 //
 // FFT field (periodic lattices, the FFTW extension's convention
 // ext/CellularAutomataCoreFFTWExt.jl:17-30): U = irfft(rfft(u) .* conj(rfft(kpad))) with
@@ -94,37 +95,19 @@ constexpr int lenia13_pitch() {
     return sp;
 }
 
-// R = 13. The Lenia kernel depends on the distance only, so rows dj and -dj carry the same
-// weights: each thread adds the two rows' windows first (one add per window cell) and then
-// runs one fused multiply-add per tap of the pair for each of its 16 cells, 271 per cell for
-// the 516 taps. Windows arrive by 16-byte shared-memory loads. Thread layout: the eight lanes
-// of a quarter-warp take eight consecutive output rows at the same 16 columns (lanes 8q..8q+7,
-// column block 4 (warp / 4) + q), so with lenia13_pitch each of their loads is conflict-free.
-template <typename T>
-__global__ void __launch_bounds__(256) k_lenia13(const T* __restrict__ u, T* __restrict__ out, int64_t n1, int64_t n2,
-                                                 int64_t pe, int b1, int b2, Box13<T> wb, T mu, T sigma, T dt) {
-    extern __shared__ __align__(16) unsigned char lsm[];
-    T* s = (T*)lsm;
-    constexpr int sx = kDirTX + 2 * kR13, sy = kDirTY + 2 * kR13;
-    constexpr int sp = lenia13_pitch<T>();
-    constexpr int V = 16 / sizeof(T);          // elements per 16-byte load
-    constexpr int W = kDirCells + 2 * kR13;    // window: cells x - R .. x + 15 + R
-    constexpr int WL = (W + V - 1) / V * V;    // loaded window
-    static_assert(kDirTX / kDirCells == 8 && kDirTY == 32, "thread layout: 8 column blocks x 32 rows");
-    const int64_t X0 = (int64_t)blockIdx.x * kDirTX, Y0 = (int64_t)blockIdx.y * kDirTY;
-    load_tile<T>(u, n1, n2, pe, b1, b2, X0 - kR13, Y0 - kR13, sx, sy, sp, s);
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tx = 4 * (warp >> 2) + (lane >> 3), ty = 8 * (warp & 3) + (lane & 7);
-    const int lx0 = tx * kDirCells;                // local x of the first output (tile coords)
-    const T* centre = s + (ty + kR13) * sp + lx0;  // the thread's row, from cell lx0 - R
-    T acc[kDirCells];
-#pragma unroll
-    for (int k = 0; k < kDirCells; ++k) acc[k] = T(0);
-#pragma unroll
-    for (int dj = 0; dj <= kR13; ++dj) {
+// Rows dj = D0..D1 of the R = 13 disk (and -dj), whose taps all have |di| <= EXT (di != 0 when
+// dj = 0), into the thread's 16 accumulators: the two rows' 16-byte window loads, their sum, then
+// one multiply-add per tap and cell, the weight read from the parameter bank by dj. A loop over
+// dj (not unrolled) when D1 > D0, so rows of one extent share their code.
+template <typename T, int EXT, int D0, int D1>
+__device__ __forceinline__ void lenia13_rows(const T* centre, int sp, const Box13<T>& wb, T* acc) {
+    constexpr int V = 16 / sizeof(T);
+    constexpr int W = kDirCells + 2 * kR13;
+    constexpr int WL = (W + V - 1) / V * V;
+#pragma unroll 1
+    for (int dj = D0; dj <= D1; ++dj) {
         T win[WL];
-        if (dj == 0) {
+        if (D0 == 0) {
 #pragma unroll
             for (int k = 0; k < WL; k += V) load16<T>(centre + k, win + k);
         } else {
@@ -137,14 +120,51 @@ __global__ void __launch_bounds__(256) k_lenia13(const T* __restrict__ u, T* __r
 #pragma unroll
             for (int k = 0; k < W; ++k) win[k] += lo[k];
         }
+        const T* wrow = wb.w + (dj + kR13) * kBox13 + kR13;
 #pragma unroll
-        for (int di = -kR13; di <= kR13; ++di) {
-            if (!in_disk13(di, dj)) continue;
-            const T w = wb.w[(dj + kR13) * kBox13 + (di + kR13)];
+        for (int di = -EXT; di <= EXT; ++di) {
+            if (D0 == 0 && di == 0) continue;
+            const T w = wrow[di];
 #pragma unroll
             for (int k = 0; k < kDirCells; ++k) acc[k] = fma(w, win[k + di + kR13], acc[k]);
         }
     }
+}
+
+// R = 13. The Lenia kernel depends on the distance only, so rows dj and -dj carry the same
+// weights: each thread adds the two rows' windows first (one add per window cell) and then
+// runs one fused multiply-add per tap of the pair for each of its 16 cells, 271 per cell for
+// the 516 taps (lenia13_rows, by groups of rows of one extent). Windows arrive by 16-byte shared-memory loads. Thread layout: the eight lanes
+// of a quarter-warp take eight consecutive output rows at the same 16 columns (lanes 8q..8q+7,
+// column block 4 (warp / 4) + q), so with lenia13_pitch each of their loads is conflict-free.
+template <typename T>
+__global__ void __launch_bounds__(256) k_lenia13(const T* __restrict__ u, T* __restrict__ out, int64_t n1, int64_t n2,
+                                                 int64_t pe, int b1, int b2, Box13<T> wb, T mu, T sigma, T dt) {
+    extern __shared__ __align__(16) unsigned char lsm[];
+    T* s = (T*)lsm;
+    constexpr int sx = kDirTX + 2 * kR13, sy = kDirTY + 2 * kR13;
+    constexpr int sp = lenia13_pitch<T>();
+    static_assert(kDirTX / kDirCells == 8 && kDirTY == 32, "thread layout: 8 column blocks x 32 rows");
+    const int64_t X0 = (int64_t)blockIdx.x * kDirTX, Y0 = (int64_t)blockIdx.y * kDirTY;
+    load_tile<T>(u, n1, n2, pe, b1, b2, X0 - kR13, Y0 - kR13, sx, sy, sp, s);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tx = 4 * (warp >> 2) + (lane >> 3), ty = 8 * (warp & 3) + (lane & 7);
+    const int lx0 = tx * kDirCells;                // local x of the first output (tile coords)
+    const T* centre = s + (ty + kR13) * sp + lx0;  // the thread's row, from cell lx0 - R
+    T acc[kDirCells];
+#pragma unroll
+    for (int k = 0; k < kDirCells; ++k) acc[k] = T(0);
+    // rows with the same tap extent |di| <= EXT share one loop body: dj = 1..4 (12), 5..6 (11),
+    // 7..8 (10); the weights of the pair come from the parameter bank by dj
+    lenia13_rows<T, 12, 0, 0>(centre, sp, wb, acc);
+    lenia13_rows<T, 12, 1, 4>(centre, sp, wb, acc);
+    lenia13_rows<T, 11, 5, 6>(centre, sp, wb, acc);
+    lenia13_rows<T, 10, 7, 8>(centre, sp, wb, acc);
+    lenia13_rows<T, 9, 9, 9>(centre, sp, wb, acc);
+    lenia13_rows<T, 8, 10, 10>(centre, sp, wb, acc);
+    lenia13_rows<T, 6, 11, 11>(centre, sp, wb, acc);
+    lenia13_rows<T, 4, 12, 12>(centre, sp, wb, acc);
     const int64_t gy = Y0 + ty;
     if (gy >= n2) return;
 #pragma unroll
