@@ -6,20 +6,21 @@
 // (src/environment.jl:63). Each step is
 //     u' = clamp(u + dt * (2 exp(-(U - mu)^2 / (2 sigma^2)) - 1), 0, 1).
 //
-// Direct field: a fused kernel per step. The CTA stages a tile of u plus a halo of R
+// Direct field: a fused kernel per step. A CTA stages a tile of u plus a halo of R
 // cells in shared memory (periodic / reflecting / Constant(0) through the boundary map);
 // each thread computes 16 consecutive cells of a row, sliding a 16+2R register window
 // over the kernel rows, so each shared-memory value feeds up to 16 fused multiply-adds.
 // R = 13 (the standard Lenia radius) is specialised: the rows dj and -dj (equal weights) summed
 // before the multiply-adds, the taps of a row unrolled at compile time, rows of equal extent
 // sharing one loop body (a quarter of the code of a fully unrolled disk), the weights in the
-// parameter bank; other radii loop over a tap list.
+// parameter bank, and the kernel persistent: each CTA stages its next tile by cp.async into a
+// second buffer while it computes the current one; other radii loop over a tap list.
 //
 // FFT field (periodic lattices, the FFTW extension's convention
 // ext/CellularAutomataCoreFFTWExt.jl:17-30): U = irfft(rfft(u) .* conj(rfft(kpad))) with
 // kpad the kernel wrapped onto the lattice. Sides that are products of 2, 3 and 5 run this
-// library's own transforms with the growth fused into the last one (spectral.cu: three launches
-// a step); other sides run cuFFT (a library call) with this file's spectral product and growth.
+// library's own transforms with the growth fused into the last one (spectral.cu: two launches a
+// step in a run of steps); other sides run cuFFT (a library call) with this file's spectral product and growth.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -134,20 +135,15 @@ __device__ __forceinline__ void lenia13_rows(const T* centre, int sp, const Box1
 // R = 13. The Lenia kernel depends on the distance only, so rows dj and -dj carry the same
 // weights: each thread adds the two rows' windows first (one add per window cell) and then
 // runs one fused multiply-add per tap of the pair for each of its 16 cells, 271 per cell for
-// the 516 taps (lenia13_rows, by groups of rows of one extent). Windows arrive by 16-byte shared-memory loads. Thread layout: the eight lanes
-// of a quarter-warp take eight consecutive output rows at the same 16 columns (lanes 8q..8q+7,
-// column block 4 (warp / 4) + q), so with lenia13_pitch each of their loads is conflict-free.
+// the 516 taps (lenia13_rows, by groups of rows of one extent). Windows arrive by 16-byte
+// shared-memory loads. Thread layout: the eight lanes of a quarter-warp take eight consecutive
+// output rows at the same 16 columns (lanes 8q..8q+7, column block 4 (warp / 4) + q), so with
+// lenia13_pitch each of their loads is conflict-free. The tile (X0, Y0) is staged in s.
 template <typename T>
-__global__ void __launch_bounds__(256) k_lenia13(const T* __restrict__ u, T* __restrict__ out, int64_t n1, int64_t n2,
-                                                 int64_t pe, int b1, int b2, Box13<T> wb, T mu, T sigma, T dt) {
-    extern __shared__ __align__(16) unsigned char lsm[];
-    T* s = (T*)lsm;
-    constexpr int sx = kDirTX + 2 * kR13, sy = kDirTY + 2 * kR13;
+__device__ __forceinline__ void lenia13_tile(const T* s, T* __restrict__ out, int64_t n1, int64_t n2, int64_t pe,
+                                             int64_t X0, int64_t Y0, const Box13<T>& wb, T mu, T sigma, T dt) {
     constexpr int sp = lenia13_pitch<T>();
     static_assert(kDirTX / kDirCells == 8 && kDirTY == 32, "thread layout: 8 column blocks x 32 rows");
-    const int64_t X0 = (int64_t)blockIdx.x * kDirTX, Y0 = (int64_t)blockIdx.y * kDirTY;
-    load_tile<T>(u, n1, n2, pe, b1, b2, X0 - kR13, Y0 - kR13, sx, sy, sp, s);
-    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tx = 4 * (warp >> 2) + (lane >> 3), ty = 8 * (warp & 3) + (lane & 7);
     const int lx0 = tx * kDirCells;                // local x of the first output (tile coords)
@@ -172,6 +168,65 @@ __global__ void __launch_bounds__(256) k_lenia13(const T* __restrict__ u, T* __r
         const int64_t gx = X0 + lx0 + k;
         if (gx < n1) out[gx + gy * pe] = growth_step<T>(centre[k + kR13], acc[k], mu, sigma, dt);
     }
+}
+
+// cp.async of one lattice value into shared memory, or zeros (a source size of 0) beyond a
+// Constant(0) edge.
+template <typename T>
+__device__ __forceinline__ void cp_async_value(T* dst, const T* src, bool zero) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src), "n"((int)sizeof(T)),
+                 "r"(zero ? 0 : (int)sizeof(T))
+                 : "memory");
+}
+
+// The halo-padded tile at lattice (x0, y0) into s by asynchronous copies through the boundary
+// map, committed as one group.
+template <typename T>
+__device__ __forceinline__ void stage_tile_async(const T* __restrict__ u, int64_t n1, int64_t n2, int64_t pe, int b1,
+                                                 int b2, int64_t x0, int64_t y0, T* s) {
+    constexpr int sx = kDirTX + 2 * kR13, sy = kDirTY + 2 * kR13;
+    constexpr int sp = lenia13_pitch<T>();
+    for (int q = threadIdx.x; q < sx * sy; q += blockDim.x) {
+        const int lx = q % sx, ly = q / sx;
+        const int64_t mx = map_axis(b1, x0 + lx, n1), my = map_axis(b2, y0 + ly, n2);
+        const bool zero = mx < 0 || my < 0;
+        cp_async_value<T>(s + ly * sp + lx, zero ? u : u + mx + my * pe, zero);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// Persistent form: CTA b takes tiles b, b + gridDim.x, ... and stages each next tile into the
+// other of two buffers by cp.async while it computes the current one.
+template <typename T>
+__global__ void __launch_bounds__(256) k_lenia13p(const T* __restrict__ u, T* __restrict__ out, int64_t n1, int64_t n2,
+                                                  int64_t pe, int b1, int b2, Box13<T> wb, T mu, T sigma, T dt,
+                                                  int tiles_x, int ntiles) {
+    extern __shared__ __align__(16) unsigned char lsm[];
+    constexpr int sy = kDirTY + 2 * kR13;
+    constexpr int sp = lenia13_pitch<T>();
+    T* buf0 = (T*)lsm;
+    T* buf1 = buf0 + sp * sy;
+    int tile = blockIdx.x;
+    if (tile < ntiles)
+        stage_tile_async<T>(u, n1, n2, pe, b1, b2, (int64_t)(tile % tiles_x) * kDirTX - kR13,
+                            (int64_t)(tile / tiles_x) * kDirTY - kR13, buf0);
+    for (int i = 0; tile < ntiles; ++i) {
+        const int next = tile + (int)gridDim.x;
+        T* cur = (i & 1) ? buf1 : buf0;
+        if (next < ntiles)
+            stage_tile_async<T>(u, n1, n2, pe, b1, b2, (int64_t)(next % tiles_x) * kDirTX - kR13,
+                                (int64_t)(next / tiles_x) * kDirTY - kR13, (i & 1) ? buf0 : buf1);
+        else
+            asm volatile("cp.async.commit_group;" ::: "memory");  // an empty group: the wait below stays one behind
+        asm volatile("cp.async.wait_group 1;" ::: "memory");       // this tile's copies have landed
+        __syncthreads();
+        lenia13_tile<T>(cur, out, n1, n2, pe, (int64_t)(tile % tiles_x) * kDirTX, (int64_t)(tile / tiles_x) * kDirTY,
+                        wb, mu, sigma, dt);
+        __syncthreads();  // every thread is done with cur before the next iteration refills it
+        tile = next;
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 // Any radius: one cell per thread, taps from a list in global memory (read-only cache).
@@ -465,15 +520,22 @@ int advance_t(LeniaPlan* P, int64_t nsteps, cudaStream_t st, int* cur, void* con
             count_launch(2);
         } else if (P->box13) {
             constexpr int sy = kDirTY + 2 * kR13, sp = lenia13_pitch<T>();
-            const size_t smem = sizeof(T) * sp * sy;
-            e = ensure_dynamic_smem((const void*)k_lenia13<T>, smem);
-            if (e != cudaSuccess) return fail_to(err, GBCA_ERR_CUDA, cudaGetErrorString(e));
-            dim3 grid((unsigned)((P->n1 + kDirTX - 1) / kDirTX), (unsigned)((P->n2 + kDirTY - 1) / kDirTY));
             const Box13<T>* wb;
             if constexpr (sizeof(T) == 4) wb = &P->b32;
             else wb = &P->b64;
-            k_lenia13<T><<<grid, (kDirTX / kDirCells) * kDirTY, smem, st>>>(u, out, P->n1, P->n2, P->pe, b1, b2, *wb,
-                                                                            mu, sigma, dt);
+            const int tiles_x = (int)((P->n1 + kDirTX - 1) / kDirTX), tiles_y = (int)((P->n2 + kDirTY - 1) / kDirTY);
+            const size_t smem = 2 * sizeof(T) * sp * sy;
+            e = ensure_dynamic_smem((const void*)k_lenia13p<T>, smem);
+            if (e != cudaSuccess) return fail_to(err, GBCA_ERR_CUDA, cudaGetErrorString(e));
+            int per_sm = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lenia13p<T>, (kDirTX / kDirCells) * kDirTY,
+                                                              smem);
+            if (e != cudaSuccess) return fail_to(err, GBCA_ERR_CUDA, cudaGetErrorString(e));
+            const int ntiles = tiles_x * tiles_y;
+            int blocks = P->nsm * (per_sm > 0 ? per_sm : 1);
+            if (blocks > ntiles) blocks = ntiles;
+            k_lenia13p<T><<<blocks, (kDirTX / kDirCells) * kDirTY, smem, st>>>(u, out, P->n1, P->n2, P->pe, b1, b2,
+                                                                               *wb, mu, sigma, dt, tiles_x, ntiles);
             count_launch();
         } else {
             const int R = P->d.lenia_R, tile = 32;
