@@ -127,10 +127,12 @@ def test_config_2048_float64_within_1e5_after_100_steps(ca, oracle):
         assert np.isfinite(e).all() and g32.min() >= 0 and g32.max() <= 1
 
 
-@pytest.mark.parametrize("dims", [(360, 150), (250, 96), (112, 98)])
+@pytest.mark.parametrize("dims", [(360, 150), (250, 96), (135, 75), (112, 98)])
 def test_fft_on_mixed_radix_and_other_sides(ca, oracle, dims):
     """The FFT field on sides that are products of 2, 3 and 5 (this library's transforms: 360 =
-    2^3 3^2 5, 150 = 2 3 5^2, 250 = 2 5^3) and on a side with a factor 7 (98, the cuFFT path):
+    2^3 3^2 5, 150 = 2 3 5^2, 250 = 2 5^3, and the odd sides 135 = 3^3 5, 75 = 3 5^2, with no
+    Nyquist frequency and a last column pair of one line) and on a side with a factor 7 (98, the
+    cuFFT path):
     Float64 steps within 1e-10 of the FP64 oracle's FFT, Float32 steps within the per-step
     tolerance, on a soup that fills the torus."""
     n1, n2 = dims
