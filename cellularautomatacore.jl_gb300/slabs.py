@@ -245,24 +245,35 @@ def _context(shard):
 
 class ProcessGroupTransport:
     """Halo exchange and sums over torch.distributed: NCCL with device slabs, gloo with host
-    ones. Sends and receives of one exchange go out as one batch (batch_isend_irecv)."""
+    ones. Sends and receives of one exchange go out as one batch (batch_isend_irecv). A gloo
+    group with device slabs (gloo moves host memory only) stages the columns through host
+    memory: the sent ones copied out first, the received ones copied in after the batch."""
 
     def __init__(self, group=None):
         import torch.distributed as dist
         self.dist, self.group = dist, group
+        self.host_staged = dist.get_backend(group) == "gloo"
 
     def exchange(self, shard, ops) -> None:
         dist = self.dist
         with _context(shard):
-            p2p = []
+            p2p, landing = [], []
             for kind, peer, tag, a, k in ops:
                 if k == 0:
                     continue
+                cols = shard.columns(a, k)
+                if self.host_staged and cols.is_cuda:
+                    host = cols.cpu() if kind == "send" else cols.new_empty(cols.shape, device="cpu")
+                    if kind == "recv":
+                        landing.append((cols, host))
+                    cols = host
                 fn = dist.isend if kind == "send" else dist.irecv
-                p2p.append(dist.P2POp(fn, shard.columns(a, k), peer, self.group, tag))
+                p2p.append(dist.P2POp(fn, cols, peer, self.group, tag))
             if p2p:
                 for req in dist.batch_isend_irecv(p2p):
                     req.wait()
+            for cols, host in landing:
+                cols.copy_(host)
 
     def allreduce_sums(self, local: np.ndarray, device) -> np.ndarray:
         import torch
