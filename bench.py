@@ -949,8 +949,9 @@ def main():
     fire_draws = parts["fire"]["gcell_updates_s"] * 1e9
     philox_roof = {"kernel": "k_fire", "achieved": fire_draws / 1e9, "peak": rate.value / 1e9, "unit": "Gdraws/s",
                    "frac": fire_draws / rate.value, "peak_source": "measured in this run (draw-only kernel)"}
-    # the kernel's own pipe roof: its fmaheavy cycles per 32 cell-updates (ncu, profiles/
-    # k_fire_forest_fire_16384.md) on every SM sub-partition at the SM clock seen in the timed region
+    # the kernel's own pipe roof: its fmaheavy cycles per 32 cell-updates (from the ncu pipe
+    # counters of a capture of this kernel) on every SM sub-partition at the SM clock seen in the
+    # timed region
     sm_mhz = clocks.summary().get("sm_mhz") or 2070.0
     pipe_roof = 32 * 4 * 152 * sm_mhz * 1e6 / FIRE_FMAHEAVY_CYCLES_PER_WARP / 1e9
     philox_roof["pipe_roof"] = {"pipe": "fmaheavy (integer multiplies)", "cycles_per_32_cells": FIRE_FMAHEAVY_CYCLES_PER_WARP,
