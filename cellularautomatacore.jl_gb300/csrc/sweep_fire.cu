@@ -39,6 +39,12 @@ namespace {
 
 constexpr int kFireTX = kFireTileCols, kFireTY = kFireTileRows;
 constexpr int kFireThreadsX = 32, kFireThreadsY = 16;
+// k_fire and the batched kernel run 256-thread CTAs, four an SM within 64 registers (a
+// one-step pass keeps one shared buffer, 46 KB for 158-row tiles), against two 512-thread CTAs
+// before: smaller CTAs fill the SMs more evenly (ensemble of 4096 instances 294.9 -> 311.2
+// Gcell-updates/s; 16384^2 fire 387 -> 408 on a box where the wider form ran slower).
+// k_fire_stream keeps 512 threads.
+constexpr int kFireBatchThreadsY = 8, kFireTileThreadsY = 8;
 constexpr int kFireRowsOneStep = 160;  // the tallest tile the one-step model considers
 constexpr int kFireTileCost = 16;      // a tile's fixed cost in rows (see launch_fire)
 constexpr int kTmaSpins = 1 << 22;  // try_wait polls before a tile gives up
@@ -149,7 +155,7 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
     const int sx = kFireTX + 2 * hx, sy = TY + 2 * hy;
     const int sw = sx / 4;  // words per shared row
     const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
-    const int nthr = kFireThreadsX * kFireThreadsY;
+    const int nthr = kFireThreadsX * blockDim.y;  // 8 rows of threads (16 in k_fire_stream)
 
     if (staged) {  // the tile arrived by TMA
     } else if (INTERIOR) {  // 16-byte loads: X0 - hx, sx and the pitch are multiples of 16
@@ -222,7 +228,7 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
 // GATED: a one-step sweep with a gate or a mask (compiled apart, so the synchronous kernel keeps
 // its registers).
 template <bool GATED>
-__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
+__global__ void __launch_bounds__(kFireThreadsX* kFireTileThreadsY, 4)
     k_fire(SweepParams p, const int8_t* __restrict__ src, int8_t* __restrict__ dst,
            const __grid_constant__ CUtensorMap tmap, int tma) {
     extern __shared__ __align__(128) int8_t smem_f[];
@@ -264,7 +270,7 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY)
 // of a job reads buffer cur0 ^ (q & 1) and writes the other, so a job's passes ping-pong as a
 // single lattice's do; a job with no steps left at pass q leaves its blocks idle. Tiles load
 // with 16-byte vector loads inside the lattice and through the boundary map at its edges.
-__global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY, 2)
+__global__ void __launch_bounds__(kFireThreadsX* kFireBatchThreadsY, 4)
     k_fire_batch(const FireJob* __restrict__ jobs, const int32_t* __restrict__ tile_job, int pass, int K) {
     extern __shared__ __align__(128) int8_t smem_f[];
     __shared__ SweepParams sp;
@@ -273,7 +279,7 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireThreadsY, 2)
     if (done >= J.nsteps) return;  // the whole block: the job ended in an earlier pass
     const int nsub = (int)(J.nsteps - done < K ? J.nsteps - done : K);
     const int tid = threadIdx.y * kFireThreadsX + threadIdx.x;
-    for (int k = tid; k < (int)(sizeof(SweepParams) / 4); k += kFireThreadsX * kFireThreadsY)
+    for (int k = tid; k < (int)(sizeof(SweepParams) / 4); k += kFireThreadsX * kFireBatchThreadsY)
         ((uint32_t*)&sp)[k] = ((const uint32_t*)&J.p)[k];
     __syncthreads();
     if (tid == 0) {
@@ -499,7 +505,7 @@ cudaError_t launch_fire_batch(const FireJob* jobs, const int32_t* tile_job, int 
     const size_t smem = 2 * (size_t)(kFireTX + 2 * hx) * (size_t)(kFireTY + 2 * K);
     cudaError_t e = ensure_dynamic_smem((const void*)k_fire_batch, smem);
     if (e != cudaSuccess) return e;
-    k_fire_batch<<<ntiles, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(jobs, tile_job, pass, K);
+    k_fire_batch<<<ntiles, dim3(kFireThreadsX, kFireBatchThreadsY), smem, st>>>(jobs, tile_job, pass, K);
     return cudaGetLastError();
 }
 
@@ -564,7 +570,7 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     p.halo_x = (p.nsub + 15) / 16 * 16;
     p.keys = philox_keys(p.seed);
     const int sx = kFireTX + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
-    const size_t smem = 2 * (size_t)sx * (size_t)sy;
+    const size_t smem = (p.nsub == 1 ? 1 : 2) * (size_t)sx * (size_t)sy;  // a one-step pass stores straight to HBM
     const bool gated = fire_gated(p);  // one sub-step per launch (p.nsub == 1), compiled apart
     auto* fire_fn = gated ? k_fire<true> : k_fire<false>;
     auto* stream_fn = gated ? k_fire_stream<true> : k_fire_stream<false>;
@@ -594,7 +600,7 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
         return cudaGetLastError();
     }
     dim3 grid((unsigned)tiles_x, (unsigned)tiles_y);
-    fire_fn<<<grid, dim3(kFireThreadsX, kFireThreadsY), smem, st>>>(p, src, dst, map, tma);
+    fire_fn<<<grid, dim3(kFireThreadsX, kFireTileThreadsY), smem, st>>>(p, src, dst, map, tma);
     return cudaGetLastError();
 }
 
