@@ -39,11 +39,13 @@ namespace {
 
 constexpr int kFireTX = kFireTileCols, kFireTY = kFireTileRows;
 constexpr int kFireThreadsX = 32, kFireThreadsY = 16;
-// k_fire and the batched kernel run 256-thread CTAs, four an SM within 64 registers (a
-// one-step pass keeps one shared buffer, 46 KB for 158-row tiles), against two 512-thread CTAs
-// before: smaller CTAs fill the SMs more evenly (ensemble of 4096 instances 294.9 -> 311.2
-// Gcell-updates/s; 16384^2 fire 387 -> 408 on a box where the wider form ran slower).
-// k_fire_stream keeps 512 threads.
+// k_fire (one-step passes over at least as many tiles as SMs) and the batched kernel run
+// 256-thread CTAs, four an SM within 64 registers (a one-step pass keeps one shared buffer, 46 KB
+// for 158-row tiles), against two 512-thread CTAs before: smaller CTAs fill the SMs more evenly
+// (ensemble of 4096 instances 294.9 -> 311.2 Gcell-updates/s; 4096^2 fire 304 -> 329, 16384^2
+// 387 -> 408 on a box where the wider form ran slower). Deeper passes and lattices of fewer tiles
+// than SMs keep 512-thread CTAs: each tile's work spread over more threads. k_fire_stream keeps
+// 512 threads.
 constexpr int kFireBatchThreadsY = 8, kFireTileThreadsY = 8;
 constexpr int kFireRowsOneStep = 160;  // the tallest tile the one-step model considers
 constexpr int kFireTileCost = 16;      // a tile's fixed cost in rows (see launch_fire)
@@ -227,8 +229,8 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
 // tma: 0 = no tensor map; 1 = stage interior tiles by TMA; 2 = every tile (Constant(0) edges).
 // GATED: a one-step sweep with a gate or a mask (compiled apart, so the synchronous kernel keeps
 // its registers).
-template <bool GATED>
-__global__ void __launch_bounds__(kFireThreadsX* kFireTileThreadsY, 4)
+template <bool GATED, bool WIDE>
+__global__ void __launch_bounds__(kFireThreadsX*(WIDE ? kFireThreadsY : kFireTileThreadsY), WIDE ? 1 : 4)
     k_fire(SweepParams p, const int8_t* __restrict__ src, int8_t* __restrict__ dst,
            const __grid_constant__ CUtensorMap tmap, int tma) {
     extern __shared__ __align__(128) int8_t smem_f[];
@@ -570,9 +572,14 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
     p.halo_x = (p.nsub + 15) / 16 * 16;
     p.keys = philox_keys(p.seed);
     const int sx = kFireTX + 2 * p.halo_x, sy = p.tile_y + 2 * p.halo_y;
-    const size_t smem = (p.nsub == 1 ? 1 : 2) * (size_t)sx * (size_t)sy;  // a one-step pass stores straight to HBM
+    const int tiles_x = (int)((p.n1 + kFireTX - 1) / kFireTX), tiles_y = (int)((p.n2 + p.tile_y - 1) / p.tile_y);
+    // one-step passes over at least as many tiles as SMs: 256-thread CTAs, four an SM, one
+    // shared buffer; deeper passes (two buffers) and fewer tiles: 512-thread CTAs
+    const bool wide = p.nsub > 1 || (int64_t)tiles_x * tiles_y < device_sms();
+    const size_t smem = (wide ? 2 : 1) * (size_t)sx * (size_t)sy;
     const bool gated = fire_gated(p);  // one sub-step per launch (p.nsub == 1), compiled apart
-    auto* fire_fn = gated ? k_fire<true> : k_fire<false>;
+    auto* fire_fn = gated ? (wide ? k_fire<true, true> : k_fire<true, false>)
+                          : (wide ? k_fire<false, true> : k_fire<false, false>);
     auto* stream_fn = gated ? k_fire_stream<true> : k_fire_stream<false>;
     cudaError_t e = ensure_dynamic_smem((const void*)fire_fn, smem);
     if (e != cudaSuccess) return e;
@@ -588,7 +595,6 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
                                 p.cval[1] == 0 && p.n1 % 16 == 0;
         tma = zero_edges ? 2 : 1;
     }
-    const int tiles_x = (int)((p.n1 + kFireTX - 1) / kFireTX), tiles_y = (int)((p.n2 + p.tile_y - 1) / p.tile_y);
     if (p.nsub == 1 && tma && p.staging == 2) {  // one step per pass: the persistent, double-buffered kernel
         const size_t smem2 = 2 * (((size_t)sx * sy + 127) / 128 * 128);  // two 128-byte-aligned buffers
         e = ensure_dynamic_smem((const void*)stream_fn, smem2);
@@ -600,7 +606,7 @@ cudaError_t launch_fire(const SweepParams& p0, const int8_t* src, int8_t* dst, c
         return cudaGetLastError();
     }
     dim3 grid((unsigned)tiles_x, (unsigned)tiles_y);
-    fire_fn<<<grid, dim3(kFireThreadsX, kFireTileThreadsY), smem, st>>>(p, src, dst, map, tma);
+    fire_fn<<<grid, dim3(kFireThreadsX, wide ? kFireThreadsY : kFireTileThreadsY), smem, st>>>(p, src, dst, map, tma);
     return cudaGetLastError();
 }
 
