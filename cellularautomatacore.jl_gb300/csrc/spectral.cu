@@ -231,9 +231,11 @@ __device__ __forceinline__ T load_source(const void* u, int64_t pitch, int x, in
 // frequencies of a row as one 32-byte (Float32) piece.
 __host__ __device__ inline int spec_pitch(int n1) { return (n1 / 2 + 1 + 3) / 4 * 4; }
 
-// Axis-1 kernels take four real lines (y = 4 b .. 4 b + 3) a CTA, as two complex lines of
-// n1 points (lines 4b, 4b+1 and 4b+2, 4b+3), each transformed by T = line_threads(n1) threads.
-constexpr int kAxis1Lines = 4;
+// Axis-1 kernels take two real lines (y = 2 b, 2 b + 1) a CTA, as one complex line of n1 points
+// transformed by T = line_threads(n1) threads (one such line a CTA ran a Lenia step in 67.9 us
+// against 71.9 with two).
+constexpr int kAxis1Complex = 1;  // complex lines a CTA
+constexpr int kAxis1Lines = 2 * kAxis1Complex;
 // The axis-2 kernel takes up to four frequencies a CTA (fewer when four lines would need more
 // than kFftMaxThreads threads).
 __host__ __device__ inline int axis2_lines(int n2) {
@@ -256,7 +258,7 @@ __device__ __forceinline__ void split_rows(const C* a, int n1, C* ra, int ncp, b
     }
 }
 
-// Step 1: the four lines along axis 1 into rows y of spec.
+// Step 1: the CTA's lines along axis 1 into rows y of spec.
 template <typename T, bool MIX>
 __global__ void __launch_bounds__(kFftMaxThreads, 1)
     k_axis1_forward(const void* __restrict__ u, int64_t pitch, int src, int n1, int n2, FftFactors f,
@@ -266,7 +268,7 @@ __global__ void __launch_bounds__(kFftMaxThreads, 1)
     C* tws = (C*)smem;  // the twiddles, then the two lines
     stage_twiddles(tws, tw, ntw);
     const int TL = line_threads(n1);
-    const int li = threadIdx.x / TL, t = threadIdx.x - li * TL;  // complex line 0 or 1
+    const int li = threadIdx.x / TL, t = threadIdx.x - li * TL;  // the CTA's complex line li
     C* a = tws + ntw + li * padded_len(n1);
     const int64_t ya = (int64_t)kAxis1Lines * blockIdx.x + 2 * li;
     const bool h0 = ya < n2, h1 = ya + 1 < n2;
@@ -333,7 +335,7 @@ __device__ __forceinline__ T growth(T u, T U, T mu, T sigma, T dt) {
     return v > T(1) ? T(1) : v;
 }
 
-// Step 3: four lines back along axis 1. Each complex line reads its two lines' rows of half
+// Step 3: the CTA's lines back along axis 1. Each complex line reads its two lines' rows of half
 // spectra, made Hermitian (the imaginary parts of frequencies 0 and n1/2 dropped), as Fa + i Fb
 // over all n1 frequencies; its inverse transform holds the two real fields. Then LENIA:
 // out = growth(u, U) (pitch pe), and with `next` the new state's lines are transformed at once
@@ -462,11 +464,11 @@ cudaError_t launch_axis1_forward(SpecConv* p, const void* u, int64_t pitch, int 
                                  cudaStream_t st) {
     using C = typename CxOf<T>::type;
     const int n1 = (int)p->n1, n2 = (int)p->n2;
-    const size_t smem = sizeof(C) * (size_t)(p->ntw1 + 2 * padded_len(n1));
+    const size_t smem = sizeof(C) * (size_t)(p->ntw1 + kAxis1Complex * padded_len(n1));
     cudaError_t e = ensure_dynamic_smem((const void*)k_axis1_forward<T, MIX>, smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)((n2 + kAxis1Lines - 1) / kAxis1Lines);
-    k_axis1_forward<T, MIX><<<grid, 2 * line_threads(n1), smem, st>>>(u, pitch, src, n1, n2, p->f1, (const C*)tw,
+    k_axis1_forward<T, MIX><<<grid, kAxis1Complex * line_threads(n1), smem, st>>>(u, pitch, src, n1, n2, p->f1, (const C*)tw,
                                                                        p->ntw1, (C*)spec);
     count_launch();
     return cudaGetLastError();
@@ -491,11 +493,11 @@ cudaError_t launch_axis1_inverse(SpecConv* p, const T* u, T* out, int64_t pe, do
                                  bool next, cudaStream_t st) {
     using C = typename CxOf<T>::type;
     const int n1 = (int)p->n1, n2 = (int)p->n2;
-    const size_t smem = sizeof(C) * (size_t)(p->ntw1 + 2 * padded_len(n1));
+    const size_t smem = sizeof(C) * (size_t)(p->ntw1 + kAxis1Complex * padded_len(n1));
     cudaError_t e = ensure_dynamic_smem((const void*)k_axis1_inverse<T, LENIA, MIX>, smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)((n2 + kAxis1Lines - 1) / kAxis1Lines);
-    k_axis1_inverse<T, LENIA, MIX><<<grid, 2 * line_threads(n1), smem, st>>>(
+    k_axis1_inverse<T, LENIA, MIX><<<grid, kAxis1Complex * line_threads(n1), smem, st>>>(
         (C*)p->spec, n1, n2, p->f1, (const C*)p->tw1, p->ntw1, u, out, pe, (T)mu, (T)sigma, (T)dt, next);
     count_launch();
     return cudaGetLastError();
