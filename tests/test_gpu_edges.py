@@ -113,3 +113,75 @@ def test_more_than_2_to_32_cells(ca, oracle):
         assert read(i, j) == want, ((i, j), cid, c, nb)
     assert any((i - 1) + (j - 1) * n1 + 1 > 2 ** 32 for i, j in cells)
     st.close()
+
+
+class _DeviceBytes:
+    """A device byte range as a (rows, pitch) int8 array for torch.as_tensor."""
+
+    def __init__(self, ptr, rows, pitch):
+        self.__cuda_array_interface__ = {"shape": (rows, pitch), "typestr": "|i1", "data": (ptr, False),
+                                         "version": 3, "strides": None, "stream": None}
+
+
+@pytest.mark.parametrize("kind", ["life", "ltl"])
+def test_bit_sliced_past_2_to_32_cells(ca, kind):
+    """Life B3/S23 on Moore(1) (3 steps) and Larger than Life
+    B34..45/S34..58 on Moore(5) (2 steps) on a 65541 x 65539 torus: 4.295e9 cells, so the
+    bit-sliced kernel's column offsets (column x pitch) pass 2^32 bytes and its tiles wrap at
+    both far edges. The state is a density-0.5 device soup; the (2 r K + 1)^2 window around each
+    chosen cell is read from device memory before the advance (wrapped periodically,
+    src/spaces.jl:46-51), stepped by the oracle, and its centre compared with the cell after
+    the advance."""
+    import torch
+
+    import oracle as o
+    o.build()
+    n1, n2 = 65541, 65539
+    if kind == "life":
+        rule, r, nsteps, birth, survive = ca.Life([3], [2, 3]), 1, 3, [3], [2, 3]
+    else:
+        birth, survive = list(range(34, 46)), list(range(34, 59))
+        rule, r, nsteps = ca.Life(birth, survive, neighbourhood=ca.Moore(5)), 5, 2
+    prob = ca.CAProblem(rule=rule, u0=np.zeros(0, np.int8), tspan=(0, nsteps), p=None,
+                        space=ca.Lattice((n1, n2), (ca.Periodic(), ca.Periodic())), seed=3,
+                        neighbours=ca.Moore(r))
+    d = ca.backend.make_desc(prob, ca.Synchronous())
+    st = ca.GB300State(d, np.int8)
+    capi, lib = ca.capi, ca.capi.lib()
+    try:
+        capi.check(lib.gbca_set_state_soup(st.handle, 0.5, 2024))
+
+        def device_columns():
+            ptr, pitch = ctypes.c_void_p(), ctypes.c_int64()
+            capi.check(lib.gbca_device_state(st.handle, ctypes.byref(ptr), ctypes.byref(pitch)))
+            assert pitch.value >= n1 and pitch.value * n2 > 2 ** 32
+            torch.cuda.synchronize()
+            return torch.as_tensor(_DeviceBytes(ptr.value, n2, pitch.value), device="cuda")
+
+        cells = [(1, 1), (n1, n2), (n1 // 2, n2 - 1), (n1 - 7, n2 - 2), (5, n2), (n1 - 1, 65536), (300, 65535),
+                 (40000, 65538), (n1, 1), (1, n2)]
+        R = r * nsteps
+        cols = device_columns()
+        windows = {}
+        for i, j in cells:
+            ii = torch.tensor([(i - 1 + a) % n1 for a in range(-R, R + 1)], device="cuda")
+            jj = torch.tensor([(j - 1 + a) % n2 for a in range(-R, R + 1)], device="cuda")
+            windows[(i, j)] = np.asfortranarray(cols[jj][:, ii].cpu().numpy().T)  # [i, j] like the lattice
+        del cols
+        capi.check(lib.gbca_advance(st.handle, 0, nsteps, None, 0))
+        k, rows, staging = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        capi.check(lib.gbca_geometry(st.handle, None, ctypes.byref(k), ctypes.byref(rows), ctypes.byref(staging)))
+        assert k.value >= 1, "the bit-sliced kernel must run this problem"
+        cols = device_columns()
+        w = 2 * R + 1
+        P = o.Problem(o.RULE_LIFE, w, w, radius=r, birth=o.mask(birth), survive=o.mask(survive))
+        live = 0
+        for (i, j), win in windows.items():
+            # the centre of a (2 R + 1)^2 window after R / r steps depends only on the window
+            want = int(o.run_array(P, win, 0, nsteps)[R, R])
+            got = int(cols[j - 1, i - 1].item())
+            assert got == want, ((i, j), (i - 1) + (j - 1) * n1 + 1, got, want)
+            live += int(win.sum())
+        assert 0.3 < live / (len(cells) * w * w) < 0.7  # the soup is a soup
+    finally:
+        st.close()
