@@ -979,15 +979,17 @@ def main():
     step_e2e()
     barrier()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step_e2e()
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    with ClockSampler(local) as e2e_clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step_e2e()
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     nbytes = sum(x.numel() for x in host_in)
     e2e = {"value": replica_value(world, cell_updates(), e2e_s / args.steps * 1e3), "unit": "Gcell-updates/s",
-           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3}
+           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3,
+           "clocks": e2e_clocks.summary()}
 
     batched = None
     if rank == 0 and not args.no_batched:

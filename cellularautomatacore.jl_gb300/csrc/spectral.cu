@@ -3,18 +3,23 @@
 // kpad the kernel's weights wrapped onto the lattice at 0-based (offset mod n) per axis.
 //
 // Three launches per field, each line of the lattice transformed inside one CTA's shared memory
-// by a mixed-radix Stockham FFT (radix 4, 2, 3, 5; self-sorting, so no bit reversal), twiddles
-// from a table computed in FP64 on the host:
-//   1. axis 1 (the contiguous axis): two real lines per CTA packed as one complex line,
-//      transformed, split into the two half spectra (n1/2 + 1 frequencies each), and written
-//      transposed, frequency-major, so that axis-2 lines are contiguous;
-//   2. axis 2, one CTA per axis-1 frequency: forward transform, product with the kernel's
+// by a mixed-radix Stockham FFT (radix 8, 4, 2, 3, 5; self-sorting, so no bit reversal),
+// twiddles from per-stage tables computed in FP64 on the host:
+//   1. axis 1 (the contiguous axis): two real lines packed as one complex line, transformed,
+//      split into the two half spectra (n1/2 + 1 frequencies each), stored as two rows of the
+//      work spectrum;
+//   2. axis 2, a few axis-1 frequencies a CTA: forward transform, product with the kernel's
 //      spectrum (conjugated, with the inverse's 1/(n1 n2) folded in), inverse transform, in place;
-//   3. axis 1 inverse, two lines per CTA: the Hermitian halves rebuilt into one complex line
-//      whose inverse transform holds the two real fields, then the epilogue (Lenia's growth and
-//      clamp, or the field stored for the kernel-field sweep).
+//   3. axis 1 inverse: the Hermitian halves of two rows rebuilt into one complex line whose
+//      inverse transform holds the two real fields, then the epilogue (Lenia's growth and clamp,
+//      or the field stored for the kernel-field sweep); in a run of Lenia steps the same CTA
+//      then transforms the new state's two lines (step 1 of the next step).
+// Float32 lines of 512, 1024, 2048 or 4096 points take kernels compiled for their length
+// (k_p2_*), whose transforms keep their first inputs and last outputs in registers; other
+// lengths, and Float64, take the general ones.
 // The kernel's spectrum is made once by the same launches in FP64 (steps 1 and 2, forward only).
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "gbca_internal.cuh"
@@ -395,6 +400,306 @@ __global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis1_inverse(typename Cx
     }
 }
 
+// ----------------------------------------------- power-of-two lines of compile-time length
+// Lines of N = 512, 1024, 2048 or 4096 points (the usual lattice sides) run the same Stockham
+// stages with every index known at compile time but the thread's own: a first stage of radix 8
+// (l = 1, no twiddles), middle stages of radix 8 (l = 8, 64), and a last stage of radix 8, 4
+// or 2 (l = N / R). Thread t < N / 8 holds the first stage's inputs x[t + q N / 8] and the
+// last stage's outputs X[t + q N / 8] (q < 8) in registers: the same points. So a forward
+// transform's outputs feed the inverse's first stage (the axis-2 product between them), an
+// inverse's outputs feed the growth and the next step's forward transform, and loads and
+// stores of whole lines go straight between global memory and registers, each transform
+// passing through shared memory only between its stages.
+template <int N>
+struct P2 {
+    static_assert(N == 512 || N == 1024 || N == 2048 || N == 4096, "a power-of-two line of 512 .. 4096 points");
+    static constexpr int LOG = N == 512 ? 9 : (N == 1024 ? 10 : (N == 2048 ? 11 : 12));
+    static constexpr int T = N / 8;                                        // threads a line
+    static constexpr int RL = LOG % 3 == 0 ? 8 : (LOG % 3 == 2 ? 4 : 2);  // the last stage's radix
+    static constexpr int LL = N / RL;                                      // its sub-transform length
+    static constexpr int TS = T + T / 16;                                  // slots from point e to e + T
+};
+
+// The first stage from registers (v[q] = x[t + q T]) into points 8 t + m (slots pad16(8 t) + m).
+template <int DIR, typename C>
+__device__ __forceinline__ void p2_first(C* x, C (&v)[8], int t) {
+    dft_small<8, DIR>(v);
+    C* o = x + pad16(8 * t);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) o[m] = v[m];
+}
+
+// A middle stage of radix 8 with sub-transform length L (8 or a multiple of 16), in place:
+// butterfly t reads points t + q T, writes points (t - k) 8 + k + m L (k = t mod L); a barrier
+// between the reads and the writes and one after.
+template <int N, int DIR, int L, typename C>
+__device__ __forceinline__ void p2_middle(C* x, const C* tw, int t) {
+    static_assert(L == 8 || L % 16 == 0, "slot offsets below assume L = 8 or a multiple of 16");
+    constexpr int TS = P2<N>::TS;
+    const int k = t & (L - 1);
+    const C* in = x + pad16(t);
+    const C* w = tw + (L - 1) + k;  // the stage's table follows the earlier stages' L - 1 entries
+    C v[8];
+    v[0] = in[0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+        C c = w[(q - 1) * L];
+        if (DIR > 0) c.y = -c.y;
+        v[q] = cmul(in[q * TS], c);
+    }
+    dft_small<8, DIR>(v);
+    __syncthreads();
+    C* o = x + pad16((t - k) * 8 + k);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) o[L == 8 ? 8 * m + (m >> 1) : m * (L + L / 16)] = v[m];
+    __syncthreads();
+}
+
+template <int N, int DIR, int L, typename C>
+__device__ __forceinline__ void p2_middles(C* x, const C* tw, int t) {
+    if constexpr (L < P2<N>::LL) {
+        p2_middle<N, DIR, L>(x, tw, t);
+        p2_middles<N, DIR, L * 8>(x, tw, t);
+    }
+}
+
+// The last stage into registers: v[q] = X[t + q T]. Leaves shared memory being read.
+template <int N, int DIR, typename C>
+__device__ __forceinline__ void p2_last(const C* x, const C* tw, int t, C (&v)[8]) {
+    constexpr int R = P2<N>::RL, L = P2<N>::LL, B = 8 / R, T = P2<N>::T, TS = P2<N>::TS, LS = L + L / 16;
+    const C* in = x + pad16(t);
+    const C* w = tw + (L - 1);
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = t + b * T;  // < L: its own k
+        C u[R];
+        u[0] = in[b * TS];
+#pragma unroll
+        for (int q = 1; q < R; ++q) {
+            C c = w[(q - 1) * L + j];
+            if (DIR > 0) c.y = -c.y;
+            u[q] = cmul(in[b * TS + q * LS], c);
+        }
+        dft_small<R, DIR>(u);
+#pragma unroll
+        for (int m = 0; m < R; ++m) v[b + m * B] = u[m];  // point j + m L = t + (b + m B) T
+    }
+}
+
+// One line's DFT (exponent sign DIR) from registers to registers through x (the line's padded
+// slots, free on entry; still being read on return), in two parts: p2_first, then a barrier and
+// the rest (so that a caller can wait for its asynchronous copies in between).
+template <int N, int DIR, typename C>
+__device__ __forceinline__ void p2_rest(C* x, const C* tw, int t, C (&v)[8]) {
+    __syncthreads();
+    p2_middles<N, DIR, 8>(x, tw, t);
+    p2_last<N, DIR>(x, tw, t, v);
+}
+
+// Asynchronous 16-byte copies global -> shared (cp.async, cached in L2 only): the 16-byte chunks
+// of `bytes` (a multiple of 16; both addresses 16-byte aligned) by the CTA's threads, then one
+// commit group.
+__device__ __forceinline__ void copy_async16(void* dst, const void* src, int bytes) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16u * i), "l"((const char*)src + 16 * i)
+                     : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void commit_empty() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void wait_async() {  // all but the PENDING most recent groups have landed
+    asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
+}
+// A per-stage twiddle table's bytes rounded up to 16 (the tables are allocated one entry long).
+__host__ __device__ constexpr int tw_bytes16(int ntw) { return (ntw * 8 + 15) / 16 * 16; }
+
+// Axis-2 lines a CTA: two (512 threads for 2048 points; a line of 4096 points takes 512 threads
+// alone); thread i takes line i mod L and point index t = i / L, so a warp's loads and stores
+// cover 32 / L rows of L consecutive frequencies. Line stride: 8 slots modulo 16 (64 bytes
+// modulo 128), so that lines kk and kk + 1 fall in different banks. (Two 256-thread lines a CTA
+// ran a 2048^2 Lenia step in 51.8 us, four in 53.4, one in 62.2.)
+template <int N> __host__ __device__ constexpr int p2_axis2_lines() { return N <= 2048 ? 2 : 1; }
+template <int N> __host__ __device__ constexpr int p2_axis2_stride() {
+    return ((N - 1) + ((N - 1) >> 4) + 1 + 15) / 16 * 16 + 8;  // padded_len(N) rounded up to 16, + 8
+}
+template <int N> __host__ __device__ constexpr int p2_axis2_smem(int ntw) {  // bytes
+    return tw_bytes16(ntw) + 8 * p2_axis2_lines<N>() * (N + p2_axis2_stride<N>());
+}
+
+// Step 2 for Float32 lines of N points along axis 2: forward transform, product with the
+// kernel's spectrum, inverse transform, the L frequencies L blockIdx.x + kk of spec in place.
+// The twiddles and the CTA's rows of the kernel's spectrum (L consecutive frequencies, 8 L bytes
+// a row) are copied into shared memory asynchronously while the lines load and the forward
+// transform runs.
+template <int N>
+__global__ void __launch_bounds__(p2_axis2_lines<N>() * P2<N>::T, 2)
+    k_p2_axis2(float2* __restrict__ spec, const float2* __restrict__ ks, int n1, const float2* __restrict__ tw,
+               int ntw) {
+    constexpr int L = p2_axis2_lines<N>(), T = P2<N>::T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* tws = (float2*)smem;
+    float2* kss = (float2*)(smem + tw_bytes16(ntw));  // row y, frequency col0 + kk at [y L + kk]
+    float2* lines = kss + N * L;                       // line kk at lines + kk stride
+    const int ncp = spec_pitch(n1), col0 = L * blockIdx.x;
+    copy_async16(tws, tw, tw_bytes16(ntw));
+    {   // one 8 L-byte piece a row (col0 a multiple of L, ncp of 4: 16-byte aligned for L = 2)
+        const uint32_t d = (uint32_t)__cvta_generic_to_shared(kss);
+        for (int y = threadIdx.x; y < N; y += blockDim.x) {
+            const float2* g = ks + (int64_t)y * ncp + col0;
+            if constexpr (L == 2)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16u * y), "l"(g) : "memory");
+            else
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d + 8u * y), "l"(g) : "memory");
+        }
+        commit_empty();
+    }
+    const int kk = threadIdx.x % L, t = threadIdx.x / L;
+    const int col = col0 + kk;
+    const bool ok = col < n1 / 2 + 1;
+    float2* x = lines + kk * p2_axis2_stride<N>();
+    float2 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = ok ? spec[(int64_t)(t + q * T) * ncp + col] : float2{0.f, 0.f};
+    p2_first<-1>(x, v, t);
+    wait_async<1>();  // the twiddles
+    p2_rest<N, -1>(x, tws, t, v);
+    wait_async<0>();  // the kernel's spectrum
+    __syncthreads();  // ... visible to all, and every thread's last-stage reads done
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = cmul(v[q], kss[(t + q * T) * L + kk]);
+    p2_first<1>(x, v, t);
+    p2_rest<N, 1>(x, tws, t, v);
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if (ok) spec[(int64_t)(t + q * T) * ncp + col] = v[q];
+}
+
+// The transformed line (registers, natural order) into shared memory, split into the two
+// lines' half spectra (rows ya, ya + 1 of spec).
+template <int N>
+__device__ __forceinline__ void p2_split(float2* a, float2 (&v)[8], float2* ra, int ncp, bool h0, bool h1, int t) {
+    constexpr int TS = P2<N>::TS;
+    __syncthreads();  // the last stage's reads are done
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[pad16(t) + q * TS] = v[q];
+    __syncthreads();
+    split_rows<float>(a, N, ra, ncp, h0, h1, t, P2<N>::T);
+}
+
+// Axis-1 kernels: one complex line (two real lines, N / 8 threads) a CTA (two such lines a CTA
+// ran a 2048^2 Lenia step in 55.9 us against 51.8; twiddles read from global memory instead of
+// shared, 59.8).
+template <int N> __host__ __device__ constexpr int p2_axis1_line_bytes() {  // the line's slots, to 16 bytes
+    return (8 * ((N - 1) + ((N - 1) >> 4) + 1) + 15) / 16 * 16;
+}
+template <int N> __host__ __device__ constexpr int p2_axis1_smem(int ntw, bool lenia) {  // bytes
+    return tw_bytes16(ntw) + p2_axis1_line_bytes<N>() + (lenia ? 2 * 4 * N : 0);
+}
+
+// Step 1 for Float32 lines of N points along axis 1: lines 2 b and 2 b + 1 (b = blockIdx.x) as
+// one complex line.
+template <int N>
+__global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_forward(const void* __restrict__ u, int64_t pitch, int src,
+                                                               int n2, const float2* __restrict__ tw, int ntw,
+                                                               float2* __restrict__ spec) {
+    constexpr int T = P2<N>::T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* tws = (float2*)smem;
+    float2* a = (float2*)(smem + tw_bytes16(ntw));
+    copy_async16(tws, tw, tw_bytes16(ntw));
+    const int t = threadIdx.x;
+    const int64_t ya = 2 * (int64_t)blockIdx.x;
+    const bool h0 = ya < n2, h1 = ya + 1 < n2;
+    float2 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int x = t + q * T;
+        v[q] = float2{h0 ? load_source<float>(u, pitch, x, ya, src) : 0.f,
+                      h1 ? load_source<float>(u, pitch, x, ya + 1, src) : 0.f};
+    }
+    p2_first<-1>(a, v, t);
+    wait_async<0>();  // the twiddles
+    p2_rest<N, -1>(a, tws, t, v);
+    const int ncp = spec_pitch(N);
+    p2_split<N>(a, v, spec + ya * ncp, ncp, h0, h1, t);
+}
+
+// Step 3 for Float32 lines of N points along axis 1, as k_axis1_inverse: the Hermitian halves of
+// rows ya, ya + 1 as one complex line straight into the first stage's registers; the inverse's
+// outputs to the growth (LENIA; with `next`, on to the next step's forward transform) or to
+// the field (packed). The twiddles and, for the growth, the two state lines (pitch pe; rows
+// 16-byte aligned) are copied into shared memory asynchronously meanwhile.
+template <int N, bool LENIA>
+__global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_inverse(float2* __restrict__ spec, int n2,
+                                                               const float2* __restrict__ tw, int ntw,
+                                                               const float* __restrict__ u, float* __restrict__ out,
+                                                               int64_t pe, float mu, float sigma, float dt, bool next) {
+    constexpr int T = P2<N>::T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* tws = (float2*)smem;
+    float2* a = (float2*)(smem + tw_bytes16(ntw));
+    float* us = (float*)((unsigned char*)a + p2_axis1_line_bytes<N>());  // state lines ya, ya + 1 (LENIA)
+    const int t = threadIdx.x;
+    const int64_t ya = 2 * (int64_t)blockIdx.x;
+    const bool h0 = ya < n2, h1 = ya + 1 < n2;
+    copy_async16(tws, tw, tw_bytes16(ntw));
+    if constexpr (LENIA) {
+        if (h0) copy_async16(us, u + ya * pe, 4 * N);
+        else commit_empty();
+        if (h1) copy_async16(us + N, u + (ya + 1) * pe, 4 * N);
+        else commit_empty();
+    }
+    const int ncp = spec_pitch(N);
+    const float2* ra = spec + ya * ncp;
+    float2 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int k = t + q * T;
+        const bool lo = q < 4 || (q == 4 && t == 0);  // 2 k <= N
+        const int m = lo ? k : N - k;
+        float2 fa = h0 ? ra[m] : float2{0.f, 0.f}, fb = h1 ? ra[ncp + m] : float2{0.f, 0.f};
+        if (!lo) {
+            fa.y = -fa.y;
+            fb.y = -fb.y;
+        }
+        if (k == 0 || 2 * k == N) {
+            fa.y = 0.f;
+            fb.y = 0.f;
+        }
+        v[q] = float2{fa.x - fb.y, fa.y + fb.x};  // Fa + i Fb
+    }
+    p2_first<1>(a, v, t);
+    if constexpr (LENIA) wait_async<2>();  // the twiddles
+    else wait_async<0>();
+    p2_rest<N, 1>(a, tws, t, v);
+    if constexpr (LENIA) {
+        wait_async<0>();  // the state lines
+        __syncthreads();  // ... visible to all, and every thread's last-stage reads done
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int x = t + q * T;
+            const float g0 = h0 ? growth<float>(us[x], v[q].x, mu, sigma, dt) : 0.f;
+            const float g1 = h1 ? growth<float>(us[N + x], v[q].y, mu, sigma, dt) : 0.f;
+            if (h0) out[x + ya * pe] = g0;
+            if (h1) out[x + (ya + 1) * pe] = g1;
+            v[q] = float2{g0, g1};
+        }
+        if (next) {  // uniform over the CTA
+            p2_first<-1>(a, v, t);
+            p2_rest<N, -1>(a, tws, t, v);
+            p2_split<N>(a, v, spec + ya * ncp, ncp, h0, h1, t);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int x = t + q * T;
+            if (h0) out[x + ya * N] = v[q].x;
+            if (h1) out[x + (ya + 1) * N] = v[q].y;
+        }
+    }
+}
+
 // The kernel's spectrum for the per-step product: conj(S) / (n1 n2) in the plan's precision.
 template <typename C>
 __global__ void k_finish_kspec(const double2* __restrict__ s, C* __restrict__ ks, int64_t n, double scale) {
@@ -503,9 +808,55 @@ cudaError_t launch_axis1_inverse(SpecConv* p, const T* u, T* out, int64_t pe, do
     return cudaGetLastError();
 }
 
+template <int N>
+cudaError_t p2_axis1_forward(SpecConv* p, const void* u, int64_t pitch, int src, const void* tw1, void* spec,
+                             cudaStream_t st) {
+    const size_t smem = (size_t)p2_axis1_smem<N>(p->ntw1, false);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_p2_axis1_forward<N>, smem);
+    if (e != cudaSuccess) return e;
+    k_p2_axis1_forward<N><<<(unsigned)((p->n2 + 1) / 2), P2<N>::T, smem, st>>>(
+        u, pitch, src, (int)p->n2, (const float2*)tw1, p->ntw1, (float2*)spec);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t p2_axis2(SpecConv* p, cudaStream_t st) {
+    constexpr int L = p2_axis2_lines<N>();
+    const size_t smem = (size_t)p2_axis2_smem<N>(p->ntw2);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_p2_axis2<N>, smem);
+    if (e != cudaSuccess) return e;
+    k_p2_axis2<N><<<(unsigned)((p->n1 / 2 + 1 + L - 1) / L), L * P2<N>::T, smem, st>>>(
+        (float2*)p->spec, (const float2*)p->ks, (int)p->n1, (const float2*)p->tw2, p->ntw2);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int N, bool LENIA>
+cudaError_t p2_axis1_inverse(SpecConv* p, const float* u, float* out, int64_t pe, double mu, double sigma, double dt,
+                             bool next, cudaStream_t st) {
+    const size_t smem = (size_t)p2_axis1_smem<N>(p->ntw1, LENIA);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_p2_axis1_inverse<N, LENIA>, smem);
+    if (e != cudaSuccess) return e;
+    k_p2_axis1_inverse<N, LENIA><<<(unsigned)((p->n2 + 1) / 2), P2<N>::T, smem, st>>>(
+        (float2*)p->spec, (int)p->n2, (const float2*)p->tw1, p->ntw1, u, out, pe, (float)mu, (float)sigma, (float)dt,
+        next);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // Step 1 alone: the lines of u along axis 1 into spec.
 template <typename T>
 cudaError_t run_axis1(SpecConv* p, const void* u, int64_t pitch, int src, const void* tw1, void* spec, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        switch (p->n1) {
+            case 512: return p2_axis1_forward<512>(p, u, pitch, src, tw1, spec, st);
+            case 1024: return p2_axis1_forward<1024>(p, u, pitch, src, tw1, spec, st);
+            case 2048: return p2_axis1_forward<2048>(p, u, pitch, src, tw1, spec, st);
+            case 4096: return p2_axis1_forward<4096>(p, u, pitch, src, tw1, spec, st);
+            default: break;
+        }
+    }
     return pow2(p->n1) ? launch_axis1_forward<T, false>(p, u, pitch, src, tw1, spec, st)
                        : launch_axis1_forward<T, true>(p, u, pitch, src, tw1, spec, st);
 }
@@ -514,6 +865,15 @@ cudaError_t run_axis1(SpecConv* p, const void* u, int64_t pitch, int src, const 
 // forward spectrum into out.
 template <typename T>
 cudaError_t run_axis2(SpecConv* p, void* spec, const void* ks, void* out, const void* tw2, bool mul, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (mul && spec == p->spec && ks == p->ks && tw2 == p->tw2) switch (p->n2) {
+                case 512: return p2_axis2<512>(p, st);
+                case 1024: return p2_axis2<1024>(p, st);
+                case 2048: return p2_axis2<2048>(p, st);
+                case 4096: return p2_axis2<4096>(p, st);
+                default: break;
+            }
+    }
     const bool m2 = !pow2(p->n2);
     if (mul) return m2 ? launch_axis2<T, true, true>(p, spec, ks, nullptr, tw2, st)
                        : launch_axis2<T, true, false>(p, spec, ks, nullptr, tw2, st);
@@ -526,6 +886,19 @@ cudaError_t run_axis2(SpecConv* p, void* spec, const void* ks, void* out, const 
 template <typename T>
 cudaError_t run_inverse(SpecConv* p, const T* u, T* out, int64_t pe, bool lenia, double mu, double sigma, double dt,
                         bool next, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        switch (p->n1) {
+            case 512: return lenia ? p2_axis1_inverse<512, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                                   : p2_axis1_inverse<512, false>(p, u, out, pe, mu, sigma, dt, false, st);
+            case 1024: return lenia ? p2_axis1_inverse<1024, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                                    : p2_axis1_inverse<1024, false>(p, u, out, pe, mu, sigma, dt, false, st);
+            case 2048: return lenia ? p2_axis1_inverse<2048, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                                    : p2_axis1_inverse<2048, false>(p, u, out, pe, mu, sigma, dt, false, st);
+            case 4096: return lenia ? p2_axis1_inverse<4096, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                                    : p2_axis1_inverse<4096, false>(p, u, out, pe, mu, sigma, dt, false, st);
+            default: break;
+        }
+    }
     const bool m1 = !pow2(p->n1);
     if (lenia)
         return m1 ? launch_axis1_inverse<T, true, true>(p, u, out, pe, mu, sigma, dt, next, st)

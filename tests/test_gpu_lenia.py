@@ -148,3 +148,27 @@ def test_fft_on_mixed_radix_and_other_sides(ca, oracle, dims):
     u32 = u.astype(np.float32)
     g32 = gpu_step(ca, *gpu_state(ca, ca.Lenia(method="fft", precision="Float32"), u32, space), u32, 1)
     assert np.max(np.abs(g32.astype(np.float64) - fft.step(u32.astype(np.float64)))) < PER_STEP_TOL_F32
+
+
+@pytest.mark.parametrize("dims", [(1024, 2048), (2048, 512), (4096, 1024), (512, 4096)])
+def test_fft_power_of_two_sides(ca, oracle, dims):
+    """Float32 FFT fields on power-of-two sides of 512 .. 4096 points, which run the transforms
+    compiled for their length (a forward transform's outputs straight into the axis-2 product
+    and the inverse, the growth straight into the next step's forward transform): one step
+    within the per-step tolerance of the FP64 oracle, and three steps in one run (each step's
+    last launch also transforming the new state) bit-equal to three runs of one step."""
+    n1, n2 = dims
+    rng = np.random.default_rng(n1 + 7 * n2)
+    u = rng.random((n1, n2)).astype(np.float32)
+    fft = oracle.LeniaFFT(n1, n2)
+    space = ca.Torus(n1, n2)
+    rule = ca.Lenia(method="fft", precision="Float32")
+    one = gpu_step(ca, *gpu_state(ca, rule, u, space), u, 1)
+    assert np.max(np.abs(one.astype(np.float64) - fft.step(u.astype(np.float64)))) < PER_STEP_TOL_F32
+    fused = gpu_step(ca, *gpu_state(ca, rule, u, space), u, 3)
+    B, prob, st = gpu_state(ca, rule, u, space)
+    single = u
+    for _ in range(3):
+        single = gpu_step(ca, B, prob, st, single, 1)
+    assert np.array_equal(fused, single)
+    assert 0.0 < float(fused.mean()) < 1.0
