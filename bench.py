@@ -10,10 +10,12 @@ One bench step runs both from their initial states. Metric: Gcell-updates/s
 
   value : device-resident — initial states are copied device-to-device into the handles,
           then advanced; CUDA events on the stream the library launches on.
-  e2e   : the same through the C ABI with host buffers — set_state from pinned host memory,
-          advance, current_state back to pinned host memory, every step. Each handle runs on
-          its own stream, and both inputs and both sweeps are issued before either result is
-          read, so one lattice's copies overlap the other's sweep.
+  e2e   : the same through the C ABI with host buffers — every step copies both initial
+          states from pinned host memory (gbca_set_state_async), advances them, and copies both
+          results back to pinned host memory (gbca_get_state_async, two result buffers used in
+          turn); each handle runs on its own stream, so one step's result copies and the next
+          step's input copies overlap the sweeps; the clock stops when the last result is on
+          the host, and the last results are checked against the device-resident run's.
   roofline: the dominant kernel (by device time), algorithmic bytes 2 B per cell-update
           (Int8 read + write) over its average launch duration, against the measured HBM copy
           bandwidth in MEASURED_PEAKS.json.
@@ -910,6 +912,10 @@ def main():
         torch.cuda.synchronize()
     barrier()
     launches = lib.gbca_kernel_launches() - launches0
+    # the device-resident run's results, for the end-to-end run to match
+    resident_out = [np.empty((n2, n1), np.int8) for n1, n2 in sizes]
+    for h, r in zip(handles, resident_out):
+        capi.check(lib.gbca_get_state(h, r.ctypes.data, r.nbytes))
     ms_total = start.elapsed_time(stop)
     part_ms = [sum(e[0].elapsed_time(e[1]) for e in ev), sum(e[2].elapsed_time(e[3]) for e in ev)]
     ms_total = max_over_ranks(ms_total, dist, "cuda")
@@ -960,36 +966,45 @@ def main():
 
     # ---- end to end through the C ABI with host buffers
     host_in = [torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory() for a in (ltl0, fire0)]
-    host_out = [torch.empty_like(x).pin_memory() for x in host_in]
+    host_out = [[torch.empty_like(x).pin_memory() for x in host_in] for _ in range(2)]
     for h in handles:
         capi.check(lib.gbca_set_stream(h, None))
 
-    def step_e2e():
-        # inputs and sweeps first (each handle on its own stream), results after: the forest
-        # fire's input copy overlaps the Larger-than-Life sweep, whose result copy overlaps the fire
-        for k, (h, hi) in enumerate(zip(handles, host_in)):
-            capi.check(lib.gbca_set_state(h, ctypes.c_void_p(hi.data_ptr()), hi.numel()))
-            if k == 0:
+    def step_e2e(k):
+        # each handle on its own stream, every copy queued: the inputs in, the sweeps, the
+        # results out into the step's result buffers (two sets used in turn)
+        for i, (h, hi) in enumerate(zip(handles, host_in)):
+            capi.check(lib.gbca_set_state_async(h, ctypes.c_void_p(hi.data_ptr()), hi.numel()))
+            if i == 0:
                 capi.check(lib.gbca_advance(h, 0, LTL["steps"], None, 0))
             else:
                 capi.check(lib.gbca_advance(h, 0, FIRE["steps"], params_fire, 2))
-        for h, ho in zip(handles, host_out):
-            capi.check(lib.gbca_get_state(h, ctypes.c_void_p(ho.data_ptr()), ho.numel()))
+        for h, ho in zip(handles, host_out[k % 2]):
+            capi.check(lib.gbca_get_state_async(h, ctypes.c_void_p(ho.data_ptr()), ho.numel()))
 
-    step_e2e()
+    def sync_all():
+        for h in handles:
+            capi.check(lib.gbca_sync(h))
+
+    step_e2e(0)
+    sync_all()
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as e2e_clocks:
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            step_e2e()
-        torch.cuda.synchronize()
+        for k in range(args.steps):
+            step_e2e(k)
+        sync_all()
         e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     nbytes = sum(x.numel() for x in host_in)
+    last = host_out[(args.steps - 1) % 2]
+    e2e_equal = all(np.array_equal(o.numpy(), r) for o, r in zip(last, resident_out))
     e2e = {"value": replica_value(world, cell_updates(), e2e_s / args.steps * 1e3), "unit": "Gcell-updates/s",
            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3,
-           "clocks": e2e_clocks.summary()}
+           "results_equal_resident": e2e_equal, "clocks": e2e_clocks.summary()}
+    if not e2e_equal:
+        raise SystemExit("end-to-end results differ from the device-resident run's")
 
     batched = None
     if rank == 0 and not args.no_batched:

@@ -62,6 +62,8 @@ SIGNATURES = {
     "gbca_set_state": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
     "gbca_get_state": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
     "gbca_set_state_device": (ctypes.c_int, [_V, _V, _I64]),
+    "gbca_set_state_async": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
+    "gbca_get_state_async": (ctypes.c_int, [_V, _V, ctypes.c_size_t]),
     "gbca_advance": (ctypes.c_int, [_V, _I64, _I64, _P(ctypes.c_double), ctypes.c_int32]),
     "gbca_read_cell": (ctypes.c_int, [_V, _I64, _I64, _V]),
     "gbca_write_cell": (ctypes.c_int, [_V, _I64, _I64, _V]),

@@ -458,6 +458,30 @@ int gbca_set_state(gbca_handle* h, const void* host, size_t nbytes) {
     return GBCA_OK;
 }
 
+int gbca_set_state_async(gbca_handle* h, const void* host, size_t nbytes) {
+    if (!h || !host) return fail(GBCA_ERR_ARGUMENT, "null handle or state");
+    const size_t row = (size_t)h->d.n1 * h->esize;
+    if (nbytes != row * (size_t)h->d.n2)
+        return fail(GBCA_ERR_STATE, "the state has %zu bytes, the lattice needs %zu", nbytes, row * (size_t)h->d.n2);
+    GBCA_CUDA(cudaMemcpy2DAsync(h->buf[h->cur], (size_t)h->pitch, host, row, row, (size_t)h->d.n2,
+                                cudaMemcpyHostToDevice, h->stream),
+              "set_state_async copy");
+    h->states_valid = false;
+    h->sparse_dirty = true;
+    return GBCA_OK;
+}
+
+int gbca_get_state_async(gbca_handle* h, void* host, size_t nbytes) {
+    if (!h || !host) return fail(GBCA_ERR_ARGUMENT, "null handle or state");
+    const size_t row = (size_t)h->d.n1 * h->esize;
+    if (nbytes != row * (size_t)h->d.n2)
+        return fail(GBCA_ERR_STATE, "the buffer has %zu bytes, the lattice needs %zu", nbytes, row * (size_t)h->d.n2);
+    GBCA_CUDA(cudaMemcpy2DAsync(host, row, h->buf[h->cur], (size_t)h->pitch, row, (size_t)h->d.n2,
+                                cudaMemcpyDeviceToHost, h->stream),
+              "get_state_async copy");
+    return GBCA_OK;
+}
+
 int gbca_set_state_device(gbca_handle* h, const void* dptr, int64_t src_pitch) {
     if (!h || !dptr) return fail(GBCA_ERR_ARGUMENT, "null handle or state");
     const size_t row = (size_t)h->d.n1 * h->esize;

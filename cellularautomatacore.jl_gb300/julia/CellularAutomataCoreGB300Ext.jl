@@ -396,6 +396,31 @@ function CAC.set_state!(::GB300Backend, st::GB300State{T}, u) where {T}
     return nothing
 end
 
+# Queued copies (gbca_set_state_async / gbca_get_state_async): `buf` should be page-locked
+# (Base.Libc.malloc'd memory registered with CUDA.Mem.register, say) and must be left alone
+# until sync!(st); they let one lattice's or one step's copies overlap another's sweeps.
+function set_state_async!(st::GB300State{T}, buf::Array{T}) where {T}
+    flush!(st)
+    size(buf) == st.dims || throw(CAC.StateShapeError("the state", st.dims, size(buf)))
+    check(ccall((:gbca_set_state_async, libgbca), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t), st.handle, buf,
+                sizeof(buf)))
+    return nothing
+end
+
+function get_state_async!(buf::Array{T}, st::GB300State{T}) where {T}
+    flush!(st)
+    size(buf) == st.dims || throw(CAC.StateShapeError("the buffer", st.dims, size(buf)))
+    check(ccall((:gbca_get_state_async, libgbca), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t), st.handle, buf,
+                sizeof(buf)))
+    return buf
+end
+
+function sync!(st::GB300State)
+    flush!(st)
+    check(ccall((:gbca_sync, libgbca), Cint, (Ptr{Cvoid},), st.handle))
+    return nothing
+end
+
 function CAC.read_cell(::GB300Backend, st::GB300State{T}, I) where {T}
     flush!(st)
     v = Ref{T}()

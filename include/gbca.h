@@ -115,6 +115,16 @@ int gbca_set_state_soup(gbca_handle* h, double density, uint64_t seed);
  * pending work and copies the whole state to host memory. */
 int gbca_get_state(gbca_handle* h, void* host, size_t nbytes);
 
+/* gbca_set_state and gbca_get_state without the wait: the copy is queued on the handle's stream
+ * (after the work queued before it) and the call returns at once, so a caller can overlap one
+ * lattice's copies with another's sweeps, or one step's result with the next step's input.
+ * The host buffer should be page-locked (pinned; otherwise the driver stages it and the copy
+ * is not asynchronous) and must be left untouched until the copy has run: until gbca_sync(h)
+ * or any call that waits on the handle's stream. The reference's set_state! and
+ * current_state (src/backends.jl:132-148) are synchronous; these are their queued forms. */
+int gbca_set_state_async(gbca_handle* h, const void* host, size_t nbytes);
+int gbca_get_state_async(gbca_handle* h, void* host, size_t nbytes);
+
 /* Replaces advance!(b, st, prob, scheme, p, t) (src/backends.jl:121-130; KA ext :92-110),
  * `nsteps` times: the state goes from time t to t + nsteps. `params` is the integrator's
  * p: forest fire {p, f}; the kernel-field SI rule {beta}; unused otherwise (may be NULL

@@ -185,3 +185,48 @@ def test_bit_sliced_past_2_to_32_cells(ca, kind):
         assert 0.3 < live / (len(cells) * w * w) < 0.7  # the soup is a soup
     finally:
         st.close()
+
+
+def test_async_state_copies(ca):
+    """gbca_set_state_async / gbca_get_state_async from pinned host memory, queued on the
+    handle's stream around an advance, give the states the synchronous calls give; a second
+    handle's copies and sweep run meanwhile on its own stream."""
+    import torch
+
+    capi, lib = ca.capi, ca.capi.lib()
+    rng = np.random.default_rng(11)
+    states = [(rng.random((300, 200)) < 0.4).astype(np.int8), (rng.random((257, 130)) < 0.5).astype(np.int8)]
+    rules = [ca.Life(":highlife"), ca.Life([3], [2, 3])]
+    got, want = [], []
+    handles = []
+    try:
+        pins = []
+        for u0, rule in zip(states, rules):
+            prob = ca.CAProblem.new(rule, u0, 7, space=ca.Torus(*u0.shape))
+            d = ca.backend.make_desc(prob, ca.Synchronous())
+            h = ctypes.c_void_p()
+            capi.check(lib.gbca_create(ctypes.byref(d), ctypes.byref(h)))
+            handles.append(h)
+            hin = torch.from_numpy(np.asfortranarray(u0).ravel(order="F").copy()).pin_memory()
+            hout = torch.empty_like(hin).pin_memory()
+            pins.append((hin, hout))
+        for h, (hin, hout) in zip(handles, pins):
+            capi.check(lib.gbca_set_state_async(h, ctypes.c_void_p(hin.data_ptr()), hin.numel()))
+            capi.check(lib.gbca_advance(h, 0, 7, None, 0))
+            capi.check(lib.gbca_get_state_async(h, ctypes.c_void_p(hout.data_ptr()), hout.numel()))
+        for h, (hin, hout), u0 in zip(handles, pins, states):
+            capi.check(lib.gbca_sync(h))
+            got.append(hout.numpy().reshape(u0.shape, order="F").copy())
+            a = np.asfortranarray(u0)
+            capi.check(lib.gbca_set_state(h, a.ctypes.data, a.nbytes))
+            capi.check(lib.gbca_advance(h, 0, 7, None, 0))
+            w = np.empty_like(a, order="F")
+            capi.check(lib.gbca_get_state(h, w.ctypes.data, w.nbytes))
+            want.append(w)
+        with pytest.raises(ca.errors.StateShapeError):  # a buffer of the wrong size
+            capi.check(lib.gbca_get_state_async(handles[0], ctypes.c_void_p(pins[0][1].data_ptr()), 5))
+    finally:
+        for h in handles:
+            lib.gbca_destroy(h)
+    for g, w, u0 in zip(got, want, states):
+        assert np.array_equal(g, w) and not np.array_equal(w, u0)
