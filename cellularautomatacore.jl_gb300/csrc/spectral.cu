@@ -15,7 +15,7 @@
 //      or the field stored for the kernel-field sweep); in a run of Lenia steps the same CTA
 //      then transforms the new state's two lines (step 1 of the next step).
 // Float32 lines of 512, 1024, 2048 or 4096 points take kernels compiled for their length
-// (k_p2_*), whose transforms keep their first inputs and last outputs in registers; other
+// (k_pl_*), whose transforms keep their first inputs and last outputs in registers; other
 // lengths, and Float64, take the general ones.
 // The kernel's spectrum is made once by the same launches in FP64 (steps 1 and 2, forward only).
 #include <cmath>
@@ -72,7 +72,7 @@ __host__ __device__ inline int line_threads(int n) {
     return t < 32 ? 32 : (t + 31) / 32 * 32;
 }
 
-// The DFT of R points in place (R = 2, 3, 4, 5, 8), exponent sign DIR.
+// The DFT of R points in place (R = 2, 3, 4, 5, 8, 16), exponent sign DIR.
 template <int R, int DIR, typename C>
 __device__ __forceinline__ void dft_small(C* v) {
     using T = decltype(v[0].x);
@@ -111,6 +111,34 @@ __device__ __forceinline__ void dft_small(C* v) {
         v[0] = cadd(v[0], t);
         v[1] = C{m.x + s3 * d.x, m.y + s3 * d.y};
         v[2] = C{m.x - s3 * d.x, m.y - s3 * d.y};
+    } else if constexpr (R == 16) {  // 4 x 4: DFTs over stride-4 points, twiddles W16^(n2 k1), DFTs across
+        C a[4][4];                        // a[n2][k1]
+#pragma unroll
+        for (int n2 = 0; n2 < 4; ++n2) {
+            C w[4] = {v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]};
+            dft_small<4, DIR>(w);
+#pragma unroll
+            for (int k1 = 0; k1 < 4; ++k1) a[n2][k1] = w[k1];
+        }
+        const T c1 = T(0.92387953251128675613), s1 = T(0.38268343236508977173);  // cos, sin(pi / 8)
+        const T r = T(0.70710678118654752440);                                   // cos, sin(pi / 4)
+        // exp(DIR 2 pi i j / 16) for j = n2 k1: 1 (c1, s1), 2 (r, r), 3 (s1, c1), 4 (0, 1), 6 (-r, r), 9 (-c1, -s1)
+        a[1][1] = cmul(a[1][1], C{c1, DIR * s1});
+        a[1][2] = cmul(a[1][2], C{r, DIR * r});
+        a[1][3] = cmul(a[1][3], C{s1, DIR * c1});
+        a[2][1] = cmul(a[2][1], C{r, DIR * r});
+        a[2][2] = cmul_i<DIR>(a[2][2]);
+        a[2][3] = cmul(a[2][3], C{-r, DIR * r});
+        a[3][1] = cmul(a[3][1], C{s1, DIR * c1});
+        a[3][2] = cmul(a[3][2], C{-r, DIR * r});
+        a[3][3] = cmul(a[3][3], C{-c1, -DIR * s1});
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) {
+            C w[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+            dft_small<4, DIR>(w);
+#pragma unroll
+            for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = w[k2];
+        }
     } else {  // R == 5
         const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);  // cos(2 pi / 5), cos(4 pi / 5)
         const T s1 = T(0.95105651629515357212), s2 = T(0.58778525229247312917);   // sin(2 pi / 5), sin(4 pi / 5)
@@ -401,72 +429,77 @@ __global__ void __launch_bounds__(kFftMaxThreads, 1) k_axis1_inverse(typename Cx
 }
 
 // ----------------------------------------------- power-of-two lines of compile-time length
-// Lines of N = 512, 1024, 2048 or 4096 points (the usual lattice sides) run the same Stockham
-// stages with every index known at compile time but the thread's own: a first stage of radix 8
-// (l = 1, no twiddles), middle stages of radix 8 (l = 8, 64), and a last stage of radix 8, 4
-// or 2 (l = N / R). Thread t < N / 8 holds the first stage's inputs x[t + q N / 8] and the
-// last stage's outputs X[t + q N / 8] (q < 8) in registers: the same points. So a forward
-// transform's outputs feed the inverse's first stage (the axis-2 product between them), an
-// inverse's outputs feed the growth and the next step's forward transform, and loads and
-// stores of whole lines go straight between global memory and registers, each transform
-// passing through shared memory only between its stages.
-template <int N>
-struct P2 {
+// Lines of N = 512, 1024, 2048 or 4096 points (the usual lattice sides) run Stockham stages with
+// every index known at compile time but the thread's own. A thread holds P points (P = 8 or 16):
+// a first stage of radix P (l = 1, no twiddles), middle stages of radix P (l = P, P^2, ...), and
+// a last stage of radix R = N / LL (l = LL). Thread t < N / P holds the first stage's inputs
+// x[t + q N / P] and the last stage's outputs X[t + q N / P] (q < P) in registers: the same
+// points. So a forward transform's outputs feed the inverse's first stage (the axis-2 product
+// between them), an inverse's outputs feed the growth and the next step's forward transform,
+// and loads and stores of whole lines go straight between global memory and registers, each
+// transform passing through shared memory only between its stages.
+constexpr int kPts1 = 8, kPts2 = 16;  // points a thread in the compile-time kernels: axis 1, axis 2
+
+template <int N, int P>
+struct PL {
     static_assert(N == 512 || N == 1024 || N == 2048 || N == 4096, "a power-of-two line of 512 .. 4096 points");
+    static_assert(P == 8 || P == 16, "8 or 16 points a thread");
     static constexpr int LOG = N == 512 ? 9 : (N == 1024 ? 10 : (N == 2048 ? 11 : 12));
-    static constexpr int T = N / 8;                                        // threads a line
-    static constexpr int RL = LOG % 3 == 0 ? 8 : (LOG % 3 == 2 ? 4 : 2);  // the last stage's radix
-    static constexpr int LL = N / RL;                                      // its sub-transform length
-    static constexpr int TS = T + T / 16;                                  // slots from point e to e + T
+    static constexpr int T = N / P;  // threads a line
+    // P = 8: radix 8, 8, ... then 8, 4 or 2 (N = 8^a 2^b); P = 16: radix 16, 16, then N / 256
+    static constexpr int RL = P == 8 ? (LOG % 3 == 0 ? 8 : (LOG % 3 == 2 ? 4 : 2)) : N / 256;
+    static constexpr int LL = N / RL;      // the last stage's sub-transform length
+    static constexpr int TS = T + T / 16;  // slots from point e to e + T
 };
 
-// The first stage from registers (v[q] = x[t + q T]) into points 8 t + m (slots pad16(8 t) + m).
-template <int DIR, typename C>
-__device__ __forceinline__ void p2_first(C* x, C (&v)[8], int t) {
-    dft_small<8, DIR>(v);
-    C* o = x + pad16(8 * t);
+// The first stage from registers (v[q] = x[t + q T]) into points P t + m (slots pad16(P t) + m).
+template <int P, int DIR, typename C>
+__device__ __forceinline__ void pl_first(C* x, C (&v)[P], int t) {
+    dft_small<P, DIR>(v);
+    C* o = x + pad16(P * t);
 #pragma unroll
-    for (int m = 0; m < 8; ++m) o[m] = v[m];
+    for (int m = 0; m < P; ++m) o[m] = v[m];
 }
 
-// A middle stage of radix 8 with sub-transform length L (8 or a multiple of 16), in place:
-// butterfly t reads points t + q T, writes points (t - k) 8 + k + m L (k = t mod L); a barrier
+// A middle stage of radix P with sub-transform length L (8 or a multiple of 16), in place:
+// butterfly t reads points t + q T, writes points (t - k) P + k + m L (k = t mod L); a barrier
 // between the reads and the writes and one after.
-template <int N, int DIR, int L, typename C>
-__device__ __forceinline__ void p2_middle(C* x, const C* tw, int t) {
-    static_assert(L == 8 || L % 16 == 0, "slot offsets below assume L = 8 or a multiple of 16");
-    constexpr int TS = P2<N>::TS;
+template <int N, int P, int DIR, int L, typename C>
+__device__ __forceinline__ void pl_middle(C* x, const C* tw, int t) {
+    static_assert((L == 8 && P == 8) || L % 16 == 0, "slot offsets below assume L = 8 or a multiple of 16");
+    constexpr int TS = PL<N, P>::TS;
     const int k = t & (L - 1);
     const C* in = x + pad16(t);
     const C* w = tw + (L - 1) + k;  // the stage's table follows the earlier stages' L - 1 entries
-    C v[8];
+    C v[P];
     v[0] = in[0];
 #pragma unroll
-    for (int q = 1; q < 8; ++q) {
+    for (int q = 1; q < P; ++q) {
         C c = w[(q - 1) * L];
         if (DIR > 0) c.y = -c.y;
         v[q] = cmul(in[q * TS], c);
     }
-    dft_small<8, DIR>(v);
+    dft_small<P, DIR>(v);
     __syncthreads();
-    C* o = x + pad16((t - k) * 8 + k);
+    C* o = x + pad16((t - k) * P + k);
 #pragma unroll
-    for (int m = 0; m < 8; ++m) o[L == 8 ? 8 * m + (m >> 1) : m * (L + L / 16)] = v[m];
+    for (int m = 0; m < P; ++m) o[L == 8 ? 8 * m + (m >> 1) : m * (L + L / 16)] = v[m];
     __syncthreads();
 }
 
-template <int N, int DIR, int L, typename C>
-__device__ __forceinline__ void p2_middles(C* x, const C* tw, int t) {
-    if constexpr (L < P2<N>::LL) {
-        p2_middle<N, DIR, L>(x, tw, t);
-        p2_middles<N, DIR, L * 8>(x, tw, t);
+template <int N, int P, int DIR, int L, typename C>
+__device__ __forceinline__ void pl_middles(C* x, const C* tw, int t) {
+    if constexpr (L < PL<N, P>::LL) {
+        pl_middle<N, P, DIR, L>(x, tw, t);
+        pl_middles<N, P, DIR, L * P>(x, tw, t);
     }
 }
 
 // The last stage into registers: v[q] = X[t + q T]. Leaves shared memory being read.
-template <int N, int DIR, typename C>
-__device__ __forceinline__ void p2_last(const C* x, const C* tw, int t, C (&v)[8]) {
-    constexpr int R = P2<N>::RL, L = P2<N>::LL, B = 8 / R, T = P2<N>::T, TS = P2<N>::TS, LS = L + L / 16;
+template <int N, int P, int DIR, typename C>
+__device__ __forceinline__ void pl_last(const C* x, const C* tw, int t, C (&v)[P]) {
+    constexpr int R = PL<N, P>::RL, L = PL<N, P>::LL, B = P / R, T = PL<N, P>::T, TS = PL<N, P>::TS;
+    constexpr int LS = L + L / 16;
     const C* in = x + pad16(t);
     const C* w = tw + (L - 1);
 #pragma unroll
@@ -487,13 +520,13 @@ __device__ __forceinline__ void p2_last(const C* x, const C* tw, int t, C (&v)[8
 }
 
 // One line's DFT (exponent sign DIR) from registers to registers through x (the line's padded
-// slots, free on entry; still being read on return), in two parts: p2_first, then a barrier and
+// slots, free on entry; still being read on return), in two parts: pl_first, then a barrier and
 // the rest (so that a caller can wait for its asynchronous copies in between).
-template <int N, int DIR, typename C>
-__device__ __forceinline__ void p2_rest(C* x, const C* tw, int t, C (&v)[8]) {
+template <int N, int P, int DIR, typename C>
+__device__ __forceinline__ void pl_rest(C* x, const C* tw, int t, C (&v)[P]) {
     __syncthreads();
-    p2_middles<N, DIR, 8>(x, tw, t);
-    p2_last<N, DIR>(x, tw, t, v);
+    pl_middles<N, P, DIR, P>(x, tw, t);
+    pl_last<N, P, DIR>(x, tw, t, v);
 }
 
 // Asynchronous 16-byte copies global -> shared (cp.async, cached in L2 only): the 16-byte chunks
@@ -514,17 +547,17 @@ __device__ __forceinline__ void wait_async() {  // all but the PENDING most rece
 // A per-stage twiddle table's bytes rounded up to 16 (the tables are allocated one entry long).
 __host__ __device__ constexpr int tw_bytes16(int ntw) { return (ntw * 8 + 15) / 16 * 16; }
 
-// Axis-2 lines a CTA: two (512 threads for 2048 points; a line of 4096 points takes 512 threads
-// alone); thread i takes line i mod L and point index t = i / L, so a warp's loads and stores
-// cover 32 / L rows of L consecutive frequencies. Line stride: 8 slots modulo 16 (64 bytes
-// modulo 128), so that lines kk and kk + 1 fall in different banks. (Two 256-thread lines a CTA
-// ran a 2048^2 Lenia step in 51.8 us, four in 53.4, one in 62.2.)
-template <int N> __host__ __device__ constexpr int p2_axis2_lines() { return N <= 2048 ? 2 : 1; }
-template <int N> __host__ __device__ constexpr int p2_axis2_stride() {
+// Axis-2 lines a CTA: two while that keeps a CTA within 512 threads; thread i takes line i mod L
+// and point index t = i / L, so a warp's loads and stores cover 32 / L rows of L consecutive
+// frequencies. Line stride: 8 slots modulo 16 (64 bytes modulo 128), so that lines kk and kk + 1
+// fall in different banks. (With 8 points a thread, two 256-thread lines a CTA ran a 2048^2
+// Lenia step in 51.8 us, four in 53.4, one in 62.2.)
+template <int N, int P> __host__ __device__ constexpr int pl_axis2_lines() { return N / P <= 256 ? 2 : 1; }
+template <int N> __host__ __device__ constexpr int pl_axis2_stride() {
     return ((N - 1) + ((N - 1) >> 4) + 1 + 15) / 16 * 16 + 8;  // padded_len(N) rounded up to 16, + 8
 }
-template <int N> __host__ __device__ constexpr int p2_axis2_smem(int ntw) {  // bytes
-    return tw_bytes16(ntw) + 8 * p2_axis2_lines<N>() * (N + p2_axis2_stride<N>());
+template <int N, int P> __host__ __device__ constexpr int pl_axis2_smem(int ntw) {  // bytes
+    return tw_bytes16(ntw) + 8 * pl_axis2_lines<N, P>() * (N + pl_axis2_stride<N>());
 }
 
 // Step 2 for Float32 lines of N points along axis 2: forward transform, product with the
@@ -532,11 +565,11 @@ template <int N> __host__ __device__ constexpr int p2_axis2_smem(int ntw) {  // 
 // The twiddles and the CTA's rows of the kernel's spectrum (L consecutive frequencies, 8 L bytes
 // a row) are copied into shared memory asynchronously while the lines load and the forward
 // transform runs.
-template <int N>
-__global__ void __launch_bounds__(p2_axis2_lines<N>() * P2<N>::T, 2)
-    k_p2_axis2(float2* __restrict__ spec, const float2* __restrict__ ks, int n1, const float2* __restrict__ tw,
+template <int N, int P>
+__global__ void __launch_bounds__(pl_axis2_lines<N, P>() * PL<N, P>::T, 2)
+    k_pl_axis2(float2* __restrict__ spec, const float2* __restrict__ ks, int n1, const float2* __restrict__ tw,
                int ntw) {
-    constexpr int L = p2_axis2_lines<N>(), T = P2<N>::T;
+    constexpr int L = pl_axis2_lines<N, P>(), T = PL<N, P>::T;
     extern __shared__ __align__(16) unsigned char smem[];
     float2* tws = (float2*)smem;
     float2* kss = (float2*)(smem + tw_bytes16(ntw));  // row y, frequency col0 + kk at [y L + kk]
@@ -557,53 +590,53 @@ __global__ void __launch_bounds__(p2_axis2_lines<N>() * P2<N>::T, 2)
     const int kk = threadIdx.x % L, t = threadIdx.x / L;
     const int col = col0 + kk;
     const bool ok = col < n1 / 2 + 1;
-    float2* x = lines + kk * p2_axis2_stride<N>();
-    float2 v[8];
+    float2* x = lines + kk * pl_axis2_stride<N>();
+    float2 v[P];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) v[q] = ok ? spec[(int64_t)(t + q * T) * ncp + col] : float2{0.f, 0.f};
-    p2_first<-1>(x, v, t);
+    for (int q = 0; q < P; ++q) v[q] = ok ? spec[(int64_t)(t + q * T) * ncp + col] : float2{0.f, 0.f};
+    pl_first<P, -1>(x, v, t);
     wait_async<1>();  // the twiddles
-    p2_rest<N, -1>(x, tws, t, v);
+    pl_rest<N, P, -1>(x, tws, t, v);
     wait_async<0>();  // the kernel's spectrum
     __syncthreads();  // ... visible to all, and every thread's last-stage reads done
 #pragma unroll
-    for (int q = 0; q < 8; ++q) v[q] = cmul(v[q], kss[(t + q * T) * L + kk]);
-    p2_first<1>(x, v, t);
-    p2_rest<N, 1>(x, tws, t, v);
+    for (int q = 0; q < P; ++q) v[q] = cmul(v[q], kss[(t + q * T) * L + kk]);
+    pl_first<P, 1>(x, v, t);
+    pl_rest<N, P, 1>(x, tws, t, v);
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
+    for (int q = 0; q < P; ++q)
         if (ok) spec[(int64_t)(t + q * T) * ncp + col] = v[q];
 }
 
 // The transformed line (registers, natural order) into shared memory, split into the two
 // lines' half spectra (rows ya, ya + 1 of spec).
-template <int N>
-__device__ __forceinline__ void p2_split(float2* a, float2 (&v)[8], float2* ra, int ncp, bool h0, bool h1, int t) {
-    constexpr int TS = P2<N>::TS;
+template <int N, int P>
+__device__ __forceinline__ void pl_split(float2* a, float2 (&v)[P], float2* ra, int ncp, bool h0, bool h1, int t) {
+    constexpr int TS = PL<N, P>::TS;
     __syncthreads();  // the last stage's reads are done
 #pragma unroll
-    for (int q = 0; q < 8; ++q) a[pad16(t) + q * TS] = v[q];
+    for (int q = 0; q < P; ++q) a[pad16(t) + q * TS] = v[q];
     __syncthreads();
-    split_rows<float>(a, N, ra, ncp, h0, h1, t, P2<N>::T);
+    split_rows<float>(a, N, ra, ncp, h0, h1, t, PL<N, P>::T);
 }
 
-// Axis-1 kernels: one complex line (two real lines, N / 8 threads) a CTA (two such lines a CTA
-// ran a 2048^2 Lenia step in 55.9 us against 51.8; twiddles read from global memory instead of
-// shared, 59.8).
-template <int N> __host__ __device__ constexpr int p2_axis1_line_bytes() {  // the line's slots, to 16 bytes
+// Axis-1 kernels: one complex line (two real lines, N / P threads) a CTA (with 8 points a thread,
+// two such lines a CTA ran a 2048^2 Lenia step in 55.9 us against 51.8; twiddles read from
+// global memory instead of shared, 59.8).
+template <int N> __host__ __device__ constexpr int pl_axis1_line_bytes() {  // the line's slots, to 16 bytes
     return (8 * ((N - 1) + ((N - 1) >> 4) + 1) + 15) / 16 * 16;
 }
-template <int N> __host__ __device__ constexpr int p2_axis1_smem(int ntw, bool lenia) {  // bytes
-    return tw_bytes16(ntw) + p2_axis1_line_bytes<N>() + (lenia ? 2 * 4 * N : 0);
+template <int N> __host__ __device__ constexpr int pl_axis1_smem(int ntw, bool lenia) {  // bytes
+    return tw_bytes16(ntw) + pl_axis1_line_bytes<N>() + (lenia ? 2 * 4 * N : 0);
 }
 
 // Step 1 for Float32 lines of N points along axis 1: lines 2 b and 2 b + 1 (b = blockIdx.x) as
 // one complex line.
-template <int N>
-__global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_forward(const void* __restrict__ u, int64_t pitch, int src,
-                                                               int n2, const float2* __restrict__ tw, int ntw,
-                                                               float2* __restrict__ spec) {
-    constexpr int T = P2<N>::T;
+template <int N, int P>
+__global__ void __launch_bounds__(PL<N, P>::T) k_pl_axis1_forward(const void* __restrict__ u, int64_t pitch, int src,
+                                                                  int n2, const float2* __restrict__ tw, int ntw,
+                                                                  float2* __restrict__ spec) {
+    constexpr int T = PL<N, P>::T;
     extern __shared__ __align__(16) unsigned char smem[];
     float2* tws = (float2*)smem;
     float2* a = (float2*)(smem + tw_bytes16(ntw));
@@ -611,18 +644,18 @@ __global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_forward(const void* __res
     const int t = threadIdx.x;
     const int64_t ya = 2 * (int64_t)blockIdx.x;
     const bool h0 = ya < n2, h1 = ya + 1 < n2;
-    float2 v[8];
+    float2 v[P];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < P; ++q) {
         const int x = t + q * T;
         v[q] = float2{h0 ? load_source<float>(u, pitch, x, ya, src) : 0.f,
                       h1 ? load_source<float>(u, pitch, x, ya + 1, src) : 0.f};
     }
-    p2_first<-1>(a, v, t);
+    pl_first<P, -1>(a, v, t);
     wait_async<0>();  // the twiddles
-    p2_rest<N, -1>(a, tws, t, v);
+    pl_rest<N, P, -1>(a, tws, t, v);
     const int ncp = spec_pitch(N);
-    p2_split<N>(a, v, spec + ya * ncp, ncp, h0, h1, t);
+    pl_split<N, P>(a, v, spec + ya * ncp, ncp, h0, h1, t);
 }
 
 // Step 3 for Float32 lines of N points along axis 1, as k_axis1_inverse: the Hermitian halves of
@@ -630,16 +663,17 @@ __global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_forward(const void* __res
 // outputs to the growth (LENIA; with `next`, on to the next step's forward transform) or to
 // the field (packed). The twiddles and, for the growth, the two state lines (pitch pe; rows
 // 16-byte aligned) are copied into shared memory asynchronously meanwhile.
-template <int N, bool LENIA>
-__global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_inverse(float2* __restrict__ spec, int n2,
-                                                               const float2* __restrict__ tw, int ntw,
-                                                               const float* __restrict__ u, float* __restrict__ out,
-                                                               int64_t pe, float mu, float sigma, float dt, bool next) {
-    constexpr int T = P2<N>::T;
+template <int N, int P, bool LENIA>
+__global__ void __launch_bounds__(PL<N, P>::T) k_pl_axis1_inverse(float2* __restrict__ spec, int n2,
+                                                                  const float2* __restrict__ tw, int ntw,
+                                                                  const float* __restrict__ u, float* __restrict__ out,
+                                                                  int64_t pe, float mu, float sigma, float dt,
+                                                                  bool next) {
+    constexpr int T = PL<N, P>::T;
     extern __shared__ __align__(16) unsigned char smem[];
     float2* tws = (float2*)smem;
     float2* a = (float2*)(smem + tw_bytes16(ntw));
-    float* us = (float*)((unsigned char*)a + p2_axis1_line_bytes<N>());  // state lines ya, ya + 1 (LENIA)
+    float* us = (float*)((unsigned char*)a + pl_axis1_line_bytes<N>());  // state lines ya, ya + 1 (LENIA)
     const int t = threadIdx.x;
     const int64_t ya = 2 * (int64_t)blockIdx.x;
     const bool h0 = ya < n2, h1 = ya + 1 < n2;
@@ -652,11 +686,11 @@ __global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_inverse(float2* __restric
     }
     const int ncp = spec_pitch(N);
     const float2* ra = spec + ya * ncp;
-    float2 v[8];
+    float2 v[P];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < P; ++q) {
         const int k = t + q * T;
-        const bool lo = q < 4 || (q == 4 && t == 0);  // 2 k <= N
+        const bool lo = q < P / 2 || (q == P / 2 && t == 0);  // 2 k <= N
         const int m = lo ? k : N - k;
         float2 fa = h0 ? ra[m] : float2{0.f, 0.f}, fb = h1 ? ra[ncp + m] : float2{0.f, 0.f};
         if (!lo) {
@@ -669,15 +703,15 @@ __global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_inverse(float2* __restric
         }
         v[q] = float2{fa.x - fb.y, fa.y + fb.x};  // Fa + i Fb
     }
-    p2_first<1>(a, v, t);
+    pl_first<P, 1>(a, v, t);
     if constexpr (LENIA) wait_async<2>();  // the twiddles
     else wait_async<0>();
-    p2_rest<N, 1>(a, tws, t, v);
+    pl_rest<N, P, 1>(a, tws, t, v);
     if constexpr (LENIA) {
         wait_async<0>();  // the state lines
         __syncthreads();  // ... visible to all, and every thread's last-stage reads done
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
+        for (int q = 0; q < P; ++q) {
             const int x = t + q * T;
             const float g0 = h0 ? growth<float>(us[x], v[q].x, mu, sigma, dt) : 0.f;
             const float g1 = h1 ? growth<float>(us[N + x], v[q].y, mu, sigma, dt) : 0.f;
@@ -686,13 +720,13 @@ __global__ void __launch_bounds__(P2<N>::T) k_p2_axis1_inverse(float2* __restric
             v[q] = float2{g0, g1};
         }
         if (next) {  // uniform over the CTA
-            p2_first<-1>(a, v, t);
-            p2_rest<N, -1>(a, tws, t, v);
-            p2_split<N>(a, v, spec + ya * ncp, ncp, h0, h1, t);
+            pl_first<P, -1>(a, v, t);
+            pl_rest<N, P, -1>(a, tws, t, v);
+            pl_split<N, P>(a, v, spec + ya * ncp, ncp, h0, h1, t);
         }
     } else {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
+        for (int q = 0; q < P; ++q) {
             const int x = t + q * T;
             if (h0) out[x + ya * N] = v[q].x;
             if (h1) out[x + (ya + 1) * N] = v[q].y;
@@ -710,12 +744,11 @@ __global__ void k_finish_kspec(const double2* __restrict__ s, C* __restrict__ ks
 }
 
 template <typename C>
-std::vector<C> stage_table(const FftFactors& f) {
+std::vector<C> radix_table(const std::vector<int>& radices) {
     std::vector<C> t;
     const double pi = 3.14159265358979323846;
     int l = 1;
-    for (int s = 0; s < f.nst; ++s) {
-        const int R = f.radix(s);
+    for (const int R : radices) {
         for (int q = 1; q < R; ++q)
             for (int k = 0; k < l; ++k) {
                 const double a = -2.0 * pi * (double)k * (double)q / (double)(R * l);
@@ -724,6 +757,13 @@ std::vector<C> stage_table(const FftFactors& f) {
         l *= R;
     }
     return t;
+}
+
+template <typename C>
+std::vector<C> stage_table(const FftFactors& f) {
+    std::vector<int> r;
+    for (int s = 0; s < f.nst; ++s) r.push_back(f.radix(s));
+    return radix_table<C>(r);
 }
 
 }  // namespace
@@ -735,6 +775,7 @@ struct SpecConv {
     int ntw1 = 0, ntw2 = 0;  // entries of the per-stage twiddle tables
     void* tw1 = nullptr;  // twiddles of axis 1 and 2 in the plan's precision
     void* tw2 = nullptr;
+    void* tw16[2] = {nullptr, nullptr};  // Float32 tables of the 16-point plans (radix 16, 16, n / 256), axes 1, 2
     void* ks = nullptr;    // conj(rfft2(kpad)) / (n1 n2), frequency-major: [k][ky]
     void* spec = nullptr;  // work spectrum, the same layout
 };
@@ -755,6 +796,8 @@ void specconv_destroy(SpecConv* p) {
     if (!p) return;
     cudaFree(p->tw1);
     cudaFree(p->tw2);
+    cudaFree(p->tw16[0]);
+    cudaFree(p->tw16[1]);
     cudaFree(p->ks);
     cudaFree(p->spec);
     delete p;
@@ -808,38 +851,47 @@ cudaError_t launch_axis1_inverse(SpecConv* p, const T* u, T* out, int64_t pe, do
     return cudaGetLastError();
 }
 
+// Points a thread in the compile-time kernels: 8 on axis 1, 16 on axis 2 (2048^2 Lenia step:
+// 45.3 us; 8 and 8: 47.4; 16 and 16: 47.1; 16 and 8: 49.5).
+// A compile-time kernel's twiddle table: the 8-point plan's is the general plan's (radix 8, ...,
+// then 4 or 2); the 16-point plan (radix 16, 16, n / 256) has its own.
+inline const float2* pl_table(const SpecConv* p, int axis, int pts) {
+    return (const float2*)(pts == 16 ? p->tw16[axis] : (axis == 0 ? p->tw1 : p->tw2));
+}
+
 template <int N>
-cudaError_t p2_axis1_forward(SpecConv* p, const void* u, int64_t pitch, int src, const void* tw1, void* spec,
-                             cudaStream_t st) {
-    const size_t smem = (size_t)p2_axis1_smem<N>(p->ntw1, false);
-    cudaError_t e = ensure_dynamic_smem((const void*)k_p2_axis1_forward<N>, smem);
+cudaError_t pl_axis1_forward(SpecConv* p, const void* u, int64_t pitch, int src, void* spec, cudaStream_t st) {
+    constexpr int P = kPts1;
+    const size_t smem = (size_t)pl_axis1_smem<N>(N - 1, false);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_pl_axis1_forward<N, P>, smem);
     if (e != cudaSuccess) return e;
-    k_p2_axis1_forward<N><<<(unsigned)((p->n2 + 1) / 2), P2<N>::T, smem, st>>>(
-        u, pitch, src, (int)p->n2, (const float2*)tw1, p->ntw1, (float2*)spec);
+    k_pl_axis1_forward<N, P><<<(unsigned)((p->n2 + 1) / 2), PL<N, P>::T, smem, st>>>(
+        u, pitch, src, (int)p->n2, pl_table(p, 0, P), N - 1, (float2*)spec);
     count_launch();
     return cudaGetLastError();
 }
 
 template <int N>
-cudaError_t p2_axis2(SpecConv* p, cudaStream_t st) {
-    constexpr int L = p2_axis2_lines<N>();
-    const size_t smem = (size_t)p2_axis2_smem<N>(p->ntw2);
-    cudaError_t e = ensure_dynamic_smem((const void*)k_p2_axis2<N>, smem);
+cudaError_t pl_axis2(SpecConv* p, cudaStream_t st) {
+    constexpr int P = kPts2, L = pl_axis2_lines<N, P>();
+    const size_t smem = (size_t)pl_axis2_smem<N, P>(N - 1);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_pl_axis2<N, P>, smem);
     if (e != cudaSuccess) return e;
-    k_p2_axis2<N><<<(unsigned)((p->n1 / 2 + 1 + L - 1) / L), L * P2<N>::T, smem, st>>>(
-        (float2*)p->spec, (const float2*)p->ks, (int)p->n1, (const float2*)p->tw2, p->ntw2);
+    k_pl_axis2<N, P><<<(unsigned)((p->n1 / 2 + 1 + L - 1) / L), L * PL<N, P>::T, smem, st>>>(
+        (float2*)p->spec, (const float2*)p->ks, (int)p->n1, pl_table(p, 1, P), N - 1);
     count_launch();
     return cudaGetLastError();
 }
 
 template <int N, bool LENIA>
-cudaError_t p2_axis1_inverse(SpecConv* p, const float* u, float* out, int64_t pe, double mu, double sigma, double dt,
+cudaError_t pl_axis1_inverse(SpecConv* p, const float* u, float* out, int64_t pe, double mu, double sigma, double dt,
                              bool next, cudaStream_t st) {
-    const size_t smem = (size_t)p2_axis1_smem<N>(p->ntw1, LENIA);
-    cudaError_t e = ensure_dynamic_smem((const void*)k_p2_axis1_inverse<N, LENIA>, smem);
+    constexpr int P = kPts1;
+    const size_t smem = (size_t)pl_axis1_smem<N>(N - 1, LENIA);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_pl_axis1_inverse<N, P, LENIA>, smem);
     if (e != cudaSuccess) return e;
-    k_p2_axis1_inverse<N, LENIA><<<(unsigned)((p->n2 + 1) / 2), P2<N>::T, smem, st>>>(
-        (float2*)p->spec, (int)p->n2, (const float2*)p->tw1, p->ntw1, u, out, pe, (float)mu, (float)sigma, (float)dt,
+    k_pl_axis1_inverse<N, P, LENIA><<<(unsigned)((p->n2 + 1) / 2), PL<N, P>::T, smem, st>>>(
+        (float2*)p->spec, (int)p->n2, pl_table(p, 0, P), N - 1, u, out, pe, (float)mu, (float)sigma, (float)dt,
         next);
     count_launch();
     return cudaGetLastError();
@@ -850,10 +902,10 @@ template <typename T>
 cudaError_t run_axis1(SpecConv* p, const void* u, int64_t pitch, int src, const void* tw1, void* spec, cudaStream_t st) {
     if constexpr (std::is_same<T, float>::value) {
         switch (p->n1) {
-            case 512: return p2_axis1_forward<512>(p, u, pitch, src, tw1, spec, st);
-            case 1024: return p2_axis1_forward<1024>(p, u, pitch, src, tw1, spec, st);
-            case 2048: return p2_axis1_forward<2048>(p, u, pitch, src, tw1, spec, st);
-            case 4096: return p2_axis1_forward<4096>(p, u, pitch, src, tw1, spec, st);
+            case 512: return pl_axis1_forward<512>(p, u, pitch, src, spec, st);
+            case 1024: return pl_axis1_forward<1024>(p, u, pitch, src, spec, st);
+            case 2048: return pl_axis1_forward<2048>(p, u, pitch, src, spec, st);
+            case 4096: return pl_axis1_forward<4096>(p, u, pitch, src, spec, st);
             default: break;
         }
     }
@@ -867,10 +919,10 @@ template <typename T>
 cudaError_t run_axis2(SpecConv* p, void* spec, const void* ks, void* out, const void* tw2, bool mul, cudaStream_t st) {
     if constexpr (std::is_same<T, float>::value) {
         if (mul && spec == p->spec && ks == p->ks && tw2 == p->tw2) switch (p->n2) {
-                case 512: return p2_axis2<512>(p, st);
-                case 1024: return p2_axis2<1024>(p, st);
-                case 2048: return p2_axis2<2048>(p, st);
-                case 4096: return p2_axis2<4096>(p, st);
+                case 512: return pl_axis2<512>(p, st);
+                case 1024: return pl_axis2<1024>(p, st);
+                case 2048: return pl_axis2<2048>(p, st);
+                case 4096: return pl_axis2<4096>(p, st);
                 default: break;
             }
     }
@@ -888,14 +940,14 @@ cudaError_t run_inverse(SpecConv* p, const T* u, T* out, int64_t pe, bool lenia,
                         bool next, cudaStream_t st) {
     if constexpr (std::is_same<T, float>::value) {
         switch (p->n1) {
-            case 512: return lenia ? p2_axis1_inverse<512, true>(p, u, out, pe, mu, sigma, dt, next, st)
-                                   : p2_axis1_inverse<512, false>(p, u, out, pe, mu, sigma, dt, false, st);
-            case 1024: return lenia ? p2_axis1_inverse<1024, true>(p, u, out, pe, mu, sigma, dt, next, st)
-                                    : p2_axis1_inverse<1024, false>(p, u, out, pe, mu, sigma, dt, false, st);
-            case 2048: return lenia ? p2_axis1_inverse<2048, true>(p, u, out, pe, mu, sigma, dt, next, st)
-                                    : p2_axis1_inverse<2048, false>(p, u, out, pe, mu, sigma, dt, false, st);
-            case 4096: return lenia ? p2_axis1_inverse<4096, true>(p, u, out, pe, mu, sigma, dt, next, st)
-                                    : p2_axis1_inverse<4096, false>(p, u, out, pe, mu, sigma, dt, false, st);
+            case 512: return lenia ? pl_axis1_inverse<512, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                                   : pl_axis1_inverse<512, false>(p, u, out, pe, mu, sigma, dt, false, st);
+            case 1024: return lenia ? pl_axis1_inverse<1024, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                                    : pl_axis1_inverse<1024, false>(p, u, out, pe, mu, sigma, dt, false, st);
+            case 2048: return lenia ? pl_axis1_inverse<2048, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                                    : pl_axis1_inverse<2048, false>(p, u, out, pe, mu, sigma, dt, false, st);
+            case 4096: return lenia ? pl_axis1_inverse<4096, true>(p, u, out, pe, mu, sigma, dt, next, st)
+                                    : pl_axis1_inverse<4096, false>(p, u, out, pe, mu, sigma, dt, false, st);
             default: break;
         }
     }
@@ -972,6 +1024,15 @@ int specconv_create(int64_t n1, int64_t n2, bool f64, const double* kpad, cudaSt
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(p->tw2, t2f.data(), sizeof(float2) * p->ntw2, cudaMemcpyHostToDevice, st);
         }
+    }
+    std::vector<float2> t16[2];
+    for (int a = 0; a < 2 && e == cudaSuccess && !f64; ++a) {
+        const int64_t n = a == 0 ? n1 : n2;
+        if ((a == 0 ? kPts1 : kPts2) != 16 || (n != 512 && n != 1024 && n != 2048 && n != 4096)) continue;
+        t16[a] = radix_table<float2>({16, 16, (int)(n / 256)});
+        e = cudaMalloc(&p->tw16[a], sizeof(float2) * (size_t)n);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p->tw16[a], t16[a].data(), sizeof(float2) * t16[a].size(), cudaMemcpyHostToDevice, st);
     }
     if (e == cudaSuccess) e = run_axis1<double>(p, d_k, n1, kSpecReal, d_t1, d_s, st);
     if (e == cudaSuccess) e = run_axis2<double>(p, d_s, nullptr, d_o, d_t2, false, st);
