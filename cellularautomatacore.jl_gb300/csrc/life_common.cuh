@@ -36,7 +36,7 @@ inline int life_planes(const SweepParams& p) {
 template <int R>
 cudaError_t launch_life_radius(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
                                int8_t* dst, cudaStream_t st, int ntiles);
-// The same for von Neumann(R), R = 1..3 (sweep_life_vnR.cu).
+// The same for von Neumann(R), R = 1..7 (sweep_life_vnR.cu; Generations for R <= 3).
 template <int R>
 cudaError_t launch_life_vn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
                            int8_t* dst, cudaStream_t st, int ntiles);

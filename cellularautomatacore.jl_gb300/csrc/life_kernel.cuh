@@ -1,5 +1,5 @@
 // life_kernel.cuh — the bit-sliced sweep kernel: Life-like and Larger-than-Life rules
-// (src/rules.jl:354-389) on Moore(r), r = 1..7, and von Neumann(r), r = 1..3, and Generations
+// (src/rules.jl:354-389) on Moore(r) and von Neumann(r), r = 1..7, and Generations
 // rules with up to 8 states on Moore(1..2) and von Neumann(1..3), Synchronous, Stochastic(p) or
 // Checkerboard and masks (r <= 5), as a bit-sliced, temporally blocked sweep.
 //
@@ -423,10 +423,54 @@ __device__ __forceinline__ void vn_count(const uint32_t* ca, int y, int sw, int 
     }
 }
 
+// von Neumann(R), R = 4..7, down a column (the diamond of 2R^2 + 2R + 1 cells is too wide for one
+// adder tree): the count at row y + 1 is the count at y plus the diamond's lower rim and minus
+// its upper rim (the cells one and not the other covers), 2R + 1 cells each:
+//   lower rim: rows y + 1 + i at horizontal distance R - i, i = 0..R;
+//   upper rim: rows y - R + i at horizontal distance i, i = 0..R.
+// vn_rim counts one rim of the step from y to y + 1 (R + 1 rows; one word at distance 0, two
+// otherwise).
+template <int R, int PL, bool LOWER>
+__device__ __forceinline__ void vn_rim(const uint32_t* ca, int y, int sw, int ps, uint32_t* h) {
+    uint32_t x[2 * R + 1];
+#pragma unroll
+    for (int i = 0; i <= R; ++i) {
+        const int dy = LOWER ? 1 + i : i - R, d = LOWER ? R - i : i;
+        const uint32_t* row = ca + (y + dy) * sw;
+        const uint32_t c = alive_word<PL>(row, ps);
+        if (d == 0) {
+            x[2 * R] = c;
+        } else {
+            const int j = LOWER ? 2 * i : 2 * (i - 1);  // slots 0 .. 2R - 1 for the pairs
+            x[j] = __funnelshift_l(alive_word<PL>(row - 1, ps), c, d);  // cell x - d
+            x[j + 1] = __funnelshift_r(c, alive_word<PL>(row + 1, ps), d);  // cell x + d
+        }
+    }
+    hcount<R>(x, h);
+}
+
+// The full von Neumann(R) count at row y (centre included): row y + DY's 2 (R - |DY|) + 1 cells
+// for DY = -R..R, each row's count added in.
+template <int R, int PL, int BV, int DY>
+__device__ __forceinline__ void vn_full(const uint32_t* ca, int y, int sw, int ps, uint32_t* v) {
+    constexpr int K = R - (DY < 0 ? -DY : DY);
+    const uint32_t* row = ca + (y + DY) * sw;
+    if constexpr (K == 0) {
+        const uint32_t one[1] = {alive_word<PL>(row, ps)};
+        vadd<1, BV>(v, one);
+    } else {
+        uint32_t h[LifeBits<K>::H];
+        hrow_words<K>(alive_word<PL>(row - 1, ps), alive_word<PL>(row, ps), alive_word<PL>(row + 1, ps), h);
+        vadd<LifeBits<K>::H, BV>(v, h);
+    }
+    if constexpr (DY < R) vn_full<R, PL, BV, DY + 1>(ca, y, sw, ps, v);
+}
+
 // One sub-step of word column w over rows [r0, r1). Moore(R): a ring of the last 2R+1 rows'
 // horizontal counts and their running vertical sum. VN, von Neumann(1): each row's count is its
 // 3-cell horizontal count plus the cells above and below; von Neumann(2, 3): the diamond's
-// shifted words through an adder tree (vn_count).
+// shifted words through an adder tree (vn_count); von Neumann(4..7): a running count, the rims
+// added and taken away row by row (vn_rim).
 template <int R, int NI, int PL, bool GATED, bool VN>
 __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint32_t* __restrict__ B,
                                             const uint32_t* __restrict__ M, int sw, int ps, int w, int r0, int r1,
@@ -439,7 +483,22 @@ __device__ __forceinline__ void life_column(const uint32_t* __restrict__ A, uint
     if constexpr (GATED) {
         if (gt.mode == 1) cc = checker_col(p, gt.X0 + 32 * w);
     }
-    if constexpr (VN && R > 1) {
+    if constexpr (VN && R > 3) {
+        uint32_t v[BV];
+#pragma unroll
+        for (int i = 0; i < BV; ++i) v[i] = 0u;
+        vn_full<R, PL, BV, -R>(ca, r0, sw, ps, v);
+        for (int y = r0; y < r1; ++y) {
+            life_emit<BV, NI, PL, GATED>(v, ca, cb, cm, y, sw, ps, w, tb, p, gt, cc);
+            if (y + 1 < r1) {
+                uint32_t h[BH];
+                vn_rim<R, PL, true>(ca, y, sw, ps, h);
+                vadd<BH, BV>(v, h);
+                vn_rim<R, PL, false>(ca, y, sw, ps, h);
+                vsub<BH, BV>(v, h);
+            }
+        }
+    } else if constexpr (VN && R > 1) {
         for (int y = r0; y < r1; ++y) {
             uint32_t v[BV];
             vn_count<R, PL, BV>(ca, y, sw, ps, v);
@@ -774,13 +833,15 @@ cudaError_t launch_life_radius(const SweepParams& p, const LifeGeom& g, const Li
     return launch_r<R, 1>(p, g, tb, src, dst, st, ntiles);
 }
 
-// von Neumann(R): Life-like rules and Generations (two or three planes).
+// von Neumann(R): Life-like rules, and Generations (two or three planes) for R <= 3.
 template <int R>
 cudaError_t launch_life_vn(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
                            int8_t* dst, cudaStream_t st, int ntiles) {
-    if (p.rule == GBCA_RULE_GENERATIONS) {
-        if (p.states <= 4) return launch_r<R, 2, true>(p, g, tb, src, dst, st, ntiles);
-        return launch_r<R, 3, true>(p, g, tb, src, dst, st, ntiles);
+    if constexpr (R <= 3) {
+        if (p.rule == GBCA_RULE_GENERATIONS) {
+            if (p.states <= 4) return launch_r<R, 2, true>(p, g, tb, src, dst, st, ntiles);
+            return launch_r<R, 3, true>(p, g, tb, src, dst, st, ntiles);
+        }
     }
     return launch_r<R, 1, true>(p, g, tb, src, dst, st, ntiles);
 }

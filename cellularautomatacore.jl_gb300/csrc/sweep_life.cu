@@ -1,7 +1,7 @@
 // sweep_life.cu — host side of the bit-sliced Life-like / Larger-than-Life / Generations sweep
 // (the kernel and its layout are described in life_kernel.cuh): the rule's comparator tables,
 // tile geometry and its cost model, and the dispatch to the per-radius kernels
-// (sweep_life_r1.cu .. sweep_life_r7.cu, sweep_life_vn1.cu .. sweep_life_vn3.cu).
+// (sweep_life_r1.cu .. sweep_life_r7.cu, sweep_life_vn1.cu .. sweep_life_vn7.cu).
 #include "life_common.cuh"
 
 namespace gbca {
@@ -83,10 +83,16 @@ namespace {
 // The kernel of the problem's rule, neighbourhood and radius (life_simd_supported holds).
 cudaError_t launch_by_rule(const SweepParams& p, const LifeGeom& g, const LifeTables& tb, const int8_t* src,
                            int8_t* dst, cudaStream_t st, int ntiles) {
-    if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1..3
-        if (p.radius == 1) return launch_life_vn<1>(p, g, tb, src, dst, st, ntiles);
-        if (p.radius == 2) return launch_life_vn<2>(p, g, tb, src, dst, st, ntiles);
-        return launch_life_vn<3>(p, g, tb, src, dst, st, ntiles);
+    if (p.nbhd == GBCA_VON_NEUMANN) {  // radius 1..7
+        switch (p.radius) {
+            case 1: return launch_life_vn<1>(p, g, tb, src, dst, st, ntiles);
+            case 2: return launch_life_vn<2>(p, g, tb, src, dst, st, ntiles);
+            case 3: return launch_life_vn<3>(p, g, tb, src, dst, st, ntiles);
+            case 4: return launch_life_vn<4>(p, g, tb, src, dst, st, ntiles);
+            case 5: return launch_life_vn<5>(p, g, tb, src, dst, st, ntiles);
+            case 6: return launch_life_vn<6>(p, g, tb, src, dst, st, ntiles);
+            default: return launch_life_vn<7>(p, g, tb, src, dst, st, ntiles);
+        }
     }
     switch (p.radius) {
         case 1: return launch_life_radius<1>(p, g, tb, src, dst, st, ntiles);
@@ -104,7 +110,7 @@ cudaError_t launch_by_rule(const SweepParams& p, const LifeGeom& g, const LifeTa
 bool life_simd_supported(const SweepParams& p) {
     if (p.radius < 1 || p.pitch % 16 != 0) return false;
     if (p.mask && (((uintptr_t)p.mask & 15u) != 0 || p.radius > 5)) return false;  // the gated kernels: r <= 5
-    if (p.nbhd != GBCA_MOORE && !(p.nbhd == GBCA_VON_NEUMANN && p.radius <= 3)) return false;
+    if (p.nbhd != GBCA_MOORE && p.nbhd != GBCA_VON_NEUMANN) return false;
     if (p.scheme == GBCA_CHECKERBOARD) {
         // any boundary: the gate maps halo cells to the cells they image (checker_gate)
     } else if (p.scheme == GBCA_STOCHASTIC) {

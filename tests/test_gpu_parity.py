@@ -426,7 +426,7 @@ def test_generations_three_planes(ca, oracle, case):
 
 
 WIDENED = [
-    # name, kind, dims, kwargs, steps, saveat — von Neumann(2, 3) and gated / masked Moore(3..5), which
+    # name, kind, dims, kwargs, steps, saveat — von Neumann(2..7) and gated / masked Moore(3..5), which
     # the bit-sliced kernel runs
     ("von Neumann(2) Life-like torus", "life", (300, 200), dict(nb="vn", r=2, birth=[3, 4], survive=[2, 3, 4]), 30,
      10),
@@ -442,6 +442,18 @@ WIDENED = [
      dict(nb="vn", r=2, birth=[3, 4], survive=[2, 3, 4], seed=41, scheme="stoch", sp=0.5, bnd=("p", "c")), 25, 5),
     ("von Neumann(3) Checkerboard, Constant grid", "life", (131, 97),
      dict(nb="vn", r=3, birth=[5, 6, 7, 8], survive=[4, 5, 6, 7, 8, 9], scheme="check", bnd=("c", "c")), 20, 5),
+    ("von Neumann(4) Life-like, reflecting x periodic", "life", (260, 190),
+     dict(nb="vn", r=4, birth=range(10, 14), survive=range(8, 22), bnd=("r", "p")), 20, 5),
+    ("von Neumann(5) Life-like, Constant(1) grid", "life", (231, 170),
+     dict(nb="vn", r=5, birth=range(20, 24), survive=range(18, 32), bnd=("c", "c"), const=(1, 1)), 16, 4),
+    ("von Neumann(6) Life-like torus", "life", (300, 140),
+     dict(nb="vn", r=6, birth=range(32, 38), survive=range(36, 50)), 16, 4),
+    ("von Neumann(7) Life-like, periodic x Constant(0)", "life", (257, 200),
+     dict(nb="vn", r=7, birth=range(20, 32), survive=range(40, 54), bnd=("p", "c")), 12, 4),
+    ("von Neumann(4) Stochastic(0.6), torus", "life", (200, 130),
+     dict(nb="vn", r=4, birth=range(10, 14), survive=range(8, 22), seed=46, scheme="stoch", sp=0.6), 16, 4),
+    ("von Neumann(5) Checkerboard, reflecting", "life", (151, 121),
+     dict(nb="vn", r=5, birth=range(20, 24), survive=range(18, 32), scheme="check", bnd=("r", "r")), 12, 4),
     ("Checkerboard Moore(3), odd torus", "life", (151, 103),
      dict(r=3, birth=range(9, 15), survive=range(8, 20), scheme="check"), 20, 5),
     ("Stochastic(0.4) Moore(4), reflecting", "life", (180, 150),
@@ -456,9 +468,9 @@ WIDENED = [
 
 @pytest.mark.parametrize("case", WIDENED, ids=[c[0] for c in WIDENED])
 def test_widened_bit_sliced(ca, oracle, case):
-    """von Neumann(2) and (3) (13 and 25 cells, src/neighbourhoods.jl:33-42,148-153) and the
-    gated schemes on Moore(3..5) run the bit-sliced kernel: every save equals the oracle's, and
-    the geometry query names a bit-sliced geometry."""
+    """von Neumann(2) .. (7) (13 .. 113 cells, src/neighbourhoods.jl:33-42,148-153; radii 4..7 by
+    the running count) and the gated schemes on Moore(3..5) run the bit-sliced kernel: every
+    save equals the oracle's, and the geometry query names a bit-sliced geometry."""
     import ctypes
     name, kind, (n1, n2), kw, steps, saveat = case
     rule, space, scheme, P = spec_pair(ca, oracle, kind, n1, n2, **kw)
