@@ -547,12 +547,13 @@ __device__ __forceinline__ void wait_async() {  // all but the PENDING most rece
 // A per-stage twiddle table's bytes rounded up to 16 (the tables are allocated one entry long).
 __host__ __device__ constexpr int tw_bytes16(int ntw) { return (ntw * 8 + 15) / 16 * 16; }
 
-// Axis-2 lines a CTA: two while that keeps a CTA within 512 threads; thread i takes line i mod L
-// and point index t = i / L, so a warp's loads and stores cover 32 / L rows of L consecutive
-// frequencies. Line stride: 8 slots modulo 16 (64 bytes modulo 128), so that lines kk and kk + 1
-// fall in different banks. (With 8 points a thread, two 256-thread lines a CTA ran a 2048^2
-// Lenia step in 51.8 us, four in 53.4, one in 62.2.)
-template <int N, int P> __host__ __device__ constexpr int pl_axis2_lines() { return N / P <= 256 ? 2 : 1; }
+// Axis-2 lines a CTA: two while that keeps a CTA within 256 threads (two CTAs an SM of up to 128
+// registers a thread); thread i takes line i mod L and point index t = i / L, so a warp's loads
+// and stores cover 32 / L rows of L consecutive frequencies. Line stride: 8 slots modulo 16 (64
+// bytes modulo 128), so that lines kk and kk + 1 fall in different banks. (With 8 points a
+// thread, two 256-thread lines a CTA ran a 2048^2 Lenia step in 51.8 us, four in 53.4, one in
+// 62.2.)
+template <int N, int P> __host__ __device__ constexpr int pl_axis2_lines() { return N / P <= 128 ? 2 : 1; }
 template <int N> __host__ __device__ constexpr int pl_axis2_stride() {
     return ((N - 1) + ((N - 1) >> 4) + 1 + 15) / 16 * 16 + 8;  // padded_len(N) rounded up to 16, + 8
 }

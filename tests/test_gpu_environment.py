@@ -128,11 +128,12 @@ def test_si_field_fft_float64(ca, oracle):
     assert want.sum() > 50
 
 
-@pytest.mark.parametrize("dims", [(256, 256), (512, 1024)])
+@pytest.mark.parametrize("dims", [(256, 256), (512, 1024), (1024, 75)])
 def test_si_field_fft_float32(ca, oracle, dims):
     """Float32 FFT fields carry ~1e-7 relative rounding, so an outcome changes when a
     24-bit draw falls within it: at most 0.1% of the cells may differ after 10 steps (256^2:
-    the mixed-radix transforms; 512 x 1024: the ones compiled for power-of-two lengths)."""
+    the mixed-radix transforms; 512 x 1024: the ones compiled for power-of-two lengths;
+    1024 x 75: those on axis 1 with an odd number of lines, the mixed-radix ones on axis 2)."""
     case = (f"FFT Float32, {dims[0]} x {dims[1]} torus", dims, "pp", ("gauss", 2.0, 0, 0), "Float32", 0, False, "sync",
             2.0, 17, 10)
     prob, sch, P, E, u0, beta, steps = _si_pair(ca, oracle, case, method="fft")

@@ -150,13 +150,15 @@ def test_fft_on_mixed_radix_and_other_sides(ca, oracle, dims):
     assert np.max(np.abs(g32.astype(np.float64) - fft.step(u32.astype(np.float64)))) < PER_STEP_TOL_F32
 
 
-@pytest.mark.parametrize("dims", [(1024, 2048), (2048, 512), (4096, 1024), (512, 4096)])
+@pytest.mark.parametrize("dims", [(1024, 2048), (2048, 512), (4096, 1024), (512, 4096), (1024, 75), (360, 2048)])
 def test_fft_power_of_two_sides(ca, oracle, dims):
     """Float32 FFT fields on power-of-two sides of 512 .. 4096 points, which run the transforms
     compiled for their length (a forward transform's outputs straight into the axis-2 product
-    and the inverse, the growth straight into the next step's forward transform): one step
-    within the per-step tolerance of the FP64 oracle, and three steps in one run (each step's
-    last launch also transforming the new state) bit-equal to three runs of one step."""
+    and the inverse, the growth straight into the next step's forward transform), also beside
+    a mixed-radix side (1024 x 75: an odd number of axis-1 lines, the last complex line half
+    empty; 360 x 2048): one step within the per-step tolerance of the FP64 oracle, and three
+    steps in one run (each step's last launch also transforming the new state) bit-equal to
+    three runs of one step."""
     n1, n2 = dims
     rng = np.random.default_rng(n1 + 7 * n2)
     u = rng.random((n1, n2)).astype(np.float32)
