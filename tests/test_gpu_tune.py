@@ -121,9 +121,8 @@ def test_tune_fire_and_general(ca, oracle):
                        boundary=(oracle.CONSTANT, oracle.CONSTANT))
     assert np.array_equal(got, oracle.run_array(P, u0, 0, 20, (0.05, 0.002), nthreads=16))
     st.close()
-    # von Neumann(4) Life runs on the general kernel: nothing to tune, no geometry to pin
-    prob2 = ca.CAProblem.new(ca.Life([2, 3], [1, 2], neighbourhood=ca.VonNeumann(4)),
-                             np.zeros((64, 64), np.int8), 5)
+    # Generations with 10 states runs on the general kernel: nothing to tune, no geometry to pin
+    prob2 = ca.CAProblem.new(ca.Generations("B2/S/C10"), np.zeros((64, 64), np.int8), 5)
     st2 = ca.allocate_state(B, prob2, ca.Synchronous())
     assert ca.tune(st2, prob2) == (0, 0, 0)
     with pytest.raises(ca.UnsupportedCombinationError):
