@@ -12,10 +12,11 @@ One bench step runs both from their initial states. Metric: Gcell-updates/s
           then advanced; CUDA events on the stream the library launches on.
   e2e   : the same through the C ABI with host buffers — every step copies both initial
           states from pinned host memory (gbca_set_state_async), advances them, and copies both
-          results back to pinned host memory (gbca_get_state_async, two result buffers used in
-          turn); each handle runs on its own stream, so one step's result copies and the next
-          step's input copies overlap the sweeps; the clock stops when the last result is on
-          the host, and the last results are checked against the device-resident run's.
+          results back to pinned host memory (gbca_get_state_async); two handles per lattice
+          and two sets of result buffers are used in turn, each handle on its own stream, so a
+          step's copies overlap the neighbouring steps' sweeps; the clock stops when the last
+          result is on the host, and the last results are checked against the device-resident
+          run's.
   roofline: the dominant kernel (by device time), algorithmic bytes 2 B per cell-update
           (Int8 read + write) over its average launch duration, against the measured HBM copy
           bandwidth in MEASURED_PEAKS.json.
@@ -967,26 +968,37 @@ def main():
     # ---- end to end through the C ABI with host buffers
     host_in = [torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory() for a in (ltl0, fire0)]
     host_out = [[torch.empty_like(x).pin_memory() for x in host_in] for _ in range(2)]
+    # two handles per lattice used in turn (the second takes the tuned geometry from the cache),
+    # each on its own stream: a step's input copy runs on one handle's stream while the previous
+    # step sweeps on the other's
+    pairs = []
+    for d, h in zip((d1, d2), handles):
+        h2 = ctypes.c_void_p()
+        capi.check(lib.gbca_create(ctypes.byref(d), ctypes.byref(h2)))
+        pairs.append((h, h2))
     for h in handles:
         capi.check(lib.gbca_set_stream(h, None))
 
     def step_e2e(k):
-        # each handle on its own stream, every copy queued: the inputs in, the sweeps, the
-        # results out into the step's result buffers (two sets used in turn)
-        for i, (h, hi) in enumerate(zip(handles, host_in)):
+        # every copy queued: the inputs in, the sweeps, the results out into the step's result
+        # buffers (two sets used in turn)
+        hs = [pr[k % 2] for pr in pairs]
+        for i, (h, hi) in enumerate(zip(hs, host_in)):
             capi.check(lib.gbca_set_state_async(h, ctypes.c_void_p(hi.data_ptr()), hi.numel()))
             if i == 0:
                 capi.check(lib.gbca_advance(h, 0, LTL["steps"], None, 0))
             else:
                 capi.check(lib.gbca_advance(h, 0, FIRE["steps"], params_fire, 2))
-        for h, ho in zip(handles, host_out[k % 2]):
+        for h, ho in zip(hs, host_out[k % 2]):
             capi.check(lib.gbca_get_state_async(h, ctypes.c_void_p(ho.data_ptr()), ho.numel()))
 
     def sync_all():
-        for h in handles:
-            capi.check(lib.gbca_sync(h))
+        for pr in pairs:
+            for h in pr:
+                capi.check(lib.gbca_sync(h))
 
     step_e2e(0)
+    step_e2e(1)
     sync_all()
     barrier()
     torch.cuda.synchronize()
@@ -1003,6 +1015,8 @@ def main():
     e2e = {"value": replica_value(world, cell_updates(), e2e_s / args.steps * 1e3), "unit": "Gcell-updates/s",
            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s / args.steps * 1e3,
            "results_equal_resident": e2e_equal, "clocks": e2e_clocks.summary()}
+    for pr in pairs:
+        lib.gbca_destroy(pr[1])
     if not e2e_equal:
         raise SystemExit("end-to-end results differ from the device-resident run's")
 
