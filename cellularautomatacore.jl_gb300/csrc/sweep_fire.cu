@@ -148,7 +148,7 @@ __device__ __forceinline__ void load_region_mapped(const SweepParams& p, const i
 
 // Four cells (one 32-bit word of the shared tile) per work item: neighbour tests in byte
 // SIMD, then four independent Philox chains.
-template <bool INTERIOR, bool GATED>
+template <bool INTERIOR, bool GATED, int ROWS>
 __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __restrict__ src,
                                           int8_t* __restrict__ dst, int8_t* A, int8_t* B, bool staged,
                                           int64_t X0, int64_t Y0) {
@@ -199,8 +199,8 @@ __device__ __forceinline__ void fire_tile(const SweepParams& p, const int8_t* __
             }
             FireGate fg;  // a gated or masked sweep runs one sub-step per launch, half p.sub0
             if constexpr (GATED) fire_gate(p.scheme, p.sub0 % p.ngates, p.gate_thr, p.gate_f32, p.mask, p.pitch, fg);
-            fire_substep_rows<!INTERIOR, GATED>((const uint32_t*)A, sw, hx >> 2, nw, hy, nrows, X0 - hx, Y0 - hy, g,
-                                                ds, p.keys, tid, nthr, exact, dst, p.pitch, &fg);
+            fire_substep_rows<!INTERIOR, GATED, ROWS>((const uint32_t*)A, sw, hx >> 2, nw, hy, nrows, X0 - hx,
+                                                      Y0 - hy, g, ds, p.keys, tid, nthr, exact, dst, p.pitch, &fg);
             return;
         }
         // deeper passes: the region is wider than the tile in early sub-steps, so the flat
@@ -263,8 +263,9 @@ __global__ void __launch_bounds__(kFireThreadsX*(WIDE ? kFireThreadsY : kFireTil
             return;
         }
     }
-    if (interior) fire_tile<true, GATED>(p, src, dst, A, B, staged, X0, Y0);
-    else fire_tile<false, GATED>(p, src, dst, A, B, staged, X0, Y0);
+    // two rows of the walk unrolled together; the gated form keeps one (its registers)
+    if (interior) fire_tile<true, GATED, GATED ? 1 : 2>(p, src, dst, A, B, staged, X0, Y0);
+    else fire_tile<false, GATED, GATED ? 1 : 2>(p, src, dst, A, B, staged, X0, Y0);
 }
 
 // Many lattices per launch (a batched ensemble's large instances): one pass of up to K steps
@@ -303,8 +304,8 @@ __global__ void __launch_bounds__(kFireThreadsX* kFireBatchThreadsY, 4)
     int8_t* B = smem_f + sx * sy;
     const bool interior = X0 - sp.halo_x >= 0 && X0 + kFireTX + sp.halo_x <= sp.n1 && Y0 - sp.halo_y >= 0 &&
                           Y0 + kFireTY + sp.halo_y <= sp.n2;
-    if (interior) fire_tile<true, false>(sp, src, dst, A, B, false, X0, Y0);
-    else fire_tile<false, false>(sp, src, dst, A, B, false, X0, Y0);
+    if (interior) fire_tile<true, false, 1>(sp, src, dst, A, B, false, X0, Y0);
+    else fire_tile<false, false, 1>(sp, src, dst, A, B, false, X0, Y0);
 }
 
 // One step per pass with TMA staging, persistent: each CTA walks the tiles blockIdx.x,
