@@ -441,7 +441,7 @@ def bench_sparse(ca):
     return out
 
 
-FIRE_FMAHEAVY_CYCLES_PER_WARP = 81.33  # k_fire: fmaheavy pipe cycles per 32 cell-updates (ncu)
+FIRE_FMAHEAVY_CYCLES_PER_WARP = 79.15  # k_fire: fmaheavy pipe cycles per 32 cell-updates (ncu)
 
 
 def bench_lenia(capi, lib, reps: int = 3):
