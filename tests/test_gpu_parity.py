@@ -494,13 +494,18 @@ def test_widened_bit_sliced(ca, oracle, case):
     st.close()
 
 
-@pytest.mark.parametrize("r", [3, 5])
-def test_masked_moore_bit_sliced(ca, oracle, r):
-    """A masked Larger-than-Life sweep on Moore(3) and Moore(5) (src/environment.jl:123-130): masked
-    cells keep their state though their neighbours read them; equal to the oracle step by step."""
+@pytest.mark.parametrize("r,nb", [(3, "moore"), (5, "moore"), (5, "vn")])
+def test_masked_moore_bit_sliced(ca, oracle, r, nb):
+    """A masked Larger-than-Life sweep on Moore(3), Moore(5) and von Neumann(5) (the running
+    count; src/environment.jl:123-130): masked cells keep their state though their neighbours read
+    them; equal to the oracle step by step."""
     n1, n2 = 170, 130
-    birth, survive = (range(9, 15), range(8, 20)) if r == 3 else (range(34, 46), range(34, 59))
-    rule, space, scheme, P = spec_pair(ca, oracle, "life", n1, n2, r=r, birth=birth, survive=survive, bnd=("p", "r"))
+    if nb == "vn":
+        birth, survive = range(20, 24), range(18, 32)
+    else:
+        birth, survive = (range(9, 15), range(8, 20)) if r == 3 else (range(34, 46), range(34, 59))
+    rule, space, scheme, P = spec_pair(ca, oracle, "life", n1, n2, nb=nb, r=r, birth=birth, survive=survive,
+                                       bnd=("p", "r"))
     rng = np.random.default_rng(70 + r)
     u0 = rng.integers(0, 2, (n1, n2)).astype(np.int8)
     mask = np.ones((n1, n2), bool)
@@ -512,7 +517,7 @@ def test_masked_moore_bit_sliced(ca, oracle, r):
     want = u0
     for k, t in enumerate(range(0, 12, 4)):
         want = oracle.run_array_env(P, env, want, t, 4, nthreads=8)
-        assert np.array_equal(sol.u[k + 1], want), f"Moore({r}) masked, t = {t + 4}"
+        assert np.array_equal(sol.u[k + 1], want), f"{nb}({r}) masked, t = {t + 4}"
     assert np.array_equal(sol.u[-1][~mask], u0[~mask]) and not np.array_equal(sol.u[-1], u0)
 
 
